@@ -1,0 +1,221 @@
+/*
+ * mocca_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the MOCCa
+ * per-iteration mesh hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and opaque
+ * handles, and returns an int status (MG_OK = 0, > 0 non-convergence, < 0
+ * error).  A Fortran host binds them with `interface ... bind(C)` blocks; the
+ * status replaces the reference's `stp()` call, which the shim raises on a
+ * non-zero status.
+ *
+ * Data conventions (identical to the reference's Fortran memory order):
+ *   - one real grid is (nx,ny,nz) with x fastest: g[x + nx*(y + ny*z)];
+ *   - one spinor is Grid(nx,ny,nz,4): component c (0..3 = Re up, Im up,
+ *     Re down, Im down) at offset c*V, V = nx*ny*nz
+ *     (src/Spinor.f90:6-19, src/Spinor.f90:69);
+ *   - isospin index it = 0 for neutrons (isospin -1), 1 for protons (+1)
+ *     (the reference's it = (isospin+3)/2 minus one);
+ *   - vector fields F(nx,ny,nz,3,2) are [it][k][V]; tensor fields
+ *     W(nx,ny,nz,3,3,2) are [it][n][m][V] (m fastest), matching
+ *     src/MeanFields.f90:79-85.
+ *
+ * Threading: one context per host thread; calls on a context are
+ * stream-ordered on the context's stream and not re-entrant.
+ */
+#ifndef MOCCA_GPU_H
+#define MOCCA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define MG_OK               0
+#define MG_NOT_CONVERGED    1   /* iterative solver hit its cap           */
+#define MG_ERR_ARG         -1   /* invalid argument / unsupported mode    */
+#define MG_ERR_CUDA        -2   /* CUDA runtime error                     */
+#define MG_ERR_STATE       -3   /* call out of order (e.g. no spinors)    */
+#define MG_ERR_TIMEOUT     -4   /* a device-side wait ran out of its cap  */
+#define MG_ERR_NAN         -5   /* NaN detected (reference: x .eq. x+1)   */
+
+/* ---- precision modes ----------------------------------------------------- */
+#define MG_FP64   0   /* plain path: every kernel in FP64                 */
+#define MG_MIXED  1   /* tensor-core derivative GEMMs, FP32 mean fields   */
+
+/* ---- bases --------------------------------------------------------------- */
+#define MG_HF_BASIS   0   /* HFBasis(:), src/SpwfStorage.f90:27            */
+#define MG_CAN_BASIS  1   /* CanBasis(:), src/SpwfStorage.f90:31           */
+
+/* ---- pairing types (src/Pairing.f90:33-37) ------------------------------- */
+#define MG_PAIRING_HF   0
+#define MG_PAIRING_HFB  2
+
+typedef struct mg_ctx mg_ctx;   /* opaque device context */
+
+/*
+ * Run parameters: the &GenInfo / &SpwfStorage / &Coulomb namelist values the
+ * hot path needs (src/GenInfo.f90:302-378, src/Coulomb.f90:120-150).
+ * nx,ny,nz are the STORED point counts.  Supported symmetry modes:
+ *   pc=sc=tsc=1 (EV8, folded Lagrange matrices, src/OptimizedDerivatives.f90)
+ *   pc=sc=tsc=0 (full box, unfolded Lagrange matrices,
+ *                src/Derivatives.f90:1080-1217 with zero line extension).
+ */
+typedef struct mg_params {
+    int    nx, ny, nz;
+    double dx;                 /* fm */
+    int    pc, sc, tsc, trc;   /* parity, signature, time simplex, time reversal conserved */
+    int    nwt;                /* number of stored spwfs per basis */
+    double neutrons, protons;
+    int    precision;          /* MG_FP64 or MG_MIXED */
+    int    pairing;            /* MG_PAIRING_HF or MG_PAIRING_HFB */
+    int    coulomb_max;        /* CoulombMax, default 500 (src/Coulomb.f90:24) */
+    int    max_l_coul;         /* MaxLCoul, default MaxMoment = 10 */
+    int    coulomb_solver;     /* 0 none, 1 CG (reference default) */
+} mg_params;
+
+/*
+ * Skyrme parameters as read from a forces.param &skf group
+ * (src/Force.f90:188-255).  hbm is hbar^2/m, i.e. already doubled as in
+ * src/Force.f90:246 (41.4710382 for the default 20.73551910).
+ * nucleonmass is used as given (pass the averaged mass when averagemass).
+ */
+typedef struct mg_force {
+    double t0, x0, t1, x1, t2, x2, t3a, x3a, yt3a, t3b, x3b, yt3b, te, to;
+    double wso, wsoq;
+    double hbm, e2, hbar;
+    double nucleonmass[2];
+    int    com1body, com2body, cexchange;
+} mg_force;
+
+/* The B-coefficients of the energy density (src/Force.f90:467-560). */
+typedef struct mg_skyrme_b {
+    double B1, B2, B3, B4, B5, B6, B7a, B7b, B8a, B8b, byt3a, byt3b, B9, B9q;
+    double B10, B11, B12a, B12b, B13a, B13b, B14, B15, B16, B17;
+} mg_skyrme_b;
+
+/* Energy decomposition of CompEnergy (src/Energy.f90:62-179). */
+typedef struct mg_energy_terms {
+    double total;            /* TotalEnergy                                  */
+    double kinetic[2];       /* Kinetic(it), src/Energy.f90:1426-1456        */
+    double skyrme[36];       /* SkyrmeTerms, term by term, already times dv  */
+    double coulomb;          /* CompCoulombEnergy, src/Coulomb.f90:215-231   */
+    double coulomb_exchange; /* Slater exchange energy                       */
+    double com[2][2];        /* COMCorrection(body, it)                      */
+    double pairing[2];       /* PairingEnergy(it)                            */
+    double sp_energy;        /* SpwfEnergy, src/Energy.f90:1483-1554         */
+} mg_energy_terms;
+
+/* ---- host-side helpers (no device work) ---------------------------------- */
+
+/* B-coefficients from Skyrme parameters; replaces CalcEDFCoef
+ * (src/Force.f90:467-560, TRC and J2Terms=.false. branch). */
+int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* out);
+
+/* Lagrange derivative matrices for one axis; replaces IniLag + reduceLag
+ * (src/Derivatives.f90:899-1078).  folded=1: the EV8 matrices LagXMat /
+ * LagXXMat for a stored half-line of n points (full line 2n); out arrays are
+ * [s][i][j] row-major, s=0 the odd extension (Fortran index 1), s=1 the even
+ * one (index 2).  folded=0: the full-line matrices of DerLag_1D /
+ * SecondDerLag with zero extension (src/Derivatives.f90:1177-1312), written
+ * to both s slots. */
+int mg_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2);
+
+/* ---- context --------------------------------------------------------------- */
+
+/* Allocates every device buffer of the hot path (spinors of both bases and
+ * their derivatives, densities, fields, Coulomb box, HFB matrices) and builds
+ * the Lagrange matrices; replaces the setup done by ReadDerivativesInfo,
+ * SetupCoulomb and IniMoments.  stream: a cudaStream_t or NULL (a private
+ * stream is created). */
+int mg_create(const mg_params* p, const mg_force* f, void* stream, mg_ctx** out);
+int mg_destroy(mg_ctx* ctx);
+int mg_synchronize(mg_ctx* ctx);
+
+/* ---- spinor transfer ------------------------------------------------------- */
+
+/* grids[i] points at one Fortran Grid(nx,ny,nz,4) (4V doubles) for spwf
+ * first+i; qn[4*i..] = (isospin, parity, signature, time simplex) as in
+ * src/Spwf.f90:63-85.  qn may be NULL on later uploads to keep the numbers. */
+int mg_upload_spinors(mg_ctx* ctx, int basis, const double* const* grids,
+                      const int* qn, int first, int count);
+int mg_download_spinors(mg_ctx* ctx, int basis, double* const* grids,
+                        int first, int count);
+/* der[i] receives Der(1:3) of spwf first+i as 3 consecutive spinors (12V
+ * doubles), lap[i] the Laplacian (4V); either may be NULL. */
+int mg_download_derivatives(mg_ctx* ctx, int basis, double* const* der,
+                            double* const* lap, int first, int count);
+
+/* Occupations / single-particle energies of a basis (Spwf%Occupation,
+ * Spwf%Energy).  Arrays of nwt doubles. */
+int mg_set_occupations(mg_ctx* ctx, int basis, const double* occ);
+int mg_get_occupations(mg_ctx* ctx, int basis, double* occ);
+int mg_set_energies(mg_ctx* ctx, int basis, const double* e);
+int mg_get_energies(mg_ctx* ctx, int basis, double* e, double* disp);
+
+/* ---- compute entry points --------------------------------------------------- */
+
+/* Der(1:3) and Lap of every spwf of one basis; replaces CompDer over the
+ * basis (src/Spwf.f90:778-792 via DeriveSpinor / LapSpinor with the Lagrange
+ * kernels of src/OptimizedDerivatives.f90:115-615). */
+int mg_derive_basis(mg_ctx* ctx, int basis);
+/* DeriveAll (src/SpwfStorage.f90:586-604): HFBasis, and CanBasis under HFB. */
+int mg_derive_all(mg_ctx* ctx);
+
+/* h.psi for every spwf of a basis from the current fields; replaces hPsi
+ * (src/ImaginaryTime.f90:213-304).  hpsi (nwt*4V, may be NULL) receives the
+ * spinors, e[i] = <psi|h psi> and disp[i] = <h psi|h psi> - e^2 (may be NULL). */
+int mg_hpsi(mg_ctx* ctx, int basis, double* hpsi, double* e, double* disp);
+
+/* One GradDesc step on the HF basis (src/ImaginaryTime.f90:439-500), with
+ * its Gram-Schmidt; dt in 1e-22 s as in &GenInfo. */
+int mg_grad_desc(mg_ctx* ctx, double dt, double momentum);
+
+/* Energy-ordered Gram-Schmidt of the HF basis (src/SpwfStorage.f90:372-480). */
+int mg_gram_schmidt(mg_ctx* ctx);
+
+/* Naive HF filling by energy (src/HartreeFock.f90:177-260). */
+int mg_hf_fill(mg_ctx* ctx);
+
+/* ComputeDensity over the density basis (src/Densities.f90:431-550):
+ * rho, tau, div J, grad rho, lap rho. */
+int mg_update_densities(mg_ctx* ctx);
+/* Arrays of 2V (rho,tau,nablaj,laprho) and 6V (derrho); any may be NULL. */
+int mg_get_densities(mg_ctx* ctx, double* rho, double* tau, double* nablaj,
+                     double* derrho, double* laprho);
+int mg_set_densities(mg_ctx* ctx, const double* rho, const double* tau,
+                     const double* nablaj, const double* derrho,
+                     const double* laprho);
+
+/* Electric multipole moments of the densities needed by the Coulomb
+ * boundary (Calculate_Multipole, src/Moments.f90:1907-2004). */
+int mg_calculate_moments(mg_ctx* ctx);
+
+/* Coulomb solve (src/Coulomb.f90:255-346): multipole boundary, CG, Slater
+ * exchange.  iters may be NULL.  Returns MG_NOT_CONVERGED when the CG hits
+ * CoulombMax (the reference prints and continues; so does this library). */
+int mg_solve_coulomb(mg_ctx* ctx, int* iters);
+
+/* ConstructPotentials (src/PotentialMixing.f90:17-201, MixingScheme 0):
+ * Coulomb, U, W (+div W), B (+grad B).  iters may be NULL. */
+int mg_construct_potentials(mg_ctx* ctx, int* coulomb_iters);
+/* U,B,coul,coulex: 2V/2V/V/V; nablab,divw: 6V; w: 18V; any may be NULL. */
+int mg_get_potentials(mg_ctx* ctx, double* u, double* b, double* nablab,
+                      double* w, double* divw, double* coul, double* coulex);
+int mg_set_potentials(mg_ctx* ctx, const double* u, const double* b,
+                      const double* nablab, const double* w, const double* divw);
+
+/* CompEnergy (src/Energy.f90:62-179). */
+int mg_energy(mg_ctx* ctx, mg_energy_terms* out);
+
+/* n_iter passes of the Evolve loop body (src/Main.f90:255-328) with fixed
+ * dt and momentum; out (may be NULL) receives the last iteration's energy. */
+int mg_iterate(mg_ctx* ctx, int n_iter, double dt, double momentum,
+               mg_energy_terms* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOCCA_GPU_H */

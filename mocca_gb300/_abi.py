@@ -1,0 +1,161 @@
+"""ctypes declarations of the C ABI in include/mocca_gpu.h.
+
+The structures mirror the header field by field; `load()` opens the in-tree
+libmocca_gpu.so and declares every entry point's signature.  No compute
+happens here and nothing falls back to another implementation: when the
+library is missing, `load()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+MG_OK = 0
+MG_NOT_CONVERGED = 1
+MG_ERR_ARG = -1
+MG_ERR_CUDA = -2
+MG_ERR_STATE = -3
+MG_ERR_TIMEOUT = -4
+MG_ERR_NAN = -5
+
+MG_FP64 = 0
+MG_MIXED = 1
+MG_HF_BASIS = 0
+MG_CAN_BASIS = 1
+MG_PAIRING_HF = 0
+MG_PAIRING_HFB = 2
+
+STATUS_NAMES = {
+    MG_OK: "ok", MG_NOT_CONVERGED: "not converged", MG_ERR_ARG: "invalid argument",
+    MG_ERR_CUDA: "CUDA error", MG_ERR_STATE: "call out of order",
+    MG_ERR_TIMEOUT: "device wait timed out", MG_ERR_NAN: "NaN detected",
+}
+
+
+class MgParams(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("dx", C.c_double),
+        ("pc", C.c_int), ("sc", C.c_int), ("tsc", C.c_int), ("trc", C.c_int),
+        ("nwt", C.c_int),
+        ("neutrons", C.c_double), ("protons", C.c_double),
+        ("precision", C.c_int),
+        ("pairing", C.c_int),
+        ("coulomb_max", C.c_int),
+        ("max_l_coul", C.c_int),
+        ("coulomb_solver", C.c_int),
+    ]
+
+
+class MgForce(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "t0", "x0", "t1", "x1", "t2", "x2", "t3a", "x3a", "yt3a", "t3b", "x3b", "yt3b",
+        "te", "to", "wso", "wsoq", "hbm", "e2", "hbar")] + [
+        ("nucleonmass", C.c_double * 2),
+        ("com1body", C.c_int), ("com2body", C.c_int), ("cexchange", C.c_int),
+    ]
+
+
+class MgSkyrmeB(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "B1", "B2", "B3", "B4", "B5", "B6", "B7a", "B7b", "B8a", "B8b", "byt3a", "byt3b",
+        "B9", "B9q", "B10", "B11", "B12a", "B12b", "B13a", "B13b", "B14", "B15", "B16",
+        "B17")]
+
+
+class MgEnergyTerms(C.Structure):
+    _fields_ = [
+        ("total", C.c_double),
+        ("kinetic", C.c_double * 2),
+        ("skyrme", C.c_double * 36),
+        ("coulomb", C.c_double),
+        ("coulomb_exchange", C.c_double),
+        ("com", (C.c_double * 2) * 2),
+        ("pairing", C.c_double * 2),
+        ("sp_energy", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {
+            "total": self.total,
+            "kinetic": list(self.kinetic),
+            "skyrme": list(self.skyrme),
+            "coulomb": self.coulomb,
+            "coulomb_exchange": self.coulomb_exchange,
+            "com": [list(r) for r in self.com],
+            "pairing": list(self.pairing),
+            "sp_energy": self.sp_energy,
+        }
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_PP = C.POINTER(C.c_void_p)
+
+# name -> argtypes (every function returns int status)
+SIGNATURES = {
+    "mg_skyrme_coefficients": [C.POINTER(MgForce), C.c_int, C.POINTER(MgSkyrmeB)],
+    "mg_lagrange_matrices": [C.c_int, C.c_double, C.c_int, _D, _D],
+    "mg_create": [C.POINTER(MgParams), C.POINTER(MgForce), _P, C.POINTER(_P)],
+    "mg_destroy": [_P],
+    "mg_synchronize": [_P],
+    "mg_upload_spinors": [_P, C.c_int, _PP, _I, C.c_int, C.c_int],
+    "mg_download_spinors": [_P, C.c_int, _PP, C.c_int, C.c_int],
+    "mg_download_derivatives": [_P, C.c_int, _PP, _PP, C.c_int, C.c_int],
+    "mg_set_occupations": [_P, C.c_int, _D],
+    "mg_get_occupations": [_P, C.c_int, _D],
+    "mg_set_energies": [_P, C.c_int, _D],
+    "mg_get_energies": [_P, C.c_int, _D, _D],
+    "mg_derive_basis": [_P, C.c_int],
+    "mg_derive_all": [_P],
+    "mg_hpsi": [_P, C.c_int, _D, _D, _D],
+    "mg_grad_desc": [_P, C.c_double, C.c_double],
+    "mg_gram_schmidt": [_P],
+    "mg_hf_fill": [_P],
+    "mg_update_densities": [_P],
+    "mg_get_densities": [_P, _D, _D, _D, _D, _D],
+    "mg_set_densities": [_P, _D, _D, _D, _D, _D],
+    "mg_calculate_moments": [_P],
+    "mg_solve_coulomb": [_P, _I],
+    "mg_construct_potentials": [_P, _I],
+    "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],
+    "mg_set_potentials": [_P, _D, _D, _D, _D, _D],
+    "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
+    "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
+}
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmocca_gpu.so"
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Open libmocca_gpu.so (built by mocca_gb300.build) and bind signatures."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+            " (there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class MgError(RuntimeError):
+    def __init__(self, fn: str, status: int):
+        super().__init__(f"{fn} returned {status} ({STATUS_NAMES.get(status, 'unknown')})")
+        self.status = status
+
+
+def check(fn: str, status: int, allow_not_converged: bool = False) -> int:
+    if status < 0 or (status > 0 and not allow_not_converged):
+        raise MgError(fn, status)
+    return status

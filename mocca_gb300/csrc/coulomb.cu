@@ -1,0 +1,357 @@
+// coulomb.cu -- Coulomb Poisson solve on the symmetry-reduced box, FP64.
+//
+// Replaces SolveCoulomb with CoulombSolver = 1 (src/Coulomb.f90:255-346):
+//   CoulombBound (:583-674): source -4 pi e2 rho_p on the stored box and
+//     Dirichlet values sum_lm e2 4pi/(2l+1) Q_lm r^l Y_lm / r^(2l+1) on the
+//     BCNumber = 2 extra planes of the extended box;
+//   ConjugGrad (:755-900) with CoulombLaplacian (5-point FD, even mirror at
+//     the low end of each axis, src/CoulombDerivatives.f90:144-281);
+//   Slater exchange -(3/pi)^(1/3) e2 rho_p^(1/3) (:338-344).
+// The CG runs as ONE cooperative kernel: every block owns a slice of the
+// extended box, the two dot products per iteration are block partials summed
+// by every block in the same order (so every block takes the same branch),
+// and blocks meet at a sense-reversing grid barrier whose spin is bounded:
+// a barrier that waits longer than its cap sets the timeout status and the
+// kernel returns instead of hanging.
+#include <cmath>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr long long kSpinCap = 1ll << 22;  // ~0.2 s of 50 ns sleeps per barrier
+
+struct CgArgs {
+    double* sol;
+    double* res;
+    double* p;
+    double* t;
+    const double* src;
+    double* red;          // 2 * gridDim.x
+    unsigned* bar;        // [0] arrival count, [1] generation
+    int* status;          // [0] state, [1] iterations
+    int nx, ny, nz, mx, my, mz;
+    double inv_dx2;
+    double prec;
+    int maxit;
+};
+
+__device__ bool grid_barrier(unsigned* bar, int* status) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (++spins > kSpinCap) {
+                    atomicExch(status, 2);
+                    break;
+                }
+                __nanosleep(50);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)status != 2;
+}
+
+__device__ __forceinline__ double lap_at(const double* g, int i, int j, int k, int mx, int my,
+                                         double inv_dx2) {
+    const double cf[5] = {-1.0 / 12.0, 4.0 / 3.0, -5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0};
+    double ax = 0.0, ay = 0.0, az = 0.0;
+#pragma unroll
+    for (int q = -2; q <= 2; ++q) {
+        const int ii = i + q < 0 ? -(i + q) - 1 : i + q;
+        const int jj = j + q < 0 ? -(j + q) - 1 : j + q;
+        const int kk = k + q < 0 ? -(k + q) - 1 : k + q;
+        ax = fma(cf[q + 2], g[ii + mx * (j + (long)my * k)], ax);
+        ay = fma(cf[q + 2], g[i + mx * (jj + (long)my * k)], ay);
+        az = fma(cf[q + 2], g[i + mx * (j + (long)my * kk)], az);
+    }
+    return ax * inv_dx2 + ay * inv_dx2 + az * inv_dx2;
+}
+
+__device__ double block_sum(double x, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (threadIdx.x % 32 == 0) sh[threadIdx.x / 32] = x;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kThreads / 32; ++q) s += sh[q];
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+__device__ double grid_total(const double* red, double* bc) {
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (unsigned q = 0; q < gridDim.x; ++q) s += ((volatile const double*)red)[q];
+        *bc = s;
+    }
+    __syncthreads();
+    const double v = *bc;
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_cg(CgArgs a) {
+    __shared__ double sh[kThreads / 32];
+    __shared__ double bcast;
+    const long M = (long)a.mx * a.my * a.mz;
+    const long stride = (long)gridDim.x * kThreads;
+    const long t0 = (long)blockIdx.x * kThreads + threadIdx.x;
+    double* red1 = a.red;
+    double* red2 = a.red + gridDim.x;
+
+    // r0 = src - Lap(sol); p0 = r0; pnorm = r0.r0
+    double loc = 0.0;
+    for (long o = t0; o < M; o += stride) {
+        const int i = (int)(o % a.mx), j = (int)((o / a.mx) % a.my), k = (int)(o / ((long)a.mx * a.my));
+        double lap = 0.0;
+        if (i < a.nx && j < a.ny && k < a.nz) lap = lap_at(a.sol, i, j, k, a.mx, a.my, a.inv_dx2);
+        const double r = -lap + a.src[o];
+        a.res[o] = r;
+        a.p[o] = r;
+        loc = fma(r, r, loc);
+    }
+    double s = block_sum(loc, sh);
+    if (threadIdx.x == 0) red2[blockIdx.x] = s;
+    if (!grid_barrier(a.bar, a.status)) return;
+    double pnorm = grid_total(red2, &bcast);
+    int it;
+    for (it = 1; it <= a.maxit; ++it) {
+        // t = Lap(p), integral = r.t
+        loc = 0.0;
+        for (long o = t0; o < M; o += stride) {
+            const int i = (int)(o % a.mx), j = (int)((o / a.mx) % a.my), k = (int)(o / ((long)a.mx * a.my));
+            double lap = 0.0;
+            if (i < a.nx && j < a.ny && k < a.nz) lap = lap_at(a.p, i, j, k, a.mx, a.my, a.inv_dx2);
+            a.t[o] = lap;
+            loc = fma(a.res[o], lap, loc);
+        }
+        s = block_sum(loc, sh);
+        if (threadIdx.x == 0) red1[blockIdx.x] = s;
+        if (!grid_barrier(a.bar, a.status)) return;
+        const double integral = grid_total(red1, &bcast);
+        const double ak = pnorm / integral;
+        loc = 0.0;
+        for (long o = t0; o < M; o += stride) {
+            a.sol[o] = fma(ak, a.p[o], a.sol[o]);
+            const double r = fma(-ak, a.t[o], a.res[o]);
+            a.res[o] = r;
+            loc = fma(r, r, loc);
+        }
+        s = block_sum(loc, sh);
+        if (threadIdx.x == 0) red2[blockIdx.x] = s;
+        if (!grid_barrier(a.bar, a.status)) return;
+        const double nn = grid_total(red2, &bcast);
+        if (nn <= a.prec) break;
+        const double ck = nn / pnorm;
+        pnorm = nn;
+        for (long o = t0; o < M; o += stride) a.p[o] = fma(ck, a.p[o], a.res[o]);
+        if (!grid_barrier(a.bar, a.status)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.status[1] = it > a.maxit ? a.maxit : it;
+        if (it > a.maxit && a.status[0] == 0) a.status[0] = 1;
+    }
+}
+
+// Source and multipole Dirichlet values on the extended box.
+__global__ void k_coulomb_bound(const double* __restrict__ rho_p, const double* __restrict__ sh,
+                                const double* __restrict__ rpow, const double* __restrict__ mval,
+                                const double* __restrict__ mfac, int nmom, int nx, int ny, int nz,
+                                int mx, int my, int mz, double e2, double* __restrict__ src,
+                                double* __restrict__ sol) {
+    const long M = (long)mx * my * mz;
+    const long o = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= M) return;
+    const int i = (int)(o % mx), j = (int)((o / mx) % my), k = (int)(o / ((long)mx * my));
+    const double pi = 4.0 * atan2(1.0, 1.0);
+    if (i < nx && j < ny && k < nz) {
+        src[o] = -4 * pi * e2 * rho_p[i + nx * (j + (long)ny * k)];
+        return;
+    }
+    src[o] = 0.0;
+    double bc = 0.0;
+    for (int m = 0; m < nmom; ++m) {
+        const double value = mval[2 * m + 1] * mfac[m];
+        bc = bc + value * sh[(long)m * M + o] * e2 / rpow[(long)m * M + o];
+    }
+    if (bc != 0.0) sol[o] = bc;
+}
+
+__global__ void k_coulomb_out(const double* __restrict__ sol, const double* __restrict__ rho_p,
+                              int nx, int ny, int nz, int mx, int my, double fac,
+                              double* __restrict__ coul, double* __restrict__ coulex) {
+    const long V = (long)nx * ny * nz;
+    const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long)nx * ny));
+    coul[v] = sol[i + mx * (j + (long)my * k)];
+    coulex[v] = fac * pow(rho_p[v], 1 / 3.0);
+}
+
+// ---- host-side restatement of the spherical harmonics of the moments -----
+// legendre_pnm src/Mesh.f90:96-262; SphericalHarmonics src/Moments.f90:584-691
+void legendre(int n, int m, double x, double* cx) {
+    for (int i = 0; i < m; ++i) cx[i] = 0.0;
+    cx[m] = 1.0;
+    const double somx2 = std::sqrt(1.0 - x * x);
+    double fact = 1.0;
+    for (int i = 1; i <= m; ++i) { cx[m] = -cx[m] * fact * somx2; fact += 2.0; }
+    if (m == n) return;
+    cx[m + 1] = x * double(2 * m + 1) * cx[m];
+    for (int i = m + 2; i <= n; ++i)
+        cx[i] = (double(2 * i - 1) * x * cx[i - 1] - double(i + m - 1) * cx[i - 2]) / double(i - m);
+}
+
+double ipow(double x, int n) {
+    double r = 1.0;
+    for (int i = 0; i < n; ++i) r *= x;
+    return r;
+}
+
+double rlylm(int l, int m, int im, double X, double Y, double Z) {
+    const double pi = 4.0 * std::atan2(1.0, 1.0);
+    const int maxl = 10;
+    const double r = std::sqrt(X * X + Y * Y + Z * Z);
+    double leg[16];
+    legendre(maxl, m, Z / r, leg);
+    double fq = 1.0;
+    for (int q = 1; q <= 2 * m; ++q) fq = fq / double(l + m - q + 1);
+    double fac = ((m % 2) ? -1.0 : 1.0) * std::sqrt(fq) * ipow(r, l);
+    fac = fac * std::sqrt(double(2 * l + 1) / (4 * pi));
+    const double phi = std::atan2(Y, X);
+    return fac * leg[l] * (im ? std::sin(m * phi) : std::cos(m * phi));
+}
+
+}  // namespace
+
+// Moment table (IniMoments, src/Moments.f90:372-582; EV8 selection of
+// NewMoment_Electric), spherical harmonics on the stored and extended
+// meshes, the extended-box geometry and the initial guess (SetupCoulomb
+// :348-540, InitialGuess :542-581).
+int coulomb_setup(mg_ctx* c) {
+    const double pi = 4.0 * std::atan2(1.0, 1.0);
+    const int maxl = c->p.max_l_coul > 0 ? std::min(c->p.max_l_coul, 10) : 10;
+    std::vector<int> L, Mm, Im;
+    L.push_back(0); Mm.push_back(0); Im.push_back(0);
+    for (int l = 1; l <= 10; ++l)
+        for (int m = 0; m <= l; ++m)
+            for (int im = 0; im <= 1; ++im) {
+                if (c->p.pc && (l % 2)) continue;
+                if (c->p.tsc && im == 1) continue;
+                if (c->p.sc && (m % 2)) continue;
+                if (m == 0 && im == 1) continue;
+                L.push_back(l); Mm.push_back(m); Im.push_back(im);
+            }
+    const int nmom_all = (int)L.size();
+    int nmom_bc = 0;
+    while (nmom_bc < nmom_all && L[nmom_bc] <= maxl) ++nmom_bc;
+    c->n_moments = nmom_all;
+    for (int q = 0; q < nmom_all && q < kNumMoments; ++q) c->h_moment_l[q] = L[q];
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const long V = c->V;
+    std::vector<double> sh(nmom_all * V);
+    for (int q = 0; q < nmom_all; ++q)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const double X = c->p.dx / 2.0 + c->p.dx * i, Y = c->p.dx / 2.0 + c->p.dx * j,
+                                 Z = c->p.dx / 2.0 + c->p.dx * k;
+                    sh[q * V + i + nx * (j + (long)ny * k)] =
+                        q == 0 ? 1.0 / std::sqrt(4.0 * pi) : rlylm(L[q], Mm[q], Im[q], X, Y, Z);
+                }
+    MG_CUDA(cudaMalloc(&c->sh_mesh, sh.size() * sizeof(double)));
+    MG_CUDA(cudaMemcpy(c->sh_mesh, sh.data(), sh.size() * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMalloc(&c->moment_values, 2 * nmom_all * sizeof(double)));
+    MG_CUDA(cudaMemset(c->moment_values, 0, 2 * nmom_all * sizeof(double)));
+
+    // extended box: BCNumber = 2 planes beyond the stored box on each axis
+    c->mx = nx + 2; c->my = ny + 2; c->mz = nz + 2;
+    const long M = (long)c->mx * c->my * c->mz;
+    c->M = M;
+    std::vector<double> shx(nmom_bc * M), rp(nmom_bc * M), guess(M, 0.0), mfac(nmom_bc);
+    for (int q = 0; q < nmom_bc; ++q) mfac[q] = 4 * pi / (2 * L[q] + 1);
+    const double R = 1.25 * std::pow(c->p.neutrons + c->p.protons, 1.0 / 3.0);
+    const double charge = c->p.protons * c->f.e2, fac = charge / (2 * R);
+    for (int k = 0; k < c->mz; ++k)
+        for (int j = 0; j < c->my; ++j)
+            for (int i = 0; i < c->mx; ++i) {
+                const long o = i + c->mx * (j + (long)c->my * k);
+                const double X = (0.5 + i) * c->p.dx, Y = (0.5 + j) * c->p.dx, Z = (0.5 + k) * c->p.dx;
+                const double r = std::sqrt(X * X + Y * Y + Z * Z);
+                for (int q = 0; q < nmom_bc; ++q) {
+                    shx[q * M + o] = rlylm(L[q], Mm[q], Im[q], X, Y, Z);
+                    rp[q * M + o] = ipow(r, 2 * L[q] + 1);
+                }
+                if (i < nx && j < ny && k < nz) guess[o] = r <= R ? fac * (3 - r * r / (R * R)) : charge / r;
+            }
+    c->n_bc_moments = nmom_bc;
+    MG_CUDA(cudaMalloc(&c->sh_ext, shx.size() * sizeof(double) + 8));
+    MG_CUDA(cudaMalloc(&c->rpow_ext, rp.size() * sizeof(double) + 8));
+    MG_CUDA(cudaMalloc(&c->mfac, mfac.size() * sizeof(double) + 8));
+    MG_CUDA(cudaMemcpy(c->sh_ext, shx.data(), shx.size() * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(c->rpow_ext, rp.data(), rp.size() * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(c->mfac, mfac.data(), mfac.size() * sizeof(double), cudaMemcpyHostToDevice));
+    for (double** b : {&c->cpot, &c->csource, &c->cres, &c->cp, &c->ct})
+        MG_CUDA(cudaMalloc(b, M * sizeof(double)));
+    MG_CUDA(cudaMemcpy(c->cpot, guess.data(), M * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMalloc(&c->cg_bar, 4 * sizeof(unsigned)));
+    MG_CUDA(cudaMalloc(&c->cg_status, 4 * sizeof(int)));
+    int per_sm = 0;
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kThreads, 0));
+    if (per_sm < 1) return MG_ERR_CUDA;
+    c->cg_blocks = std::max(1, std::min(c->num_sms, div_up(M, kThreads)));
+    c->coulomb_init = true;
+    return MG_OK;
+}
+
+int coulomb_solve(mg_ctx* c, int* iters) {
+    if (!c->coulomb_init) MG_TRY(coulomb_setup(c));
+    const long M = c->M;
+    k_coulomb_bound<<<div_up(M, kThreads), kThreads, 0, c->stream>>>(
+        c->rho + c->V, c->sh_ext, c->rpow_ext, c->moment_values, c->mfac, c->n_bc_moments, c->nx,
+        c->ny, c->nz, c->mx, c->my, c->mz, c->f.e2, c->csource, c->cpot);
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaMemsetAsync(c->cg_bar, 0, 4 * sizeof(unsigned), c->stream));
+    MG_CUDA(cudaMemsetAsync(c->cg_status, 0, 4 * sizeof(int), c->stream));
+    CgArgs a;
+    a.sol = c->cpot; a.res = c->cres; a.p = c->cp; a.t = c->ct; a.src = c->csource;
+    a.red = c->red; a.bar = c->cg_bar; a.status = c->cg_status;
+    a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.mx = c->mx; a.my = c->my; a.mz = c->mz;
+    a.inv_dx2 = 1.0 / (c->p.dx * c->p.dx);
+    a.prec = 1.0e-9 / (c->p.dx * c->p.dx * c->p.dx * c->nx * c->ny * c->nz);
+    a.maxit = c->p.coulomb_max > 0 ? c->p.coulomb_max : 500;
+    void* args[] = {&a};
+    MG_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg, dim3(c->cg_blocks), dim3(kThreads), args,
+                                        0, c->stream));
+    const double pi = 4.0 * std::atan2(1.0, 1.0);
+    const double fac = -std::pow(3 / pi, 1 / 3.0) * c->f.e2;
+    k_coulomb_out<<<div_up(c->V, kThreads), kThreads, 0, c->stream>>>(
+        c->cpot, c->rho + c->V, c->nx, c->ny, c->nz, c->mx, c->my, fac, c->coulomb, c->coulex);
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaMemcpyAsync(c->h_cg_status, c->cg_status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
+                            c->stream));
+    if (iters) {
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+        *iters = c->h_cg_status[1];
+        if (c->h_cg_status[0] == 2) return MG_ERR_TIMEOUT;
+        if (c->h_cg_status[0] == 1) return MG_NOT_CONVERGED;
+    }
+    return MG_OK;
+}
+
+}  // namespace mg

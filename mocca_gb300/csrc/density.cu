@@ -1,0 +1,116 @@
+// density.cu -- density accumulation over the density basis, FP64.
+//
+// Replaces ComputeDensity (src/Densities.f90:431-550) for time-reversal
+// invariant functionals without tensor / N2LO terms:
+//   rho_q    += v^2 |psi|^2                      GetDensity src/Spwf.f90:536-546
+//   tau_q    += v^2 sum_m |d_m psi|^2             GetTau     :1897-1909
+//   divJ_q   += v^2 sum eps_ijk Im(d_i psi^+ sigma_k d_j psi)  GetNablaJ :2206-2243
+// then grad rho and lap rho with the Lagrange kernels (deriv.cu).
+// Grid = (point chunks) x (spwf groups): each thread walks its group's spwfs
+// in index order for one mesh point (16 doubles per spwf, coalesced along
+// x), writes six group partials, and k_dens_reduce adds the groups in order,
+// so the result is deterministic.
+#include "mg_internal.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void pauli(const double* p, int dir, double* o) {
+    if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
+    else if (dir == 2) { o[0] = p[3]; o[1] = -p[2]; o[2] = -p[1]; o[3] = p[0]; }
+    else { o[0] = p[0]; o[1] = p[1]; o[2] = -p[2]; o[3] = -p[3]; }
+}
+__device__ __forceinline__ double imag_mult(const double* a, const double* b) {
+    return a[0] * b[1] - a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_dens_partial(const double* __restrict__ psi, const double* __restrict__ der,
+               const double* __restrict__ occ, const int* __restrict__ qn, int nwt,
+               int per_group, long V, double* __restrict__ part) {
+    const long v = (long)blockIdx.x * kThreads + threadIdx.x;
+    const int g = blockIdx.y;
+    if (v >= V) return;
+    double acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    const int i0 = g * per_group, i1 = min(nwt, i0 + per_group);
+    for (int i = i0; i < i1; ++i) {
+        const double o = occ[i];
+        if (o == 0.0) continue;
+        const int it = (qn[4 * i] + 3) / 2 - 1;
+        const double* ps = psi + (long)i * 4 * V;
+        const double* dr = der + (long)i * 12 * V;
+        double p[4], d[3][4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            p[l] = ps[l * V + v];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) d[m][l] = dr[(m * 4 + l) * V + v];
+        }
+        const double den = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + p[3] * p[3];
+        double t = 0.0;
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+            t = t + (d[m][0] * d[m][0] + d[m][1] * d[m][1] + d[m][2] * d[m][2] + d[m][3] * d[m][3]);
+        // (i, j, k, eps_ijk) in the order of GetNablaJ
+        double nj = 0.0, s[4];
+        pauli(d[1], 3, s); nj = nj + imag_mult(d[0], s);
+        pauli(d[2], 2, s); nj = nj - imag_mult(d[0], s);
+        pauli(d[1], 1, s); nj = nj - imag_mult(d[2], s);
+        pauli(d[0], 2, s); nj = nj + imag_mult(d[2], s);
+        pauli(d[0], 3, s); nj = nj - imag_mult(d[1], s);
+        pauli(d[2], 1, s); nj = nj + imag_mult(d[1], s);
+        acc[it][0] = fma(o, den, acc[it][0]);
+        acc[it][1] = fma(o, t, acc[it][1]);
+        acc[it][2] = fma(o, nj, acc[it][2]);
+    }
+    double* pg = part + (long)g * 6 * V;
+#pragma unroll
+    for (int it = 0; it < 2; ++it)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) pg[(q * 2 + it) * V + v] = acc[it][q];
+}
+
+__global__ void k_dens_reduce(const double* __restrict__ part, int ngroups, long V,
+                              double* __restrict__ rho, double* __restrict__ tau,
+                              double* __restrict__ nablaj) {
+    const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int g = 0; g < ngroups; ++g)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) a[q] += part[((long)g * 6 + q) * V + v];
+    rho[v] = a[0]; rho[V + v] = a[1];
+    tau[v] = a[2]; tau[V + v] = a[3];
+    nablaj[v] = a[4]; nablaj[V + v] = a[5];
+}
+
+}  // namespace
+
+int density_groups(const mg_ctx* c) {
+    const int chunks = div_up(c->V, kThreads);
+    int g = std::max(1, (4 * c->num_sms + chunks - 1) / chunks);
+    return std::min(g, c->p.nwt);
+}
+
+int densities(mg_ctx* c) {
+    const int b = c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS;
+    Basis& B = c->bas[b];
+    if (!B.have_qn) return MG_ERR_STATE;
+    const long V = c->V;
+    const int ng = density_groups(c);
+    const int per = div_up(c->p.nwt, ng);
+    dim3 grid(div_up(V, kThreads), ng);
+    k_dens_partial<<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.occ, B.qn, c->p.nwt, per, V,
+                                                     c->red);
+    MG_CUDA(cudaGetLastError());
+    k_dens_reduce<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(c->red, ng, V, c->rho, c->tau,
+                                                                   c->nablaj);
+    MG_CUDA(cudaGetLastError());
+    // grad rho, lap rho: the first two field jobs
+    return run_jobs(c, c->field_jobs, 2);
+}
+
+}  // namespace mg

@@ -1,0 +1,187 @@
+// energy.cu -- total energy, FP64 (CompEnergy, src/Energy.f90:62-179).
+//
+// Device side: per-spwf <psi|lap psi> of the density basis (CompKinetic,
+// :1426-1456) and block partials of the mesh integrals of compSkyrme
+// (:623-860, time-even terms) and of the Coulomb direct / Slater exchange
+// energies (src/Coulomb.f90:215-253).  Host side: the block partials are
+// added in block order and combined exactly as CompEnergy / SpwfEnergy do.
+#include <cmath>
+#include <cstring>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTerms = 20;
+
+// per-spwf dot products over 4V, block partials
+__global__ void __launch_bounds__(kThreads)
+k_dots(const double* __restrict__ a, const double* __restrict__ b, long V4,
+       double* __restrict__ part) {
+    const int i = blockIdx.y;
+    double s = 0.0;
+    for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4; o += (long)gridDim.x * kThreads)
+        s = fma(a[(long)i * V4 + o], b[(long)i * V4 + o], s);
+    __shared__ double red[kThreads / 32];
+    for (int q = 16; q > 0; q >>= 1) s += __shfl_xor_sync(0xffffffffu, s, q);
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < kThreads / 32; ++q) t += red[q];
+        part[(long)i * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+struct ECoef {
+    double B4, B6, B8a, B8b, B9q, byt3a, byt3b, B7b;
+};
+
+__global__ void __launch_bounds__(kThreads)
+k_energy_partial(const double* __restrict__ rho, const double* __restrict__ tau,
+                 const double* __restrict__ laprho, const double* __restrict__ nablaj,
+                 const double* __restrict__ coul, ECoef k, long V, double* __restrict__ part) {
+    double acc[kTerms];
+#pragma unroll
+    for (int q = 0; q < kTerms; ++q) acc[q] = 0.0;
+    for (long v = (long)blockIdx.x * kThreads + threadIdx.x; v < V; v += (long)gridDim.x * kThreads) {
+        const double rn = rho[v], rp = rho[V + v];
+        const double rt = rn + rp;
+        const double tt = tau[v] + tau[V + v];
+        const double lt = laprho[v] + laprho[V + v];
+        const double jt = nablaj[v] + nablaj[V + v];
+        const double pa = pow(rt, k.byt3a);
+        acc[0] += rt * rt;                 // B1
+        acc[1] += rt * tt;                 // B3
+        acc[2] += rt * lt;                 // B5
+        acc[3] += pow(rt, 2 + k.byt3a);    // B7a
+        acc[4] += rt * jt;                 // B9
+        if (k.B7b != 0.0) acc[5] += pow(rt, 2 + k.byt3b);
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            const double r = rho[it * V + v];
+            acc[6 + it] += r * r;                       // B2
+            acc[8 + it] += r * tau[it * V + v];         // B4
+            acc[10 + it] += r * laprho[it * V + v];     // B6
+            acc[12 + it] += r * r * pa;                 // B8a
+            acc[14 + it] += r * nablaj[it * V + v];     // B9q
+            if (k.B8b != 0.0) acc[16 + it] += r * r * pow(rt, k.byt3b);
+        }
+        acc[18] += rp * coul[v];                        // Coulomb direct
+        acc[19] += rp * pow(rp, 1 / 3.0);               // Slater exchange
+    }
+    __shared__ double red[kThreads / 32];
+    for (int q = 0; q < kTerms; ++q) {
+        double s = acc[q];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        __syncthreads();
+        if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+            part[(long)blockIdx.x * kTerms + q] = t;
+        }
+    }
+}
+
+}  // namespace
+
+// nwt dot products <a_i|b_i> * dv of a basis into host array out.
+int basis_dots(mg_ctx* c, const double* a, const double* b, double* out) {
+    const long V4 = 4 * c->V;
+    const int nch = std::max(1, std::min(64, div_up(V4, kThreads * 8)));
+    k_dots<<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
+    MG_CUDA(cudaGetLastError());
+    std::vector<double> h((size_t)nch * c->p.nwt);
+    MG_CUDA(cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < c->p.nwt; ++i) {
+        double s = 0.0;
+        for (int q = 0; q < nch; ++q) s += h[(size_t)i * nch + q];
+        out[i] = s * c->dv;
+    }
+    return MG_OK;
+}
+
+int energy(mg_ctx* c, mg_energy_terms* out) {
+    std::memset(out, 0, sizeof(*out));
+    const int db = c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS;
+    Basis& D = c->bas[db];
+    const int nwt = c->p.nwt;
+    const long V = c->V;
+    const mg_skyrme_b& B = c->B;
+    std::vector<double> ip(nwt);
+    MG_TRY(basis_dots(c, D.psi, D.lap, ip.data()));
+    std::vector<double> occ(nwt), e(nwt);
+    MG_CUDA(cudaMemcpyAsync(occ.data(), D.occ, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaMemcpyAsync(e.data(), D.e, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    const int nblk = std::max(1, std::min(2 * c->num_sms, div_up(V, kThreads)));
+    ECoef k{B.B4, B.B6, B.B8a, B.B8b, B.B9q, B.byt3a, B.byt3b, B.B7b};
+    k_energy_partial<<<nblk, kThreads, 0, c->stream>>>(c->rho, c->tau, c->laprho, c->nablaj,
+                                                       c->coulomb, k, V, c->red);
+    MG_CUDA(cudaGetLastError());
+    std::vector<double> part((size_t)nblk * kTerms);
+    MG_CUDA(cudaMemcpyAsync(part.data(), c->red, part.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    double S[kTerms] = {0};
+    for (int b = 0; b < nblk; ++b)
+        for (int q = 0; q < kTerms; ++q) S[q] += part[(size_t)b * kTerms + q];
+
+    double kin[2] = {0, 0};
+    for (int l = 0; l < nwt; ++l) {
+        const int it = (D.h_qn[4 * l] + 3) / 2 - 1;
+        kin[it] = kin[it] + occ[l] * ip[l];
+    }
+    for (int it = 0; it < 2; ++it) out->kinetic[it] = -kin[it] / 2.0 * c->f.hbm;
+    double* t = out->skyrme;
+    t[0] = B.B1 * S[0];
+    t[1] = B.B2 * (S[6] + S[7]);
+    t[2] = B.B3 * S[1];
+    t[3] = B.B4 * S[8] + B.B4 * S[9];
+    t[6] = B.B5 * S[2];
+    t[7] = B.B6 * S[10] + B.B6 * S[11];
+    t[8] = B.B7a * S[3];
+    t[9] = B.B8a * S[12] + B.B8a * S[13];
+    t[10] = B.B9 * S[4];
+    t[11] = B.B9q * S[14] + B.B9q * S[15];
+    t[32] = B.B7b * S[5];
+    t[33] = B.B8b * S[16] + B.B8b * S[17];
+    for (int q = 0; q < 36; ++q) t[q] *= c->dv;
+    double sk = 0.0;
+    for (int q = 0; q < 36; ++q) sk += t[q];
+    const double pi = 4.0 * std::atan2(1.0, 1.0);
+    double ec = 0.0, ex = 0.0;
+    if (c->p.coulomb_solver != 0) {
+        ec = S[18] * c->dv * 0.5;
+        if (c->f.cexchange >= 1) ex = -std::pow(3 / pi, 1 / 3.0) * c->f.e2 * 0.75 * c->dv * S[19];
+    }
+    out->coulomb = ec;
+    out->coulomb_exchange = ex;
+    if (c->f.com1body > 0) {
+        const double mt = c->p.neutrons * c->f.nucleonmass[0] + c->p.protons * c->f.nucleonmass[1];
+        for (int it = 0; it < 2; ++it) out->com[0][it] = -out->kinetic[it] * c->f.nucleonmass[it] / mt;
+    }
+    out->pairing[0] = c->pairing_energy[0];
+    out->pairing[1] = c->pairing_energy[1];
+    const double com = out->com[0][0] + out->com[1][0] + out->com[0][1] + out->com[1][1];
+    out->total = sk + (out->kinetic[0] + out->kinetic[1]) + ec + com + ex +
+                 (out->pairing[0] + out->pairing[1]);
+    double sp = 0.0;
+    for (int i = 0; i < nwt; ++i) sp += occ[i] * e[i];
+    sp = 0.5 * (sp + (out->kinetic[0] + out->kinetic[1])) -
+         0.5 * B.byt3a * ((t[8] + t[9]) + (t[16] + t[17])) -
+         0.5 * B.byt3b * ((t[32] + t[33]) + (t[34] + t[35])) + ex / 3.0;
+    sp = sp + (out->pairing[0] + out->pairing[1]);
+    if (c->f.com1body > 0) sp = sp + (out->com[0][0] + out->com[0][1]) / 2.0;
+    if (c->f.com2body == 1) sp = sp + (out->com[1][0] + out->com[1][1]);
+    out->sp_energy = sp;
+    return MG_OK;
+}
+
+}  // namespace mg

@@ -1,0 +1,492 @@
+// host.cu -- the extern "C" entry points of libmocca_gpu (include/mocca_gpu.h).
+//
+// Each entry point validates its arguments, enqueues its kernels on the
+// context's stream and returns an int status; the Fortran shim turns a
+// non-zero status into the reference's stp() (src/GenInfo.f90:84-177).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "mg_internal.cuh"
+
+using namespace mg;
+
+namespace {
+
+const double kPi = 4.0 * std::atan2(1.0, 1.0);
+
+bool valid_basis(const mg_ctx* c, int b) {
+    if (b == MG_HF_BASIS) return true;
+    return b == MG_CAN_BASIS && c->p.pairing == MG_PAIRING_HFB;
+}
+
+void free_all(mg_ctx* c) {
+    auto F = [](void* p) { if (p) cudaFree(p); };
+    F(c->mats);
+    for (int b = 0; b < 2; ++b) {
+        Basis& B = c->bas[b];
+        F(B.psi); F(B.der); F(B.lap); F(B.qn); F(B.occ); F(B.e); F(B.disp); F(B.jobs);
+    }
+    F(c->updates); F(c->hbuf);
+    F(c->rho); F(c->tau); F(c->nablaj); F(c->derrho); F(c->laprho);
+    F(c->U); F(c->Bp); F(c->nablaB); F(c->W); F(c->divW); F(c->divw_tmp); F(c->field_jobs);
+    F(c->gs_S); F(c->gs_R); F(c->gs_index);
+    F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
+    F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
+    F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags);
+    if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host helpers
+// ---------------------------------------------------------------------------
+extern "C" int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* B) {
+    // CalcEDFCoef, src/Force.f90:467-560 (J2Terms = .false.)
+    if (!f || !B) return MG_ERR_ARG;
+    std::memset(B, 0, sizeof(*B));
+    B->B1 = f->t0 * (1.0 + 0.5 * f->x0) / 2.0;
+    B->B2 = -f->t0 * (0.5 + f->x0) / 2.0;
+    B->B3 = (f->t1 * (1 + 0.5 * f->x1) + f->t2 * (1 + 0.5 * f->x2)) / 4.0;
+    B->B4 = -(f->t1 * (0.5 + f->x1) - f->t2 * (0.5 + f->x2)) / 4.0;
+    B->B5 = -(3.0 * f->t1 * (1 + f->x1 / 2.0) - f->t2 * (1 + f->x2 / 2.0)) / 16.0;
+    B->B6 = (3.0 * f->t1 * (f->x1 + 0.5) + f->t2 * (f->x2 + 0.5)) / 16.0;
+    B->B7a = f->t3a * (1 + f->x3a / 2.0) / 12.0;
+    B->B8a = -f->t3a * (f->x3a + 0.5) / 12.0;
+    B->B7b = f->t3b * (1 + f->x3b / 2.0) / 12.0;
+    B->B8b = -f->t3b * (f->x3b + 0.5) / 12.0;
+    B->B9 = -f->wso / 2.0;
+    B->B9q = -f->wsoq / 2.0;
+    B->byt3a = f->yt3a;
+    B->byt3b = f->yt3b;
+    if (!trc) {
+        B->B10 = f->t0 * f->x0 / 4.0;
+        B->B11 = -f->t0 / 4.0;
+        B->B12a = f->t3a * f->x3a / 24.0;
+        B->B13a = -f->t3a / 24.0;
+        B->B12b = f->t3b * f->x3b / 24.0;
+        B->B13b = -f->t3b / 24.0;
+    }
+    B->B16 = -(3.0 / 8.0) * (f->te + f->to);
+    B->B17 = (3.0 / 8.0) * (f->te - f->to);
+    return MG_OK;
+}
+
+extern "C" int mg_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2) {
+    // Baye-Heenen coefficients on the full line of N points (IniLag,
+    // src/Derivatives.f90:899-973):
+    //   C1(k) = pi/(N dx) (-1)^k / sin(pi k/N)
+    //   C2(k) = (-1)^(k+1) 2 (pi/(N dx))^2 cos(pi k/N) / sin(pi k/N)^2
+    //   diag  = -pi^2/(3 dx^2) (1 - 1/N^2)
+    // folded (reduceLag, :975-1078): M_s(i,j) = sgn(i-j) C1(|i-j|) + s C1(i+j-1),
+    // L_s(i,j) = C2(|i-j|) + s C2(i+j-1) (+ diag on i=j), s = -1 / +1.
+    if (n <= 0 || n > kMaxN || !(dx > 0) || !d1 || !d2) return MG_ERR_ARG;
+    const int N = folded ? 2 * n : n;
+    std::vector<double> C1(N + 1, 0.0), C2(N + 1, 0.0);
+    const double factor = kPi / N, dxf = factor / dx;
+    const double diag = -(kPi * kPi) / (3.0 * (dx * dx)) * (1.0 - 1.0 / double(N * N));
+    for (int k = 1; k < N; ++k) {
+        const double s = std::sin(factor * k), c = std::cos(factor * k);
+        const double sg = (k % 2 == 0) ? 1.0 : -1.0;
+        C1[k] = dxf * sg / s;
+        C2[k] = -sg * 2.0 * (dxf * dxf) * c / (s * s);
+    }
+    const long nn = (long)n * n;
+    for (int i = 1; i <= n; ++i)
+        for (int j = 1; j <= n; ++j) {
+            const long o = (long)(i - 1) * n + (j - 1);
+            const double sgn = i > j ? 1.0 : (i < j ? -1.0 : 0.0);
+            const double t1 = i == j ? 0.0 : sgn * C1[std::abs(i - j)];
+            const double t2 = i == j ? diag : C2[std::abs(i - j)];
+            if (folded) {
+                const double e1 = C1[i + j - 1], e2 = C2[i + j - 1];
+                d1[o] = t1 - e1; d1[nn + o] = t1 + e1;
+                d2[o] = t2 - e2; d2[nn + o] = t2 + e2;
+            } else {
+                d1[o] = d1[nn + o] = t1;
+                d2[o] = d2[nn + o] = t2;
+            }
+        }
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg_ctx** out) {
+    if (!p || !f || !out) return MG_ERR_ARG;
+    *out = nullptr;
+    if (p->nx <= 0 || p->ny <= 0 || p->nz <= 0 || p->nx > kMaxN || p->ny > kMaxN ||
+        p->nz > kMaxN || !(p->dx > 0) || p->nwt <= 0)
+        return MG_ERR_ARG;
+    const bool ev8 = p->pc && p->sc && p->tsc;
+    const bool full = !p->pc && !p->sc && !p->tsc;
+    if (!ev8 && !full) return MG_ERR_ARG;
+    if (p->precision != MG_FP64 && p->precision != MG_MIXED) return MG_ERR_ARG;
+    if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
+    int dev = 0;
+    MG_CUDA(cudaGetDevice(&dev));
+    mg_ctx* c = new mg_ctx();
+    c->p = *p;
+    c->f = *f;
+    mg_skyrme_coefficients(f, p->trc, &c->B);
+    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz;
+    c->V = (long)p->nx * p->ny * p->nz;
+    const int nsym = (p->pc ? 1 : 0) + (p->sc ? 1 : 0) + (p->tsc ? 1 : 0);
+    c->dv = p->dx * p->dx * p->dx * std::pow(2.0, nsym);  // src/GenInfo.f90:296
+    c->folded = ev8;
+    int st = MG_OK;
+    auto fail = [&](int s) { free_all(c); delete c; return s; };
+    if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return fail(MG_ERR_CUDA);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(MG_ERR_CUDA);
+        c->own_stream = true;
+    }
+    const long V = c->V, nwt = p->nwt;
+    auto A = [&](double** ptr, long n) {
+        if (cudaMalloc(ptr, std::max(1L, n) * sizeof(double)) != cudaSuccess) return false;
+        return cudaMemset(*ptr, 0, std::max(1L, n) * sizeof(double)) == cudaSuccess;
+    };
+    bool ok = true;
+    const int nb = p->pairing == MG_PAIRING_HFB ? 2 : 1;
+    for (int b = 0; b < nb && ok; ++b) {
+        Basis& B = c->bas[b];
+        ok = A(&B.psi, nwt * 4 * V) && A(&B.der, nwt * 12 * V) && A(&B.lap, nwt * 4 * V) &&
+             A(&B.occ, nwt) && A(&B.e, nwt) && A(&B.disp, nwt) &&
+             cudaMalloc(&B.qn, nwt * 4 * sizeof(int)) == cudaSuccess &&
+             cudaMalloc(&B.jobs, nwt * 4 * sizeof(GridJob)) == cudaSuccess;
+        B.h_qn.assign(nwt * 4, 1);
+        B.h_occ.assign(nwt, 0.0);
+        B.h_e.assign(nwt, 0.0);
+        B.h_disp.assign(nwt, 0.0);
+    }
+    ok = ok && A(&c->updates, nwt * 4 * V) && A(&c->rho, 2 * V) && A(&c->tau, 2 * V) &&
+         A(&c->nablaj, 2 * V) && A(&c->derrho, 6 * V) && A(&c->laprho, 2 * V) &&
+         A(&c->U, 2 * V) && A(&c->Bp, 2 * V) && A(&c->nablaB, 6 * V) && A(&c->W, 18 * V) &&
+         A(&c->divW, 6 * V) && A(&c->divw_tmp, 18 * V) && A(&c->coulomb, V) && A(&c->coulex, V);
+    if (!ok) return fail(MG_ERR_CUDA);
+    // reduction scratch: the largest of the per-kernel partial tables
+    const long hp = nwt * div_up(V, 256) * 2;
+    const long dens = (long)density_groups(c) * 6 * V;
+    const long dots = 64 * nwt;
+    const long en = 2L * c->num_sms * 20 + 4L * c->num_sms;
+    c->red_len = (size_t)std::max(std::max(hp, dens), std::max(dots, en));
+    if (!A(&c->red, (long)c->red_len)) return fail(MG_ERR_CUDA);
+    if (cudaMalloc(&c->flags, 16 * sizeof(int)) != cudaSuccess ||
+        cudaMemset(c->flags, 0, 16 * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&c->h_cg_status, 4 * sizeof(int)) != cudaSuccess)
+        return fail(MG_ERR_CUDA);
+    if ((st = upload_matrices(c)) != MG_OK) return fail(st);
+    if ((st = build_field_jobs(c)) != MG_OK) return fail(st);
+    if (ev8 && p->coulomb_solver != 0) {
+        if ((st = coulomb_setup(c)) != MG_OK) return fail(st);
+    }
+    *out = c;
+    return MG_OK;
+}
+
+extern "C" int mg_destroy(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return MG_OK;
+}
+
+extern "C" int mg_synchronize(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Transfers
+// ---------------------------------------------------------------------------
+extern "C" int mg_upload_spinors(mg_ctx* c, int b, const double* const* grids, const int* qn,
+                                 int first, int count) {
+    if (!c || !valid_basis(c, b) || first < 0 || count < 0 || first + count > c->p.nwt)
+        return MG_ERR_ARG;
+    Basis& B = c->bas[b];
+    const long V4 = 4 * c->V;
+    if (grids)
+        for (int i = 0; i < count; ++i) {
+            if (!grids[i]) return MG_ERR_ARG;
+            MG_CUDA(cudaMemcpyAsync(B.psi + (long)(first + i) * V4, grids[i], V4 * sizeof(double),
+                                    cudaMemcpyHostToDevice, c->stream));
+        }
+    if (qn) {
+        for (int i = 0; i < 4 * count; ++i) {
+            const int q = qn[i];
+            if ((i % 4 == 0 && q != 1 && q != -1) || q < -1 || q > 1) return MG_ERR_ARG;
+            B.h_qn[4 * first + i] = q;
+        }
+        MG_CUDA(cudaMemcpyAsync(B.qn, B.h_qn.data(), B.h_qn.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, c->stream));
+        if (first + count == c->p.nwt || B.have_qn) {
+            B.have_qn = true;
+            MG_TRY(build_basis_jobs(c, b));
+            if (b == MG_HF_BASIS) c->gs_nblk = 0;  // rebuild Gram-Schmidt blocks
+        }
+    }
+    return MG_OK;
+}
+
+extern "C" int mg_download_spinors(mg_ctx* c, int b, double* const* grids, int first, int count) {
+    if (!c || !valid_basis(c, b) || !grids || first < 0 || count < 0 || first + count > c->p.nwt)
+        return MG_ERR_ARG;
+    const long V4 = 4 * c->V;
+    for (int i = 0; i < count; ++i)
+        MG_CUDA(cudaMemcpyAsync(grids[i], c->bas[b].psi + (long)(first + i) * V4,
+                                V4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_download_derivatives(mg_ctx* c, int b, double* const* der, double* const* lap,
+                                       int first, int count) {
+    if (!c || !valid_basis(c, b) || first < 0 || count < 0 || first + count > c->p.nwt)
+        return MG_ERR_ARG;
+    const long V = c->V;
+    for (int i = 0; i < count; ++i) {
+        if (der && der[i])
+            MG_CUDA(cudaMemcpyAsync(der[i], c->bas[b].der + (long)(first + i) * 12 * V,
+                                    12 * V * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (lap && lap[i])
+            MG_CUDA(cudaMemcpyAsync(lap[i], c->bas[b].lap + (long)(first + i) * 4 * V,
+                                    4 * V * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_set_occupations(mg_ctx* c, int b, const double* occ) {
+    if (!c || !valid_basis(c, b) || !occ) return MG_ERR_ARG;
+    std::copy(occ, occ + c->p.nwt, c->bas[b].h_occ.begin());
+    MG_CUDA(cudaMemcpyAsync(c->bas[b].occ, c->bas[b].h_occ.data(), c->p.nwt * sizeof(double),
+                            cudaMemcpyHostToDevice, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_get_occupations(mg_ctx* c, int b, double* occ) {
+    if (!c || !valid_basis(c, b) || !occ) return MG_ERR_ARG;
+    MG_CUDA(cudaMemcpyAsync(occ, c->bas[b].occ, c->p.nwt * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_set_energies(mg_ctx* c, int b, const double* e) {
+    if (!c || !valid_basis(c, b) || !e) return MG_ERR_ARG;
+    MG_CUDA(cudaMemcpyAsync(c->bas[b].e, e, c->p.nwt * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_get_energies(mg_ctx* c, int b, double* e, double* disp) {
+    if (!c || !valid_basis(c, b)) return MG_ERR_ARG;
+    if (e)
+        MG_CUDA(cudaMemcpyAsync(e, c->bas[b].e, c->p.nwt * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+    if (disp)
+        MG_CUDA(cudaMemcpyAsync(disp, c->bas[b].disp, c->p.nwt * sizeof(double),
+                                cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Compute
+// ---------------------------------------------------------------------------
+extern "C" int mg_derive_basis(mg_ctx* c, int b) {
+    if (!c || !valid_basis(c, b)) return MG_ERR_ARG;
+    return derive_basis(c, b);
+}
+
+extern "C" int mg_derive_all(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    MG_TRY(derive_basis(c, MG_HF_BASIS));
+    if (c->p.pairing == MG_PAIRING_HFB) MG_TRY(derive_basis(c, MG_CAN_BASIS));
+    return MG_OK;
+}
+
+extern "C" int mg_hpsi(mg_ctx* c, int b, double* hpsi, double* e, double* disp) {
+    if (!c || !valid_basis(c, b)) return MG_ERR_ARG;
+    const long total = (long)c->p.nwt * 4 * c->V;
+    double* dev_out = nullptr;
+    if (hpsi) {
+        if (!c->hbuf) MG_CUDA(cudaMalloc(&c->hbuf, total * sizeof(double)));
+        dev_out = c->hbuf;
+    }
+    MG_TRY(hpsi_basis(c, b, dev_out, false, 0.0, 0.0));
+    if (hpsi)
+        MG_CUDA(cudaMemcpyAsync(hpsi, c->hbuf, total * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+    return mg_get_energies(c, b, e, disp);
+}
+
+extern "C" int mg_grad_desc(mg_ctx* c, double dt, double momentum) {
+    if (!c) return MG_ERR_ARG;
+    MG_TRY(hpsi_basis(c, MG_HF_BASIS, nullptr, true, dt / c->f.hbar, momentum));
+    return gram_schmidt_impl(c, c->updates);
+}
+
+extern "C" int mg_gram_schmidt(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    return gram_schmidt(c);
+}
+
+extern "C" int mg_hf_fill(mg_ctx* c) {
+    // NaiveFill, src/HartreeFock.f90:177-260 (no blocking)
+    if (!c) return MG_ERR_ARG;
+    Basis& B = c->bas[MG_HF_BASIS];
+    const int nwt = c->p.nwt;
+    std::vector<double> e(nwt);
+    MG_CUDA(cudaMemcpyAsync(e.data(), B.e, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int> order(nwt);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return e[a] < e[b2]; });
+    std::vector<double> occ(nwt, 0.0);
+    const int pub = c->p.trc ? (int)std::floor(c->p.protons / 2) : (int)std::floor(c->p.protons);
+    const int nub = c->p.trc ? (int)std::floor(c->p.neutrons / 2) : (int)std::floor(c->p.neutrons);
+    int np = 0, nn = 0;
+    for (int i = 0; i < nwt && np < pub; ++i)
+        if (occ[order[i]] == 0.0 && B.h_qn[4 * order[i]] == 1) { occ[order[i]] = 1.0; ++np; }
+    for (int i = 0; i < nwt && nn < nub; ++i)
+        if (occ[order[i]] == 0.0 && B.h_qn[4 * order[i]] == -1) { occ[order[i]] = 1.0; ++nn; }
+    if (c->p.trc)
+        for (double& o : occ) o = 2.0 * o;
+    return mg_set_occupations(c, MG_HF_BASIS, occ.data());
+}
+
+extern "C" int mg_update_densities(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    return densities(c);
+}
+
+static int copy_out(mg_ctx* c, double* dst, const double* src, long n) {
+    if (!dst) return MG_OK;
+    MG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return MG_OK;
+}
+static int copy_in(mg_ctx* c, double* dst, const double* src, long n) {
+    if (!src) return MG_OK;
+    MG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_get_densities(mg_ctx* c, double* rho, double* tau, double* nablaj,
+                                double* derrho, double* laprho) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(copy_out(c, rho, c->rho, 2 * V));
+    MG_TRY(copy_out(c, tau, c->tau, 2 * V));
+    MG_TRY(copy_out(c, nablaj, c->nablaj, 2 * V));
+    MG_TRY(copy_out(c, derrho, c->derrho, 6 * V));
+    MG_TRY(copy_out(c, laprho, c->laprho, 2 * V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_set_densities(mg_ctx* c, const double* rho, const double* tau,
+                                const double* nablaj, const double* derrho, const double* laprho) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(copy_in(c, c->rho, rho, 2 * V));
+    MG_TRY(copy_in(c, c->tau, tau, 2 * V));
+    MG_TRY(copy_in(c, c->nablaj, nablaj, 2 * V));
+    MG_TRY(copy_in(c, c->derrho, derrho, 6 * V));
+    MG_TRY(copy_in(c, c->laprho, laprho, 2 * V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_calculate_moments(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    return moments(c);
+}
+
+extern "C" int mg_solve_coulomb(mg_ctx* c, int* iters) {
+    if (!c || !c->folded) return MG_ERR_ARG;
+    int it = 0;
+    const int st = coulomb_solve(c, &it);
+    if (iters) *iters = it;
+    return st;
+}
+
+extern "C" int mg_construct_potentials(mg_ctx* c, int* iters) {
+    if (!c) return MG_ERR_ARG;
+    int st = MG_OK;
+    if (c->p.coulomb_solver != 0) {
+        if (!c->folded) return MG_ERR_ARG;
+        int it = 0;
+        st = coulomb_solve(c, iters ? &it : nullptr);
+        if (st < 0) return st;
+        if (iters) *iters = it;
+    } else if (iters) {
+        *iters = 0;
+    }
+    MG_TRY(potentials(c));
+    return st;
+}
+
+extern "C" int mg_get_potentials(mg_ctx* c, double* u, double* b, double* nablab, double* w,
+                                 double* divw, double* coul, double* coulex) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(copy_out(c, u, c->U, 2 * V));
+    MG_TRY(copy_out(c, b, c->Bp, 2 * V));
+    MG_TRY(copy_out(c, nablab, c->nablaB, 6 * V));
+    MG_TRY(copy_out(c, w, c->W, 18 * V));
+    MG_TRY(copy_out(c, divw, c->divW, 6 * V));
+    MG_TRY(copy_out(c, coul, c->coulomb, V));
+    MG_TRY(copy_out(c, coulex, c->coulex, V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_set_potentials(mg_ctx* c, const double* u, const double* b,
+                                 const double* nablab, const double* w, const double* divw) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(copy_in(c, c->U, u, 2 * V));
+    MG_TRY(copy_in(c, c->Bp, b, 2 * V));
+    MG_TRY(copy_in(c, c->nablaB, nablab, 6 * V));
+    MG_TRY(copy_in(c, c->W, w, 18 * V));
+    MG_TRY(copy_in(c, c->divW, divw, 6 * V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_energy(mg_ctx* c, mg_energy_terms* out) {
+    if (!c || !out) return MG_ERR_ARG;
+    return energy(c, out);
+}
+
+extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
+                          mg_energy_terms* out) {
+    // Evolve loop body, src/Main.f90:255-328 (HF: SolvePairing = NaiveFill)
+    if (!c || n_iter < 0) return MG_ERR_ARG;
+    if (c->p.pairing != MG_PAIRING_HF) return MG_ERR_ARG;
+    int st = MG_OK;
+    for (int k = 0; k < n_iter; ++k) {
+        MG_TRY(mg_grad_desc(c, dt, momentum));
+        MG_TRY(mg_hf_fill(c));
+        MG_TRY(mg_derive_all(c));
+        MG_TRY(densities(c));
+        MG_TRY(moments(c));
+        st = mg_construct_potentials(c, nullptr);
+        if (st < 0) return st;
+        if (out) MG_TRY(energy(c, out));
+    }
+    return st;
+}

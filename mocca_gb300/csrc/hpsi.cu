@@ -1,0 +1,181 @@
+// hpsi.cu -- action of the single-particle Hamiltonian, FP64, with the fused
+// imaginary-time (GradDesc) update.
+//
+// h.psi = B + U + W (src/ImaginaryTime.f90:213-304, time-even fields):
+//   B = -(B_q + hbm/2 mu_red) lap psi - sum_m d_m B_q d_m psi   ActionOfBNew
+//                                                  src/MeanFields.f90:811-851
+//   U = U_q psi                                    ActionOfU :792-809
+//   W = -i [sum_mn W_mn sigma_n d_m psi + 1/2 sum_n (div W)_n sigma_n psi]
+//                                                  ActionOfW :1029-1065
+// One thread owns one mesh point of one spwf: it reads psi, Der(1:3), Lap at
+// that point (20 doubles) and the isospin's fields (L2-resident), and writes
+// either h.psi or, for a GradDesc step (src/ImaginaryTime.f90:467-491),
+// psi <- psi - dt/hbar h.psi + mu*update and update <- psi_old in place, so
+// h.psi never goes to HBM.  The per-spwf sums <psi|h psi> and <h psi|h psi>
+// are reduced per block into a partial table and finished in block order
+// (deterministic).
+#include "mg_internal.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct Fields {
+    const double* U;
+    const double* B;
+    const double* nablaB;
+    const double* W;
+    const double* divW;
+};
+
+__device__ __forceinline__ void pauli(const double* p, int dir, double* o) {
+    if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
+    else if (dir == 2) { o[0] = p[3]; o[1] = -p[2]; o[2] = -p[1]; o[3] = p[0]; }
+    else { o[0] = p[0]; o[1] = p[1]; o[2] = -p[2]; o[3] = -p[3]; }
+}
+
+template <bool kGradStep>
+__global__ void __launch_bounds__(kThreads)
+k_hpsi(double* __restrict__ psi, const double* __restrict__ der,
+       const double* __restrict__ lap, const int* __restrict__ qn, Fields F,
+       double* __restrict__ hout, double* __restrict__ upd, double* __restrict__ partial,
+       long V, double kin0, double kin1, double fac, double mom) {
+    const int i = blockIdx.y;
+    const long v = (long)blockIdx.x * kThreads + threadIdx.x;
+    double s_eh = 0.0, s_hh = 0.0;
+    if (v < V) {
+        const int it = (qn[4 * i] + 3) / 2 - 1;
+        const double kin = it == 0 ? kin0 : kin1;
+        double* ps = psi + (long)i * 4 * V;
+        const double* dr = der + (long)i * 12 * V;
+        const double* lp = lap + (long)i * 4 * V;
+        double p[4], d[3][4], L[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            p[l] = ps[l * V + v];
+            L[l] = lp[l * V + v];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) d[m][l] = dr[(m * 4 + l) * V + v];
+        }
+        const double Bq = F.B[it * V + v];
+        const double Uq = F.U[it * V + v];
+        const double nb0 = F.nablaB[(it * 3 + 0) * V + v];
+        const double nb1 = F.nablaB[(it * 3 + 1) * V + v];
+        const double nb2 = F.nablaB[(it * 3 + 2) * V + v];
+        double w[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int mu = 0; mu < 3; ++mu)
+#pragma unroll
+            for (int nu = 0; nu < 3; ++nu) {
+                double s[4];
+                pauli(d[mu], nu + 1, s);
+                const double wv = F.W[((it * 3 + nu) * 3 + mu) * V + v];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) w[l] = fma(wv, s[l], w[l]);
+            }
+#pragma unroll
+        for (int nu = 0; nu < 3; ++nu) {
+            double s[4];
+            pauli(p, nu + 1, s);
+            const double hv = 0.5 * F.divW[(it * 3 + nu) * V + v];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) w[l] = fma(hv, s[l], w[l]);
+        }
+        const double wf[4] = {w[1], -w[0], w[3], -w[2]};
+        double h[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            double t = -(Bq * L[l]);
+            t = t - kin * L[l];
+            double sd = fma(nb1, d[1][l], nb0 * d[0][l]);
+            sd = fma(nb2, d[2][l], sd);
+            const double b = t - sd;
+            const double u = Uq * p[l];
+            h[l] = (b + u) + wf[l];
+            s_eh = fma(p[l], h[l], s_eh);
+            s_hh = fma(h[l], h[l], s_hh);
+        }
+        if (kGradStep) {
+            double* up = upd + (long)i * 4 * V;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double a = fma(-fac, h[l], mom * up[l * V + v]);
+                up[l * V + v] = p[l];
+                ps[l * V + v] = p[l] + a;
+            }
+        } else if (hout) {
+            double* ho = hout + (long)i * 4 * V;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) ho[l * V + v] = h[l];
+        }
+    }
+    // block reduction of (s_eh, s_hh)
+    __shared__ double red[2][kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s_eh += __shfl_xor_sync(0xffffffffu, s_eh, o);
+        s_hh += __shfl_xor_sync(0xffffffffu, s_hh, o);
+    }
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (lane == 0) { red[0][warp] = s_eh; red[1][warp] = s_hh; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < kThreads / 32; ++q) { a += red[0][q]; b += red[1][q]; }
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 0] = a;
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 1] = b;
+    }
+}
+
+// e[i] = dv * sum <psi|h psi>, disp[i] = dv * sum <h psi|h psi> - e^2
+__global__ void k_finish_energies(const double* __restrict__ partial, int nchunk, int nwt,
+                                  double dv, double* __restrict__ e, double* __restrict__ disp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nwt) return;
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < nchunk; ++q) {
+        a += partial[((long)i * nchunk + q) * 2 + 0];
+        b += partial[((long)i * nchunk + q) * 2 + 1];
+    }
+    const double en = a * dv;
+    e[i] = en;
+    disp[i] = b * dv - en * en;
+}
+
+double reduced_mass(const mg_ctx* c, int it) {
+    if (c->f.com1body == 2)
+        return 1.0 - c->f.nucleonmass[it] /
+                         (c->p.neutrons * c->f.nucleonmass[0] + c->p.protons * c->f.nucleonmass[1]);
+    return 1.0;
+}
+
+}  // namespace
+
+// h.psi over a basis.  grad_step: GradDesc update of the HF basis in place
+// (fac = dt/hbar, mom = momentum); otherwise h.psi goes to out (may be NULL).
+// Energies and dispersions land in the basis' e / disp arrays.
+int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom) {
+    Basis& B = c->bas[b];
+    if (!B.have_qn) return MG_ERR_STATE;
+    const long V = c->V;
+    const int nchunk = div_up(V, kThreads);
+    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW};
+    const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
+    const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
+    dim3 grid(nchunk, c->p.nwt);
+    if (grad_step)
+        k_hpsi<true><<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.lap, B.qn, F, nullptr,
+                                                       c->updates, c->red, V, kin0, kin1, fac, mom);
+    else
+        k_hpsi<false><<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.lap, B.qn, F, out,
+                                                        nullptr, c->red, V, kin0, kin1, 0.0, 0.0);
+    MG_CUDA(cudaGetLastError());
+    k_finish_energies<<<div_up(c->p.nwt, 128), 128, 0, c->stream>>>(c->red, nchunk, c->p.nwt,
+                                                                     c->dv, B.e, B.disp);
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+}  // namespace mg

@@ -1,0 +1,153 @@
+// mg_internal.cuh -- device context and shared helpers of libmocca_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "../../include/mocca_gpu.h"
+
+#define MG_CUDA(call)                                                              \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            fprintf(stderr, "mocca_gpu: %s failed at %s:%d: %s\n", #call, __FILE__, \
+                    __LINE__, cudaGetErrorString(e_));                             \
+            return MG_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+#define MG_TRY(call)            \
+    do {                        \
+        int s_ = (call);        \
+        if (s_ < 0) return s_;  \
+    } while (0)
+
+namespace mg {
+
+constexpr int kMaxN = 64;       // largest supported stored line length
+constexpr int kNumMoments = 64; // capacity of the multipole table
+
+// One derivative job: a real grid and where its derivatives go.  slot[d] is
+// the Lagrange matrix slot (0 odd, 1 even) along axis d; a NULL output is
+// skipped.  lap receives (Lxx + Lyy) + Lzz.
+struct GridJob {
+    const double* in;
+    double* dx;
+    double* dy;
+    double* dz;
+    double* lap;
+    int8_t slot[3];
+    int8_t pad[5];
+};
+
+// Per-basis device state.
+struct Basis {
+    double* psi = nullptr;   // nwt*4V
+    double* der = nullptr;   // nwt*12V : [i][d][l][V]
+    double* lap = nullptr;   // nwt*4V
+    int* qn = nullptr;       // nwt*4 (device)
+    double* occ = nullptr;   // nwt
+    double* e = nullptr;     // nwt
+    double* disp = nullptr;  // nwt
+    GridJob* jobs = nullptr; // 4*nwt derivative jobs
+    std::vector<int> h_qn;
+    std::vector<double> h_occ, h_e, h_disp;
+    bool have_qn = false;
+};
+
+}  // namespace mg
+
+struct mg_ctx {
+    mg_params p;
+    mg_force f;
+    mg_skyrme_b B;
+    int nx, ny, nz;
+    long V;
+    double dv;
+    bool folded;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+
+    // Lagrange matrices: [axis][kind: 0 first, 1 second][slot][q*n+i]
+    // (stored transposed so consecutive output points read consecutive words)
+    double* mats = nullptr;
+    long mat_off[3][2][2];
+
+    mg::Basis bas[2];
+    double* updates = nullptr;   // nwt*4V heavy-ball history
+    double* hbuf = nullptr;      // nwt*4V h.psi scratch
+
+    // densities [it][...][V]
+    double *rho = nullptr, *tau = nullptr, *nablaj = nullptr, *derrho = nullptr,
+           *laprho = nullptr;
+    // potentials
+    double *U = nullptr, *Bp = nullptr, *nablaB = nullptr, *W = nullptr, *divW = nullptr;
+    double* divw_tmp = nullptr;   // 3 * 6V
+    mg::GridJob* field_jobs = nullptr;  // rho derivs (2), B derivs (2), divW (18)
+    int n_field_jobs = 0;
+
+    // Gram-Schmidt scratch
+    double* gs_S = nullptr;       // overlap blocks
+    double* gs_R = nullptr;       // inverse Cholesky factors
+    int* gs_index = nullptr;      // block lists + energy-ordered members
+    int gs_nblk = 0, gs_nbmax = 0, gs_nchunk = 0, gs_lists_len = 0;
+
+    // Coulomb
+    int mx, my, mz;
+    long M = 0;
+    double *cpot = nullptr, *csource = nullptr, *cres = nullptr, *cp = nullptr,
+           *ct = nullptr, *rext = nullptr, *sh_ext = nullptr, *sh_mesh = nullptr,
+           *coulomb = nullptr, *coulex = nullptr;
+    int n_moments = 0, n_bc_moments = 0;
+    int h_moment_l[mg::kNumMoments];
+    double* moment_values = nullptr;   // [n_moments][2]
+    double* rpow_ext = nullptr;        // r^(2l+1) on the extended box per moment
+    double* mfac = nullptr;            // 4 pi / (2l+1) per moment
+    unsigned* cg_bar = nullptr;        // grid barrier state of the CG kernel
+    int* cg_status = nullptr;          // [state, iterations]
+    int* h_cg_status = nullptr;        // pinned host copy
+    int cg_blocks = 0;
+    double* red = nullptr;             // reduction scratch
+    size_t red_len = 0;
+    int* flags = nullptr;              // device status flags
+    bool coulomb_init = false;
+
+    double pairing_energy[2] = {0.0, 0.0};
+};
+
+namespace mg {
+
+int upload_matrices(mg_ctx* c);
+int build_basis_jobs(mg_ctx* c, int b);
+int build_field_jobs(mg_ctx* c);
+int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs);
+int derive_basis(mg_ctx* c, int b);
+
+int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom);
+int gram_schmidt(mg_ctx* c);
+int gram_schmidt_impl(mg_ctx* c, double* upd);
+int densities(mg_ctx* c);
+int moments(mg_ctx* c);
+int coulomb_setup(mg_ctx* c);
+int coulomb_solve(mg_ctx* c, int* iters);
+int potentials(mg_ctx* c);
+int energy(mg_ctx* c, mg_energy_terms* out);
+int basis_dots(mg_ctx* c, const double* a, const double* b, double* out);
+int density_groups(const mg_ctx* c);
+
+// Lagrange matrix slot selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8.
+__host__ __device__ inline int lag_slot(int dir, int P, int S, int TS, int comp) {
+    int s;
+    if (dir == 0) s = (comp == 1 || comp == 4) ? S * TS : -S * TS;
+    else if (dir == 1) s = (comp == 1 || comp == 3) ? TS : -TS;
+    else s = (comp == 1 || comp == 2) ? S * P : -S * P;
+    return s > 0 ? 1 : 0;
+}
+
+inline int div_up(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace mg

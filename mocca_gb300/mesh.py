@@ -1,0 +1,216 @@
+"""Host-side mirror of the reference's module procedures for the hot path.
+
+`MeshState` owns one libmocca_gpu context.  Its methods carry the names of
+the Fortran procedures they replace, with the same argument meaning, and
+every one of them runs on the GPU through the C ABI:
+
+    DeriveAll          src/SpwfStorage.f90:586-604
+    hPsi               src/ImaginaryTime.f90:213-304   (whole basis)
+    GradDesc           src/ImaginaryTime.f90:439-500
+    GramSchmidt        src/SpwfStorage.f90:372-480
+    HFFill             src/HartreeFock.f90:177-260     (NaiveFill)
+    UpdateDensities    src/Densities.f90:406-550
+    CalculateAllMoments src/Moments.f90:2250-2334      (electric moments)
+    SolveCoulomb       src/Coulomb.f90:255-346
+    ConstructPotentials src/PotentialMixing.f90:17-201
+    CompEnergy         src/Energy.f90:62-179
+    Evolve             src/Main.f90:255-328            (n passes of the loop body)
+
+A non-zero status raises `MgError` (the reference stops through stp()).
+Arrays follow the reference's memory order: a spinor batch is
+[nwt, 4, nz, ny, nx] float64, fields are [it, ..., nz, ny, nx].
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .forces import Force, RunParams
+
+
+def _dptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_abi._D)
+
+
+class MeshState:
+    def __init__(self, params: RunParams, force: Force, stream=None):
+        self.lib = _abi.load()
+        self.p = params
+        self.force = force
+        self._cp = params.to_c()
+        self._cf = force.to_c()
+        h = C.c_void_p()
+        st = self.lib.mg_create(C.byref(self._cp), C.byref(self._cf),
+                                C.c_void_p(stream) if stream else None, C.byref(h))
+        _abi.check("mg_create", st)
+        self.h = h
+
+    # ---- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def V(self) -> int:
+        return self.p.V
+
+    def _call(self, name, *args, allow_not_converged=False):
+        return _abi.check(name, getattr(self.lib, name)(self.h, *args), allow_not_converged)
+
+    def synchronize(self):
+        self._call("mg_synchronize")
+
+    # ---- transfers ---------------------------------------------------------------
+    def set_spinors(self, psi: np.ndarray, qn: np.ndarray | None = None,
+                    basis: int = _abi.MG_HF_BASIS):
+        psi = np.ascontiguousarray(psi, dtype=np.float64).reshape(self.p.nwt, -1)
+        ptrs = (C.c_void_p * self.p.nwt)(*[psi[i].ctypes.data for i in range(self.p.nwt)])
+        q = None
+        if qn is not None:
+            qn = np.ascontiguousarray(qn, dtype=np.int32).reshape(-1)
+            q = qn.ctypes.data_as(_abi._I)
+        self._keep = psi
+        self._call("mg_upload_spinors", basis, ptrs, q, 0, self.p.nwt)
+        self.synchronize()
+
+    def get_spinors(self, basis: int = _abi.MG_HF_BASIS) -> np.ndarray:
+        out = np.empty((self.p.nwt, 4 * self.V))
+        ptrs = (C.c_void_p * self.p.nwt)(*[out[i].ctypes.data for i in range(self.p.nwt)])
+        self._call("mg_download_spinors", basis, ptrs, 0, self.p.nwt)
+        return out.reshape(self.p.nwt, 4, self.p.nz, self.p.ny, self.p.nx)
+
+    def get_derivatives(self, basis: int = _abi.MG_HF_BASIS):
+        n = self.p.nwt
+        der = np.empty((n, 12 * self.V))
+        lap = np.empty((n, 4 * self.V))
+        dp = (C.c_void_p * n)(*[der[i].ctypes.data for i in range(n)])
+        lp = (C.c_void_p * n)(*[lap[i].ctypes.data for i in range(n)])
+        self._call("mg_download_derivatives", basis, dp, lp, 0, n)
+        s = (self.p.nz, self.p.ny, self.p.nx)
+        return der.reshape(n, 3, 4, *s), lap.reshape(n, 4, *s)
+
+    def set_occupations(self, occ, basis: int = _abi.MG_HF_BASIS):
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        self._call("mg_set_occupations", basis, _dptr(occ))
+
+    def get_occupations(self, basis: int = _abi.MG_HF_BASIS) -> np.ndarray:
+        out = np.empty(self.p.nwt)
+        self._call("mg_get_occupations", basis, _dptr(out))
+        return out
+
+    def set_energies(self, e, basis: int = _abi.MG_HF_BASIS):
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        self._call("mg_set_energies", basis, _dptr(e))
+
+    def get_energies(self, basis: int = _abi.MG_HF_BASIS):
+        e = np.empty(self.p.nwt)
+        d = np.empty(self.p.nwt)
+        self._call("mg_get_energies", basis, _dptr(e), _dptr(d))
+        return e, d
+
+    def get_densities(self) -> dict:
+        V = self.V
+        out = {k: np.empty(n * V) for k, n in
+               (("rho", 2), ("tau", 2), ("nablaj", 2), ("derrho", 6), ("laprho", 2))}
+        self._call("mg_get_densities", *(_dptr(out[k]) for k in
+                                         ("rho", "tau", "nablaj", "derrho", "laprho")))
+        return out
+
+    def set_densities(self, rho=None, tau=None, nablaj=None, derrho=None, laprho=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+                for a in (rho, tau, nablaj, derrho, laprho)]
+        self._call("mg_set_densities", *(_dptr(a) for a in arrs))
+
+    def get_potentials(self) -> dict:
+        V = self.V
+        out = {k: np.empty(n * V) for k, n in
+               (("U", 2), ("B", 2), ("nablaB", 6), ("W", 18), ("divW", 6), ("coulomb", 1),
+                ("coulex", 1))}
+        self._call("mg_get_potentials", *(_dptr(out[k]) for k in
+                                          ("U", "B", "nablaB", "W", "divW", "coulomb", "coulex")))
+        return out
+
+    def set_potentials(self, U=None, B=None, nablaB=None, W=None, divW=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+                for a in (U, B, nablaB, W, divW)]
+        self._call("mg_set_potentials", *(_dptr(a) for a in arrs))
+
+    # ---- reference procedures ----------------------------------------------------
+    def DeriveAll(self):
+        self._call("mg_derive_all")
+
+    def DeriveBasis(self, basis: int = _abi.MG_HF_BASIS):
+        self._call("mg_derive_basis", basis)
+
+    def hPsi(self, basis: int = _abi.MG_HF_BASIS, want_spinors: bool = True):
+        e = np.empty(self.p.nwt)
+        d = np.empty(self.p.nwt)
+        h = np.empty((self.p.nwt, 4 * self.V)) if want_spinors else None
+        self._call("mg_hpsi", basis, _dptr(h), _dptr(e), _dptr(d))
+        if h is not None:
+            h = h.reshape(self.p.nwt, 4, self.p.nz, self.p.ny, self.p.nx)
+        return h, e, d
+
+    def GradDesc(self, dt: float, momentum: float = 0.0):
+        self._call("mg_grad_desc", C.c_double(dt), C.c_double(momentum))
+
+    def GramSchmidt(self):
+        self._call("mg_gram_schmidt")
+
+    def HFFill(self):
+        self._call("mg_hf_fill")
+
+    def UpdateDensities(self):
+        self._call("mg_update_densities")
+
+    def CalculateAllMoments(self):
+        self._call("mg_calculate_moments")
+
+    def SolveCoulomb(self) -> int:
+        it = C.c_int(0)
+        self._call("mg_solve_coulomb", C.byref(it), allow_not_converged=True)
+        return it.value
+
+    def ConstructPotentials(self) -> int:
+        it = C.c_int(0)
+        self._call("mg_construct_potentials", C.byref(it), allow_not_converged=True)
+        return it.value
+
+    def CompEnergy(self) -> dict:
+        e = _abi.MgEnergyTerms()
+        self._call("mg_energy", C.byref(e))
+        return e.as_dict()
+
+    def Evolve(self, n_iter: int, dt: float, momentum: float = 0.0) -> dict:
+        e = _abi.MgEnergyTerms()
+        self._call("mg_iterate", int(n_iter), C.c_double(dt), C.c_double(momentum), C.byref(e),
+                   allow_not_converged=True)
+        return e.as_dict()
+
+    def Start(self):
+        """Iteration-0 preparation of Evolve (src/Main.f90:177-231) for an HF
+        run started from spinors with given energies: fill, derive, densities,
+        moments, potentials."""
+        self.HFFill()
+        self.DeriveAll()
+        self.UpdateDensities()
+        self.CalculateAllMoments()
+        return self.ConstructPotentials()

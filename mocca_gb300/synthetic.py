@@ -1,0 +1,141 @@
+"""Seeded synthetic inputs with the shapes of the benchmark configurations.
+
+The reference ships no wavefunction files and no datasets, so these stand in
+for them:
+
+* `ho_basis` -- harmonic-oscillator start for an EV8 + time-reversal run:
+  one stored spwf per Cartesian HO orbital (nx, ny, nz), signature +1 and
+  time simplex +1 as the reference's from-scratch guess uses
+  (src/InOut.f90:1418-1473), placed in the spinor component whose mirror
+  parities match the orbital (the sign rules of
+  src/Derivatives.f90:348-439), plus a seeded uniform perturbation.
+* `gaussian_hermite_spinors` / `woods_saxon_fields` -- the mesh microbench
+  (32^3 full box, 200 spinors): Gaussian envelopes of random width and
+  centre times random Hermite polynomials, and Woods-Saxon U, B, W fields.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .forces import RunParams
+
+
+def mesh_axes(p: RunParams):
+    """Stored mesh coordinates (Mesh.f90:49-73)."""
+    def axis(n, conserved):
+        x = p.dx / 2.0 + p.dx * np.arange(n)
+        return x if conserved else x - n / 2.0 * p.dx
+    return axis(p.nx, p.sc), axis(p.ny, p.tsc), axis(p.nz, p.pc)
+
+
+def _hermite(n: int, x: np.ndarray) -> np.ndarray:
+    h0, h1 = np.ones_like(x), 2 * x
+    if n == 0:
+        return h0
+    for k in range(1, n):
+        h0, h1 = h1, 2 * x * h1 - 2 * k * h0
+    return h1
+
+
+def ho_orbitals(count: int):
+    """Cartesian HO orbitals (nx,ny,nz) by shell, then lexicographic."""
+    out = []
+    N = 0
+    while len(out) < count:
+        for a in range(N, -1, -1):
+            for b in range(N - a, -1, -1):
+                out.append((a, b, N - a - b))
+        N += 1
+    return out[:count]
+
+
+# spinor component (0..3) holding an orbital with x/y parities (odd?) for
+# signature +1: (even,even)->Re up, (odd,odd)->Im up, (odd,even)->Re down,
+# (even,odd)->Im down; the spwf parity follows from nz.
+_COMP = {(0, 0): 0, (1, 1): 1, (1, 0): 2, (0, 1): 3}
+
+
+def ho_basis(p: RunParams, n_neutron: int, seed: int = 1234, amplitude: float = 1e-3,
+             b_osc: float | None = None):
+    """HO start for an EV8 run: returns (psi[nwt,4,nz,ny,nx], qn[nwt,4], energies)."""
+    if not (p.pc and p.sc and p.tsc):
+        raise ValueError("ho_basis builds EV8 (all spatial symmetries conserved) states")
+    nwt = p.nwt
+    n_proton = nwt - n_neutron
+    A = p.neutrons + p.protons
+    hw = 41.0 * A ** (-1.0 / 3.0)
+    if b_osc is None:
+        b_osc = math.sqrt(41.47 / hw)  # hbar^2/m / (hbar omega), fm^2
+    x, y, z = mesh_axes(p)
+    rng = np.random.default_rng(seed)
+    psi = np.zeros((nwt, 4, p.nz, p.ny, p.nx))
+    qn = np.zeros((nwt, 4), dtype=np.int32)
+    en = np.zeros(nwt)
+    k = 0
+    for iso, count in ((-1, n_neutron), (1, n_proton)):
+        for (a, b, c) in ho_orbitals(count):
+            comp = _COMP[(a % 2, b % 2)]
+            parity = (-1) ** c if comp in (0, 1) else -((-1) ** c)
+            fx = _hermite(a, x / b_osc) * np.exp(-0.5 * (x / b_osc) ** 2)
+            fy = _hermite(b, y / b_osc) * np.exp(-0.5 * (y / b_osc) ** 2)
+            fz = _hermite(c, z / b_osc) * np.exp(-0.5 * (z / b_osc) ** 2)
+            g = fz[:, None, None] * fy[None, :, None] * fx[None, None, :]
+            psi[k, comp] = g
+            psi[k] += amplitude * rng.uniform(-1.0, 1.0, size=psi[k].shape) * np.abs(g).max()
+            nrm = math.sqrt(float(np.sum(psi[k] ** 2)) * p.dv)
+            psi[k] /= nrm
+            qn[k] = (iso, parity, 1, 1)
+            en[k] = -50.0 + hw * (a + b + c + 1.5)
+            k += 1
+    return psi, qn, en
+
+
+def gaussian_hermite_spinors(p: RunParams, count: int, seed: int = 42):
+    """Microbench spinors on the full (symmetry-free) box."""
+    x, y, z = mesh_axes(p)
+    rng = np.random.default_rng(seed)
+    out = np.zeros((count, 4, p.nz, p.ny, p.nx))
+    for i in range(count):
+        for l in range(4):
+            w = rng.uniform(1.5, 3.0)
+            c = rng.uniform(-3.0, 3.0, size=3)
+            d = rng.integers(0, 4, size=3)
+            fx = _hermite(int(d[0]), (x - c[0]) / w) * np.exp(-0.5 * ((x - c[0]) / w) ** 2)
+            fy = _hermite(int(d[1]), (y - c[1]) / w) * np.exp(-0.5 * ((y - c[1]) / w) ** 2)
+            fz = _hermite(int(d[2]), (z - c[2]) / w) * np.exp(-0.5 * ((z - c[2]) / w) ** 2)
+            out[i, l] = fz[:, None, None] * fy[None, :, None] * fx[None, None, :]
+        out[i] /= math.sqrt(float(np.sum(out[i] ** 2)) * p.dv)
+    return out
+
+
+def woods_saxon_fields(p: RunParams, R: float = 3.5, a: float = 0.65, u0: float = -50.0,
+                       b0: float = 20.7, w0: float = 120.0):
+    """U, B, grad B, W, div W of Woods-Saxon form, both isospins equal.
+
+    U = u0 f, B = b0 f, W_mn = -eps_kmn w0 d_k f, f = 1/(1+exp((r-R)/a)).
+    """
+    x, y, z = mesh_axes(p)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    f = 1.0 / (1.0 + np.exp((r - R) / a))
+    df = -f * (1 - f) / a
+    rs = np.where(r > 0, r, 1.0)
+    grad = [df * X / rs, df * Y / rs, df * Z / rs]
+    V = p.V
+    U = np.stack([u0 * f, u0 * f]).reshape(2, V)
+    B = np.stack([b0 * f, b0 * f]).reshape(2, V)
+    nablaB = np.stack([np.stack([b0 * g for g in grad])] * 2).reshape(2, 3, V)
+    W = np.zeros((2, 3, 3, V))
+    eps = np.zeros((3, 3, 3))
+    eps[0, 1, 2] = eps[1, 2, 0] = eps[2, 0, 1] = 1
+    eps[0, 2, 1] = eps[2, 1, 0] = eps[1, 0, 2] = -1
+    for n in range(3):
+        for m in range(3):
+            acc = np.zeros(V)
+            for k in range(3):
+                acc -= eps[k, m, n] * w0 * grad[k].reshape(V)
+            W[:, n, m] = acc
+    divW = np.zeros((2, 3, V))
+    return U, B, nablaB, W, divW

@@ -1,0 +1,1065 @@
+// oracle.cpp -- CPU FP64 restatement of MOCCa's mesh hot path.
+//
+// TEST INFRASTRUCTURE ONLY: the parity checker for the CUDA library.  Only
+// tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
+//
+// Each routine cites the reference routine (path:line inside the MOCCa
+// sources) it restates.  Loops keep the reference's summation order where it
+// fixes the rounding (matmul over j ascending, spwf sums in index order,
+// Laplacian = (X + Y) + Z).
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+namespace {
+
+const double kPi = 4.0 * std::atan2(1.0, 1.0);  // src/GenInfo.f90:47
+
+struct Basis {
+    std::vector<double> psi, der, lap;  // nwt*4V, nwt*12V, nwt*4V
+    std::vector<int> qn;                // nwt*4: isospin, parity, signature, timesimplex
+    std::vector<double> occ, e, disp;
+};
+
+struct Moment {  // one electric multipole moment (src/Moments.f90:372-582)
+    int l, m, im;
+    std::vector<double> sh;  // SpherHarm on the stored mesh
+    double value[2] = {0.0, 0.0};
+};
+
+}  // namespace
+
+struct orc_ctx {
+    mg_params p;
+    mg_force f;
+    mg_skyrme_b B;
+    int nx, ny, nz;
+    long V;
+    double dx, dv;
+    bool folded;
+    // Lagrange matrices per axis: [s][i*n+j], s=0 odd, s=1 even
+    std::vector<double> D[3][2], L[3][2];
+    Basis bas[2];
+    std::vector<double> updates;
+    // densities (src/Densities.f90:39-94)
+    std::vector<double> rho, tau, nablaj, derrho, laprho;
+    // potentials (src/MeanFields.f90:79-85)
+    std::vector<double> U, Bp, nablaB, W, divW;
+    // Coulomb (src/Coulomb.f90:20-105)
+    int mx, my, mz;
+    std::vector<double> cpot_complete, source, bc, rext, coulomb, coulex;
+    std::vector<double> sh_ext;  // [moment][mx*my*mz]
+    std::vector<Moment> moments;
+    bool coulomb_init = false;
+};
+
+// --------------------------------------------------------------------------
+// Force coefficients: CalcEDFCoef, src/Force.f90:467-560
+// --------------------------------------------------------------------------
+extern "C" int orc_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* B) {
+    if (!f || !B) return MG_ERR_ARG;
+    std::memset(B, 0, sizeof(*B));
+    const double t0 = f->t0, x0 = f->x0, t1 = f->t1, x1 = f->x1, t2 = f->t2, x2 = f->x2;
+    B->B1 = t0 * (1.0 + 1 / 2.0 * x0) / 2.0;
+    B->B2 = -t0 * (1 / 2.0 + x0) / 2.0;
+    B->B3 = (t1 * (1 + 1 / 2.0 * x1) + t2 * (1 + 1 / 2.0 * x2)) / 4.0;
+    B->B4 = -(t1 * (1 / 2.0 + x1) - t2 * (1 / 2.0 + x2)) / 4.0;
+    B->B5 = -(3.0 * t1 * (1 + x1 / 2.0) - t2 * (1 + x2 / 2.0)) / 16.0;
+    B->B6 = (3.0 * t1 * (x1 + 1 / 2.0) + t2 * (x2 + 1 / 2.0)) / 16.0;
+    B->B7a = f->t3a * (1 + f->x3a / 2.0) / 12.0;
+    B->B8a = -f->t3a * (f->x3a + 1 / 2.0) / 12.0;
+    B->B7b = f->t3b * (1 + f->x3b / 2.0) / 12.0;
+    B->B8b = -f->t3b * (f->x3b + 1 / 2.0) / 12.0;
+    B->B9 = -f->wso / 2.0;
+    B->B9q = -f->wsoq / 2.0;
+    B->byt3a = f->yt3a;
+    B->byt3b = f->yt3b;
+    if (!trc) {
+        B->B10 = t0 * x0 / 4.0;
+        B->B11 = -t0 / 4.0;
+        B->B12a = f->t3a * f->x3a / 24.0;
+        B->B13a = -f->t3a / 24.0;
+        B->B12b = f->t3b * f->x3b / 24.0;
+        B->B13b = -f->t3b / 24.0;
+    }
+    B->B16 = -(3.0 / 8.0) * (f->te + f->to);
+    B->B17 = (3.0 / 8.0) * (f->te - f->to);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Lagrange coefficients: IniLag src/Derivatives.f90:899-973,
+// folded matrices: reduceLag src/Derivatives.f90:975-1078,
+// unfolded: DerLag_1D / SecondDerLag src/Derivatives.f90:1177-1312.
+// --------------------------------------------------------------------------
+static void ini_lag(int N, double dx, std::vector<double>& c1, std::vector<double>& c2,
+                    double& diag) {
+    c1.assign(N + 1, 0.0);
+    c2.assign(N + 1, 0.0);
+    double factor = kPi / N;
+    double dxf = factor / dx;
+    diag = -(kPi * kPi) / (3.0 * (dx * dx)) * (1.0 - 1.0 / double(N * N));
+    for (int k = 1; k <= N - 1; ++k) {
+        double s = std::sin(factor * k), c = std::cos(factor * k);
+        double sg_k = (k % 2 == 0) ? 1.0 : -1.0;
+        double sg_k1 = -sg_k;
+        c1[k] = dxf * sg_k / s;
+        c2[k] = sg_k1 * 2.0 * (dxf * dxf) * c / (s * s);
+    }
+}
+
+extern "C" int orc_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2) {
+    if (n <= 0 || dx <= 0 || !d1 || !d2) return MG_ERR_ARG;
+    std::vector<double> C, Lc;
+    double diag;
+    const long nn = (long)n * n;
+    if (folded) {
+        ini_lag(2 * n, dx, C, Lc, diag);
+        for (int i = 1; i <= n; ++i) {
+            for (int j = 1; j <= n; ++j) {
+                double m1, m2, l1, l2;
+                if (j < i) {
+                    m2 = C[i - j] + C[i + j - 1];
+                    m1 = C[i - j] - C[i + j - 1];
+                    l2 = Lc[i - j] + Lc[i + j - 1];
+                    l1 = Lc[i - j] - Lc[i + j - 1];
+                } else if (j == i) {
+                    l1 = diag - Lc[2 * i - 1];
+                    l2 = diag + Lc[2 * i - 1];
+                    m1 = -C[2 * i - 1];
+                    m2 = +C[2 * i - 1];
+                } else {
+                    m2 = -C[j - i] + C[i + j - 1];
+                    m1 = -C[j - i] - C[i + j - 1];
+                    l2 = Lc[j - i] + Lc[i + j - 1];
+                    l1 = Lc[j - i] - Lc[i + j - 1];
+                }
+                long o = (long)(i - 1) * n + (j - 1);
+                d1[o] = m1; d1[nn + o] = m2;
+                d2[o] = l1; d2[nn + o] = l2;
+            }
+        }
+    } else {
+        ini_lag(n, dx, C, Lc, diag);
+        for (int i = 1; i <= n; ++i)
+            for (int j = 1; j <= n; ++j) {
+                long o = (long)(i - 1) * n + (j - 1);
+                double m, l;
+                if (i == j) { m = 0.0; l = diag; }
+                else { m = (i > j ? 1.0 : -1.0) * C[std::abs(i - j)]; l = Lc[std::abs(i - j)]; }
+                d1[o] = d1[nn + o] = m;
+                d2[o] = d2[nn + o] = l;
+            }
+    }
+    return MG_OK;
+}
+
+// Extension sign selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8
+// (src/OptimizedDerivatives.f90:115-148, :306-338, :432-464, :551-615):
+// returns the matrix slot, 1 = even (Fortran index 2), 0 = odd (index 1).
+static int lag_slot(int dir, int P, int S, int TS, int comp) {
+    int s = 0;
+    if (dir == 0) s = (comp == 1 || comp == 4) ? S * TS : -S * TS;
+    else if (dir == 1) s = (comp == 1 || comp == 3) ? TS : -TS;
+    else s = (comp == 1 || comp == 2) ? S * P : -S * P;
+    return s > 0 ? 1 : 0;
+}
+
+// out(i along dir) = sum_j M(i,j) in(j along dir); j ascending (matmul)
+static void apply_axis(const orc_ctx* c, const double* M, int dir, const double* in,
+                       double* out) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    if (dir == 0) {
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j) {
+                const double* line = in + (long)nx * (j + (long)ny * k);
+                double* o = out + (long)nx * (j + (long)ny * k);
+                for (int i = 0; i < nx; ++i) {
+                    double s = 0.0;
+                    for (int q = 0; q < nx; ++q) s += M[(long)i * nx + q] * line[q];
+                    o[i] = s;
+                }
+            }
+    } else if (dir == 1) {
+        for (int k = 0; k < nz; ++k)
+            for (int x = 0; x < nx; ++x)
+                for (int i = 0; i < ny; ++i) {
+                    double s = 0.0;
+                    for (int q = 0; q < ny; ++q)
+                        s += M[(long)i * ny + q] * in[x + (long)nx * (q + (long)ny * k)];
+                    out[x + (long)nx * (i + (long)ny * k)] = s;
+                }
+    } else {
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x)
+                for (int i = 0; i < nz; ++i) {
+                    double s = 0.0;
+                    for (int q = 0; q < nz; ++q)
+                        s += M[(long)i * nz + q] * in[x + (long)nx * (y + (long)ny * q)];
+                    out[x + (long)nx * (y + (long)ny * i)] = s;
+                }
+    }
+}
+
+// DeriveX/Y/Z (dir 0..2) or Laplacian (dir 3) of one real grid.
+static void derive_grid(const orc_ctx* c, const double* g, int dir, int P, int S, int TS,
+                        int comp, double* out) {
+    if (dir < 3) {
+        apply_axis(c, c->D[dir][lag_slot(dir, P, S, TS, comp)].data(), dir, g, out);
+        return;
+    }
+    std::vector<double> a(c->V), b(c->V), d(c->V);
+    apply_axis(c, c->L[0][lag_slot(0, P, S, TS, comp)].data(), 0, g, a.data());
+    apply_axis(c, c->L[1][lag_slot(1, P, S, TS, comp)].data(), 1, g, b.data());
+    apply_axis(c, c->L[2][lag_slot(2, P, S, TS, comp)].data(), 2, g, d.data());
+    for (long v = 0; v < c->V; ++v) out[v] = a[v] + b[v] + d[v];
+}
+
+extern "C" int orc_derive_grid(orc_ctx* c, const double* g, int dir, int P, int S, int TS,
+                               int comp, double* out) {
+    if (!c || !g || !out || dir < 0 || dir > 3) return MG_ERR_ARG;
+    derive_grid(c, g, dir, P, S, TS, comp, out);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Context
+// --------------------------------------------------------------------------
+extern "C" orc_ctx* orc_create(const mg_params* p, const mg_force* f) {
+    if (!p || !f || p->nx <= 0 || p->ny <= 0 || p->nz <= 0 || p->nwt <= 0) return nullptr;
+    bool ev8 = p->pc && p->sc && p->tsc;
+    bool full = !p->pc && !p->sc && !p->tsc;
+    if (!ev8 && !full) return nullptr;
+    orc_ctx* c = new orc_ctx();
+    c->p = *p;
+    c->f = *f;
+    orc_skyrme_coefficients(f, p->trc, &c->B);
+    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz;
+    c->V = (long)p->nx * p->ny * p->nz;
+    c->dx = p->dx;
+    // dv = dx^3 * 2^(number of conserved spatial symmetries), src/GenInfo.f90:296
+    int nsym = (p->pc ? 1 : 0) + (p->sc ? 1 : 0) + (p->tsc ? 1 : 0);
+    c->dv = p->dx * p->dx * p->dx * std::pow(2.0, nsym);
+    c->folded = ev8;
+    int ns[3] = {p->nx, p->ny, p->nz};
+    for (int d = 0; d < 3; ++d) {
+        long nn = (long)ns[d] * ns[d];
+        std::vector<double> d1(2 * nn), d2(2 * nn);
+        orc_lagrange_matrices(ns[d], p->dx, ev8 ? 1 : 0, d1.data(), d2.data());
+        for (int s = 0; s < 2; ++s) {
+            c->D[d][s].assign(d1.begin() + s * nn, d1.begin() + (s + 1) * nn);
+            c->L[d][s].assign(d2.begin() + s * nn, d2.begin() + (s + 1) * nn);
+        }
+    }
+    for (int b = 0; b < 2; ++b) {
+        Basis& B = c->bas[b];
+        B.psi.assign(p->nwt * 4 * c->V, 0.0);
+        B.der.assign(p->nwt * 12 * c->V, 0.0);
+        B.lap.assign(p->nwt * 4 * c->V, 0.0);
+        B.qn.assign(p->nwt * 4, 1);
+        B.occ.assign(p->nwt, 0.0);
+        B.e.assign(p->nwt, 0.0);
+        B.disp.assign(p->nwt, 0.0);
+    }
+    c->updates.assign(p->nwt * 4 * c->V, 0.0);
+    long V = c->V;
+    c->rho.assign(2 * V, 0); c->tau.assign(2 * V, 0); c->nablaj.assign(2 * V, 0);
+    c->derrho.assign(6 * V, 0); c->laprho.assign(2 * V, 0);
+    c->U.assign(2 * V, 0); c->Bp.assign(2 * V, 0); c->nablaB.assign(6 * V, 0);
+    c->W.assign(18 * V, 0); c->divW.assign(6 * V, 0);
+    c->coulomb.assign(V, 0); c->coulex.assign(V, 0);
+    return c;
+}
+
+extern "C" void orc_destroy(orc_ctx* c) { delete c; }
+
+extern "C" int orc_set_spinors(orc_ctx* c, int b, const double* psi, const int* qn) {
+    if (!c || b < 0 || b > 1) return MG_ERR_ARG;
+    Basis& B = c->bas[b];
+    if (psi) std::memcpy(B.psi.data(), psi, B.psi.size() * sizeof(double));
+    if (qn) std::memcpy(B.qn.data(), qn, B.qn.size() * sizeof(int));
+    return MG_OK;
+}
+extern "C" int orc_get_spinors(orc_ctx* c, int b, double* psi) {
+    if (!c || b < 0 || b > 1 || !psi) return MG_ERR_ARG;
+    std::memcpy(psi, c->bas[b].psi.data(), c->bas[b].psi.size() * sizeof(double));
+    return MG_OK;
+}
+extern "C" int orc_get_qn(orc_ctx* c, int b, int* qn) {
+    if (!c || b < 0 || b > 1 || !qn) return MG_ERR_ARG;
+    std::memcpy(qn, c->bas[b].qn.data(), c->bas[b].qn.size() * sizeof(int));
+    return MG_OK;
+}
+extern "C" int orc_get_derivatives(orc_ctx* c, int b, double* der, double* lap) {
+    if (!c || b < 0 || b > 1) return MG_ERR_ARG;
+    if (der) std::memcpy(der, c->bas[b].der.data(), c->bas[b].der.size() * sizeof(double));
+    if (lap) std::memcpy(lap, c->bas[b].lap.data(), c->bas[b].lap.size() * sizeof(double));
+    return MG_OK;
+}
+extern "C" int orc_set_occupations(orc_ctx* c, int b, const double* occ) {
+    if (!c || b < 0 || b > 1 || !occ) return MG_ERR_ARG;
+    std::copy(occ, occ + c->p.nwt, c->bas[b].occ.begin());
+    return MG_OK;
+}
+extern "C" int orc_get_occupations(orc_ctx* c, int b, double* occ) {
+    if (!c || b < 0 || b > 1 || !occ) return MG_ERR_ARG;
+    std::copy(c->bas[b].occ.begin(), c->bas[b].occ.end(), occ);
+    return MG_OK;
+}
+extern "C" int orc_set_energies(orc_ctx* c, int b, const double* e) {
+    if (!c || b < 0 || b > 1 || !e) return MG_ERR_ARG;
+    std::copy(e, e + c->p.nwt, c->bas[b].e.begin());
+    return MG_OK;
+}
+extern "C" int orc_get_energies(orc_ctx* c, int b, double* e, double* disp) {
+    if (!c || b < 0 || b > 1) return MG_ERR_ARG;
+    if (e) std::copy(c->bas[b].e.begin(), c->bas[b].e.end(), e);
+    if (disp) std::copy(c->bas[b].disp.begin(), c->bas[b].disp.end(), disp);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// CompDer / DeriveSpinor / LapSpinor, src/Spwf.f90:778-792,
+// src/Spinor.f90:516-552, :661-687; DeriveAll src/SpwfStorage.f90:586-604
+// --------------------------------------------------------------------------
+extern "C" int orc_derive_basis(orc_ctx* c, int b) {
+    if (!c || b < 0 || b > 1) return MG_ERR_ARG;
+    Basis& B = c->bas[b];
+    const long V = c->V;
+    for (int i = 0; i < c->p.nwt; ++i) {
+        int P = B.qn[4 * i + 1], S = B.qn[4 * i + 2], TS = B.qn[4 * i + 3];
+        const double* psi = &B.psi[(long)i * 4 * V];
+        for (int l = 0; l < 4; ++l) {
+            for (int d = 0; d < 3; ++d)
+                derive_grid(c, psi + l * V, d, P, S, TS, l + 1,
+                            &B.der[((long)i * 12 + d * 4 + l) * V]);
+            derive_grid(c, psi + l * V, 3, P, S, TS, l + 1, &B.lap[((long)i * 4 + l) * V]);
+        }
+    }
+    return MG_OK;
+}
+
+extern "C" int orc_derive_all(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    orc_derive_basis(c, MG_HF_BASIS);
+    if (c->p.pairing == MG_PAIRING_HFB) orc_derive_basis(c, MG_CAN_BASIS);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Spinor helpers (src/Spinor.f90)
+// --------------------------------------------------------------------------
+// Pauli(Psi, dir) at one point, src/Spinor.f90:113-157
+static inline void pauli(const double* p, int dir, double* o) {
+    if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
+    else if (dir == 2) { o[0] = p[3]; o[1] = -p[2]; o[2] = -p[1]; o[3] = p[0]; }
+    else { o[0] = p[0]; o[1] = p[1]; o[2] = -p[2]; o[3] = -p[3]; }
+}
+// InproductSpinorReal, src/Spinor.f90:715-731
+static double inprod_real(const orc_ctx* c, const double* a, const double* b) {
+    double s = 0.0;
+    for (long i = 0; i < 4 * c->V; ++i) s += a[i] * b[i];
+    return s * c->dv;
+}
+
+static double reduced_mass(const orc_ctx* c, int it) {
+    // ActionOfBNew, src/MeanFields.f90:829-833
+    if (c->f.com1body == 2)
+        return 1.0 - c->f.nucleonmass[it] /
+                         (c->p.neutrons * c->f.nucleonmass[0] + c->p.protons * c->f.nucleonmass[1]);
+    return 1.0;
+}
+
+// hPsi for one spwf: B (ActionOfBNew) + U + W, src/ImaginaryTime.f90:213-304,
+// src/MeanFields.f90:792-851, :1029-1065.
+static void hpsi_one(const orc_ctx* c, const Basis& B, int i, double* out) {
+    const long V = c->V;
+    const int it = (B.qn[4 * i] + 3) / 2 - 1;
+    const double* psi = &B.psi[(long)i * 4 * V];
+    const double* der = &B.der[(long)i * 12 * V];
+    const double* lap = &B.lap[(long)i * 4 * V];
+    const double kin = c->f.hbm / 2.0 * reduced_mass(c, it);
+    const double* Bq = &c->Bp[it * V];
+    const double* Uq = &c->U[it * V];
+    for (long v = 0; v < V; ++v) {
+        double p[4], d[3][4], L[4];
+        for (int l = 0; l < 4; ++l) {
+            p[l] = psi[l * V + v];
+            L[l] = lap[l * V + v];
+            for (int m = 0; m < 3; ++m) d[m][l] = der[(m * 4 + l) * V + v];
+        }
+        double b[4], u[4], w[4] = {0, 0, 0, 0};
+        for (int l = 0; l < 4; ++l) {
+            double t = -(Bq[v] * L[l]);
+            t = t - kin * L[l];
+            double sd = c->nablaB[(it * 3 + 0) * V + v] * d[0][l] +
+                        c->nablaB[(it * 3 + 1) * V + v] * d[1][l];
+            sd = sd + c->nablaB[(it * 3 + 2) * V + v] * d[2][l];
+            b[l] = t - sd;
+            u[l] = Uq[v] * p[l];
+        }
+        // ActionOfW: sum_mu sum_nu W(mu,nu) sigma_nu d_mu psi + 1/2 sum_nu divW(nu) sigma_nu psi
+        for (int mu = 0; mu < 3; ++mu)
+            for (int nu = 0; nu < 3; ++nu) {
+                double s[4];
+                pauli(d[mu], nu + 1, s);
+                double wv = c->W[((it * 3 + nu) * 3 + mu) * V + v];
+                for (int l = 0; l < 4; ++l) w[l] = w[l] + wv * s[l];
+            }
+        for (int nu = 0; nu < 3; ++nu) {
+            double s[4];
+            pauli(p, nu + 1, s);
+            double hv = 0.5 * c->divW[(it * 3 + nu) * V + v];
+            for (int l = 0; l < 4; ++l) w[l] = w[l] + hv * s[l];
+        }
+        // (-1) * MultiplyI(w): (w1,w2,w3,w4) -> (w2,-w1,w4,-w3)
+        double wf[4] = {w[1], -w[0], w[3], -w[2]};
+        for (int l = 0; l < 4; ++l) out[l * V + v] = (b[l] + u[l]) + wf[l];
+    }
+}
+
+extern "C" int orc_hpsi(orc_ctx* c, int b, double* hpsi, double* e, double* disp) {
+    if (!c || b < 0 || b > 1) return MG_ERR_ARG;
+    const Basis& B = c->bas[b];
+    const long V4 = 4 * c->V;
+    std::vector<double> h(V4);
+    for (int i = 0; i < c->p.nwt; ++i) {
+        hpsi_one(c, B, i, h.data());
+        double en = inprod_real(c, &B.psi[i * V4], h.data());
+        double hh = inprod_real(c, h.data(), h.data());
+        if (hpsi) std::memcpy(hpsi + i * V4, h.data(), V4 * sizeof(double));
+        if (e) e[i] = en;
+        if (disp) disp[i] = hh - en * en;
+    }
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// GramSchmidt, src/SpwfStorage.f90:372-480 (TSC, SC conserved branch);
+// OrderSpwfsISO src/SpwfStorage.f90:795-848 (stable ascending insertion sort)
+// --------------------------------------------------------------------------
+static std::vector<int> order_iso(const Basis& B, int nwt, int iso) {
+    std::vector<int> idx;
+    for (int i = 0; i < nwt; ++i)
+        if (B.qn[4 * i] == iso) idx.push_back(i);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b2) { return B.e[a] < B.e[b2]; });
+    return idx;
+}
+
+extern "C" int orc_gram_schmidt(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    Basis& B = c->bas[MG_HF_BASIS];
+    const long V4 = 4 * c->V;
+    for (int it = 1; it <= 2; ++it) {
+        std::vector<int> idx = order_iso(B, c->p.nwt, it * 2 - 3);
+        for (size_t k = 0; k < idx.size(); ++k) {
+            int nw = idx[k];
+            double* pn = &B.psi[nw * V4];
+            double norm = inprod_real(c, pn, pn);
+            double sc = 1.0 / std::sqrt(norm);
+            for (long v = 0; v < V4; ++v) pn[v] = sc * pn[v];
+            for (size_t l = k + 1; l < idx.size(); ++l) {
+                int mw = idx[l];
+                if (B.qn[4 * mw] != B.qn[4 * nw] || B.qn[4 * mw + 1] != B.qn[4 * nw + 1] ||
+                    B.qn[4 * mw + 2] != B.qn[4 * nw + 2])
+                    continue;
+                double* pm = &B.psi[mw * V4];
+                double me = inprod_real(c, pm, pn);  // InProduct(HFBasis(mw), HFBasis(nw))
+                for (long v = 0; v < V4; ++v) pm[v] = pm[v] - me * pn[v];
+            }
+        }
+    }
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// GradDesc, src/ImaginaryTime.f90:439-500 (ParameterEstimation = 0, no
+// InverseKineticDamping)
+// --------------------------------------------------------------------------
+extern "C" int orc_grad_desc(orc_ctx* c, double dt, double momentum) {
+    if (!c) return MG_ERR_ARG;
+    Basis& B = c->bas[MG_HF_BASIS];
+    const long V4 = 4 * c->V;
+    const double fac = dt / c->f.hbar;
+    std::vector<double> h(V4);
+    for (int i = 0; i < c->p.nwt; ++i) {
+        double* cur = &B.psi[i * V4];
+        hpsi_one(c, B, i, h.data());
+        double en = inprod_real(c, cur, h.data());
+        double ds = inprod_real(c, h.data(), h.data()) - en * en;
+        double* up = &c->updates[i * V4];
+        for (long v = 0; v < V4; ++v) {
+            double a = -fac * h[v] + momentum * up[v];
+            up[v] = cur[v];
+            cur[v] = cur[v] + a;
+        }
+        B.e[i] = en;
+        B.disp[i] = ds;
+    }
+    orc_gram_schmidt(c);
+    for (int i = 0; i < c->p.nwt; ++i)
+        for (long v = 0; v < V4; ++v) c->updates[i * V4 + v] = B.psi[i * V4 + v] - c->updates[i * V4 + v];
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// NaiveFill, src/HartreeFock.f90:177-260 (no blocking)
+// --------------------------------------------------------------------------
+extern "C" int orc_hf_fill(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    Basis& B = c->bas[MG_HF_BASIS];
+    const int nwt = c->p.nwt;
+    std::fill(B.occ.begin(), B.occ.end(), 0.0);
+    int pub = c->p.trc ? (int)std::floor(c->p.protons / 2) : (int)std::floor(c->p.protons);
+    int nub = c->p.trc ? (int)std::floor(c->p.neutrons / 2) : (int)std::floor(c->p.neutrons);
+    std::vector<int> order(nwt);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return B.e[a] < B.e[b2]; });
+    int n = 0, pp = 0;
+    for (int i = 0; i < nwt && pp < pub; ++i) {
+        int j = order[i];
+        if (B.occ[j] == 0.0 && B.qn[4 * j] == 1) { B.occ[j] = 1.0; ++pp; }
+    }
+    for (int i = 0; i < nwt && n < nub; ++i) {
+        int j = order[i];
+        if (B.occ[j] == 0.0 && B.qn[4 * j] == -1) { B.occ[j] = 1.0; ++n; }
+    }
+    if (c->p.trc)
+        for (int i = 0; i < nwt; ++i) B.occ[i] = 2.0 * B.occ[i];
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// ComputeDensity, src/Densities.f90:431-550 (TRC, no tensor / N2LO):
+// rho (GetDensity src/Spwf.f90:536-546), tau (GetTau :1897-1909),
+// NablaJ (GetNablaJ :2206-2243), then DerRho and LapRho.
+// --------------------------------------------------------------------------
+static inline double imag_mult(const double* a, const double* b) {
+    // ImagMultiplySpinor, src/Spinor.f90:264-281
+    return a[0] * b[1] - a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+}
+
+extern "C" int orc_update_densities(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    const Basis& B = c->bas[c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS];
+    std::fill(c->rho.begin(), c->rho.end(), 0.0);
+    std::fill(c->tau.begin(), c->tau.end(), 0.0);
+    std::fill(c->nablaj.begin(), c->nablaj.end(), 0.0);
+    // (i,j,k, LeviCivita) in the reference's order
+    static const int trip[6][4] = {{1, 2, 3, 1}, {1, 3, 2, -1}, {3, 2, 1, -1},
+                                   {3, 1, 2, 1}, {2, 1, 3, -1}, {2, 3, 1, 1}};
+    for (int i = 0; i < c->p.nwt; ++i) {
+        double occ = B.occ[i];
+        if (occ == 0.0) continue;
+        int it = (B.qn[4 * i] + 3) / 2 - 1;
+        const double* psi = &B.psi[(long)i * 4 * V];
+        const double* der = &B.der[(long)i * 12 * V];
+        for (long v = 0; v < V; ++v) {
+            double p[4], d[3][4];
+            for (int l = 0; l < 4; ++l) {
+                p[l] = psi[l * V + v];
+                for (int m = 0; m < 3; ++m) d[m][l] = der[(m * 4 + l) * V + v];
+            }
+            double den = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + p[3] * p[3];
+            c->rho[it * V + v] = c->rho[it * V + v] + occ * den;
+            double t = 0.0;
+            for (int m = 0; m < 3; ++m)
+                t = t + (d[m][0] * d[m][0] + d[m][1] * d[m][1] + d[m][2] * d[m][2] + d[m][3] * d[m][3]);
+            c->tau[it * V + v] = c->tau[it * V + v] + occ * t;
+            double nj = 0.0;
+            for (int q = 0; q < 6; ++q) {
+                double s[4];
+                pauli(d[trip[q][1] - 1], trip[q][2], s);
+                nj = nj + double(trip[q][3]) * imag_mult(d[trip[q][0] - 1], s);
+            }
+            c->nablaj[it * V + v] = c->nablaj[it * V + v] + occ * nj;
+        }
+    }
+    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+    for (int it = 0; it < 2; ++it) {
+        for (int d = 0; d < 3; ++d)
+            derive_grid(c, &c->rho[it * V], d, P, S, TS, 1, &c->derrho[(it * 3 + d) * V]);
+        derive_grid(c, &c->rho[it * V], 3, P, S, TS, 1, &c->laprho[it * V]);
+    }
+    return MG_OK;
+}
+
+extern "C" int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* nablaj,
+                                 double* derrho, double* laprho) {
+    if (!c) return MG_ERR_ARG;
+    auto cp = [](double* dst, const std::vector<double>& s) {
+        if (dst) std::memcpy(dst, s.data(), s.size() * sizeof(double));
+    };
+    cp(rho, c->rho); cp(tau, c->tau); cp(nablaj, c->nablaj); cp(derrho, c->derrho); cp(laprho, c->laprho);
+    return MG_OK;
+}
+extern "C" int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
+                                 const double* nablaj, const double* derrho, const double* laprho) {
+    if (!c) return MG_ERR_ARG;
+    auto cp = [](std::vector<double>& d, const double* s) {
+        if (s) std::memcpy(d.data(), s, d.size() * sizeof(double));
+    };
+    cp(c->rho, rho); cp(c->tau, tau); cp(c->nablaj, nablaj); cp(c->derrho, derrho); cp(c->laprho, laprho);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Multipole moments for the Coulomb boundary.
+// legendre_pnm src/Mesh.f90:96-262, SphericalHarmonics src/Moments.f90:584-691
+// (QuantisationAxis 3, SecondaryAxis 1), IniMoments src/Moments.f90:372-582,
+// Calculate_Multipole src/Moments.f90:1907-1966.
+// --------------------------------------------------------------------------
+static void legendre_pnm(int n, int m, double x, double* cx) {
+    for (int i = 0; i < m; ++i) cx[i] = 0.0;
+    cx[m] = 1.0;
+    double somx2 = std::sqrt(1.0 - x * x), fact = 1.0;
+    for (int i = 1; i <= m; ++i) { cx[m] = -cx[m] * fact * somx2; fact += 2.0; }
+    if (m == n) return;
+    cx[m + 1] = x * double(2 * m + 1) * cx[m];
+    for (int i = m + 2; i <= n; ++i)
+        cx[i] = (double(2 * i - 1) * x * cx[i - 1] - double(i + m - 1) * cx[i - 2]) / double(i - m);
+}
+
+static double ipow(double x, int n) {
+    double r = 1.0;
+    for (int i = 0; i < n; ++i) r *= x;
+    return r;
+}
+
+// r^l Y_lm (real part if im==0) at (X,Y,Z), as SphericalHarmonics
+static double spher_harm(int l, int m, int im, double X, double Y, double Z, int maxl) {
+    double r = std::sqrt(X * X + Y * Y + Z * Z);
+    double cost = Z / r;
+    double phi = std::atan2(Y, X);
+    std::vector<double> leg(maxl + 1);
+    legendre_pnm(maxl, m, cost, leg.data());
+    double fq = 1.0;
+    for (int q = 1; q <= 2 * m; ++q) fq = fq / double(l + m - q + 1);
+    double fac = ((m % 2) ? -1.0 : 1.0) * std::sqrt(fq) * ipow(r, l);
+    fac = fac * std::sqrt(double(2 * l + 1) / (4 * kPi));
+    double ang = im ? std::sin(m * phi) : std::cos(m * phi);
+    return fac * leg[l] * ang;
+}
+
+// Electric moments allowed for EV8 with quantisation axis z
+// (NewMoment_Electric: odd l removed by parity, imaginary parts by time
+// simplex, odd m by signature).
+static void init_moments(orc_ctx* c) {
+    const int maxl = 10;  // MaxMoment default, src/Moments.f90:229
+    c->moments.clear();
+    Moment root;
+    root.l = 0; root.m = 0; root.im = 0;
+    root.sh.assign(c->V, 1.0 / std::sqrt(4.0 * kPi));
+    c->moments.push_back(root);
+    for (int l = 1; l <= maxl; ++l)
+        for (int m = 0; m <= l; ++m)
+            for (int im = 0; im <= 1; ++im) {
+                if (c->p.pc && (l % 2)) continue;
+                if (c->p.tsc && im == 1) continue;
+                if (c->p.sc && (m % 2)) continue;
+                if (m == 0 && im == 1) continue;
+                Moment mo;
+                mo.l = l; mo.m = m; mo.im = im;
+                mo.sh.resize(c->V);
+                for (int k = 0; k < c->nz; ++k)
+                    for (int j = 0; j < c->ny; ++j)
+                        for (int i = 0; i < c->nx; ++i) {
+                            double X = c->dx / 2.0 + c->dx * i, Y = c->dx / 2.0 + c->dx * j,
+                                   Z = c->dx / 2.0 + c->dx * k;
+                            mo.sh[i + c->nx * (j + (long)c->ny * k)] = spher_harm(l, m, im, X, Y, Z, maxl);
+                        }
+                c->moments.push_back(mo);
+            }
+}
+
+extern "C" int orc_calculate_moments(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    if (c->moments.empty()) init_moments(c);
+    for (Moment& mo : c->moments)
+        for (int it = 0; it < 2; ++it) {
+            double s = 0.0;
+            for (long v = 0; v < c->V; ++v) s += mo.sh[v] * c->rho[it * c->V + v];
+            mo.value[it] = s * c->dv;
+        }
+    return MG_OK;
+}
+
+extern "C" int orc_get_moments(orc_ctx* c, double* values, int* lm, int max_count) {
+    if (!c) return MG_ERR_ARG;
+    int n = (int)c->moments.size();
+    for (int i = 0; i < n && i < max_count; ++i) {
+        if (values) { values[2 * i] = c->moments[i].value[0]; values[2 * i + 1] = c->moments[i].value[1]; }
+        if (lm) { lm[2 * i] = c->moments[i].l; lm[2 * i + 1] = c->moments[i].m; }
+    }
+    return n;
+}
+
+// --------------------------------------------------------------------------
+// Coulomb: SetupCoulomb / InitialGuess / CoulombBound / ConjugGrad
+// (src/Coulomb.f90:255-900) with CoulombLaplacian / Coulomb_1D
+// (src/CoulombDerivatives.f90:144-281), CoulombLapOrder = 2, EV8 box.
+// --------------------------------------------------------------------------
+static void coulomb_setup(orc_ctx* c) {
+    const int bcn = 2;
+    c->mx = c->nx + bcn; c->my = c->ny + bcn; c->mz = c->nz + bcn;
+    long M = (long)c->mx * c->my * c->mz;
+    c->cpot_complete.assign(M, 0.0);
+    c->source.assign(M, 0.0);
+    c->bc.assign(M, 0.0);
+    c->rext.assign(M, 0.0);
+    for (int k = 0; k < c->mz; ++k)
+        for (int j = 0; j < c->my; ++j)
+            for (int i = 0; i < c->mx; ++i) {
+                double X = (0.5 + i) * c->dx, Y = (0.5 + j) * c->dx, Z = (0.5 + k) * c->dx;
+                c->rext[i + c->mx * (j + (long)c->my * k)] = std::sqrt(X * X + Y * Y + Z * Z);
+            }
+    if (c->moments.empty()) init_moments(c);
+    c->sh_ext.assign(c->moments.size() * M, 0.0);
+    for (size_t q = 0; q < c->moments.size(); ++q) {
+        const Moment& mo = c->moments[q];
+        for (int k = 0; k < c->mz; ++k)
+            for (int j = 0; j < c->my; ++j)
+                for (int i = 0; i < c->mx; ++i) {
+                    double X = (0.5 + i) * c->dx, Y = (0.5 + j) * c->dx, Z = (0.5 + k) * c->dx;
+                    c->sh_ext[q * M + i + c->mx * (j + (long)c->my * k)] =
+                        spher_harm(mo.l, mo.m, mo.im, X, Y, Z, 10);
+                }
+    }
+    // InitialGuess, src/Coulomb.f90:542-581
+    double R = 1.25 * std::pow(c->p.neutrons + c->p.protons, 1.0 / 3.0);
+    double charge = c->p.protons * c->f.e2, fac = charge / (2 * R);
+    for (int k = 0; k < c->nz; ++k)
+        for (int j = 0; j < c->ny; ++j)
+            for (int i = 0; i < c->nx; ++i) {
+                long o = i + c->mx * (j + (long)c->my * k);
+                double r = c->rext[o];
+                c->cpot_complete[o] = (r <= R) ? fac * (3 - r * r / (R * R)) : charge / r;
+            }
+    c->coulomb_init = true;
+}
+
+// 5-point FD Laplacian on the interior (1..n per axis) with an even mirror
+// at the low end; zero outside the interior.
+static void coulomb_laplacian(const orc_ctx* c, const double* g, double* out) {
+    static const double cf[5] = {-1.0 / 12.0, 4.0 / 3.0, -5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0};
+    const int mx = c->mx, my = c->my, mz = c->mz;
+    const long M = (long)mx * my * mz;
+    std::fill(out, out + M, 0.0);
+    const double factor = 1.0 / (c->dx * c->dx);
+    auto at = [&](int i, int j, int k) { return g[i + mx * (j + (long)my * k)]; };
+    for (int k = 0; k < c->nz; ++k)
+        for (int j = 0; j < c->ny; ++j)
+            for (int i = 0; i < c->nx; ++i) {
+                double dxl = 0.0, dyl = 0.0, dzl = 0.0;
+                for (int q = -2; q <= 2; ++q) {
+                    int ii = i + q;  // 0-based; mirror: -1 -> 0, -2 -> 1
+                    dxl += cf[q + 2] * at(ii < 0 ? -ii - 1 : ii, j, k);
+                    int jj = j + q;
+                    dyl += cf[q + 2] * at(i, jj < 0 ? -jj - 1 : jj, k);
+                    int kk = k + q;
+                    dzl += cf[q + 2] * at(i, j, kk < 0 ? -kk - 1 : kk);
+                }
+                out[i + mx * (j + (long)my * k)] = dxl * factor + dyl * factor + dzl * factor;
+            }
+}
+
+extern "C" int orc_solve_coulomb(orc_ctx* c, int* iters) {
+    if (!c) return MG_ERR_ARG;
+    if (!c->p.pc || !c->p.sc || !c->p.tsc) return MG_ERR_ARG;
+    if (!c->coulomb_init) coulomb_setup(c);
+    const int mx = c->mx, my = c->my, mz = c->mz;
+    const long M = (long)mx * my * mz;
+    // CoulombBound, src/Coulomb.f90:583-674
+    std::fill(c->bc.begin(), c->bc.end(), 0.0);
+    std::fill(c->source.begin(), c->source.end(), 0.0);
+    for (int k = 0; k < c->nz; ++k)
+        for (int j = 0; j < c->ny; ++j)
+            for (int i = 0; i < c->nx; ++i)
+                c->source[i + mx * (j + (long)my * k)] =
+                    -4 * kPi * c->f.e2 * c->rho[c->V + i + c->nx * (j + (long)c->ny * k)];
+    int maxl = c->p.max_l_coul > 0 ? c->p.max_l_coul : 10;
+    for (size_t q = 0; q < c->moments.size(); ++q) {
+        const Moment& mo = c->moments[q];
+        if (mo.l > maxl) break;
+        double value = mo.value[1] * (4 * kPi / (2 * mo.l + 1));
+        for (int k = 0; k < mz; ++k)
+            for (int j = 0; j < my; ++j)
+                for (int i = 0; i < mx; ++i) {
+                    if (i < c->nx && j < c->ny && k < c->nz) continue;
+                    long o = i + mx * (j + (long)my * k);
+                    c->bc[o] = c->bc[o] + value * c->sh_ext[q * M + o] * c->f.e2 /
+                                              ipow(c->rext[o], 2 * mo.l + 1);
+                }
+    }
+    for (long o = 0; o < M; ++o)
+        if (c->bc[o] != 0.0) c->cpot_complete[o] = c->bc[o];
+    // ConjugGrad, src/Coulomb.f90:755-900
+    double prec = 1.0e-9 / (c->dx * c->dx * c->dx * c->nx * c->ny * c->nz);
+    std::vector<double> res(M), p(M), t(M);
+    double* sol = c->cpot_complete.data();
+    coulomb_laplacian(c, sol, t.data());
+    for (long o = 0; o < M; ++o) res[o] = -t[o] + c->source[o];
+    p = res;
+    double pnorm = 0.0;
+    for (long o = 0; o < M; ++o) pnorm += res[o] * res[o];
+    int maxit = c->p.coulomb_max > 0 ? c->p.coulomb_max : 500;
+    int it = 0, status = MG_NOT_CONVERGED;
+    for (it = 1; it <= maxit; ++it) {
+        coulomb_laplacian(c, p.data(), t.data());
+        double integral = 0.0;
+        for (long o = 0; o < M; ++o) integral += res[o] * t[o];
+        double a = pnorm / integral;
+        for (long o = 0; o < M; ++o) sol[o] = sol[o] + a * p[o];
+        for (long o = 0; o < M; ++o) res[o] = res[o] - a * t[o];
+        double nn = 0.0;
+        for (long o = 0; o < M; ++o) nn += res[o] * res[o];
+        if (nn <= prec) { status = MG_OK; break; }
+        double ck = nn / pnorm;
+        pnorm = nn;
+        for (long o = 0; o < M; ++o) p[o] = res[o] + ck * p[o];
+    }
+    if (iters) *iters = std::min(it, maxit);
+    for (int k = 0; k < c->nz; ++k)
+        for (int j = 0; j < c->ny; ++j)
+            for (int i = 0; i < c->nx; ++i)
+                c->coulomb[i + c->nx * (j + (long)c->ny * k)] = sol[i + mx * (j + (long)my * k)];
+    double fac = -std::pow(3 / kPi, 1 / 3.0) * c->f.e2;
+    for (long v = 0; v < c->V; ++v) c->coulex[v] = fac * std::pow(c->rho[c->V + v], 1 / 3.0);
+    return status;
+}
+
+// --------------------------------------------------------------------------
+// Potentials: CalcUPot src/MeanFields.f90:269-409, CalcWPot :494-597,
+// CalcBPot :115-150; ConstructPotentials src/PotentialMixing.f90:17-201.
+// --------------------------------------------------------------------------
+static void calc_potentials(orc_ctx* c) {
+    const long V = c->V;
+    const mg_skyrme_b& B = c->B;
+    const double eps = 1.0e-20;
+    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+    for (long v = 0; v < V; ++v) {
+        double rn = c->rho[v], rp = c->rho[V + v];
+        double rt = rn + rp;
+        double njt = c->nablaj[v] + c->nablaj[V + v];
+        double u[2];
+        u[0] = (2.0 * B.B1 + 2.0 * B.B2) * rn + 2.0 * B.B1 * rp;
+        u[1] = (2.0 * B.B1 + 2.0 * B.B2) * rp + 2.0 * B.B1 * rn;
+        for (int it = 0; it < 2; ++it) {
+            int at = 1 - it;
+            double ri = c->rho[it * V + v], ra = c->rho[at * V + v];
+            double x = u[it] + (B.B3 + B.B4) * c->tau[it * V + v] + B.B3 * c->tau[at * V + v] +
+                       2.0 * ((B.B5 + B.B6) * c->laprho[it * V + v] + B.B5 * c->laprho[at * V + v]) +
+                       (2 + B.byt3a) * B.B7a * std::pow(rt + eps, 1 + B.byt3a) +
+                       B.B8a * (B.byt3a * std::pow(rt, B.byt3a) / (rt + eps) * (ri * ri + ra * ra) +
+                                2.0 * std::pow(rt, B.byt3a) * ri) +
+                       B.B9 * njt + B.B9q * c->nablaj[it * V + v];
+            if (B.B7b != 0.0 || B.B8b != 0.0)
+                x = x + (2 + B.byt3b) * B.B7b * std::pow(rt + eps, 1 + B.byt3b) +
+                    B.B8b * (B.byt3b * std::pow(rt, B.byt3b) / (rt + eps) * (ri * ri + ra * ra) +
+                             2.0 * std::pow(rt, B.byt3b) * ri);
+            u[it] = x;
+        }
+        u[1] = u[1] + c->coulomb[v];
+        if (c->f.cexchange == 2) u[1] = u[1] + c->coulex[v];
+        c->U[v] = u[0];
+        c->U[V + v] = u[1];
+    }
+    // W: -sum_k eps_{kmn} ((B9+B9q) d_k rho_q + B9 d_k rho_q')
+    std::fill(c->W.begin(), c->W.end(), 0.0);
+    auto lc = [](int i, int j, int k) {
+        if (i == j || j == k || k == i) return 0;
+        if ((i == 1 && j == 2 && k == 3) || (i == 3 && j == 1 && k == 2) || (i == 2 && j == 3 && k == 1))
+            return 1;
+        return -1;
+    };
+    for (int it = 0; it < 2; ++it)
+        for (int m = 1; m <= 3; ++m)
+            for (int n = 1; n <= 3; ++n)
+                for (int k = 1; k <= 3; ++k) {
+                    int e = lc(k, m, n);
+                    double* w = &c->W[((it * 3 + (n - 1)) * 3 + (m - 1)) * V];
+                    const double* dq = &c->derrho[(it * 3 + k - 1) * V];
+                    const double* dqa = &c->derrho[((1 - it) * 3 + k - 1) * V];
+                    for (long v = 0; v < V; ++v)
+                        w[v] = w[v] - e * ((B.B9 + B.B9q) * dq[v] + B.B9 * dqa[v]);
+                }
+    // div W with the symmetry arguments of src/MeanFields.f90:575-591
+    std::vector<double> t1(V), t2(V), t3(V);
+    struct Term { int dir, m, n, P, S, TS, comp; };
+    static const Term terms[3][3] = {
+        {{0, 1, 1, -1, 1, 1, 2}, {1, 2, 1, -1, 1, 1, 1}, {2, 3, 1, -1, -1, 1, 2}},
+        {{0, 1, 2, -1, 1, 1, 1}, {1, 2, 2, -1, 1, 1, 2}, {2, 3, 2, -1, -1, 1, 1}},
+        {{0, 1, 3, -1, -1, 1, 2}, {1, 2, 3, -1, -1, 1, 1}, {2, 3, 3, -1, 1, 1, 2}}};
+    for (int it = 0; it < 2; ++it)
+        for (int nu = 0; nu < 3; ++nu) {
+            std::vector<double>* tv[3] = {&t1, &t2, &t3};
+            for (int q = 0; q < 3; ++q) {
+                const Term& T = terms[nu][q];
+                const double* w = &c->W[((it * 3 + (T.n - 1)) * 3 + (T.m - 1)) * V];
+                derive_grid(c, w, T.dir, T.P * P, T.S * S, T.TS * TS, T.comp, tv[q]->data());
+            }
+            for (long v = 0; v < V; ++v) c->divW[(it * 3 + nu) * V + v] = t1[v] + t2[v] + t3[v];
+        }
+    // B and grad B
+    for (int it = 0; it < 2; ++it) {
+        int at = 1 - it;
+        for (long v = 0; v < V; ++v)
+            c->Bp[it * V + v] = B.B3 * c->rho[at * V + v] + (B.B3 + B.B4) * c->rho[it * V + v];
+        for (int d = 0; d < 3; ++d)
+            derive_grid(c, &c->Bp[it * V], d, P, S, TS, 1, &c->nablaB[(it * 3 + d) * V]);
+    }
+}
+
+extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
+    if (!c) return MG_ERR_ARG;
+    int st = MG_OK;
+    if (c->p.coulomb_solver != 0) {
+        st = orc_solve_coulomb(c, iters);
+        if (st < 0) return st;
+    } else {
+        std::fill(c->coulomb.begin(), c->coulomb.end(), 0.0);
+        std::fill(c->coulex.begin(), c->coulex.end(), 0.0);
+        if (iters) *iters = 0;
+    }
+    calc_potentials(c);
+    return st;
+}
+
+extern "C" int orc_get_potentials(orc_ctx* c, double* u, double* b, double* nablab, double* w,
+                                  double* divw, double* coul, double* coulex) {
+    if (!c) return MG_ERR_ARG;
+    auto cp = [](double* dst, const std::vector<double>& s) {
+        if (dst) std::memcpy(dst, s.data(), s.size() * sizeof(double));
+    };
+    cp(u, c->U); cp(b, c->Bp); cp(nablab, c->nablaB); cp(w, c->W); cp(divw, c->divW);
+    cp(coul, c->coulomb); cp(coulex, c->coulex);
+    return MG_OK;
+}
+extern "C" int orc_set_potentials(orc_ctx* c, const double* u, const double* b,
+                                  const double* nablab, const double* w, const double* divw) {
+    if (!c) return MG_ERR_ARG;
+    auto cp = [](std::vector<double>& d, const double* s) {
+        if (s) std::memcpy(d.data(), s, d.size() * sizeof(double));
+    };
+    cp(c->U, u); cp(c->Bp, b); cp(c->nablaB, nablab); cp(c->W, w); cp(c->divW, divw);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// CompEnergy, src/Energy.f90:62-179: CompKinetic :1426-1456, compSkyrme
+// :623-860 (TRC terms), CompCoulombEnergy / CompCoulombExchange
+// src/Coulomb.f90:215-253, CompCOMCorrection src/Energy.f90:1608-1660,
+// SpwfEnergy :1483-1554.
+// --------------------------------------------------------------------------
+extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
+    if (!c || !out) return MG_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    const long V = c->V;
+    const mg_skyrme_b& B = c->B;
+    const Basis& D = c->bas[c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS];
+    double kin[2] = {0, 0};
+    for (int l = 0; l < c->p.nwt; ++l) {
+        int it = (D.qn[4 * l] + 3) / 2 - 1;
+        double ip = inprod_real(c, &D.psi[(long)l * 4 * V], &D.lap[(long)l * 4 * V]);
+        kin[it] = kin[it] + D.occ[l] * ip;
+    }
+    for (int it = 0; it < 2; ++it) out->kinetic[it] = -kin[it] / 2.0 * c->f.hbm;
+    double* t = out->skyrme;
+    double s1 = 0, s2 = 0, s3 = 0, s4 = 0, s7 = 0, s8 = 0, s9 = 0, s10 = 0, s11 = 0, s12 = 0;
+    double s33 = 0, s34 = 0;
+    for (long v = 0; v < V; ++v) {
+        double rt = c->rho[v] + c->rho[V + v];
+        double tt = c->tau[v] + c->tau[V + v];
+        double lt = c->laprho[v] + c->laprho[V + v];
+        double jt = c->nablaj[v] + c->nablaj[V + v];
+        s1 += rt * rt;
+        s3 += rt * tt;
+        s7 += rt * lt;
+        s9 += std::pow(rt, 2 + B.byt3a);
+        s11 += rt * jt;
+        if (B.B7b != 0.0) s33 += std::pow(rt, 2 + B.byt3b);
+    }
+    for (int it = 0; it < 2; ++it) {
+        double a2 = 0, a4 = 0, a8 = 0, a10 = 0, a12 = 0, a34 = 0;
+        for (long v = 0; v < V; ++v) {
+            double r = c->rho[it * V + v];
+            double rt = c->rho[v] + c->rho[V + v];
+            a2 += r * r;
+            a4 += r * c->tau[it * V + v];
+            a8 += r * c->laprho[it * V + v];
+            a10 += r * r * std::pow(rt, B.byt3a);
+            a12 += r * c->nablaj[it * V + v];
+            if (B.B8b != 0.0) a34 += r * r * std::pow(rt, B.byt3b);
+        }
+        s2 += a2;
+        s4 += B.B4 * a4;
+        s8 += B.B6 * a8;
+        s10 += B.B8a * a10;
+        s12 += B.B9q * a12;
+        s34 += B.B8b * a34;
+    }
+    t[0] = B.B1 * s1; t[1] = B.B2 * s2; t[2] = B.B3 * s3; t[3] = s4;
+    t[6] = B.B5 * s7; t[7] = s8; t[8] = B.B7a * s9; t[9] = s10;
+    t[10] = B.B9 * s11; t[11] = s12;
+    t[32] = B.B7b * s33; t[33] = s34;
+    for (int q = 0; q < 36; ++q) t[q] *= c->dv;
+    double sk = 0;
+    for (int q = 0; q < 36; ++q) sk += t[q];
+    double ec = 0, ex = 0;
+    if (c->p.coulomb_solver != 0) {
+        for (long v = 0; v < V; ++v) ec += c->rho[V + v] * c->coulomb[v];
+        ec = ec * c->dv * 0.5;
+        if (c->f.cexchange >= 1) {
+            double fac = -std::pow(3 / kPi, 1 / 3.0) * c->f.e2 * 0.75 * c->dv;
+            for (long v = 0; v < V; ++v) ex += c->rho[V + v] * std::pow(c->rho[V + v], 1 / 3.0);
+            ex = fac * ex;
+        }
+    }
+    out->coulomb = ec;
+    out->coulomb_exchange = ex;
+    if (c->f.com1body > 0) {
+        double mt = c->p.neutrons * c->f.nucleonmass[0] + c->p.protons * c->f.nucleonmass[1];
+        for (int it = 0; it < 2; ++it) out->com[0][it] = -out->kinetic[it] * c->f.nucleonmass[it] / mt;
+    }
+    double com = out->com[0][0] + out->com[1][0] + out->com[0][1] + out->com[1][1];
+    out->total = sk + (out->kinetic[0] + out->kinetic[1]) + ec + com + ex +
+                 (out->pairing[0] + out->pairing[1]);
+    // SpwfEnergy (TermByTerm)
+    double sp = 0;
+    for (int i = 0; i < c->p.nwt; ++i) sp += D.occ[i] * D.e[i];
+    sp = 0.5 * (sp + (out->kinetic[0] + out->kinetic[1])) -
+         0.5 * B.byt3a * ((t[8] + t[9]) + (t[16] + t[17])) -
+         0.5 * B.byt3b * ((t[32] + t[33]) + (t[34] + t[35])) + ex / 3.0;
+    sp = sp + (out->pairing[0] + out->pairing[1]);
+    if (c->f.com1body > 0) sp = sp + (out->com[0][0] + out->com[0][1]) / 2.0;
+    if (c->f.com2body == 1) sp = sp + (out->com[1][0] + out->com[1][1]);
+    out->sp_energy = sp;
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Evolve loop body, src/Main.f90:255-328, HF pairing type (SolvePairing =
+// NaiveFill), no constraints, MixingScheme 0.
+// --------------------------------------------------------------------------
+extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
+                           mg_energy_terms* out) {
+    if (!c) return MG_ERR_ARG;
+    if (c->p.pairing != MG_PAIRING_HF) return MG_ERR_ARG;
+    int st = MG_OK;
+    for (int k = 0; k < n_iter; ++k) {
+        orc_grad_desc(c, dt, momentum);
+        orc_hf_fill(c);
+        orc_derive_all(c);
+        orc_update_densities(c);
+        orc_calculate_moments(c);
+        st = orc_construct_potentials(c, nullptr);
+        if (st < 0) return st;
+        if (out) orc_energy(c, out);
+    }
+    return st;
+}

@@ -1,0 +1,78 @@
+/*
+ * oracle.h -- CPU FP64 restatement of MOCCa's per-iteration mesh hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the
+ * CUDA library (mocca_gb300/csrc): only tests/, __graft_entry__.smoke() and
+ * bench.py's cpu_baseline leg load it.  Nothing in the product links it.
+ *
+ * Parity status: the reference is Fortran and no Fortran compiler exists in
+ * the build container, and the reference ships no golden outputs, so this
+ * restatement is pinned against self-derived known-answer tests (Lagrange
+ * derivatives exact on the Fourier basis of the full line, folded = unfolded
+ * on mirror-extended lines, Gram-Schmidt orthonormality, analytic Coulomb of
+ * a uniform sphere) rather than reference-produced numbers: parity unpinned
+ * by reference artefacts.
+ *
+ * Every function follows the reference routine cited beside it, in the same
+ * operation order where that order fixes the rounding.
+ */
+#ifndef MOCCA_ORACLE_H
+#define MOCCA_ORACLE_H
+
+#include "../include/mocca_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_ctx orc_ctx;
+
+int  orc_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* out);
+int  orc_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2);
+
+orc_ctx* orc_create(const mg_params* p, const mg_force* f);
+void orc_destroy(orc_ctx* c);
+
+/* psi: count*4V doubles (spwf-major), qn: count*4 ints (may be NULL). */
+int orc_set_spinors(orc_ctx* c, int basis, const double* psi, const int* qn);
+int orc_get_spinors(orc_ctx* c, int basis, double* psi);
+int orc_get_qn(orc_ctx* c, int basis, int* qn);
+int orc_get_derivatives(orc_ctx* c, int basis, double* der, double* lap);
+int orc_set_occupations(orc_ctx* c, int basis, const double* occ);
+int orc_get_occupations(orc_ctx* c, int basis, double* occ);
+int orc_set_energies(orc_ctx* c, int basis, const double* e);
+int orc_get_energies(orc_ctx* c, int basis, double* e, double* disp);
+
+/* one real grid, derivative along dir (0,1,2) or Laplacian (dir=3), with the
+ * symmetry arguments of DeriveX/Y/Z(Grid, P, S, TS, Component). */
+int orc_derive_grid(orc_ctx* c, const double* grid, int dir, int P, int S,
+                    int TS, int comp, double* out);
+
+int orc_derive_basis(orc_ctx* c, int basis);
+int orc_derive_all(orc_ctx* c);
+int orc_hpsi(orc_ctx* c, int basis, double* hpsi, double* e, double* disp);
+int orc_grad_desc(orc_ctx* c, double dt, double momentum);
+int orc_gram_schmidt(orc_ctx* c);
+int orc_hf_fill(orc_ctx* c);
+int orc_update_densities(orc_ctx* c);
+int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* nablaj,
+                      double* derrho, double* laprho);
+int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
+                      const double* nablaj, const double* derrho,
+                      const double* laprho);
+int orc_calculate_moments(orc_ctx* c);
+int orc_get_moments(orc_ctx* c, double* values, int* lm, int max_count);
+int orc_solve_coulomb(orc_ctx* c, int* iters);
+int orc_construct_potentials(orc_ctx* c, int* iters);
+int orc_get_potentials(orc_ctx* c, double* u, double* b, double* nablab,
+                       double* w, double* divw, double* coul, double* coulex);
+int orc_set_potentials(orc_ctx* c, const double* u, const double* b,
+                       const double* nablab, const double* w, const double* divw);
+int orc_energy(orc_ctx* c, mg_energy_terms* out);
+int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
+                mg_energy_terms* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,72 @@
+"""CPU checks of the C ABI boundary (no device work).
+
+* libmocca_gpu.so loads and exports every function include/mocca_gpu.h
+  declares, and the ctypes table in mocca_gb300/_abi.py covers them all;
+* the host-only helpers (Lagrange matrices, Skyrme coefficients) agree with
+  the oracle's independent restatement;
+* the product package never imports or links the oracle.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from mocca_gb300 import SLY4, _abi
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*int\s+(mg_\w+)\s*\(", txt, flags=re.M)
+    return names
+
+
+def test_every_declared_symbol_is_exported(built):
+    names = header_functions()
+    assert len(names) >= 25
+    lib = C.CDLL(str(_abi.LIB_PATH))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(_abi.SIGNATURES), set(names) - set(_abi.SIGNATURES)
+
+
+@pytest.mark.parametrize("n,folded", [(10, True), (24, True), (32, False), (7, False)])
+def test_lagrange_matrices_match_oracle(built, n, folded):
+    lib = _abi.load()
+    d1 = np.empty(2 * n * n)
+    d2 = np.empty(2 * n * n)
+    assert lib.mg_lagrange_matrices(n, 0.8, int(folded), d1.ctypes.data_as(_abi._D),
+                                    d2.ctypes.data_as(_abi._D)) == 0
+    o1, o2 = O.lagrange_matrices(n, 0.8, folded)
+    assert np.array_equal(d1.reshape(2, n, n), o1)
+    assert np.array_equal(d2.reshape(2, n, n), o2)
+
+
+def test_invalid_arguments_are_rejected(built):
+    lib = _abi.load()
+    d = np.empty(8)
+    assert lib.mg_lagrange_matrices(0, 0.8, 1, d.ctypes.data_as(_abi._D),
+                                    d.ctypes.data_as(_abi._D)) == _abi.MG_ERR_ARG
+    assert lib.mg_lagrange_matrices(2, -1.0, 1, d.ctypes.data_as(_abi._D),
+                                    d.ctypes.data_as(_abi._D)) == _abi.MG_ERR_ARG
+    assert lib.mg_destroy(None) == _abi.MG_ERR_ARG
+
+
+def test_skyrme_coefficients_match_oracle(built):
+    a, b = _abi.MgSkyrmeB(), _abi.MgSkyrmeB()
+    assert _abi.load().mg_skyrme_coefficients(SLY4.to_c(), 1, a) == 0
+    assert O.load().orc_skyrme_coefficients(SLY4.to_c(), 1, b) == 0
+    for name, _ in _abi.MgSkyrmeB._fields_:
+        assert getattr(a, name) == pytest.approx(getattr(b, name), rel=1e-15, abs=0), name
+
+
+def test_product_does_not_use_the_oracle():
+    for p in list((ROOT / "mocca_gb300").rglob("*.py")) + list((ROOT / "mocca_gb300").rglob("*.cu")):
+        txt = p.read_text()
+        assert "import oracle" not in txt and "liboracle" not in txt and "orc_" not in txt, p

@@ -1,0 +1,143 @@
+"""CPU checks of the FP64 oracle against known answers.
+
+The reference ships no golden outputs, so the oracle is pinned by
+self-derived known-answer tests from the formulas it restates:
+Lagrange-mesh derivatives exact on the anti-periodic half-integer Fourier
+modes of the full line (Baye-Heenen, src/Derivatives.f90:899-973), folded
+EV8 matrices equal to the unfolded line operator applied to mirror-extended
+lines (reduceLag, :975-1078), the SLy4 coupling constants, orthonormality
+after Gram-Schmidt, the Coulomb potential of a uniform sphere, and the
+committed golden fixture produced by tests/golden/make_golden.py.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import rel
+from mocca_gb300 import SLY4, RunParams, _abi, synthetic
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("n", [6, 10, 24])
+def test_lagrange_exact_on_half_integer_modes(n):
+    dx = 0.8
+    d1, d2 = O.lagrange_matrices(n, dx, True)
+    x = dx / 2 + dx * np.arange(n)
+    L = 2 * n * dx
+    for k in range(n):
+        w = math.pi * (2 * k + 1) / L
+        assert np.abs(d1[1] @ np.cos(w * x) + w * np.sin(w * x)).max() < 1e-12 * w * 50
+        assert np.abs(d1[0] @ np.sin(w * x) - w * np.cos(w * x)).max() < 1e-12 * w * 50
+        assert np.abs(d2[1] @ np.cos(w * x) + w * w * np.cos(w * x)).max() < 1e-12 * w * w * 50
+        assert np.abs(d2[0] @ np.sin(w * x) + w * w * np.sin(w * x)).max() < 1e-12 * w * w * 50
+
+
+@pytest.mark.parametrize("n", [5, 12])
+def test_folded_equals_unfolded_on_mirrored_line(n):
+    dx = 0.7
+    d1, d2 = O.lagrange_matrices(n, dx, True)
+    u1, u2 = O.lagrange_matrices(2 * n, dx, False)
+    rng = np.random.default_rng(3)
+    half = rng.normal(size=n)
+    for s, slot in ((1.0, 1), (-1.0, 0)):
+        # full line ordered -x_n..-x_1, x_1..x_n with f(-x) = s f(x)
+        full = np.concatenate([s * half[::-1], half])
+        assert np.allclose((u1[0] @ full)[n:], d1[slot] @ half, atol=1e-12, rtol=0)
+        assert np.allclose((u2[0] @ full)[n:], d2[slot] @ half, atol=1e-11, rtol=0)
+
+
+def test_sly4_coefficients():
+    b = _abi.MgSkyrmeB()
+    st = O.load().orc_skyrme_coefficients(SLY4.to_c(), 1, b)
+    assert st == 0
+    t0, x0, t1, x1, t2, x2, t3, x3 = -2488.913, 0.834, 486.818, -0.344, -546.395, -1.0, 13777.0, 1.354
+    assert b.B1 == pytest.approx(t0 / 2 * (1 + x0 / 2))
+    assert b.B2 == pytest.approx(-t0 / 2 * (x0 + 0.5))
+    assert b.B3 == pytest.approx((t1 * (1 + x1 / 2) + t2 * (1 + x2 / 2)) / 4)
+    assert b.B7a == pytest.approx(t3 / 12 * (1 + x3 / 2))
+    assert b.B9 == pytest.approx(-123.0 / 2)
+    assert b.B16 == 0.0 and b.B17 == 0.0
+
+
+def _mg24(nwt=40):
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=nwt, neutrons=12, protons=12)
+    psi, qn, en = synthetic.ho_basis(p, nwt // 2, seed=1234)
+    return p, psi, qn, en
+
+
+def test_gram_schmidt_orthonormal():
+    p, psi, qn, en = _mg24()
+    o = O.OracleState(p, SLY4)
+    rng = np.random.default_rng(5)
+    o.set_spinors(psi + 0.05 * rng.normal(size=psi.shape), qn)
+    o.set_energies(en)
+    o.GramSchmidt()
+    q = o.get_spinors().reshape(p.nwt, -1)
+    S = q @ q.T * p.dv
+    same = (qn[:, None, 0] == qn[None, :, 0]) & (qn[:, None, 1] == qn[None, :, 1])
+    assert np.abs(S[same] - np.eye(p.nwt)[same]).max() < 1e-13
+
+
+def test_uniform_sphere_coulomb():
+    """Coulomb of a uniform proton sphere against Q/R (3 - r^2/R^2)/2 inside."""
+    p = RunParams(nx=16, ny=16, nz=16, dx=0.8, nwt=2, neutrons=20, protons=20)
+    o = O.OracleState(p, SLY4)
+    x, y, z = synthetic.mesh_axes(p)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    R = 5.0
+    rho0 = 20.0 / (4.0 / 3.0 * math.pi * R ** 3)
+    # smooth the edge so the FD Laplacian sees a resolvable profile
+    prof = rho0 / (1.0 + np.exp((r - R) / 0.3))
+    prof *= 20.0 / (prof.sum() * p.dv)
+    rho = np.stack([prof, prof]).reshape(2, -1)
+    o.set_densities(rho=rho)
+    o.CalculateAllMoments()
+    it = o.SolveCoulomb()
+    assert 0 < it < 500
+    pot = o.get_potentials()["coulomb"].reshape(p.nz, p.ny, p.nx)
+    e2 = SLY4.e2
+    # radial quadrature of the same (renormalised) profile:
+    # V(r) = 4 pi e2 [ (1/r) int_0^r rho r'^2 dr' + int_r^inf rho r' dr' ]
+    scale = prof.max() / (rho0 / (1.0 + np.exp(-R / 0.3)))
+    s = np.linspace(0.0, 30.0, 300001)
+    f = scale * rho0 / (1.0 + np.exp((s - R) / 0.3))
+    ds = s[1] - s[0]
+    q_in = np.concatenate([[0.0], np.cumsum((f[1:] * s[1:] ** 2 + f[:-1] * s[:-1] ** 2) / 2 * ds)])
+    g = f * s
+    tail = np.concatenate([np.cumsum(((g[1:] + g[:-1]) / 2 * ds)[::-1])[::-1], [0.0]])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        Vr = 4 * math.pi * e2 * (np.where(s > 0, q_in / np.where(s > 0, s, 1), 0.0) + tail)
+    ana = np.interp(r, s, Vr)
+    assert np.abs(pot - ana).max() / ana.max() < 2e-3
+
+
+def test_hf_iterations_lower_the_energy():
+    p, psi, qn, en = _mg24()
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.Start()
+    e0 = o.CompEnergy()["total"]
+    e = o.Evolve(5, 0.010, 0.0)["total"]
+    assert e < e0 - 5.0
+
+
+def test_golden_fixture():
+    """The oracle reproduces the committed golden numbers (make_golden.py)."""
+    g = json.loads((GOLDEN / "mg24_hf.json").read_text())
+    p, psi, qn, en = _mg24()
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.Start()
+    assert o.CompEnergy()["total"] == pytest.approx(g["E_start"], abs=1e-9)
+    e = o.Evolve(g["iterations"], g["dt"], g["momentum"])
+    assert e["total"] == pytest.approx(g["E_final"], abs=1e-9)
+    sp, _ = o.get_energies()
+    assert np.allclose(sp, g["sp_energies"], atol=1e-9, rtol=0)
