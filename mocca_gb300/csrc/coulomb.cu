@@ -47,7 +47,7 @@ __device__ bool grid_barrier(unsigned* bar, int* status) {
         __threadfence();
         const unsigned arrived = atomicAdd(bar, 1u) + 1u;
         if (arrived == gridDim.x) {
-            bar[0] = 0u;
+            atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
