@@ -214,6 +214,11 @@ int mg_energy(mg_ctx* ctx, mg_energy_terms* out);
 int mg_iterate(mg_ctx* ctx, int n_iter, double dt, double momentum,
                mg_energy_terms* out);
 
+/* Number of kernels this context has launched so far (instrumentation; the
+ * reference's only counterpart is the CoulombTime accumulator,
+ * src/Coulomb.f90:288, :333-334). */
+int mg_launch_count(mg_ctx* ctx, long long* count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,6 +123,7 @@ SIGNATURES = {
     "mg_set_potentials": [_P, _D, _D, _D, _D, _D],
     "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
+    "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmocca_gpu.so"

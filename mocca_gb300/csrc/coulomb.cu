@@ -325,7 +325,7 @@ int coulomb_solve(mg_ctx* c, int* iters) {
     k_coulomb_bound<<<div_up(M, kThreads), kThreads, 0, c->stream>>>(
         c->rho + c->V, c->sh_ext, c->rpow_ext, c->moment_values, c->mfac, c->n_bc_moments, c->nx,
         c->ny, c->nz, c->mx, c->my, c->mz, c->f.e2, c->csource, c->cpot);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     MG_CUDA(cudaMemsetAsync(c->cg_bar, 0, 4 * sizeof(unsigned), c->stream));
     MG_CUDA(cudaMemsetAsync(c->cg_status, 0, 4 * sizeof(int), c->stream));
     CgArgs a;
@@ -338,11 +338,12 @@ int coulomb_solve(mg_ctx* c, int* iters) {
     void* args[] = {&a};
     MG_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg, dim3(c->cg_blocks), dim3(kThreads), args,
                                         0, c->stream));
+    ++c->launches;
     const double pi = 4.0 * std::atan2(1.0, 1.0);
     const double fac = -std::pow(3 / pi, 1 / 3.0) * c->f.e2;
     k_coulomb_out<<<div_up(c->V, kThreads), kThreads, 0, c->stream>>>(
         c->cpot, c->rho + c->V, c->nx, c->ny, c->nz, c->mx, c->my, fac, c->coulomb, c->coulex);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     MG_CUDA(cudaMemcpyAsync(c->h_cg_status, c->cg_status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
                             c->stream));
     if (iters) {

@@ -105,10 +105,10 @@ int densities(mg_ctx* c) {
     dim3 grid(div_up(V, kThreads), ng);
     k_dens_partial<<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.occ, B.qn, c->p.nwt, per, V,
                                                      c->red);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     k_dens_reduce<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(c->red, ng, V, c->rho, c->tau,
                                                                    c->nablaj);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     // grad rho, lap rho: the first two field jobs
     return run_jobs(c, c->field_jobs, 2);
 }

@@ -206,10 +206,10 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
     }
     dim3 gxy(njobs, div_up(nz, ppb));
     k_deriv_xy<<<gxy, kThreads, sm_xy, c->stream>>>(jobs, mp, nx, ny, nz, ppb);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     dim3 gz(njobs, div_up((long)nx * ny, kColTile));
     k_deriv_z<<<gz, kThreads, sm_z, c->stream>>>(jobs, mp, nx, ny, nz);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 

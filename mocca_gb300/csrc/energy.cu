@@ -95,7 +95,7 @@ int basis_dots(mg_ctx* c, const double* a, const double* b, double* out) {
     const long V4 = 4 * c->V;
     const int nch = std::max(1, std::min(64, div_up(V4, kThreads * 8)));
     k_dots<<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     std::vector<double> h((size_t)nch * c->p.nwt);
     MG_CUDA(cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
                             c->stream));
@@ -124,7 +124,7 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     ECoef k{B.B4, B.B6, B.B8a, B.B8b, B.B9q, B.byt3a, B.byt3b, B.B7b};
     k_energy_partial<<<nblk, kThreads, 0, c->stream>>>(c->rho, c->tau, c->laprho, c->nablaj,
                                                        c->coulomb, k, V, c->red);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     std::vector<double> part((size_t)nblk * kTerms);
     MG_CUDA(cudaMemcpyAsync(part.data(), c->red, part.size() * sizeof(double),
                             cudaMemcpyDeviceToHost, c->stream));

@@ -177,10 +177,10 @@ int potentials(mg_ctx* c) {
     k_potentials<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(
         c->rho, c->tau, c->nablaj, c->derrho, c->laprho, c->coulomb, c->coulex, k, V, c->U, c->Bp,
         c->W);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     MG_TRY(run_jobs(c, c->field_jobs + 2, c->n_field_jobs - 2));
     k_sum3<<<div_up(6 * V, kThreads), kThreads, 0, c->stream>>>(c->divw_tmp, 6 * V, c->divW);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 
@@ -188,7 +188,7 @@ int moments(mg_ctx* c) {
     if (c->n_moments == 0) return MG_OK;
     k_moments<<<c->n_moments, kThreads, 0, c->stream>>>(c->sh_mesh, c->rho, c->V, c->dv,
                                                         c->moment_values);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 

@@ -233,20 +233,20 @@ int gram_schmidt_impl(mg_ctx* c, double* upd) {
     const int* d_lists = c->gs_index;
     int* d_ordered = c->gs_index + c->gs_lists_len;
     k_gs_order<<<div_up(nblk, 32), 32, 0, c->stream>>>(d_lists, nblk, c->p.nwt, B.e, d_ordered);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     const int npair_max = nbmax * (nbmax + 1) / 2;
     const size_t sm_ov = (size_t)(nbmax * kPts + npair_max) * sizeof(double);
     const size_t sm_f = (size_t)(2 * nbmax * nbmax) * sizeof(double);
     const size_t sm_ap = (size_t)(nbmax * nbmax + nbmax * kPts) * sizeof(double);
     k_gs_overlap<<<dim3(nchunk, nblk), kThreads, sm_ov, c->stream>>>(B.psi, d_lists, d_ordered,
                                                                       nbmax, V4, nchunk, c->gs_S);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     k_gs_factor<<<nblk, kThreads, sm_f, c->stream>>>(c->gs_S, d_lists, nbmax, nchunk, c->dv,
                                                      c->gs_R, c->flags);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     k_gs_apply<<<dim3(div_up(V4, kPts), nblk), kThreads, sm_ap, c->stream>>>(
         B.psi, upd, d_lists, d_ordered, c->gs_R, nbmax, V4);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 

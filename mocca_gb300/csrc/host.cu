@@ -472,6 +472,12 @@ extern "C" int mg_energy(mg_ctx* c, mg_energy_terms* out) {
     return energy(c, out);
 }
 
+extern "C" int mg_launch_count(mg_ctx* c, long long* count) {
+    if (!c || !count) return MG_ERR_ARG;
+    *count = c->launches;
+    return MG_OK;
+}
+
 extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
                           mg_energy_terms* out) {
     // Evolve loop body, src/Main.f90:255-328 (HF: SolvePairing = NaiveFill)

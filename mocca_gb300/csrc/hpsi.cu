@@ -171,10 +171,10 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     else
         k_hpsi<false><<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.lap, B.qn, F, out,
                                                         nullptr, c->red, V, kin0, kin1, 0.0, 0.0);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     k_finish_energies<<<div_up(c->p.nwt, 128), 128, 0, c->stream>>>(c->red, nchunk, c->p.nwt,
                                                                      c->dv, B.e, B.disp);
-    MG_CUDA(cudaGetLastError());
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 

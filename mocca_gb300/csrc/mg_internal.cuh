@@ -19,6 +19,13 @@
         }                                                                          \
     } while (0)
 
+// After a kernel launch: check the launch and count it (mg_launch_count).
+#define MG_LAUNCHED(ctx)                    \
+    do {                                    \
+        MG_CUDA(cudaGetLastError());        \
+        ++(ctx)->launches;                  \
+    } while (0)
+
 #define MG_TRY(call)            \
     do {                        \
         int s_ = (call);        \
@@ -117,6 +124,7 @@ struct mg_ctx {
     bool coulomb_init = false;
 
     double pairing_energy[2] = {0.0, 0.0};
+    long long launches = 0;
 };
 
 namespace mg {
