@@ -107,6 +107,33 @@ typedef struct mg_energy_terms {
     double sp_energy;        /* SpwfEnergy, src/Energy.f90:1483-1554         */
 } mg_energy_terms;
 
+/* HFB pairing parameters: the &Pairing namelist values of the HFB path
+ * (src/Pairing.f90:164-305, src/PairingInteraction.f90:19-94,
+ * src/HFB.f90:86).  Density-dependent delta pairing ("ULB",
+ * DensityFactor = -G (1 - alpha rho0/rhosat)), symmetric-Fermi cutoffs. */
+typedef struct mg_pairing_params {
+    double strength[2];   /* PairingNeutron / PairingProton (MeV fm^3)     */
+    double alpha[2];      /* AlphaNeutron / AlphaProton                     */
+    double rhosat;        /* RhoSat, 0.16 fm^-3                             */
+    double cut[2];        /* PairingCut, 5 MeV                              */
+    double mu[2];         /* PairingMu, 0.5 MeV                             */
+    double mix;           /* HFBMix, 0.1                                    */
+    double fermi_prec;    /* FermiPrec, 1e-12                               */
+    int    max_iter;      /* HFBIter, 50                                    */
+    int    guess_kappa;   /* GuessKappa                                     */
+    double fermi_start[2];/* initial Fermi energies (module default -10)    */
+} mg_pairing_params;
+
+/* Per-call diagnostics of the HFB pairing step. */
+typedef struct mg_pairing_info {
+    double fermi[2];          /* converged Fermi energies                   */
+    double particles[2];      /* Tr rho per isospin at the converged Fermi  */
+    int    evaluations;       /* particle-number evaluations used           */
+    int    converged;         /* 1 when |N - N0| < FermiPrec for both       */
+    double pairing_energy[2]; /* HFBEnergy with the new kappa               */
+    double dispersion[2];     /* PairingDisp                                */
+} mg_pairing_info;
+
 /* ---- host-side helpers (no device work) ---------------------------------- */
 
 /* B-coefficients from Skyrme parameters; replaces CalcEDFCoef
@@ -187,6 +214,25 @@ int mg_get_densities(mg_ctx* ctx, double* rho, double* tau, double* nablaj,
 int mg_set_densities(mg_ctx* ctx, const double* rho, const double* tau,
                      const double* nablaj, const double* derrho,
                      const double* laprho);
+
+/* HFB pairing parameters (before the first mg_solve_pairing). */
+int mg_set_pairing(mg_ctx* ctx, const mg_pairing_params* pp);
+
+/* SolvePairing for HFB (src/Pairing.f90:743-890): density factor, cutoffs,
+ * pairing field (HFBPairingField, src/HFB.f90:350-518), gaps (HFBGaps,
+ * :520-632), Fermi energies (FindFermiEnergy, same particle-number equation
+ * and tolerance as HFBFindFermiEnergyBroyden :1849-2161), the canonical
+ * basis (HFBOccupations :3361-3560) and rho/kappa mixing.  The canonical
+ * spinors land in MG_CAN_BASIS.  info may be NULL. */
+int mg_solve_pairing(mg_ctx* ctx, mg_pairing_info* info);
+
+/* Block b = it*2 + (parity+1)/2 of rho, kappa and Delta (N*N each, N the
+ * block size including time-reversed partners); returns N, any pointer may
+ * be NULL (then only N is returned). */
+int mg_get_hfb_block(mg_ctx* ctx, int b, double* rho, double* kappa, double* delta);
+
+/* Pairing field (real, imaginary) and DensityFactor, 2V each, may be NULL. */
+int mg_get_pairing_field(mg_ctx* ctx, double* re, double* im, double* dfac);
 
 /* Electric multipole moments of the densities needed by the Coulomb
  * boundary (Calculate_Multipole, src/Moments.f90:1907-2004). */

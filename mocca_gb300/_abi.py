@@ -63,6 +63,43 @@ class MgSkyrmeB(C.Structure):
         "B17")]
 
 
+class MgPairingParams(C.Structure):
+    _fields_ = [
+        ("strength", C.c_double * 2), ("alpha", C.c_double * 2), ("rhosat", C.c_double),
+        ("cut", C.c_double * 2), ("mu", C.c_double * 2), ("mix", C.c_double),
+        ("fermi_prec", C.c_double), ("max_iter", C.c_int), ("guess_kappa", C.c_int),
+        ("fermi_start", C.c_double * 2),
+    ]
+
+    @classmethod
+    def defaults(cls, strength=1250.0, alpha=1.0, guess_kappa=True):
+        """The README Mg24 &Pairing values with the reference's defaults."""
+        p = cls()
+        p.strength[0] = p.strength[1] = strength
+        p.alpha[0] = p.alpha[1] = alpha
+        p.rhosat = 0.16
+        p.cut[0] = p.cut[1] = 5.0
+        p.mu[0] = p.mu[1] = 0.5
+        p.mix = 0.1
+        p.fermi_prec = 1e-12
+        p.max_iter = 50
+        p.guess_kappa = int(guess_kappa)
+        p.fermi_start[0] = p.fermi_start[1] = -10.0
+        return p
+
+
+class MgPairingInfo(C.Structure):
+    _fields_ = [
+        ("fermi", C.c_double * 2), ("particles", C.c_double * 2), ("evaluations", C.c_int),
+        ("converged", C.c_int), ("pairing_energy", C.c_double * 2), ("dispersion", C.c_double * 2),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"fermi": list(self.fermi), "particles": list(self.particles),
+                "evaluations": self.evaluations, "converged": bool(self.converged),
+                "pairing_energy": list(self.pairing_energy), "dispersion": list(self.dispersion)}
+
+
 class MgEnergyTerms(C.Structure):
     _fields_ = [
         ("total", C.c_double),
@@ -124,6 +161,10 @@ SIGNATURES = {
     "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
     "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "mg_set_pairing": [_P, C.POINTER(MgPairingParams)],
+    "mg_solve_pairing": [_P, C.POINTER(MgPairingInfo)],
+    "mg_get_hfb_block": [_P, C.c_int, _D, _D, _D],
+    "mg_get_pairing_field": [_P, _D, _D, _D],
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmocca_gpu.so"

@@ -35,6 +35,7 @@ void free_all(mg_ctx* c) {
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags);
+    hfb_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
@@ -472,6 +473,46 @@ extern "C" int mg_energy(mg_ctx* c, mg_energy_terms* out) {
     return energy(c, out);
 }
 
+extern "C" int mg_set_pairing(mg_ctx* c, const mg_pairing_params* pp) {
+    if (!c || !pp || c->p.pairing != MG_PAIRING_HFB || !c->p.trc || !c->folded) return MG_ERR_ARG;
+    if (c->hfb.ready) return MG_ERR_STATE;
+    if (!(pp->rhosat > 0) || pp->mu[0] <= 0 || pp->mu[1] <= 0 || pp->cut[0] <= 0 || pp->cut[1] <= 0)
+        return MG_ERR_ARG;
+    c->hfb.pp = *pp;
+    c->hfb.fermi[0] = pp->fermi_start[0];
+    c->hfb.fermi[1] = pp->fermi_start[1];
+    return MG_OK;
+}
+
+extern "C" int mg_solve_pairing(mg_ctx* c, mg_pairing_info* info) {
+    if (!c || c->p.pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
+    if (!(c->hfb.pp.rhosat > 0)) return MG_ERR_STATE;  // mg_set_pairing first
+    if (!c->bas[MG_HF_BASIS].have_qn) return MG_ERR_STATE;
+    return hfb_solve(c, info);
+}
+
+extern "C" int mg_get_hfb_block(mg_ctx* c, int b, double* rho, double* kappa, double* delta) {
+    if (!c || b < 0 || b > 3 || !c->hfb.ready) return MG_ERR_ARG;
+    const Hfb& H = c->hfb;
+    const int N = 2 * H.hsz_h[b];
+    const long off = (long)b * H.nmax * H.nmax;
+    if (rho) MG_CUDA(cudaMemcpyAsync(rho, H.rho + off, (size_t)N * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (kappa) MG_CUDA(cudaMemcpyAsync(kappa, H.kappa + off, (size_t)N * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (delta) MG_CUDA(cudaMemcpyAsync(delta, H.delta + off, (size_t)N * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return N;
+}
+
+extern "C" int mg_get_pairing_field(mg_ctx* c, double* re, double* im, double* dfac) {
+    if (!c || !c->hfb.ready) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(copy_out(c, re, c->hfb.fre, 2 * V));
+    MG_TRY(copy_out(c, im, c->hfb.fim, 2 * V));
+    MG_TRY(copy_out(c, dfac, c->hfb.dfac, 2 * V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
 extern "C" int mg_launch_count(mg_ctx* c, long long* count) {
     if (!c || !count) return MG_ERR_ARG;
     *count = c->launches;
@@ -482,12 +523,16 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
                           mg_energy_terms* out) {
     // Evolve loop body, src/Main.f90:255-328 (HF: SolvePairing = NaiveFill)
     if (!c || n_iter < 0) return MG_ERR_ARG;
-    if (c->p.pairing != MG_PAIRING_HF) return MG_ERR_ARG;
+    const bool hfb = c->p.pairing == MG_PAIRING_HFB;
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
         MG_TRY(mg_grad_desc(c, dt, momentum));
-        MG_TRY(mg_hf_fill(c));
+        if (hfb) MG_TRY(mg_solve_pairing(c, nullptr));
+        else MG_TRY(mg_hf_fill(c));
         MG_TRY(mg_derive_all(c));
+        // canonical single-particle energies with the previous potentials
+        // (src/Main.f90:282-289)
+        if (hfb) MG_TRY(hpsi_basis(c, MG_CAN_BASIS, nullptr, false, 0.0, 0.0));
         MG_TRY(densities(c));
         MG_TRY(moments(c));
         st = mg_construct_potentials(c, nullptr);

@@ -65,6 +65,41 @@ struct Basis {
     bool have_qn = false;
 };
 
+struct PairCoef {
+    double cut[2];
+    double mu[2];
+};
+
+// HFB pairing state.  Blocks b = it*2 + (parity+1)/2 hold h stored spwfs
+// (members, in index order) and N = 2h HFB indices (stored, then their
+// time-reversed partners).  rho / kappa / delta are N x N per block,
+// row-major, padded to nmax.
+struct Hfb {
+    mg_pairing_params pp{};
+    PairCoef pc{};
+    bool ready = false;
+    bool oldrho_zero = true;
+    int hmax = 0, nmax = 0;
+    int hsz_h[4] = {0, 0, 0, 0};
+    int parity_h[4] = {0, 0, 0, 0};
+    std::vector<int> members_h;        // 4*hmax
+    int *members = nullptr, *hsz = nullptr, *cstart = nullptr;
+    double *rho = nullptr, *kappa = nullptr, *oldrho = nullptr, *oldkappa = nullptr,
+           *delta = nullptr, *qe = nullptr;
+    double *dfac = nullptr, *pcut = nullptr, *ktil = nullptr, *fpart = nullptr, *fre = nullptr,
+           *fim = nullptr, *gpart = nullptr;
+    int gchunk = 0;
+    double *cantr = nullptr, *occ = nullptr;   // 4*hmax*hmax, 4*hmax
+    double* fermi_d = nullptr;                 // 2
+    double* trace_d = nullptr;                 // 4 block traces of rho
+    double* scal_d = nullptr;                  // [energy(2), disp(2)]
+    double* h_pinned = nullptr;                // 8 pinned doubles
+    double fermi[2] = {-10.0, -10.0};
+    double slope[2] = {0.0, 0.0};              // dN/dlambda from the last solve
+    bool fermi_hist[7] = {false, false, false, false, false, false, false};
+    double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
+};
+
 }  // namespace mg
 
 struct mg_ctx {
@@ -125,6 +160,8 @@ struct mg_ctx {
 
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
+
+    mg::Hfb hfb;
 };
 
 namespace mg {
@@ -145,6 +182,12 @@ int coulomb_solve(mg_ctx* c, int* iters);
 int potentials(mg_ctx* c);
 int energy(mg_ctx* c, mg_energy_terms* out);
 int basis_dots(mg_ctx* c, const double* a, const double* b, double* out);
+int pairing_mesh(mg_ctx* c);
+int canonical_transform(mg_ctx* c);
+int pairing_set_smem(mg_ctx* c);
+int hfb_prepare(mg_ctx* c);
+int hfb_solve(mg_ctx* c, mg_pairing_info* info);
+void hfb_free(mg_ctx* c);
 int density_groups(const mg_ctx* c);
 
 // Lagrange matrix slot selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8.

@@ -205,12 +205,44 @@ class MeshState:
                    allow_not_converged=True)
         return e.as_dict()
 
+    def set_pairing(self, pp=None):
+        """&Pairing values of an HFB run (defaults: the README Mg24 input)."""
+        pp = pp if pp is not None else _abi.MgPairingParams.defaults()
+        self._call("mg_set_pairing", C.byref(pp))
+
+    def SolvePairing(self) -> dict:
+        info = _abi.MgPairingInfo()
+        self._call("mg_solve_pairing", C.byref(info), allow_not_converged=True)
+        return info.as_dict()
+
+    def get_hfb_block(self, b: int):
+        N = self.lib.mg_get_hfb_block(self.h, b, None, None, None)
+        if N < 0:
+            raise _abi.MgError("mg_get_hfb_block", N)
+        r, k, d = (np.empty(N * N) for _ in range(3))
+        self.lib.mg_get_hfb_block(self.h, b, _dptr(r), _dptr(k), _dptr(d))
+        return r.reshape(N, N), k.reshape(N, N), d.reshape(N, N)
+
+    def get_pairing_field(self):
+        V = self.V
+        re, im, df = np.empty(2 * V), np.empty(2 * V), np.empty(2 * V)
+        self._call("mg_get_pairing_field", _dptr(re), _dptr(im), _dptr(df))
+        return re, im, df
+
     def Start(self):
-        """Iteration-0 preparation of Evolve (src/Main.f90:177-231) for an HF
-        run started from spinors with given energies: fill, derive, densities,
-        moments, potentials."""
-        self.HFFill()
+        """Iteration-0 preparation of Evolve (src/Main.f90:177-231) for a run
+        started from spinors with given energies: pairing step (HF filling or
+        HFB), derivatives, densities, moments, potentials and, under HFB, the
+        canonical single-particle energies."""
+        hfb = self.p.pairing == _abi.MG_PAIRING_HFB
+        if hfb:
+            self.SolvePairing()
+        else:
+            self.HFFill()
         self.DeriveAll()
         self.UpdateDensities()
         self.CalculateAllMoments()
-        return self.ConstructPotentials()
+        it = self.ConstructPotentials()
+        if hfb:
+            self.hPsi(_abi.MG_CAN_BASIS, want_spinors=False)
+        return it

@@ -55,6 +55,23 @@ struct orc_ctx {
     std::vector<double> sh_ext;  // [moment][mx*my*mz]
     std::vector<Moment> moments;
     bool coulomb_init = false;
+
+    // HFB pairing (src/HFB.f90, src/PairingInteraction.f90).  Blocks are the
+    // (isospin, parity) blocks b = it*2 + (parity+1)/2; a block lists HFB
+    // indices 0..2nwt-1 (stored spwfs first, then their time-reversed
+    // partners, as PrepareHFBModule orders them).  All matrices are real
+    // (time simplex conserved) and row-major [i*N + j].
+    mg_pairing_params pp{};
+    bool hfb_ready = false;
+    std::vector<int> bidx[4];
+    std::vector<double> rho_h[4], kappa_h[4], oldrho[4], oldkappa[4], delta[4];
+    std::vector<double> Um[4], Vm[4], qe[4], cantr[4], occs[4];
+    double fermi[2] = {-10.0, -10.0};
+    std::vector<double> pcut, dfac, pf_re, pf_im;
+    double epair[2] = {0.0, 0.0};
+    double pdisp[2] = {0.0, 0.0};
+    bool fermi_hist[7] = {false, false, false, false, false, false, false};
+    int last_evals = 0;
 };
 
 // --------------------------------------------------------------------------
@@ -1026,6 +1043,10 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
         double mt = c->p.neutrons * c->f.nucleonmass[0] + c->p.protons * c->f.nucleonmass[1];
         for (int it = 0; it < 2; ++it) out->com[0][it] = -out->kinetic[it] * c->f.nucleonmass[it] / mt;
     }
+    if (c->p.pairing == MG_PAIRING_HFB) {
+        out->pairing[0] = c->epair[0];
+        out->pairing[1] = c->epair[1];
+    }
     double com = out->com[0][0] + out->com[1][0] + out->com[0][1] + out->com[1][1];
     out->total = sk + (out->kinetic[0] + out->kinetic[1]) + ec + com + ex +
                  (out->pairing[0] + out->pairing[1]);
@@ -1043,18 +1064,601 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
 }
 
 // --------------------------------------------------------------------------
+// Symmetric eigensolver: Householder tridiagonalisation followed by implicit
+// QL with eigenvector accumulation (the published tred2 / tql2 algorithm of
+// Martin, Reinsch and Wilkinson that diagoncr8, src/HFB.f90:5880-6087, also
+// implements), eigenvalues sorted ascending with their vectors.
+// a: n*n row-major symmetric input; w: eigenvalues; z: n*n, column k = vector k.
+// --------------------------------------------------------------------------
+extern "C" int orc_eigh(int n, const double* a_in, double* w, double* z) {
+    if (n <= 0) return MG_ERR_ARG;
+    std::vector<double> A(a_in, a_in + (size_t)n * n), d(n), e(n);
+    auto a = [&](int i, int j) -> double& { return A[(size_t)i * n + j]; };
+    for (int i = n - 1; i > 0; --i) {
+        const int l = i - 1;
+        double h = 0.0, scale = 0.0;
+        if (l > 0) {
+            for (int k = 0; k <= l; ++k) scale += std::fabs(a(i, k));
+            if (scale == 0.0) {
+                e[i] = a(i, l);
+            } else {
+                for (int k = 0; k <= l; ++k) { a(i, k) /= scale; h += a(i, k) * a(i, k); }
+                double f = a(i, l);
+                double g = f >= 0.0 ? -std::sqrt(h) : std::sqrt(h);
+                e[i] = scale * g;
+                h -= f * g;
+                a(i, l) = f - g;
+                f = 0.0;
+                for (int j = 0; j <= l; ++j) {
+                    a(j, i) = a(i, j) / h;
+                    g = 0.0;
+                    for (int k = 0; k <= j; ++k) g += a(j, k) * a(i, k);
+                    for (int k = j + 1; k <= l; ++k) g += a(k, j) * a(i, k);
+                    e[j] = g / h;
+                    f += e[j] * a(i, j);
+                }
+                const double hh = f / (h + h);
+                for (int j = 0; j <= l; ++j) {
+                    f = a(i, j);
+                    e[j] = g = e[j] - hh * f;
+                    for (int k = 0; k <= j; ++k) a(j, k) -= (f * e[k] + g * a(i, k));
+                }
+            }
+        } else {
+            e[i] = a(i, l);
+        }
+        d[i] = h;
+    }
+    d[0] = 0.0;
+    e[0] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const int l = i - 1;
+        if (d[i] != 0.0) {
+            for (int j = 0; j <= l; ++j) {
+                double g = 0.0;
+                for (int k = 0; k <= l; ++k) g += a(i, k) * a(k, j);
+                for (int k = 0; k <= l; ++k) a(k, j) -= g * a(k, i);
+            }
+        }
+        d[i] = a(i, i);
+        a(i, i) = 1.0;
+        for (int j = 0; j <= l; ++j) a(j, i) = a(i, j) = 0.0;
+    }
+    for (int i = 1; i < n; ++i) e[i - 1] = e[i];
+    e[n - 1] = 0.0;
+    for (int l = 0; l < n; ++l) {
+        int iter = 0, m;
+        do {
+            for (m = l; m < n - 1; ++m) {
+                const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+                if (std::fabs(e[m]) <= 2.2e-16 * dd) break;
+            }
+            if (m != l) {
+                if (iter++ == 60) return MG_NOT_CONVERGED;
+                double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                double r = std::hypot(g, 1.0);
+                g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? std::fabs(r) : -std::fabs(r)));
+                double s = 1.0, c = 1.0, p = 0.0;
+                int i;
+                for (i = m - 1; i >= l; --i) {
+                    double f = s * e[i], b = c * e[i];
+                    e[i + 1] = (r = std::hypot(f, g));
+                    if (r == 0.0) {
+                        d[i + 1] -= p;
+                        e[m] = 0.0;
+                        break;
+                    }
+                    s = f / r;
+                    c = g / r;
+                    g = d[i + 1] - p;
+                    r = (d[i] - g) * s + 2.0 * c * b;
+                    d[i + 1] = g + (p = s * r);
+                    g = c * r - b;
+                    for (int k = 0; k < n; ++k) {
+                        f = a(k, i + 1);
+                        a(k, i + 1) = s * a(k, i) + c * f;
+                        a(k, i) = c * a(k, i) - s * f;
+                    }
+                }
+                if (r == 0.0 && i >= l) continue;
+                d[l] -= p;
+                e[l] = g;
+                e[m] = 0.0;
+            }
+        } while (m != l);
+    }
+    // selection sort ascending, as the last loop of diagoncr8
+    for (int i = 0; i < n - 1; ++i) {
+        int k = i;
+        double p = d[i];
+        for (int j = i + 1; j < n; ++j)
+            if (d[j] < p) { k = j; p = d[j]; }
+        if (k != i) {
+            d[k] = d[i];
+            d[i] = p;
+            for (int j = 0; j < n; ++j) std::swap(a(j, i), a(j, k));
+        }
+    }
+    std::copy(d.begin(), d.end(), w);
+    std::copy(A.begin(), A.end(), z);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// HFB pairing step (PairingType 2, FermiSolver 'BROYDEN', PairingIter 1,
+// no Lipkin-Nogami, no blocking, ULB density-dependent delta pairing).
+// --------------------------------------------------------------------------
+static const double kHFBNumCut = 1e-12;  // src/HFB.f90:46
+
+extern "C" int orc_set_pairing(orc_ctx* c, const mg_pairing_params* pp) {
+    if (!c || !pp || c->p.pairing != MG_PAIRING_HFB || !c->p.trc || !c->folded) return MG_ERR_ARG;
+    c->pp = *pp;
+    c->fermi[0] = pp->fermi_start[0];
+    c->fermi[1] = pp->fermi_start[1];
+    return MG_OK;
+}
+
+// PrepareHFBModule, src/HFB.f90:245-292
+static void hfb_prepare(orc_ctx* c) {
+    const Basis& B = c->bas[MG_HF_BASIS];
+    const int nwt = c->p.nwt;
+    for (int b = 0; b < 4; ++b) c->bidx[b].clear();
+    for (int i = 0; i < 2 * nwt; ++i) {
+        const int ii = i % nwt;
+        const int P = (B.qn[4 * ii + 1] + 1) / 2, it = (B.qn[4 * ii] + 3) / 2 - 1;
+        c->bidx[it * 2 + P].push_back(i);
+    }
+    for (int b = 0; b < 4; ++b) {
+        const size_t N = c->bidx[b].size();
+        for (auto* v : {&c->rho_h[b], &c->kappa_h[b], &c->oldrho[b], &c->oldkappa[b], &c->delta[b],
+                        &c->cantr[b]})
+            v->assign(N * N, 0.0);
+        c->Um[b].assign(N * 2 * N, 0.0);
+        c->Vm[b].assign(N * 2 * N, 0.0);
+        c->qe[b].assign(2 * N, 0.0);
+        c->occs[b].assign(N, 0.0);
+    }
+    c->pcut.assign(nwt, 0.0);
+    c->dfac.assign(2 * c->V, 0.0);
+    c->pf_re.assign(2 * c->V, 0.0);
+    c->pf_im.assign(2 * c->V, 0.0);
+    c->hfb_ready = true;
+}
+
+// sig of HFB index i (time-reversed partner flips the signature)
+static int hfb_sig(const orc_ctx* c, int i) {
+    const int nwt = c->p.nwt;
+    const int s = c->bas[MG_HF_BASIS].qn[4 * (i % nwt) + 2];
+    return i >= nwt ? -s : s;
+}
+
+// ComputePairingCutoffs + SymmetricFermi, src/PairingInteraction.f90:182-228
+static void pairing_cutoffs(orc_ctx* c, const double* lambda) {
+    const Basis& B = c->bas[MG_HF_BASIS];
+    for (int i = 0; i < c->p.nwt; ++i) {
+        const int it = (B.qn[4 * i] + 3) / 2 - 1;
+        const double E = B.e[i];
+        const double up = (E - lambda[it] - c->pp.cut[it]) / c->pp.mu[it];
+        const double down = -(E - lambda[it] + c->pp.cut[it]) / c->pp.mu[it];
+        double f = std::sqrt(std::sqrt(1.0 / (1.0 + std::exp(up))));
+        f = f * std::sqrt(std::sqrt(1.0 / (1.0 + std::exp(down))));
+        c->pcut[i] = f;
+    }
+}
+
+// GetPairDensity, src/PairingInteraction.f90:101-180, at one point
+static inline void pair_density(const double* l, const double* r, bool tr, double& re, double& im) {
+    if (!tr) {
+        re = l[0] * r[2] - l[1] * r[3] - l[2] * r[0] + l[3] * r[1];
+        im = l[0] * r[3] + l[1] * r[2] - l[2] * r[1] - l[3] * r[0];
+    } else {
+        re = -l[0] * r[0] - l[1] * r[1] - l[2] * r[2] - l[3] * r[3];
+        im = l[0] * r[1] - l[1] * r[0] + l[2] * r[3] - l[3] * r[2];
+    }
+}
+
+// HFBPairingField, src/HFB.f90:350-518 (no LN), with CompDensityFactor (ULB)
+static void pairing_field(orc_ctx* c) {
+    const long V = c->V;
+    const int nwt = c->p.nwt;
+    const Basis& B = c->bas[MG_HF_BASIS];
+    for (int it = 0; it < 2; ++it)
+        for (long v = 0; v < V; ++v) {
+            const double rho0 = c->rho[v] + c->rho[V + v];
+            c->dfac[it * V + v] = -c->pp.strength[it] * (1.0 - c->pp.alpha[it] / c->pp.rhosat * rho0);
+        }
+    std::fill(c->pf_re.begin(), c->pf_re.end(), 0.0);
+    std::fill(c->pf_im.begin(), c->pf_im.end(), 0.0);
+    for (int b = 0; b < 4; ++b) {
+        const int it = b / 2;
+        const auto& idx = c->bidx[b];
+        const int N = (int)idx.size();
+        for (int j = 0; j < N; ++j) {
+            const int jj = idx[j], jjj = jj % nwt;
+            const int sig1 = hfb_sig(c, jj);
+            const double c1 = c->pcut[jjj];
+            if (c1 < kHFBNumCut) continue;
+            for (int i = j + 1; i < N; ++i) {
+                const int ii = idx[i], iii = ii % nwt;
+                const int sig2 = hfb_sig(c, ii);
+                if (sig1 != -sig2) continue;
+                const double c2 = c->pcut[iii];
+                const double kij = c->kappa_h[b][(size_t)i * N + j];
+                if (c1 * c2 * std::fabs(kij) < kHFBNumCut) continue;
+                const bool tr = (ii >= nwt || jj >= nwt) && !(ii >= nwt && jj >= nwt);
+                const double factor = c1 * c2 * kij;
+                const double* pl = &B.psi[(long)jjj * 4 * V];
+                const double* pr = &B.psi[(long)iii * 4 * V];
+                for (long v = 0; v < V; ++v) {
+                    const double l[4] = {pl[v], pl[V + v], pl[2 * V + v], pl[3 * V + v]};
+                    const double r[4] = {pr[v], pr[V + v], pr[2 * V + v], pr[3 * V + v]};
+                    double re, im;
+                    pair_density(l, r, tr, re, im);
+                    c->pf_re[it * V + v] = c->pf_re[it * V + v] - factor * re;
+                    c->pf_im[it * V + v] = c->pf_im[it * V + v] - factor * im;
+                }
+            }
+        }
+    }
+    for (int it = 0; it < 2; ++it)
+        for (long v = 0; v < V; ++v) {
+            c->pf_re[it * V + v] = c->pf_re[it * V + v] * c->dfac[it * V + v] * 1.0;
+            c->pf_im[it * V + v] = c->pf_im[it * V + v] * c->dfac[it * V + v] * 1.0;
+        }
+}
+
+// HFBGaps, src/HFB.f90:520-632
+static void pairing_gaps(orc_ctx* c) {
+    const long V = c->V;
+    const int nwt = c->p.nwt;
+    const Basis& B = c->bas[MG_HF_BASIS];
+    for (int b = 0; b < 4; ++b) {
+        const int it = b / 2;
+        const auto& idx = c->bidx[b];
+        const int N = (int)idx.size();
+        std::fill(c->delta[b].begin(), c->delta[b].end(), 0.0);
+        for (int i = 0; i < N; ++i) {
+            const int ii = idx[i], iii = ii % nwt;
+            const int sig1 = hfb_sig(c, ii);
+            const double c1 = c->pcut[iii];
+            for (int j = i + 1; j < N; ++j) {
+                const int jj = idx[j], jjj = jj % nwt;
+                const int sig2 = hfb_sig(c, jj);
+                if (sig1 != -sig2) continue;
+                const double c2 = c->pcut[jjj];
+                if (c1 * c2 < kHFBNumCut) continue;
+                const bool tr = (ii >= nwt || jj >= nwt) && !(ii >= nwt && jj >= nwt);
+                const double* pl = &B.psi[(long)iii * 4 * V];
+                const double* pr = &B.psi[(long)jjj * 4 * V];
+                double s1 = 0.0, s2 = 0.0;
+                for (long v = 0; v < V; ++v) {
+                    const double l[4] = {pl[v], pl[V + v], pl[2 * V + v], pl[3 * V + v]};
+                    const double r[4] = {pr[v], pr[V + v], pr[2 * V + v], pr[3 * V + v]};
+                    double re, im;
+                    pair_density(l, r, tr, re, im);
+                    s1 += re * c->pf_re[it * V + v];
+                    s2 += im * c->pf_im[it * V + v];
+                }
+                const double d = c->dv * c1 * c2 * (s1 + s2);
+                c->delta[b][(size_t)i * N + j] = d;
+                c->delta[b][(size_t)j * N + i] = -d;
+            }
+        }
+    }
+}
+
+// HFBNumberofParticles_ordinary (PfSolver off, SC conserved: the CR8 column
+// choice), with ConstructHFBHamiltonian, DiagonaliseHFBHamiltonian_Signature,
+// constructRhoHFB and ConstructKappaHFB (src/HFB.f90:810-1072, :2554-2786,
+// :3128-3154, :3335-3359).  Returns Tr rho per isospin.
+static int hfb_number(orc_ctx* c, const double* lambda, double* Nout) {
+    const Basis& B = c->bas[MG_HF_BASIS];
+    const int nwt = c->p.nwt;
+    Nout[0] = Nout[1] = 0.0;
+    for (int b = 0; b < 4; ++b) {
+        const int it = b / 2;
+        const auto& idx = c->bidx[b];
+        const int N = (int)idx.size(), h = N / 2;
+        if (N == 0) continue;
+        std::vector<double> T((size_t)N * N, 0.0), w(N), X((size_t)N * N);
+        for (int j = 0; j < h; ++j)
+            for (int i = 0; i < h; ++i) {
+                const double hij = (i == j) ? B.e[idx[i] % nwt] - lambda[it] : 0.0;
+                const double hr = (i == j) ? -(B.e[idx[i + h] % nwt] - lambda[it]) : 0.0;
+                T[(size_t)i * N + j] = hij;
+                T[(size_t)j * N + i] = hij;
+                T[(size_t)(i + h) * N + j + h] = hr;
+                T[(size_t)(j + h) * N + i + h] = hr;
+                const double dd = c->delta[b][(size_t)i * N + j + h];
+                T[(size_t)i * N + j + h] = dd;
+                T[(size_t)(j + h) * N + i] = dd;
+            }
+        if (orc_eigh(N, T.data(), w.data(), X.data()) != MG_OK) return MG_NOT_CONVERGED;
+        std::vector<double>& U = c->Um[b];
+        std::vector<double>& Vv = c->Vm[b];
+        std::fill(U.begin(), U.end(), 0.0);
+        std::fill(Vv.begin(), Vv.end(), 0.0);
+        const int N2 = 2 * N;
+        for (int k = 0; k < N; ++k) {
+            for (int r = 0; r < h; ++r) {
+                U[(size_t)r * N2 + k] = X[(size_t)r * N + k];
+                Vv[(size_t)(h + r) * N2 + k] = X[(size_t)(h + r) * N + k];
+                U[(size_t)(h + r) * N2 + N + k] = -X[(size_t)r * N + k];
+                Vv[(size_t)r * N2 + N + k] = X[(size_t)(h + r) * N + k];
+            }
+            c->qe[b][k] = w[k];
+            c->qe[b][N + k] = w[k];
+        }
+        std::vector<int> cols(N);
+        for (int i = 0; i < h; ++i) cols[i] = 2 * N - 1 - i;
+        for (int i = h; i < N; ++i) cols[i] = i;
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                double s = 0.0;
+                for (int k = 0; k < N; ++k) s += Vv[(size_t)i * N2 + cols[k]] * Vv[(size_t)j * N2 + cols[k]];
+                c->rho_h[b][(size_t)i * N + j] = s;
+            }
+        for (int j = 0; j < N; ++j)
+            for (int i = j + 1; i < N; ++i) {
+                double s = 0.0;
+                for (int k = 0; k < N; ++k) s += Vv[(size_t)i * N2 + cols[k]] * U[(size_t)j * N2 + cols[k]];
+                c->kappa_h[b][(size_t)i * N + j] = s;
+                c->kappa_h[b][(size_t)j * N + i] = -s;
+            }
+        for (int i = 0; i < N; ++i) Nout[it] += c->rho_h[b][(size_t)i * N + i];
+    }
+    return MG_OK;
+}
+
+// HFBFindFermiEnergyBroyden, src/HFB.f90:1849-2161 (no LN, no dispersion
+// constraint): damped (step 0.5) Broyden on N(lambda) - N0 per isospin.
+static int fermi_broyden(orc_ctx* c, int* evals) {
+    const double part[2] = {c->p.neutrons, c->p.protons};
+    const double prec = c->pp.fermi_prec;
+    double hist[2] = {c->fermi[0] + 0.01, c->fermi[1] + 0.01};
+    bool conv[2] = {false, false};
+    double N[2], NX[2], J[2], upd[2] = {0, 0}, norm[2] = {1, 1};
+    int ne = 0, st;
+    if ((st = hfb_number(c, c->fermi, N)) != MG_OK) return st;
+    ++ne;
+    for (int it = 0; it < 2; ++it) {
+        N[it] -= part[it];
+        if (std::fabs(N[it]) < prec) conv[it] = true;
+    }
+    if ((st = hfb_number(c, hist, NX)) != MG_OK) return st;
+    ++ne;
+    for (int it = 0; it < 2; ++it) {
+        NX[it] -= part[it];
+        J[it] = (N[it] - NX[it]) / (c->fermi[it] - hist[it]);
+    }
+    const double step = 0.5;
+    for (int iter = 1; iter <= c->pp.max_iter; ++iter) {
+        double invJ[2];
+        for (int it = 0; it < 2; ++it)
+            invJ[it] = std::fabs(J[it]) < 0.001 ? (J[it] >= 0 ? 0.99 : -0.99) : 1.0 / J[it];
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            upd[it] = -invJ[it] * N[it];
+            norm[it] = upd[it] * upd[it];
+        }
+        for (int it = 0; it < 2; ++it) upd[it] = step * upd[it];
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            hist[it] = c->fermi[it];
+            c->fermi[it] = c->fermi[it] + upd[it];
+        }
+        if ((st = hfb_number(c, c->fermi, N)) != MG_OK) return st;
+        ++ne;
+        for (int it = 0; it < 2; ++it) {
+            N[it] -= part[it];
+            if (std::fabs(N[it]) < prec) conv[it] = true;
+        }
+        if (conv[0] && conv[1]) break;
+        if (iter > 1)
+            for (int it = 0; it < 2; ++it) {
+                if (conv[it]) continue;
+                J[it] = J[it] + N[it] * upd[it] / norm[it];
+            }
+        for (int it = 0; it < 2; ++it)
+            if (std::isnan(N[it])) return MG_ERR_NAN;
+    }
+    for (int i = 0; i < 6; ++i) c->fermi_hist[i] = c->fermi_hist[i + 1];
+    c->fermi_hist[6] = std::fabs(N[0]) > 0.9 || std::fabs(N[1]) > 0.9;
+    bool lost = true;
+    for (int i = 0; i < 7; ++i) lost = lost && c->fermi_hist[i];
+    if (evals) *evals = ne;
+    if (lost) return MG_ERR_STATE;
+    return (conv[0] && conv[1]) ? MG_OK : MG_NOT_CONVERGED;
+}
+
+// DiagonaliseRhoHFB + HFBOccupations, src/HFB.f90:3156-3284, :3361-3560:
+// canonical basis from the eigenvectors of rho, occupations, rho / kappa mixing.
+static int hfb_occupations(orc_ctx* c) {
+    const int nwt = c->p.nwt;
+    const long V4 = 4 * c->V;
+    Basis& H = c->bas[MG_HF_BASIS];
+    Basis& C = c->bas[MG_CAN_BASIS];
+    std::fill(C.psi.begin(), C.psi.end(), 0.0);
+    c->pdisp[0] = c->pdisp[1] = 0.0;
+    int index = 0;
+    for (int b = 0; b < 4; ++b) {
+        const int it = b / 2;
+        const auto& idx = c->bidx[b];
+        const int N = (int)idx.size(), h = N / 2;
+        if (N == 0) continue;
+        std::vector<double> T(c->rho_h[b]), w(N), X((size_t)N * N);
+        for (int i = 0; i < N; ++i)
+            if (idx[i] >= nwt || hfb_sig(c, idx[i]) == -1) T[(size_t)i * N + i] -= 2.0;
+        if (orc_eigh(N, T.data(), w.data(), X.data()) != MG_OK) return MG_NOT_CONVERGED;
+        for (int k = 0; k < N; ++k) {
+            double o = w[k];
+            if (o < -0.1) o += 2.0;
+            if (o < 0.0) o = 0.0;
+            if (o > 1.0) o = 1.0;
+            c->occs[b][k] = 2.0 * o;
+        }
+        for (size_t q = 0; q < X.size(); ++q)
+            if (std::fabs(X[q]) < 1e-11) X[q] = 0.0;
+        c->cantr[b] = X;
+        for (int col = 0; col < N; ++col) {
+            bool neg = false;
+            for (int r = h; r < N; ++r) neg = neg || std::fabs(X[(size_t)r * N + col]) > kHFBNumCut;
+            if (neg) continue;
+            if (index >= nwt) return MG_ERR_STATE;
+            int loc = 0;
+            for (int r = 1; r < N; ++r)
+                if (std::fabs(X[(size_t)r * N + col]) > std::fabs(X[(size_t)loc * N + col])) loc = r;
+            const int dom = idx[loc] % nwt;
+            C.qn[4 * index + 0] = 2 * it - 1;
+            C.qn[4 * index + 1] = H.qn[4 * dom + 1];
+            C.qn[4 * index + 2] = hfb_sig(c, idx[loc]);
+            C.qn[4 * index + 3] = H.qn[4 * dom + 3];
+            double* out = &C.psi[(long)index * V4];
+            for (int r = 0; r < N; ++r) {
+                const double ct = X[(size_t)r * N + col];
+                if (std::fabs(ct) < kHFBNumCut) continue;
+                const double* src = &H.psi[(long)(idx[r] % nwt) * V4];
+                for (long q = 0; q < V4; ++q) out[q] = out[q] + ct * src[q];
+            }
+            const double o = c->occs[b][col];
+            c->pdisp[it] += o * (2.0 - o);
+            C.occ[index] = o;
+            ++index;
+        }
+    }
+    if (index != nwt) return MG_ERR_STATE;
+    bool oldzero = true, kzero = true;
+    for (int b = 0; b < 4; ++b) {
+        for (double x : c->oldrho[b]) oldzero = oldzero && x == 0.0;
+        for (double x : c->kappa_h[b]) kzero = kzero && x == 0.0;
+    }
+    const double m = c->pp.mix;
+    for (int b = 0; b < 4; ++b) {
+        if (!oldzero)
+            for (size_t q = 0; q < c->rho_h[b].size(); ++q)
+                c->rho_h[b][q] = m * c->rho_h[b][q] + (1.0 - m) * c->oldrho[b][q];
+        if (!kzero)
+            for (size_t q = 0; q < c->kappa_h[b].size(); ++q)
+                c->kappa_h[b][q] = m * c->kappa_h[b][q] + (1.0 - m) * c->oldkappa[b][q];
+        c->oldrho[b] = c->rho_h[b];
+        c->oldkappa[b] = c->kappa_h[b];
+    }
+    return MG_OK;
+}
+
+// GuessHFBMatrices case(2), src/HFB.f90:3645-3835, time-reversal conserved:
+// every stored spwf is paired with its own time-reversed partner.
+static void guess_kappa(orc_ctx* c) {
+    for (int b = 0; b < 4; ++b) {
+        const int N = (int)c->bidx[b].size(), h = N / 2;
+        std::fill(c->kappa_h[b].begin(), c->kappa_h[b].end(), 0.0);
+        for (int i = 0; i < h; ++i) {
+            c->kappa_h[b][(size_t)i * N + i + h] = -0.25;
+            c->kappa_h[b][(size_t)(i + h) * N + i] = 0.25;
+        }
+    }
+}
+
+// HFBEnergy, src/HFB.f90:296-348
+static void hfb_energy(orc_ctx* c) {
+    c->epair[0] = c->epair[1] = 0.0;
+    for (int b = 0; b < 4; ++b) {
+        const int it = b / 2;
+        const size_t n = c->delta[b].size();
+        double e = 0.0;
+        for (size_t q = 0; q < n; ++q) e = e - c->delta[b][q] * c->kappa_h[b][q];
+        c->epair[it] += e;
+    }
+    c->epair[0] *= -0.5;
+    c->epair[1] *= -0.5;
+}
+
+// SolvePairing, src/Pairing.f90:743-890
+extern "C" int orc_solve_pairing(orc_ctx* c, mg_pairing_info* info) {
+    if (!c || c->p.pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
+    if (!c->hfb_ready) {
+        hfb_prepare(c);
+        if (c->pp.guess_kappa) {
+            guess_kappa(c);
+            c->pp.guess_kappa = 0;
+        }
+    }
+    bool oz = true;
+    for (int b = 0; b < 4; ++b)
+        for (double x : c->oldrho[b]) oz = oz && x == 0.0;
+    if (oz)
+        for (int b = 0; b < 4; ++b) {
+            c->oldrho[b] = c->rho_h[b];
+            c->oldkappa[b] = c->kappa_h[b];
+        }
+    pairing_cutoffs(c, c->fermi);
+    pairing_field(c);
+    pairing_gaps(c);
+    int evals = 0;
+    const int st = fermi_broyden(c, &evals);
+    if (st < 0 && st != MG_ERR_STATE) return st;
+    double tr[2] = {0.0, 0.0};
+    for (int b = 0; b < 4; ++b) {
+        const int N = (int)c->bidx[b].size();
+        for (int i = 0; i < N; ++i) tr[b / 2] += c->rho_h[b][(size_t)i * N + i];
+    }
+    pairing_cutoffs(c, c->fermi);
+    const int so = hfb_occupations(c);
+    if (so != MG_OK) return so < 0 ? so : MG_ERR_STATE;
+    hfb_energy(c);
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->fermi[0] = c->fermi[0];
+        info->fermi[1] = c->fermi[1];
+        info->particles[0] = tr[0];
+        info->particles[1] = tr[1];
+        info->evaluations = evals;
+        info->converged = st == MG_OK;
+        info->pairing_energy[0] = c->epair[0];
+        info->pairing_energy[1] = c->epair[1];
+        info->dispersion[0] = c->pdisp[0];
+        info->dispersion[1] = c->pdisp[1];
+    }
+    return st == MG_ERR_STATE ? MG_ERR_STATE : MG_OK;
+}
+
+extern "C" int orc_get_hfb_block(orc_ctx* c, int b, double* rho, double* kappa, double* delta) {
+    if (!c || b < 0 || b > 3 || !c->hfb_ready) return MG_ERR_ARG;
+    const size_t n = c->rho_h[b].size();
+    if (rho) std::copy(c->rho_h[b].begin(), c->rho_h[b].end(), rho);
+    if (kappa) std::copy(c->kappa_h[b].begin(), c->kappa_h[b].end(), kappa);
+    if (delta) std::copy(c->delta[b].begin(), c->delta[b].end(), delta);
+    return (int)std::lround(std::sqrt((double)n));
+}
+
+extern "C" int orc_get_pairing_field(orc_ctx* c, double* re, double* im, double* dfac) {
+    if (!c || !c->hfb_ready) return MG_ERR_ARG;
+    if (re) std::copy(c->pf_re.begin(), c->pf_re.end(), re);
+    if (im) std::copy(c->pf_im.begin(), c->pf_im.end(), im);
+    if (dfac) std::copy(c->dfac.begin(), c->dfac.end(), dfac);
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
 // Evolve loop body, src/Main.f90:255-328, HF pairing type (SolvePairing =
 // NaiveFill), no constraints, MixingScheme 0.
 // --------------------------------------------------------------------------
 extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
                            mg_energy_terms* out) {
     if (!c) return MG_ERR_ARG;
-    if (c->p.pairing != MG_PAIRING_HF) return MG_ERR_ARG;
+    const bool hfb = c->p.pairing == MG_PAIRING_HFB;
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
         orc_grad_desc(c, dt, momentum);
-        orc_hf_fill(c);
+        if (hfb) {
+            const int sp = orc_solve_pairing(c, nullptr);
+            if (sp < 0) return sp;
+        } else {
+            orc_hf_fill(c);
+        }
         orc_derive_all(c);
+        if (hfb) orc_hpsi(c, MG_CAN_BASIS, nullptr, c->bas[MG_CAN_BASIS].e.data(),
+                          c->bas[MG_CAN_BASIS].disp.data());
         orc_update_densities(c);
         orc_calculate_moments(c);
         st = orc_construct_potentials(c, nullptr);

@@ -72,6 +72,15 @@ int orc_energy(orc_ctx* c, mg_energy_terms* out);
 int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
                 mg_energy_terms* out);
 
+/* HFB pairing (src/Pairing.f90:743-890 with the HFB procedures). */
+int orc_set_pairing(orc_ctx* c, const mg_pairing_params* pp);
+int orc_solve_pairing(orc_ctx* c, mg_pairing_info* info);
+/* block b = it*2 + (parity+1)/2: size N, rho/kappa/delta (N*N each), may be NULL */
+int orc_get_hfb_block(orc_ctx* c, int b, double* rho, double* kappa, double* delta);
+int orc_get_pairing_field(orc_ctx* c, double* re, double* im, double* dfac);
+/* symmetric eigensolver of the oracle (tred2 + tql2, ascending) */
+int orc_eigh(int n, const double* a, double* w, double* z);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,11 @@ _SIG = {
     "orc_set_potentials": ([_P, _D, _D, _D, _D, _D], C.c_int),
     "orc_energy": ([_P, C.POINTER(_abi.MgEnergyTerms)], C.c_int),
     "orc_iterate": ([_P, C.c_int, C.c_double, C.c_double, C.POINTER(_abi.MgEnergyTerms)], C.c_int),
+    "orc_set_pairing": ([_P, C.POINTER(_abi.MgPairingParams)], C.c_int),
+    "orc_solve_pairing": ([_P, C.POINTER(_abi.MgPairingInfo)], C.c_int),
+    "orc_get_hfb_block": ([_P, C.c_int, _D, _D, _D], C.c_int),
+    "orc_get_pairing_field": ([_P, _D, _D, _D], C.c_int),
+    "orc_eigh": ([C.c_int, _D, _D, _D], C.c_int),
 }
 
 _lib = None
@@ -249,9 +254,51 @@ class OracleState:
                    allow_not_converged=True)
         return e.as_dict()
 
+    def set_pairing(self, pp=None):
+        pp = pp if pp is not None else _abi.MgPairingParams.defaults()
+        self._call("orc_set_pairing", C.byref(pp))
+
+    def SolvePairing(self):
+        info = _abi.MgPairingInfo()
+        self._call("orc_solve_pairing", C.byref(info), allow_not_converged=True)
+        return info.as_dict()
+
+    def get_hfb_block(self, b):
+        N = self.lib.orc_get_hfb_block(self.h, b, None, None, None)
+        if N < 0:
+            raise RuntimeError("no HFB state")
+        r, k, d = (np.empty(N * N) for _ in range(3))
+        self.lib.orc_get_hfb_block(self.h, b, _d(r), _d(k), _d(d))
+        return r.reshape(N, N), k.reshape(N, N), d.reshape(N, N)
+
+    def get_pairing_field(self):
+        V = self.V
+        re, im, df = np.empty(2 * V), np.empty(2 * V), np.empty(2 * V)
+        self._call("orc_get_pairing_field", _d(re), _d(im), _d(df))
+        return re, im, df
+
     def Start(self):
-        self.HFFill()
+        """Iteration-0 preparation of Evolve (src/Main.f90:177-231)."""
+        hfb = self.p.pairing == _abi.MG_PAIRING_HFB
+        if hfb:
+            self.SolvePairing()
+        else:
+            self.HFFill()
         self.DeriveAll()
         self.UpdateDensities()
         self.CalculateAllMoments()
-        return self.ConstructPotentials()
+        it = self.ConstructPotentials()
+        if hfb:
+            _, e, d = self.hPsi(_abi.MG_CAN_BASIS, want_spinors=False)
+            self.set_energies(e, _abi.MG_CAN_BASIS)
+        return it
+
+
+def eigh(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    n = a.shape[0]
+    w = np.empty(n)
+    z = np.empty((n, n))
+    st = load().orc_eigh(n, _d(a), _d(w), _d(z))
+    _abi.check("orc_eigh", st)
+    return w, z
