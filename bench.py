@@ -42,9 +42,9 @@ METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
 
 
 def _params(precision):
-    from mocca_gb300 import MG_FP64, MG_MIXED, MG_PAIRING_HF, RunParams
+    from mocca_gb300 import MG_FP64, MG_MIXED, MG_PAIRING_HFB, RunParams
     return RunParams(**WORKLOAD, precision=MG_MIXED if precision == "mixed" else MG_FP64,
-                     pairing=MG_PAIRING_HF)
+                     pairing=MG_PAIRING_HFB)
 
 
 def _start_state(p, seed):
@@ -135,13 +135,14 @@ def cpu_baseline(sample_steps=1):
     o = O.OracleState(p, SLY4)
     o.set_spinors(psi, qn)
     o.set_energies(en)
+    o.set_pairing()
     o.Start()
     t = time.perf_counter()
     o.Evolve(sample_steps, DT, MOMENTUM)
     dt = time.perf_counter() - t
     o.close()
     return {"value": sample_steps / dt, "unit": "iter/s", "cores": 1, "kind": "port",
-            "sample": f"{sample_steps} HF iteration(s) of the full 24^3 nwt=160 workload, "
+            "sample": f"{sample_steps} HFB iteration(s) of the full 24^3 nwt=160 workload, "
                       f"oracle (C++ FP64 restatement, 1 thread), {dt:.1f} s"}
 
 
@@ -159,6 +160,7 @@ def run_reference(args, rank, world):
     o = O.OracleState(p, SLY4)
     o.set_spinors(psi, qn)
     o.set_energies(en)
+    o.set_pairing()
     o.Start()
     if warm:
         o.Evolve(warm, DT, MOMENTUM)
@@ -172,7 +174,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": "Mg-like HO start, N=Z=28, 24^3 EV8, "
-                                        "nwt=160, SLy4, HF filling", **WORKLOAD},
+                                        "nwt=160, SLy4, HFB (G=1250, alpha=1)", **WORKLOAD},
         "cpu_baseline": {"value": val, "unit": "iter/s", "cores": 1, "kind": "port",
                          "sample": f"{steps} full iteration(s); the reference is single-threaded "
                                    "Fortran (no OpenMP) and no Fortran compiler exists here or on "
@@ -194,6 +196,7 @@ def run_ours(args, rank, world, local_rank):
         g = MeshState(p, SLY4, stream=stream.cuda_stream)
     g.set_spinors(psi, qn)
     g.set_energies(en)
+    g.set_pairing()
     g.Start()
     g.Evolve(max(3, args.warmup), DT, MOMENTUM)
     torch.cuda.synchronize()
@@ -282,8 +285,8 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f64" if args.precision == "fp64" else "f64+tf32",
         "data": "synthetic",
         "config": {"workload": "N=Z=28 HO start (seed 1234), 24^3 EV8 stored mesh, dx=0.8, "
-                               "nwt=160, SLy4, TRC; pairing step = HF filling (HFB pairing "
-                               "not yet on the GPU path)",
+                               "nwt=160, SLy4, TRC, HFB pairing G=1250 alpha=1 "
+                               "(surface delta, 5 MeV cutoff)",
                    **WORKLOAD, "precision": args.precision, "dt": DT, "momentum": MOMENTUM,
                    "l2": "working set ~0.7 GB > 129 MB L2, no flush",
                    "parallelism": f"replicas x{world}"},
@@ -325,7 +328,7 @@ def stage_breakdown(g, torch, stream):
 
     t("grad_desc(hpsi+gs)", lambda: g.GradDesc(DT, MOMENTUM))
     t("gram_schmidt", g.GramSchmidt)
-    t("hf_fill", g.HFFill)
+    t("solve_pairing", g.SolvePairing, reps=1)
     t("derive_all", g.DeriveAll)
     t("densities", g.UpdateDensities)
     t("moments", g.CalculateAllMoments)

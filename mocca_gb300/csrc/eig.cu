@@ -1,0 +1,549 @@
+// eig.cu -- batched symmetric eigensolver for the small dense HFB matrices.
+//
+// GB300 runs FP64 at ~1.75 FMA/clk/SM and long dependent FP64 chains (the
+// tridiagonal QL sweeps of a Householder/QL solver such as diagoncr8,
+// src/HFB.f90:5880-6087) at a small fraction of that, so the FP64 work is
+// arranged as batched GEMMs and the sequential part runs in FP32:
+//
+//   1. k_jacobi32: cyclic two-sided Jacobi in FP32, one CTA per matrix, the
+//      n/2 rotations of a round-robin round applied in parallel (rows, then
+//      columns and vectors), optionally warm-started from earlier vectors
+//      (B = X^T A X).  Eigenpairs sorted ascending.
+//   2. FP64 iterative refinement (Ogita & Aishima, "Iterative refinement for
+//      symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35
+//      (2018) 1007-1035):  R = I - X^T X, S = X^T A X, lambda_i = s_ii/(1-r_ii),
+//      E_ij = (s_ij + lambda_j r_ij)/(lambda_j - lambda_i) for separated
+//      pairs, r_ij/2 inside clusters (|lambda_i - lambda_j| <= delta),
+//      X <- X (I + E).  Each step is three batched FP64 GEMM launches plus one
+//      correction launch, quadratically convergent from the FP32 seed.
+//
+// The result has FP64 accuracy: eigenvalues to ~1e-15 relative, and the
+// invariant subspaces to the same level; inside an exactly degenerate
+// cluster any orthonormal basis of the cluster is returned (the HFB density
+// matrices are projector blocks and do not depend on that choice).
+#include <cmath>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTile = 16;
+
+__device__ float cta_sumf(float x, float* red) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = x;
+    __syncthreads();
+    float s = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+    __syncthreads();
+    return s;
+}
+
+__device__ double cta_sumd(double x, double* red) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = x;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+    __syncthreads();
+    return s;
+}
+
+// round-robin tournament: in round r, slot j of n (n even) holds player f(j);
+// pairs (f(i), f(n-1-i)), i < n/2, cover every pair once in n-1 rounds.
+__device__ __forceinline__ int rr_player(int j, int r, int n) {
+    return j == 0 ? 0 : 1 + (j - 1 + r) % (n - 1);
+}
+
+}  // namespace
+
+// One matrix per CTA.  A: FP64 n x n (lda) input; Xw: optional FP64 warm
+// start (n x n, ldx); X: FP64 output vectors (n x n, ldx, column k <-> w[k]);
+// w: eigenvalues ascending.  n <= 128.
+__global__ void __launch_bounds__(kThreads)
+k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __restrict__ nsz,
+           const double* __restrict__ Xw, double* __restrict__ X, long xstride, int ldx,
+           double* __restrict__ w, long wstride, int max_sweeps, int* __restrict__ flag) {
+    extern __shared__ float smf[];
+    __shared__ float red[32];
+    __shared__ float cs[2][64];
+    __shared__ int perm[128];
+    const int b = blockIdx.x;
+    const int n0 = nsz[b];
+    if (n0 == 0) return;
+    const int n = n0 + (n0 & 1);  // pad odd sizes with an isolated zero row
+    const int ld = n + 1;
+    float* a = smf;             // n x ld
+    float* v = a + n * ld;      // n x ld
+    float* t = v + n * ld;      // n x ld scratch
+    const double* Ab = A + b * astride;
+    const int tid = threadIdx.x;
+    for (int q = tid; q < n * n; q += kThreads) {
+        const int i = q / n, j = q % n;
+        a[i * ld + j] = (i < n0 && j < n0) ? (float)Ab[(long)i * lda + j] : 0.0f;
+        float vv = i == j ? 1.0f : 0.0f;
+        if (Xw && i < n0 && j < n0) vv = (float)Xw[b * xstride + (long)i * ldx + j];
+        v[i * ld + j] = vv;
+    }
+    __syncthreads();
+    if (Xw) {
+        // a <- V^T A V
+        for (int q = tid; q < n * n; q += kThreads) {
+            const int i = q / n, j = q % n;
+            float s = 0.0f;
+            for (int k = 0; k < n; ++k) s = fmaf(a[i * ld + k], v[k * ld + j], s);
+            t[i * ld + j] = s;
+        }
+        __syncthreads();
+        for (int q = tid; q < n * n; q += kThreads) {
+            const int i = q / n, j = q % n;
+            float s = 0.0f;
+            for (int k = 0; k < n; ++k) s = fmaf(v[k * ld + i], t[k * ld + j], s);
+            a[i * ld + j] = s;
+        }
+        __syncthreads();
+        // symmetrise
+        for (int q = tid; q < n * n; q += kThreads) {
+            const int i = q / n, j = q % n;
+            if (i < j) {
+                const float m = 0.5f * (a[i * ld + j] + a[j * ld + i]);
+                a[i * ld + j] = m;
+                a[j * ld + i] = m;
+            }
+        }
+        __syncthreads();
+    }
+    float part = 0.0f;
+    for (int q = tid; q < n * n; q += kThreads) part += a[(q / n) * ld + q % n] * a[(q / n) * ld + q % n];
+    const float norm2 = cta_sumf(part, red);
+    const float tol2 = 1e-11f * norm2;  // off-diagonal <= 3e-6 |A|: an FP32-level seed
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        part = 0.0f;
+        for (int q = tid; q < n * n; q += kThreads) {
+            const int i = q / n, j = q % n;
+            if (i != j) part += a[i * ld + j] * a[i * ld + j];
+        }
+        const float off = cta_sumf(part, red);
+        if (off <= tol2) break;
+        for (int r = 0; r < n - 1; ++r) {
+            if (tid < n / 2) {
+                const int p = rr_player(tid, r, n), q = rr_player(n - 1 - tid, r, n);
+                const float apq = a[p * ld + q];
+                float c = 1.0f, s = 0.0f;
+                if (fabsf(apq) > 1e-30f) {
+                    const float th = (a[q * ld + q] - a[p * ld + p]) / (2.0f * apq);
+                    const float tt = (th >= 0.0f ? 1.0f : -1.0f) / (fabsf(th) + sqrtf(th * th + 1.0f));
+                    c = rsqrtf(tt * tt + 1.0f);
+                    s = tt * c;
+                }
+                cs[0][tid] = c;
+                cs[1][tid] = s;
+            }
+            __syncthreads();
+            for (int q2 = tid; q2 < (n / 2) * n; q2 += kThreads) {
+                const int k = q2 / n, col = q2 % n;
+                const int p = rr_player(k, r, n), q = rr_player(n - 1 - k, r, n);
+                const float c = cs[0][k], s = cs[1][k];
+                const float ap = a[p * ld + col], aq = a[q * ld + col];
+                a[p * ld + col] = c * ap - s * aq;
+                a[q * ld + col] = s * ap + c * aq;
+            }
+            __syncthreads();
+            for (int q2 = tid; q2 < (n / 2) * n; q2 += kThreads) {
+                const int k = q2 / n, row = q2 % n;
+                const int p = rr_player(k, r, n), q = rr_player(n - 1 - k, r, n);
+                const float c = cs[0][k], s = cs[1][k];
+                const float ap = a[row * ld + p], aq = a[row * ld + q];
+                a[row * ld + p] = c * ap - s * aq;
+                a[row * ld + q] = s * ap + c * aq;
+                const float vp = v[row * ld + p], vq = v[row * ld + q];
+                v[row * ld + p] = c * vp - s * vq;
+                v[row * ld + q] = s * vp + c * vq;
+            }
+            __syncthreads();
+        }
+    }
+    if (sweep == max_sweeps && tid == 0 && flag) atomicExch(flag, 1);
+    // sort the n0 real eigenpairs ascending (the padding row stays last)
+    if (tid == 0) {
+        for (int i = 0; i < n0; ++i) perm[i] = i;
+        for (int i = 1; i < n0; ++i) {
+            const int pi = perm[i];
+            const float di = a[pi * ld + pi];
+            int j = i;
+            while (j > 0 && a[perm[j - 1] * ld + perm[j - 1]] > di) {
+                perm[j] = perm[j - 1];
+                --j;
+            }
+            perm[j] = pi;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < n0 * n0; q += kThreads) {
+        const int i = q / n0, k = q % n0;
+        X[b * xstride + (long)i * ldx + k] = (double)v[i * ld + perm[k]];
+    }
+    for (int k = tid; k < n0; k += kThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
+}
+
+// Batched FP64 GEMM, C = alpha op(A) op(B) + beta C, m,n,k <= 128, row-major.
+__global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict__ descs) {
+    __shared__ double sA[kTile][129];
+    __shared__ double sB[129][kTile + 1];
+    const GemmDesc g = descs[blockIdx.y];
+    const int tiles_n = (g.n + kTile - 1) / kTile;
+    const int ti = blockIdx.x / tiles_n, tj = blockIdx.x % tiles_n;
+    if (ti * kTile >= g.m) return;
+    const int r = threadIdx.x / kTile, cidx = threadIdx.x % kTile;
+    for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
+        const int i = q / g.k, kk = q % g.k;
+        const int gi = ti * kTile + i;
+        double x = 0.0;
+        if (gi < g.m) x = g.ta ? g.A[(long)kk * g.lda + gi] : g.A[(long)gi * g.lda + kk];
+        sA[i][kk] = x;
+    }
+    for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
+        const int kk = q / kTile, j = q % kTile;
+        const int gj = tj * kTile + j;
+        double x = 0.0;
+        if (gj < g.n) x = g.tb ? g.B[(long)gj * g.ldb + kk] : g.B[(long)kk * g.ldb + gj];
+        sB[kk][j] = x;
+    }
+    __syncthreads();
+    const int gi = ti * kTile + r, gj = tj * kTile + cidx;
+    if (gi >= g.m || gj >= g.n) return;
+    double s = 0.0;
+    for (int kk = 0; kk < g.k; ++kk) s = fma(sA[r][kk], sB[kk][cidx], s);
+    double* c = g.C + (long)gi * g.ldc + gj;
+    *c = g.beta == 0.0 ? g.alpha * s : fma(g.alpha, s, g.beta * *c);
+}
+
+// Ogita-Aishima correction for one matrix per CTA: from S = X^T A X and
+// G = X^T X form lambda, delta and F = I + E (written over G).
+__global__ void __launch_bounds__(kThreads)
+k_oa_correct(const double* __restrict__ S, double* __restrict__ G, long stride, int ld,
+             const int* __restrict__ nsz, const double* __restrict__ anorm,
+             double* __restrict__ w, long wstride) {
+    __shared__ double red[32];
+    __shared__ double lam[128];
+    const int b = blockIdx.x;
+    const int n = nsz[b];
+    if (n == 0) return;
+    const double* Sb = S + b * stride;
+    double* Gb = G + b * stride;
+    for (int i = threadIdx.x; i < n; i += kThreads) lam[i] = Sb[(long)i * ld + i] / Gb[(long)i * ld + i];
+    __syncthreads();
+    double ps = 0.0, pr = 0.0;
+    for (int q = threadIdx.x; q < n * n; q += kThreads) {
+        const int i = q / n, j = q % n;
+        const double sd = Sb[(long)i * ld + j] - (i == j ? lam[i] : 0.0);
+        const double rd = (i == j ? 1.0 : 0.0) - Gb[(long)i * ld + j];
+        ps += sd * sd;
+        pr += rd * rd;
+    }
+    const double ns = sqrt(cta_sumd(ps, red));
+    const double nr = sqrt(cta_sumd(pr, red));
+    const double delta = 2.0 * (ns + anorm[b] * nr);
+    for (int q = threadIdx.x; q < n * n; q += kThreads) {
+        const int i = q / n, j = q % n;
+        const double r = (i == j ? 1.0 : 0.0) - Gb[(long)i * ld + j];
+        double e;
+        if (i == j) {
+            e = 0.5 * r;
+        } else if (fabs(lam[j] - lam[i]) > delta) {
+            e = (Sb[(long)i * ld + j] + lam[j] * r) / (lam[j] - lam[i]);
+        } else {
+            e = 0.5 * r;
+        }
+        // read of G(i,j) happens before the write of F(i,j) by the same thread
+        Gb[(long)i * ld + j] = (i == j ? 1.0 : 0.0) + e;
+    }
+    for (int i = threadIdx.x; i < n; i += kThreads) w[b * wstride + i] = lam[i];
+}
+
+// FP64 Jacobi polish of S = X^T A X after refinement: S is diagonal up to
+// rounding outside clusters of (near-)degenerate eigenvalues, so only the
+// pairs with |s_pq| above the rounding level rotate.  Q accumulates the
+// rotations (X <- X Q afterwards) and w receives diag(S).  Needed where the
+// individual vectors inside a cluster matter (the canonical basis: the
+// occupation-weighted density sum is not invariant under rotations between
+// states of slightly different occupation).
+__global__ void __launch_bounds__(kThreads)
+k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* __restrict__ nsz,
+                  const double* __restrict__ anorm, double* __restrict__ Q,
+                  double* __restrict__ w, long wstride, int* __restrict__ flag) {
+    extern __shared__ double smd[];
+    __shared__ double red[32];
+    __shared__ double cs[2][64];
+    __shared__ int act[64];
+    const int b = blockIdx.x;
+    const int n0 = nsz[b];
+    if (n0 == 0) return;
+    const int n = n0 + (n0 & 1);
+    const int l2 = n + 1;
+    double* a = smd;
+    // Q accumulates in the output buffer (global, L1/L2 resident): row r, col c
+    double* q = Q + b * stride;
+    auto Qa = [&](int r, int c) -> double& { return q[(long)r * ld + c]; };
+    const int tid = threadIdx.x;
+    for (int t = tid; t < n * n; t += kThreads) {
+        const int i = t / n, j = t % n;
+        const double x = (i < n0 && j < n0) ? S[b * stride + (long)i * ld + j] : 0.0;
+        const double y = (i < n0 && j < n0) ? S[b * stride + (long)j * ld + i] : 0.0;
+        a[i * l2 + j] = i == j ? x : 0.5 * (x + y);
+    }
+    for (int t = tid; t < n0 * n0; t += kThreads) Qa(t / n0, t % n0) = (t / n0 == t % n0) ? 1.0 : 0.0;
+    __syncthreads();
+    const double thr = 1e-15 * anorm[b];
+    int sweep = 0;
+    for (; sweep < 12; ++sweep) {
+        double part = 0.0;
+        for (int t = tid; t < n * n; t += kThreads) {
+            const int i = t / n, j = t % n;
+            if (i != j && fabs(a[i * l2 + j]) > thr) part += 1.0;
+        }
+        if (cta_sumd(part, red) == 0.0) break;
+        for (int r = 0; r < n - 1; ++r) {
+            if (tid < n / 2) {
+                const int p = rr_player(tid, r, n), qq = rr_player(n - 1 - tid, r, n);
+                const double apq = a[p * l2 + qq];
+                int on = 0;
+                double c = 1.0, s = 0.0;
+                if (fabs(apq) > thr) {
+                    const double th = (a[qq * l2 + qq] - a[p * l2 + p]) / (2.0 * apq);
+                    const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                    c = 1.0 / sqrt(tt * tt + 1.0);
+                    s = tt * c;
+                    on = 1;
+                }
+                cs[0][tid] = c;
+                cs[1][tid] = s;
+                act[tid] = on;
+            }
+            __syncthreads();
+            for (int t = tid; t < (n / 2) * n; t += kThreads) {
+                const int k = t / n, col = t % n;
+                if (!act[k]) continue;
+                const int p = rr_player(k, r, n), qq = rr_player(n - 1 - k, r, n);
+                const double c = cs[0][k], s = cs[1][k];
+                const double ap = a[p * l2 + col], aq = a[qq * l2 + col];
+                a[p * l2 + col] = c * ap - s * aq;
+                a[qq * l2 + col] = s * ap + c * aq;
+            }
+            __syncthreads();
+            for (int t = tid; t < (n / 2) * n; t += kThreads) {
+                const int k = t / n, row = t % n;
+                if (!act[k]) continue;
+                const int p = rr_player(k, r, n), qq = rr_player(n - 1 - k, r, n);
+                const double c = cs[0][k], s = cs[1][k];
+                const double ap = a[row * l2 + p], aq = a[row * l2 + qq];
+                a[row * l2 + p] = c * ap - s * aq;
+                a[row * l2 + qq] = s * ap + c * aq;
+                if (row < n0 && p < n0 && qq < n0) {
+                    const double vp = Qa(row, p), vq = Qa(row, qq);
+                    Qa(row, p) = c * vp - s * vq;
+                    Qa(row, qq) = s * vp + c * vq;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (sweep == 12 && tid == 0 && flag) atomicExch(flag, 1);
+    for (int i = tid; i < n0; i += kThreads) w[b * wstride + i] = a[i * l2 + i];
+}
+
+// Re-orthonormalisation X <- X (I + R/2 + 3/8 R^2), R = I - X^T X (third-order
+// accurate): from G = X^T X write R into Rm and I + R/2 into F.
+__global__ void k_orth_prep(const double* __restrict__ G, double* __restrict__ Rm,
+                            double* __restrict__ F, long stride, int ld,
+                            const int* __restrict__ nsz) {
+    const int b = blockIdx.y, n = nsz[b];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int i = t / n, j = t % n;
+    const long o = b * stride + (long)i * ld + j;
+    const double r = (i == j ? 1.0 : 0.0) - G[o];
+    Rm[o] = r;
+    F[o] = (i == j ? 1.0 : 0.0) + 0.5 * r;
+}
+
+// Frobenius norms of the batch matrices (delta of the refinement uses ||A||).
+__global__ void k_frob(const double* __restrict__ A, long stride, int ld, const int* __restrict__ nsz,
+                       double* __restrict__ out) {
+    __shared__ double red[32];
+    const int b = blockIdx.x, n = nsz[b];
+    double p = 0.0;
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+        const double x = A[b * stride + (long)(q / n) * ld + q % n];
+        p += x * x;
+    }
+    const double s = cta_sumd(p, red);
+    if (threadIdx.x == 0) out[b] = sqrt(s);
+}
+
+size_t jacobi_smem(int n) {
+    const int np = n + (n & 1);
+    return (size_t)3 * np * (np + 1) * sizeof(float);
+}
+
+// Eigen-decomposition of a batch (nb <= 8) of symmetric matrices of sizes
+// nsz (device) <= nmax, stored with leading dimension ld and stride `stride`.
+// X (in/out: warm start when warm != 0), w: eigenvalues, ws: workspace of
+// 4 * nb * stride doubles; descs: GemmDesc workspace (3 * nb entries).
+int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish) {
+    if (!E.attr_done) {
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        E.attr_done = true;
+    }
+    const size_t sm = jacobi_smem(E.nmax);
+    k_jacobi32<<<E.nb, kThreads, sm, c->stream>>>(E.A, E.stride, E.ld, E.nsz, warm ? E.X : nullptr,
+                                                  E.X, E.stride, E.ld, E.w, E.wstride,
+                                                  warm ? 12 : 30, c->flags + 4);
+    MG_LAUNCHED(c);
+    k_frob<<<E.nb, 128, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
+    MG_LAUNCHED(c);
+    const int tiles = div_up(E.nmax, kTile) * div_up(E.nmax, kTile);
+    for (int s = 0; s < nref; ++s) {
+        // AX = A X ; S = X^T AX ; G = X^T X ; F = I + E ; X2 = X F ; X <- X2
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax);
+        MG_LAUNCHED(c);
+        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+        MG_LAUNCHED(c);
+        k_oa_correct<<<E.nb, kThreads, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz, E.anorm,
+                                                       E.w, E.wstride);
+        MG_LAUNCHED(c);
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
+    }
+    // re-orthonormalise: G = X^T X, F = I + R/2 + 3/8 R^2, X <- X F
+    k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+    MG_LAUNCHED(c);
+    k_orth_prep<<<dim3(div_up((long)E.nmax * E.nmax, kThreads), E.nb), kThreads, 0, c->stream>>>(
+        E.G, E.AX, E.G, E.stride, E.ld, E.nsz);
+    MG_LAUNCHED(c);
+    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_rr);
+    MG_LAUNCHED(c);
+    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+    MG_LAUNCHED(c);
+    MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                            cudaMemcpyDeviceToDevice, c->stream));
+    if (polish) {
+        const int np = E.nmax + (E.nmax & 1);
+        const size_t psm = (size_t)np * (np + 1) * sizeof(double);
+        if (psm > 200 * 1024) return MG_ERR_ARG;
+        // Rayleigh-Ritz matrix and the FP64 Jacobi polish
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax);
+        MG_LAUNCHED(c);
+        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+        MG_LAUNCHED(c);
+        k_jacobi64_polish<<<E.nb, kThreads, psm, c->stream>>>(
+            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, c->flags + 5);
+        MG_LAUNCHED(c);
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return MG_OK;
+}
+
+// Workspace and GEMM descriptor tables for a batch.
+int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, double* A, long stride,
+              int ld) {
+    E.nb = nb;
+    E.nmax = nmax;
+    E.nsz = nsz_dev;
+    E.A = A;
+    E.stride = stride;
+    E.ld = ld;
+    E.wstride = nmax;
+    const size_t bytes = (size_t)nb * stride * sizeof(double);
+    MG_CUDA(cudaMalloc(&E.X, bytes));
+    MG_CUDA(cudaMemset(E.X, 0, bytes));
+    MG_CUDA(cudaMalloc(&E.X2, bytes));
+    MG_CUDA(cudaMalloc(&E.AX, bytes));
+    MG_CUDA(cudaMalloc(&E.S, bytes));
+    MG_CUDA(cudaMalloc(&E.G, bytes));
+    MG_CUDA(cudaMalloc(&E.w, (size_t)nb * nmax * sizeof(double)));
+    MG_CUDA(cudaMalloc(&E.anorm, (size_t)nb * sizeof(double)));
+    std::vector<int> hn(nb);
+    MG_CUDA(cudaMemcpy(hn.data(), nsz_dev, nb * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<GemmDesc> ax(nb), sg(2 * nb), xf(nb), rr(nb);
+    for (int b = 0; b < nb; ++b) {
+        const int n = hn[b];
+        const long o = (long)b * stride;
+        ax[b] = GemmDesc{A + o, E.X + o, E.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
+        sg[2 * b] = GemmDesc{E.X + o, E.AX + o, E.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
+        sg[2 * b + 1] = GemmDesc{E.X + o, E.X + o, E.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
+        xf[b] = GemmDesc{E.X + o, E.G + o, E.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
+        rr[b] = GemmDesc{E.AX + o, E.AX + o, E.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0};
+    }
+    MG_CUDA(cudaMalloc(&E.d_ax, nb * sizeof(GemmDesc)));
+    MG_CUDA(cudaMalloc(&E.d_sg, 2 * nb * sizeof(GemmDesc)));
+    MG_CUDA(cudaMalloc(&E.d_xf, nb * sizeof(GemmDesc)));
+    MG_CUDA(cudaMalloc(&E.d_rr, nb * sizeof(GemmDesc)));
+    MG_CUDA(cudaMemcpy(E.d_ax, ax.data(), nb * sizeof(GemmDesc), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(E.d_sg, sg.data(), 2 * nb * sizeof(GemmDesc), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(E.d_xf, xf.data(), nb * sizeof(GemmDesc), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(E.d_rr, rr.data(), nb * sizeof(GemmDesc), cudaMemcpyHostToDevice));
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" int mg_eigh_batched(int nb, const int* n, int ld, const double* a, double* w,
+                               double* z) {
+    using namespace mg;
+    if (nb <= 0 || nb > 64 || !n || !a || !w || !z || ld <= 0 || ld > 128) return MG_ERR_ARG;
+    for (int b = 0; b < nb; ++b)
+        if (n[b] < 0 || n[b] > ld) return MG_ERR_ARG;
+    mg_ctx tmp;  // a throw-away context carrying only the stream, flags and counters
+    MG_CUDA(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+    MG_CUDA(cudaMalloc(&tmp.flags, 16 * sizeof(int)));
+    MG_CUDA(cudaMemset(tmp.flags, 0, 16 * sizeof(int)));
+    const long stride = (long)ld * ld;
+    double* dA = nullptr;
+    int* dn = nullptr;
+    MG_CUDA(cudaMalloc(&dA, nb * stride * sizeof(double)));
+    MG_CUDA(cudaMalloc(&dn, nb * sizeof(int)));
+    MG_CUDA(cudaMemcpy(dA, a, nb * stride * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(dn, n, nb * sizeof(int), cudaMemcpyHostToDevice));
+    EigBatch E;
+    int st = eig_setup(&tmp, E, nb, ld, dn, dA, stride, ld);
+    if (st == MG_OK) st = eig_batched(&tmp, E, false, 3, true);
+    if (st == MG_OK) {
+        MG_CUDA(cudaStreamSynchronize(tmp.stream));
+        MG_CUDA(cudaMemcpy(w, E.w, nb * (size_t)ld * sizeof(double), cudaMemcpyDeviceToHost));
+        MG_CUDA(cudaMemcpy(z, E.X, nb * stride * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    eig_free(E);
+    cudaFree(dA);
+    cudaFree(dn);
+    cudaFree(tmp.flags);
+    tmp.flags = nullptr;
+    cudaStreamDestroy(tmp.stream);
+    tmp.stream = nullptr;
+    return st;
+}
+
+namespace mg {
+
+void eig_free(EigBatch& E) {
+    for (void* p : {(void*)E.X, (void*)E.X2, (void*)E.AX, (void*)E.S, (void*)E.G, (void*)E.w,
+                    (void*)E.anorm, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
+                    (void*)E.d_rr})
+        if (p) cudaFree(p);
+}
+
+}  // namespace mg

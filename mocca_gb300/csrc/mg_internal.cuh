@@ -65,6 +65,30 @@ struct Basis {
     bool have_qn = false;
 };
 
+// One FP64 GEMM of a batch: C = alpha op(A) op(B) + beta C (row-major).
+struct GemmDesc {
+    const double* A;
+    const double* B;
+    double* C;
+    int m, n, k;
+    int lda, ldb, ldc;
+    int ta, tb;
+    double alpha, beta;
+};
+
+// A batch of small symmetric eigenproblems (eig.cu).
+struct EigBatch {
+    int nb = 0, nmax = 0, ld = 0;
+    long stride = 0, wstride = 0;
+    const int* nsz = nullptr;
+    double* A = nullptr;
+    double *X = nullptr, *X2 = nullptr, *AX = nullptr, *S = nullptr, *G = nullptr, *w = nullptr,
+           *anorm = nullptr;
+    GemmDesc *d_ax = nullptr, *d_sg = nullptr, *d_xf = nullptr, *d_rr = nullptr;
+    bool attr_done = false;
+    bool have_vectors = false;
+};
+
 struct PairCoef {
     double cut[2];
     double mu[2];
@@ -98,6 +122,11 @@ struct Hfb {
     double slope[2] = {0.0, 0.0};              // dN/dlambda from the last solve
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
+    double* T = nullptr;      // 4 block HFB matrices (signature-reduced), nmax x nmax
+    double* Rpp = nullptr;    // 4 blocks of rho_++, hmax x hmax
+    int* nsz_T = nullptr;     // N per block
+    EigBatch eT, eR;          // eigensolver batches for T and rho_++
+    int nref = 2;             // FP64 refinement steps per eigen-decomposition
 };
 
 }  // namespace mg
@@ -185,6 +214,10 @@ int basis_dots(mg_ctx* c, const double* a, const double* b, double* out);
 int pairing_mesh(mg_ctx* c);
 int canonical_transform(mg_ctx* c);
 int pairing_set_smem(mg_ctx* c);
+int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, double* A,
+              long stride, int ld);
+int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish);
+void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
 void hfb_free(mg_ctx* c);
