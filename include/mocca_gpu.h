@@ -157,6 +157,22 @@ int mg_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2);
  * refinement, FP64 Jacobi polish inside clusters). */
 int mg_eigh_batched(int nb, const int* n, int ld, const double* a, double* w, double* z);
 
+/* mg_eigh_batched for callers that must not allocate device memory (hosts
+ * that own every byte through their own pool, code running while a stream is
+ * captured).  No reference counterpart: the Fortran code has no device.
+ * n: host array; a, w, z: DEVICE buffers laid out as for mg_eigh_batched;
+ * stream: a cudaStream_t (NULL: the legacy default stream).  Work is only
+ * enqueued on `stream`; the caller synchronises before reading w and z.
+ * The workspace is one static device array of ~2 MiB per device, so the
+ * limits are nb <= 64, ld <= 128 and nb*ld*ld <= 65536 (MG_ERR_ARG with a
+ * message on stderr beyond that).  z outside each leading n x n block is set
+ * to zero, w beyond n[b] is not written.  The first call on a device (that
+ * device current) looks up the workspace and loads the kernels; make it
+ * before any stream capture.  Calls share the workspace: two calls that can
+ * overlap on one device (different streams, host threads) race. */
+int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const double* a, double* w,
+                            double* z, void* stream);
+
 /* ---- context --------------------------------------------------------------- */
 
 /* Allocates every device buffer of the hot path (spinors of both bases and

@@ -162,6 +162,7 @@ SIGNATURES = {
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
     "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
     "mg_eigh_batched": [C.c_int, _I, C.c_int, _D, _D, _D],
+    "mg_eigh_batched_noalloc": [C.c_int, _I, C.c_int, _P, _P, _P, _P],
     "mg_set_pairing": [_P, C.POINTER(MgPairingParams)],
     "mg_solve_pairing": [_P, C.POINTER(MgPairingInfo)],
     "mg_get_hfb_block": [_P, C.c_int, _D, _D, _D],

@@ -22,6 +22,7 @@
 // cluster any orthonormal basis of the cluster is returned (the HFB density
 // matrices are projector blocks and do not depend on that choice).
 #include <cmath>
+#include <mutex>
 
 #include "mg_internal.cuh"
 
@@ -533,6 +534,162 @@ extern "C" int mg_eigh_batched(int nb, const int* n, int ld, const double* a, do
     cudaFree(tmp.flags);
     tmp.flags = nullptr;
     cudaStreamDestroy(tmp.stream);
+    tmp.stream = nullptr;
+    return st;
+}
+
+// ---- allocation-free variant ---------------------------------------------------------
+//
+// Hosts that own all device memory through their own pool, and code that runs
+// while a stream is being captured (where cudaMalloc is not allowed), cannot
+// let the solver allocate.  mg_eigh_batched_noalloc takes device buffers from
+// the caller and keeps its workspace in one file-scope device array, so a call
+// only launches kernels and stream-ordered memsets/copies.
+
+namespace mg {
+namespace {
+
+constexpr long kNoAllocElems = 65536;   // nb * ld * ld capacity (512 KB per work matrix)
+constexpr int kNoAllocNb = 64;
+constexpr int kNoAllocLd = 128;
+constexpr int kNoAllocMaxDevices = 64;
+
+constexpr size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kMatBytes = (size_t)kNoAllocElems * sizeof(double);
+constexpr size_t kOffX2 = 0, kOffAX = kMatBytes, kOffS = 2 * kMatBytes, kOffG = 3 * kMatBytes;
+constexpr size_t kOffNorm = 4 * kMatBytes;
+constexpr size_t kOffDesc = kOffNorm + round256(kNoAllocNb * sizeof(double));
+constexpr size_t kDescBytes = round256(5 * kNoAllocNb * sizeof(GemmDesc));
+constexpr size_t kOffNsz = kOffDesc + kDescBytes;
+constexpr size_t kOffFlags = kOffNsz + round256(kNoAllocNb * sizeof(int));
+constexpr size_t kNoAllocBytes = kOffFlags + 256;   // ~2.03 MiB
+
+// The whole workspace: four nb x ld x ld work matrices, norms, GEMM tables,
+// sizes, flags.
+static __device__ __align__(256) unsigned char g_eig_scratch[kNoAllocBytes];
+
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char* base = nullptr;
+};
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+struct NoAllocArgs {
+    int n[kNoAllocNb];
+    int nb, ld;
+    const double* A;
+    double *X, *X2, *AX, *S, *G;
+};
+
+// Same tables as eig_setup builds on the host, written by the device so that
+// a call uploads nothing from host memory.
+__global__ void k_eig_noalloc_tables(NoAllocArgs a, int* nsz, GemmDesc* ax, GemmDesc* sg,
+                                     GemmDesc* xf, GemmDesc* rr) {
+    const int b = threadIdx.x;
+    if (b >= a.nb) return;
+    const int n = a.n[b], ld = a.ld;
+    const long o = (long)b * ld * ld;
+    nsz[b] = n;
+    ax[b] = GemmDesc{a.A + o, a.X + o, a.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
+    sg[2 * b] = GemmDesc{a.X + o, a.AX + o, a.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
+    sg[2 * b + 1] = GemmDesc{a.X + o, a.X + o, a.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
+    xf[b] = GemmDesc{a.X + o, a.G + o, a.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
+    rr[b] = GemmDesc{a.AX + o, a.AX + o, a.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0};
+}
+
+// Once per device, with that device current: the scratch address, the
+// shared-memory opt-ins, and a query of every kernel the call launches so
+// that they are loaded before the first real call.
+int noalloc_setup(int dev, unsigned char** base) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void* p = nullptr;
+        MG_CUDA(cudaGetSymbolAddress(&p, g_eig_scratch));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        cudaFuncAttributes fa;
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_gemm64));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_correct));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_orth_prep));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_frob));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_eig_noalloc_tables));
+        d.base = static_cast<unsigned char*>(p);
+        d.ready = true;
+    }
+    *base = d.base;
+    return MG_OK;
+}
+
+}  // namespace
+}  // namespace mg
+
+extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const double* a, double* w,
+                                       double* z, void* stream) {
+    using namespace mg;
+    if (nb <= 0 || !n || !a || !w || !z || ld <= 0) return MG_ERR_ARG;
+    if (nb > kNoAllocNb || ld > kNoAllocLd || (long)nb * ld * ld > kNoAllocElems) {
+        fprintf(stderr,
+                "mocca_gpu: mg_eigh_batched_noalloc: nb=%d ld=%d exceeds the static workspace "
+                "(nb <= %d, ld <= %d, nb*ld*ld <= %ld)\n",
+                nb, ld, kNoAllocNb, kNoAllocLd, kNoAllocElems);
+        return MG_ERR_ARG;
+    }
+    for (int b = 0; b < nb; ++b)
+        if (n[b] < 0 || n[b] > ld) return MG_ERR_ARG;
+    int dev = 0;
+    MG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return MG_ERR_ARG;
+    unsigned char* base = nullptr;
+    MG_TRY(noalloc_setup(dev, &base));
+
+    mg_ctx tmp;   // carries the caller's stream, the scratch flags and the launch counter
+    tmp.stream = static_cast<cudaStream_t>(stream);
+    tmp.flags = reinterpret_cast<int*>(base + kOffFlags);
+    EigBatch E;
+    E.nb = nb;
+    E.nmax = ld;
+    E.ld = ld;
+    E.stride = (long)ld * ld;
+    E.wstride = ld;
+    E.nsz = reinterpret_cast<int*>(base + kOffNsz);
+    E.A = const_cast<double*>(a);   // read only
+    E.X = z;
+    E.w = w;
+    E.X2 = reinterpret_cast<double*>(base + kOffX2);
+    E.AX = reinterpret_cast<double*>(base + kOffAX);
+    E.S = reinterpret_cast<double*>(base + kOffS);
+    E.G = reinterpret_cast<double*>(base + kOffG);
+    E.anorm = reinterpret_cast<double*>(base + kOffNorm);
+    GemmDesc* desc = reinterpret_cast<GemmDesc*>(base + kOffDesc);
+    E.d_ax = desc;
+    E.d_sg = desc + nb;
+    E.d_xf = desc + 3 * nb;
+    E.d_rr = desc + 4 * nb;
+    E.attr_done = true;
+
+    // Must start at zero on every call: the flags, and X2, whose padding
+    // (outside each leading n x n block) is copied into z.
+    MG_CUDA(cudaMemsetAsync(tmp.flags, 0, 256, tmp.stream));
+    MG_CUDA(cudaMemsetAsync(E.X2, 0, (size_t)nb * E.stride * sizeof(double), tmp.stream));
+    NoAllocArgs args{};
+    for (int b = 0; b < nb; ++b) args.n[b] = n[b];
+    args.nb = nb;
+    args.ld = ld;
+    args.A = a;
+    args.X = E.X;
+    args.X2 = E.X2;
+    args.AX = E.AX;
+    args.S = E.S;
+    args.G = E.G;
+    k_eig_noalloc_tables<<<1, kNoAllocNb, 0, tmp.stream>>>(args, const_cast<int*>(E.nsz), E.d_ax,
+                                                          E.d_sg, E.d_xf, E.d_rr);
+    MG_CUDA(cudaGetLastError());
+    const int st = eig_batched(&tmp, E, false, 3, true);
+    tmp.flags = nullptr;
     tmp.stream = nullptr;
     return st;
 }
