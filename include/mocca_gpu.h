@@ -163,7 +163,7 @@ int mg_eigh_batched(int nb, const int* n, int ld, const double* a, double* w, do
  * n: host array; a, w, z: DEVICE buffers laid out as for mg_eigh_batched;
  * stream: a cudaStream_t (NULL: the legacy default stream).  Work is only
  * enqueued on `stream`; the caller synchronises before reading w and z.
- * The workspace is one static device array of ~2 MiB per device, so the
+ * The workspace is one static device array of ~2.2 MiB per device, so the
  * limits are nb <= 64, ld <= 128 and nb*ld*ld <= 65536 (MG_ERR_ARG with a
  * message on stderr beyond that).  z outside each leading n x n block is set
  * to zero, w beyond n[b] is not written.  The first call on a device (that

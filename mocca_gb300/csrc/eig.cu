@@ -73,6 +73,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     extern __shared__ float smf[];
     __shared__ float red[32];
     __shared__ float cs[2][64];
+    __shared__ int pq[2][64];
     __shared__ int perm[128];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
@@ -119,21 +120,24 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         }
         __syncthreads();
     }
+    // thread (lane, kg): column / row `lane`, every second rotation pair from kg
+    const int lane = tid & 127, kg = tid >> 7;
+    const int half = n / 2;
     float part = 0.0f;
-    for (int q = tid; q < n * n; q += kThreads) part += a[(q / n) * ld + q % n] * a[(q / n) * ld + q % n];
+    if (lane < n)
+        for (int i = kg; i < n; i += 2) part += a[i * ld + lane] * a[i * ld + lane];
     const float norm2 = cta_sumf(part, red);
     const float tol2 = 1e-11f * norm2;  // off-diagonal <= 3e-6 |A|: an FP32-level seed
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         part = 0.0f;
-        for (int q = tid; q < n * n; q += kThreads) {
-            const int i = q / n, j = q % n;
-            if (i != j) part += a[i * ld + j] * a[i * ld + j];
-        }
+        if (lane < n)
+            for (int i = kg; i < n; i += 2)
+                if (i != lane) part += a[i * ld + lane] * a[i * ld + lane];
         const float off = cta_sumf(part, red);
         if (off <= tol2) break;
         for (int r = 0; r < n - 1; ++r) {
-            if (tid < n / 2) {
+            if (tid < half) {
                 const int p = rr_player(tid, r, n), q = rr_player(n - 1 - tid, r, n);
                 const float apq = a[p * ld + q];
                 float c = 1.0f, s = 0.0f;
@@ -145,51 +149,52 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
                 }
                 cs[0][tid] = c;
                 cs[1][tid] = s;
+                pq[0][tid] = p;
+                pq[1][tid] = q;
             }
             __syncthreads();
-            for (int q2 = tid; q2 < (n / 2) * n; q2 += kThreads) {
-                const int k = q2 / n, col = q2 % n;
-                const int p = rr_player(k, r, n), q = rr_player(n - 1 - k, r, n);
-                const float c = cs[0][k], s = cs[1][k];
-                const float ap = a[p * ld + col], aq = a[q * ld + col];
-                a[p * ld + col] = c * ap - s * aq;
-                a[q * ld + col] = s * ap + c * aq;
-            }
+            if (lane < n)
+                for (int k = kg; k < half; k += 2) {
+                    const int p = pq[0][k], q = pq[1][k];
+                    const float c = cs[0][k], s = cs[1][k];
+                    const float ap = a[p * ld + lane], aq = a[q * ld + lane];
+                    a[p * ld + lane] = c * ap - s * aq;
+                    a[q * ld + lane] = s * ap + c * aq;
+                }
             __syncthreads();
-            for (int q2 = tid; q2 < (n / 2) * n; q2 += kThreads) {
-                const int k = q2 / n, row = q2 % n;
-                const int p = rr_player(k, r, n), q = rr_player(n - 1 - k, r, n);
-                const float c = cs[0][k], s = cs[1][k];
-                const float ap = a[row * ld + p], aq = a[row * ld + q];
-                a[row * ld + p] = c * ap - s * aq;
-                a[row * ld + q] = s * ap + c * aq;
-                const float vp = v[row * ld + p], vq = v[row * ld + q];
-                v[row * ld + p] = c * vp - s * vq;
-                v[row * ld + q] = s * vp + c * vq;
-            }
+            if (lane < n)
+                for (int k = kg; k < half; k += 2) {
+                    const int p = pq[0][k], q = pq[1][k];
+                    const float c = cs[0][k], s = cs[1][k];
+                    const float ap = a[lane * ld + p], aq = a[lane * ld + q];
+                    a[lane * ld + p] = c * ap - s * aq;
+                    a[lane * ld + q] = s * ap + c * aq;
+                    const float vp = v[lane * ld + p], vq = v[lane * ld + q];
+                    v[lane * ld + p] = c * vp - s * vq;
+                    v[lane * ld + q] = s * vp + c * vq;
+                }
             __syncthreads();
         }
     }
     if (sweep == max_sweeps && tid == 0 && flag) atomicExch(flag, 1);
-    // sort the n0 real eigenpairs ascending (the padding row stays last)
-    if (tid == 0) {
-        for (int i = 0; i < n0; ++i) perm[i] = i;
-        for (int i = 1; i < n0; ++i) {
-            const int pi = perm[i];
-            const float di = a[pi * ld + pi];
-            int j = i;
-            while (j > 0 && a[perm[j - 1] * ld + perm[j - 1]] > di) {
-                perm[j] = perm[j - 1];
-                --j;
-            }
-            perm[j] = pi;
+    // sort the n0 real eigenpairs ascending, ties by index (the padding row
+    // stays last): rank of each diagonal entry; perm starts as the identity
+    // so that it stays a valid index table whatever the values
+    for (int i = tid; i < n0; i += kThreads) perm[i] = i;
+    __syncthreads();
+    for (int i = tid; i < n0; i += kThreads) {
+        const float di = a[i * ld + i];
+        int rank = 0;
+        for (int j = 0; j < n0; ++j) {
+            const float dj = a[j * ld + j];
+            rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
         }
+        if (rank < n0) perm[rank] = i;
     }
     __syncthreads();
-    for (int q = tid; q < n0 * n0; q += kThreads) {
-        const int i = q / n0, k = q % n0;
-        X[b * xstride + (long)i * ldx + k] = (double)v[i * ld + perm[k]];
-    }
+    if (lane < n0)
+        for (int i = kg; i < n0; i += 2)
+            X[b * xstride + (long)i * ldx + lane] = (double)v[i * ld + perm[lane]];
     for (int k = tid; k < n0; k += kThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
 }
 
@@ -225,47 +230,84 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
     *c = g.beta == 0.0 ? g.alpha * s : fma(g.alpha, s, g.beta * *c);
 }
 
-// Ogita-Aishima correction for one matrix per CTA: from S = X^T A X and
-// G = X^T X form lambda, delta and F = I + E (written over G).
-__global__ void __launch_bounds__(kThreads)
-k_oa_correct(const double* __restrict__ S, double* __restrict__ G, long stride, int ld,
-             const int* __restrict__ nsz, const double* __restrict__ anorm,
-             double* __restrict__ w, long wstride) {
+// Ogita-Aishima correction, spread over one CTA per matrix row so that the
+// FP64 work (divisions included) runs on many SMs.  k_oa_rows: lambda_i =
+// s_ii / g_ii (into w) and the row sums of (S - diag lambda)^2 and
+// (I - G)^2; k_oa_apply: delta from those sums (every CTA of a matrix adds
+// them in the same order), then row i of F = I + E written over row i of G,
+// and emax(i) = max |S_ij| / |A| over the pairs whose eigenvalue estimates
+// have opposite signs: how far the vectors still are from splitting the
+// space into its positive and negative parts (the refinement leaves pairs
+// inside a cluster |lambda_i - lambda_j| <= delta unrotated, so a start too
+// far away shows here and not in E).
+__global__ void __launch_bounds__(128)
+k_oa_rows(const double* __restrict__ S, const double* __restrict__ G, long stride, int ld,
+          const int* __restrict__ nsz, double* __restrict__ w, long wstride,
+          double* __restrict__ part) {
     __shared__ double red[32];
-    __shared__ double lam[128];
-    const int b = blockIdx.x;
-    const int n = nsz[b];
-    if (n == 0) return;
-    const double* Sb = S + b * stride;
-    double* Gb = G + b * stride;
-    for (int i = threadIdx.x; i < n; i += kThreads) lam[i] = Sb[(long)i * ld + i] / Gb[(long)i * ld + i];
-    __syncthreads();
+    const int b = blockIdx.y, i = blockIdx.x, n = nsz[b];
+    if (i >= n) return;
+    const double* Sr = S + b * stride + (long)i * ld;
+    const double* Gr = G + b * stride + (long)i * ld;
+    const double lam = Sr[i] / Gr[i];
     double ps = 0.0, pr = 0.0;
-    for (int q = threadIdx.x; q < n * n; q += kThreads) {
-        const int i = q / n, j = q % n;
-        const double sd = Sb[(long)i * ld + j] - (i == j ? lam[i] : 0.0);
-        const double rd = (i == j ? 1.0 : 0.0) - Gb[(long)i * ld + j];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double sd = Sr[j] - (j == i ? lam : 0.0);
+        const double rd = (j == i ? 1.0 : 0.0) - Gr[j];
         ps += sd * sd;
         pr += rd * rd;
     }
-    const double ns = sqrt(cta_sumd(ps, red));
-    const double nr = sqrt(cta_sumd(pr, red));
-    const double delta = 2.0 * (ns + anorm[b] * nr);
-    for (int q = threadIdx.x; q < n * n; q += kThreads) {
-        const int i = q / n, j = q % n;
-        const double r = (i == j ? 1.0 : 0.0) - Gb[(long)i * ld + j];
+    ps = cta_sumd(ps, red);
+    pr = cta_sumd(pr, red);
+    if (threadIdx.x == 0) {
+        part[2 * ((long)b * ld + i)] = ps;
+        part[2 * ((long)b * ld + i) + 1] = pr;
+        w[b * wstride + i] = lam;
+    }
+}
+
+__global__ void __launch_bounds__(128)
+k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, int ld,
+           const int* __restrict__ nsz, const double* __restrict__ anorm,
+           const double* __restrict__ w, long wstride, const double* __restrict__ part,
+           double* __restrict__ emax) {
+    __shared__ double red[32];
+    const int b = blockIdx.y, i = blockIdx.x, n = nsz[b];
+    if (i >= n) return;
+    double ps = 0.0, pr = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        ps += part[2 * ((long)b * ld + j)];
+        pr += part[2 * ((long)b * ld + j) + 1];
+    }
+    ps = cta_sumd(ps, red);
+    pr = cta_sumd(pr, red);
+    const double delta = 2.0 * (sqrt(ps) + anorm[b] * sqrt(pr));
+    const double* lam = w + b * wstride;
+    const double li = lam[i];
+    const double* Sr = S + b * stride + (long)i * ld;
+    double* Gr = G + b * stride + (long)i * ld;
+    double em = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double r = (j == i ? 1.0 : 0.0) - Gr[j];
         double e;
-        if (i == j) {
-            e = 0.5 * r;
-        } else if (fabs(lam[j] - lam[i]) > delta) {
-            e = (Sb[(long)i * ld + j] + lam[j] * r) / (lam[j] - lam[i]);
+        if (j != i && fabs(lam[j] - li) > delta) {
+            e = (Sr[j] + lam[j] * r) / (lam[j] - li);
         } else {
             e = 0.5 * r;
         }
-        // read of G(i,j) happens before the write of F(i,j) by the same thread
-        Gb[(long)i * ld + j] = (i == j ? 1.0 : 0.0) + e;
+        if (lam[j] * li < 0.0) em = fmax(em, fabs(Sr[j]));
+        Gr[j] = (j == i ? 1.0 : 0.0) + e;
     }
-    for (int i = threadIdx.x; i < n; i += kThreads) w[b * wstride + i] = lam[i];
+    em /= anorm[b];
+    for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
+    __syncthreads();
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = em;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int k = 0; k < (int)(blockDim.x / 32); ++k) m = fmax(m, red[k]);
+        emax[(long)b * ld + i] = m;
+    }
 }
 
 // FP64 Jacobi polish of S = X^T A X after refinement: S is diagonal up to
@@ -283,6 +325,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     __shared__ double red[32];
     __shared__ double cs[2][64];
     __shared__ int act[64];
+    __shared__ int pqi[2][64];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
     if (n0 == 0) return;
@@ -302,19 +345,20 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     for (int t = tid; t < n0 * n0; t += kThreads) Qa(t / n0, t % n0) = (t / n0 == t % n0) ? 1.0 : 0.0;
     __syncthreads();
     const double thr = 1e-15 * anorm[b];
+    const int lane = tid & 127, kg = tid >> 7;
+    const int half = n / 2;
     int sweep = 0;
     for (; sweep < 12; ++sweep) {
-        double part = 0.0;
-        for (int t = tid; t < n * n; t += kThreads) {
-            const int i = t / n, j = t % n;
-            if (i != j && fabs(a[i * l2 + j]) > thr) part += 1.0;
-        }
-        if (cta_sumd(part, red) == 0.0) break;
+        int any = 0;
+        if (lane < n)
+            for (int i = kg; i < n; i += 2)
+                if (i != lane && fabs(a[i * l2 + lane]) > thr) any = 1;
+        if (!__syncthreads_or(any)) break;
         for (int r = 0; r < n - 1; ++r) {
-            if (tid < n / 2) {
+            int on = 0;
+            if (tid < half) {
                 const int p = rr_player(tid, r, n), qq = rr_player(n - 1 - tid, r, n);
                 const double apq = a[p * l2 + qq];
-                int on = 0;
                 double c = 1.0, s = 0.0;
                 if (fabs(apq) > thr) {
                     const double th = (a[qq * l2 + qq] - a[p * l2 + p]) / (2.0 * apq);
@@ -326,32 +370,35 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
                 cs[0][tid] = c;
                 cs[1][tid] = s;
                 act[tid] = on;
+                pqi[0][tid] = p;
+                pqi[1][tid] = qq;
             }
-            __syncthreads();
-            for (int t = tid; t < (n / 2) * n; t += kThreads) {
-                const int k = t / n, col = t % n;
-                if (!act[k]) continue;
-                const int p = rr_player(k, r, n), qq = rr_player(n - 1 - k, r, n);
-                const double c = cs[0][k], s = cs[1][k];
-                const double ap = a[p * l2 + col], aq = a[qq * l2 + col];
-                a[p * l2 + col] = c * ap - s * aq;
-                a[qq * l2 + col] = s * ap + c * aq;
-            }
-            __syncthreads();
-            for (int t = tid; t < (n / 2) * n; t += kThreads) {
-                const int k = t / n, row = t % n;
-                if (!act[k]) continue;
-                const int p = rr_player(k, r, n), qq = rr_player(n - 1 - k, r, n);
-                const double c = cs[0][k], s = cs[1][k];
-                const double ap = a[row * l2 + p], aq = a[row * l2 + qq];
-                a[row * l2 + p] = c * ap - s * aq;
-                a[row * l2 + qq] = s * ap + c * aq;
-                if (row < n0 && p < n0 && qq < n0) {
-                    const double vp = Qa(row, p), vq = Qa(row, qq);
-                    Qa(row, p) = c * vp - s * vq;
-                    Qa(row, qq) = s * vp + c * vq;
+            // rounds without a pair above the threshold rotate nothing
+            if (!__syncthreads_or(on)) continue;
+            if (lane < n)
+                for (int k = kg; k < half; k += 2) {
+                    if (!act[k]) continue;
+                    const int p = pqi[0][k], qq = pqi[1][k];
+                    const double c = cs[0][k], s = cs[1][k];
+                    const double ap = a[p * l2 + lane], aq = a[qq * l2 + lane];
+                    a[p * l2 + lane] = c * ap - s * aq;
+                    a[qq * l2 + lane] = s * ap + c * aq;
                 }
-            }
+            __syncthreads();
+            if (lane < n)
+                for (int k = kg; k < half; k += 2) {
+                    if (!act[k]) continue;
+                    const int p = pqi[0][k], qq = pqi[1][k];
+                    const double c = cs[0][k], s = cs[1][k];
+                    const double ap = a[lane * l2 + p], aq = a[lane * l2 + qq];
+                    a[lane * l2 + p] = c * ap - s * aq;
+                    a[lane * l2 + qq] = s * ap + c * aq;
+                    if (lane < n0 && p < n0 && qq < n0) {
+                        const double vp = Qa(lane, p), vq = Qa(lane, qq);
+                        Qa(lane, p) = c * vp - s * vq;
+                        Qa(lane, qq) = s * vp + c * vq;
+                    }
+                }
             __syncthreads();
         }
     }
@@ -397,7 +444,7 @@ size_t jacobi_smem(int n) {
 // nsz (device) <= nmax, stored with leading dimension ld and stride `stride`.
 // X (in/out: warm start when warm != 0), w: eigenvalues, ws: workspace of
 // 4 * nb * stride doubles; descs: GemmDesc workspace (3 * nb entries).
-int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish) {
+int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     if (!E.attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      200 * 1024));
@@ -405,11 +452,14 @@ int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish) {
                                      200 * 1024));
         E.attr_done = true;
     }
-    const size_t sm = jacobi_smem(E.nmax);
-    k_jacobi32<<<E.nb, kThreads, sm, c->stream>>>(E.A, E.stride, E.ld, E.nsz, warm ? E.X : nullptr,
-                                                  E.X, E.stride, E.ld, E.w, E.wstride,
-                                                  warm ? 12 : 30, c->flags + 4);
-    MG_LAUNCHED(c);
+    if (seed != kSeedRefine) {
+        const bool warm = seed == kSeedJacobiWarm;
+        const size_t sm = jacobi_smem(E.nmax);
+        k_jacobi32<<<E.nb, kThreads, sm, c->stream>>>(E.A, E.stride, E.ld, E.nsz,
+                                                      warm ? E.X : nullptr, E.X, E.stride, E.ld,
+                                                      E.w, E.wstride, warm ? 12 : 30, c->flags + 4);
+        MG_LAUNCHED(c);
+    }
     k_frob<<<E.nb, 128, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
     MG_LAUNCHED(c);
     const int tiles = div_up(E.nmax, kTile) * div_up(E.nmax, kTile);
@@ -419,8 +469,12 @@ int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish) {
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
         MG_LAUNCHED(c);
-        k_oa_correct<<<E.nb, kThreads, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz, E.anorm,
-                                                       E.w, E.wstride);
+        k_oa_rows<<<dim3(E.nmax, E.nb), 128, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz,
+                                                             E.w, E.wstride, E.part);
+        MG_LAUNCHED(c);
+        k_oa_apply<<<dim3(E.nmax, E.nb), 128, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz,
+                                                              E.anorm, E.w, E.wstride, E.part,
+                                                              E.emax);
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
         MG_LAUNCHED(c);
@@ -478,6 +532,9 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
     MG_CUDA(cudaMalloc(&E.G, bytes));
     MG_CUDA(cudaMalloc(&E.w, (size_t)nb * nmax * sizeof(double)));
     MG_CUDA(cudaMalloc(&E.anorm, (size_t)nb * sizeof(double)));
+    MG_CUDA(cudaMalloc(&E.part, (size_t)nb * ld * 2 * sizeof(double)));
+    MG_CUDA(cudaMalloc(&E.emax, (size_t)nb * ld * sizeof(double)));
+    MG_CUDA(cudaMemset(E.emax, 0, (size_t)nb * ld * sizeof(double)));
     std::vector<int> hn(nb);
     MG_CUDA(cudaMemcpy(hn.data(), nsz_dev, nb * sizeof(int), cudaMemcpyDeviceToHost));
     std::vector<GemmDesc> ax(nb), sg(2 * nb), xf(nb), rr(nb);
@@ -522,7 +579,7 @@ extern "C" int mg_eigh_batched(int nb, const int* n, int ld, const double* a, do
     MG_CUDA(cudaMemcpy(dn, n, nb * sizeof(int), cudaMemcpyHostToDevice));
     EigBatch E;
     int st = eig_setup(&tmp, E, nb, ld, dn, dA, stride, ld);
-    if (st == MG_OK) st = eig_batched(&tmp, E, false, 3, true);
+    if (st == MG_OK) st = eig_batched(&tmp, E, kSeedCold, 3, true);
     if (st == MG_OK) {
         MG_CUDA(cudaStreamSynchronize(tmp.stream));
         MG_CUDA(cudaMemcpy(w, E.w, nb * (size_t)ld * sizeof(double), cudaMemcpyDeviceToHost));
@@ -562,10 +619,13 @@ constexpr size_t kOffDesc = kOffNorm + round256(kNoAllocNb * sizeof(double));
 constexpr size_t kDescBytes = round256(5 * kNoAllocNb * sizeof(GemmDesc));
 constexpr size_t kOffNsz = kOffDesc + kDescBytes;
 constexpr size_t kOffFlags = kOffNsz + round256(kNoAllocNb * sizeof(int));
-constexpr size_t kNoAllocBytes = kOffFlags + 256;   // ~2.03 MiB
+constexpr size_t kOffPart = kOffFlags + 256;
+constexpr size_t kOffEmax = kOffPart + (size_t)2 * kNoAllocNb * kNoAllocLd * sizeof(double);
+constexpr size_t kNoAllocBytes = kOffEmax + (size_t)kNoAllocNb * kNoAllocLd * sizeof(double);
+// ~2.2 MiB
 
 // The whole workspace: four nb x ld x ld work matrices, norms, GEMM tables,
-// sizes, flags.
+// sizes, flags, refinement row sums.
 static __device__ __align__(256) unsigned char g_eig_scratch[kNoAllocBytes];
 
 struct NoAllocDevice {
@@ -613,7 +673,8 @@ int noalloc_setup(int dev, unsigned char** base) {
                                      200 * 1024));
         cudaFuncAttributes fa;
         MG_CUDA(cudaFuncGetAttributes(&fa, k_gemm64));
-        MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_correct));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_rows));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_apply));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_orth_prep));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_frob));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_eig_noalloc_tables));
@@ -664,6 +725,8 @@ extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const doubl
     E.S = reinterpret_cast<double*>(base + kOffS);
     E.G = reinterpret_cast<double*>(base + kOffG);
     E.anorm = reinterpret_cast<double*>(base + kOffNorm);
+    E.part = reinterpret_cast<double*>(base + kOffPart);
+    E.emax = reinterpret_cast<double*>(base + kOffEmax);
     GemmDesc* desc = reinterpret_cast<GemmDesc*>(base + kOffDesc);
     E.d_ax = desc;
     E.d_sg = desc + nb;
@@ -688,7 +751,7 @@ extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const doubl
     k_eig_noalloc_tables<<<1, kNoAllocNb, 0, tmp.stream>>>(args, const_cast<int*>(E.nsz), E.d_ax,
                                                           E.d_sg, E.d_xf, E.d_rr);
     MG_CUDA(cudaGetLastError());
-    const int st = eig_batched(&tmp, E, false, 3, true);
+    const int st = eig_batched(&tmp, E, kSeedCold, 3, true);
     tmp.flags = nullptr;
     tmp.stream = nullptr;
     return st;
@@ -698,7 +761,7 @@ namespace mg {
 
 void eig_free(EigBatch& E) {
     for (void* p : {(void*)E.X, (void*)E.X2, (void*)E.AX, (void*)E.S, (void*)E.G, (void*)E.w,
-                    (void*)E.anorm, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
+                    (void*)E.anorm, (void*)E.part, (void*)E.emax, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
                     (void*)E.d_rr})
         if (p) cudaFree(p);
 }

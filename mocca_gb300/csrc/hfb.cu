@@ -20,10 +20,11 @@
 // eig.cu: FP32 Jacobi seed + FP64 Ogita-Aishima refinement to FP64 accuracy.
 //
 // FindFermiEnergy: the reference's damped Broyden (src/HFB.f90:1849-2161)
-// is replaced by a safeguarded secant iteration on the same equation
+// is replaced by a safeguarded Newton iteration on the same equation
 // N(lambda) = N0 with the same tolerance FermiPrec per isospin; both reach the
-// same root.  Every particle-number evaluation is one short stream of
-// launches ending in a 4-double read-back.
+// same root.  dN/dlambda comes analytically from the eigen-decomposition, and
+// every particle-number evaluation is one short stream of launches ending in
+// a 12-double read-back.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -99,16 +100,63 @@ __global__ void k_rho_kappa(const double* __restrict__ X, const int* __restrict_
     K[(long)(h + r) * N + h + s] = 0.0;
 }
 
-// Tr rho per block (the particle number of HFBNumberofParticles)
+// dN/dlambda of a block from its eigen-decomposition.  T(lambda) = T0 -
+// lambda Sigma, Sigma = diag(I, -I); first-order perturbation of the vectors
+// gives, with P the projector on the lower (time-reversed) half and the
+// quasiparticle energies E,
+//   dN/dlambda = 8 sum_{m > 0 > n} (x_m^T P x_n)^2 / (E_m - E_n)  (> 0).
+// One CTA per positive state m; dpart[b][m - h] receives its row of the sum.
+__global__ void __launch_bounds__(128)
+k_dn_dlambda(const double* __restrict__ X, const double* __restrict__ E,
+             const int* __restrict__ hsz, int nmax, double* __restrict__ dpart) {
+    __shared__ double xm[64];
+    __shared__ double red[32];
+    const int b = blockIdx.y, h = hsz[b], N = 2 * h;
+    const int mm = blockIdx.x;
+    if (mm >= h) return;
+    const int m = h + mm;
+    const double* Xb = X + (long)b * nmax * nmax;
+    for (int r = threadIdx.x; r < h; r += blockDim.x) xm[r] = Xb[(long)(h + r) * nmax + m];
+    __syncthreads();
+    const double Em = E[(long)b * nmax + m];
+    double part = 0.0;
+    for (int n = threadIdx.x; n < h; n += blockDim.x) {
+        double p = 0.0;
+        for (int r = 0; r < h; ++r) p = fma(xm[r], Xb[(long)(h + r) * nmax + n], p);
+        part += p * p / (Em - E[(long)b * nmax + n]);
+    }
+    const double s = cta_sum(part, red);
+    if (threadIdx.x == 0) dpart[(long)b * (nmax / 2) + mm] = 8.0 * s;
+    (void)N;
+}
+
+// Per block: Tr rho (the particle number of HFBNumberofParticles) into
+// out[b], dN/dlambda into out[4 + b], and the largest opposite-sign coupling
+// seen by the last refinement step into out[8 + b].
 __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ hsz, int nmax,
-                        double* __restrict__ trace) {
+                        const double* __restrict__ dpart, const double* __restrict__ emax,
+                        double* __restrict__ out) {
     __shared__ double red[32];
     const int b = blockIdx.x;
-    const int N = 2 * hsz[b];
-    double p = 0.0;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) p += rho[(long)b * nmax * nmax + (long)i * N + i];
+    const int h = hsz[b], N = 2 * h;
+    double p = 0.0, d = 0.0, e = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        p += rho[(long)b * nmax * nmax + (long)i * N + i];
+        e = fmax(e, emax[(long)b * nmax + i]);
+    }
+    for (int i = threadIdx.x; i < h; i += blockDim.x) d += dpart[(long)b * (nmax / 2) + i];
     const double s = cta_sum(p, red);
-    if (threadIdx.x == 0) trace[b] = s;
+    const double ds = cta_sum(d, red);
+    for (int o = 16; o > 0; o >>= 1) e = fmax(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double em = 0.0;
+        for (int k = 0; k < (int)(blockDim.x / 32); ++k) em = fmax(em, red[k]);
+        out[b] = s;
+        out[4 + b] = ds;
+        out[8 + b] = em;
+    }
 }
 
 // rho_++ blocks into the eigensolver batch (leading dimension hmax); HF
@@ -224,7 +272,7 @@ int hfb_prepare(mg_ctx* c) {
               A(&H.dfac, 2 * V) && A(&H.pcut, nwt) && A(&H.ktil, 4L * hmax * hmax) &&
               A(&H.fpart, 8 * V) && A(&H.fre, 2 * V) && A(&H.fim, 2 * V) &&
               A(&H.gpart, 4L * H.gchunk * hmax * hmax) && A(&H.cantr, 4L * hmax * hmax) &&
-              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.trace_d, 4) && A(&H.scal_d, 16) &&
+              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.trace_d, 12) && A(&H.dpart, 4L * hmax) && A(&H.scal_d, 16) &&
               cudaMalloc(&H.members, 4 * hmax * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.hsz, 4 * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.nsz_T, 4 * sizeof(int)) == cudaSuccess &&
@@ -271,7 +319,7 @@ int hfb_prepare(mg_ctx* c) {
 void hfb_free(mg_ctx* c) {
     Hfb& H = c->hfb;
     for (double* p : {H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.qe, H.dfac, H.pcut, H.ktil,
-                      H.fpart, H.fre, H.fim, H.gpart, H.cantr, H.occ, H.fermi_d, H.trace_d,
+                      H.fpart, H.fre, H.fim, H.gpart, H.cantr, H.occ, H.fermi_d, H.trace_d, H.dpart,
                       H.scal_d, H.T, H.Rpp})
         if (p) cudaFree(p);
     for (int* p : {H.members, H.hsz, H.cstart, H.nsz_T})
@@ -282,27 +330,44 @@ void hfb_free(mg_ctx* c) {
 }
 
 // One particle-number evaluation at lambda (both isospins): T(lambda),
-// eigen-decomposition, rho, kappa, block traces.
-static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out) {
+// eigen-decomposition, rho, kappa, block traces and dN/dlambda.  The vectors
+// of the previous evaluation seed the refinement directly; when, before its
+// last step, states of opposite quasiparticle-energy sign were still coupled
+// by more than 1e-10 |T| (the start was too far for the quadratic regime),
+// the evaluation is redone from an FP32 Jacobi seed.
+static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out) {
     Hfb& H = c->hfb;
     double* hp = H.h_pinned;
-    hp[8] = lam[0];
-    hp[9] = lam[1];
-    MG_CUDA(cudaMemcpyAsync(H.fermi_d, hp + 8, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    hp[24] = lam[0];
+    hp[25] = lam[1];
+    MG_CUDA(cudaMemcpyAsync(H.fermi_d, hp + 24, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     k_build_T<<<dim3(div_up(H.nmax * H.nmax, kThreads), 4), kThreads, 0, c->stream>>>(
         H.delta, c->bas[MG_HF_BASIS].e, H.members, H.hsz, H.hmax, H.nmax, H.fermi_d, H.T);
     MG_LAUNCHED(c);
-    MG_TRY(eig_batched(c, H.eT, H.eT.have_vectors, H.nref, false));
-    H.eT.have_vectors = true;
-    k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
-        H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
-    MG_LAUNCHED(c);
-    k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.trace_d);
-    MG_LAUNCHED(c);
-    MG_CUDA(cudaMemcpyAsync(hp, H.trace_d, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    MG_CUDA(cudaStreamSynchronize(c->stream));
+    int seed = H.eT.have_vectors ? kSeedRefine : kSeedCold;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        MG_TRY(eig_batched(c, H.eT, seed, H.nref, false));
+        H.eT.have_vectors = true;
+        k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
+            H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
+        MG_LAUNCHED(c);
+        k_dn_dlambda<<<dim3(H.hmax, 4), 128, 0, c->stream>>>(H.eT.X, H.eT.w, H.hsz, H.nmax,
+                                                            H.dpart);
+        MG_LAUNCHED(c);
+        k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.dpart, H.eT.emax, H.trace_d);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(hp, H.trace_d, 12 * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+        const double em = std::max(std::max(hp[8], hp[9]), std::max(hp[10], hp[11]));
+        if (seed != kSeedRefine || em <= 1e-10) break;
+        seed = kSeedJacobiWarm;
+        ++H.reseeds;
+    }
     N_out[0] = hp[0] + hp[1] - c->p.neutrons;
     N_out[1] = hp[2] + hp[3] - c->p.protons;
+    dN_out[0] = hp[4] + hp[5];
+    dN_out[1] = hp[6] + hp[7];
     if (std::isnan(N_out[0]) || std::isnan(N_out[1])) return MG_ERR_NAN;
     return MG_OK;
 }
@@ -325,58 +390,44 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     MG_CUDA(cudaMemsetAsync(c->flags, 0, 16 * sizeof(int), c->stream));
     MG_TRY(pairing_mesh(c));
 
-    // ---- particle-number root finder (safeguarded secant) -----------------------
+    // ---- particle-number root finder: Newton with the analytic dN/dlambda,
+    // safeguarded by the bracket the evaluations build (bisection when a step
+    // leaves it, steps clamped to 5 MeV) ----------------------------------------
     const double prec = H.pp.fermi_prec;
     int evals = 0;
-    double lam[2] = {H.fermi[0], H.fermi[1]}, f[2];
-    MG_TRY(hfb_evaluate(c, lam, f));
+    double lam[2] = {H.fermi[0], H.fermi[1]}, f[2], fp[2];
+    MG_TRY(hfb_evaluate(c, lam, f, fp));
     ++evals;
     bool conv[2] = {std::fabs(f[0]) < prec, std::fabs(f[1]) < prec};
     double lo[2] = {0, 0}, hi[2] = {0, 0};
     bool has_lo[2] = {false, false}, has_hi[2] = {false, false};
-    double plam[2], pf[2], slope[2];
-    for (int it = 0; it < 2; ++it) {
+    auto bracket = [&](int it) {
         if (f[it] < 0) { lo[it] = lam[it]; has_lo[it] = true; }
         else { hi[it] = lam[it]; has_hi[it] = true; }
-        plam[it] = lam[it];
-        pf[it] = f[it];
-        slope[it] = H.slope[it] > 0.0 ? H.slope[it] : 0.0;
-    }
+    };
+    bracket(0);
+    bracket(1);
     const int maxit = H.pp.max_iter > 0 ? H.pp.max_iter : 50;
     for (int k = 0; k < maxit && !(conv[0] && conv[1]); ++k) {
         for (int it = 0; it < 2; ++it) {
             if (conv[it]) continue;
-            double next;
-            if (slope[it] <= 0.0) {
-                next = lam[it] + (f[it] < 0 ? 0.01 : -0.01);  // first probe, as the reference
-            } else {
-                double step = -f[it] / slope[it];
-                step = std::max(-5.0, std::min(5.0, step));
-                next = lam[it] + step;
-            }
+            double step = fp[it] > 1e-12 ? -f[it] / fp[it] : (f[it] < 0 ? 0.5 : -0.5);
+            step = std::max(-5.0, std::min(5.0, step));
+            double next = lam[it] + step;
             if (has_lo[it] && has_hi[it] && !(next > lo[it] && next < hi[it]))
                 next = 0.5 * (lo[it] + hi[it]);
-            plam[it] = lam[it];
-            pf[it] = f[it];
             lam[it] = next;
         }
-        MG_TRY(hfb_evaluate(c, lam, f));
+        MG_TRY(hfb_evaluate(c, lam, f, fp));
         ++evals;
         for (int it = 0; it < 2; ++it) {
             if (conv[it]) continue;
             if (std::fabs(f[it]) < prec) { conv[it] = true; continue; }
-            if (lam[it] != plam[it]) {
-                const double s = (f[it] - pf[it]) / (lam[it] - plam[it]);
-                if (s > 0.0) slope[it] = s;
-            }
-            if (f[it] < 0) { lo[it] = lam[it]; has_lo[it] = true; }
-            else { hi[it] = lam[it]; has_hi[it] = true; }
+            bracket(it);
         }
     }
     H.fermi[0] = lam[0];
     H.fermi[1] = lam[1];
-    for (int it = 0; it < 2; ++it)
-        if (slope[it] > 0.0) H.slope[it] = slope[it];
     for (int i = 0; i < 6; ++i) H.fermi_hist[i] = H.fermi_hist[i + 1];
     H.fermi_hist[6] = std::fabs(f[0]) > 0.9 || std::fabs(f[1]) > 0.9;
     bool lost = true;
@@ -388,7 +439,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
         H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
     MG_LAUNCHED(c);
-    MG_TRY(eig_batched(c, H.eR, H.eR.have_vectors, H.nref, true));
+    MG_TRY(eig_batched(c, H.eR, H.eR.have_vectors ? kSeedJacobiWarm : kSeedCold, H.nref, true));
     H.eR.have_vectors = true;
     k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax, H.cantr,
                                                  c->bas[MG_CAN_BASIS].occ, H.scal_d, c->flags);

@@ -84,6 +84,8 @@ struct EigBatch {
     double* A = nullptr;
     double *X = nullptr, *X2 = nullptr, *AX = nullptr, *S = nullptr, *G = nullptr, *w = nullptr,
            *anorm = nullptr;
+    double* part = nullptr;   // nb * ld * 2 row sums of a refinement step
+    double* emax = nullptr;   // nb * ld largest opposite-sign coupling |S_ij|/|A| per row
     GemmDesc *d_ax = nullptr, *d_sg = nullptr, *d_xf = nullptr, *d_rr = nullptr;
     bool attr_done = false;
     bool have_vectors = false;
@@ -115,11 +117,12 @@ struct Hfb {
     int gchunk = 0;
     double *cantr = nullptr, *occ = nullptr;   // 4*hmax*hmax, 4*hmax
     double* fermi_d = nullptr;                 // 2
-    double* trace_d = nullptr;                 // 4 block traces of rho
+    double* trace_d = nullptr;                 // traces, dN/dlambda, refinement size
+    double* dpart = nullptr;                   // 4*hmax dN/dlambda row sums
     double* scal_d = nullptr;                  // [energy(2), disp(2)]
     double* h_pinned = nullptr;                // 8 pinned doubles
     double fermi[2] = {-10.0, -10.0};
-    double slope[2] = {0.0, 0.0};              // dN/dlambda from the last solve
+    long long reseeds = 0;                     // evaluations redone from a Jacobi seed
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
     double* T = nullptr;      // 4 block HFB matrices (signature-reduced), nmax x nmax
@@ -216,7 +219,10 @@ int canonical_transform(mg_ctx* c);
 int pairing_set_smem(mg_ctx* c);
 int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, double* A,
               long stride, int ld);
-int eig_batched(mg_ctx* c, EigBatch& E, bool warm, int nref, bool polish);
+// Seeds of eig_batched: FP32 Jacobi from scratch, FP32 Jacobi on X^T A X of
+// the vectors in E.X, or refinement started directly from E.X.
+enum EigSeed { kSeedCold = 0, kSeedJacobiWarm = 1, kSeedRefine = 2 };
+int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish);
 void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
