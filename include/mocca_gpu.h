@@ -183,6 +183,13 @@ int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const double* a, doubl
 int mg_create(const mg_params* p, const mg_force* f, void* stream, mg_ctx** out);
 int mg_destroy(mg_ctx* ctx);
 int mg_synchronize(mg_ctx* ctx);
+/* Precision of the following calls (MG_FP64 or MG_MIXED), e.g. an FP64
+ * polish after mixed-precision iterations.  MG_MIXED runs the Lagrange
+ * derivative contractions and the mean-field multiplies in FP32 with FP64
+ * storage; overlaps, Gram-Schmidt, energies, the HFB matrices and their
+ * diagonalisation stay FP64.  No reference counterpart (the reference is
+ * FP64 throughout). */
+int mg_set_precision(mg_ctx* ctx, int precision);
 
 /* ---- spinor transfer ------------------------------------------------------- */
 

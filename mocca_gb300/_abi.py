@@ -137,6 +137,7 @@ SIGNATURES = {
     "mg_create": [C.POINTER(MgParams), C.POINTER(MgForce), _P, C.POINTER(_P)],
     "mg_destroy": [_P],
     "mg_synchronize": [_P],
+    "mg_set_precision": [_P, C.c_int],
     "mg_upload_spinors": [_P, C.c_int, _PP, _I, C.c_int, C.c_int],
     "mg_download_spinors": [_P, C.c_int, _PP, C.c_int, C.c_int],
     "mg_download_derivatives": [_P, C.c_int, _PP, _PP, C.c_int, C.c_int],

@@ -15,6 +15,8 @@
 // so the Laplacian is summed (X + Y) + Z as in Lapla_LAG_EV8.
 // Matrices are stored transposed, MT[q*n + i], so the threads of a warp
 // (consecutive output points i) read consecutive shared-memory words.
+#include <algorithm>
+
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -128,6 +130,203 @@ k_deriv_z(const GridJob* __restrict__ jobs, MatPtrs mp, int nx, int ny, int nz) 
     }
 }
 
+// ---- mixed precision: double-float arithmetic, FP64 grids in and out -------------
+//
+// GB300 issues FP32 at ~70x its FP64 rate, so the mixed form evaluates the
+// contractions in double-float: every FP64 value is split into an unevaluated
+// sum hi + lo of two floats (48 significant bits), products are formed
+// exactly with an FMA (TwoProduct) and the running sum is carried as a
+// (hi, lo) pair with Knuth's TwoSum (Dekker 1971, "A floating-point
+// technique for extending the available precision", Numer. Math. 18).  The
+// result is FP64-accurate to ~1e-14 relative at ~12 FP32 operations per
+// term.  Each thread owns four consecutive outputs along the contracted axis
+// (or four rows for d/dx), so every shared-memory pair it loads feeds four or
+// eight terms.  Matrices are stored transposed as (hi, lo) float planes with
+// a row stride rounded up to a multiple of 4 (zero padding).
+
+struct MatPtrs32 {
+    const float* m[3][2][2];  // [axis][kind][slot]: hi plane [q][ld4], lo plane after it
+    int ld4[3];
+};
+
+// s += a * b in double-float.  The rounded product and the TwoSum steps use
+// the _rn intrinsics so that the compiler cannot fuse them into FMAs (which
+// would change the rounding the error terms rely on).
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh,
+                                       float bl) {
+    const float ph = __fmul_rn(ah, bh);
+    float pl = fmaf(ah, bh, -ph);
+    pl = fmaf(ah, bl, pl);
+    pl = fmaf(al, bh, pl);
+    const float t = __fadd_rn(sh, ph);
+    const float bp = __fsub_rn(t, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+    sh = t;
+    sl += e + pl;
+}
+
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+    h = (float)x;
+    l = (float)(x - (double)h);
+}
+
+__global__ void __launch_bounds__(256)
+k_deriv_xy_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int nz,
+              int planes_per_block) {
+    extern __shared__ float smf[];
+    const GridJob J = jobs[blockIdx.x];
+    const bool want_x = J.dx != nullptr || J.lap != nullptr;
+    const bool want_y = J.dy != nullptr || J.lap != nullptr;
+    if (!want_x && !want_y) return;
+    const int lx = mp.ld4[0], ly = mp.ld4[1];
+    const int ny4 = (ny + 3) / 4;
+    const int mx = nx * lx, my = ny * ly;
+    float* sDx = smf;              // hi [mx], lo [mx]
+    float* sLx = sDx + 2 * mx;
+    float* sDy = sLx + 2 * mx;
+    float* sLy = sDy + 2 * my;
+    float* sPh = sLy + 2 * my;     // (4 * ny4) rows x nx, rows >= ny zero
+    float* sPl = sPh + 4 * ny4 * nx;
+    const float* gDx = J.slot[0] ? mp.m[0][0][1] : mp.m[0][0][0];
+    const float* gLx = J.slot[0] ? mp.m[0][1][1] : mp.m[0][1][0];
+    const float* gDy = J.slot[1] ? mp.m[1][0][1] : mp.m[1][0][0];
+    const float* gLy = J.slot[1] ? mp.m[1][1][1] : mp.m[1][1][0];
+    for (int t = threadIdx.x; t < 2 * mx; t += blockDim.x) {
+        sDx[t] = gDx[t];
+        sLx[t] = gLx[t];
+    }
+    for (int t = threadIdx.x; t < 2 * my; t += blockDim.x) {
+        sDy[t] = gDy[t];
+        sLy[t] = gLy[t];
+    }
+    for (int t = ny * nx + threadIdx.x; t < 4 * ny4 * nx; t += blockDim.x) {
+        sPh[t] = 0.0f;
+        sPl[t] = 0.0f;
+    }
+    const int plane = nx * ny;
+    const int items = nx * ny4;
+    const int k0 = blockIdx.y * planes_per_block;
+    const int k1 = min(nz, k0 + planes_per_block);
+    for (int k = k0; k < k1; ++k) {
+        const double* in = J.in + (long)k * plane;
+        __syncthreads();
+        for (int t = threadIdx.x; t < plane; t += blockDim.x) df_split(in[t], sPh[t], sPl[t]);
+        __syncthreads();
+        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+            const int x = it % nx, y0 = 4 * (it / nx);
+            float axh[4] = {0.f, 0.f, 0.f, 0.f}, axl[4] = {0.f, 0.f, 0.f, 0.f};
+            float bxh[4] = {0.f, 0.f, 0.f, 0.f}, bxl[4] = {0.f, 0.f, 0.f, 0.f};
+            float ayh[4] = {0.f, 0.f, 0.f, 0.f}, ayl[4] = {0.f, 0.f, 0.f, 0.f};
+            float byh[4] = {0.f, 0.f, 0.f, 0.f}, byl[4] = {0.f, 0.f, 0.f, 0.f};
+            if (want_x) {
+                for (int q = 0; q < nx; ++q) {
+                    const float dh = sDx[q * lx + x], dl = sDx[mx + q * lx + x];
+                    const float lh = sLx[q * lx + x], ll = sLx[mx + q * lx + x];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float vh = sPh[(y0 + j) * nx + q], vl = sPl[(y0 + j) * nx + q];
+                        df_fma(axh[j], axl[j], dh, dl, vh, vl);
+                        df_fma(bxh[j], bxl[j], lh, ll, vh, vl);
+                    }
+                }
+            }
+            if (want_y) {
+                for (int q = 0; q < ny; ++q) {
+                    const float vh = sPh[q * nx + x], vl = sPl[q * nx + x];
+                    const float4 dh = *reinterpret_cast<const float4*>(sDy + q * ly + y0);
+                    const float4 dl = *reinterpret_cast<const float4*>(sDy + my + q * ly + y0);
+                    const float4 lh = *reinterpret_cast<const float4*>(sLy + q * ly + y0);
+                    const float4 ll = *reinterpret_cast<const float4*>(sLy + my + q * ly + y0);
+                    df_fma(ayh[0], ayl[0], dh.x, dl.x, vh, vl);
+                    df_fma(ayh[1], ayl[1], dh.y, dl.y, vh, vl);
+                    df_fma(ayh[2], ayl[2], dh.z, dl.z, vh, vl);
+                    df_fma(ayh[3], ayl[3], dh.w, dl.w, vh, vl);
+                    df_fma(byh[0], byl[0], lh.x, ll.x, vh, vl);
+                    df_fma(byh[1], byl[1], lh.y, ll.y, vh, vl);
+                    df_fma(byh[2], byl[2], lh.z, ll.z, vh, vl);
+                    df_fma(byh[3], byl[3], lh.w, ll.w, vh, vl);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (y0 + j >= ny) break;
+                const long o = (long)k * plane + (long)(y0 + j) * nx + x;
+                if (J.dx) J.dx[o] = (double)axh[j] + (double)axl[j];
+                if (J.dy) J.dy[o] = (double)ayh[j] + (double)ayl[j];
+                if (J.lap)
+                    J.lap[o] = ((double)bxh[j] + (double)bxl[j]) + ((double)byh[j] + (double)byl[j]);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(512)
+k_deriv_z_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int nz) {
+    extern __shared__ float smf[];
+    const GridJob J = jobs[blockIdx.x];
+    if (J.dz == nullptr && J.lap == nullptr) return;
+    const int lz = mp.ld4[2];
+    const int mz = nz * lz;
+    float* sDz = smf;
+    float* sLz = sDz + 2 * mz;
+    float* sGh = sLz + 2 * mz;  // [q][col]
+    float* sGl = sGh + nz * kColTile;
+    const float* gDz = J.slot[2] ? mp.m[2][0][1] : mp.m[2][0][0];
+    const float* gLz = J.slot[2] ? mp.m[2][1][1] : mp.m[2][1][0];
+    for (int t = threadIdx.x; t < 2 * mz; t += blockDim.x) {
+        sDz[t] = gDz[t];
+        sLz[t] = gLz[t];
+    }
+    const int plane = nx * ny;
+    const int c0 = blockIdx.y * kColTile;
+    for (int t = threadIdx.x; t < nz * kColTile; t += blockDim.x) {
+        const int q = t / kColTile, cc = t % kColTile;
+        const double v = (c0 + cc < plane) ? J.in[(long)q * plane + c0 + cc] : 0.0;
+        df_split(v, sGh[t], sGl[t]);
+    }
+    __syncthreads();
+    const int nz4 = (nz + 3) / 4;
+    for (int it = threadIdx.x; it < kColTile * nz4; it += blockDim.x) {
+        const int col = it % kColTile, i0 = 4 * (it / kColTile);
+        if (c0 + col >= plane) continue;
+        float azh[4] = {0.f, 0.f, 0.f, 0.f}, azl[4] = {0.f, 0.f, 0.f, 0.f};
+        float bzh[4] = {0.f, 0.f, 0.f, 0.f}, bzl[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int q = 0; q < nz; ++q) {
+            const float vh = sGh[q * kColTile + col], vl = sGl[q * kColTile + col];
+            const float4 dh = *reinterpret_cast<const float4*>(sDz + q * lz + i0);
+            const float4 dl = *reinterpret_cast<const float4*>(sDz + mz + q * lz + i0);
+            const float4 lh = *reinterpret_cast<const float4*>(sLz + q * lz + i0);
+            const float4 ll = *reinterpret_cast<const float4*>(sLz + mz + q * lz + i0);
+            df_fma(azh[0], azl[0], dh.x, dl.x, vh, vl);
+            df_fma(azh[1], azl[1], dh.y, dl.y, vh, vl);
+            df_fma(azh[2], azl[2], dh.z, dl.z, vh, vl);
+            df_fma(azh[3], azl[3], dh.w, dl.w, vh, vl);
+            df_fma(bzh[0], bzl[0], lh.x, ll.x, vh, vl);
+            df_fma(bzh[1], bzl[1], lh.y, ll.y, vh, vl);
+            df_fma(bzh[2], bzl[2], lh.z, ll.z, vh, vl);
+            df_fma(bzh[3], bzl[3], lh.w, ll.w, vh, vl);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (i0 + j >= nz) break;
+            const long o = (long)(i0 + j) * plane + c0 + col;
+            if (J.dz) J.dz[o] = (double)azh[j] + (double)azl[j];
+            if (J.lap) J.lap[o] = J.lap[o] + ((double)bzh[j] + (double)bzl[j]);
+        }
+    }
+}
+
+MatPtrs32 mat_ptrs32(const mg_ctx* c) {
+    MatPtrs32 mp;
+    const int ns[3] = {c->nx, c->ny, c->nz};
+    for (int a = 0; a < 3; ++a) {
+        mp.ld4[a] = (ns[a] + 3) / 4 * 4;
+        for (int k = 0; k < 2; ++k)
+            for (int s = 0; s < 2; ++s) mp.m[a][k][s] = c->mats32 + c->mat32_off[a][k][s];
+    }
+    return mp;
+}
+
 MatPtrs mat_ptrs(const mg_ctx* c) {
     MatPtrs mp;
     for (int a = 0; a < 3; ++a)
@@ -163,6 +362,33 @@ int upload_matrices(mg_ctx* c) {
     }
     MG_CUDA(cudaMalloc(&c->mats, total * sizeof(double)));
     MG_CUDA(cudaMemcpy(c->mats, h.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    // double-float copy for the mixed-precision kernels: hi plane [q][ld4]
+    // then lo plane, zero padding
+    long total32 = 0;
+    for (int a = 0; a < 3; ++a) {
+        const int ld4 = (ns[a] + 3) / 4 * 4;
+        for (int k = 0; k < 2; ++k)
+            for (int s = 0; s < 2; ++s) {
+                c->mat32_off[a][k][s] = total32;
+                total32 += 2L * ns[a] * ld4;
+            }
+    }
+    std::vector<float> h32(total32, 0.0f);
+    for (int a = 0; a < 3; ++a) {
+        const int n = ns[a], ld4 = (n + 3) / 4 * 4;
+        for (int k = 0; k < 2; ++k)
+            for (int s = 0; s < 2; ++s)
+                for (int q = 0; q < n; ++q)
+                    for (int i = 0; i < n; ++i) {
+                        const double x = h[c->mat_off[a][k][s] + (long)q * n + i];
+                        const float hi = (float)x;
+                        const long o = c->mat32_off[a][k][s] + (long)q * ld4 + i;
+                        h32[o] = hi;
+                        h32[o + (long)n * ld4] = (float)(x - (double)hi);
+                    }
+    }
+    MG_CUDA(cudaMalloc(&c->mats32, total32 * sizeof(float)));
+    MG_CUDA(cudaMemcpy(c->mats32, h32.data(), total32 * sizeof(float), cudaMemcpyHostToDevice));
     return MG_OK;
 }
 
@@ -192,18 +418,38 @@ int build_basis_jobs(mg_ctx* c, int b) {
 int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
     if (njobs <= 0) return MG_OK;
     const int nx = c->nx, ny = c->ny, nz = c->nz;
-    MatPtrs mp = mat_ptrs(c);
     const int ppb = 4;
-    size_t sm_xy = (size_t)(2 * nx * nx + 2 * ny * ny + nx * ny) * sizeof(double);
-    size_t sm_z = (size_t)(2 * nz * nz + nz * kColTile) * sizeof(double);
     static bool attr_done = false;
     if (!attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_deriv_xy, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      200 * 1024));
         MG_CUDA(cudaFuncSetAttribute(k_deriv_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      200 * 1024));
+        MG_CUDA(cudaFuncSetAttribute(k_deriv_xy_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        MG_CUDA(cudaFuncSetAttribute(k_deriv_z_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
         attr_done = true;
     }
+    if (c->cur_precision == MG_MIXED) {
+        MatPtrs32 mp = mat_ptrs32(c);
+        const int ny4 = (ny + 3) / 4, nz4 = (nz + 3) / 4;
+        const size_t sm_xy =
+            (size_t)(4 * nx * mp.ld4[0] + 4 * ny * mp.ld4[1] + 8 * ny4 * nx) * sizeof(float);
+        const size_t sm_z = (size_t)(4 * nz * mp.ld4[2] + 2 * nz * kColTile) * sizeof(float);
+        const int txy = std::min(256, div_up((long)nx * ny4, 32) * 32);
+        const int tz = std::min(512, kColTile * nz4);
+        k_deriv_xy_df<<<dim3(njobs, div_up(nz, ppb)), txy, sm_xy, c->stream>>>(jobs, mp, nx, ny,
+                                                                             nz, ppb);
+        MG_LAUNCHED(c);
+        k_deriv_z_df<<<dim3(njobs, div_up((long)nx * ny, kColTile)), tz, sm_z, c->stream>>>(
+            jobs, mp, nx, ny, nz);
+        MG_LAUNCHED(c);
+        return MG_OK;
+    }
+    MatPtrs mp = mat_ptrs(c);
+    size_t sm_xy = (size_t)(2 * nx * nx + 2 * ny * ny + nx * ny) * sizeof(double);
+    size_t sm_z = (size_t)(2 * nz * nz + nz * kColTile) * sizeof(double);
     dim3 gxy(njobs, div_up(nz, ppb));
     k_deriv_xy<<<gxy, kThreads, sm_xy, c->stream>>>(jobs, mp, nx, ny, nz, ppb);
     MG_LAUNCHED(c);

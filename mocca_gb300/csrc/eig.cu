@@ -198,11 +198,35 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     for (int k = tid; k < n0; k += kThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
 }
 
+// Early exit of the refinement steps (EigBatch::skip_tol).  Step s of
+// matrix b is skipped when done[b] <= s.  The first launch of step s (decide)
+// sets done[b] = s when step s - 1 saw |S - diag S|_F <= tol |A|_F: its
+// correction already left every off-diagonal element at ~tol^2 |A|^2 / gap,
+// clusters included.  Every CTA of the deciding launch reads the same value
+// and so takes the same branch; the later launches of the step read done[b].
+struct SkipCtl {
+    int* done;              // nullptr: no early exit
+    const double* offrel;   // nb: |S - diag S|_F / |A|_F of the last step run
+    int step, decide;
+    double tol;
+};
+
+__device__ __forceinline__ bool skip_step(const SkipCtl& k, int b) {
+    if (k.done == nullptr) return false;
+    if (k.done[b] <= k.step) return true;
+    if (!k.decide || k.step == 0) return false;
+    if (!(k.offrel[b] <= k.tol)) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) k.done[b] = k.step;
+    return true;
+}
+
 // Batched FP64 GEMM, C = alpha op(A) op(B) + beta C, m,n,k <= 128, row-major.
-__global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict__ descs) {
+__global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict__ descs,
+                                                     SkipCtl sk) {
     __shared__ double sA[kTile][129];
     __shared__ double sB[129][kTile + 1];
     const GemmDesc g = descs[blockIdx.y];
+    if (skip_step(sk, g.mat)) return;
     const int tiles_n = (g.n + kTile - 1) / kTile;
     const int ti = blockIdx.x / tiles_n, tj = blockIdx.x % tiles_n;
     if (ti * kTile >= g.m) return;
@@ -234,19 +258,20 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
 // FP64 work (divisions included) runs on many SMs.  k_oa_rows: lambda_i =
 // s_ii / g_ii (into w) and the row sums of (S - diag lambda)^2 and
 // (I - G)^2; k_oa_apply: delta from those sums (every CTA of a matrix adds
-// them in the same order), then row i of F = I + E written over row i of G,
-// and emax(i) = max |S_ij| / |A| over the pairs whose eigenvalue estimates
-// have opposite signs: how far the vectors still are from splitting the
-// space into its positive and negative parts (the refinement leaves pairs
-// inside a cluster |lambda_i - lambda_j| <= delta unrotated, so a start too
-// far away shows here and not in E).
+// them in the same order; row 0 records |S - diag S|_F / |A|_F in offrel),
+// then row i of F = I + E written over row i of G,
+// and emax(i) = max |S_ij| / |lambda_i - lambda_j| over the pairs whose
+// eigenvalue estimates have opposite signs: the rotation angle by which the
+// vectors still miss the split of the space into its positive and negative
+// parts (the refinement leaves pairs inside a cluster |lambda_i - lambda_j|
+// <= delta unrotated, so a start too far away shows here and not in E).
 __global__ void __launch_bounds__(128)
 k_oa_rows(const double* __restrict__ S, const double* __restrict__ G, long stride, int ld,
           const int* __restrict__ nsz, double* __restrict__ w, long wstride,
-          double* __restrict__ part) {
+          double* __restrict__ part, SkipCtl sk) {
     __shared__ double red[32];
     const int b = blockIdx.y, i = blockIdx.x, n = nsz[b];
-    if (i >= n) return;
+    if (i >= n || skip_step(sk, b)) return;
     const double* Sr = S + b * stride + (long)i * ld;
     const double* Gr = G + b * stride + (long)i * ld;
     const double lam = Sr[i] / Gr[i];
@@ -270,10 +295,10 @@ __global__ void __launch_bounds__(128)
 k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, int ld,
            const int* __restrict__ nsz, const double* __restrict__ anorm,
            const double* __restrict__ w, long wstride, const double* __restrict__ part,
-           double* __restrict__ emax) {
+           double* __restrict__ emax, double* __restrict__ offrel, SkipCtl sk) {
     __shared__ double red[32];
     const int b = blockIdx.y, i = blockIdx.x, n = nsz[b];
-    if (i >= n) return;
+    if (i >= n || skip_step(sk, b)) return;
     double ps = 0.0, pr = 0.0;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
         ps += part[2 * ((long)b * ld + j)];
@@ -282,6 +307,7 @@ k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, in
     ps = cta_sumd(ps, red);
     pr = cta_sumd(pr, red);
     const double delta = 2.0 * (sqrt(ps) + anorm[b] * sqrt(pr));
+    if (i == 0 && threadIdx.x == 0) offrel[b] = sqrt(ps) / anorm[b];
     const double* lam = w + b * wstride;
     const double li = lam[i];
     const double* Sr = S + b * stride + (long)i * ld;
@@ -295,10 +321,9 @@ k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, in
         } else {
             e = 0.5 * r;
         }
-        if (lam[j] * li < 0.0) em = fmax(em, fabs(Sr[j]));
+        if (lam[j] * li < 0.0) em = fmax(em, fabs(Sr[j]) / fabs(lam[j] - li));
         Gr[j] = (j == i ? 1.0 : 0.0) + e;
     }
-    em /= anorm[b];
     for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
     __syncthreads();
     if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = em;
@@ -421,6 +446,32 @@ __global__ void k_orth_prep(const double* __restrict__ G, double* __restrict__ R
     F[o] = (i == j ? 1.0 : 0.0) + 0.5 * r;
 }
 
+// Ascending order after a refinement that started from earlier vectors (the
+// eigenvalue estimates keep the column order of the start, which need not be
+// sorted any more): rank each eigenvalue (ties by index), move column j of X
+// to column rank(j) of X2 and reorder w.
+__global__ void __launch_bounds__(128)
+k_sort_cols(const double* __restrict__ X, double* __restrict__ X2, double* __restrict__ w,
+            long stride, int ld, long wstride, const int* __restrict__ nsz) {
+    __shared__ double sw[128];
+    __shared__ int rank[128];
+    const int b = blockIdx.x, n = nsz[b];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sw[i] = w[b * wstride + i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double di = sw[i];
+        int r = 0;
+        for (int j = 0; j < n; ++j) r += (sw[j] < di || (sw[j] == di && j < i)) ? 1 : 0;
+        rank[i] = r < n ? r : n - 1;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[b * wstride + rank[i]] = sw[i];
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int r = t / n, j = t % n;
+        X2[b * stride + (long)r * ld + rank[j]] = X[b * stride + (long)r * ld + j];
+    }
+}
+
 // Frobenius norms of the batch matrices (delta of the refinement uses ||A||).
 __global__ void k_frob(const double* __restrict__ A, long stride, int ld, const int* __restrict__ nsz,
                        double* __restrict__ out) {
@@ -463,49 +514,60 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     k_frob<<<E.nb, 128, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
     MG_LAUNCHED(c);
     const int tiles = div_up(E.nmax, kTile) * div_up(E.nmax, kTile);
+    const SkipCtl none{nullptr, nullptr, 0, 0, 0.0};
+    if (E.skip_tol >= 0.0)
+        MG_CUDA(cudaMemsetAsync(E.done, 0x7f, (size_t)E.nb * sizeof(int), c->stream));
     for (int s = 0; s < nref; ++s) {
         // AX = A X ; S = X^T AX ; G = X^T X ; F = I + E ; X2 = X F ; X <- X2
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax);
+        SkipCtl sk{E.skip_tol >= 0.0 ? E.done : nullptr, E.offrel, s, 1, E.skip_tol};
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax, sk);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+        sk.decide = 0;
+        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, sk);
         MG_LAUNCHED(c);
         k_oa_rows<<<dim3(E.nmax, E.nb), 128, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz,
-                                                             E.w, E.wstride, E.part);
+                                                             E.w, E.wstride, E.part, sk);
         MG_LAUNCHED(c);
         k_oa_apply<<<dim3(E.nmax, E.nb), 128, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz,
                                                               E.anorm, E.w, E.wstride, E.part,
-                                                              E.emax);
+                                                              E.emax, E.offrel, sk);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, sk);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
     }
     // re-orthonormalise: G = X^T X, F = I + R/2 + 3/8 R^2, X <- X F
-    k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+    k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
     MG_LAUNCHED(c);
     k_orth_prep<<<dim3(div_up((long)E.nmax * E.nmax, kThreads), E.nb), kThreads, 0, c->stream>>>(
         E.G, E.AX, E.G, E.stride, E.ld, E.nsz);
     MG_LAUNCHED(c);
-    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_rr);
+    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_rr, none);
     MG_LAUNCHED(c);
-    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+    k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
     MG_LAUNCHED(c);
     MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                             cudaMemcpyDeviceToDevice, c->stream));
+    if (seed == kSeedRefine) {
+        k_sort_cols<<<E.nb, 128, 0, c->stream>>>(E.X, E.X2, E.w, E.stride, E.ld, E.wstride, E.nsz);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
+    }
     if (polish) {
         const int np = E.nmax + (E.nmax & 1);
         const size_t psm = (size_t)np * (np + 1) * sizeof(double);
         if (psm > 200 * 1024) return MG_ERR_ARG;
         // Rayleigh-Ritz matrix and the FP64 Jacobi polish
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax);
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax, none);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg);
+        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
         MG_LAUNCHED(c);
         k_jacobi64_polish<<<E.nb, kThreads, psm, c->stream>>>(
             E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, c->flags + 5);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf);
+        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
@@ -535,17 +597,19 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
     MG_CUDA(cudaMalloc(&E.part, (size_t)nb * ld * 2 * sizeof(double)));
     MG_CUDA(cudaMalloc(&E.emax, (size_t)nb * ld * sizeof(double)));
     MG_CUDA(cudaMemset(E.emax, 0, (size_t)nb * ld * sizeof(double)));
+    MG_CUDA(cudaMalloc(&E.done, (size_t)nb * sizeof(int)));
+    MG_CUDA(cudaMalloc(&E.offrel, (size_t)nb * sizeof(double)));
     std::vector<int> hn(nb);
     MG_CUDA(cudaMemcpy(hn.data(), nsz_dev, nb * sizeof(int), cudaMemcpyDeviceToHost));
     std::vector<GemmDesc> ax(nb), sg(2 * nb), xf(nb), rr(nb);
     for (int b = 0; b < nb; ++b) {
         const int n = hn[b];
         const long o = (long)b * stride;
-        ax[b] = GemmDesc{A + o, E.X + o, E.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
-        sg[2 * b] = GemmDesc{E.X + o, E.AX + o, E.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
-        sg[2 * b + 1] = GemmDesc{E.X + o, E.X + o, E.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
-        xf[b] = GemmDesc{E.X + o, E.G + o, E.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
-        rr[b] = GemmDesc{E.AX + o, E.AX + o, E.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0};
+        ax[b] = GemmDesc{A + o, E.X + o, E.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
+        sg[2 * b] = GemmDesc{E.X + o, E.AX + o, E.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+        sg[2 * b + 1] = GemmDesc{E.X + o, E.X + o, E.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+        xf[b] = GemmDesc{E.X + o, E.G + o, E.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
+        rr[b] = GemmDesc{E.AX + o, E.AX + o, E.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b};
     }
     MG_CUDA(cudaMalloc(&E.d_ax, nb * sizeof(GemmDesc)));
     MG_CUDA(cudaMalloc(&E.d_sg, 2 * nb * sizeof(GemmDesc)));
@@ -621,7 +685,8 @@ constexpr size_t kOffNsz = kOffDesc + kDescBytes;
 constexpr size_t kOffFlags = kOffNsz + round256(kNoAllocNb * sizeof(int));
 constexpr size_t kOffPart = kOffFlags + 256;
 constexpr size_t kOffEmax = kOffPart + (size_t)2 * kNoAllocNb * kNoAllocLd * sizeof(double);
-constexpr size_t kNoAllocBytes = kOffEmax + (size_t)kNoAllocNb * kNoAllocLd * sizeof(double);
+constexpr size_t kOffOffrel = kOffEmax + (size_t)kNoAllocNb * kNoAllocLd * sizeof(double);
+constexpr size_t kNoAllocBytes = kOffOffrel + kNoAllocNb * sizeof(double);
 // ~2.2 MiB
 
 // The whole workspace: four nb x ld x ld work matrices, norms, GEMM tables,
@@ -651,11 +716,11 @@ __global__ void k_eig_noalloc_tables(NoAllocArgs a, int* nsz, GemmDesc* ax, Gemm
     const int n = a.n[b], ld = a.ld;
     const long o = (long)b * ld * ld;
     nsz[b] = n;
-    ax[b] = GemmDesc{a.A + o, a.X + o, a.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
-    sg[2 * b] = GemmDesc{a.X + o, a.AX + o, a.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
-    sg[2 * b + 1] = GemmDesc{a.X + o, a.X + o, a.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0};
-    xf[b] = GemmDesc{a.X + o, a.G + o, a.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0};
-    rr[b] = GemmDesc{a.AX + o, a.AX + o, a.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0};
+    ax[b] = GemmDesc{a.A + o, a.X + o, a.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
+    sg[2 * b] = GemmDesc{a.X + o, a.AX + o, a.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+    sg[2 * b + 1] = GemmDesc{a.X + o, a.X + o, a.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+    xf[b] = GemmDesc{a.X + o, a.G + o, a.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
+    rr[b] = GemmDesc{a.AX + o, a.AX + o, a.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b};
 }
 
 // Once per device, with that device current: the scratch address, the
@@ -727,6 +792,7 @@ extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const doubl
     E.anorm = reinterpret_cast<double*>(base + kOffNorm);
     E.part = reinterpret_cast<double*>(base + kOffPart);
     E.emax = reinterpret_cast<double*>(base + kOffEmax);
+    E.offrel = reinterpret_cast<double*>(base + kOffOffrel);
     GemmDesc* desc = reinterpret_cast<GemmDesc*>(base + kOffDesc);
     E.d_ax = desc;
     E.d_sg = desc + nb;
@@ -761,7 +827,8 @@ namespace mg {
 
 void eig_free(EigBatch& E) {
     for (void* p : {(void*)E.X, (void*)E.X2, (void*)E.AX, (void*)E.S, (void*)E.G, (void*)E.w,
-                    (void*)E.anorm, (void*)E.part, (void*)E.emax, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
+                    (void*)E.anorm, (void*)E.part, (void*)E.emax, (void*)E.done,
+                    (void*)E.offrel, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
                     (void*)E.d_rr})
         if (p) cudaFree(p);
 }

@@ -36,6 +36,11 @@ namespace mg {
 namespace {
 
 constexpr int kThreads = 256;
+// Rotation angle |S_mn| / |E_m - E_n| between states of opposite
+// quasiparticle-energy sign below which the refinement step that measured it
+// leaves the positive/negative split exact to FP64 rounding (the angle left
+// is ~ tol^2).
+constexpr double kRefineTol = 1e-8;
 
 __device__ double cta_sum(double x, double* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -131,7 +136,7 @@ k_dn_dlambda(const double* __restrict__ X, const double* __restrict__ E,
 }
 
 // Per block: Tr rho (the particle number of HFBNumberofParticles) into
-// out[b], dN/dlambda into out[4 + b], and the largest opposite-sign coupling
+// out[b], dN/dlambda into out[4 + b], and the largest opposite-sign angle
 // seen by the last refinement step into out[8 + b].
 __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ hsz, int nmax,
                         const double* __restrict__ dpart, const double* __restrict__ emax,
@@ -285,6 +290,7 @@ int hfb_prepare(mg_ctx* c) {
     MG_CUDA(cudaMemcpy(H.cstart, cst.data(), 4 * sizeof(int), cudaMemcpyHostToDevice));
     MG_TRY(pairing_set_smem(c));
     MG_TRY(eig_setup(c, H.eT, 4, H.nmax, H.nsz_T, H.T, (long)H.nmax * H.nmax, H.nmax));
+    H.eT.skip_tol = 1e-10;
     MG_TRY(eig_setup(c, H.eR, 4, hmax, H.hsz, H.Rpp, (long)hmax * hmax, hmax));
     H.nref = c->p.precision == MG_FP64 ? 3 : 2;
     // canonical basis quantum numbers: block order (it, parity -1 then +1)
@@ -332,9 +338,11 @@ void hfb_free(mg_ctx* c) {
 // One particle-number evaluation at lambda (both isospins): T(lambda),
 // eigen-decomposition, rho, kappa, block traces and dN/dlambda.  The vectors
 // of the previous evaluation seed the refinement directly; when, before its
-// last step, states of opposite quasiparticle-energy sign were still coupled
-// by more than 1e-10 |T| (the start was too far for the quadratic regime),
-// the evaluation is redone from an FP32 Jacobi seed.
+// last step, states of opposite quasiparticle-energy sign were still mixed
+// by an angle above kRefineTol (the start was too far for the quadratic
+// regime), the evaluation is redone from an FP32 Jacobi seed.  Up to four
+// refinement steps run; a matrix whose off-diagonal part fell below 1e-10 of
+// its norm skips the remaining ones.
 static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out) {
     Hfb& H = c->hfb;
     double* hp = H.h_pinned;
@@ -346,7 +354,7 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     MG_LAUNCHED(c);
     int seed = H.eT.have_vectors ? kSeedRefine : kSeedCold;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        MG_TRY(eig_batched(c, H.eT, seed, H.nref, false));
+        MG_TRY(eig_batched(c, H.eT, seed, seed == kSeedRefine ? 4 : H.nref, false));
         H.eT.have_vectors = true;
         k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
             H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
@@ -360,7 +368,7 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
         const double em = std::max(std::max(hp[8], hp[9]), std::max(hp[10], hp[11]));
-        if (seed != kSeedRefine || em <= 1e-10) break;
+        if (seed != kSeedRefine || em <= kRefineTol) break;
         seed = kSeedJacobiWarm;
         ++H.reseeds;
     }

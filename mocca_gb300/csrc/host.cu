@@ -24,6 +24,7 @@ bool valid_basis(const mg_ctx* c, int b) {
 void free_all(mg_ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(c->mats);
+    F(c->mats32);
     for (int b = 0; b < 2; ++b) {
         Basis& B = c->bas[b];
         F(B.psi); F(B.der); F(B.lap); F(B.qn); F(B.occ); F(B.e); F(B.disp); F(B.jobs);
@@ -184,12 +185,19 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
         cudaMemset(c->flags, 0, 16 * sizeof(int)) != cudaSuccess ||
         cudaMallocHost(&c->h_cg_status, 4 * sizeof(int)) != cudaSuccess)
         return fail(MG_ERR_CUDA);
+    c->cur_precision = p->precision;
     if ((st = upload_matrices(c)) != MG_OK) return fail(st);
     if ((st = build_field_jobs(c)) != MG_OK) return fail(st);
     if (ev8 && p->coulomb_solver != 0) {
         if ((st = coulomb_setup(c)) != MG_OK) return fail(st);
     }
     *out = c;
+    return MG_OK;
+}
+
+extern "C" int mg_set_precision(mg_ctx* c, int precision) {
+    if (!c || (precision != MG_FP64 && precision != MG_MIXED)) return MG_ERR_ARG;
+    c->cur_precision = precision;
     return MG_OK;
 }
 

@@ -74,6 +74,7 @@ struct GemmDesc {
     int lda, ldb, ldc;
     int ta, tb;
     double alpha, beta;
+    int mat;   // matrix of the batch (for the refinement's early exit)
 };
 
 // A batch of small symmetric eigenproblems (eig.cu).
@@ -85,7 +86,10 @@ struct EigBatch {
     double *X = nullptr, *X2 = nullptr, *AX = nullptr, *S = nullptr, *G = nullptr, *w = nullptr,
            *anorm = nullptr;
     double* part = nullptr;   // nb * ld * 2 row sums of a refinement step
-    double* emax = nullptr;   // nb * ld largest opposite-sign coupling |S_ij|/|A| per row
+    double* emax = nullptr;   // nb * ld largest opposite-sign angle |S_ij|/|l_i - l_j| per row
+    int* done = nullptr;      // nb: first refinement step skipped (INT_MAX: none)
+    double* offrel = nullptr; // nb: |S - diag S|_F / |A|_F seen by the last refinement step
+    double skip_tol = -1.0;   // skip the remaining steps once offrel <= skip_tol (< 0: never)
     GemmDesc *d_ax = nullptr, *d_sg = nullptr, *d_xf = nullptr, *d_rr = nullptr;
     bool attr_done = false;
     bool have_vectors = false;
@@ -150,6 +154,9 @@ struct mg_ctx {
     // (stored transposed so consecutive output points read consecutive words)
     double* mats = nullptr;
     long mat_off[3][2][2];
+    float* mats32 = nullptr;      // double-float copy: hi, lo planes [q][round4(n)] per matrix
+    long mat32_off[3][2][2];
+    int cur_precision = MG_FP64;  // precision of the next kernels (MG_FP64 / MG_MIXED)
 
     mg::Basis bas[2];
     double* updates = nullptr;   // nwt*4V heavy-ball history

@@ -62,6 +62,10 @@ class MeshState:
         except Exception:
             pass
 
+    def set_precision(self, precision: int):
+        """MG_FP64 or MG_MIXED for the following calls (mixed iterations, FP64 polish)."""
+        self._call("mg_set_precision", precision)
+
     def __enter__(self):
         return self
 

@@ -1,8 +1,8 @@
 """GPU parity of the HFB pairing step against the CPU oracle.
 
 The oracle follows the reference's damped Broyden Fermi solver and its
-EISPACK-style eigensolver; the GPU uses a secant root finder and its own
-CTA eigensolver.  Both stop at |N - N0| < 1e-12, so the converged states
+EISPACK-style eigensolver; the GPU uses a Newton root finder (analytic
+dN/dlambda) and its batched Jacobi + refinement eigensolver.  Both stop at |N - N0| < 1e-12, so the converged states
 agree to ~1e-12: rho, kappa, Delta and the pairing field are compared
 norm-wise at 1e-10, the canonical densities at 1e-10, energies at 1e-8 MeV.
 rho and kappa are projector blocks of the positive quasiparticle space and

@@ -1,0 +1,88 @@
+"""Mixed-precision path (MG_MIXED): double-float (FP32 pair) derivative
+contractions with FP64 storage, checked against the FP64 oracle, and the
+mixed iterations followed by an FP64 polish checked against the plain FP64
+GPU path.
+
+Bars: derivatives and Laplacians within 1e-11 relative (norm-wise): inputs
+and matrices carry 48 significant bits and the sums are carried as (hi, lo)
+pairs, so the error is a few units of 2^-48 times the cancellation of the
+sums.  After mixed iterations and an FP64 polish the total energy agrees
+with the all-FP64 run to 1e-5 MeV.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import rel
+from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, _abi, synthetic
+from mocca_gb300.mesh import MeshState
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,nwt", [(10, 8), (13, 6), (24, 8)])
+def test_mixed_derivatives_ev8(built, n, nwt):
+    p = RunParams(nx=n, ny=n, nz=n, dx=0.8, nwt=nwt, neutrons=8, protons=8, precision=MG_MIXED)
+    psi, qn, en = synthetic.ho_basis(p, nwt // 2, seed=5)
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    for s in (g, o):
+        s.set_spinors(psi, qn)
+        s.set_energies(en)
+    g.DeriveAll()
+    o.DeriveAll()
+    dg, lg = g.get_derivatives()
+    do, lo = o.get_derivatives()
+    assert rel(dg, do) < 1e-11
+    assert rel(lg, lo) < 1e-11
+    assert rel(dg, do) > 1e-15   # the double-float kernels ran, not the FP64 ones
+    g.set_precision(MG_FP64)
+    g.DeriveAll()
+    dg, lg = g.get_derivatives()
+    assert rel(dg, do) < 1e-12 and rel(lg, lo) < 1e-12
+    g.close()
+
+
+def test_mixed_derivatives_full_box(built):
+    p = RunParams(nx=12, ny=12, nz=12, dx=0.8, pc=0, sc=0, tsc=0, trc=1, nwt=6,
+                  neutrons=8, protons=8, coulomb_solver=0, precision=MG_MIXED)
+    psi = synthetic.gaussian_hermite_spinors(p, p.nwt, seed=42)
+    qn = np.tile(np.array([-1, 0, 0, 0], dtype=np.int32), (p.nwt, 1))
+    qn[3:, 0] = 1
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    for s in (g, o):
+        s.set_spinors(psi, qn)
+        s.set_energies(np.zeros(p.nwt))
+    g.DeriveAll()
+    o.DeriveAll()
+    dg, lg = g.get_derivatives()
+    do, lo = o.get_derivatives()
+    assert rel(dg, do) < 1e-11
+    assert rel(lg, lo) < 1e-11
+    g.close()
+
+
+def _hfb(precision):
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB, precision=precision)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    g = MeshState(p, SLY4)
+    g.set_spinors(psi, qn)
+    g.set_energies(en)
+    g.set_pairing()
+    g.Start()
+    return g
+
+
+def test_mixed_iterations_with_fp64_polish(built):
+    ref = _hfb(MG_FP64)
+    e_ref = ref.Evolve(40, 0.01, 0.3)["total"]
+    mix = _hfb(MG_MIXED)
+    e_mid = mix.Evolve(30, 0.01, 0.3)["total"]
+    mix.set_precision(MG_FP64)
+    e_mix = mix.Evolve(10, 0.01, 0.3)["total"]
+    assert np.isfinite(e_mid)
+    assert abs(e_mix - e_ref) <= 1e-5, (e_mix, e_ref)
+    ref.close()
+    mix.close()
