@@ -1,4 +1,5 @@
-// density.cu -- density accumulation over the density basis, FP64.
+// density.cu -- density accumulation over the density basis, FP64 (double-float
+// in the mixed form).
 //
 // Replaces ComputeDensity (src/Densities.f90:431-550) for time-reversal
 // invariant functionals without tensor / N2LO terms:
@@ -10,6 +11,7 @@
 // in index order for one mesh point (16 doubles per spwf, coalesced along
 // x), writes six group partials, and k_dens_reduce adds the groups in order,
 // so the result is deterministic.
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -73,6 +75,81 @@ k_dens_partial(const double* __restrict__ psi, const double* __restrict__ der,
         for (int q = 0; q < 3; ++q) pg[(q * 2 + it) * V + v] = acc[it][q];
 }
 
+// Mixed form: the same sums in double-float from double-float derivatives
+// (psi split from its FP64 bits); group partials leave as FP64.
+__device__ __forceinline__ void imag_acc(float& sh, float& sl, const dfl* a, const dfl* b,
+                                         float sgn) {
+    // sgn * (a0 b1 - a1 b0 + a2 b3 - a3 b2)
+    const dfl s{sgn, 0.0f}, m{-sgn, 0.0f};
+    df_acc(sh, sl, df_mul(s, a[0]), b[1]);
+    df_acc(sh, sl, df_mul(m, a[1]), b[0]);
+    df_acc(sh, sl, df_mul(s, a[2]), b[3]);
+    df_acc(sh, sl, df_mul(m, a[3]), b[2]);
+}
+
+__device__ __forceinline__ void pauli_df(const dfl* p, int dir, dfl* o) {
+    if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
+    else if (dir == 2) { o[0] = p[3]; o[1] = df_neg(p[2]); o[2] = df_neg(p[1]); o[3] = p[0]; }
+    else { o[0] = p[0]; o[1] = p[1]; o[2] = df_neg(p[2]); o[3] = df_neg(p[3]); }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_dens_partial_df(const double* __restrict__ psi, const float2* __restrict__ der,
+                  const double* __restrict__ occ, const int* __restrict__ qn, int nwt,
+                  int per_group, long V, double* __restrict__ part) {
+    const long v = (long)blockIdx.x * kThreads + threadIdx.x;
+    const int g = blockIdx.y;
+    if (v >= V) return;
+    // per isospin (n: 0, p: 1) accumulators of rho, tau, divJ; kept in named
+    // registers (a runtime-indexed array would live in local memory)
+    float nh[3] = {0.f, 0.f, 0.f}, nl[3] = {0.f, 0.f, 0.f};
+    float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
+    const int i0 = g * per_group, i1 = min(nwt, i0 + per_group);
+    for (int i = i0; i < i1; ++i) {
+        const double o64 = occ[i];
+        if (o64 == 0.0) continue;
+        const dfl o = df_split(o64);
+        const int it = (qn[4 * i] + 3) / 2 - 1;
+        const double* ps = psi + (long)i * 4 * V;
+        const float2* dr = der + (long)i * 12 * V;
+        dfl p[4], d[3][4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            p[l] = df_split(ps[l * V + v]);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) d[m][l] = df_ld(dr + (m * 4 + l) * V + v);
+        }
+        float dh = 0.f, dl = 0.f, th = 0.f, tl = 0.f, jh = 0.f, jl = 0.f;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) df_acc(dh, dl, p[l], p[l]);
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int l = 0; l < 4; ++l) df_acc(th, tl, d[m][l], d[m][l]);
+        dfl s[4];
+        pauli_df(d[1], 3, s); imag_acc(jh, jl, d[0], s, 1.0f);
+        pauli_df(d[2], 2, s); imag_acc(jh, jl, d[0], s, -1.0f);
+        pauli_df(d[1], 1, s); imag_acc(jh, jl, d[2], s, -1.0f);
+        pauli_df(d[0], 2, s); imag_acc(jh, jl, d[2], s, 1.0f);
+        pauli_df(d[0], 3, s); imag_acc(jh, jl, d[1], s, -1.0f);
+        pauli_df(d[2], 1, s); imag_acc(jh, jl, d[1], s, 1.0f);
+        const dfl q3[3] = {df_norm(dfl{dh, dl}), df_norm(dfl{th, tl}), df_norm(dfl{jh, jl})};
+        if (it == 0) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) df_acc(nh[q], nl[q], o, q3[q]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) df_acc(ph[q], pl[q], o, q3[q]);
+        }
+    }
+    double* pg = part + (long)g * 6 * V;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        pg[(q * 2 + 0) * V + v] = df_to(dfl{nh[q], nl[q]});
+        pg[(q * 2 + 1) * V + v] = df_to(dfl{ph[q], pl[q]});
+    }
+}
+
 __global__ void k_dens_reduce(const double* __restrict__ part, int ngroups, long V,
                               double* __restrict__ rho, double* __restrict__ tau,
                               double* __restrict__ nablaj) {
@@ -103,8 +180,12 @@ int densities(mg_ctx* c) {
     const int ng = density_groups(c);
     const int per = div_up(c->p.nwt, ng);
     dim3 grid(div_up(V, kThreads), ng);
-    k_dens_partial<<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.occ, B.qn, c->p.nwt, per, V,
-                                                     c->red);
+    if (B.der_df)
+        k_dens_partial_df<<<grid, kThreads, 0, c->stream>>>(
+            B.psi, reinterpret_cast<const float2*>(B.der), B.occ, B.qn, c->p.nwt, per, V, c->red);
+    else
+        k_dens_partial<<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.occ, B.qn, c->p.nwt, per,
+                                                         V, c->red);
     MG_LAUNCHED(c);
     k_dens_reduce<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(c->red, ng, V, c->rho, c->tau,
                                                                    c->nablaj);

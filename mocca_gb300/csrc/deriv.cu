@@ -17,6 +17,7 @@
 // (consecutive output points i) read consecutive shared-memory words.
 #include <algorithm>
 
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -132,14 +133,10 @@ k_deriv_z(const GridJob* __restrict__ jobs, MatPtrs mp, int nx, int ny, int nz) 
 
 // ---- mixed precision: double-float arithmetic, FP64 grids in and out -------------
 //
-// GB300 issues FP32 at ~70x its FP64 rate, so the mixed form evaluates the
-// contractions in double-float: every FP64 value is split into an unevaluated
-// sum hi + lo of two floats (48 significant bits), products are formed
-// exactly with an FMA (TwoProduct) and the running sum is carried as a
-// (hi, lo) pair with Knuth's TwoSum (Dekker 1971, "A floating-point
-// technique for extending the available precision", Numer. Math. 18).  The
-// result is FP64-accurate to ~1e-14 relative at ~12 FP32 operations per
-// term.  Each thread owns four consecutive outputs along the contracted axis
+// The mixed form evaluates the contractions in double-float (df.cuh): every
+// FP64 value is split into hi + lo floats, products are exact FMA residuals
+// and the running sum is a (hi, lo) pair (df_acc), ~1e-14 relative at ~12
+// FP32 operations per term.  Each thread owns four consecutive outputs along the contracted axis
 // (or four rows for d/dx), so every shared-memory pair it loads feeds four or
 // eight terms.  Matrices are stored transposed as (hi, lo) float planes with
 // a row stride rounded up to a multiple of 4 (zero padding).
@@ -149,30 +146,10 @@ struct MatPtrs32 {
     int ld4[3];
 };
 
-// s += a * b in double-float.  The rounded product and the TwoSum steps use
-// the _rn intrinsics so that the compiler cannot fuse them into FMAs (which
-// would change the rounding the error terms rely on).
-__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh,
-                                       float bl) {
-    const float ph = __fmul_rn(ah, bh);
-    float pl = fmaf(ah, bh, -ph);
-    pl = fmaf(ah, bl, pl);
-    pl = fmaf(al, bh, pl);
-    const float t = __fadd_rn(sh, ph);
-    const float bp = __fsub_rn(t, sh);
-    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
-    sh = t;
-    sl += e + pl;
-}
-
-__device__ __forceinline__ void df_split(double x, float& h, float& l) {
-    h = (float)x;
-    l = (float)(x - (double)h);
-}
 
 __global__ void __launch_bounds__(256)
 k_deriv_xy_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int nz,
-              int planes_per_block) {
+              int planes_per_block, int out_df) {
     extern __shared__ float smf[];
     const GridJob J = jobs[blockIdx.x];
     const bool want_x = J.dx != nullptr || J.lap != nullptr;
@@ -210,7 +187,11 @@ k_deriv_xy_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, in
     for (int k = k0; k < k1; ++k) {
         const double* in = J.in + (long)k * plane;
         __syncthreads();
-        for (int t = threadIdx.x; t < plane; t += blockDim.x) df_split(in[t], sPh[t], sPl[t]);
+        for (int t = threadIdx.x; t < plane; t += blockDim.x) {
+            const dfl v = df_split(in[t]);
+            sPh[t] = v.h;
+            sPl[t] = v.l;
+        }
         __syncthreads();
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
             const int x = it % nx, y0 = 4 * (it / nx);
@@ -225,8 +206,8 @@ k_deriv_xy_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, in
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         const float vh = sPh[(y0 + j) * nx + q], vl = sPl[(y0 + j) * nx + q];
-                        df_fma(axh[j], axl[j], dh, dl, vh, vl);
-                        df_fma(bxh[j], bxl[j], lh, ll, vh, vl);
+                        df_acc(axh[j], axl[j], dfl{dh, dl}, dfl{vh, vl});
+                        df_acc(bxh[j], bxl[j], dfl{lh, ll}, dfl{vh, vl});
                     }
                 }
             }
@@ -237,31 +218,39 @@ k_deriv_xy_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, in
                     const float4 dl = *reinterpret_cast<const float4*>(sDy + my + q * ly + y0);
                     const float4 lh = *reinterpret_cast<const float4*>(sLy + q * ly + y0);
                     const float4 ll = *reinterpret_cast<const float4*>(sLy + my + q * ly + y0);
-                    df_fma(ayh[0], ayl[0], dh.x, dl.x, vh, vl);
-                    df_fma(ayh[1], ayl[1], dh.y, dl.y, vh, vl);
-                    df_fma(ayh[2], ayl[2], dh.z, dl.z, vh, vl);
-                    df_fma(ayh[3], ayl[3], dh.w, dl.w, vh, vl);
-                    df_fma(byh[0], byl[0], lh.x, ll.x, vh, vl);
-                    df_fma(byh[1], byl[1], lh.y, ll.y, vh, vl);
-                    df_fma(byh[2], byl[2], lh.z, ll.z, vh, vl);
-                    df_fma(byh[3], byl[3], lh.w, ll.w, vh, vl);
+                    df_acc(ayh[0], ayl[0], dfl{dh.x, dl.x}, dfl{vh, vl});
+                    df_acc(ayh[1], ayl[1], dfl{dh.y, dl.y}, dfl{vh, vl});
+                    df_acc(ayh[2], ayl[2], dfl{dh.z, dl.z}, dfl{vh, vl});
+                    df_acc(ayh[3], ayl[3], dfl{dh.w, dl.w}, dfl{vh, vl});
+                    df_acc(byh[0], byl[0], dfl{lh.x, ll.x}, dfl{vh, vl});
+                    df_acc(byh[1], byl[1], dfl{lh.y, ll.y}, dfl{vh, vl});
+                    df_acc(byh[2], byl[2], dfl{lh.z, ll.z}, dfl{vh, vl});
+                    df_acc(byh[3], byl[3], dfl{lh.w, ll.w}, dfl{vh, vl});
                 }
             }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (y0 + j >= ny) break;
                 const long o = (long)k * plane + (long)(y0 + j) * nx + x;
-                if (J.dx) J.dx[o] = (double)axh[j] + (double)axl[j];
-                if (J.dy) J.dy[o] = (double)ayh[j] + (double)ayl[j];
-                if (J.lap)
-                    J.lap[o] = ((double)bxh[j] + (double)bxl[j]) + ((double)byh[j] + (double)byl[j]);
+                const dfl ox = df_norm(dfl{axh[j], axl[j]}), oy = df_norm(dfl{ayh[j], ayl[j]});
+                const dfl ol = df_add(df_norm(dfl{bxh[j], bxl[j]}), df_norm(dfl{byh[j], byl[j]}));
+                if (out_df) {
+                    if (J.dx) df_st(reinterpret_cast<float2*>(J.dx) + o, ox);
+                    if (J.dy) df_st(reinterpret_cast<float2*>(J.dy) + o, oy);
+                    if (J.lap) df_st(reinterpret_cast<float2*>(J.lap) + o, ol);
+                } else {
+                    if (J.dx) J.dx[o] = df_to(ox);
+                    if (J.dy) J.dy[o] = df_to(oy);
+                    if (J.lap) J.lap[o] = df_to(ol);
+                }
             }
         }
     }
 }
 
 __global__ void __launch_bounds__(512)
-k_deriv_z_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int nz) {
+k_deriv_z_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int nz,
+             int out_df) {
     extern __shared__ float smf[];
     const GridJob J = jobs[blockIdx.x];
     if (J.dz == nullptr && J.lap == nullptr) return;
@@ -281,8 +270,9 @@ k_deriv_z_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int
     const int c0 = blockIdx.y * kColTile;
     for (int t = threadIdx.x; t < nz * kColTile; t += blockDim.x) {
         const int q = t / kColTile, cc = t % kColTile;
-        const double v = (c0 + cc < plane) ? J.in[(long)q * plane + c0 + cc] : 0.0;
-        df_split(v, sGh[t], sGl[t]);
+        const dfl v = df_split((c0 + cc < plane) ? J.in[(long)q * plane + c0 + cc] : 0.0);
+        sGh[t] = v.h;
+        sGl[t] = v.l;
     }
     __syncthreads();
     const int nz4 = (nz + 3) / 4;
@@ -297,21 +287,30 @@ k_deriv_z_df(const GridJob* __restrict__ jobs, MatPtrs32 mp, int nx, int ny, int
             const float4 dl = *reinterpret_cast<const float4*>(sDz + mz + q * lz + i0);
             const float4 lh = *reinterpret_cast<const float4*>(sLz + q * lz + i0);
             const float4 ll = *reinterpret_cast<const float4*>(sLz + mz + q * lz + i0);
-            df_fma(azh[0], azl[0], dh.x, dl.x, vh, vl);
-            df_fma(azh[1], azl[1], dh.y, dl.y, vh, vl);
-            df_fma(azh[2], azl[2], dh.z, dl.z, vh, vl);
-            df_fma(azh[3], azl[3], dh.w, dl.w, vh, vl);
-            df_fma(bzh[0], bzl[0], lh.x, ll.x, vh, vl);
-            df_fma(bzh[1], bzl[1], lh.y, ll.y, vh, vl);
-            df_fma(bzh[2], bzl[2], lh.z, ll.z, vh, vl);
-            df_fma(bzh[3], bzl[3], lh.w, ll.w, vh, vl);
+            df_acc(azh[0], azl[0], dfl{dh.x, dl.x}, dfl{vh, vl});
+            df_acc(azh[1], azl[1], dfl{dh.y, dl.y}, dfl{vh, vl});
+            df_acc(azh[2], azl[2], dfl{dh.z, dl.z}, dfl{vh, vl});
+            df_acc(azh[3], azl[3], dfl{dh.w, dl.w}, dfl{vh, vl});
+            df_acc(bzh[0], bzl[0], dfl{lh.x, ll.x}, dfl{vh, vl});
+            df_acc(bzh[1], bzl[1], dfl{lh.y, ll.y}, dfl{vh, vl});
+            df_acc(bzh[2], bzl[2], dfl{lh.z, ll.z}, dfl{vh, vl});
+            df_acc(bzh[3], bzl[3], dfl{lh.w, ll.w}, dfl{vh, vl});
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (i0 + j >= nz) break;
             const long o = (long)(i0 + j) * plane + c0 + col;
-            if (J.dz) J.dz[o] = (double)azh[j] + (double)azl[j];
-            if (J.lap) J.lap[o] = J.lap[o] + ((double)bzh[j] + (double)bzl[j]);
+            const dfl oz = df_norm(dfl{azh[j], azl[j]}), olz = df_norm(dfl{bzh[j], bzl[j]});
+            if (out_df) {
+                if (J.dz) df_st(reinterpret_cast<float2*>(J.dz) + o, oz);
+                if (J.lap) {
+                    float2* pl = reinterpret_cast<float2*>(J.lap) + o;
+                    df_st(pl, df_add(df_ld(pl), olz));
+                }
+            } else {
+                if (J.dz) J.dz[o] = df_to(oz);
+                if (J.lap) J.lap[o] = J.lap[o] + df_to(olz);
+            }
         }
     }
 }
@@ -415,7 +414,7 @@ int build_basis_jobs(mg_ctx* c, int b) {
     return MG_OK;
 }
 
-int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
+int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     if (njobs <= 0) return MG_OK;
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     const int ppb = 4;
@@ -432,6 +431,7 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
         attr_done = true;
     }
     if (c->cur_precision == MG_MIXED) {
+        // out_df: the outputs stay double-float ({hi, lo} float pairs)
         MatPtrs32 mp = mat_ptrs32(c);
         const int ny4 = (ny + 3) / 4, nz4 = (nz + 3) / 4;
         const size_t sm_xy =
@@ -440,13 +440,14 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
         const int txy = std::min(256, div_up((long)nx * ny4, 32) * 32);
         const int tz = std::min(512, kColTile * nz4);
         k_deriv_xy_df<<<dim3(njobs, div_up(nz, ppb)), txy, sm_xy, c->stream>>>(jobs, mp, nx, ny,
-                                                                             nz, ppb);
+                                                                             nz, ppb, out_df);
         MG_LAUNCHED(c);
         k_deriv_z_df<<<dim3(njobs, div_up((long)nx * ny, kColTile)), tz, sm_z, c->stream>>>(
-            jobs, mp, nx, ny, nz);
+            jobs, mp, nx, ny, nz, out_df ? 1 : 0);
         MG_LAUNCHED(c);
         return MG_OK;
     }
+    if (out_df) return MG_ERR_STATE;   // double-float outputs only from the mixed kernels
     MatPtrs mp = mat_ptrs(c);
     size_t sm_xy = (size_t)(2 * nx * nx + 2 * ny * ny + nx * ny) * sizeof(double);
     size_t sm_z = (size_t)(2 * nz * nz + nz * kColTile) * sizeof(double);
@@ -459,9 +460,15 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs) {
     return MG_OK;
 }
 
+// In the mixed form the basis derivatives stay double-float in HBM (the same
+// 8 bytes per value), so that h.psi and the densities read them without FP64
+// conversions; Basis::der_df records the format.
 int derive_basis(mg_ctx* c, int b) {
     if (!c->bas[b].have_qn) return MG_ERR_STATE;
-    return run_jobs(c, c->bas[b].jobs, 4 * c->p.nwt);
+    const bool df = c->cur_precision == MG_MIXED;
+    MG_TRY(run_jobs(c, c->bas[b].jobs, 4 * c->p.nwt, df));
+    c->bas[b].der_df = df;
+    return MG_OK;
 }
 
 }  // namespace mg

@@ -345,7 +345,7 @@ k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, in
 __global__ void __launch_bounds__(kThreads)
 k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* __restrict__ nsz,
                   const double* __restrict__ anorm, double* __restrict__ Q,
-                  double* __restrict__ w, long wstride, int* __restrict__ flag) {
+                  double* __restrict__ w, long wstride, int* __restrict__ pfail) {
     extern __shared__ double smd[];
     __shared__ double red[32];
     __shared__ double cs[2][64];
@@ -374,22 +374,38 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     const int half = n / 2;
     int sweep = 0;
     for (; sweep < 12; ++sweep) {
+        // a pair rotates when its coupling is above the rounding level of S and
+        // its rotation angle ~ |a_pq| / |a_qq - a_pp| is representable (pairs
+        // far apart whose coupling is rounding noise stay put)
         int any = 0;
         if (lane < n)
-            for (int i = kg; i < n; i += 2)
-                if (i != lane && fabs(a[i * l2 + lane]) > thr) any = 1;
+            for (int i = kg; i < n; i += 2) {
+                const double x = fabs(a[i * l2 + lane]);
+                if (i != lane && x > thr && x > 1e-16 * fabs(a[i * l2 + i] - a[lane * l2 + lane]))
+                    any = 1;
+            }
         if (!__syncthreads_or(any)) break;
         for (int r = 0; r < n - 1; ++r) {
             int on = 0;
             if (tid < half) {
                 const int p = rr_player(tid, r, n), qq = rr_player(n - 1 - tid, r, n);
                 const double apq = a[p * l2 + qq];
+                const double d = a[qq * l2 + qq] - a[p * l2 + p];
                 double c = 1.0, s = 0.0;
-                if (fabs(apq) > thr) {
-                    const double th = (a[qq * l2 + qq] - a[p * l2 + p]) / (2.0 * apq);
-                    const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-                    c = 1.0 / sqrt(tt * tt + 1.0);
-                    s = tt * c;
+                if (fabs(apq) > thr && fabs(apq) > 1e-16 * fabs(d)) {
+                    if (fabs(d) > 1e8 * fabs(apq)) {
+                        // small angle: tan = a_pq / d to 1/(4 tau^2) < 1e-16 relative
+                        // (FP64 divides and square roots are slow on this part)
+                        const double tt = apq / d;
+                        c = 1.0 - 0.5 * tt * tt;
+                        s = tt * c;
+                    } else {
+                        const double th = d / (2.0 * apq);
+                        const double tt =
+                            (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                        c = 1.0 / sqrt(tt * tt + 1.0);
+                        s = tt * c;
+                    }
                     on = 1;
                 }
                 cs[0][tid] = c;
@@ -427,7 +443,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
             __syncthreads();
         }
     }
-    if (sweep == 12 && tid == 0 && flag) atomicExch(flag, 1);
+    if (tid == 0 && pfail) pfail[b] = sweep == 12 ? 1 : 0;
     for (int i = tid; i < n0; i += kThreads) w[b * wstride + i] = a[i * l2 + i];
 }
 
@@ -549,12 +565,6 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     MG_LAUNCHED(c);
     MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                             cudaMemcpyDeviceToDevice, c->stream));
-    if (seed == kSeedRefine) {
-        k_sort_cols<<<E.nb, 128, 0, c->stream>>>(E.X, E.X2, E.w, E.stride, E.ld, E.wstride, E.nsz);
-        MG_LAUNCHED(c);
-        MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
-                                cudaMemcpyDeviceToDevice, c->stream));
-    }
     if (polish) {
         const int np = E.nmax + (E.nmax & 1);
         const size_t psm = (size_t)np * (np + 1) * sizeof(double);
@@ -565,9 +575,17 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
         MG_LAUNCHED(c);
         k_jacobi64_polish<<<E.nb, kThreads, psm, c->stream>>>(
-            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, c->flags + 5);
+            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail);
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
+    }
+    // ascending order: the refinement keeps the column order of its start and
+    // the polish leaves diag(S) in place
+    if (seed == kSeedRefine || polish) {
+        k_sort_cols<<<E.nb, 128, 0, c->stream>>>(E.X, E.X2, E.w, E.stride, E.ld, E.wstride, E.nsz);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
@@ -599,6 +617,8 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
     MG_CUDA(cudaMemset(E.emax, 0, (size_t)nb * ld * sizeof(double)));
     MG_CUDA(cudaMalloc(&E.done, (size_t)nb * sizeof(int)));
     MG_CUDA(cudaMalloc(&E.offrel, (size_t)nb * sizeof(double)));
+    MG_CUDA(cudaMalloc(&E.pfail, (size_t)nb * sizeof(int)));
+    MG_CUDA(cudaMemset(E.pfail, 0, (size_t)nb * sizeof(int)));
     std::vector<int> hn(nb);
     MG_CUDA(cudaMemcpy(hn.data(), nsz_dev, nb * sizeof(int), cudaMemcpyDeviceToHost));
     std::vector<GemmDesc> ax(nb), sg(2 * nb), xf(nb), rr(nb);
@@ -686,7 +706,8 @@ constexpr size_t kOffFlags = kOffNsz + round256(kNoAllocNb * sizeof(int));
 constexpr size_t kOffPart = kOffFlags + 256;
 constexpr size_t kOffEmax = kOffPart + (size_t)2 * kNoAllocNb * kNoAllocLd * sizeof(double);
 constexpr size_t kOffOffrel = kOffEmax + (size_t)kNoAllocNb * kNoAllocLd * sizeof(double);
-constexpr size_t kNoAllocBytes = kOffOffrel + kNoAllocNb * sizeof(double);
+constexpr size_t kOffPfail = kOffOffrel + kNoAllocNb * sizeof(double);
+constexpr size_t kNoAllocBytes = kOffPfail + kNoAllocNb * sizeof(int);
 // ~2.2 MiB
 
 // The whole workspace: four nb x ld x ld work matrices, norms, GEMM tables,
@@ -793,6 +814,7 @@ extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const doubl
     E.part = reinterpret_cast<double*>(base + kOffPart);
     E.emax = reinterpret_cast<double*>(base + kOffEmax);
     E.offrel = reinterpret_cast<double*>(base + kOffOffrel);
+    E.pfail = reinterpret_cast<int*>(base + kOffPfail);
     GemmDesc* desc = reinterpret_cast<GemmDesc*>(base + kOffDesc);
     E.d_ax = desc;
     E.d_sg = desc + nb;
@@ -828,7 +850,7 @@ namespace mg {
 void eig_free(EigBatch& E) {
     for (void* p : {(void*)E.X, (void*)E.X2, (void*)E.AX, (void*)E.S, (void*)E.G, (void*)E.w,
                     (void*)E.anorm, (void*)E.part, (void*)E.emax, (void*)E.done,
-                    (void*)E.offrel, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
+                    (void*)E.offrel, (void*)E.pfail, (void*)E.d_ax, (void*)E.d_sg, (void*)E.d_xf,
                     (void*)E.d_rr})
         if (p) cudaFree(p);
 }

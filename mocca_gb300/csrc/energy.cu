@@ -17,14 +17,24 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kTerms = 20;
 
-// per-spwf dot products over 4V, block partials
+// per-spwf dot products over 4V, block partials (b as double-float pairs when
+// kBdf: the Laplacians of the mixed form)
+template <bool kBdf>
 __global__ void __launch_bounds__(kThreads)
 k_dots(const double* __restrict__ a, const double* __restrict__ b, long V4,
        double* __restrict__ part) {
     const int i = blockIdx.y;
     double s = 0.0;
-    for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4; o += (long)gridDim.x * kThreads)
-        s = fma(a[(long)i * V4 + o], b[(long)i * V4 + o], s);
+    for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4; o += (long)gridDim.x * kThreads) {
+        double bv;
+        if (kBdf) {
+            const float2 p = reinterpret_cast<const float2*>(b)[(long)i * V4 + o];
+            bv = (double)p.x + (double)p.y;
+        } else {
+            bv = b[(long)i * V4 + o];
+        }
+        s = fma(a[(long)i * V4 + o], bv, s);
+    }
     __shared__ double red[kThreads / 32];
     for (int q = 16; q > 0; q >>= 1) s += __shfl_xor_sync(0xffffffffu, s, q);
     if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = s;
@@ -91,10 +101,13 @@ k_energy_partial(const double* __restrict__ rho, const double* __restrict__ tau,
 }  // namespace
 
 // nwt dot products <a_i|b_i> * dv of a basis into host array out.
-int basis_dots(mg_ctx* c, const double* a, const double* b, double* out) {
+int basis_dots(mg_ctx* c, const double* a, const double* b, double* out, bool b_df) {
     const long V4 = 4 * c->V;
     const int nch = std::max(1, std::min(64, div_up(V4, kThreads * 8)));
-    k_dots<<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
+    if (b_df)
+        k_dots<true><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
+    else
+        k_dots<false><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
     MG_LAUNCHED(c);
     std::vector<double> h((size_t)nch * c->p.nwt);
     MG_CUDA(cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
@@ -116,7 +129,7 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     const long V = c->V;
     const mg_skyrme_b& B = c->B;
     std::vector<double> ip(nwt);
-    MG_TRY(basis_dots(c, D.psi, D.lap, ip.data()));
+    MG_TRY(basis_dots(c, D.psi, D.lap, ip.data(), D.der_df));
     std::vector<double> occ(nwt), e(nwt);
     MG_CUDA(cudaMemcpyAsync(occ.data(), D.occ, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaMemcpyAsync(e.data(), D.e, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

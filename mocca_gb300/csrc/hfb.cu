@@ -136,8 +136,8 @@ k_dn_dlambda(const double* __restrict__ X, const double* __restrict__ E,
 }
 
 // Per block: Tr rho (the particle number of HFBNumberofParticles) into
-// out[b], dN/dlambda into out[4 + b], and the largest opposite-sign angle
-// seen by the last refinement step into out[8 + b].
+// out[b], dN/dlambda into out[4 + b], and the largest opposite-sign rotation
+// angle seen by the last refinement step into out[8 + b].
 __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ hsz, int nmax,
                         const double* __restrict__ dpart, const double* __restrict__ emax,
                         double* __restrict__ out) {
@@ -292,7 +292,7 @@ int hfb_prepare(mg_ctx* c) {
     MG_TRY(eig_setup(c, H.eT, 4, H.nmax, H.nsz_T, H.T, (long)H.nmax * H.nmax, H.nmax));
     H.eT.skip_tol = 1e-10;
     MG_TRY(eig_setup(c, H.eR, 4, hmax, H.hsz, H.Rpp, (long)hmax * hmax, hmax));
-    H.nref = c->p.precision == MG_FP64 ? 3 : 2;
+    H.nref = 3;
     // canonical basis quantum numbers: block order (it, parity -1 then +1)
     std::vector<int> cqn(4 * nwt);
     for (int b = 0; b < 4; ++b)
@@ -336,14 +336,18 @@ void hfb_free(mg_ctx* c) {
 }
 
 // One particle-number evaluation at lambda (both isospins): T(lambda),
-// eigen-decomposition, rho, kappa, block traces and dN/dlambda.  The vectors
-// of the previous evaluation seed the refinement directly; when, before its
-// last step, states of opposite quasiparticle-energy sign were still mixed
-// by an angle above kRefineTol (the start was too far for the quadratic
-// regime), the evaluation is redone from an FP32 Jacobi seed.  Up to four
-// refinement steps run; a matrix whose off-diagonal part fell below 1e-10 of
-// its norm skips the remaining ones.
-static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out) {
+// eigen-decomposition, rho, kappa, block traces and dN/dlambda.  The first
+// evaluation of a pairing step (T changed with the mean fields) starts from
+// an FP32 Jacobi seed warm-started from the previous vectors; the later ones
+// (only lambda moved) refine the previous vectors directly, up to four steps,
+// a matrix whose off-diagonal part fell below 1e-10 of its norm skipping the
+// rest.  An FP64 Jacobi polish of X^T T X then rotates the pairs the
+// refinement leaves coupled inside its clusters (a quasiparticle pair close
+// to zero energy decides the particle number).  If before the last step
+// states of opposite sign were still mixed by an angle above kRefineTol, the
+// evaluation is redone from the Jacobi seed.
+static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out,
+                        bool first) {
     Hfb& H = c->hfb;
     double* hp = H.h_pinned;
     hp[24] = lam[0];
@@ -352,9 +356,9 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     k_build_T<<<dim3(div_up(H.nmax * H.nmax, kThreads), 4), kThreads, 0, c->stream>>>(
         H.delta, c->bas[MG_HF_BASIS].e, H.members, H.hsz, H.hmax, H.nmax, H.fermi_d, H.T);
     MG_LAUNCHED(c);
-    int seed = H.eT.have_vectors ? kSeedRefine : kSeedCold;
+    int seed = !H.eT.have_vectors ? kSeedCold : first ? kSeedJacobiWarm : kSeedRefine;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        MG_TRY(eig_batched(c, H.eT, seed, seed == kSeedRefine ? 4 : H.nref, false));
+        MG_TRY(eig_batched(c, H.eT, seed, seed == kSeedRefine ? 4 : H.nref, true));
         H.eT.have_vectors = true;
         k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
             H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
@@ -404,7 +408,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     const double prec = H.pp.fermi_prec;
     int evals = 0;
     double lam[2] = {H.fermi[0], H.fermi[1]}, f[2], fp[2];
-    MG_TRY(hfb_evaluate(c, lam, f, fp));
+    MG_TRY(hfb_evaluate(c, lam, f, fp, true));
     ++evals;
     bool conv[2] = {std::fabs(f[0]) < prec, std::fabs(f[1]) < prec};
     double lo[2] = {0, 0}, hi[2] = {0, 0};
@@ -426,7 +430,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
                 next = 0.5 * (lo[it] + hi[it]);
             lam[it] = next;
         }
-        MG_TRY(hfb_evaluate(c, lam, f, fp));
+        MG_TRY(hfb_evaluate(c, lam, f, fp, false));
         ++evals;
         for (int it = 0; it < 2; ++it) {
             if (conv[it]) continue;
@@ -447,6 +451,10 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
         H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
     MG_LAUNCHED(c);
+    // canonical basis: the occupations cluster near 0 and 1 and the
+    // individual vectors matter, so the FP32 Jacobi seed (warm-started from
+    // last iteration's vectors) resolves the clusters before the refinement
+    // and the FP64 polish
     MG_TRY(eig_batched(c, H.eR, H.eR.have_vectors ? kSeedJacobiWarm : kSeedCold, H.nref, true));
     H.eR.have_vectors = true;
     k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax, H.cantr,

@@ -272,6 +272,20 @@ extern "C" int mg_download_derivatives(mg_ctx* c, int b, double* const* der, dou
                                     4 * V * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
     MG_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->bas[b].der_df) {
+        // mixed form: {hi, lo} float pairs -> FP64 in place
+        auto widen = [](double* p, long n) {
+            for (long k = 0; k < n; ++k) {
+                float hl[2];
+                std::memcpy(hl, p + k, sizeof(hl));
+                p[k] = (double)hl[0] + (double)hl[1];
+            }
+        };
+        for (int i = 0; i < count; ++i) {
+            if (der && der[i]) widen(der[i], 12 * V);
+            if (lap && lap[i]) widen(lap[i], 4 * V);
+        }
+    }
     return MG_OK;
 }
 

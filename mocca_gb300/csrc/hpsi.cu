@@ -14,6 +14,7 @@
 // h.psi never goes to HBM.  The per-spwf sums <psi|h psi> and <h psi|h psi>
 // are reduced per block into a partial table and finished in block order
 // (deterministic).
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -129,6 +130,114 @@ k_hpsi(double* __restrict__ psi, const double* __restrict__ der,
     }
 }
 
+// Mixed precision: the same action in double-float arithmetic (df.cuh).  The
+// derivatives arrive as double-float pairs, psi and the fields are split from
+// their FP64 bits (no FP64 instructions); the GradDesc update and the energy
+// sums stay FP64.
+__device__ __forceinline__ void pauli_df(const dfl* p, int dir, dfl* o) {
+    if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
+    else if (dir == 2) { o[0] = p[3]; o[1] = df_neg(p[2]); o[2] = df_neg(p[1]); o[3] = p[0]; }
+    else { o[0] = p[0]; o[1] = p[1]; o[2] = df_neg(p[2]); o[3] = df_neg(p[3]); }
+}
+
+template <bool kGradStep>
+__global__ void __launch_bounds__(kThreads)
+k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
+          const float2* __restrict__ lap, const int* __restrict__ qn, Fields F,
+          double* __restrict__ hout, double* __restrict__ upd, double* __restrict__ partial,
+          long V, double kin0, double kin1, double fac, double mom) {
+    const int i = blockIdx.y;
+    const long v = (long)blockIdx.x * kThreads + threadIdx.x;
+    double s_eh = 0.0, s_hh = 0.0;
+    if (v < V) {
+        const int it = (qn[4 * i] + 3) / 2 - 1;
+        const double kin = it == 0 ? kin0 : kin1;
+        double* ps = psi + (long)i * 4 * V;
+        const float2* dr = der + (long)i * 12 * V;
+        const float2* lp = lap + (long)i * 4 * V;
+        double p64[4];
+        dfl p[4], d[3][4], L[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            p64[l] = ps[l * V + v];
+            p[l] = df_split(p64[l]);
+            L[l] = df_ld(lp + l * V + v);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) d[m][l] = df_ld(dr + (m * 4 + l) * V + v);
+        }
+        const dfl kB = df_add(df_split(F.B[it * V + v]), df_split(kin));
+        const dfl Uq = df_split(F.U[it * V + v]);
+        const dfl nb[3] = {df_split(F.nablaB[(it * 3 + 0) * V + v]),
+                           df_split(F.nablaB[(it * 3 + 1) * V + v]),
+                           df_split(F.nablaB[(it * 3 + 2) * V + v])};
+        float wh[4] = {0.f, 0.f, 0.f, 0.f}, wl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int mu = 0; mu < 3; ++mu)
+#pragma unroll
+            for (int nu = 0; nu < 3; ++nu) {
+                dfl sg[4];
+                pauli_df(d[mu], nu + 1, sg);
+                const dfl wv = df_split(F.W[((it * 3 + nu) * 3 + mu) * V + v]);
+#pragma unroll
+                for (int l = 0; l < 4; ++l) df_acc(wh[l], wl[l], wv, sg[l]);
+            }
+#pragma unroll
+        for (int nu = 0; nu < 3; ++nu) {
+            dfl sg[4];
+            pauli_df(p, nu + 1, sg);
+            dfl hv = df_split(F.divW[(it * 3 + nu) * V + v]);
+            hv.h *= 0.5f;   // exact
+            hv.l *= 0.5f;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) df_acc(wh[l], wl[l], hv, sg[l]);
+        }
+        const dfl w[4] = {df_norm(dfl{wh[0], wl[0]}), df_norm(dfl{wh[1], wl[1]}),
+                          df_norm(dfl{wh[2], wl[2]}), df_norm(dfl{wh[3], wl[3]})};
+        const dfl wf[4] = {w[1], df_neg(w[0]), w[3], df_neg(w[2])};
+        double h[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            float th = 0.f, tl = 0.f;
+            df_acc(th, tl, df_neg(kB), L[l]);
+            df_acc(th, tl, df_neg(nb[0]), d[0][l]);
+            df_acc(th, tl, df_neg(nb[1]), d[1][l]);
+            df_acc(th, tl, df_neg(nb[2]), d[2][l]);
+            df_acc(th, tl, Uq, p[l]);
+            h[l] = df_to(df_add(df_norm(dfl{th, tl}), wf[l]));
+            s_eh = fma(p64[l], h[l], s_eh);
+            s_hh = fma(h[l], h[l], s_hh);
+        }
+        if (kGradStep) {
+            double* up = upd + (long)i * 4 * V;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double a = fma(-fac, h[l], mom * up[l * V + v]);
+                up[l * V + v] = p64[l];
+                ps[l * V + v] = p64[l] + a;
+            }
+        } else if (hout) {
+            double* ho = hout + (long)i * 4 * V;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) ho[l * V + v] = h[l];
+        }
+    }
+    __shared__ double red[2][kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s_eh += __shfl_xor_sync(0xffffffffu, s_eh, o);
+        s_hh += __shfl_xor_sync(0xffffffffu, s_hh, o);
+    }
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (lane == 0) { red[0][warp] = s_eh; red[1][warp] = s_hh; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < kThreads / 32; ++q) { a += red[0][q]; b += red[1][q]; }
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 0] = a;
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 1] = b;
+    }
+}
+
 // e[i] = dv * sum <psi|h psi>, disp[i] = dv * sum <h psi|h psi> - e^2
 __global__ void k_finish_energies(const double* __restrict__ partial, int nchunk, int nwt,
                                   double dv, double* __restrict__ e, double* __restrict__ disp) {
@@ -165,7 +274,20 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
     const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
     dim3 grid(nchunk, c->p.nwt);
-    if (grad_step)
+    // the derivative format decides: double-float derivatives come from the
+    // mixed kernels
+    const bool mixed = B.der_df;
+    const float2* der2 = reinterpret_cast<const float2*>(B.der);
+    const float2* lap2 = reinterpret_cast<const float2*>(B.lap);
+    if (grad_step && mixed)
+        k_hpsi_df<true><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn, F, nullptr,
+                                                          c->updates, c->red, V, kin0, kin1, fac,
+                                                          mom);
+    else if (mixed)
+        k_hpsi_df<false><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn, F, out,
+                                                           nullptr, c->red, V, kin0, kin1, 0.0,
+                                                           0.0);
+    else if (grad_step)
         k_hpsi<true><<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.lap, B.qn, F, nullptr,
                                                        c->updates, c->red, V, kin0, kin1, fac, mom);
     else

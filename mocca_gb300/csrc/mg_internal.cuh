@@ -60,6 +60,7 @@ struct Basis {
     double* e = nullptr;     // nwt
     double* disp = nullptr;  // nwt
     GridJob* jobs = nullptr; // 4*nwt derivative jobs
+    bool der_df = false;     // der / lap hold double-float {hi, lo} pairs (mixed form)
     std::vector<int> h_qn;
     std::vector<double> h_occ, h_e, h_disp;
     bool have_qn = false;
@@ -89,6 +90,7 @@ struct EigBatch {
     double* emax = nullptr;   // nb * ld largest opposite-sign angle |S_ij|/|l_i - l_j| per row
     int* done = nullptr;      // nb: first refinement step skipped (INT_MAX: none)
     double* offrel = nullptr; // nb: |S - diag S|_F / |A|_F seen by the last refinement step
+    int* pfail = nullptr;     // nb: 1 when the FP64 Jacobi polish hit its sweep cap
     double skip_tol = -1.0;   // skip the remaining steps once offrel <= skip_tol (< 0: never)
     GemmDesc *d_ax = nullptr, *d_sg = nullptr, *d_xf = nullptr, *d_rr = nullptr;
     bool attr_done = false;
@@ -208,7 +210,7 @@ namespace mg {
 int upload_matrices(mg_ctx* c);
 int build_basis_jobs(mg_ctx* c, int b);
 int build_field_jobs(mg_ctx* c);
-int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs);
+int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df = false);
 int derive_basis(mg_ctx* c, int b);
 
 int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom);
@@ -220,7 +222,7 @@ int coulomb_setup(mg_ctx* c);
 int coulomb_solve(mg_ctx* c, int* iters);
 int potentials(mg_ctx* c);
 int energy(mg_ctx* c, mg_energy_terms* out);
-int basis_dots(mg_ctx* c, const double* a, const double* b, double* out);
+int basis_dots(mg_ctx* c, const double* a, const double* b, double* out, bool b_df = false);
 int pairing_mesh(mg_ctx* c);
 int canonical_transform(mg_ctx* c);
 int pairing_set_smem(mg_ctx* c);

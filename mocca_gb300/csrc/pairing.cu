@@ -1,4 +1,5 @@
-// pairing.cu -- mesh side of the HFB pairing step, FP64.
+// pairing.cu -- mesh side of the HFB pairing step, FP64 (double-float in the
+// mixed-precision form).
 //
 // With time reversal and signature conserved, the pairs that enter the
 // pairing field and the gaps are (stored spwf j, time-reversed partner of
@@ -23,6 +24,7 @@
 // entries here.
 #include <cmath>
 
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -251,6 +253,149 @@ k_can_transform(const double* __restrict__ psi, const int* __restrict__ members,
     }
 }
 
+// ---- mixed precision: the three mesh contractions in double-float -----------------
+// (df.cuh; same tiling, a dfl takes the 8 bytes of a double in shared memory;
+// partial sums leave the kernels as FP64)
+
+__global__ void __launch_bounds__(kThreads)
+k_pair_field_df(const double* __restrict__ psi, const int* __restrict__ members,
+                const int* __restrict__ hsz, int hmax, const double* __restrict__ K, long V,
+                double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int b = blockIdx.y;
+    const int h = hsz[b];
+    const long p0 = (long)blockIdx.x * kPts;
+    dfl* sK = reinterpret_cast<dfl*>(sm);   // h*h
+    dfl* sP = sK + h * h;                   // [j][c][kPts]
+    double* red = sm + h * h + h * 4 * kPts;  // [2][kThreads]
+    for (int t = threadIdx.x; t < h * h; t += kThreads) sK[t] = df_from(K[(long)b * hmax * hmax + t]);
+    for (int t = threadIdx.x; t < h * 4 * kPts; t += kThreads) {
+        const int j = t / (4 * kPts), c = (t / kPts) % 4, q = t % kPts;
+        const long v = p0 + q;
+        sP[t] = df_from(v < V ? psi[((long)members[b * hmax + j] * 4 + c) * V + v] : 0.0);
+    }
+    __syncthreads();
+    const int q = threadIdx.x % kPts;
+    const int grp = threadIdx.x / kPts;
+    constexpr int kGroups = kThreads / kPts;
+    float frh = 0.f, frl = 0.f, fih = 0.f, fil = 0.f;
+    for (int i = grp; i < h; i += kGroups) {
+        float yh[4] = {0.f, 0.f, 0.f, 0.f}, yl[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int j = 0; j < h; ++j) {
+            const dfl k = sK[j * h + i];
+            const dfl* pj = sP + j * 4 * kPts + q;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) df_acc(yh[c], yl[c], pj[c * kPts], k);
+        }
+        dfl y[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) y[c] = df_norm(dfl{yh[c], yl[c]});
+        const dfl* pi = sP + i * 4 * kPts + q;
+        const dfl a0 = pi[0], a1 = pi[kPts], a2 = pi[2 * kPts], a3 = pi[3 * kPts];
+        df_acc(frh, frl, y[0], a0);
+        df_acc(frh, frl, y[1], a1);
+        df_acc(frh, frl, y[2], a2);
+        df_acc(frh, frl, y[3], a3);
+        df_acc(fih, fil, y[0], df_neg(a1));
+        df_acc(fih, fil, y[1], a0);
+        df_acc(fih, fil, y[2], df_neg(a3));
+        df_acc(fih, fil, y[3], a2);
+    }
+    red[threadIdx.x] = df_to(dfl{frh, frl});
+    red[kThreads + threadIdx.x] = df_to(dfl{fih, fil});
+    __syncthreads();
+    if (grp == 0 && p0 + q < V) {
+        double sr = 0.0, si = 0.0;
+        for (int g = 0; g < kGroups; ++g) {
+            sr += red[g * kPts + q];
+            si += red[kThreads + g * kPts + q];
+        }
+        part[((long)b * 2 + 0) * V + p0 + q] = sr;
+        part[((long)b * 2 + 1) * V + p0 + q] = si;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_pair_gaps_df(const double* __restrict__ psi, const int* __restrict__ members,
+               const int* __restrict__ hsz, int hmax, const double* __restrict__ fre,
+               const double* __restrict__ fim, long V, int nchunk, double* __restrict__ gpart) {
+    extern __shared__ double sm[];
+    const int b = blockIdx.y, it = b / 2;
+    const int h = hsz[b];
+    constexpr int kRow = 4 * kGPts + 1;
+    dfl* sA = reinterpret_cast<dfl*>(sm);   // [i][c][kGPts] psi
+    dfl* sZ = sA + h * kRow;                // [j][c][kGPts] M psi
+    double* acc = sm + 2 * h * kRow;        // h*h accumulators (FP64)
+    for (int t = threadIdx.x; t < h * h; t += kThreads) acc[t] = 0.0;
+    const long per = (V + nchunk - 1) / nchunk;
+    const long v0 = (long)blockIdx.x * per, v1 = min(V, v0 + per);
+    for (long base = v0; base < v1; base += kGPts) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < h * kGPts; t += kThreads) {
+            const int j = t / kGPts, q = t % kGPts;
+            const long v = base + q;
+            dfl a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            dfl r = {0.f, 0.f}, m = {0.f, 0.f};
+            if (v < v1) {
+                const long o = (long)members[b * hmax + j] * 4 * V + v;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) a[c] = df_from(psi[o + c * V]);
+                r = df_from(fre[it * V + v]);
+                m = df_from(fim[it * V + v]);
+            }
+            dfl* pa = sA + j * kRow + q;
+            dfl* pz = sZ + j * kRow + q;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) pa[c * kGPts] = a[c];
+            const dfl nr = df_neg(r), nm = df_neg(m);
+            pz[0] = df_fma(m, a[1], df_mul(nr, a[0]));
+            pz[kGPts] = df_fma(nm, a[0], df_mul(nr, a[1]));
+            pz[2 * kGPts] = df_fma(m, a[3], df_mul(nr, a[2]));
+            pz[3 * kGPts] = df_fma(nm, a[2], df_mul(nr, a[3]));
+        }
+        __syncthreads();
+        for (int pr = threadIdx.x; pr < h * h; pr += kThreads) {
+            const int i = pr / h, j = pr % h;
+            const dfl* pa = sA + i * kRow;
+            const dfl* pz = sZ + j * kRow;
+            float sh = 0.f, sl = 0.f;
+#pragma unroll 4
+            for (int q = 0; q < 4 * kGPts; ++q) df_acc(sh, sl, pa[q], pz[q]);
+            acc[pr] += df_to(dfl{sh, sl});
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < h * h; t += kThreads)
+        gpart[((long)b * nchunk + blockIdx.x) * hmax * hmax + t] = acc[t];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_can_transform_df(const double* __restrict__ psi, const int* __restrict__ members,
+                   const int* __restrict__ hsz, const int* __restrict__ cstart, int hmax,
+                   const double* __restrict__ T, long V4, double* __restrict__ can) {
+    extern __shared__ double sm[];
+    const int b = blockIdx.y;
+    const int h = hsz[b];
+    dfl* sT = reinterpret_cast<dfl*>(sm);   // h*h
+    dfl* sP = sT + h * h;                   // [j][kPts]
+    for (int t = threadIdx.x; t < h * h; t += kThreads) sT[t] = df_from(T[(long)b * hmax * hmax + t]);
+    const long p0 = (long)blockIdx.x * kPts;
+    for (int t = threadIdx.x; t < h * kPts; t += kThreads) {
+        const int j = t / kPts, q = t % kPts;
+        const long p = p0 + q;
+        sP[t] = df_from(p < V4 ? psi[(long)members[b * hmax + j] * V4 + p] : 0.0);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < h * kPts; t += kThreads) {
+        const int C = t / kPts, q = t % kPts;
+        const long p = p0 + q;
+        if (p >= V4) continue;
+        float sh = 0.f, sl = 0.f;
+        for (int j = 0; j < h; ++j) df_acc(sh, sl, sT[j * h + C], sP[j * kPts + q]);
+        can[(long)(cstart[b] + C) * V4 + p] = df_to(dfl{sh, sl});
+    }
+}
+
 }  // namespace
 
 int pairing_mesh(mg_ctx* c) {
@@ -269,15 +414,24 @@ int pairing_mesh(mg_ctx* c) {
                                                                        hmax, nmax, H.pcut, H.ktil);
     MG_LAUNCHED(c);
     const size_t sm_f = (size_t)(hmax * hmax + hmax * 4 * kPts + 2 * kThreads) * sizeof(double);
-    k_pair_field<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
-        B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
+    const bool mixed = c->cur_precision == MG_MIXED;
+    if (mixed)
+        k_pair_field_df<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
+            B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
+    else
+        k_pair_field<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
+            B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
     MG_LAUNCHED(c);
     k_pair_field_finish<<<div_up(2 * V, kThreads), kThreads, 0, c->stream>>>(H.fpart, H.dfac, V,
                                                                            H.fre, H.fim);
     MG_LAUNCHED(c);
     const size_t sm_g = (size_t)(2 * hmax * (4 * kGPts + 1) + hmax * hmax) * sizeof(double);
-    k_pair_gaps<<<dim3(H.gchunk, 4), kThreads, sm_g, c->stream>>>(
-        B.psi, H.members, H.hsz, hmax, H.fre, H.fim, V, H.gchunk, H.gpart);
+    if (mixed)
+        k_pair_gaps_df<<<dim3(H.gchunk, 4), kThreads, sm_g, c->stream>>>(
+            B.psi, H.members, H.hsz, hmax, H.fre, H.fim, V, H.gchunk, H.gpart);
+    else
+        k_pair_gaps<<<dim3(H.gchunk, 4), kThreads, sm_g, c->stream>>>(
+            B.psi, H.members, H.hsz, hmax, H.fre, H.fim, V, H.gchunk, H.gpart);
     MG_LAUNCHED(c);
     k_gaps_finish<<<dim3(div_up(nmax * nmax, 128), 4), 128, 0, c->stream>>>(
         H.gpart, H.members, H.hsz, hmax, nmax, H.gchunk, H.pcut, c->dv, H.delta);
@@ -289,9 +443,14 @@ int canonical_transform(mg_ctx* c) {
     Hfb& H = c->hfb;
     const long V4 = 4 * c->V;
     const size_t sm = (size_t)(H.hmax * H.hmax + H.hmax * kPts) * sizeof(double);
-    k_can_transform<<<dim3(div_up(V4, kPts), 4), kThreads, sm, c->stream>>>(
-        c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.cstart, H.hmax, H.cantr, V4,
-        c->bas[MG_CAN_BASIS].psi);
+    if (c->cur_precision == MG_MIXED)
+        k_can_transform_df<<<dim3(div_up(V4, kPts), 4), kThreads, sm, c->stream>>>(
+            c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.cstart, H.hmax, H.cantr, V4,
+            c->bas[MG_CAN_BASIS].psi);
+    else
+        k_can_transform<<<dim3(div_up(V4, kPts), 4), kThreads, sm, c->stream>>>(
+            c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.cstart, H.hmax, H.cantr, V4,
+            c->bas[MG_CAN_BASIS].psi);
     MG_LAUNCHED(c);
     return MG_OK;
 }
@@ -304,6 +463,9 @@ int pairing_set_smem(mg_ctx* c) {
     MG_CUDA(cudaFuncSetAttribute(k_pair_field, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     MG_CUDA(cudaFuncSetAttribute(k_pair_gaps, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     MG_CUDA(cudaFuncSetAttribute(k_can_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    MG_CUDA(cudaFuncSetAttribute(k_pair_field_df, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    MG_CUDA(cudaFuncSetAttribute(k_pair_gaps_df, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    MG_CUDA(cudaFuncSetAttribute(k_can_transform_df, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     return MG_OK;
 }
 

@@ -63,6 +63,76 @@ def test_mixed_derivatives_full_box(built):
     g.close()
 
 
+def test_mixed_hpsi_full_box(built):
+    """h.psi with Woods-Saxon fields in double-float against the FP64 oracle."""
+    p = RunParams(nx=12, ny=12, nz=12, dx=0.8, pc=0, sc=0, tsc=0, trc=1, nwt=6,
+                  neutrons=8, protons=8, coulomb_solver=0, precision=MG_MIXED)
+    psi = synthetic.gaussian_hermite_spinors(p, p.nwt, seed=42)
+    qn = np.tile(np.array([-1, 0, 0, 0], dtype=np.int32), (p.nwt, 1))
+    qn[3:, 0] = 1
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    U, B, nB, W, dW = synthetic.woods_saxon_fields(p)
+    for s in (g, o):
+        s.set_spinors(psi, qn)
+        s.set_energies(np.zeros(p.nwt))
+        s.set_potentials(U=U, B=B, nablaB=nB, W=W, divW=dW)
+        s.DeriveAll()
+    hg, eg, _ = g.hPsi()
+    ho, eo, _ = o.hPsi()
+    assert rel(hg, ho) < 1e-11
+    assert np.allclose(eg, eo, rtol=0, atol=1e-9)
+    g.close()
+
+
+def test_mixed_start_densities_energy(built):
+    """HF start of the Mg24 case with every mesh kernel in double-float."""
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  precision=MG_MIXED)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    for s in (g, o):
+        s.set_spinors(psi, qn)
+        s.set_energies(en)
+    g.Start()
+    o.Start()
+    dg, do = g.get_densities(), o.get_densities()
+    for k in dg:
+        assert rel(dg[k], do[k]) < 1e-11, k
+    pg, po = g.get_potentials(), o.get_potentials()
+    for k in ("U", "B", "nablaB", "W"):
+        assert rel(pg[k], po[k]) < 1e-10, k
+    eg, eo = g.CompEnergy(), o.CompEnergy()
+    assert abs(eg["total"] - eo["total"]) < 1e-8
+    hg, e1, _ = g.hPsi()
+    ho, e2, _ = o.hPsi()
+    assert rel(hg, ho) < 1e-11
+    assert np.allclose(e1, e2, rtol=0, atol=1e-9)
+    g.close()
+
+
+def test_mixed_hfb_start(built):
+    """Pairing field, gaps and canonical basis from the double-float mesh kernels."""
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB, precision=MG_MIXED)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    for s in (g, o):
+        s.set_spinors(psi, qn)
+        s.set_energies(en)
+        s.set_pairing()
+    ig = g.SolvePairing()
+    io = o.SolvePairing()
+    assert ig["converged"] and io["converged"]
+    fg, fo = g.get_pairing_field(), o.get_pairing_field()
+    for a, b in zip(fg, fo):
+        assert rel(a, b) < 1e-10
+    assert abs(sum(ig["pairing_energy"]) - sum(io["pairing_energy"])) < 1e-9
+    g.close()
+
+
 def _hfb(precision):
     p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
                   pairing=_abi.MG_PAIRING_HFB, precision=precision)
