@@ -2,21 +2,26 @@
 
 Workload (the 24^3 configuration the headline metric is quoted on): N=Z=28,
 24^3 stored EV8 mesh (48^3 full box), dx=0.8 fm, nwt=160 spinors (80 n +
-80 p), SLy4, time-reversal invariant, seeded harmonic-oscillator start.  A
-step is one pass of the Evolve loop body (src/Main.f90:255-328): GradDesc
-with Gram-Schmidt, the pairing step, DeriveAll, densities, moments,
-potentials with the Coulomb CG, energy.
+80 p), SLy4, time-reversal invariant, HFB pairing (G=1250 MeV fm^3,
+alpha=1), seeded harmonic-oscillator start, imaginary-time step dt=0.005
+with momentum 0.3.  A step is one pass of the Evolve loop body
+(src/Main.f90:255-328): GradDesc with Gram-Schmidt, the HFB pairing step,
+DeriveAll, densities, moments, potentials with the Coulomb CG, energy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed] [--breakdown]
+                  [--precision mixed|fp64] [--accuracy-iters A] [--breakdown]
 
-One JSON line on rank 0.  `value` times K steps with every input resident in
-HBM (CUDA events on the library's stream, barrier + synchronize on both
-sides, max over ranks); `e2e` times the same steps through the C ABI with
-the spinors uploaded from pinned host memory and the spinors plus the
-energy read back every step.  The working set (spinors, derivatives,
-updates: ~0.7 GB) is larger than the 129 MB L2, so no flush is needed
-between steps.  Multi-GPU runs are independent replicas (weak scaling).
+One JSON line on rank 0.  `value` is the headline form (mixed precision by
+default): K steps with every input resident in HBM (CUDA events on the
+library's stream, barrier + synchronize on both sides, max over ranks).
+`fp64` is the plain FP64 path timed the same way in the same job, and
+`accuracy` compares A iterations of the mixed form (the last 20 in FP64)
+with A iterations of the FP64 path: |dE_total| in MeV.  `e2e` times the same
+steps through the C ABI with the spinors uploaded from pinned host memory and
+the spinors plus the energy read back every step.  The working set
+(spinors, derivatives, updates: ~0.7 GB) is larger than the 129 MB L2, so
+no flush is needed between steps.  Multi-GPU runs are independent replicas
+(weak scaling).
 """
 from __future__ import annotations
 
@@ -34,11 +39,13 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-import numpy as np  # noqa: E402
-
 WORKLOAD = dict(nx=24, ny=24, nz=24, dx=0.8, nwt=160, neutrons=28.0, protons=28.0)
-DT, MOMENTUM = 0.010, 0.3
+DT, MOMENTUM = 0.005, 0.3
+POLISH = 20   # final FP64 iterations of the mixed form
 METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
+# DRAM traffic of one DeriveBasis launch pair (k_deriv_xy_df + k_deriv_z_df,
+# nwt=160, 24^3) from ncu dram__bytes_read.sum + dram__bytes_write.sum
+DERIV_DF_TRAFFIC = 450.0e6
 
 
 def _params(precision):
@@ -47,9 +54,31 @@ def _params(precision):
                      pairing=MG_PAIRING_HFB)
 
 
+def _config(precision, world):
+    return {"workload": "N=Z=28 HO start (seed 1234), 24^3 EV8 stored mesh, dx=0.8, nwt=160, "
+                        "SLy4, TRC, HFB pairing G=1250 alpha=1 (surface delta, 5 MeV cutoff), "
+                        "dt=0.005, momentum 0.3",
+            **WORKLOAD, "precision": precision, "dt": DT, "momentum": MOMENTUM,
+            "l2": "working set ~0.7 GB > 129 MB L2, no flush",
+            "parallelism": f"replicas x{world}"}
+
+
 def _start_state(p, seed):
     from mocca_gb300 import synthetic
     return synthetic.ho_basis(p, p.nwt // 2, seed=seed)
+
+
+def _make(precision, seed, stream=None):
+    from mocca_gb300 import SLY4
+    from mocca_gb300.mesh import MeshState
+    p = _params(precision)
+    psi, qn, en = _start_state(p, seed)
+    g = MeshState(p, SLY4, stream=stream)
+    g.set_spinors(psi, qn)
+    g.set_energies(en)
+    g.set_pairing()
+    g.Start()
+    return p, g
 
 
 class ClockSampler:
@@ -68,7 +97,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -107,7 +136,7 @@ def measured_peaks():
 
 
 def fp64_dgemm_peak(torch):
-    """Measured FP64 throughput of a cuBLAS DGEMM (denominator for the FP64 kernels)."""
+    """Measured FP64 throughput of a cuBLAS DGEMM (denominator for FP64-equivalent rates)."""
     n = 4096
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
     b = torch.randn(n, n, dtype=torch.float64, device="cuda")
@@ -125,8 +154,7 @@ def fp64_dgemm_peak(torch):
     return 2 * n ** 3 / best / 1e12
 
 
-def cpu_baseline(sample_steps=1):
-    """The FP64 oracle (single-threaded C++ port) on a bounded sample of the workload."""
+def _oracle_state():
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     from mocca_gb300 import SLY4
@@ -137,6 +165,12 @@ def cpu_baseline(sample_steps=1):
     o.set_energies(en)
     o.set_pairing()
     o.Start()
+    return o
+
+
+def cpu_baseline(sample_steps=1):
+    """The FP64 oracle (single-threaded C++ port) on a bounded sample of the workload."""
+    o = _oracle_state()
     t = time.perf_counter()
     o.Evolve(sample_steps, DT, MOMENTUM)
     dt = time.perf_counter() - t
@@ -150,83 +184,95 @@ def run_reference(args, rank, world):
     """--impl reference: the reference's CPU path (oracle port; Fortran build unavailable)."""
     if rank != 0:
         return None
-    steps = max(1, args.steps)
+    steps = max(1, min(args.steps, 30))
     warm = max(0, min(args.warmup, 1))
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle as O
-    from mocca_gb300 import SLY4
-    p = _params("fp64")
-    psi, qn, en = _start_state(p, 1234)
-    o = O.OracleState(p, SLY4)
-    o.set_spinors(psi, qn)
-    o.set_energies(en)
-    o.set_pairing()
-    o.Start()
+    o = _oracle_state()
     if warm:
         o.Evolve(warm, DT, MOMENTUM)
-    per_step = 1  # one full iteration per step keeps K steps within minutes
     t = time.perf_counter()
-    o.Evolve(steps * per_step, DT, MOMENTUM)
+    o.Evolve(steps, DT, MOMENTUM)
     dt = time.perf_counter() - t
-    val = steps * per_step / dt
+    o.close()
+    val = steps / dt
     return {
         "metric": METRIC, "value": val, "unit": "iter/s", "impl": "reference",
         "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "Mg-like HO start, N=Z=28, 24^3 EV8, "
-                                        "nwt=160, SLy4, HFB (G=1250, alpha=1)", **WORKLOAD},
+        "data": "synthetic", "config": _config(args.precision, world),
         "cpu_baseline": {"value": val, "unit": "iter/s", "cores": 1, "kind": "port",
-                         "sample": f"{steps} full iteration(s); the reference is single-threaded "
-                                   "Fortran (no OpenMP) and no Fortran compiler exists here or on "
-                                   "the GPU host, so its C++ FP64 restatement is timed"},
+                         "sample": f"{steps} full HFB iteration(s) (at most 30 to bound the run); "
+                                   "the reference is single-threaded Fortran (no OpenMP) and no "
+                                   "Fortran compiler exists here or on the GPU host, so its C++ "
+                                   "FP64 restatement is timed"},
         "e2e": {"value": val, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
+def _timed_steps(g, torch, stream, steps, barrier, clk_index=None):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    l0 = g.launch_count()
+    if clk_index is not None:
+        with ClockSampler(clk_index) as clk:
+            ev0.record(stream)
+            last = g.Evolve(steps, DT, MOMENTUM)
+            ev1.record(stream)
+            barrier()
+        clocks = clk.summary()
+    else:
+        ev0.record(stream)
+        last = g.Evolve(steps, DT, MOMENTUM)
+        ev1.record(stream)
+        barrier()
+        clocks = None
+    return ev0.elapsed_time(ev1) / 1e3, last, g.launch_count() - l0, clocks
+
+
+def accuracy_check(iters, seed):
+    """|dE_total| after `iters` iterations: mixed form (last POLISH in FP64) vs the FP64 path."""
+    from mocca_gb300 import MG_FP64
+    _, gm = _make("mixed", seed)
+    em = gm.Evolve(iters - POLISH, DT, MOMENTUM)["total"]
+    gm.set_precision(MG_FP64)
+    e_mix = gm.Evolve(POLISH, DT, MOMENTUM)["total"]
+    gm.close()
+    _, gf = _make("fp64", seed)
+    e_f64 = gf.Evolve(iters, DT, MOMENTUM)["total"]
+    gf.close()
+    return {"iterations": iters, "fp64_polish": POLISH, "E_fp64": e_f64, "E_mixed": e_mix,
+            "E_mixed_before_polish": em, "dE_total_MeV": e_mix - e_f64,
+            "pass": abs(e_mix - e_f64) <= 1e-5}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
-    from mocca_gb300 import SLY4, _abi
-    from mocca_gb300.mesh import MeshState
+    from mocca_gb300 import _abi
 
     torch.cuda.set_device(local_rank)
     stream = torch.cuda.Stream()
-    p = _params(args.precision)
-    psi, qn, en = _start_state(p, 1234 + rank)
-    with torch.cuda.stream(stream):
-        g = MeshState(p, SLY4, stream=stream.cuda_stream)
-    g.set_spinors(psi, qn)
-    g.set_energies(en)
-    g.set_pairing()
-    g.Start()
-    g.Evolve(max(3, args.warmup), DT, MOMENTUM)
-    torch.cuda.synchronize()
     dist = world > 1
+    seed = 1234 + rank
 
     def barrier():
         if dist:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def launches():
-        n = C.c_longlong(0)
-        g.lib.mg_launch_count(g.h, C.byref(n))
-        return n.value
-
-    # ---- device-resident throughput --------------------------------------------------
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    l0 = launches()
-    with ClockSampler(local_rank) as clk:
-        ev0.record(stream)
-        last = g.Evolve(args.steps, DT, MOMENTUM)
-        ev1.record(stream)
-        barrier()
-    l1 = launches()
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    if dist:
-        t = torch.tensor([t_dev], device="cuda")
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+        return float(t.item())
+
+    with torch.cuda.stream(stream):
+        p, g = _make(args.precision, seed, stream=stream.cuda_stream)
+    g.Evolve(max(3, args.warmup), DT, MOMENTUM)
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput of the headline form --------------------------
+    t_dev, last, launches, clocks = _timed_steps(g, torch, stream, args.steps, barrier, local_rank)
+    t_dev = max_over_ranks(t_dev)
 
     # ---- end-to-end through the C ABI with host buffers --------------------------------
     host_psi = torch.empty((p.nwt, 4 * p.V), dtype=torch.float64, pin_memory=True)
@@ -245,13 +291,9 @@ def run_ours(args, rank, world, local_rank):
         host_psi, out_psi = out_psi, host_psi
         up, dn = dn, up
     barrier()
-    t_e2e = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([t_e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
 
-    # ---- dominant kernel: the Lagrange derivative kernels of DeriveAll ------------------
+    # ---- dominant kernel pair: the Lagrange derivatives of one basis ------------------
     reps = 5
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -261,54 +303,70 @@ def run_ours(args, rank, world, local_rank):
     k1.record(stream)
     torch.cuda.synchronize()
     t_der = k0.elapsed_time(k1) / 1e3 / reps
-    n_line = p.nx  # line length
-    flops = 48.0 * n_line * p.V * p.nwt          # 4 comps x 6 line-GEMMs x 2 n flops per point
-    bytes_ = 160.0 * p.V * p.nwt                 # psi in + 3 der + lap out, FP64
+    flops = 48.0 * p.nx * p.V * p.nwt     # 4 comps x 6 line contractions x 2 n flops per point
+    bytes_ = 160.0 * p.V * p.nwt          # FP64 psi in, 3 first derivatives + Laplacian out
 
-    breakdown = None
-    if args.breakdown:
-        breakdown = stage_breakdown(g, torch, stream)
+    breakdown = stage_breakdown(g, torch, stream) if args.breakdown else None
+    g.close()
+
+    # ---- the plain FP64 path on the same workload (same job, same GPU) ------------------
+    fp64 = None
+    if args.precision == "mixed":
+        with torch.cuda.stream(stream):
+            _, g64 = _make("fp64", seed, stream=stream.cuda_stream)
+        g64.Evolve(max(3, args.warmup), DT, MOMENTUM)
+        t64, _, _, _ = _timed_steps(g64, torch, stream, args.steps, barrier)
+        t64 = max_over_ranks(t64)
+        g64.close()
+        fp64 = {"value": world * args.steps / t64, "unit": "iter/s",
+                "ms_per_step": t64 / args.steps * 1e3}
+
+    accuracy = None
+    if rank == 0 and args.precision == "mixed" and args.accuracy_iters > POLISH:
+        accuracy = accuracy_check(args.accuracy_iters, seed)
 
     if rank != 0:
-        g.close()
         return None
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = fp64_dgemm_peak(torch)
+    mixed = args.precision == "mixed"
+    value = world * args.steps / t_dev
     res = {
         "metric": METRIC,
-        "value": world * args.steps / t_dev,
+        "value": value,
         "unit": "iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_dev / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f64+tf32",
+        "dtype": "f64 (double-float mesh kernels)" if mixed else "f64",
         "data": "synthetic",
-        "config": {"workload": "N=Z=28 HO start (seed 1234), 24^3 EV8 stored mesh, dx=0.8, "
-                               "nwt=160, SLy4, TRC, HFB pairing G=1250 alpha=1 "
-                               "(surface delta, 5 MeV cutoff)",
-                   **WORKLOAD, "precision": args.precision, "dt": DT, "momentum": MOMENTUM,
-                   "l2": "working set ~0.7 GB > 129 MB L2, no flush",
-                   "parallelism": f"replicas x{world}"},
+        "config": _config(args.precision, world),
         "e2e": {"value": world * args.steps / t_e2e, "unit": "iter/s",
                 "h2d_bytes_per_step": int(host_psi.numel() * 8),
                 "d2h_bytes_per_step": int(out_psi.numel() * 8 + C.sizeof(e_terms))},
-        "roofline": {"kernel": "k_deriv_xy + k_deriv_z (DeriveAll, HF basis)",
+        "roofline": {"kernel": ("k_deriv_xy_df + k_deriv_z_df" if mixed else
+                                "k_deriv_xy + k_deriv_z") + " (DeriveBasis, HF basis)",
                      "bound": "hbm", "achieved": bytes_ / t_der / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": bytes_ / t_der / 1e9 / hbm,
-                     "traffic": None,
-                     "fp64": {"achieved_tflops": flops / t_der / 1e12,
-                              "peak_tflops_dgemm": fp64_peak,
-                              "frac": flops / t_der / 1e12 / fp64_peak},
+                     "traffic": DERIV_DF_TRAFFIC if mixed else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)",
+                     "fp64_equivalent": {"achieved_tflops": flops / t_der / 1e12,
+                                         "dgemm_tflops_measured": fp64_peak,
+                                         "frac_of_dgemm": flops / t_der / 1e12 / fp64_peak},
                      "ms_per_launch_pair": t_der * 1e3},
-        "cpu_baseline": cpu_baseline(1) if world == 1 or rank == 0 else None,
-        "clocks": clk.summary(),
-        "gpu_launches": int(l1 - l0),
+        "cpu_baseline": cpu_baseline(1),
+        "clocks": clocks,
+        "gpu_launches": int(launches),
         "energy_last": last["total"],
     }
+    if fp64:
+        res["fp64"] = fp64
+        res["speedup_vs_fp64"] = value / fp64["value"]
+    if accuracy:
+        res["accuracy"] = accuracy
     if breakdown:
         res["breakdown_ms"] = breakdown
-    g.close()
     return res
 
 
@@ -340,10 +398,11 @@ def stage_breakdown(g, torch, stream):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--accuracy-iters", type=int, default=300)
     ap.add_argument("--breakdown", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -62,6 +62,12 @@ class MeshState:
         except Exception:
             pass
 
+    def launch_count(self) -> int:
+        """Kernels this context has launched (mg_launch_count)."""
+        n = C.c_longlong(0)
+        self._call("mg_launch_count", C.byref(n))
+        return n.value
+
     def set_precision(self, precision: int):
         """MG_FP64 or MG_MIXED for the following calls (mixed iterations, FP64 polish)."""
         self._call("mg_set_precision", precision)
