@@ -465,27 +465,47 @@ __global__ void k_orth_prep(const double* __restrict__ G, double* __restrict__ R
 // Ascending order after a refinement that started from earlier vectors (the
 // eigenvalue estimates keep the column order of the start, which need not be
 // sorted any more): rank each eigenvalue (ties by index), move column j of X
-// to column rank(j) of X2 and reorder w.
+// to column rank(j) of X2 and reorder w.  Grid (row chunks, matrices): every
+// CTA ranks the eigenvalues itself (integer compares of order-preserving
+// keys of the FP64 bit patterns) and moves kSortRows rows.
+constexpr int kSortRows = 8;
+
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 __global__ void __launch_bounds__(128)
-k_sort_cols(const double* __restrict__ X, double* __restrict__ X2, double* __restrict__ w,
-            long stride, int ld, long wstride, const int* __restrict__ nsz) {
+k_sort_cols(const double* __restrict__ X, double* __restrict__ X2, const double* __restrict__ w,
+            double* __restrict__ w2, long stride, int ld, long wstride,
+            const int* __restrict__ nsz) {
+    __shared__ unsigned long long key[128];
     __shared__ double sw[128];
     __shared__ int rank[128];
-    const int b = blockIdx.x, n = nsz[b];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) sw[i] = w[b * wstride + i];
+    const int b = blockIdx.y, n = nsz[b];
+    const int r0 = blockIdx.x * kSortRows;
+    if (r0 >= n) return;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        sw[i] = w[b * wstride + i];
+        key[i] = order_key(sw[i]);
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double di = sw[i];
+        const unsigned long long ki = key[i];
         int r = 0;
-        for (int j = 0; j < n; ++j) r += (sw[j] < di || (sw[j] == di && j < i)) ? 1 : 0;
+        for (int j = 0; j < n; ++j) r += (key[j] < ki || (key[j] == ki && j < i)) ? 1 : 0;
         rank[i] = r < n ? r : n - 1;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) w[b * wstride + rank[i]] = sw[i];
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-        const int r = t / n, j = t % n;
+    const int r1 = min(n, r0 + kSortRows);
+    for (int t = threadIdx.x; t < (r1 - r0) * n; t += blockDim.x) {
+        const int r = r0 + t / n, j = t % n;
         X2[b * stride + (long)r * ld + rank[j]] = X[b * stride + (long)r * ld + j];
     }
+    // every CTA holds the same values; the first writes the sorted w (to a
+    // second buffer: the other CTAs may still be reading w)
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) w2[b * wstride + rank[i]] = sw[i];
 }
 
 // Frobenius norms of the batch matrices (delta of the refinement uses ||A||).
@@ -527,7 +547,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
                                                       E.w, E.wstride, warm ? 12 : 30, c->flags + 4);
         MG_LAUNCHED(c);
     }
-    k_frob<<<E.nb, 128, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
+    k_frob<<<E.nb, 1024, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
     MG_LAUNCHED(c);
     const int tiles = div_up(E.nmax, kTile) * div_up(E.nmax, kTile);
     const SkipCtl none{nullptr, nullptr, 0, 0, 0.0};
@@ -585,8 +605,12 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     // ascending order: the refinement keeps the column order of its start and
     // the polish leaves diag(S) in place
     if (seed == kSeedRefine || polish) {
-        k_sort_cols<<<E.nb, 128, 0, c->stream>>>(E.X, E.X2, E.w, E.stride, E.ld, E.wstride, E.nsz);
+        // E.part (2 * nb * ld doubles, free after the refinement) takes the sorted w
+        k_sort_cols<<<dim3(div_up(E.nmax, kSortRows), E.nb), 128, 0, c->stream>>>(
+            E.X, E.X2, E.w, E.part, E.stride, E.ld, E.wstride, E.nsz);
         MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(E.w, E.part, (size_t)E.nb * E.wstride * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
     }

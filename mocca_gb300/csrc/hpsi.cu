@@ -132,8 +132,9 @@ k_hpsi(double* __restrict__ psi, const double* __restrict__ der,
 
 // Mixed precision: the same action in double-float arithmetic (df.cuh).  The
 // derivatives arrive as double-float pairs, psi and the fields are split from
-// their FP64 bits (no FP64 instructions); the GradDesc update and the energy
-// sums stay FP64.
+// their FP64 bits (no FP64 instructions); the GradDesc update and the
+// per-point energy terms are double-float too, so the only FP64 work left is
+// the final rounding of the new psi and the per-thread partial sums.
 __device__ __forceinline__ void pauli_df(const dfl* p, int dir, dfl* o) {
     if (dir == 1) { o[0] = p[2]; o[1] = p[3]; o[2] = p[0]; o[3] = p[1]; }
     else if (dir == 2) { o[0] = p[3]; o[1] = df_neg(p[2]); o[2] = df_neg(p[1]); o[3] = p[0]; }
@@ -148,23 +149,28 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
           long V, double kin0, double kin1, double fac, double mom) {
     const int i = blockIdx.y;
     const long v = (long)blockIdx.x * kThreads + threadIdx.x;
-    double s_eh = 0.0, s_hh = 0.0;
+    // <psi|h psi> and <h psi|h psi> accumulate in double-float and become
+    // FP64 once per thread
+    float eh = 0.f, el = 0.f, hh = 0.f, hl = 0.f;
     if (v < V) {
         const int it = (qn[4 * i] + 3) / 2 - 1;
         const double kin = it == 0 ? kin0 : kin1;
         double* ps = psi + (long)i * 4 * V;
         const float2* dr = der + (long)i * 12 * V;
         const float2* lp = lap + (long)i * 4 * V;
-        double p64[4];
+        // every load first: the spinor, its derivatives, the update history
+        double p64[4], u64[4];
         dfl p[4], d[3][4], L[4];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             p64[l] = ps[l * V + v];
-            p[l] = df_split(p64[l]);
+            if (kGradStep) u64[l] = upd[(long)i * 4 * V + l * V + v];
             L[l] = df_ld(lp + l * V + v);
 #pragma unroll
             for (int m = 0; m < 3; ++m) d[m][l] = df_ld(dr + (m * 4 + l) * V + v);
         }
+#pragma unroll
+        for (int l = 0; l < 4; ++l) p[l] = df_split(p64[l]);
         const dfl kB = df_add(df_split(F.B[it * V + v]), df_split(kin));
         const dfl Uq = df_split(F.U[it * V + v]);
         const dfl nb[3] = {df_split(F.nablaB[(it * 3 + 0) * V + v]),
@@ -194,7 +200,7 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
         const dfl w[4] = {df_norm(dfl{wh[0], wl[0]}), df_norm(dfl{wh[1], wl[1]}),
                           df_norm(dfl{wh[2], wl[2]}), df_norm(dfl{wh[3], wl[3]})};
         const dfl wf[4] = {w[1], df_neg(w[0]), w[3], df_neg(w[2])};
-        double h[4];
+        dfl h[4];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             float th = 0.f, tl = 0.f;
@@ -203,24 +209,29 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
             df_acc(th, tl, df_neg(nb[1]), d[1][l]);
             df_acc(th, tl, df_neg(nb[2]), d[2][l]);
             df_acc(th, tl, Uq, p[l]);
-            h[l] = df_to(df_add(df_norm(dfl{th, tl}), wf[l]));
-            s_eh = fma(p64[l], h[l], s_eh);
-            s_hh = fma(h[l], h[l], s_hh);
+            h[l] = df_add(df_norm(dfl{th, tl}), wf[l]);
+            df_acc(eh, el, p[l], h[l]);
+            df_acc(hh, hl, h[l], h[l]);
         }
         if (kGradStep) {
+            // psi <- psi - fac h + mom update ; update <- psi_old (FP64 copy)
+            const dfl nf = df_neg(df_split(fac)), mm = df_split(mom);
             double* up = upd + (long)i * 4 * V;
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
-                const double a = fma(-fac, h[l], mom * up[l * V + v]);
+                float ah = 0.f, al = 0.f;
+                df_acc(ah, al, nf, h[l]);
+                df_acc(ah, al, mm, df_split(u64[l]));
                 up[l * V + v] = p64[l];
-                ps[l * V + v] = p64[l] + a;
+                ps[l * V + v] = df_to(df_add(p[l], df_norm(dfl{ah, al})));
             }
         } else if (hout) {
             double* ho = hout + (long)i * 4 * V;
 #pragma unroll
-            for (int l = 0; l < 4; ++l) ho[l * V + v] = h[l];
+            for (int l = 0; l < 4; ++l) ho[l * V + v] = df_to(h[l]);
         }
     }
+    double s_eh = df_to(dfl{eh, el}), s_hh = df_to(dfl{hh, hl});
     __shared__ double red[2][kThreads / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
