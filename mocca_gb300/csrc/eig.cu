@@ -369,21 +369,17 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     }
     for (int t = tid; t < n0 * n0; t += kThreads) Qa(t / n0, t % n0) = (t / n0 == t % n0) ? 1.0 : 0.0;
     __syncthreads();
-    const double thr = 1e-15 * anorm[b];
+    const double thr = 1e-14 * anorm[b];
     const int lane = tid & 127, kg = tid >> 7;
     const int half = n / 2;
     int sweep = 0;
     for (; sweep < 12; ++sweep) {
-        // a pair rotates when its coupling is above the rounding level of S and
-        // its rotation angle ~ |a_pq| / |a_qq - a_pp| is representable (pairs
-        // far apart whose coupling is rounding noise stay put)
+        // a pair rotates when its coupling is above the FP64 noise of X^T A X
+        // (~ sqrt(n) eps |A|): rotating noise would only churn, at FP64 cost
         int any = 0;
         if (lane < n)
-            for (int i = kg; i < n; i += 2) {
-                const double x = fabs(a[i * l2 + lane]);
-                if (i != lane && x > thr && x > 1e-16 * fabs(a[i * l2 + i] - a[lane * l2 + lane]))
-                    any = 1;
-            }
+            for (int i = kg; i < n; i += 2)
+                if (i != lane && fabs(a[i * l2 + lane]) > thr) any = 1;
         if (!__syncthreads_or(any)) break;
         for (int r = 0; r < n - 1; ++r) {
             int on = 0;
@@ -392,7 +388,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
                 const double apq = a[p * l2 + qq];
                 const double d = a[qq * l2 + qq] - a[p * l2 + p];
                 double c = 1.0, s = 0.0;
-                if (fabs(apq) > thr && fabs(apq) > 1e-16 * fabs(d)) {
+                if (fabs(apq) > thr) {
                     if (fabs(d) > 1e8 * fabs(apq)) {
                         // small angle: tan = a_pq / d to 1/(4 tau^2) < 1e-16 relative
                         // (FP64 divides and square roots are slow on this part)

@@ -331,6 +331,8 @@ void hfb_free(mg_ctx* c) {
     for (int* p : {H.members, H.hsz, H.cstart, H.nsz_T})
         if (p) cudaFree(p);
     if (H.h_pinned) cudaFreeHost(H.h_pinned);
+    for (cudaGraphExec_t& g : H.eval_graph)
+        if (g) cudaGraphExecDestroy(g);
     eig_free(H.eT);
     eig_free(H.eR);
 }
@@ -346,6 +348,58 @@ void hfb_free(mg_ctx* c) {
 // to zero energy decides the particle number).  If before the last step
 // states of opposite sign were still mixed by an angle above kRefineTol, the
 // evaluation is redone from the Jacobi seed.
+// The launches of one evaluation after lambda is on the device: T(lambda),
+// eigen-decomposition, rho, kappa, dN/dlambda, block traces.
+static int eval_launches(mg_ctx* c, int seed) {
+    Hfb& H = c->hfb;
+    k_build_T<<<dim3(div_up(H.nmax * H.nmax, kThreads), 4), kThreads, 0, c->stream>>>(
+        H.delta, c->bas[MG_HF_BASIS].e, H.members, H.hsz, H.hmax, H.nmax, H.fermi_d, H.T);
+    MG_LAUNCHED(c);
+    MG_TRY(eig_batched(c, H.eT, seed, seed == kSeedRefine ? 4 : H.nref, true));
+    k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
+        H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
+    MG_LAUNCHED(c);
+    k_dn_dlambda<<<dim3(H.hmax, 4), 128, 0, c->stream>>>(H.eT.X, H.eT.w, H.hsz, H.nmax, H.dpart);
+    MG_LAUNCHED(c);
+    k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.dpart, H.eT.emax, H.trace_d);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+// One evaluation's launches.  The warm seeds (every evaluation after the
+// first pairing step) replay a CUDA graph captured on first use: ~40 small
+// launches become one, the early exits inside stay device-side decisions.
+static int eval_run(mg_ctx* c, int seed) {
+    Hfb& H = c->hfb;
+    if (seed == kSeedCold || H.no_graph) return eval_launches(c, seed);
+    if (!H.eval_graph[seed]) {
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();    // e.g. the legacy default stream: launch directly
+            H.no_graph = true;
+            return eval_launches(c, seed);
+        }
+        const long long l0 = c->launches;
+        const int st = eval_launches(c, seed);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (st != MG_OK || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return st != MG_OK ? st : MG_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&H.eval_graph[seed], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            H.eval_graph[seed] = nullptr;
+            return MG_ERR_CUDA;
+        }
+        H.eval_graph_launches[seed] = c->launches - l0;
+        c->launches = l0;
+    }
+    MG_CUDA(cudaGraphLaunch(H.eval_graph[seed], c->stream));
+    c->launches += H.eval_graph_launches[seed];
+    return MG_OK;
+}
+
 static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out,
                         bool first) {
     Hfb& H = c->hfb;
@@ -353,27 +407,16 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     hp[24] = lam[0];
     hp[25] = lam[1];
     MG_CUDA(cudaMemcpyAsync(H.fermi_d, hp + 24, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_build_T<<<dim3(div_up(H.nmax * H.nmax, kThreads), 4), kThreads, 0, c->stream>>>(
-        H.delta, c->bas[MG_HF_BASIS].e, H.members, H.hsz, H.hmax, H.nmax, H.fermi_d, H.T);
-    MG_LAUNCHED(c);
     int seed = !H.eT.have_vectors ? kSeedCold : first ? kSeedJacobiWarm : kSeedRefine;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        MG_TRY(eig_batched(c, H.eT, seed, seed == kSeedRefine ? 4 : H.nref, true));
+        MG_TRY(eval_run(c, seed));
         H.eT.have_vectors = true;
-        k_rho_kappa<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
-            H.eT.X, H.hsz, H.nmax, H.rho, H.kappa);
-        MG_LAUNCHED(c);
-        k_dn_dlambda<<<dim3(H.hmax, 4), 128, 0, c->stream>>>(H.eT.X, H.eT.w, H.hsz, H.nmax,
-                                                            H.dpart);
-        MG_LAUNCHED(c);
-        k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.dpart, H.eT.emax, H.trace_d);
-        MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(hp, H.trace_d, 12 * sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
         const double em = std::max(std::max(hp[8], hp[9]), std::max(hp[10], hp[11]));
         if (seed != kSeedRefine || em <= kRefineTol) break;
-        seed = kSeedJacobiWarm;
+        seed = kSeedJacobiWarm;   // T is rebuilt identically (same lambda)
         ++H.reseeds;
     }
     N_out[0] = hp[0] + hp[1] - c->p.neutrons;

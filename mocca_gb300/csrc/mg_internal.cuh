@@ -129,6 +129,9 @@ struct Hfb {
     double* h_pinned = nullptr;                // 8 pinned doubles
     double fermi[2] = {-10.0, -10.0};
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
+    cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
+    long long eval_graph_launches[3] = {0, 0, 0};
+    bool no_graph = false;
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
     double* T = nullptr;      // 4 block HFB matrices (signature-reduced), nmax x nmax
