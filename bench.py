@@ -9,7 +9,7 @@ with momentum 0.3.  A step is one pass of the Evolve loop body
 DeriveAll, densities, moments, potentials with the Coulomb CG, energy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision mixed|fp64] [--accuracy-iters A] [--breakdown]
+                  [--precision mixed|fp64] [--accuracy-iters A] [--breakdown] [--no-micro]
 
 One JSON line on rank 0.  `value` is the headline form (mixed precision by
 default): K steps with every input resident in HBM (CUDA events on the
@@ -21,7 +21,8 @@ steps through the C ABI with the spinors uploaded from pinned host memory and
 the spinors plus the energy read back every step.  The working set
 (spinors, derivatives, updates: ~0.7 GB) is larger than the 129 MB L2, so
 no flush is needed between steps.  Multi-GPU runs are independent replicas
-(weak scaling).
+(weak scaling).  `microbench_32c_200` times DeriveAll and h.psi of 200
+spinors on the 32^3 symmetry-free box in both precisions.
 """
 from __future__ import annotations
 
@@ -244,6 +245,51 @@ def accuracy_check(iters, seed):
             "pass": abs(e_mix - e_f64) <= 1e-5}
 
 
+def microbench_c2(torch, stream, reps=5):
+    """Mesh-kernel microbench on the 32^3 full (symmetry-free) box: 200
+    Gaussian x Hermite spinors (seed 42) in Woods-Saxon fields; d/dx,y,z +
+    Laplacian of every spinor (DeriveAll) and h.psi, FP64 and mixed."""
+    import numpy as np
+    from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, synthetic
+    from mocca_gb300.mesh import MeshState
+    out = {"workload": "32^3 full box (no symmetries, unfolded Lagrange matrices), dx=0.8, "
+                       "200 spinors, Woods-Saxon U/B/W (R=3.5, a=0.65)"}
+    for name, prec in (("fp64", MG_FP64), ("mixed", MG_MIXED)):
+        p = RunParams(nx=32, ny=32, nz=32, dx=0.8, pc=0, sc=0, tsc=0, trc=1, nwt=200,
+                      neutrons=8, protons=8, coulomb_solver=0, precision=prec)
+        psi = synthetic.gaussian_hermite_spinors(p, p.nwt, seed=42)
+        qn = np.tile(np.array([-1, 0, 0, 0], dtype=np.int32), (p.nwt, 1))
+        qn[p.nwt // 2:, 0] = 1
+        with torch.cuda.stream(stream):
+            g = MeshState(p, SLY4, stream=stream.cuda_stream)
+        g.set_spinors(psi, qn)
+        g.set_energies(np.zeros(p.nwt))
+        U, B, nB, W, dW = synthetic.woods_saxon_fields(p)
+        g.set_potentials(U=U, B=B, nablaB=nB, W=W, divW=dW)
+        g.DeriveBasis(0)
+        g.hPsi(want_spinors=False)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        for _ in range(reps):
+            g.DeriveBasis(0)
+        ev[1].record(stream)
+        for _ in range(reps):
+            g.hPsi(want_spinors=False)
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        t_d = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+        t_h = ev[1].elapsed_time(ev[2]) / 1e3 / reps
+        V = p.V
+        out[name] = {"derive_ms": t_d * 1e3,
+                     "derive_gflops": 48.0 * 32 * V * p.nwt / t_d / 1e9,
+                     "derive_gbs": 160.0 * V * p.nwt / t_d / 1e9,
+                     "hpsi_ms": t_h * 1e3,
+                     "hpsi_gbs": 192.0 * V * p.nwt / t_h / 1e9}
+        g.close()
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mocca_gb300 import _abi
@@ -324,6 +370,7 @@ def run_ours(args, rank, world, local_rank):
     accuracy = None
     if rank == 0 and args.precision == "mixed" and args.accuracy_iters > POLISH:
         accuracy = accuracy_check(args.accuracy_iters, seed)
+    micro = microbench_c2(torch, stream) if rank == 0 and args.micro else None
 
     if rank != 0:
         return None
@@ -367,6 +414,8 @@ def run_ours(args, rank, world, local_rank):
         res["accuracy"] = accuracy
     if breakdown:
         res["breakdown_ms"] = breakdown
+    if micro:
+        res["microbench_32c_200"] = micro
     return res
 
 
@@ -404,6 +453,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--accuracy-iters", type=int, default=300)
     ap.add_argument("--breakdown", action="store_true")
+    ap.add_argument("--no-micro", dest="micro", action="store_false",
+                    help="skip the 32^3 mesh-kernel microbench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

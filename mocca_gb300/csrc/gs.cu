@@ -10,6 +10,7 @@
 // block instead of nb^2 sequential dot/axpy sweeps:
 //   k_gs_order    : stable insertion sort of each block by energy (device)
 //   k_gs_overlap  : S partial sums over point chunks (block-owned, deterministic)
+//   k_gs_sum      : chunk partials of S summed in order, one entry per thread
 //   k_gs_factor   : S = R^T R, X = R^{-1} (one block per CTA, in smem)
 //   k_gs_apply    : psi'_l = sum_{k<=l} X_kl psi_k in place (+ update history)
 // For the near-orthonormal input of an imaginary-time step cond(S) ~ 1, so
@@ -89,7 +90,19 @@ k_gs_overlap(const double* __restrict__ psi, const int* __restrict__ starts,
     }
 }
 
-// Sum partials, Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].
+// Sum the chunk partials of the upper triangle in chunk order (many threads:
+// one entry each); the result goes to chunk slot 0.
+__global__ void k_gs_sum(double* __restrict__ part, int nbmax, int nchunk) {
+    const int b = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nbmax * nbmax || t / nbmax > t % nbmax) return;
+    double* pb = part + (long)b * nchunk * nbmax * nbmax;
+    double s = 0.0;
+    for (int q = 0; q < nchunk; ++q) s += pb[(long)q * nbmax * nbmax + t];
+    pb[t] = s;
+}
+
+// Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].
 __global__ void __launch_bounds__(kThreads)
 k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int nbmax,
             int nchunk, double dv, double* __restrict__ xout, int* __restrict__ flag) {
@@ -101,11 +114,7 @@ k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int
     double* X = sm + nb * nb;    // nb x nb
     for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
         const int k = t / nb, l = t % nb;
-        double s = 0.0;
-        if (k <= l)
-            for (int q = 0; q < nchunk; ++q)
-                s += part[((long)b * nchunk + q) * nbmax * nbmax + k * nbmax + l];
-        S[t] = s * dv;
+        S[t] = k <= l ? part[(long)b * nchunk * nbmax * nbmax + k * nbmax + l] * dv : 0.0;
         X[t] = 0.0;
     }
     __syncthreads();
@@ -240,6 +249,9 @@ int gram_schmidt_impl(mg_ctx* c, double* upd) {
     const size_t sm_ap = (size_t)(nbmax * nbmax + nbmax * kPts) * sizeof(double);
     k_gs_overlap<<<dim3(nchunk, nblk), kThreads, sm_ov, c->stream>>>(B.psi, d_lists, d_ordered,
                                                                       nbmax, V4, nchunk, c->gs_S);
+    MG_LAUNCHED(c);
+    k_gs_sum<<<dim3(div_up((long)nbmax * nbmax, kThreads), nblk), kThreads, 0, c->stream>>>(
+        c->gs_S, nbmax, nchunk);
     MG_LAUNCHED(c);
     k_gs_factor<<<nblk, kThreads, sm_f, c->stream>>>(c->gs_S, d_lists, nbmax, nchunk, c->dv,
                                                      c->gs_R, c->flags);
