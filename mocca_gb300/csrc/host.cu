@@ -35,7 +35,7 @@ void free_all(mg_ctx* c) {
     F(c->gs_S); F(c->gs_R); F(c->gs_index);
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
-    F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags);
+    F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast);
     hfb_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);

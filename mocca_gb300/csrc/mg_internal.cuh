@@ -201,6 +201,8 @@ struct mg_ctx {
     size_t red_len = 0;
     int* flags = nullptr;              // device status flags
     bool coulomb_init = false;
+    double* cfast = nullptr;           // 1-D eigenvectors and eigenvalues of the direct solve
+    long cfast_off[3][2];              // [axis][0: C (n x n), 1: mu (n)]
 
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
