@@ -32,6 +32,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTile = 16;
+// Jacobi kernels: one CTA per matrix, so the whole SM's warps work on its
+// rounds (128 lanes for the columns / rows x 8 groups of rotation pairs)
+constexpr int kJThreads = 1024;
+constexpr int kJGroups = kJThreads / 128;
 
 __device__ float cta_sumf(float x, float* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -66,7 +70,7 @@ __device__ __forceinline__ int rr_player(int j, int r, int n) {
 // One matrix per CTA.  A: FP64 n x n (lda) input; Xw: optional FP64 warm
 // start (n x n, ldx); X: FP64 output vectors (n x n, ldx, column k <-> w[k]);
 // w: eigenvalues ascending.  n <= 128.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kJThreads)
 k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __restrict__ nsz,
            const double* __restrict__ Xw, double* __restrict__ X, long xstride, int ldx,
            double* __restrict__ w, long wstride, int max_sweeps, int* __restrict__ flag) {
@@ -85,7 +89,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     float* t = v + n * ld;      // n x ld scratch
     const double* Ab = A + b * astride;
     const int tid = threadIdx.x;
-    for (int q = tid; q < n * n; q += kThreads) {
+    for (int q = tid; q < n * n; q += kJThreads) {
         const int i = q / n, j = q % n;
         a[i * ld + j] = (i < n0 && j < n0) ? (float)Ab[(long)i * lda + j] : 0.0f;
         float vv = i == j ? 1.0f : 0.0f;
@@ -95,14 +99,14 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     __syncthreads();
     if (Xw) {
         // a <- V^T A V
-        for (int q = tid; q < n * n; q += kThreads) {
+        for (int q = tid; q < n * n; q += kJThreads) {
             const int i = q / n, j = q % n;
             float s = 0.0f;
             for (int k = 0; k < n; ++k) s = fmaf(a[i * ld + k], v[k * ld + j], s);
             t[i * ld + j] = s;
         }
         __syncthreads();
-        for (int q = tid; q < n * n; q += kThreads) {
+        for (int q = tid; q < n * n; q += kJThreads) {
             const int i = q / n, j = q % n;
             float s = 0.0f;
             for (int k = 0; k < n; ++k) s = fmaf(v[k * ld + i], t[k * ld + j], s);
@@ -110,7 +114,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         }
         __syncthreads();
         // symmetrise
-        for (int q = tid; q < n * n; q += kThreads) {
+        for (int q = tid; q < n * n; q += kJThreads) {
             const int i = q / n, j = q % n;
             if (i < j) {
                 const float m = 0.5f * (a[i * ld + j] + a[j * ld + i]);
@@ -120,19 +124,19 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         }
         __syncthreads();
     }
-    // thread (lane, kg): column / row `lane`, every second rotation pair from kg
+    // thread (lane, kg): column / row `lane`, every kJGroups-th rotation pair from kg
     const int lane = tid & 127, kg = tid >> 7;
     const int half = n / 2;
     float part = 0.0f;
     if (lane < n)
-        for (int i = kg; i < n; i += 2) part += a[i * ld + lane] * a[i * ld + lane];
+        for (int i = kg; i < n; i += kJGroups) part += a[i * ld + lane] * a[i * ld + lane];
     const float norm2 = cta_sumf(part, red);
     const float tol2 = 1e-11f * norm2;  // off-diagonal <= 3e-6 |A|: an FP32-level seed
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         part = 0.0f;
         if (lane < n)
-            for (int i = kg; i < n; i += 2)
+            for (int i = kg; i < n; i += kJGroups)
                 if (i != lane) part += a[i * ld + lane] * a[i * ld + lane];
         const float off = cta_sumf(part, red);
         if (off <= tol2) break;
@@ -154,7 +158,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
             }
             __syncthreads();
             if (lane < n)
-                for (int k = kg; k < half; k += 2) {
+                for (int k = kg; k < half; k += kJGroups) {
                     const int p = pq[0][k], q = pq[1][k];
                     const float c = cs[0][k], s = cs[1][k];
                     const float ap = a[p * ld + lane], aq = a[q * ld + lane];
@@ -163,7 +167,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
                 }
             __syncthreads();
             if (lane < n)
-                for (int k = kg; k < half; k += 2) {
+                for (int k = kg; k < half; k += kJGroups) {
                     const int p = pq[0][k], q = pq[1][k];
                     const float c = cs[0][k], s = cs[1][k];
                     const float ap = a[lane * ld + p], aq = a[lane * ld + q];
@@ -180,9 +184,9 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     // sort the n0 real eigenpairs ascending, ties by index (the padding row
     // stays last): rank of each diagonal entry; perm starts as the identity
     // so that it stays a valid index table whatever the values
-    for (int i = tid; i < n0; i += kThreads) perm[i] = i;
+    for (int i = tid; i < n0; i += kJThreads) perm[i] = i;
     __syncthreads();
-    for (int i = tid; i < n0; i += kThreads) {
+    for (int i = tid; i < n0; i += kJThreads) {
         const float di = a[i * ld + i];
         int rank = 0;
         for (int j = 0; j < n0; ++j) {
@@ -193,9 +197,9 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     }
     __syncthreads();
     if (lane < n0)
-        for (int i = kg; i < n0; i += 2)
+        for (int i = kg; i < n0; i += kJGroups)
             X[b * xstride + (long)i * ldx + lane] = (double)v[i * ld + perm[lane]];
-    for (int k = tid; k < n0; k += kThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
+    for (int k = tid; k < n0; k += kJThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
 }
 
 // Early exit of the refinement steps (EigBatch::skip_tol).  Step s of
@@ -342,7 +346,7 @@ k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, in
 // individual vectors inside a cluster matter (the canonical basis: the
 // occupation-weighted density sum is not invariant under rotations between
 // states of slightly different occupation).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kJThreads)
 k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* __restrict__ nsz,
                   const double* __restrict__ anorm, double* __restrict__ Q,
                   double* __restrict__ w, long wstride, int* __restrict__ pfail) {
@@ -361,13 +365,13 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     double* q = Q + b * stride;
     auto Qa = [&](int r, int c) -> double& { return q[(long)r * ld + c]; };
     const int tid = threadIdx.x;
-    for (int t = tid; t < n * n; t += kThreads) {
+    for (int t = tid; t < n * n; t += kJThreads) {
         const int i = t / n, j = t % n;
         const double x = (i < n0 && j < n0) ? S[b * stride + (long)i * ld + j] : 0.0;
         const double y = (i < n0 && j < n0) ? S[b * stride + (long)j * ld + i] : 0.0;
         a[i * l2 + j] = i == j ? x : 0.5 * (x + y);
     }
-    for (int t = tid; t < n0 * n0; t += kThreads) Qa(t / n0, t % n0) = (t / n0 == t % n0) ? 1.0 : 0.0;
+    for (int t = tid; t < n0 * n0; t += kJThreads) Qa(t / n0, t % n0) = (t / n0 == t % n0) ? 1.0 : 0.0;
     __syncthreads();
     const double thr = 1e-14 * anorm[b];
     const int lane = tid & 127, kg = tid >> 7;
@@ -378,7 +382,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
         // (~ sqrt(n) eps |A|): rotating noise would only churn, at FP64 cost
         int any = 0;
         if (lane < n)
-            for (int i = kg; i < n; i += 2)
+            for (int i = kg; i < n; i += kJGroups)
                 if (i != lane && fabs(a[i * l2 + lane]) > thr) any = 1;
         if (!__syncthreads_or(any)) break;
         for (int r = 0; r < n - 1; ++r) {
@@ -413,7 +417,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
             // rounds without a pair above the threshold rotate nothing
             if (!__syncthreads_or(on)) continue;
             if (lane < n)
-                for (int k = kg; k < half; k += 2) {
+                for (int k = kg; k < half; k += kJGroups) {
                     if (!act[k]) continue;
                     const int p = pqi[0][k], qq = pqi[1][k];
                     const double c = cs[0][k], s = cs[1][k];
@@ -423,7 +427,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
                 }
             __syncthreads();
             if (lane < n)
-                for (int k = kg; k < half; k += 2) {
+                for (int k = kg; k < half; k += kJGroups) {
                     if (!act[k]) continue;
                     const int p = pqi[0][k], qq = pqi[1][k];
                     const double c = cs[0][k], s = cs[1][k];
@@ -440,7 +444,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
         }
     }
     if (tid == 0 && pfail) pfail[b] = sweep == 12 ? 1 : 0;
-    for (int i = tid; i < n0; i += kThreads) w[b * wstride + i] = a[i * l2 + i];
+    for (int i = tid; i < n0; i += kJThreads) w[b * wstride + i] = a[i * l2 + i];
 }
 
 // Re-orthonormalisation X <- X (I + R/2 + 3/8 R^2), R = I - X^T X (third-order
@@ -538,7 +542,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     if (seed != kSeedRefine) {
         const bool warm = seed == kSeedJacobiWarm;
         const size_t sm = jacobi_smem(E.nmax);
-        k_jacobi32<<<E.nb, kThreads, sm, c->stream>>>(E.A, E.stride, E.ld, E.nsz,
+        k_jacobi32<<<E.nb, kJThreads, sm, c->stream>>>(E.A, E.stride, E.ld, E.nsz,
                                                       warm ? E.X : nullptr, E.X, E.stride, E.ld,
                                                       E.w, E.wstride, warm ? 12 : 30, c->flags + 4);
         MG_LAUNCHED(c);
@@ -590,7 +594,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
         MG_LAUNCHED(c);
-        k_jacobi64_polish<<<E.nb, kThreads, psm, c->stream>>>(
+        k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(
             E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail);
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
