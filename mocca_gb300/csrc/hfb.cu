@@ -450,7 +450,13 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     // leaves it, steps clamped to 5 MeV) ----------------------------------------
     const double prec = H.pp.fermi_prec;
     int evals = 0;
+    // start from the last Fermi energies, linearly extrapolated along the
+    // iterations once two converged ones exist (the root is the same; the
+    // first evaluation only lands closer to it)
     double lam[2] = {H.fermi[0], H.fermi[1]}, f[2], fp[2];
+    for (int it = 0; it < 2; ++it)
+        if (H.n_solved >= 2 && std::fabs(H.fermi[it] - H.fermi_prev[it]) < 0.5)
+            lam[it] = 2.0 * H.fermi[it] - H.fermi_prev[it];
     MG_TRY(hfb_evaluate(c, lam, f, fp, true));
     ++evals;
     bool conv[2] = {std::fabs(f[0]) < prec, std::fabs(f[1]) < prec};
@@ -480,6 +486,13 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
             if (std::fabs(f[it]) < prec) { conv[it] = true; continue; }
             bracket(it);
         }
+    }
+    if (conv[0] && conv[1]) {
+        H.fermi_prev[0] = H.fermi[0];
+        H.fermi_prev[1] = H.fermi[1];
+        ++H.n_solved;
+    } else {
+        H.n_solved = 0;
     }
     H.fermi[0] = lam[0];
     H.fermi[1] = lam[1];

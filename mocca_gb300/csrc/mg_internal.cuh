@@ -128,6 +128,8 @@ struct Hfb {
     double* scal_d = nullptr;                  // [energy(2), disp(2)]
     double* h_pinned = nullptr;                // 8 pinned doubles
     double fermi[2] = {-10.0, -10.0};
+    double fermi_prev[2] = {-10.0, -10.0};     // Fermi energies of the solve before
+    int n_solved = 0;                          // consecutive converged solves
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
     long long eval_graph_launches[3] = {0, 0, 0};
