@@ -3,7 +3,7 @@
 Workload (the 24^3 configuration the headline metric is quoted on): N=Z=28,
 24^3 stored EV8 mesh (48^3 full box), dx=0.8 fm, nwt=160 spinors (80 n +
 80 p), SLy4, time-reversal invariant, HFB pairing (G=1250 MeV fm^3,
-alpha=1), seeded harmonic-oscillator start, imaginary-time step dt=0.005
+alpha=1), seeded harmonic-oscillator start, imaginary-time step dt=0.010
 with momentum 0.3.  A step is one pass of the Evolve loop body
 (src/Main.f90:255-328): GradDesc with Gram-Schmidt, the HFB pairing step,
 DeriveAll, densities, moments, potentials with the Coulomb CG, energy.
@@ -22,7 +22,8 @@ the spinors plus the energy read back every step.  The working set
 (spinors, derivatives, updates: ~0.7 GB) is larger than the 129 MB L2, so
 no flush is needed between steps.  Multi-GPU runs are independent replicas
 (weak scaling).  `microbench_32c_200` times DeriveAll and h.psi of 200
-spinors on the 32^3 symmetry-free box in both precisions.
+spinors on the 32^3 symmetry-free box in both precisions, and `poisson_64c`
+one Coulomb solve on a 64^3 mesh.
 """
 from __future__ import annotations
 
@@ -41,7 +42,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOAD = dict(nx=24, ny=24, nz=24, dx=0.8, nwt=160, neutrons=28.0, protons=28.0)
-DT, MOMENTUM = 0.005, 0.3
+DT, MOMENTUM = 0.010, 0.3
 POLISH = 20   # final FP64 iterations of the mixed form
 METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
 # DRAM traffic of one DeriveBasis launch pair (k_deriv_xy_df + k_deriv_z_df,
@@ -58,7 +59,7 @@ def _params(precision):
 def _config(precision, world):
     return {"workload": "N=Z=28 HO start (seed 1234), 24^3 EV8 stored mesh, dx=0.8, nwt=160, "
                         "SLy4, TRC, HFB pairing G=1250 alpha=1 (surface delta, 5 MeV cutoff), "
-                        "dt=0.005, momentum 0.3",
+                        "dt=0.010, momentum 0.3, MixingScheme 0 (DampingParam 0.75)",
             **WORKLOAD, "precision": precision, "dt": DT, "momentum": MOMENTUM,
             "l2": "working set ~0.7 GB > 129 MB L2, no flush",
             "parallelism": f"replicas x{world}"}
@@ -290,6 +291,40 @@ def microbench_c2(torch, stream, reps=5):
     return out
 
 
+def poisson_64c(torch, stream):
+    """Coulomb problem on the 64^3 stored EV8 mesh (128^3 full box), dx=0.8: a
+    deformed Gaussian proton density (Z=40, axes 1:1:1.3, width 3 fm), multipole
+    boundary values; one cold solve from the uniform-sphere guess.  FP64: the
+    reference's CG to its tolerance.  Mixed: the direct separable solve with
+    two FP64 refinement rounds."""
+    import numpy as np
+    from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, synthetic
+    from mocca_gb300.mesh import MeshState
+    out = {"workload": "64^3 EV8 stored (128^3 box), dx=0.8, Gaussian rho_p Z=40, "
+                       "axes 1:1:1.3, width 3 fm"}
+    for name, prec in (("fp64", MG_FP64), ("mixed", MG_MIXED)):
+        p = RunParams(nx=64, ny=64, nz=64, dx=0.8, nwt=2, neutrons=40, protons=40,
+                      precision=prec)
+        x, y, z = synthetic.mesh_axes(p)
+        X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+        rp = np.exp(-(X ** 2 + Y ** 2) / 9.0 - Z ** 2 / (9.0 * 1.69)).transpose(2, 1, 0)
+        rp *= 40.0 / (rp.sum() * p.dv)
+        rho = np.concatenate([rp.reshape(-1), rp.reshape(-1)])
+        with torch.cuda.stream(stream):
+            g = MeshState(p, SLY4, stream=stream.cuda_stream)
+        g.set_densities(rho=rho)
+        g.CalculateAllMoments()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        it = g.SolveCoulomb()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"ms": e0.elapsed_time(e1), "iterations": it}
+        g.close()
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mocca_gb300 import _abi
@@ -371,6 +406,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and args.precision == "mixed" and args.accuracy_iters > POLISH:
         accuracy = accuracy_check(args.accuracy_iters, seed)
     micro = microbench_c2(torch, stream) if rank == 0 and args.micro else None
+    poisson = poisson_64c(torch, stream) if rank == 0 and args.micro else None
 
     if rank != 0:
         return None
@@ -416,6 +452,8 @@ def run_ours(args, rank, world, local_rank):
         res["breakdown_ms"] = breakdown
     if micro:
         res["microbench_32c_200"] = micro
+    if poisson:
+        res["poisson_64c"] = poisson
     return res
 
 
@@ -454,7 +492,7 @@ def main():
     ap.add_argument("--accuracy-iters", type=int, default=300)
     ap.add_argument("--breakdown", action="store_true")
     ap.add_argument("--no-micro", dest="micro", action="store_false",
-                    help="skip the 32^3 mesh-kernel microbench line")
+                    help="skip the 32^3 mesh-kernel and 64^3 Poisson lines")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -73,6 +73,11 @@ typedef struct mg_params {
     int    coulomb_max;        /* CoulombMax, default 500 (src/Coulomb.f90:24) */
     int    max_l_coul;         /* MaxLCoul, default MaxMoment = 10 */
     int    coulomb_solver;     /* 0 none, 1 CG (reference default) */
+    int    mixing_scheme;      /* MixingScheme (src/DensityMixing.f90:22-86): 0 linear
+                                  density mixing (reference default), 2 preconditioned
+                                  U update (src/PotentialMixing.f90:143-154) */
+    double damping;            /* DampingParam, 0.75 (src/Densities.f90:17) */
+    double precon_u;           /* preconu, 1.0 (src/Densities.f90:34) */
 } mg_params;
 
 /*
@@ -239,6 +244,12 @@ int mg_hf_fill(mg_ctx* ctx);
 /* ComputeDensity over the density basis (src/Densities.f90:431-550):
  * rho, tau, div J, grad rho, lap rho. */
 int mg_update_densities(mg_ctx* ctx);
+/* MixDensities (src/DensityMixing.f90:22-86) after mg_update_densities:
+ * scheme 0 mixes every density with the previous iteration's,
+ * rho <- (1 - damping) rho + damping rho_previous; scheme 2 does nothing here
+ * (mg_construct_potentials preconditions the U update instead).
+ * mg_update_densities keeps the densities it replaces as that history. */
+int mg_mix_densities(mg_ctx* ctx);
 /* Arrays of 2V (rho,tau,nablaj,laprho) and 6V (derrho); any may be NULL. */
 int mg_get_densities(mg_ctx* ctx, double* rho, double* tau, double* nablaj,
                      double* derrho, double* laprho);

@@ -44,6 +44,9 @@ class MgParams(C.Structure):
         ("coulomb_max", C.c_int),
         ("max_l_coul", C.c_int),
         ("coulomb_solver", C.c_int),
+        ("mixing_scheme", C.c_int),
+        ("damping", C.c_double),
+        ("precon_u", C.c_double),
     ]
 
 
@@ -152,6 +155,7 @@ SIGNATURES = {
     "mg_gram_schmidt": [_P],
     "mg_hf_fill": [_P],
     "mg_update_densities": [_P],
+    "mg_mix_densities": [_P],
     "mg_get_densities": [_P, _D, _D, _D, _D, _D],
     "mg_set_densities": [_P, _D, _D, _D, _D, _D],
     "mg_calculate_moments": [_P],

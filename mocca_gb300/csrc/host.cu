@@ -36,6 +36,7 @@ void free_all(mg_ctx* c) {
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast);
+    F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
     hfb_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -128,6 +129,9 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     const bool full = !p->pc && !p->sc && !p->tsc;
     if (!ev8 && !full) return MG_ERR_ARG;
     if (p->precision != MG_FP64 && p->precision != MG_MIXED) return MG_ERR_ARG;
+    if ((p->mixing_scheme != 0 && p->mixing_scheme != 2) || !(p->damping >= 0.0) ||
+        p->damping > 1.0)
+        return MG_ERR_ARG;
     if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
@@ -188,6 +192,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     c->cur_precision = p->precision;
     if ((st = upload_matrices(c)) != MG_OK) return fail(st);
     if ((st = build_field_jobs(c)) != MG_OK) return fail(st);
+    if ((st = mixing_setup(c)) != MG_OK) return fail(st);
     if (ev8 && p->coulomb_solver != 0) {
         if ((st = coulomb_setup(c)) != MG_OK) return fail(st);
     }
@@ -393,7 +398,13 @@ extern "C" int mg_hf_fill(mg_ctx* c) {
 
 extern "C" int mg_update_densities(mg_ctx* c) {
     if (!c) return MG_ERR_ARG;
+    MG_TRY(save_density_history(c));
     return densities(c);
+}
+
+extern "C" int mg_mix_densities(mg_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    return mix_densities(c);
 }
 
 static int copy_out(mg_ctx* c, double* dst, const double* src, long n) {
@@ -458,7 +469,13 @@ extern "C" int mg_construct_potentials(mg_ctx* c, int* iters) {
     } else if (iters) {
         *iters = 0;
     }
+    // UpotOld = Upot (src/PotentialMixing.f90:115); MixingScheme 2 then
+    // preconditions the update once UpotOld is not all zero
+    MG_CUDA(cudaMemcpyAsync(c->Uold, c->U, 2 * c->V * sizeof(double), cudaMemcpyDeviceToDevice,
+                            c->stream));
     MG_TRY(potentials(c));
+    if (c->p.mixing_scheme == 2 && c->have_uold) MG_TRY(precondition_u(c));
+    c->have_uold = true;
     return st;
 }
 
@@ -482,6 +499,7 @@ extern "C" int mg_set_potentials(mg_ctx* c, const double* u, const double* b,
     if (!c) return MG_ERR_ARG;
     const long V = c->V;
     MG_TRY(copy_in(c, c->U, u, 2 * V));
+    if (u) c->have_uold = true;   // the next UpotOld is this U
     MG_TRY(copy_in(c, c->Bp, b, 2 * V));
     MG_TRY(copy_in(c, c->nablaB, nablab, 6 * V));
     MG_TRY(copy_in(c, c->W, w, 18 * V));
@@ -555,7 +573,9 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         // canonical single-particle energies with the previous potentials
         // (src/Main.f90:282-289)
         if (hfb) MG_TRY(hpsi_basis(c, MG_CAN_BASIS, nullptr, false, 0.0, 0.0));
+        MG_TRY(save_density_history(c));
         MG_TRY(densities(c));
+        MG_TRY(mix_densities(c));
         MG_TRY(moments(c));
         st = mg_construct_potentials(c, nullptr);
         if (st < 0) return st;

@@ -206,6 +206,14 @@ struct mg_ctx {
     double* cfast = nullptr;           // 1-D eigenvectors and eigenvalues of the direct solve
     long cfast_off[3][2];              // [axis][0: C (n x n), 1: mu (n)]
 
+    // mixing between iterations (mixing.cu)
+    double* dhist = nullptr;           // previous densities: rho, tau, nablaj, derrho, laprho (14V)
+    bool have_dhist = false;
+    double* Uold = nullptr;            // UpotOld (2V)
+    bool have_uold = false;            // UpotOld not all zero
+    double* pc_buf = nullptr;          // preconditioner CG: res, dir, upd, lap, inv (10V)
+    mg::GridJob* pc_jobs = nullptr;    // Laplacians of the two directions
+
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
 
@@ -244,6 +252,10 @@ int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
 void hfb_free(mg_ctx* c);
 int density_groups(const mg_ctx* c);
+int mixing_setup(mg_ctx* c);
+int save_density_history(mg_ctx* c);
+int mix_densities(mg_ctx* c);
+int precondition_u(mg_ctx* c);
 
 // Lagrange matrix slot selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8.
 __host__ __device__ inline int lag_slot(int dir, int P, int S, int TS, int comp) {

@@ -78,6 +78,9 @@ class RunParams:
     coulomb_max: int = 500
     max_l_coul: int = 10
     coulomb_solver: int = 1
+    mixing_scheme: int = 0      # MixingScheme: 0 linear density mixing, 2 preconditioned U
+    damping: float = 0.75       # DampingParam
+    precon_u: float = 1.0       # preconu
     extra: dict = field(default_factory=dict)
 
     @property

@@ -191,6 +191,9 @@ class MeshState:
     def UpdateDensities(self):
         self._call("mg_update_densities")
 
+    def MixDensities(self):
+        self._call("mg_mix_densities")
+
     def CalculateAllMoments(self):
         self._call("mg_calculate_moments")
 

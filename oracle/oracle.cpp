@@ -45,8 +45,11 @@ struct orc_ctx {
     std::vector<double> D[3][2], L[3][2];
     Basis bas[2];
     std::vector<double> updates;
-    // densities (src/Densities.f90:39-94)
+    // densities (src/Densities.f90:39-94) and the previous iteration's
+    // (DensityHistory(1), src/Densities.f90:406-429)
     std::vector<double> rho, tau, nablaj, derrho, laprho;
+    std::vector<double> hrho, htau, hnablaj, hderrho, hlaprho;
+    std::vector<double> Uold;   // UpotOld (src/PotentialMixing.f90:115)
     // potentials (src/MeanFields.f90:79-85)
     std::vector<double> U, Bp, nablaB, W, divW;
     // Coulomb (src/Coulomb.f90:20-105)
@@ -563,6 +566,9 @@ static inline double imag_mult(const double* a, const double* b) {
 extern "C" int orc_update_densities(orc_ctx* c) {
     if (!c) return MG_ERR_ARG;
     const long V = c->V;
+    // UpdateDensities(0): DensityHistory(1) = Density before recomputing
+    c->hrho = c->rho; c->htau = c->tau; c->hnablaj = c->nablaj;
+    c->hderrho = c->derrho; c->hlaprho = c->laprho;
     const Basis& B = c->bas[c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS];
     std::fill(c->rho.begin(), c->rho.end(), 0.0);
     std::fill(c->tau.begin(), c->tau.end(), 0.0);
@@ -603,6 +609,23 @@ extern "C" int orc_update_densities(orc_ctx* c) {
             derive_grid(c, &c->rho[it * V], d, P, S, TS, 1, &c->derrho[(it * 3 + d) * V]);
         derive_grid(c, &c->rho[it * V], 3, P, S, TS, 1, &c->laprho[it * V]);
     }
+    return MG_OK;
+}
+
+// MixDensities, src/DensityMixing.f90:22-86: scheme 0 mixes every density,
+// Density = (1 - DampingParam) Density + DampingParam DensityHistory(1);
+// scheme 2 leaves the densities (the U update is preconditioned instead).
+extern "C" int orc_mix_densities(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    if (c->p.mixing_scheme == 2) return MG_OK;
+    if (c->p.mixing_scheme != 0) return MG_ERR_ARG;
+    const double d = c->p.damping;
+    auto mix = [d](std::vector<double>& x, const std::vector<double>& h) {
+        if (h.size() != x.size()) return;
+        for (size_t k = 0; k < x.size(); ++k) x[k] = (1.0 - d) * x[k] + d * h[k];
+    };
+    mix(c->rho, c->hrho); mix(c->tau, c->htau); mix(c->nablaj, c->hnablaj);
+    mix(c->derrho, c->hderrho); mix(c->laprho, c->hlaprho);
     return MG_OK;
 }
 
@@ -932,9 +955,48 @@ static void calc_potentials(orc_ctx* c) {
     }
 }
 
+// PreconditionPotential + preconoperator, src/Damping.f90:158-228: per
+// isospin, CG on (beta + alpha Lap) x = pot with alpha = -preconu, beta = 1,
+// the Lagrange Laplacian of a (P, S, TS)-even scalar, at most 300 steps,
+// stop when sum(residual^2) dv < 1e-8.
+static void precondition_potential(orc_ctx* c, const std::vector<double>& pot,
+                                   std::vector<double>& inv) {
+    const long V = c->V;
+    const double alpha = -c->p.precon_u, beta = 1.0;
+    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+    inv.assign(2 * V, 0.0);
+    std::vector<double> res(V), dir(V), upd(V), lap(V);
+    for (int it = 0; it < 2; ++it) {
+        for (long v = 0; v < V; ++v) res[v] = pot[it * V + v];
+        dir = res;
+        double nn = 0.0;
+        for (long v = 0; v < V; ++v) nn = nn + dir[v] * dir[v];
+        nn = nn * c->dv;
+        for (int iter = 1; iter <= 300; ++iter) {
+            derive_grid(c, dir.data(), 3, P, S, TS, 1, lap.data());
+            for (long v = 0; v < V; ++v) upd[v] = beta * dir[v] + alpha * lap[v];
+            double dd = 0.0;
+            for (long v = 0; v < V; ++v) dd = dd + dir[v] * upd[v];
+            const double a = nn / (dd * c->dv);
+            for (long v = 0; v < V; ++v) {
+                inv[it * V + v] = inv[it * V + v] + a * dir[v];
+                res[v] = res[v] - a * upd[v];
+            }
+            const double old = nn;
+            nn = 0.0;
+            for (long v = 0; v < V; ++v) nn = nn + res[v] * res[v];
+            nn = nn * c->dv;
+            const double b = nn / old;
+            for (long v = 0; v < V; ++v) dir[v] = res[v] + b * dir[v];
+            if (nn < 1e-8) break;
+        }
+    }
+}
+
 extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
     if (!c) return MG_ERR_ARG;
     int st = MG_OK;
+    c->Uold = c->U;   // UpotOld = Upot (src/PotentialMixing.f90:115)
     if (c->p.coulomb_solver != 0) {
         st = orc_solve_coulomb(c, iters);
         if (st < 0) return st;
@@ -944,6 +1006,16 @@ extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
         if (iters) *iters = 0;
     }
     calc_potentials(c);
+    // MixingScheme 2: Upot = UpotOld + PreconditionPotential(Upot - UpotOld)
+    // once UpotOld is not all zero (src/PotentialMixing.f90:143-154)
+    bool have_old = false;
+    for (double u : c->Uold) have_old = have_old || u != 0.0;
+    if (c->p.mixing_scheme == 2 && have_old) {
+        std::vector<double> du(c->U.size()), inv;
+        for (size_t k = 0; k < du.size(); ++k) du[k] = c->U[k] - c->Uold[k];
+        precondition_potential(c, du, inv);
+        for (size_t k = 0; k < du.size(); ++k) c->U[k] = c->Uold[k] + inv[k];
+    }
     return st;
 }
 
@@ -1660,6 +1732,7 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
         if (hfb) orc_hpsi(c, MG_CAN_BASIS, nullptr, c->bas[MG_CAN_BASIS].e.data(),
                           c->bas[MG_CAN_BASIS].disp.data());
         orc_update_densities(c);
+        orc_mix_densities(c);
         orc_calculate_moments(c);
         st = orc_construct_potentials(c, nullptr);
         if (st < 0) return st;

@@ -55,6 +55,7 @@ int orc_grad_desc(orc_ctx* c, double dt, double momentum);
 int orc_gram_schmidt(orc_ctx* c);
 int orc_hf_fill(orc_ctx* c);
 int orc_update_densities(orc_ctx* c);
+int orc_mix_densities(orc_ctx* c);
 int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* nablaj,
                       double* derrho, double* laprho);
 int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,

@@ -44,6 +44,7 @@ _SIG = {
     "orc_gram_schmidt": ([_P], C.c_int),
     "orc_hf_fill": ([_P], C.c_int),
     "orc_update_densities": ([_P], C.c_int),
+    "orc_mix_densities": ([_P], C.c_int),
     "orc_get_densities": ([_P, _D, _D, _D, _D, _D], C.c_int),
     "orc_set_densities": ([_P, _D, _D, _D, _D, _D], C.c_int),
     "orc_calculate_moments": ([_P], C.c_int),
@@ -229,6 +230,9 @@ class OracleState:
 
     def UpdateDensities(self):
         self._call("orc_update_densities")
+
+    def MixDensities(self):
+        self._call("orc_mix_densities")
 
     def CalculateAllMoments(self):
         self._call("orc_calculate_moments")

@@ -30,7 +30,7 @@ def mg24_hf():
     sp, disp = o.get_energies()
     return {
         "config": "Mg24 (N=Z=12), EV8+TRC, 10^3 stored mesh, dx=0.8, nwt=40, SLy4, HF filling, "
-                  "HO start seed 1234 amplitude 1e-3",
+                  "HO start seed 1234 amplitude 1e-3, MixingScheme 0 (DampingParam 0.75)",
         "iterations": n, "dt": dt, "momentum": mom,
         "E_start": e0["total"], "E_final": e["total"],
         "kinetic_final": e["kinetic"], "coulomb_final": e["coulomb"],

@@ -141,3 +141,40 @@ def test_golden_fixture():
     assert e["total"] == pytest.approx(g["E_final"], abs=1e-9)
     sp, _ = o.get_energies()
     assert np.allclose(sp, g["sp_energies"], atol=1e-9, rtol=0)
+
+
+def test_precondition_potential_scheme2():
+    """MixingScheme 2 (PreconditionPotential): the oracle's CG solves
+    (1 - preconu Lap) x = dU to sum(r^2) dv < 1e-8, and the run still
+    lowers the energy."""
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  mixing_scheme=2)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.Start()
+    e1 = o.Evolve(2, 0.010, 0.3)["total"]
+    e2 = o.Evolve(4, 0.010, 0.3)["total"]
+    assert e2 < e1
+
+
+def test_mix_densities_scheme0():
+    """MixingScheme 0: after UpdateDensities + MixDensities every density is
+    (1 - 0.75) new + 0.75 previous."""
+    p = RunParams(nx=8, ny=8, nz=8, dx=0.8, nwt=16, neutrons=4, protons=4)
+    psi, qn, en = synthetic.ho_basis(p, 8, seed=3)
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.Start()
+    prev = o.get_densities()
+    o.GradDesc(0.01, 0.0)
+    o.HFFill()
+    o.DeriveAll()
+    o.UpdateDensities()
+    new = o.get_densities()
+    o.MixDensities()
+    mixed = o.get_densities()
+    for k in mixed:
+        np.testing.assert_allclose(mixed[k], 0.25 * new[k] + 0.75 * prev[k], rtol=0, atol=1e-14)
