@@ -39,6 +39,9 @@ void free_all(mg_ctx* c) {
     F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
     hfb_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -154,6 +157,16 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
             return fail(MG_ERR_CUDA);
         c->own_stream = true;
+    }
+    // side stream (lower priority) for the HF-basis derivatives, which run
+    // while the latency-bound Fermi search of the pairing step occupies few SMs
+    {
+        int lo = 0, hi = 0;
+        if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, lo) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail(MG_ERR_CUDA);
     }
     const long V = c->V, nwt = p->nwt;
     auto A = [&](double** ptr, long n) {
@@ -567,9 +580,25 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
         MG_TRY(mg_grad_desc(c, dt, momentum));
-        if (hfb) MG_TRY(mg_solve_pairing(c, nullptr));
-        else MG_TRY(mg_hf_fill(c));
-        MG_TRY(mg_derive_all(c));
+        if (hfb) {
+            // DeriveAll of the HF basis needs only the new HF spinors: it runs
+            // on the side stream while the pairing step (which reads the same
+            // spinors) runs on the main stream; the canonical basis follows
+            MG_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+            MG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+            cudaStream_t main = c->stream;
+            c->stream = c->side;
+            const int sd = derive_basis(c, MG_HF_BASIS);
+            c->stream = main;
+            MG_TRY(sd);
+            MG_CUDA(cudaEventRecord(c->ev_join, c->side));
+            MG_TRY(mg_solve_pairing(c, nullptr));
+            MG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+            MG_TRY(derive_basis(c, MG_CAN_BASIS));
+        } else {
+            MG_TRY(mg_hf_fill(c));
+            MG_TRY(mg_derive_all(c));
+        }
         // canonical single-particle energies with the previous potentials
         // (src/Main.f90:282-289)
         if (hfb) MG_TRY(hpsi_basis(c, MG_CAN_BASIS, nullptr, false, 0.0, 0.0));

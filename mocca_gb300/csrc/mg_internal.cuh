@@ -155,6 +155,8 @@ struct mg_ctx {
     bool folded;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    cudaStream_t side = nullptr;        // low-priority stream for overlapped work
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int num_sms = 0;
 
     // Lagrange matrices: [axis][kind: 0 first, 1 second][slot][q*n+i]
