@@ -47,7 +47,7 @@ POLISH = 20   # final FP64 iterations of the mixed form
 METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
 # DRAM traffic of one DeriveBasis launch pair (k_deriv_xy_df + k_deriv_z_df,
 # nwt=160, 24^3) from ncu dram__bytes_read.sum + dram__bytes_write.sum
-DERIV_DF_TRAFFIC = 450.0e6
+DERIV_DF_TRAFFIC = 456.4e6
 
 
 def _params(precision):

@@ -142,7 +142,7 @@ __device__ __forceinline__ void pauli_df(const dfl* p, int dir, dfl* o) {
 }
 
 template <bool kGradStep>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
 k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
           const float2* __restrict__ lap, const int* __restrict__ qn, Fields F,
           double* __restrict__ hout, double* __restrict__ upd, double* __restrict__ partial,
@@ -158,35 +158,48 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
         double* ps = psi + (long)i * 4 * V;
         const float2* dr = der + (long)i * 12 * V;
         const float2* lp = lap + (long)i * 4 * V;
-        // every load first: the spinor, its derivatives, the update history
+        // the spinor and the update history first; the derivatives one
+        // direction at a time (each direction's values die after use, which
+        // keeps the live registers low enough for more resident warps)
         double p64[4], u64[4];
-        dfl p[4], d[3][4], L[4];
+        dfl p[4];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             p64[l] = ps[l * V + v];
             if (kGradStep) u64[l] = upd[(long)i * 4 * V + l * V + v];
-            L[l] = df_ld(lp + l * V + v);
-#pragma unroll
-            for (int m = 0; m < 3; ++m) d[m][l] = df_ld(dr + (m * 4 + l) * V + v);
         }
 #pragma unroll
         for (int l = 0; l < 4; ++l) p[l] = df_split(p64[l]);
-        const dfl kB = df_add(df_split(F.B[it * V + v]), df_split(kin));
-        const dfl Uq = df_split(F.U[it * V + v]);
-        const dfl nb[3] = {df_split(F.nablaB[(it * 3 + 0) * V + v]),
-                           df_split(F.nablaB[(it * 3 + 1) * V + v]),
-                           df_split(F.nablaB[(it * 3 + 2) * V + v])};
+        // B, U: -(B + hbar^2/2m) lap psi + U psi
+        float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
+        {
+            const dfl nkB = df_neg(df_add(df_split(F.B[it * V + v]), df_split(kin)));
+            const dfl Uq = df_split(F.U[it * V + v]);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                df_acc(th[l], tl[l], nkB, df_ld(lp + l * V + v));
+                df_acc(th[l], tl[l], Uq, p[l]);
+            }
+        }
+        // per direction mu: -(d_mu B) d_mu psi and sum_nu W_{nu mu} sigma_nu d_mu psi
         float wh[4] = {0.f, 0.f, 0.f, 0.f}, wl[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int mu = 0; mu < 3; ++mu)
+        for (int mu = 0; mu < 3; ++mu) {
+            dfl dm[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) dm[l] = df_ld(dr + (mu * 4 + l) * V + v);
+            const dfl nb = df_neg(df_split(F.nablaB[(it * 3 + mu) * V + v]));
+#pragma unroll
+            for (int l = 0; l < 4; ++l) df_acc(th[l], tl[l], nb, dm[l]);
 #pragma unroll
             for (int nu = 0; nu < 3; ++nu) {
                 dfl sg[4];
-                pauli_df(d[mu], nu + 1, sg);
+                pauli_df(dm, nu + 1, sg);
                 const dfl wv = df_split(F.W[((it * 3 + nu) * 3 + mu) * V + v]);
 #pragma unroll
                 for (int l = 0; l < 4; ++l) df_acc(wh[l], wl[l], wv, sg[l]);
             }
+        }
 #pragma unroll
         for (int nu = 0; nu < 3; ++nu) {
             dfl sg[4];
@@ -203,13 +216,7 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
         dfl h[4];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-            float th = 0.f, tl = 0.f;
-            df_acc(th, tl, df_neg(kB), L[l]);
-            df_acc(th, tl, df_neg(nb[0]), d[0][l]);
-            df_acc(th, tl, df_neg(nb[1]), d[1][l]);
-            df_acc(th, tl, df_neg(nb[2]), d[2][l]);
-            df_acc(th, tl, Uq, p[l]);
-            h[l] = df_add(df_norm(dfl{th, tl}), wf[l]);
+            h[l] = df_add(df_norm(dfl{th[l], tl[l]}), wf[l]);
             df_acc(eh, el, p[l], h[l]);
             df_acc(hh, hl, h[l], h[l]);
         }
