@@ -130,6 +130,21 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def max_over_ranks(x, device="cuda"):
+    """The slowest rank's time (replicas: the whole job ends with it)."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, steps, seconds):
+    """Weak scaling: every rank runs `steps` iterations of its own replica."""
+    return world * steps / seconds
+
+
 def measured_peaks():
     try:
         return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -339,13 +354,6 @@ def run_ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
     with torch.cuda.stream(stream):
         p, g = _make(args.precision, seed, stream=stream.cuda_stream)
     g.Evolve(max(3, args.warmup), DT, MOMENTUM)
@@ -399,7 +407,7 @@ def run_ours(args, rank, world, local_rank):
         t64, _, _, _ = _timed_steps(g64, torch, stream, args.steps, barrier)
         t64 = max_over_ranks(t64)
         g64.close()
-        fp64 = {"value": world * args.steps / t64, "unit": "iter/s",
+        fp64 = {"value": whole_job_rate(world, args.steps, t64), "unit": "iter/s",
                 "ms_per_step": t64 / args.steps * 1e3}
 
     accuracy = None
@@ -414,7 +422,7 @@ def run_ours(args, rank, world, local_rank):
     hbm = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = fp64_dgemm_peak(torch)
     mixed = args.precision == "mixed"
-    value = world * args.steps / t_dev
+    value = whole_job_rate(world, args.steps, t_dev)
     res = {
         "metric": METRIC,
         "value": value,
@@ -425,7 +433,7 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f64 (double-float mesh kernels)" if mixed else "f64",
         "data": "synthetic",
         "config": _config(args.precision, world),
-        "e2e": {"value": world * args.steps / t_e2e, "unit": "iter/s",
+        "e2e": {"value": whole_job_rate(world, args.steps, t_e2e), "unit": "iter/s",
                 "h2d_bytes_per_step": int(host_psi.numel() * 8),
                 "d2h_bytes_per_step": int(out_psi.numel() * 8 + C.sizeof(e_terms))},
         "roofline": {"kernel": ("k_deriv_xy_df + k_deriv_z_df" if mixed else

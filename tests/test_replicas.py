@@ -1,0 +1,46 @@
+"""The multi-GPU mode of bench.py is independent replicas: no data-path
+collective, only the timing reduction (max over ranks) and the weak-scaling
+rate.  Checked here with two gloo ranks on the CPU."""
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _rank(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world))
+    sys.path.insert(0, str(ROOT))
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    t = bench.max_over_ranks(1.0 + rank, device="cpu")
+    out.put((rank, t, bench.whole_job_rate(world, 10, t)))
+    dist.destroy_process_group()
+
+
+def test_replica_timing_two_ranks():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    world, port = 2, 29517
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, t, rate in res:
+        assert t == 2.0             # the slowest rank's time on every rank
+        assert rate == 2 * 10 / 2.0  # all ranks' iterations over that time
+
+
+def test_max_over_ranks_single_process():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert bench.max_over_ranks(3.5, device="cpu") == 3.5
