@@ -388,7 +388,7 @@ int upload_matrices(mg_ctx* c) {
     }
     MG_CUDA(cudaMalloc(&c->mats32, total32 * sizeof(float)));
     MG_CUDA(cudaMemcpy(c->mats32, h32.data(), total32 * sizeof(float), cudaMemcpyHostToDevice));
-    return MG_OK;
+    return tc_setup(c);
 }
 
 int build_basis_jobs(mg_ctx* c, int b) {
@@ -462,11 +462,16 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
 
 // In the mixed form the basis derivatives stay double-float in HBM (the same
 // 8 bytes per value), so that h.psi and the densities read them without FP64
-// conversions; Basis::der_df records the format.
+// conversions; Basis::der_df records the format.  They come from the tensor
+// cores (deriv_tc.cu) when every line length is at most 32, else from the
+// double-float kernels above.
 int derive_basis(mg_ctx* c, int b) {
     if (!c->bas[b].have_qn) return MG_ERR_STATE;
     const bool df = c->cur_precision == MG_MIXED;
-    MG_TRY(run_jobs(c, c->bas[b].jobs, 4 * c->p.nwt, df));
+    if (df && c->tc_ok)
+        MG_TRY(run_jobs_tc(c, c->bas[b].jobs, 4 * c->p.nwt));
+    else
+        MG_TRY(run_jobs(c, c->bas[b].jobs, 4 * c->p.nwt, df));
     c->bas[b].der_df = df;
     return MG_OK;
 }

@@ -14,7 +14,9 @@
 //   k_gs_factor   : S = R^T R, X = R^{-1} (one block per CTA, in smem)
 //   k_gs_apply    : psi'_l = sum_{k<=l} X_kl psi_k in place (+ update history)
 // For the near-orthonormal input of an imaginary-time step cond(S) ~ 1, so
-// the Cholesky form keeps full FP64 accuracy.
+// the Cholesky form keeps full FP64 accuracy.  In the mixed form the overlap
+// and the apply run on the tensor cores instead (gs_tc.cu); the sum, the
+// factorisation and the order stay these FP64 kernels.
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -25,23 +27,29 @@ constexpr int kThreads = 256;
 constexpr int kPts = 64;  // points per shared-memory tile
 
 // gs_index layout: [0..nblk] block starts, then member lists (nwt ints) in
-// index order (static), then the energy-ordered lists (nwt ints).
+// index order (static), then the energy-ordered lists (nwt ints).  One CTA
+// per block; member i goes to its rank in (energy, list position) order, a
+// stable sort (NaN energies sort last, in list order).
 __global__ void k_gs_order(const int* __restrict__ lists, int nblk, int nwt,
                            const double* __restrict__ e, int* __restrict__ ordered) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nblk) return;
-    const int s0 = lists[b], s1 = lists[b + 1];
-    const int* mem = lists + nblk + 1;
-    int* out = ordered;
-    for (int q = s0; q < s1; ++q) {
-        const int idx = mem[q];
-        const double en = e[idx];
-        int pos = q;
-        while (pos > s0 && en < e[out[pos - 1]]) {
-            out[pos] = out[pos - 1];
-            --pos;
+    extern __shared__ double se[];
+    const int b = blockIdx.x;
+    const int s0 = lists[b], nb = lists[b + 1] - s0;
+    const int* mem = lists + nblk + 1 + s0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) se[i] = e[mem[i]];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        const double ei = se[i];
+        const bool ni = isnan(ei);
+        int rank = 0;
+        for (int j = 0; j < nb; ++j) {
+            const double ej = se[j];
+            const bool nj = isnan(ej);
+            const bool before = (!ni && !nj) ? (ej < ei || (ej == ei && j < i))
+                                             : (nj == ni ? j < i : !nj);
+            rank += before ? 1 : 0;
         }
-        out[pos] = idx;
+        ordered[s0 + rank] = mem[i];
     }
 }
 
@@ -90,19 +98,27 @@ k_gs_overlap(const double* __restrict__ psi, const int* __restrict__ starts,
     }
 }
 
-// Sum the chunk partials of the upper triangle in chunk order (many threads:
-// one entry each); the result goes to chunk slot 0.
+// Sum the chunk partials of the upper triangle, one warp per entry: lane j
+// adds chunks j, j + 32, ... in order, then a fixed xor tree combines the
+// lanes (deterministic); the result goes to chunk slot 0.
 __global__ void k_gs_sum(double* __restrict__ part, int nbmax, int nchunk) {
     const int b = blockIdx.y;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
     if (t >= nbmax * nbmax || t / nbmax > t % nbmax) return;
     double* pb = part + (long)b * nchunk * nbmax * nbmax;
     double s = 0.0;
-    for (int q = 0; q < nchunk; ++q) s += pb[(long)q * nbmax * nbmax + t];
-    pb[t] = s;
+    for (int q = lane; q < nchunk; q += 32) s += pb[(long)q * nbmax * nbmax + t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncwarp();
+    if (lane == 0) pb[t] = s;
 }
 
-// Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].
+// Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].  The elimination
+// keeps the rows unscaled (one barrier per column): after step j row j holds
+// U[j][l] = R[j][j] R[j][l].  Then R = U / sqrt(diag) and each thread finds one
+// column of X by back substitution.
 __global__ void __launch_bounds__(kThreads)
 k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int nbmax,
             int nchunk, double dv, double* __restrict__ xout, int* __restrict__ flag) {
@@ -112,46 +128,45 @@ k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int
     if (nb == 0) return;
     double* S = sm;              // nb x nb (upper used), becomes R
     double* X = sm + nb * nb;    // nb x nb
+    __shared__ double rinv[256];
     for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
         const int k = t / nb, l = t % nb;
         S[t] = k <= l ? part[(long)b * nchunk * nbmax * nbmax + k * nbmax + l] * dv : 0.0;
         X[t] = 0.0;
     }
     __syncthreads();
-    // right-looking Cholesky on the upper triangle
     for (int j = 0; j < nb; ++j) {
-        if (threadIdx.x == 0) {
-            const double d = S[j * nb + j];
-            if (!(d > 0.0)) atomicExch(flag, 1);
-            S[j * nb + j] = sqrt(fmax(d, 1e-300));
-        }
-        __syncthreads();
-        const double rjj = S[j * nb + j];
-        for (int l = j + 1 + threadIdx.x; l < nb; l += kThreads) S[j * nb + l] /= rjj;
-        __syncthreads();
-        // trailing update S[k][l] -= R[j][k] R[j][l], j < k <= l
+        const double d = S[j * nb + j];
+        if (threadIdx.x == 0 && !(d > 0.0)) atomicExch(flag, 1);
+        const double inv_d = 1.0 / fmax(d, 1e-300);
         const int m = nb - j - 1;
         for (int t = threadIdx.x; t < m * m; t += kThreads) {
             const int k = j + 1 + t / m, l = j + 1 + t % m;
-            if (k <= l) S[k * nb + l] -= S[j * nb + k] * S[j * nb + l];
+            if (k <= l) S[k * nb + l] -= S[j * nb + k] * S[j * nb + l] * inv_d;
         }
         __syncthreads();
     }
-    // X = R^{-1}: column by column, X[j][j] = 1/R[j][j],
-    // X[i][j] = -(sum_{i<=k<j} X[i][k] R[k][j]) / R[j][j]
-    for (int j = 0; j < nb; ++j) {
-        const double rjj = S[j * nb + j];
-        for (int i = threadIdx.x; i <= j; i += kThreads) {
-            if (i == j) {
-                X[j * nb + j] = 1.0 / rjj;
-            } else {
-                double s = 0.0;
-                for (int k = i; k < j; ++k) s = fma(X[i * nb + k], S[k * nb + j], s);
-                X[i * nb + j] = -s / rjj;
-            }
-        }
-        __syncthreads();
+    for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
+        const int j = t / nb, l = t % nb;
+        if (l > j) S[t] = S[t] / sqrt(fmax(S[j * nb + j], 1e-300));
     }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nb; j += kThreads) {
+        const double r = sqrt(fmax(S[j * nb + j], 1e-300));
+        S[j * nb + j] = r;
+        if (j < 256) rinv[j] = 1.0 / r;
+    }
+    __syncthreads();
+    // X[i][j] = -(sum_{i<k<=j} R[i][k] X[k][j]) / R[i][i], X[j][j] = 1 / R[j][j]
+    for (int j = threadIdx.x; j < nb; j += kThreads) {
+        X[j * nb + j] = rinv[j];
+        for (int i = j - 1; i >= 0; --i) {
+            double s = 0.0;
+            for (int k = i + 1; k <= j; ++k) s = fma(S[i * nb + k], X[k * nb + j], s);
+            X[i * nb + j] = -s * rinv[i];
+        }
+    }
+    __syncthreads();
     double* xo = xout + (long)b * nbmax * nbmax;
     for (int t = threadIdx.x; t < nb * nb; t += kThreads) xo[(t / nb) * nbmax + t % nb] = X[t];
 }
@@ -241,17 +256,30 @@ int gram_schmidt_impl(mg_ctx* c, double* upd) {
     const long V4 = 4 * c->V;
     const int* d_lists = c->gs_index;
     int* d_ordered = c->gs_index + c->gs_lists_len;
-    k_gs_order<<<div_up(nblk, 32), 32, 0, c->stream>>>(d_lists, nblk, c->p.nwt, B.e, d_ordered);
+    k_gs_order<<<nblk, 128, nbmax * sizeof(double), c->stream>>>(d_lists, nblk, c->p.nwt, B.e,
+                                                                 d_ordered);
     MG_LAUNCHED(c);
+    const size_t sm_f = (size_t)(2 * nbmax * nbmax) * sizeof(double);
+    if (c->cur_precision == MG_MIXED && gs_tc_prepare(c)) {
+        // mixed form: the overlap and the apply on the tensor cores (gs_tc.cu)
+        const int nct = c->gs_nchunk_tc;
+        MG_TRY(gs_overlap_tc(c, B.psi, d_lists, d_ordered));
+        k_gs_sum<<<dim3(div_up((long)nbmax * nbmax, kThreads / 32), nblk), kThreads, 0,
+                   c->stream>>>(c->gs_Stc, nbmax, nct);
+        MG_LAUNCHED(c);
+        k_gs_factor<<<nblk, kThreads, sm_f, c->stream>>>(c->gs_Stc, d_lists, nbmax, nct, c->dv,
+                                                         c->gs_R, c->flags);
+        MG_LAUNCHED(c);
+        return gs_apply_tc(c, B.psi, upd, d_lists, d_ordered);
+    }
     const int npair_max = nbmax * (nbmax + 1) / 2;
     const size_t sm_ov = (size_t)(nbmax * kPts + npair_max) * sizeof(double);
-    const size_t sm_f = (size_t)(2 * nbmax * nbmax) * sizeof(double);
     const size_t sm_ap = (size_t)(nbmax * nbmax + nbmax * kPts) * sizeof(double);
     k_gs_overlap<<<dim3(nchunk, nblk), kThreads, sm_ov, c->stream>>>(B.psi, d_lists, d_ordered,
                                                                       nbmax, V4, nchunk, c->gs_S);
     MG_LAUNCHED(c);
-    k_gs_sum<<<dim3(div_up((long)nbmax * nbmax, kThreads), nblk), kThreads, 0, c->stream>>>(
-        c->gs_S, nbmax, nchunk);
+    k_gs_sum<<<dim3(div_up((long)nbmax * nbmax, kThreads / 32), nblk), kThreads, 0,
+               c->stream>>>(c->gs_S, nbmax, nchunk);
     MG_LAUNCHED(c);
     k_gs_factor<<<nblk, kThreads, sm_f, c->stream>>>(c->gs_S, d_lists, nbmax, nchunk, c->dv,
                                                      c->gs_R, c->flags);

@@ -1,0 +1,393 @@
+// gs_tc.cu -- the mixed form of the Gram-Schmidt step on the tcgen05 tensor
+// cores (exact BF16 digit products, ozaki.cuh).
+//
+// Same factorisation as gs.cu (GramSchmidt, src/SpwfStorage.f90:372-480, as
+// Q = Psi R^{-1} with S = R^T R per (isospin, parity, signature) block in
+// energy order); the two mesh-sized contractions move to the tensor cores:
+//   k_gs_overlap_tc : S partial sums over 256-point chunks.  Rows of the
+//                     MMA are the block's spinors (zero beyond nb), K the
+//                     chunk's points; A and B are the same digit planes.  Each
+//                     (spinor, chunk) row gets its own power of two.  The
+//                     partials go to the same table as the FP64 kernel, so
+//                     k_gs_sum / k_gs_factor (gs.cu) finish the job.
+//   k_gs_xdigits    : digit planes of X = R^{-1} (rows: output spinor l,
+//                     K: input spinor k), one power of two per row.
+//   k_gs_apply_tc   : psi'_l(p) = sum_k X[k][l] psi_k(p) for 128 points per
+//                     CTA (MMA M), K = the block's spinors, FP64 output in
+//                     place, plus the GradDesc history upd_l = psi'_l - upd_l.
+// A 256-point chunk keeps every digit-weight group of the overlap below 2^24
+// (at most 3 pairs x 256 points x 2^14), so its FP32 sums are exact.
+#include <algorithm>
+#include <vector>
+
+#include "mg_internal.cuh"
+#include "ozaki.cuh"
+#include "tc.cuh"
+
+namespace mg {
+
+namespace {
+
+using oz::kDigits;
+constexpr int kRows = 128;            // MMA M
+constexpr int kChunk = 256;           // overlap points per CTA
+constexpr int kStage = 32;            // overlap points per MMA stage (K)
+constexpr int kStagePlane = kRows * kStage * 2;   // bytes of one digit plane of a stage
+constexpr uint32_t kTmemCols = 256;
+constexpr long long kWaitCycles = 4000000000LL;
+
+__device__ __forceinline__ double pow2d(int x) {
+    return x < -1022 ? 0.0 : __longlong_as_double((long long)(min(x, 1023) + 1023) << 52);
+}
+
+// float -> double by bit moves (normal floats; zero and subnormals give 0)
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e == 0u) return 0.0;
+    const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const uint32_t lo = u << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__global__ void __launch_bounds__(256, 2)
+k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
+                const int* __restrict__ ordered, int nbmax, long V4, int nchunk,
+                double* __restrict__ part, int* __restrict__ status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sE[64];
+    const int b = blockIdx.y, chunk = blockIdx.x;
+    const int s0 = starts[b], nb = starts[b + 1] - s0;
+    if (nb == 0) return;
+    const int N = max(16, (nb + 15) / 16 * 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = tid >> 2, g = tid & 3;   // a row's 4 K groups sit on 4 neighbouring lanes
+    const bool live = row < nb;
+
+    const uint32_t s0a = tc::smem_u32(smraw);
+    uint8_t* base = smraw + ((128u - (s0a & 127u)) & 127u);
+    // two stage buffers of kDigits planes; rows >= nb stay zero
+    for (int t = tid; t < 2 * kDigits * kStagePlane / 16; t += 256)
+        reinterpret_cast<uint4*>(base)[t] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
+    const long p0 = (long)chunk * kChunk;
+    const int npts = (int)min((long)kChunk, V4 - p0);
+    const int nst = (npts + kStage - 1) / kStage;
+    const double* src = live ? psi + (long)ordered[s0 + row] * V4 + p0 : psi;
+
+    // largest exponent of the row over the chunk
+    int emax = 0;
+    if (live) {
+        for (int s = 0; s < nst; ++s) {
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                const int q = s * kStage + 8 * g + h;
+                if (q < npts) emax = max(emax, oz::bexp(src[q]));
+            }
+        }
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    if (live && g == 0) sE[row] = emax;
+
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = tc::idesc_bf16(kRows, N);
+    bool ok = true;
+    for (int s = 0; s < nst; ++s) {
+        const int buf = s & 1;
+        uint8_t* planes = base + buf * kDigits * kStagePlane;
+        if (s >= 2) ok &= tc::mbar_wait(&mbar[buf], ((s - 2) >> 1) & 1, kWaitCycles);
+        if (live) {
+            double v[8];
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                const int q = s * kStage + 8 * g + h;
+                v[h] = q < npts ? src[q] : 0.0;
+            }
+            uint4 w[kDigits];
+            oz::digits8(v, emax, w);
+#pragma unroll
+            for (int a = 0; a < kDigits; ++a)
+                *reinterpret_cast<uint4*>(planes + a * kStagePlane + tc::kmajor_off(row, 8 * g)) =
+                    w[a];
+        }
+        tc::fence_proxy_async();
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+            const uint32_t pa = tc::smem_u32(planes);
+            oz::issue_pairs<2>(tmem, N, idesc, pa, kStagePlane, tc::kSbo, pa, kStagePlane,
+                               tc::kSbo, s > 0);
+            tc::commit(&mbar[buf]);
+        }
+    }
+    const int last = nst - 1;
+    ok &= tc::mbar_wait(&mbar[last & 1], (last >> 1) & 1, kWaitCycles);
+    ok = __syncthreads_and(ok) != 0;
+    tc::fence_after();
+    if (ok) {
+        // D[k][l], k = TMEM lane (row), l = column; warps w and w + 4 share lane quarter w % 4
+        const int quarter = warp & 3, colh = warp >> 2;
+        const int k = quarter * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+        double* out = part + ((long)b * nchunk + chunk) * nbmax * nbmax;
+        const int ek = k < nb ? sE[k] - 1023 : 0;
+        for (int q = 0; q < N / 16; ++q) {
+            const int c0 = 16 * q + 8 * colh;
+            uint32_t r0[8], r1[8], r2[8], r3[8];
+            __syncwarp();
+            tc::ld8(trow + (uint32_t)(0 * N + c0), r0);
+            tc::ld8(trow + (uint32_t)(1 * N + c0), r1);
+            tc::ld8(trow + (uint32_t)(2 * N + c0), r2);
+            tc::ld8(trow + (uint32_t)(3 * N + c0), r3);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            tc::wait_ld(r2);
+            tc::wait_ld(r3);
+            if (k >= nb) continue;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int l = c0 + u;
+                if (l >= nb || l < k) continue;
+                const dfl o = oz::combine4(__uint_as_float(r0[u]), __uint_as_float(r1[u]),
+                                           __uint_as_float(r2[u]), __uint_as_float(r3[u]));
+                const double val = (f2d_bits(o.h) + f2d_bits(o.l)) * pow2d(ek + sE[l] - 1023 - 12);
+                out[k * nbmax + l] = val;
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(status, 1);
+    }
+    if (!ok) {
+        tc::mbar_wait(&mbar[0], 0, kWaitCycles);   // let the MMAs drain before the columns go
+        tc::mbar_wait(&mbar[1], 0, kWaitCycles);
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+}
+
+// Digit planes of X (per block: kDigits planes of Np rows x Np, row l = output
+// spinor, K = input spinor k) and the row exponents (biased).
+__global__ void k_gs_xdigits(const double* __restrict__ xin, const int* __restrict__ starts,
+                             int nbmax, uint16_t* __restrict__ xd, int* __restrict__ xe) {
+    const int b = blockIdx.x;
+    const int nb = starts[b + 1] - starts[b];
+    const int Np = max(16, (nb + 15) / 16 * 16);
+    const int l = threadIdx.x;
+    if (nb == 0 || l >= Np) return;
+    const double* X = xin + (long)b * nbmax * nbmax;
+    uint16_t* out = xd + (long)b * kDigits * 64 * 64;
+    int emax = 0;
+    if (l < nb)
+        for (int k = 0; k < nb; ++k) emax = max(emax, oz::bexp(X[k * nbmax + l]));
+    xe[b * 64 + l] = emax;
+    for (int k = 0; k < Np; ++k) {
+        const double v = (l < nb && k < nb) ? X[k * nbmax + l] : 0.0;
+        uint32_t d[kDigits];
+        oz::digits(v, emax, d);
+        const uint32_t o = tc::kmajor_off_g(l, k, Np / 8) / 2;
+#pragma unroll
+        for (int a = 0; a < kDigits; ++a) out[(long)a * Np * Np + o] = (uint16_t)(d[a] >> 16);
+    }
+}
+
+// psi'_l = sum_k X[k][l] psi_k over 128 points, in place; upd_l = psi'_l - upd_l.
+// Thread t: point row = t % 128, K groups {h, h + 2, h + 4} (h = t / 128).
+__global__ void __launch_bounds__(256, 2)
+k_gs_apply_tc(double* __restrict__ psi, double* __restrict__ upd, const int* __restrict__ starts,
+              const int* __restrict__ ordered, const uint16_t* __restrict__ xd,
+              const int* __restrict__ xe, long V4, int* __restrict__ status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sEmax[256];
+    __shared__ int sXe[64];
+    __shared__ int sIdx[64];
+    const int b = blockIdx.y;
+    const int s0 = starts[b], nb = starts[b + 1] - s0;
+    if (nb == 0) return;
+    const int Np = max(16, (nb + 15) / 16 * 16);
+    const int kg = Np / 8;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = tid & (kRows - 1), half = tid >> 7;
+    const long p = (long)blockIdx.x * kRows + row;
+    const bool live = p < V4;
+
+    const uint32_t s0a = tc::smem_u32(smraw);
+    uint8_t* base = smraw + ((128u - (s0a & 127u)) & 127u);
+    const int aPlane = kRows * Np * 2, bPlane = Np * Np * 2;
+    uint8_t* sA = base;
+    uint8_t* sB = sA + kDigits * aPlane;
+    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(xd + (long)b * kDigits * 64 * 64);
+        uint4* dst = reinterpret_cast<uint4*>(sB);
+        for (int t = tid; t < kDigits * bPlane / 16; t += 256) dst[t] = src[t];
+        if (tid < 64) {
+            sXe[tid] = tid < Np ? xe[b * 64 + tid] : 0;
+            sIdx[tid] = tid < nb ? ordered[s0 + tid] : 0;
+        }
+    }
+    __syncthreads();
+    // the point's values psi_k(p) for this thread's K groups
+    double v[24];
+#pragma unroll
+    for (int u = 0; u < 24; ++u) {
+        const int k = 8 * (half + 2 * (u >> 3)) + (u & 7);
+        v[u] = (live && k < nb) ? psi[(long)sIdx[k] * V4 + p] : 0.0;
+    }
+    int emax = 0;
+#pragma unroll
+    for (int u = 0; u < 24; ++u) emax = max(emax, oz::bexp(v[u]));
+    sEmax[tid] = emax;
+    __syncthreads();
+    emax = max(sEmax[row], sEmax[row + kRows]);
+#pragma unroll
+    for (int gg = 0; gg < 3; ++gg) {
+        const int g = half + 2 * gg;
+        if (g >= kg) continue;
+        uint4 w[kDigits];
+        if (8 * g < nb) {
+            double v8[8];
+#pragma unroll
+            for (int h = 0; h < 8; ++h) v8[h] = v[8 * gg + h];
+            oz::digits8(v8, emax, w);
+        } else {
+#pragma unroll
+            for (int a = 0; a < kDigits; ++a) w[a] = make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int a = 0; a < kDigits; ++a)
+            *reinterpret_cast<uint4*>(sA + a * aPlane + tc::kmajor_off_g(row, 8 * g, kg)) = w[a];
+    }
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    if (tid == 0) {
+        const uint32_t idesc = tc::idesc_bf16(kRows, Np);
+        const uint32_t sbo = (uint32_t)kg * 128u;
+        const uint32_t aB = tc::smem_u32(sA), bB = tc::smem_u32(sB);
+        if (kg == 2)
+            oz::issue_pairs<1>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
+        else if (kg == 4)
+            oz::issue_pairs<2>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
+        else if (kg == 6)
+            oz::issue_pairs<3>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
+        else
+            oz::issue_pairs<4>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
+        tc::commit(&mbar);
+    }
+    bool ok = tc::mbar_wait(&mbar, 0, kWaitCycles);
+    ok = __syncthreads_and(ok) != 0;
+    tc::fence_after();
+    if (ok) {
+        const int quarter = warp & 3, colh = warp >> 2;
+        const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+        // the epilogue's lane is point (quarter * 32 + lane) of the tile
+        const int erow = quarter * 32 + lane;
+        const long pe = (long)blockIdx.x * kRows + erow;
+        const int ep = max(sEmax[erow], sEmax[erow + kRows]) - 1023;
+        const bool elive = pe < V4 && max(sEmax[erow], sEmax[erow + kRows]) > 0;
+        for (int q = 0; q < Np / 16; ++q) {
+            const int c0 = 16 * q + 8 * colh;
+            uint32_t r0[8], r1[8], r2[8], r3[8];
+            __syncwarp();
+            tc::ld8(trow + (uint32_t)(0 * Np + c0), r0);
+            tc::ld8(trow + (uint32_t)(1 * Np + c0), r1);
+            tc::ld8(trow + (uint32_t)(2 * Np + c0), r2);
+            tc::ld8(trow + (uint32_t)(3 * Np + c0), r3);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            tc::wait_ld(r2);
+            tc::wait_ld(r3);
+            if (pe >= V4) continue;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int l = c0 + u;
+                if (l >= nb) break;
+                double val = 0.0;
+                if (elive) {
+                    dfl o = oz::combine4(__uint_as_float(r0[u]), __uint_as_float(r1[u]),
+                                         __uint_as_float(r2[u]), __uint_as_float(r3[u]));
+                    const float sc = oz::pow2f(ep + sXe[l] - 1023 - 12);
+                    o.h = __fmul_rn(o.h, sc);
+                    o.l = __fmul_rn(o.l, sc);
+                    val = f2d_bits(o.h) + f2d_bits(o.l);
+                }
+                const long o = (long)sIdx[l] * V4 + pe;
+                psi[o] = val;
+                if (upd) upd[o] = val - upd[o];
+            }
+        }
+    } else {
+        if (tid == 0) atomicExch(status, 1);
+        tc::mbar_wait(&mbar, 0, kWaitCycles);
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+}
+
+}  // namespace
+
+// Buffers and attributes of the tensor-core Gram-Schmidt (blocks of at most
+// 64 spinors).  Returns false when the blocks are larger.
+bool gs_tc_prepare(mg_ctx* c) {
+    if (!c->tc_ok || c->gs_nbmax > 64) return false;
+    if (c->gs_xd == nullptr) {
+        const int nblk = c->gs_nblk;
+        c->gs_nchunk_tc = div_up(4 * c->V, kChunk);
+        if (cudaMalloc(&c->gs_Stc, (size_t)nblk * c->gs_nchunk_tc * c->gs_nbmax * c->gs_nbmax *
+                                       sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&c->gs_xd, (size_t)nblk * kDigits * 64 * 64 * sizeof(uint16_t)) !=
+                cudaSuccess ||
+            cudaMalloc(&c->gs_xe, (size_t)nblk * 64 * sizeof(int)) != cudaSuccess ||
+            cudaMemset(c->gs_xd, 0, (size_t)nblk * kDigits * 64 * 64 * sizeof(uint16_t)) !=
+                cudaSuccess)
+            return false;
+        cudaFuncSetAttribute(k_gs_overlap_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        cudaFuncSetAttribute(k_gs_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+    }
+    return true;
+}
+
+int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d_ordered) {
+    const size_t sm = 128 + 2 * (size_t)kDigits * kStagePlane;
+    k_gs_overlap_tc<<<dim3(c->gs_nchunk_tc, c->gs_nblk), 256, sm, c->stream>>>(
+        psi, d_lists, d_ordered, c->gs_nbmax, 4 * c->V, c->gs_nchunk_tc, c->gs_Stc,
+        c->tc_status);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered) {
+    const int nblk = c->gs_nblk;
+    k_gs_xdigits<<<nblk, 64, 0, c->stream>>>(c->gs_R, d_lists, c->gs_nbmax, c->gs_xd, c->gs_xe);
+    MG_LAUNCHED(c);
+    const int Np = std::max(16, (c->gs_nbmax + 15) / 16 * 16);
+    size_t sm = 128 + (size_t)kDigits * (kRows * Np * 2 + Np * Np * 2);
+    sm = std::max(sm, (size_t)80 * 1024);   // two CTAs per SM: 2 x 256 TMEM columns
+    const long V4 = 4 * c->V;
+    k_gs_apply_tc<<<dim3(div_up(V4, kRows), nblk), 256, sm, c->stream>>>(
+        psi, upd, d_lists, d_ordered, c->gs_xd, c->gs_xe, V4, c->tc_status);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+}  // namespace mg

@@ -25,6 +25,10 @@ void free_all(mg_ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(c->mats);
     F(c->mats32);
+    F(c->tcmats);
+    F(c->tc_erow);
+    F(c->tc_status);
+    F(c->gs_Stc); F(c->gs_xd); F(c->gs_xe);
     for (int b = 0; b < 2; ++b) {
         Basis& B = c->bas[b];
         F(B.psi); F(B.der); F(B.lap); F(B.qn); F(B.occ); F(B.e); F(B.disp); F(B.jobs);
@@ -356,7 +360,7 @@ extern "C" int mg_derive_all(mg_ctx* c) {
     if (!c) return MG_ERR_ARG;
     MG_TRY(derive_basis(c, MG_HF_BASIS));
     if (c->p.pairing == MG_PAIRING_HFB) MG_TRY(derive_basis(c, MG_CAN_BASIS));
-    return MG_OK;
+    return tc_check(c);
 }
 
 extern "C" int mg_hpsi(mg_ctx* c, int b, double* hpsi, double* e, double* disp) {
@@ -610,5 +614,6 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         if (st < 0) return st;
         if (out) MG_TRY(energy(c, out));
     }
+    MG_TRY(tc_check(c));
     return st;
 }

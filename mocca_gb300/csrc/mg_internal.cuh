@@ -166,6 +166,14 @@ struct mg_ctx {
     float* mats32 = nullptr;      // double-float copy: hi, lo planes [q][round4(n)] per matrix
     long mat32_off[3][2][2];
     int cur_precision = MG_FP64;  // precision of the next kernels (MG_FP64 / MG_MIXED)
+    // digit planes of the Lagrange blocks for the tensor-core derivatives
+    // (deriv_tc.cu): [axis][slot] blocks of 6 planes x N rows x 32, bf16
+    uint16_t* tcmats = nullptr;
+    int* tc_erow = nullptr;       // [axis][slot][64] row exponents
+    int* tc_status = nullptr;     // set when an MMA completion wait ran out
+    long tc_off[3][2];
+    int tc_N[3] = {0, 0, 0};
+    bool tc_ok = false;           // every line length <= 32
 
     mg::Basis bas[2];
     double* updates = nullptr;   // nwt*4V heavy-ball history
@@ -185,6 +193,12 @@ struct mg_ctx {
     double* gs_R = nullptr;       // inverse Cholesky factors
     int* gs_index = nullptr;      // block lists + energy-ordered members
     int gs_nblk = 0, gs_nbmax = 0, gs_nchunk = 0, gs_lists_len = 0;
+    // tensor-core form (gs_tc.cu): overlap partials per 256-point chunk, digit
+    // planes and row exponents of X = R^{-1}
+    double* gs_Stc = nullptr;
+    uint16_t* gs_xd = nullptr;
+    int* gs_xe = nullptr;
+    int gs_nchunk_tc = 0;
 
     // Coulomb
     int mx, my, mz;
@@ -229,10 +243,16 @@ int build_basis_jobs(mg_ctx* c, int b);
 int build_field_jobs(mg_ctx* c);
 int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df = false);
 int derive_basis(mg_ctx* c, int b);
+int tc_setup(mg_ctx* c);
+int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs);
+int tc_check(mg_ctx* c);
 
 int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom);
 int gram_schmidt(mg_ctx* c);
 int gram_schmidt_impl(mg_ctx* c, double* upd);
+bool gs_tc_prepare(mg_ctx* c);
+int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d_ordered);
+int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered);
 int densities(mg_ctx* c);
 int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);

@@ -1,12 +1,14 @@
-"""Mixed-precision path (MG_MIXED): double-float (FP32 pair) derivative
-contractions with FP64 storage, checked against the FP64 oracle, and the
-mixed iterations followed by an FP64 polish checked against the plain FP64
-GPU path.
+"""Mixed-precision path (MG_MIXED): derivative contractions on the tensor
+cores (exact BF16 digit products, line lengths up to 32) or as double-float
+(FP32 pair) sums (longer lines, n = 36 below), stored as double-float pairs,
+checked against the FP64 oracle; and the mixed iterations followed by an FP64
+polish checked against the plain FP64 GPU path.
 
-Bars: derivatives and Laplacians within 1e-11 relative (norm-wise): inputs
-and matrices carry 48 significant bits and the sums are carried as (hi, lo)
-pairs, so the error is a few units of 2^-48 times the cancellation of the
-sums.  After mixed iterations and an FP64 polish the total energy agrees
+Bars: derivatives and Laplacians within 1e-11 relative (norm-wise).  The
+tensor-core form rounds each line and each matrix row to 47-bit integers
+(scaled by powers of two) and sums their digit products exactly, so its error
+is a few units of 2^-47 of the line's largest terms; the double-float form
+carries 48 significant bits with (hi, lo) sums.  After mixed iterations and an FP64 polish the total energy agrees
 with the all-FP64 run to 1e-5 MeV.
 """
 import numpy as np
@@ -20,7 +22,7 @@ from mocca_gb300.mesh import MeshState
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n,nwt", [(10, 8), (13, 6), (24, 8)])
+@pytest.mark.parametrize("n,nwt", [(10, 8), (13, 6), (24, 8), (36, 4)])
 def test_mixed_derivatives_ev8(built, n, nwt):
     p = RunParams(nx=n, ny=n, nz=n, dx=0.8, nwt=nwt, neutrons=8, protons=8, precision=MG_MIXED)
     psi, qn, en = synthetic.ho_basis(p, nwt // 2, seed=5)
@@ -180,3 +182,33 @@ def test_mixed_iterations_with_fp64_polish(built):
     assert abs(e_mix - e_ref) <= 1e-5, (e_mix, e_ref)
     ref.close()
     mix.close()
+
+
+@pytest.mark.parametrize("n,nwt", [(10, 40), (24, 160)])
+def test_mixed_gram_schmidt(built, n, nwt):
+    """Tensor-core Gram-Schmidt (overlap and apply as exact digit products)
+    against the FP64 oracle: 1e-11 relative on the spinors, orthonormal to
+    5e-12 within each (isospin, parity) block.  The apply rounds each point's
+    spinor values to 47 bits of the point's largest one and this basis is far
+    from orthonormal (2% noise), so R^-1 amplifies that rounding a little."""
+    p = RunParams(nx=n, ny=n, nz=n, dx=0.8, nwt=nwt, neutrons=nwt // 4, protons=nwt // 4,
+                  precision=MG_MIXED)
+    psi, qn, en = synthetic.ho_basis(p, nwt // 2, seed=7)
+    rng = np.random.default_rng(11)
+    pert = psi + 0.02 * rng.normal(size=psi.shape) * np.abs(psi).max()
+    en = en + rng.normal(size=en.shape)
+    g = MeshState(p, SLY4)
+    o = O.OracleState(p, SLY4)
+    for s in (g, o):
+        s.set_spinors(pert, qn)
+        s.set_energies(en)
+    g.GramSchmidt()
+    o.GramSchmidt()
+    qg, qo = g.get_spinors(), o.get_spinors()
+    assert rel(qg, qo) < 1e-11
+    assert rel(qg, qo) > 1e-16   # the tensor-core kernels ran, not the FP64 ones
+    q = qg.reshape(p.nwt, -1)
+    S = q @ q.T * p.dv
+    same = (qn[:, None, 0] == qn[None, :, 0]) & (qn[:, None, 1] == qn[None, :, 1])
+    assert np.abs(S[same] - np.eye(p.nwt)[same]).max() < 5e-12
+    g.close()
