@@ -45,9 +45,11 @@ WORKLOAD = dict(nx=24, ny=24, nz=24, dx=0.8, nwt=160, neutrons=28.0, protons=28.
 DT, MOMENTUM = 0.010, 0.3
 POLISH = 20   # final FP64 iterations of the mixed form
 METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
-# DRAM traffic of one DeriveBasis launch pair (k_deriv_xy_df + k_deriv_z_df,
-# nwt=160, 24^3) from ncu dram__bytes_read.sum + dram__bytes_write.sum
-DERIV_DF_TRAFFIC = 456.4e6
+# DRAM traffic of one mixed DeriveBasis (the three k_deriv_tc passes, nwt=160,
+# 24^3) from ncu dram__bytes_read.sum + dram__bytes_write.sum, and the tensor
+# pipe's active share over those launches (profiles/deriv_tc_24c_nwt160_full.md)
+DERIV_TC_TRAFFIC = 612.7e6
+DERIV_TC_TENSOR_ACTIVE = 0.069
 
 
 def _params(precision):
@@ -430,22 +432,24 @@ def run_ours(args, rank, world, local_rank):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_dev / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (double-float mesh kernels)" if mixed else "f64",
+        "dtype": ("f64 (exact BF16-digit tensor-core and double-float mesh kernels)" if mixed
+                  else "f64"),
         "data": "synthetic",
         "config": _config(args.precision, world),
         "e2e": {"value": whole_job_rate(world, args.steps, t_e2e), "unit": "iter/s",
                 "h2d_bytes_per_step": int(host_psi.numel() * 8),
                 "d2h_bytes_per_step": int(out_psi.numel() * 8 + C.sizeof(e_terms))},
-        "roofline": {"kernel": ("k_deriv_xy_df + k_deriv_z_df" if mixed else
+        "roofline": {"kernel": ("k_deriv_tc x3 (x, y, z passes)" if mixed else
                                 "k_deriv_xy + k_deriv_z") + " (DeriveBasis, HF basis)",
                      "bound": "hbm", "achieved": bytes_ / t_der / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": bytes_ / t_der / 1e9 / hbm,
-                     "traffic": DERIV_DF_TRAFFIC if mixed else None,
+                     "traffic": DERIV_TC_TRAFFIC if mixed else None,
+                     "tensor_pipe_active_ncu": DERIV_TC_TENSOR_ACTIVE if mixed else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)",
                      "fp64_equivalent": {"achieved_tflops": flops / t_der / 1e12,
                                          "dgemm_tflops_measured": fp64_peak,
                                          "frac_of_dgemm": flops / t_der / 1e12 / fp64_peak},
-                     "ms_per_launch_pair": t_der * 1e3},
+                     "ms_per_derive": t_der * 1e3},
         "cpu_baseline": cpu_baseline(1),
         "clocks": clocks,
         "gpu_launches": int(launches),

@@ -15,7 +15,7 @@
 //   k_gs_apply    : psi'_l = sum_{k<=l} X_kl psi_k in place (+ update history)
 // For the near-orthonormal input of an imaginary-time step cond(S) ~ 1, so
 // the Cholesky form keeps full FP64 accuracy.  In the mixed form the overlap
-// and the apply run on the tensor cores instead (gs_tc.cu); the sum, the
+// and the apply run on the tensor cores instead (meshgemm_tc.cu); the sum, the
 // factorisation and the order stay these FP64 kernels.
 #include "mg_internal.cuh"
 
@@ -261,7 +261,7 @@ int gram_schmidt_impl(mg_ctx* c, double* upd) {
     MG_LAUNCHED(c);
     const size_t sm_f = (size_t)(2 * nbmax * nbmax) * sizeof(double);
     if (c->cur_precision == MG_MIXED && gs_tc_prepare(c)) {
-        // mixed form: the overlap and the apply on the tensor cores (gs_tc.cu)
+        // mixed form: the overlap and the apply on the tensor cores (meshgemm_tc.cu)
         const int nct = c->gs_nchunk_tc;
         MG_TRY(gs_overlap_tc(c, B.psi, d_lists, d_ordered));
         k_gs_sum<<<dim3(div_up((long)nbmax * nbmax, kThreads / 32), nblk), kThreads, 0,

@@ -1,20 +1,24 @@
-// gs_tc.cu -- the mixed form of the Gram-Schmidt step on the tcgen05 tensor
-// cores (exact BF16 digit products, ozaki.cuh).
+// meshgemm_tc.cu -- the mesh-sized contractions of the mixed form on the
+// tcgen05 tensor cores (exact BF16 digit products, ozaki.cuh): the
+// Gram-Schmidt overlap and apply, and the canonical-basis transform.
 //
-// Same factorisation as gs.cu (GramSchmidt, src/SpwfStorage.f90:372-480, as
+// Gram-Schmidt (gs.cu; GramSchmidt, src/SpwfStorage.f90:372-480, as
 // Q = Psi R^{-1} with S = R^T R per (isospin, parity, signature) block in
-// energy order); the two mesh-sized contractions move to the tensor cores:
+// energy order):
 //   k_gs_overlap_tc : S partial sums over 256-point chunks.  Rows of the
 //                     MMA are the block's spinors (zero beyond nb), K the
 //                     chunk's points; A and B are the same digit planes.  Each
 //                     (spinor, chunk) row gets its own power of two.  The
 //                     partials go to the same table as the FP64 kernel, so
 //                     k_gs_sum / k_gs_factor (gs.cu) finish the job.
-//   k_gs_xdigits    : digit planes of X = R^{-1} (rows: output spinor l,
-//                     K: input spinor k), one power of two per row.
-//   k_gs_apply_tc   : psi'_l(p) = sum_k X[k][l] psi_k(p) for 128 points per
-//                     CTA (MMA M), K = the block's spinors, FP64 output in
-//                     place, plus the GradDesc history upd_l = psi'_l - upd_l.
+// Block apply, out_l(p) = sum_k C[k][l] in_k(p) per block of spinors:
+//   k_coef_digits   : digit planes of C (rows: output l, K: input k), one
+//                     power of two per row;
+//   k_apply_tc      : 128 points per CTA (MMA M), K = the block's spinors, FP64
+//                     output.  Gram-Schmidt: C = R^{-1}, in place, plus the
+//                     GradDesc history upd_l = out_l - upd_l.  Canonical basis
+//                     (HFBOccupations, src/HFB.f90:3448-3487): C = CanTransfo,
+//                     HF basis in, canonical basis out.
 // A 256-point chunk keeps every digit-weight group of the overlap below 2^24
 // (at most 3 pairs x 256 points x 2^14), so its FP32 sums are exact.
 #include <algorithm>
@@ -35,6 +39,16 @@ constexpr int kStage = 32;            // overlap points per MMA stage (K)
 constexpr int kStagePlane = kRows * kStage * 2;   // bytes of one digit plane of a stage
 constexpr uint32_t kTmemCols = 256;
 constexpr long long kWaitCycles = 4000000000LL;
+
+// Block sizes and list offsets: Gram-Schmidt blocks come from a start table,
+// pairing blocks have hsz[b] members listed at b * hmax.
+struct BlockIdx {
+    const int* starts;
+    const int* hsz;
+    int hmax;
+    __device__ int nb(int b) const { return starts ? starts[b + 1] - starts[b] : hsz[b]; }
+    __device__ int off(int b) const { return starts ? starts[b] : b * hmax; }
+};
 
 __device__ __forceinline__ double pow2d(int x) {
     return x < -1022 ? 0.0 : __longlong_as_double((long long)(min(x, 1023) + 1023) << 52);
@@ -177,23 +191,25 @@ k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
     if (warp == 0) tc::dealloc(tmem, kTmemCols);
 }
 
-// Digit planes of X (per block: kDigits planes of Np rows x Np, row l = output
-// spinor, K = input spinor k) and the row exponents (biased).
-__global__ void k_gs_xdigits(const double* __restrict__ xin, const int* __restrict__ starts,
-                             int nbmax, uint16_t* __restrict__ xd, int* __restrict__ xe) {
+// Digit planes of C (per block: kDigits planes of Np rows x Np, row l = output
+// l, K = input k; C[k][l] = coef[b * bstride + k * ld + l], ld = nb when 0) and
+// the row exponents (biased).
+__global__ void k_coef_digits(const double* __restrict__ coef, long bstride, int ld, BlockIdx bi,
+                              uint16_t* __restrict__ xd, int* __restrict__ xe) {
     const int b = blockIdx.x;
-    const int nb = starts[b + 1] - starts[b];
+    const int nb = bi.nb(b);
     const int Np = max(16, (nb + 15) / 16 * 16);
     const int l = threadIdx.x;
     if (nb == 0 || l >= Np) return;
-    const double* X = xin + (long)b * nbmax * nbmax;
+    const int ldc = ld > 0 ? ld : nb;
+    const double* X = coef + (long)b * bstride;
     uint16_t* out = xd + (long)b * kDigits * 64 * 64;
     int emax = 0;
     if (l < nb)
-        for (int k = 0; k < nb; ++k) emax = max(emax, oz::bexp(X[k * nbmax + l]));
+        for (int k = 0; k < nb; ++k) emax = max(emax, oz::bexp(X[k * ldc + l]));
     xe[b * 64 + l] = emax;
     for (int k = 0; k < Np; ++k) {
-        const double v = (l < nb && k < nb) ? X[k * nbmax + l] : 0.0;
+        const double v = (l < nb && k < nb) ? X[k * ldc + l] : 0.0;
         uint32_t d[kDigits];
         oz::digits(v, emax, d);
         const uint32_t o = tc::kmajor_off_g(l, k, Np / 8) / 2;
@@ -202,20 +218,24 @@ __global__ void k_gs_xdigits(const double* __restrict__ xin, const int* __restri
     }
 }
 
-// psi'_l = sum_k X[k][l] psi_k over 128 points, in place; upd_l = psi'_l - upd_l.
+// out_l = sum_k C[k][l] in_k over 128 points (in_k = in[in_list[off + k]],
+// out_l = out[out_list[off + l]] or out[out_base[b] + l]); when upd is given,
+// upd_l = out_l - upd_l.  in and out may be the same array (in place).
 // Thread t: point row = t % 128, K groups {h, h + 2, h + 4} (h = t / 128).
 __global__ void __launch_bounds__(256, 2)
-k_gs_apply_tc(double* __restrict__ psi, double* __restrict__ upd, const int* __restrict__ starts,
-              const int* __restrict__ ordered, const uint16_t* __restrict__ xd,
-              const int* __restrict__ xe, long V4, int* __restrict__ status) {
+k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
+           const int* __restrict__ in_list, const int* __restrict__ out_list,
+           const int* __restrict__ out_base, const uint16_t* __restrict__ xd,
+           const int* __restrict__ xe, long V4, int* __restrict__ status) {
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int sEmax[256];
     __shared__ int sXe[64];
     __shared__ int sIdx[64];
+    __shared__ int sOut[64];
     const int b = blockIdx.y;
-    const int s0 = starts[b], nb = starts[b + 1] - s0;
+    const int s0 = bi.off(b), nb = bi.nb(b);
     if (nb == 0) return;
     const int Np = max(16, (nb + 15) / 16 * 16);
     const int kg = Np / 8;
@@ -237,7 +257,8 @@ k_gs_apply_tc(double* __restrict__ psi, double* __restrict__ upd, const int* __r
         for (int t = tid; t < kDigits * bPlane / 16; t += 256) dst[t] = src[t];
         if (tid < 64) {
             sXe[tid] = tid < Np ? xe[b * 64 + tid] : 0;
-            sIdx[tid] = tid < nb ? ordered[s0 + tid] : 0;
+            sIdx[tid] = tid < nb ? in_list[s0 + tid] : 0;
+            sOut[tid] = tid < nb ? (out_list ? out_list[s0 + tid] : out_base[b] + tid) : 0;
         }
     }
     __syncthreads();
@@ -246,7 +267,7 @@ k_gs_apply_tc(double* __restrict__ psi, double* __restrict__ upd, const int* __r
 #pragma unroll
     for (int u = 0; u < 24; ++u) {
         const int k = 8 * (half + 2 * (u >> 3)) + (u & 7);
-        v[u] = (live && k < nb) ? psi[(long)sIdx[k] * V4 + p] : 0.0;
+        v[u] = (live && k < nb) ? in[(long)sIdx[k] * V4 + p] : 0.0;
     }
     int emax = 0;
 #pragma unroll
@@ -328,8 +349,8 @@ k_gs_apply_tc(double* __restrict__ psi, double* __restrict__ upd, const int* __r
                     o.l = __fmul_rn(o.l, sc);
                     val = f2d_bits(o.h) + f2d_bits(o.l);
                 }
-                const long o = (long)sIdx[l] * V4 + pe;
-                psi[o] = val;
+                const long o = (long)sOut[l] * V4 + pe;
+                out[o] = val;
                 if (upd) upd[o] = val - upd[o];
             }
         }
@@ -361,7 +382,7 @@ bool gs_tc_prepare(mg_ctx* c) {
             return false;
         cudaFuncSetAttribute(k_gs_overlap_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              200 * 1024);
-        cudaFuncSetAttribute(k_gs_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              200 * 1024);
     }
     return true;
@@ -376,18 +397,44 @@ int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d
     return MG_OK;
 }
 
-int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered) {
-    const int nblk = c->gs_nblk;
-    k_gs_xdigits<<<nblk, 64, 0, c->stream>>>(c->gs_R, d_lists, c->gs_nbmax, c->gs_xd, c->gs_xe);
+static int apply_tc(mg_ctx* c, int nblk, int nbmax, const double* coef, long bstride, int ld,
+                    BlockIdx bi, const double* in, double* out, double* upd, const int* in_list,
+                    const int* out_list, const int* out_base, uint16_t* xd, int* xe) {
+    k_coef_digits<<<nblk, 64, 0, c->stream>>>(coef, bstride, ld, bi, xd, xe);
     MG_LAUNCHED(c);
-    const int Np = std::max(16, (c->gs_nbmax + 15) / 16 * 16);
+    const int Np = std::max(16, (nbmax + 15) / 16 * 16);
     size_t sm = 128 + (size_t)kDigits * (kRows * Np * 2 + Np * Np * 2);
     sm = std::max(sm, (size_t)80 * 1024);   // two CTAs per SM: 2 x 256 TMEM columns
     const long V4 = 4 * c->V;
-    k_gs_apply_tc<<<dim3(div_up(V4, kRows), nblk), 256, sm, c->stream>>>(
-        psi, upd, d_lists, d_ordered, c->gs_xd, c->gs_xe, V4, c->tc_status);
+    k_apply_tc<<<dim3(div_up(V4, kRows), nblk), 256, sm, c->stream>>>(
+        in, out, upd, bi, in_list, out_list, out_base, xd, xe, V4, c->tc_status);
     MG_LAUNCHED(c);
     return MG_OK;
+}
+
+int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered) {
+    const BlockIdx bi{d_lists, nullptr, 0};
+    return apply_tc(c, c->gs_nblk, c->gs_nbmax, c->gs_R, (long)c->gs_nbmax * c->gs_nbmax,
+                    c->gs_nbmax, bi, psi, psi, upd, d_ordered, d_ordered, nullptr, c->gs_xd,
+                    c->gs_xe);
+}
+
+// Canonical basis of the four pairing blocks (hsz[b] <= 64): CanTransfo is
+// stored densely per block (ld = h) at b * hmax^2.
+int can_transform_tc(mg_ctx* c) {
+    Hfb& H = c->hfb;
+    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    if (c->can_xd == nullptr) {
+        MG_CUDA(cudaMalloc(&c->can_xd, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
+        MG_CUDA(cudaMemset(c->can_xd, 0, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
+        MG_CUDA(cudaMalloc(&c->can_xe, (size_t)4 * 64 * sizeof(int)));
+        MG_CUDA(cudaFuncSetAttribute(k_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+    }
+    const BlockIdx bi{nullptr, H.hsz, H.hmax};
+    return apply_tc(c, 4, H.hmax, H.cantr, (long)H.hmax * H.hmax, 0, bi,
+                    c->bas[MG_HF_BASIS].psi, c->bas[MG_CAN_BASIS].psi, nullptr, H.members,
+                    nullptr, H.cstart, c->can_xd, c->can_xe);
 }
 
 }  // namespace mg

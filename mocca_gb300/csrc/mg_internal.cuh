@@ -193,12 +193,14 @@ struct mg_ctx {
     double* gs_R = nullptr;       // inverse Cholesky factors
     int* gs_index = nullptr;      // block lists + energy-ordered members
     int gs_nblk = 0, gs_nbmax = 0, gs_nchunk = 0, gs_lists_len = 0;
-    // tensor-core form (gs_tc.cu): overlap partials per 256-point chunk, digit
+    // tensor-core form (meshgemm_tc.cu): overlap partials per 256-point chunk, digit
     // planes and row exponents of X = R^{-1}
     double* gs_Stc = nullptr;
     uint16_t* gs_xd = nullptr;
     int* gs_xe = nullptr;
     int gs_nchunk_tc = 0;
+    uint16_t* can_xd = nullptr;   // digit planes of CanTransfo (tensor-core canonical basis)
+    int* can_xe = nullptr;
 
     // Coulomb
     int mx, my, mz;
@@ -253,6 +255,7 @@ int gram_schmidt_impl(mg_ctx* c, double* upd);
 bool gs_tc_prepare(mg_ctx* c);
 int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d_ordered);
 int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered);
+int can_transform_tc(mg_ctx* c);
 int densities(mg_ctx* c);
 int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);

@@ -443,6 +443,8 @@ int canonical_transform(mg_ctx* c) {
     Hfb& H = c->hfb;
     const long V4 = 4 * c->V;
     const size_t sm = (size_t)(H.hmax * H.hmax + H.hmax * kPts) * sizeof(double);
+    if (c->cur_precision == MG_MIXED && c->tc_ok && H.hmax <= 64)
+        return can_transform_tc(c);   // tensor cores (meshgemm_tc.cu)
     if (c->cur_precision == MG_MIXED)
         k_can_transform_df<<<dim3(div_up(V4, kPts), 4), kThreads, sm, c->stream>>>(
             c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.cstart, H.hmax, H.cantr, V4,

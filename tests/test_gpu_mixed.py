@@ -139,7 +139,9 @@ def test_mixed_coulomb_direct_residual(built):
 
 
 def test_mixed_hfb_start(built):
-    """Pairing field, gaps and canonical basis from the double-float mesh kernels."""
+    """Pairing field and gaps (double-float mesh kernels) and the canonical
+    basis (tensor-core block apply), the latter through the densities it
+    builds (invariant under sign and degenerate-subspace choices)."""
     p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
                   pairing=_abi.MG_PAIRING_HFB, precision=MG_MIXED)
     psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
@@ -156,6 +158,12 @@ def test_mixed_hfb_start(built):
     for a, b in zip(fg, fo):
         assert rel(a, b) < 1e-10
     assert abs(sum(ig["pairing_energy"]) - sum(io["pairing_energy"])) < 1e-9
+    for s in (g, o):
+        s.DeriveAll()
+        s.UpdateDensities()
+    dg, do = g.get_densities(), o.get_densities()
+    for k in ("rho", "tau", "nablaj"):
+        assert rel(dg[k], do[k]) < 1e-10, k
     g.close()
 
 
