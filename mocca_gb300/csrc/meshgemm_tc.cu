@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "df.cuh"
 #include "mg_internal.cuh"
 #include "ozaki.cuh"
 #include "tc.cuh"
@@ -363,6 +364,182 @@ k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
     if (warp == 0) tc::dealloc(tmem, kTmemCols);
 }
 
+// Pairing gaps, HFBGaps (src/HFB.f90:520-632), per block b (isospin b / 2):
+//   G_ij = sum_p sum_c psi_ic(p) Z_jc(p)  over a 64-point chunk,
+//   Z_j0 = -Fr psi_j0 + Fi psi_j1, Z_j1 = -Fi psi_j0 - Fr psi_j1 (same for 2, 3),
+// the form of k_pair_gaps (pairing.cu).  K runs over (component, point):
+// stage s covers 8 points, K group c = component c.  A rows are the spinors
+// (one power of two per spinor and chunk), B rows their Z, formed in
+// double-float and cut into digits through the fixed-point form with the
+// exponent bound 2 max|F| max|psi_j| of the chunk.  One plane buffer per
+// stage, two CTAs per SM.
+constexpr int kGapPts = 64;
+
+__global__ void __launch_bounds__(256, 2)
+k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
+          const int* __restrict__ hsz, int hmax, const double* __restrict__ fre,
+          const double* __restrict__ fim, long V, int nchunk, double* __restrict__ gpart,
+          int* __restrict__ status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sE[64], sEz[64], sFe[kGapPts];
+    __shared__ float4 sF[kGapPts];   // (Fr hi, Fr lo, Fi hi, Fi lo)
+    const int b = blockIdx.y, it = b >> 1, chunk = blockIdx.x;
+    const int h = hsz[b];
+    if (h == 0) return;
+    const int N = max(16, (h + 15) / 16 * 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = tid >> 2, c = tid & 3;
+    const bool live = row < h;
+    const int bPlane = N * tc::kRowBytes;
+
+    const uint32_t s0a = tc::smem_u32(smraw);
+    uint8_t* base = smraw + ((128u - (s0a & 127u)) & 127u);
+    uint8_t* sA = base;                          // kDigits planes of 128 x 32
+    uint8_t* sB = sA + kDigits * kStagePlane;    // kDigits planes of N x 32
+    for (int t = tid; t < (kDigits * kStagePlane + kDigits * bPlane) / 16; t += 256)
+        reinterpret_cast<uint4*>(base)[t] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    const long p0 = (long)chunk * kGapPts;
+    const int npts = (int)min((long)kGapPts, V - p0);
+    // the pairing field of the chunk, double-float, and its largest exponent
+    if (tid < kGapPts) {
+        double fr = 0.0, fi = 0.0;
+        if (tid < npts) {
+            fr = fre[(long)it * V + p0 + tid];
+            fi = fim[(long)it * V + p0 + tid];
+        }
+        const dfl a = df_split(fr), d = df_split(fi);
+        sF[tid] = make_float4(a.h, a.l, d.h, d.l);
+        sFe[tid] = max(oz::bexp(fr), oz::bexp(fi));
+    }
+    const int pc = c ^ 1;   // the partner component of Z
+    const double* src = live ? psi + ((long)members[b * hmax + row] * 4 + c) * V + p0 : psi;
+    const double* srp = live ? psi + ((long)members[b * hmax + row] * 4 + pc) * V + p0 : psi;
+    int emax = 0;
+    if (live)
+        for (int q = 0; q < npts; ++q) emax = max(emax, oz::bexp(src[q]));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    __syncthreads();
+    int efmax = 0;
+    for (int q = 0; q < kGapPts; ++q) efmax = max(efmax, sFe[q]);
+    // |Z| <= |F| (|psi_c| + |psi_c'|) < 2^(E_F + E_psi + 3)
+    const int ez = (emax == 0 || efmax == 0) ? 0 : emax + efmax - 1023 + 2;
+    if (live && c == 0) {
+        sE[row] = emax;
+        sEz[row] = ez;
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = tc::idesc_bf16(kRows, N);
+    bool ok = true;
+    const int nst = kGapPts / 8;
+    for (int s = 0; s < nst; ++s) {
+        if (s > 0) ok &= tc::mbar_wait(&mbar, (s - 1) & 1, kWaitCycles);
+        if (live) {
+            double a[8];
+            long long zx[8];
+#pragma unroll
+            for (int hh = 0; hh < 8; ++hh) {
+                const int q = 8 * s + hh;
+                const bool in = q < npts;
+                a[hh] = in ? src[q] : 0.0;
+                const double ap = in ? srp[q] : 0.0;
+                const float4 f = sF[q];
+                const dfl fr = {f.x, f.y}, fi = {f.z, f.w};
+                const dfl ac = df_split(a[hh]), ao = df_split(ap);
+                // c even: Z = -Fr a_c + Fi a_c' ; c odd: Z = -Fi a_c' - Fr a_c
+                const dfl t1 = df_mul(fr, ac), t2 = df_mul(fi, ao);
+                const dfl z = (c & 1) ? df_neg(df_add(t1, t2)) : df_sub(t2, t1);
+                zx[hh] = ez ? oz::fixed_f(z.h, ez) + oz::fixed_f(z.l, ez) : 0ll;
+            }
+            uint4 w[kDigits];
+            oz::digits8(a, emax, w);
+#pragma unroll
+            for (int d = 0; d < kDigits; ++d)
+                *reinterpret_cast<uint4*>(sA + d * kStagePlane + tc::kmajor_off(row, 8 * c)) = w[d];
+            oz::digits8_fixed(zx, w);
+#pragma unroll
+            for (int d = 0; d < kDigits; ++d)
+                *reinterpret_cast<uint4*>(sB + d * bPlane + tc::kmajor_off(row, 8 * c)) = w[d];
+        }
+        tc::fence_proxy_async();
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+            oz::issue_pairs<2>(tmem, N, idesc, tc::smem_u32(sA), kStagePlane, tc::kSbo,
+                               tc::smem_u32(sB), bPlane, tc::kSbo, s > 0);
+            tc::commit(&mbar);
+        }
+    }
+    ok &= tc::mbar_wait(&mbar, (nst - 1) & 1, kWaitCycles);
+    ok = __syncthreads_and(ok) != 0;
+    tc::fence_after();
+    if (ok) {
+        const int quarter = warp & 3, colh = warp >> 2;
+        const int i = quarter * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+        double* out = gpart + ((long)b * nchunk + chunk) * hmax * hmax;
+        const int ei = i < h ? sE[i] - 1023 : 0;
+        for (int q = 0; q < N / 16; ++q) {
+            const int c0 = 16 * q + 8 * colh;
+            uint32_t r0[8], r1[8], r2[8], r3[8];
+            __syncwarp();
+            tc::ld8(trow + (uint32_t)(0 * N + c0), r0);
+            tc::ld8(trow + (uint32_t)(1 * N + c0), r1);
+            tc::ld8(trow + (uint32_t)(2 * N + c0), r2);
+            tc::ld8(trow + (uint32_t)(3 * N + c0), r3);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            tc::wait_ld(r2);
+            tc::wait_ld(r3);
+            if (i >= h) continue;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int j = c0 + u;
+                if (j >= h) break;
+                double val = 0.0;
+                if (sE[i] != 0 && sEz[j] != 0) {
+                    const dfl o = oz::combine4(__uint_as_float(r0[u]), __uint_as_float(r1[u]),
+                                               __uint_as_float(r2[u]), __uint_as_float(r3[u]));
+                    val = (f2d_bits(o.h) + f2d_bits(o.l)) * pow2d(ei + sEz[j] - 1023 - 12);
+                }
+                out[i * h + j] = val;
+            }
+        }
+    } else {
+        if (tid == 0) atomicExch(status, 1);
+        tc::mbar_wait(&mbar, 0, kWaitCycles);
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+}
+
+// Chunk partials of the gaps summed per entry, one warp each (fixed order):
+// gsum[b][i * h + j].
+__global__ void k_gaps_sum(const double* __restrict__ gpart, const int* __restrict__ hsz,
+                           int hmax, int nchunk, double* __restrict__ gsum) {
+    const int b = blockIdx.y;
+    const int h = hsz[b];
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (t >= h * h) return;
+    const double* pb = gpart + (long)b * nchunk * hmax * hmax;
+    double s = 0.0;
+    for (int q = lane; q < nchunk; q += 32) s += pb[(long)q * hmax * hmax + t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncwarp();
+    if (lane == 0) gsum[(long)b * hmax * hmax + t] = s;
+}
+
 }  // namespace
 
 // Buffers and attributes of the tensor-core Gram-Schmidt (blocks of at most
@@ -435,6 +612,31 @@ int can_transform_tc(mg_ctx* c) {
     return apply_tc(c, 4, H.hmax, H.cantr, (long)H.hmax * H.hmax, 0, bi,
                     c->bas[MG_HF_BASIS].psi, c->bas[MG_CAN_BASIS].psi, nullptr, H.members,
                     nullptr, H.cstart, c->can_xd, c->can_xe);
+}
+
+// Gaps partial sums of the four pairing blocks on the tensor cores into
+// gsum[b][i * h + j] (to be finished by k_gaps_finish with one chunk).
+int gaps_tc(mg_ctx* c, double* gsum) {
+    Hfb& H = c->hfb;
+    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    const long V = c->V;
+    const int nchunk = div_up(V, kGapPts);
+    if (c->gap_part == nullptr) {
+        MG_CUDA(cudaMalloc(&c->gap_part, (size_t)4 * nchunk * H.hmax * H.hmax * sizeof(double)));
+        MG_CUDA(cudaFuncSetAttribute(k_gaps_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+    }
+    const int Np = std::max(16, (H.hmax + 15) / 16 * 16);
+    size_t sm = 128 + (size_t)kDigits * kStagePlane + (size_t)kDigits * Np * tc::kRowBytes;
+    sm = std::max(sm, (size_t)80 * 1024);   // two CTAs per SM: 2 x 256 TMEM columns
+    k_gaps_tc<<<dim3(nchunk, 4), 256, sm, c->stream>>>(c->bas[MG_HF_BASIS].psi, H.members, H.hsz,
+                                                      H.hmax, H.fre, H.fim, V, nchunk, c->gap_part,
+                                                      c->tc_status);
+    MG_LAUNCHED(c);
+    k_gaps_sum<<<dim3(div_up((long)H.hmax * H.hmax, 8), 4), 256, 0, c->stream>>>(
+        c->gap_part, H.hsz, H.hmax, nchunk, gsum);
+    MG_LAUNCHED(c);
+    return MG_OK;
 }
 
 }  // namespace mg

@@ -201,6 +201,7 @@ struct mg_ctx {
     int gs_nchunk_tc = 0;
     uint16_t* can_xd = nullptr;   // digit planes of CanTransfo (tensor-core canonical basis)
     int* can_xe = nullptr;
+    double* gap_part = nullptr;   // tensor-core gaps: partials per 64-point chunk
 
     // Coulomb
     int mx, my, mz;
@@ -256,6 +257,7 @@ bool gs_tc_prepare(mg_ctx* c);
 int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d_ordered);
 int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered);
 int can_transform_tc(mg_ctx* c);
+int gaps_tc(mg_ctx* c, double* gsum);
 int densities(mg_ctx* c);
 int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);

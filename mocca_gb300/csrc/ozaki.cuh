@@ -51,10 +51,10 @@ __device__ __forceinline__ int bexp(double v) {
     return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF);
 }
 
-// The pre-scaled digits of v (top digit first) for a row whose largest
-// biased exponent is emax, as FP32 bit patterns whose upper halves are the
-// exact BF16 values.
-__device__ __forceinline__ void digits(double v, int emax, uint32_t (&d)[kDigits]) {
+// round(v * 2^f) for a row whose largest biased exponent is emax, with
+// f = 8 kDigits - 2 - (emax - 1023): |result| <= 2^47.  Zero and subnormal v
+// give 0, as do values 2^62 below the row's largest.
+__device__ __forceinline__ long long fixed(double v, int emax) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
     const int e = (int)((b >> 52) & 0x7FF);
     const int sh = (54 - 8 * kDigits) + (emax - e);   // >= 6
@@ -64,6 +64,29 @@ __device__ __forceinline__ void digits(double v, int emax, uint32_t (&d)[kDigits
         X = (long long)((m + (1ull << (sh - 1))) >> sh);
         if (b >> 63) X = -X;
     }
+    return X;
+}
+
+// The same fixed-point value of a float (part of a double-float), exact when
+// the float's bits lie above 2^-f, rounded otherwise.
+__device__ __forceinline__ long long fixed_f(float v, int emax) {
+    const uint32_t u = __float_as_uint(v);
+    const int ef = (int)((u >> 23) & 0xFFu);
+    if (ef == 0) return 0;
+    const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
+    // v * 2^f = m * 2^sh with f = 8 kDigits - 2 - (emax - 1023)
+    const int sh = ef - 150 + (8 * kDigits - 2) - (emax - 1023);
+    long long X;
+    if (sh >= 0) X = sh < 39 ? (m << sh) : 0;   // above the row bound: not reached
+    else if (sh > -40) X = (m + (1ll << (-sh - 1))) >> (-sh);
+    else X = 0;
+    return (u >> 31) ? -X : X;
+}
+
+// The pre-scaled digits (top digit first) of a fixed-point value X
+// (|X| <= 2^47), as FP32 bit patterns whose upper halves are the exact BF16
+// values.
+__device__ __forceinline__ void digits_fixed(long long X, uint32_t (&d)[kDigits]) {
     const unsigned long long Y = (unsigned long long)(X + kDigitBias);
     const uint32_t ylo = (uint32_t)Y, yhi = (uint32_t)(Y >> 32);
     const int top = (int)yhi >> 8;   // Y >> 40 (arithmetic), in [-128, 128]
@@ -74,6 +97,28 @@ __device__ __forceinline__ void digits(double v, int emax, uint32_t (&d)[kDigits
     d[3] = low_digit<3>(ylo, 0x7542);
     d[4] = low_digit<4>(ylo, 0x7541);
     d[5] = low_digit<5>(ylo, 0x7540);
+}
+
+// The pre-scaled digits of v (top digit first) for a row whose largest
+// biased exponent is emax.
+__device__ __forceinline__ void digits(double v, int emax, uint32_t (&d)[kDigits]) {
+    digits_fixed(fixed(v, emax), d);
+}
+
+// Digits of 8 fixed-point values of a row as one 16-byte core-matrix row per
+// digit plane.
+__device__ __forceinline__ void digits8_fixed(const long long (&X)[8], uint4 (&w)[kDigits]) {
+    uint32_t x[kDigits][4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        uint32_t d0[kDigits], d1[kDigits];
+        digits_fixed(X[2 * h], d0);
+        digits_fixed(X[2 * h + 1], d1);
+#pragma unroll
+        for (int a = 0; a < kDigits; ++a) x[a][h] = __byte_perm(d0[a], d1[a], 0x7632);
+    }
+#pragma unroll
+    for (int a = 0; a < kDigits; ++a) w[a] = make_uint4(x[a][0], x[a][1], x[a][2], x[a][3]);
 }
 
 // Digits of 8 consecutive values of a row, packed as one 16-byte core-matrix

@@ -426,6 +426,14 @@ int pairing_mesh(mg_ctx* c) {
                                                                            H.fre, H.fim);
     MG_LAUNCHED(c);
     const size_t sm_g = (size_t)(2 * hmax * (4 * kGPts + 1) + hmax * hmax) * sizeof(double);
+    if (mixed && c->tc_ok && hmax <= 64) {
+        // tensor cores (meshgemm_tc.cu): the summed partials go to chunk slot 0
+        MG_TRY(gaps_tc(c, H.gpart));
+        k_gaps_finish<<<dim3(div_up(nmax * nmax, 128), 4), 128, 0, c->stream>>>(
+            H.gpart, H.members, H.hsz, hmax, nmax, 1, H.pcut, c->dv, H.delta);
+        MG_LAUNCHED(c);
+        return MG_OK;
+    }
     if (mixed)
         k_pair_gaps_df<<<dim3(H.gchunk, 4), kThreads, sm_g, c->stream>>>(
             B.psi, H.members, H.hsz, hmax, H.fre, H.fim, V, H.gchunk, H.gpart);
