@@ -26,6 +26,20 @@ __device__ __forceinline__ dfl df_from(double x) {
 
 __device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
 
+// float -> double by bit moves (normal floats; zero and subnormals give 0):
+// no FP64-pipe conversion
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0u) return 0.0;
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const unsigned lo = u << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double-float -> FP64 with one FP64 add (parts below 2^-126 are dropped)
+__device__ __forceinline__ double df_to_fast(dfl a) { return f2d_bits(a.h) + f2d_bits(a.l); }
+
 // FP64 -> double-float with integer instructions only.  FP64 adds and the
 // FP64 <-> FP32 conversions issue at the (low) FP64 rate on GB300, so the hot
 // loops split their FP64 inputs from the bit pattern: hi keeps the sign, the

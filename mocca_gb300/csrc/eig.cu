@@ -225,6 +225,9 @@ __device__ __forceinline__ bool skip_step(const SkipCtl& k, int b) {
 }
 
 // Batched FP64 GEMM, C = alpha op(A) op(B) + beta C, m,n,k <= 128, row-major.
+// With g.sym (C symmetric, and C itself when beta != 0) only the upper
+// triangle is computed and written to both halves, which also makes C
+// exactly symmetric.
 __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict__ descs,
                                                      SkipCtl sk) {
     __shared__ double sA[kTile][129];
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
     if (skip_step(sk, g.mat)) return;
     const int tiles_n = (g.n + kTile - 1) / kTile;
     const int ti = blockIdx.x / tiles_n, tj = blockIdx.x % tiles_n;
-    if (ti * kTile >= g.m) return;
+    if (ti * kTile >= g.m || (g.sym && ti > tj)) return;
     const int r = threadIdx.x / kTile, cidx = threadIdx.x % kTile;
     for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
         const int i = q / g.k, kk = q % g.k;
@@ -252,10 +255,13 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
     __syncthreads();
     const int gi = ti * kTile + r, gj = tj * kTile + cidx;
     if (gi >= g.m || gj >= g.n) return;
+    if (g.sym && gi > gj) return;   // the mirror of an entry another thread writes
     double s = 0.0;
     for (int kk = 0; kk < g.k; ++kk) s = fma(sA[r][kk], sB[kk][cidx], s);
     double* c = g.C + (long)gi * g.ldc + gj;
-    *c = g.beta == 0.0 ? g.alpha * s : fma(g.alpha, s, g.beta * *c);
+    const double v = g.beta == 0.0 ? g.alpha * s : fma(g.alpha, s, g.beta * *c);
+    *c = v;
+    if (g.sym && gi < gj) g.C[(long)gj * g.ldc + gi] = v;
 }
 
 // Ogita-Aishima correction, spread over one CTA per matrix row so that the
@@ -650,10 +656,10 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
         const int n = hn[b];
         const long o = (long)b * stride;
         ax[b] = GemmDesc{A + o, E.X + o, E.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
-        sg[2 * b] = GemmDesc{E.X + o, E.AX + o, E.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
-        sg[2 * b + 1] = GemmDesc{E.X + o, E.X + o, E.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+        sg[2 * b] = GemmDesc{E.X + o, E.AX + o, E.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b, 1};
+        sg[2 * b + 1] = GemmDesc{E.X + o, E.X + o, E.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b, 1};
         xf[b] = GemmDesc{E.X + o, E.G + o, E.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
-        rr[b] = GemmDesc{E.AX + o, E.AX + o, E.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b};
+        rr[b] = GemmDesc{E.AX + o, E.AX + o, E.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b, 1};
     }
     MG_CUDA(cudaMalloc(&E.d_ax, nb * sizeof(GemmDesc)));
     MG_CUDA(cudaMalloc(&E.d_sg, 2 * nb * sizeof(GemmDesc)));
@@ -762,10 +768,10 @@ __global__ void k_eig_noalloc_tables(NoAllocArgs a, int* nsz, GemmDesc* ax, Gemm
     const long o = (long)b * ld * ld;
     nsz[b] = n;
     ax[b] = GemmDesc{a.A + o, a.X + o, a.AX + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
-    sg[2 * b] = GemmDesc{a.X + o, a.AX + o, a.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
-    sg[2 * b + 1] = GemmDesc{a.X + o, a.X + o, a.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b};
+    sg[2 * b] = GemmDesc{a.X + o, a.AX + o, a.S + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b, 1};
+    sg[2 * b + 1] = GemmDesc{a.X + o, a.X + o, a.G + o, n, n, n, ld, ld, ld, 1, 0, 1.0, 0.0, b, 1};
     xf[b] = GemmDesc{a.X + o, a.G + o, a.X2 + o, n, n, n, ld, ld, ld, 0, 0, 1.0, 0.0, b};
-    rr[b] = GemmDesc{a.AX + o, a.AX + o, a.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b};
+    rr[b] = GemmDesc{a.AX + o, a.AX + o, a.G + o, n, n, n, ld, ld, ld, 0, 0, 0.375, 1.0, b, 1};
 }
 
 // Once per device, with that device current: the scratch address, the

@@ -141,12 +141,34 @@ __device__ __forceinline__ void pauli_df(const dfl* p, int dir, dfl* o) {
     else { o[0] = p[0]; o[1] = p[1]; o[2] = df_neg(p[2]); o[3] = df_neg(p[3]); }
 }
 
+// The isospin's fields as double-float, once per h.psi call (they are shared
+// by every spwf of the isospin): per point, in order
+//   -(B + hbm/2 mu_red), U, -dB/dx_m (3), W_nm (n-major, 9), (div W)_n / 2 (3).
+constexpr int kNF = 17;
+
+__global__ void k_fields_df(Fields F, long V, double kin0, double kin1, float2* __restrict__ out) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * V) return;
+    const int it = (int)(t / V);
+    const long v = t % V;
+    float2* o = out + (long)it * kNF * V + v;
+    auto put = [&](int f, double x) {
+        const dfl d = df_from(x);
+        o[(long)f * V] = make_float2(d.h, d.l);
+    };
+    put(0, -(F.B[it * V + v] + (it == 0 ? kin0 : kin1)));
+    put(1, F.U[it * V + v]);
+    for (int m = 0; m < 3; ++m) put(2 + m, -F.nablaB[(it * 3 + m) * V + v]);
+    for (int q = 0; q < 9; ++q) put(5 + q, F.W[(it * 9 + q) * V + v]);
+    for (int n = 0; n < 3; ++n) put(14 + n, 0.5 * F.divW[(it * 3 + n) * V + v]);
+}
+
 template <bool kGradStep>
 __global__ void __launch_bounds__(kThreads, 3)
 k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
-          const float2* __restrict__ lap, const int* __restrict__ qn, Fields F,
-          double* __restrict__ hout, double* __restrict__ upd, double* __restrict__ partial,
-          long V, double kin0, double kin1, double fac, double mom) {
+          const float2* __restrict__ lap, const int* __restrict__ qn,
+          const float2* __restrict__ Fd, double* __restrict__ hout, double* __restrict__ upd,
+          double* __restrict__ partial, long V, double fac, double mom) {
     const int i = blockIdx.y;
     const long v = (long)blockIdx.x * kThreads + threadIdx.x;
     // <psi|h psi> and <h psi|h psi> accumulate in double-float and become
@@ -154,7 +176,7 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
     float eh = 0.f, el = 0.f, hh = 0.f, hl = 0.f;
     if (v < V) {
         const int it = (qn[4 * i] + 3) / 2 - 1;
-        const double kin = it == 0 ? kin0 : kin1;
+        const float2* fd = Fd + (long)it * kNF * V + v;
         double* ps = psi + (long)i * 4 * V;
         const float2* dr = der + (long)i * 12 * V;
         const float2* lp = lap + (long)i * 4 * V;
@@ -173,8 +195,7 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
         // B, U: -(B + hbar^2/2m) lap psi + U psi
         float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
         {
-            const dfl nkB = df_neg(df_add(df_split(F.B[it * V + v]), df_split(kin)));
-            const dfl Uq = df_split(F.U[it * V + v]);
+            const dfl nkB = df_ld(fd), Uq = df_ld(fd + V);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 df_acc(th[l], tl[l], nkB, df_ld(lp + l * V + v));
@@ -188,14 +209,14 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
             dfl dm[4];
 #pragma unroll
             for (int l = 0; l < 4; ++l) dm[l] = df_ld(dr + (mu * 4 + l) * V + v);
-            const dfl nb = df_neg(df_split(F.nablaB[(it * 3 + mu) * V + v]));
+            const dfl nb = df_ld(fd + (2 + mu) * V);
 #pragma unroll
             for (int l = 0; l < 4; ++l) df_acc(th[l], tl[l], nb, dm[l]);
 #pragma unroll
             for (int nu = 0; nu < 3; ++nu) {
                 dfl sg[4];
                 pauli_df(dm, nu + 1, sg);
-                const dfl wv = df_split(F.W[((it * 3 + nu) * 3 + mu) * V + v]);
+                const dfl wv = df_ld(fd + (5 + nu * 3 + mu) * V);
 #pragma unroll
                 for (int l = 0; l < 4; ++l) df_acc(wh[l], wl[l], wv, sg[l]);
             }
@@ -204,9 +225,7 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
         for (int nu = 0; nu < 3; ++nu) {
             dfl sg[4];
             pauli_df(p, nu + 1, sg);
-            dfl hv = df_split(F.divW[(it * 3 + nu) * V + v]);
-            hv.h *= 0.5f;   // exact
-            hv.l *= 0.5f;
+            const dfl hv = df_ld(fd + (14 + nu) * V);
 #pragma unroll
             for (int l = 0; l < 4; ++l) df_acc(wh[l], wl[l], hv, sg[l]);
         }
@@ -230,15 +249,15 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
                 df_acc(ah, al, nf, h[l]);
                 df_acc(ah, al, mm, df_split(u64[l]));
                 up[l * V + v] = p64[l];
-                ps[l * V + v] = df_to(df_add(p[l], df_norm(dfl{ah, al})));
+                ps[l * V + v] = df_to_fast(df_add(p[l], df_norm(dfl{ah, al})));
             }
         } else if (hout) {
             double* ho = hout + (long)i * 4 * V;
 #pragma unroll
-            for (int l = 0; l < 4; ++l) ho[l * V + v] = df_to(h[l]);
+            for (int l = 0; l < 4; ++l) ho[l * V + v] = df_to_fast(h[l]);
         }
     }
-    double s_eh = df_to(dfl{eh, el}), s_hh = df_to(dfl{hh, hl});
+    double s_eh = df_to_fast(df_norm(dfl{eh, el})), s_hh = df_to_fast(df_norm(dfl{hh, hl}));
     __shared__ double red[2][kThreads / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -297,14 +316,20 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     const bool mixed = B.der_df;
     const float2* der2 = reinterpret_cast<const float2*>(B.der);
     const float2* lap2 = reinterpret_cast<const float2*>(B.lap);
+    if (mixed) {
+        if (!c->fields_df) MG_CUDA(cudaMalloc(&c->fields_df, 2 * kNF * V * sizeof(float2)));
+        k_fields_df<<<div_up(2 * V, kThreads), kThreads, 0, c->stream>>>(F, V, kin0, kin1,
+                                                                         c->fields_df);
+        MG_LAUNCHED(c);
+    }
     if (grad_step && mixed)
-        k_hpsi_df<true><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn, F, nullptr,
-                                                          c->updates, c->red, V, kin0, kin1, fac,
+        k_hpsi_df<true><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn, c->fields_df,
+                                                          nullptr, c->updates, c->red, V, fac,
                                                           mom);
     else if (mixed)
-        k_hpsi_df<false><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn, F, out,
-                                                           nullptr, c->red, V, kin0, kin1, 0.0,
-                                                           0.0);
+        k_hpsi_df<false><<<grid, kThreads, 0, c->stream>>>(B.psi, der2, lap2, B.qn,
+                                                           c->fields_df, out, nullptr, c->red, V,
+                                                           0.0, 0.0);
     else if (grad_step)
         k_hpsi<true><<<grid, kThreads, 0, c->stream>>>(B.psi, B.der, B.lap, B.qn, F, nullptr,
                                                        c->updates, c->red, V, kin0, kin1, fac, mom);

@@ -55,16 +55,6 @@ __device__ __forceinline__ double pow2d(int x) {
     return x < -1022 ? 0.0 : __longlong_as_double((long long)(min(x, 1023) + 1023) << 52);
 }
 
-// float -> double by bit moves (normal floats; zero and subnormals give 0)
-__device__ __forceinline__ double f2d_bits(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u) return 0.0;
-    const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
-    const uint32_t lo = u << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 __global__ void __launch_bounds__(256, 2)
 k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
                 const int* __restrict__ ordered, int nbmax, long V4, int nchunk,

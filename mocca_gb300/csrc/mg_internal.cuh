@@ -76,7 +76,9 @@ struct GemmDesc {
     int ta, tb;
     double alpha, beta;
     int mat;   // matrix of the batch (for the refinement's early exit)
+    int sym;   // C is symmetric: tiles below the diagonal are skipped and mirrored
 };
+static_assert(sizeof(GemmDesc) == 80, "GemmDesc keeps its 80-byte workspace layout");
 
 // A batch of small symmetric eigenproblems (eig.cu).
 struct EigBatch {
@@ -185,6 +187,7 @@ struct mg_ctx {
     // potentials
     double *U = nullptr, *Bp = nullptr, *nablaB = nullptr, *W = nullptr, *divW = nullptr;
     double* divw_tmp = nullptr;   // 3 * 6V
+    float2* fields_df = nullptr;  // mixed h.psi: the isospins' fields as double-float (2 x 17V)
     mg::GridJob* field_jobs = nullptr;  // rho derivs (2), B derivs (2), divW (18)
     int n_field_jobs = 0;
 
