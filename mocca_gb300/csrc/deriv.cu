@@ -417,7 +417,9 @@ int build_basis_jobs(mg_ctx* c, int b) {
 int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     if (njobs <= 0) return MG_OK;
     const int nx = c->nx, ny = c->ny, nz = c->nz;
-    const int ppb = 4;
+    // z planes per k_deriv_xy block: one when few grids (densities, fields)
+    // would leave most SMs idle
+    const int ppb = njobs < 64 ? 1 : 4;
     static bool attr_done = false;
     if (!attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_deriv_xy, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -25,15 +26,18 @@ k_dots(const double* __restrict__ a, const double* __restrict__ b, long V4,
        double* __restrict__ part) {
     const int i = blockIdx.y;
     double s = 0.0;
-    for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4; o += (long)gridDim.x * kThreads) {
-        double bv;
-        if (kBdf) {
-            const float2 p = reinterpret_cast<const float2*>(b)[(long)i * V4 + o];
-            bv = (double)p.x + (double)p.y;
-        } else {
-            bv = b[(long)i * V4 + o];
-        }
-        s = fma(a[(long)i * V4 + o], bv, s);
+    if (kBdf) {
+        // double-float products and sums (FP32 pipe), FP64 once per thread
+        float sh = 0.f, sl = 0.f;
+        const float2* bp = reinterpret_cast<const float2*>(b) + (long)i * V4;
+        for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4;
+             o += (long)gridDim.x * kThreads)
+            df_acc(sh, sl, df_split(a[(long)i * V4 + o]), df_ld(bp + o));
+        s = df_to_fast(df_norm(dfl{sh, sl}));
+    } else {
+        for (long o = (long)blockIdx.x * kThreads + threadIdx.x; o < V4;
+             o += (long)gridDim.x * kThreads)
+            s = fma(a[(long)i * V4 + o], b[(long)i * V4 + o], s);
     }
     __shared__ double red[kThreads / 32];
     for (int q = 16; q > 0; q >>= 1) s += __shfl_xor_sync(0xffffffffu, s, q);
