@@ -65,6 +65,13 @@ __device__ __forceinline__ int rr_player(int j, int r, int n) {
     return j == 0 ? 0 : 1 + (j - 1 + r) % (n - 1);
 }
 
+// The round in which players p < q meet: q mod m for p = 0, else
+// (p + q) (m + 1) / 2 mod m (m = n - 1 is odd, so 2 is invertible mod m).
+__device__ __forceinline__ int rr_round(int p, int q, int n) {
+    const int m = n - 1;
+    return p == 0 ? q % m : ((p + q) * ((m + 1) / 2)) % m;
+}
+
 }  // namespace
 
 // One matrix per CTA.  A: FP64 n x n (lda) input; Xw: optional FP64 warm
@@ -361,6 +368,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     __shared__ double cs[2][64];
     __shared__ int act[64];
     __shared__ int pqi[2][64];
+    __shared__ unsigned rmask[4];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
     if (n0 == 0) return;
@@ -385,13 +393,24 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     int sweep = 0;
     for (; sweep < 12; ++sweep) {
         // a pair rotates when its coupling is above the FP64 noise of X^T A X
-        // (~ sqrt(n) eps |A|): rotating noise would only churn, at FP64 cost
+        // (~ sqrt(n) eps |A|): rotating noise would only churn, at FP64 cost.
+        // Only the rounds holding such a pair at the start of the sweep run
+        // (after a refinement these are the few near-degenerate clusters); a
+        // pair that a rotation lifts above the threshold waits for the next
+        // sweep.
+        if (tid < 4) rmask[tid] = 0u;
+        __syncthreads();
         int any = 0;
         if (lane < n)
-            for (int i = kg; i < n; i += kJGroups)
-                if (i != lane && fabs(a[i * l2 + lane]) > thr) any = 1;
+            for (int i = kg; i < lane; i += kJGroups)
+                if (fabs(a[i * l2 + lane]) > thr) {
+                    const int r = rr_round(i, lane, n);
+                    atomicOr(&rmask[r >> 5], 1u << (r & 31));
+                    any = 1;
+                }
         if (!__syncthreads_or(any)) break;
         for (int r = 0; r < n - 1; ++r) {
+            if (!((rmask[r >> 5] >> (r & 31)) & 1u)) continue;
             int on = 0;
             if (tid < half) {
                 const int p = rr_player(tid, r, n), qq = rr_player(n - 1 - tid, r, n);
@@ -620,6 +639,15 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
     }
+    return MG_OK;
+}
+
+// ndesc FP64 GEMMs of at most maxdim x maxdim from a device descriptor table.
+int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim) {
+    const SkipCtl none{nullptr, nullptr, 0, 0, 0.0};
+    const int tiles = div_up(maxdim, kTile) * div_up(maxdim, kTile);
+    k_gemm64<<<dim3(tiles, ndesc), kThreads, 0, c->stream>>>(descs, none);
+    MG_LAUNCHED(c);
     return MG_OK;
 }
 

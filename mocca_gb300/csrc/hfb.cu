@@ -41,6 +41,10 @@ constexpr int kThreads = 256;
 // leaves the positive/negative split exact to FP64 rounding (the angle left
 // is ~ tol^2).
 constexpr double kRefineTol = 1e-8;
+// Largest Newton step of the Fermi energy finished by the first-order
+// expansion instead of an evaluation (the second-order remainder in N is
+// below 1e-13 for the curvatures seen, far inside FermiPrec = 1e-12).
+constexpr double kTaylorStep = 2e-7;
 
 __device__ double cta_sum(double x, double* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -162,6 +166,47 @@ __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ 
         out[4 + b] = ds;
         out[8 + b] = em;
     }
+}
+
+// First-order finish of the Fermi search.  With T(lambda) = T0 - lambda
+// Sigma and the eigenpairs (E, x) of the last evaluation, the vectors move as
+// dx_m = sum_{n != m} x_n 2 p_nm / (E_m - E_n), p_nm = y_n . y_m (y, w: lower
+// and upper halves).  Pairs of positive states cancel, so with the
+// positive (p) and negative (n) halves Y_p, Y_n, W_p, W_n and
+//   C[n][m] = 2 p_nm / (E_m - E_n)      (m > 0 > n)
+//   d rho_++ / d lambda = Z + Z^T,  Z = Y_n C Y_p^T
+//   d kappa_-+ / d lambda = Y_n C W_p^T + Y_p C^T W_n^T,
+// whose trace gives back dN/dlambda = 8 sum p_nm^2 / (E_m - E_n).
+__global__ void k_taylor_coef(const double* __restrict__ P, const double* __restrict__ w,
+                              long wstride, const int* __restrict__ hsz, int hmax,
+                              double* __restrict__ C) {
+    const int b = blockIdx.y, h = hsz[b];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= h * h) return;
+    const int n = t / h, m = t % h;
+    const long o = (long)b * hmax * hmax + (long)n * hmax + m;
+    C[o] = 2.0 * P[o] / (w[b * wstride + h + m] - w[b * wstride + n]);
+}
+
+// rho += dl (Z + Z^T) in both diagonal blocks, kappa_-+ += dl K and
+// kappa_+- -= dl K^T, dl = the isospin's step (0: converged already)
+__global__ void k_taylor_update(const double* __restrict__ Z, const double* __restrict__ K,
+                                const int* __restrict__ hsz, int hmax, int nmax, double dl0,
+                                double dl1, double* __restrict__ rho, double* __restrict__ kappa) {
+    const int b = blockIdx.y, h = hsz[b], N = 2 * h;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const double dl = b / 2 == 0 ? dl0 : dl1;
+    if (t >= h * h || dl == 0.0) return;
+    const int r = t / h, s = t % h;
+    const double* Zb = Z + (long)b * hmax * hmax;
+    const double dr = Zb[r * hmax + s] + Zb[s * hmax + r];
+    const double dk = K[(long)b * hmax * hmax + r * hmax + s];
+    double* R = rho + (long)b * nmax * nmax;
+    double* Kp = kappa + (long)b * nmax * nmax;
+    R[(long)r * N + s] += dl * dr;
+    R[(long)(h + r) * N + h + s] += dl * dr;
+    Kp[(long)(h + r) * N + s] += dl * dk;
+    Kp[(long)s * N + h + r] -= dl * dk;
 }
 
 // rho_++ blocks into the eigensolver batch (leading dimension hmax); HF
@@ -293,6 +338,32 @@ int hfb_prepare(mg_ctx* c) {
     H.eT.skip_tol = 1e-10;
     MG_TRY(eig_setup(c, H.eR, 4, hmax, H.hsz, H.Rpp, (long)hmax * hmax, hmax));
     H.nref = 3;
+    {
+        const long hh = 4L * hmax * hmax;
+        if (!(A(&H.tP, hh) && A(&H.tC, hh) && A(&H.tT1, hh) && A(&H.tT2, hh) && A(&H.tZ, hh) &&
+              A(&H.tK, hh)))
+            return MG_ERR_CUDA;
+        std::vector<GemmDesc> d(24);
+        const int nm = H.nmax;
+        for (int b = 0; b < 4; ++b) {
+            const int h = H.hsz_h[b];
+            const double* X = H.eT.X + (long)b * nm * nm;
+            const double *Yn = X + (long)h * nm, *Yp = X + (long)h * nm + h, *Wn = X, *Wp = X + h;
+            const long o = (long)b * hmax * hmax;
+            // P = Y_n^T Y_p
+            d[b] = GemmDesc{Yn, Yp, H.tP + o, h, h, h, nm, nm, hmax, 1, 0, 1.0, 0.0, b, 0};
+            // T1 = Y_n C, T2 = Y_p C^T
+            d[4 + 2 * b] = GemmDesc{Yn, H.tC + o, H.tT1 + o, h, h, h, nm, hmax, hmax, 0, 0, 1.0, 0.0, b, 0};
+            d[5 + 2 * b] = GemmDesc{Yp, H.tC + o, H.tT2 + o, h, h, h, nm, hmax, hmax, 0, 1, 1.0, 0.0, b, 0};
+            // Z = T1 Y_p^T, K = T1 W_p^T
+            d[12 + 2 * b] = GemmDesc{H.tT1 + o, Yp, H.tZ + o, h, h, h, hmax, nm, hmax, 0, 1, 1.0, 0.0, b, 0};
+            d[13 + 2 * b] = GemmDesc{H.tT1 + o, Wp, H.tK + o, h, h, h, hmax, nm, hmax, 0, 1, 1.0, 0.0, b, 0};
+            // K += T2 W_n^T
+            d[20 + b] = GemmDesc{H.tT2 + o, Wn, H.tK + o, h, h, h, hmax, nm, hmax, 0, 1, 1.0, 1.0, b, 0};
+        }
+        MG_CUDA(cudaMalloc(&H.d_taylor, d.size() * sizeof(GemmDesc)));
+        MG_CUDA(cudaMemcpy(H.d_taylor, d.data(), d.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice));
+    }
     // canonical basis quantum numbers: block order (it, parity -1 then +1)
     std::vector<int> cqn(4 * nwt);
     for (int b = 0; b < 4; ++b)
@@ -326,8 +397,9 @@ void hfb_free(mg_ctx* c) {
     Hfb& H = c->hfb;
     for (double* p : {H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.qe, H.dfac, H.pcut, H.ktil,
                       H.fpart, H.fre, H.fim, H.gpart, H.cantr, H.occ, H.fermi_d, H.trace_d, H.dpart,
-                      H.scal_d, H.T, H.Rpp})
+                      H.scal_d, H.T, H.Rpp, H.tP, H.tC, H.tT1, H.tT2, H.tZ, H.tK})
         if (p) cudaFree(p);
+    if (H.d_taylor) cudaFree(H.d_taylor);
     for (int* p : {H.members, H.hsz, H.cstart, H.nsz_T})
         if (p) cudaFree(p);
     if (H.h_pinned) cudaFreeHost(H.h_pinned);
@@ -427,6 +499,24 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     return MG_OK;
 }
 
+// rho and kappa moved to lambda + dl from the eigen-decomposition of the last
+// evaluation (first order in dl).
+static int taylor_finish(mg_ctx* c, const double dl[2]) {
+    Hfb& H = c->hfb;
+    const int hmax = H.hmax;
+    const dim3 g(div_up(hmax * hmax, kThreads), 4);
+    MG_TRY(gemm_batched(c, H.d_taylor, 4, hmax));
+    k_taylor_coef<<<g, kThreads, 0, c->stream>>>(H.tP, H.eT.w, H.eT.wstride, H.hsz, hmax, H.tC);
+    MG_LAUNCHED(c);
+    MG_TRY(gemm_batched(c, H.d_taylor + 4, 8, hmax));
+    MG_TRY(gemm_batched(c, H.d_taylor + 12, 8, hmax));
+    MG_TRY(gemm_batched(c, H.d_taylor + 20, 4, hmax));
+    k_taylor_update<<<g, kThreads, 0, c->stream>>>(H.tZ, H.tK, H.hsz, hmax, H.nmax, dl[0], dl[1],
+                                                  H.rho, H.kappa);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
 // SolvePairing for HFB (src/Pairing.f90:743-890, PairingIter 1).
 int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     Hfb& H = c->hfb;
@@ -470,14 +560,38 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     bracket(1);
     const int maxit = H.pp.max_iter > 0 ? H.pp.max_iter : 50;
     for (int k = 0; k < maxit && !(conv[0] && conv[1]); ++k) {
+        double dl[2] = {0.0, 0.0};
+        bool newton[2] = {true, true};
         for (int it = 0; it < 2; ++it) {
             if (conv[it]) continue;
             double step = fp[it] > 1e-12 ? -f[it] / fp[it] : (f[it] < 0 ? 0.5 : -0.5);
+            newton[it] = fp[it] > 1e-12 && std::fabs(step) <= 5.0;
             step = std::max(-5.0, std::min(5.0, step));
             double next = lam[it] + step;
-            if (has_lo[it] && has_hi[it] && !(next > lo[it] && next < hi[it]))
+            if (has_lo[it] && has_hi[it] && !(next > lo[it] && next < hi[it])) {
                 next = 0.5 * (lo[it] + hi[it]);
+                newton[it] = false;
+            }
+            dl[it] = next - lam[it];
             lam[it] = next;
+        }
+        // Last Newton step: when every remaining step is a plain Newton step
+        // below kTaylorStep, rho and kappa move to the new lambda to first
+        // order from the evaluation just made.  N(lambda) then misses N0 by
+        // ~N'' dl^2 / 2 (~1e-14 at this step), the same as an evaluation at
+        // the new lambda would report; no eigen-decomposition is redone.
+        bool taylor = true;
+        for (int it = 0; it < 2; ++it)
+            taylor = taylor && (conv[it] || (newton[it] && std::fabs(dl[it]) <= kTaylorStep));
+        if (taylor) {
+            MG_TRY(taylor_finish(c, dl));
+            ++H.taylor_steps;
+            for (int it = 0; it < 2; ++it) {
+                if (conv[it]) continue;
+                f[it] += fp[it] * dl[it];
+                conv[it] = true;
+            }
+            break;
         }
         MG_TRY(hfb_evaluate(c, lam, f, fp, false));
         ++evals;

@@ -142,6 +142,12 @@ struct Hfb {
     double* Rpp = nullptr;    // 4 blocks of rho_++, hmax x hmax
     int* nsz_T = nullptr;     // N per block
     EigBatch eT, eR;          // eigensolver batches for T and rho_++
+    // first-order finish of the Fermi search (hfb.cu): h x h workspaces per
+    // block (ld hmax) and the GEMM tables of d rho / d lambda, d kappa / d lambda
+    double *tP = nullptr, *tC = nullptr, *tT1 = nullptr, *tT2 = nullptr, *tZ = nullptr,
+           *tK = nullptr;
+    GemmDesc* d_taylor = nullptr;    // 4 + 8 + 8 + 4 descriptors
+    long long taylor_steps = 0;      // pairing steps finished by the expansion
     int nref = 2;             // FP64 refinement steps per eigen-decomposition
 };
 
@@ -277,6 +283,7 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
 // the vectors in E.X, or refinement started directly from E.X.
 enum EigSeed { kSeedCold = 0, kSeedJacobiWarm = 1, kSeedRefine = 2 };
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish);
+int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim);
 void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
