@@ -104,15 +104,25 @@ k_energy_partial(const double* __restrict__ rho, const double* __restrict__ tau,
 
 }  // namespace
 
+static int dots_chunks(long V4) { return std::max(1, std::min(64, div_up(V4, kThreads * 8))); }
+
+// block partials of the nwt dot products <a_i|b_i> into out[i * nch + chunk]
+static int launch_dots(mg_ctx* c, const double* a, const double* b, bool b_df, double* out) {
+    const long V4 = 4 * c->V;
+    const int nch = dots_chunks(V4);
+    if (b_df)
+        k_dots<true><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, out);
+    else
+        k_dots<false><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, out);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
 // nwt dot products <a_i|b_i> * dv of a basis into host array out.
 int basis_dots(mg_ctx* c, const double* a, const double* b, double* out, bool b_df) {
     const long V4 = 4 * c->V;
-    const int nch = std::max(1, std::min(64, div_up(V4, kThreads * 8)));
-    if (b_df)
-        k_dots<true><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
-    else
-        k_dots<false><<<dim3(nch, c->p.nwt), kThreads, 0, c->stream>>>(a, b, V4, c->red);
-    MG_LAUNCHED(c);
+    const int nch = dots_chunks(V4);
+    MG_TRY(launch_dots(c, a, b, b_df, c->red));
     std::vector<double> h((size_t)nch * c->p.nwt);
     MG_CUDA(cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
                             c->stream));
@@ -132,20 +142,32 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     const int nwt = c->p.nwt;
     const long V = c->V;
     const mg_skyrme_b& B = c->B;
-    std::vector<double> ip(nwt);
-    MG_TRY(basis_dots(c, D.psi, D.lap, ip.data(), D.der_df));
+    // the per-spwf <psi|lap psi> partials and the mesh-integral partials go
+    // to two regions of the reduction table and come back in one read
+    const long V4 = 4 * V;
+    const int nch = dots_chunks(V4);
+    const size_t ndots = (size_t)nch * nwt;
+    launch_dots(c, D.psi, D.lap, D.der_df, c->red);
     std::vector<double> occ(nwt), e(nwt);
     MG_CUDA(cudaMemcpyAsync(occ.data(), D.occ, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaMemcpyAsync(e.data(), D.e, nwt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     const int nblk = std::max(1, std::min(2 * c->num_sms, div_up(V, kThreads)));
+    if (ndots + (size_t)nblk * kTerms > c->red_len) return MG_ERR_STATE;
     ECoef k{B.B4, B.B6, B.B8a, B.B8b, B.B9q, B.byt3a, B.byt3b, B.B7b};
     k_energy_partial<<<nblk, kThreads, 0, c->stream>>>(c->rho, c->tau, c->laprho, c->nablaj,
-                                                       c->coulomb, k, V, c->red);
+                                                       c->coulomb, k, V, c->red + ndots);
     MG_LAUNCHED(c);
-    std::vector<double> part((size_t)nblk * kTerms);
-    MG_CUDA(cudaMemcpyAsync(part.data(), c->red, part.size() * sizeof(double),
+    std::vector<double> all(ndots + (size_t)nblk * kTerms);
+    MG_CUDA(cudaMemcpyAsync(all.data(), c->red, all.size() * sizeof(double),
                             cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<double> ip(nwt);
+    for (int i = 0; i < nwt; ++i) {
+        double s = 0.0;
+        for (int q = 0; q < nch; ++q) s += all[(size_t)i * nch + q];
+        ip[i] = s * c->dv;
+    }
+    const double* part = all.data() + ndots;
     double S[kTerms] = {0};
     for (int b = 0; b < nblk; ++b)
         for (int q = 0; q < kTerms; ++q) S[q] += part[(size_t)b * kTerms + q];

@@ -129,6 +129,9 @@ k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int
     double* S = sm;              // nb x nb (upper used), becomes R
     double* X = sm + nb * nb;    // nb x nb
     __shared__ double rinv[256];
+    __shared__ double u[256];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    constexpr int kWarps = kThreads / 32;
     for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
         const int k = t / nb, l = t % nb;
         S[t] = k <= l ? part[(long)b * nchunk * nbmax * nbmax + k * nbmax + l] * dv : 0.0;
@@ -136,13 +139,16 @@ k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int
     }
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
+        // pivot row scaled once (u_k = S_jk / S_jj), then one FMA per entry of
+        // the trailing upper triangle, a warp per row
         const double d = S[j * nb + j];
         if (threadIdx.x == 0 && !(d > 0.0)) atomicExch(flag, 1);
         const double inv_d = 1.0 / fmax(d, 1e-300);
-        const int m = nb - j - 1;
-        for (int t = threadIdx.x; t < m * m; t += kThreads) {
-            const int k = j + 1 + t / m, l = j + 1 + t % m;
-            if (k <= l) S[k * nb + l] -= S[j * nb + k] * S[j * nb + l] * inv_d;
+        for (int k = j + 1 + threadIdx.x; k < nb; k += kThreads) u[k] = S[j * nb + k] * inv_d;
+        __syncthreads();
+        for (int k = j + 1 + warp; k < nb; k += kWarps) {
+            const double uk = u[k];
+            for (int l = k + lane; l < nb; l += 32) S[k * nb + l] = fma(-uk, S[j * nb + l], S[k * nb + l]);
         }
         __syncthreads();
     }

@@ -200,7 +200,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     const long dens = (long)density_groups(c) * 6 * V;
     const long dots = 64 * nwt;
     const long en = 2L * c->num_sms * 20 + 4L * c->num_sms;
-    c->red_len = (size_t)std::max(std::max(hp, dens), std::max(dots, en));
+    c->red_len = (size_t)std::max(std::max(hp, dens), dots + en);   // energy uses both
     if (!A(&c->red, (long)c->red_len)) return fail(MG_ERR_CUDA);
     if (cudaMalloc(&c->flags, 16 * sizeof(int)) != cudaSuccess ||
         cudaMemset(c->flags, 0, 16 * sizeof(int)) != cudaSuccess ||
