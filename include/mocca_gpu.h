@@ -42,7 +42,7 @@ extern "C" {
 
 /* ---- precision modes ----------------------------------------------------- */
 #define MG_FP64   0   /* plain path: every kernel in FP64                 */
-#define MG_MIXED  1   /* tensor-core derivative GEMMs, FP32 mean fields   */
+#define MG_MIXED  1   /* tensor-core digit GEMMs, double-float mesh work  */
 
 /* ---- bases --------------------------------------------------------------- */
 #define MG_HF_BASIS   0   /* HFBasis(:), src/SpwfStorage.f90:27            */
@@ -190,10 +190,12 @@ int mg_destroy(mg_ctx* ctx);
 int mg_synchronize(mg_ctx* ctx);
 /* Precision of the following calls (MG_FP64 or MG_MIXED), e.g. an FP64
  * polish after mixed-precision iterations.  MG_MIXED runs the Lagrange
- * derivative contractions and the mean-field multiplies in FP32 with FP64
- * storage; overlaps, Gram-Schmidt, energies, the HFB matrices and their
- * diagonalisation stay FP64.  No reference counterpart (the reference is
- * FP64 throughout). */
+ * derivative contractions, the Gram-Schmidt overlap and apply, the pairing
+ * gaps and the canonical-basis transform as exact BF16 digit products on the
+ * tensor cores (47-bit operands), and h.psi, the densities and the pairing
+ * field in double-float (FP32 pairs), with FP64 storage; the Cholesky
+ * factor, energies, the HFB matrices and their diagonalisation stay FP64.
+ * No reference counterpart (the reference is FP64 throughout). */
 int mg_set_precision(mg_ctx* ctx, int precision);
 
 /* ---- spinor transfer ------------------------------------------------------- */
