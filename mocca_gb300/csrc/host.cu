@@ -246,12 +246,20 @@ extern "C" int mg_upload_spinors(mg_ctx* c, int b, const double* const* grids, c
         return MG_ERR_ARG;
     Basis& B = c->bas[b];
     const long V4 = 4 * c->V;
-    if (grids)
-        for (int i = 0; i < count; ++i) {
+    if (grids) {
+        // one copy per run of spwfs whose host grids lie back to back (a
+        // Fortran program allocates each Grid separately; a contiguous host
+        // array becomes a single transfer instead of nwt small ones)
+        for (int i = 0; i < count;) {
             if (!grids[i]) return MG_ERR_ARG;
-            MG_CUDA(cudaMemcpyAsync(B.psi + (long)(first + i) * V4, grids[i], V4 * sizeof(double),
-                                    cudaMemcpyHostToDevice, c->stream));
+            int j = i + 1;
+            while (j < count && grids[j] == grids[j - 1] + V4) ++j;
+            MG_CUDA(cudaMemcpyAsync(B.psi + (long)(first + i) * V4, grids[i],
+                                    (size_t)(j - i) * V4 * sizeof(double), cudaMemcpyHostToDevice,
+                                    c->stream));
+            i = j;
         }
+    }
     if (qn) {
         for (int i = 0; i < 4 * count; ++i) {
             const int q = qn[i];
@@ -273,9 +281,15 @@ extern "C" int mg_download_spinors(mg_ctx* c, int b, double* const* grids, int f
     if (!c || !valid_basis(c, b) || !grids || first < 0 || count < 0 || first + count > c->p.nwt)
         return MG_ERR_ARG;
     const long V4 = 4 * c->V;
-    for (int i = 0; i < count; ++i)
+    for (int i = 0; i < count;) {
+        if (!grids[i]) return MG_ERR_ARG;
+        int j = i + 1;   // a run of back-to-back host grids: one transfer
+        while (j < count && grids[j] == grids[j - 1] + V4) ++j;
         MG_CUDA(cudaMemcpyAsync(grids[i], c->bas[b].psi + (long)(first + i) * V4,
-                                V4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+                                (size_t)(j - i) * V4 * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        i = j;
+    }
     MG_CUDA(cudaStreamSynchronize(c->stream));
     return MG_OK;
 }
