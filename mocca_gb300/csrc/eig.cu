@@ -245,15 +245,22 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
     const int ti = blockIdx.x / tiles_n, tj = blockIdx.x % tiles_n;
     if (ti * kTile >= g.m || (g.sym && ti > tj)) return;
     const int r = threadIdx.x / kTile, cidx = threadIdx.x % kTile;
+    // tile loads with the fastest thread index along the operand's contiguous
+    // dimension (transposed operands included), so that a warp reads
+    // consecutive words
     for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
-        const int i = q / g.k, kk = q % g.k;
+        int i, kk;
+        if (g.ta) { i = q % kTile; kk = q / kTile; }
+        else { i = q / g.k; kk = q % g.k; }
         const int gi = ti * kTile + i;
         double x = 0.0;
         if (gi < g.m) x = g.ta ? g.A[(long)kk * g.lda + gi] : g.A[(long)gi * g.lda + kk];
         sA[i][kk] = x;
     }
     for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
-        const int kk = q / kTile, j = q % kTile;
+        int kk, j;
+        if (g.tb) { kk = q % g.k; j = q / g.k; }
+        else { kk = q / kTile; j = q % kTile; }
         const int gj = tj * kTile + j;
         double x = 0.0;
         if (gj < g.n) x = g.tb ? g.B[(long)gj * g.ldb + kk] : g.B[(long)kk * g.ldb + gj];

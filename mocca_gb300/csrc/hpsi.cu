@@ -257,21 +257,30 @@ k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
             for (int l = 0; l < 4; ++l) ho[l * V + v] = df_to_fast(h[l]);
         }
     }
-    double s_eh = df_to_fast(df_norm(dfl{eh, el})), s_hh = df_to_fast(df_norm(dfl{hh, hl}));
-    __shared__ double red[2][kThreads / 32];
+    // warp and block sums in double-float (FP32 pipe), FP64 once per block
+    dfl se = df_norm(dfl{eh, el}), sh = df_norm(dfl{hh, hl});
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        s_eh += __shfl_xor_sync(0xffffffffu, s_eh, o);
-        s_hh += __shfl_xor_sync(0xffffffffu, s_hh, o);
+        se = df_add(se, dfl{__shfl_xor_sync(0xffffffffu, se.h, o),
+                            __shfl_xor_sync(0xffffffffu, se.l, o)});
+        sh = df_add(sh, dfl{__shfl_xor_sync(0xffffffffu, sh.h, o),
+                            __shfl_xor_sync(0xffffffffu, sh.l, o)});
     }
+    __shared__ float2 red[2][kThreads / 32];
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    if (lane == 0) { red[0][warp] = s_eh; red[1][warp] = s_hh; }
+    if (lane == 0) {
+        red[0][warp] = make_float2(se.h, se.l);
+        red[1][warp] = make_float2(sh.h, sh.l);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int q = 0; q < kThreads / 32; ++q) { a += red[0][q]; b += red[1][q]; }
-        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 0] = a;
-        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 1] = b;
+        dfl a = {0.f, 0.f}, b = {0.f, 0.f};
+        for (int q = 0; q < kThreads / 32; ++q) {
+            a = df_add(a, df_ld(&red[0][q]));
+            b = df_add(b, df_ld(&red[1][q]));
+        }
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 0] = df_to_fast(a);
+        partial[((long)i * gridDim.x + blockIdx.x) * 2 + 1] = df_to_fast(b);
     }
 }
 
