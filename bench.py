@@ -504,6 +504,25 @@ def stage_breakdown(g, torch, stream):
     return out
 
 
+def profile_iteration(precision, prepare):
+    """The state after `prepare` iterations (plus 3 warm-up steps), then one
+    HFB iteration between cudaProfilerStart and cudaProfilerStop, for
+    `ncu --profile-from-start off` (launch lists and kernel captures)."""
+    import torch
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        _, g = _make(precision, 1234, stream=stream.cuda_stream)
+    if prepare > 0:
+        g.Evolve(prepare, DT, MOMENTUM)
+    g.Evolve(3, DT, MOMENTUM)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    g.Evolve(1, DT, MOMENTUM)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    g.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -515,7 +534,16 @@ def main():
     ap.add_argument("--breakdown", action="store_true")
     ap.add_argument("--no-micro", dest="micro", action="store_false",
                     help="skip the 32^3 mesh-kernel and 64^3 Poisson lines")
+    ap.add_argument("--profile-iteration", action="store_true",
+                    help="run one iteration of --precision between profiler start/stop "
+                         "(for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
+    if args.profile_iteration:
+        import __graft_entry__
+        __graft_entry__.build()
+        profile_iteration(args.precision, PREPARE)
+        print("profiled one iteration")
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
