@@ -29,6 +29,7 @@ void free_all(mg_ctx* c) {
     F(c->tc_erow);
     F(c->tc_status);
     F(c->gs_Stc); F(c->gs_xd); F(c->gs_xe); F(c->can_xd); F(c->can_xe); F(c->gap_part); F(c->fields_df);
+    F(c->field_y); F(c->field_xd); F(c->field_xe); F(c->field_ybase);
     for (int b = 0; b < 2; ++b) {
         Basis& B = c->bas[b];
         F(B.psi); F(B.der); F(B.lap); F(B.qn); F(B.occ); F(B.e); F(B.disp); F(B.jobs);

@@ -530,6 +530,39 @@ __global__ void k_gaps_sum(const double* __restrict__ gpart, const int* __restri
     if (lane == 0) gsum[(long)b * hmax * hmax + t] = s;
 }
 
+// Pairing field (HFBPairingField, src/HFB.f90:350-518) after the block apply
+// Y_i = sum_j Ktilde[j][i] psi_j (tensor cores): per point and block,
+//   Fr = sum_i sum_c Y_ic psi_ic,  Fi = sum_i (-Y_i0 psi_i1 + Y_i1 psi_i0
+//                                               - Y_i2 psi_i3 + Y_i3 psi_i2)
+// in double-float, as k_pair_field (pairing.cu) forms it; part[b][0|1][V].
+__global__ void __launch_bounds__(256)
+k_field_contract(const double* __restrict__ Y, const double* __restrict__ psi,
+                 const int* __restrict__ members, const int* __restrict__ hsz, int hmax, long V,
+                 double* __restrict__ part) {
+    const int b = blockIdx.y, h = hsz[b];
+    const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int i = 0; i < h; ++i) {
+        const double* y = Y + (long)(b * hmax + i) * 4 * V + v;
+        const double* p = psi + (long)members[b * hmax + i] * 4 * V + v;
+        dfl yy[4], pp[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            yy[c] = df_split(y[c * V]);
+            pp[c] = df_split(p[c * V]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) df_acc(rh, rl, yy[c], pp[c]);
+        df_acc(ih, il, yy[0], df_neg(pp[1]));
+        df_acc(ih, il, yy[1], pp[0]);
+        df_acc(ih, il, yy[2], df_neg(pp[3]));
+        df_acc(ih, il, yy[3], pp[2]);
+    }
+    part[((long)b * 2 + 0) * V + v] = df_to_fast(df_norm(dfl{rh, rl}));
+    part[((long)b * 2 + 1) * V + v] = df_to_fast(df_norm(dfl{ih, il}));
+}
+
 }  // namespace
 
 // Buffers and attributes of the tensor-core Gram-Schmidt (blocks of at most
@@ -625,6 +658,33 @@ int gaps_tc(mg_ctx* c, double* gsum) {
     MG_LAUNCHED(c);
     k_gaps_sum<<<dim3(div_up((long)H.hmax * H.hmax, 8), 4), 256, 0, c->stream>>>(
         c->gap_part, H.hsz, H.hmax, nchunk, gsum);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+// Pairing-field partials of the four blocks: Y = block apply of Ktilde
+// (tensor cores) into the scratch basis, then the pointwise contraction.
+int pair_field_tc(mg_ctx* c) {
+    Hfb& H = c->hfb;
+    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    const long V = c->V;
+    if (c->field_y == nullptr) {
+        MG_CUDA(cudaMalloc(&c->field_y, (size_t)4 * H.hmax * 4 * V * sizeof(double)));
+        MG_CUDA(cudaMalloc(&c->field_xd, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
+        MG_CUDA(cudaMemset(c->field_xd, 0, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
+        MG_CUDA(cudaMalloc(&c->field_xe, (size_t)4 * 64 * sizeof(int)));
+        MG_CUDA(cudaMalloc(&c->field_ybase, 4 * sizeof(int)));
+        const int yb[4] = {0, H.hmax, 2 * H.hmax, 3 * H.hmax};
+        MG_CUDA(cudaMemcpy(c->field_ybase, yb, sizeof(yb), cudaMemcpyHostToDevice));
+        MG_CUDA(cudaFuncSetAttribute(k_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+    }
+    const BlockIdx bi{nullptr, H.hsz, H.hmax};
+    MG_TRY(apply_tc(c, 4, H.hmax, H.ktil, (long)H.hmax * H.hmax, 0, bi,
+                    c->bas[MG_HF_BASIS].psi, c->field_y, nullptr, H.members, nullptr,
+                    c->field_ybase, c->field_xd, c->field_xe));
+    k_field_contract<<<dim3(div_up(V, 256), 4), 256, 0, c->stream>>>(
+        c->field_y, c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.hmax, V, H.fpart);
     MG_LAUNCHED(c);
     return MG_OK;
 }

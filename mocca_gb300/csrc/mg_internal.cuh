@@ -211,6 +211,10 @@ struct mg_ctx {
     uint16_t* can_xd = nullptr;   // digit planes of CanTransfo (tensor-core canonical basis)
     int* can_xe = nullptr;
     double* gap_part = nullptr;   // tensor-core gaps: partials per 64-point chunk
+    double* field_y = nullptr;    // tensor-core pairing field: Y = Psi Ktilde per block (4 hmax x 4V)
+    uint16_t* field_xd = nullptr;
+    int* field_xe = nullptr;
+    int* field_ybase = nullptr;   // first row of each block in field_y
 
     // Coulomb
     int mx, my, mz;
@@ -267,6 +271,7 @@ int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d
 int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const int* d_ordered);
 int can_transform_tc(mg_ctx* c);
 int gaps_tc(mg_ctx* c, double* gsum);
+int pair_field_tc(mg_ctx* c);
 int densities(mg_ctx* c);
 int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);

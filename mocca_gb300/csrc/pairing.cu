@@ -415,13 +415,15 @@ int pairing_mesh(mg_ctx* c) {
     MG_LAUNCHED(c);
     const size_t sm_f = (size_t)(hmax * hmax + hmax * 4 * kPts + 2 * kThreads) * sizeof(double);
     const bool mixed = c->cur_precision == MG_MIXED;
-    if (mixed)
+    if (mixed && c->tc_ok && hmax <= 64)
+        MG_TRY(pair_field_tc(c));   // tensor cores (meshgemm_tc.cu)
+    else if (mixed)
         k_pair_field_df<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
             B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
     else
         k_pair_field<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
             B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
-    MG_LAUNCHED(c);
+    if (!(mixed && c->tc_ok && hmax <= 64)) MG_LAUNCHED(c);
     k_pair_field_finish<<<div_up(2 * V, kThreads), kThreads, 0, c->stream>>>(H.fpart, H.dfac, V,
                                                                            H.fre, H.fim);
     MG_LAUNCHED(c);
