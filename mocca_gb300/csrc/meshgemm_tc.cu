@@ -535,15 +535,17 @@ __global__ void k_gaps_sum(const double* __restrict__ gpart, const int* __restri
 //   Fr = sum_i sum_c Y_ic psi_ic,  Fi = sum_i (-Y_i0 psi_i1 + Y_i1 psi_i0
 //                                               - Y_i2 psi_i3 + Y_i3 psi_i2)
 // in double-float, as k_pair_field (pairing.cu) forms it; part[b][0|1][V].
+// Four lanes per point (spinors i = sub, sub + 4, ...), combined by a fixed
+// shuffle order.
 __global__ void __launch_bounds__(256)
 k_field_contract(const double* __restrict__ Y, const double* __restrict__ psi,
                  const int* __restrict__ members, const int* __restrict__ hsz, int hmax, long V,
                  double* __restrict__ part) {
     const int b = blockIdx.y, h = hsz[b];
-    const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
+    const long v = (long)blockIdx.x * (blockDim.x / 4) + threadIdx.x / 4;
+    const int sub = threadIdx.x & 3;
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    for (int i = 0; i < h; ++i) {
+    for (int i = sub; i < h && v < V; i += 4) {
         const double* y = Y + (long)(b * hmax + i) * 4 * V + v;
         const double* p = psi + (long)members[b * hmax + i] * 4 * V + v;
         dfl yy[4], pp[4];
@@ -559,8 +561,18 @@ k_field_contract(const double* __restrict__ Y, const double* __restrict__ psi,
         df_acc(ih, il, yy[2], df_neg(pp[3]));
         df_acc(ih, il, yy[3], pp[2]);
     }
-    part[((long)b * 2 + 0) * V + v] = df_to_fast(df_norm(dfl{rh, rl}));
-    part[((long)b * 2 + 1) * V + v] = df_to_fast(df_norm(dfl{ih, il}));
+    dfl re = df_norm(dfl{rh, rl}), im = df_norm(dfl{ih, il});
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) {
+        re = df_add(re, dfl{__shfl_xor_sync(0xffffffffu, re.h, o),
+                            __shfl_xor_sync(0xffffffffu, re.l, o)});
+        im = df_add(im, dfl{__shfl_xor_sync(0xffffffffu, im.h, o),
+                            __shfl_xor_sync(0xffffffffu, im.l, o)});
+    }
+    if (sub == 0 && v < V) {
+        part[((long)b * 2 + 0) * V + v] = df_to_fast(re);
+        part[((long)b * 2 + 1) * V + v] = df_to_fast(im);
+    }
 }
 
 }  // namespace
@@ -683,7 +695,7 @@ int pair_field_tc(mg_ctx* c) {
     MG_TRY(apply_tc(c, 4, H.hmax, H.ktil, (long)H.hmax * H.hmax, 0, bi,
                     c->bas[MG_HF_BASIS].psi, c->field_y, nullptr, H.members, nullptr,
                     c->field_ybase, c->field_xd, c->field_xe));
-    k_field_contract<<<dim3(div_up(V, 256), 4), 256, 0, c->stream>>>(
+    k_field_contract<<<dim3(div_up(V, 64), 4), 256, 0, c->stream>>>(
         c->field_y, c->bas[MG_HF_BASIS].psi, H.members, H.hsz, H.hmax, V, H.fpart);
     MG_LAUNCHED(c);
     return MG_OK;
