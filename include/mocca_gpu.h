@@ -137,6 +137,8 @@ typedef struct mg_pairing_info {
     int    converged;         /* 1 when |N - N0| < FermiPrec for both       */
     double pairing_energy[2]; /* HFBEnergy with the new kappa               */
     double dispersion[2];     /* PairingDisp                                */
+    int    first_order;       /* 1 when rho and kappa took the last Newton  */
+                              /* step to first order (no new evaluation)    */
 } mg_pairing_info;
 
 /* ---- host-side helpers (no device work) ---------------------------------- */

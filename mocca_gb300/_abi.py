@@ -95,12 +95,14 @@ class MgPairingInfo(C.Structure):
     _fields_ = [
         ("fermi", C.c_double * 2), ("particles", C.c_double * 2), ("evaluations", C.c_int),
         ("converged", C.c_int), ("pairing_energy", C.c_double * 2), ("dispersion", C.c_double * 2),
+        ("first_order", C.c_int),
     ]
 
     def as_dict(self) -> dict:
         return {"fermi": list(self.fermi), "particles": list(self.particles),
                 "evaluations": self.evaluations, "converged": bool(self.converged),
-                "pairing_energy": list(self.pairing_energy), "dispersion": list(self.dispersion)}
+                "pairing_energy": list(self.pairing_energy), "dispersion": list(self.dispersion),
+                "first_order": bool(self.first_order)}
 
 
 class MgEnergyTerms(C.Structure):

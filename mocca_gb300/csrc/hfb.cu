@@ -559,6 +559,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     bracket(0);
     bracket(1);
     const int maxit = H.pp.max_iter > 0 ? H.pp.max_iter : 50;
+    bool first_order = false;
     for (int k = 0; k < maxit && !(conv[0] && conv[1]); ++k) {
         double dl[2] = {0.0, 0.0};
         bool newton[2] = {true, true};
@@ -581,11 +582,13 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         // ~N'' dl^2 / 2 (~1e-14 at this step), the same as an evaluation at
         // the new lambda would report; no eigen-decomposition is redone.
         bool taylor = true;
+        first_order = false;
         for (int it = 0; it < 2; ++it)
             taylor = taylor && (conv[it] || (newton[it] && std::fabs(dl[it]) <= kTaylorStep));
         if (taylor) {
             MG_TRY(taylor_finish(c, dl));
             ++H.taylor_steps;
+            first_order = true;
             for (int it = 0; it < 2; ++it) {
                 if (conv[it]) continue;
                 f[it] += fp[it] * dl[it];
@@ -657,6 +660,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         info->pairing_energy[1] = H.epair[1];
         info->dispersion[0] = H.disp[0];
         info->dispersion[1] = H.disp[1];
+        info->first_order = first_order ? 1 : 0;
     }
     if (hflags[3]) return MG_ERR_STATE;  // occupation above one (src/HFB.f90:3392-3395)
     if (lost) return MG_ERR_STATE;       // particle number lost 7 times (src/HFB.f90:2154-2158)

@@ -79,3 +79,31 @@ def test_hfb_iterations(built):
     assert abs(eg["total"] - eo["total"]) < 1e-8, (eg["total"], eo["total"])
     assert abs(sum(eg["pairing"]) - sum(eo["pairing"])) < 1e-8
     g.close()
+
+
+def test_hfb_iterations_first_order_finish(built):
+    """Iterations long enough for the Fermi search to finish its last Newton
+    step to first order (steps of at most 2e-7 MeV: rho and kappa move along
+    d rho / d lambda, d kappa / d lambda of the last evaluation) against the
+    oracle, whose Broyden search evaluates every step: 1e-8 MeV."""
+    p, g, o = _hfb_pair(seed=5)
+    g.Start()
+    o.Start()
+    pre, window = 30, 15
+    g.Evolve(pre, 0.010, 0.3)
+    used = 0
+    for _ in range(window):   # the steps of mg_iterate, one by one
+        g.GradDesc(0.010, 0.3)
+        used += g.SolvePairing()["first_order"]
+        g.DeriveAll()
+        g.lib.mg_hpsi(g.h, 1, None, None, None)
+        g.UpdateDensities()
+        g.MixDensities()
+        g.CalculateAllMoments()
+        g.ConstructPotentials()
+    eg = g.CompEnergy()
+    eo = o.Evolve(pre + window, 0.010, 0.3)
+    assert used > 0
+    assert abs(eg["total"] - eo["total"]) < 1e-8, (eg["total"], eo["total"])
+    assert abs(sum(eg["pairing"]) - sum(eo["pairing"])) < 1e-8
+    g.close()
