@@ -78,6 +78,9 @@ typedef struct mg_params {
                                   U update (src/PotentialMixing.f90:143-154) */
     double damping;            /* DampingParam, 0.75 (src/Densities.f90:17) */
     double precon_u;           /* preconu, 1.0 (src/Densities.f90:34) */
+    int    parameter_estimation; /* ParameterEstimation (src/GenInfo.f90:72): 1 re-estimates
+                                    dt and the momentum at every GradDesc
+                                    (IterativeEstimation, src/ImaginaryTime.f90:28-211) */
 } mg_params;
 
 /*
@@ -238,6 +241,10 @@ int mg_hpsi(mg_ctx* ctx, int basis, double* hpsi, double* e, double* disp);
 /* One GradDesc step on the HF basis (src/ImaginaryTime.f90:439-500), with
  * its Gram-Schmidt; dt in 1e-22 s as in &GenInfo. */
 int mg_grad_desc(mg_ctx* ctx, double dt, double momentum);
+/* dt and momentum in use: the GradDesc arguments, or with
+ * parameter_estimation = 1 the values of the last IterativeEstimation (the
+ * first GradDesc's arguments seed it). */
+int mg_get_step_parameters(mg_ctx* ctx, double* dt, double* momentum);
 
 /* Energy-ordered Gram-Schmidt of the HF basis (src/SpwfStorage.f90:372-480). */
 int mg_gram_schmidt(mg_ctx* ctx);

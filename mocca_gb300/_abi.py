@@ -47,6 +47,7 @@ class MgParams(C.Structure):
         ("mixing_scheme", C.c_int),
         ("damping", C.c_double),
         ("precon_u", C.c_double),
+        ("parameter_estimation", C.c_int),
     ]
 
 
@@ -157,6 +158,7 @@ SIGNATURES = {
     "mg_gram_schmidt": [_P],
     "mg_hf_fill": [_P],
     "mg_update_densities": [_P],
+    "mg_get_step_parameters": [_P, _D, _D],
     "mg_mix_densities": [_P],
     "mg_get_densities": [_P, _D, _D, _D, _D, _D],
     "mg_set_densities": [_P, _D, _D, _D, _D, _D],

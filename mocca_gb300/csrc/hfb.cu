@@ -209,6 +209,26 @@ __global__ void k_taylor_update(const double* __restrict__ Z, const double* __re
     Kp[(long)s * N + h + r] -= dl * dk;
 }
 
+// Quasiparticle energies moved with the same step: dE_m / d lambda =
+// -x_m^T Sigma x_m = 2 |y_m|^2 - 1 (y: lower half of the vector), so that the
+// spectrum left behind belongs to the final lambda, as an evaluation there
+// would report it (to O(dl^2)).
+__global__ void k_taylor_energies(const double* __restrict__ X, const int* __restrict__ hsz,
+                                  int nmax, long wstride, double dl0, double dl1,
+                                  double* __restrict__ w) {
+    const int b = blockIdx.y, h = hsz[b], N = 2 * h;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const double dl = b / 2 == 0 ? dl0 : dl1;
+    if (col >= N || dl == 0.0) return;
+    const double* Xb = X + (long)b * nmax * nmax;
+    double s = 0.0;
+    for (int r = h; r < N; ++r) {
+        const double y = Xb[(long)r * nmax + col];
+        s = fma(y, y, s);
+    }
+    w[(long)b * wstride + col] += dl * (2.0 * s - 1.0);
+}
+
 // rho_++ blocks into the eigensolver batch (leading dimension hmax); HF
 // occupations 2 rho_ii (HFBOccupations, src/HFB.f90:3519-3527)
 __global__ void k_copy_rpp(const double* __restrict__ rho, const int* __restrict__ hsz,
@@ -499,8 +519,8 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     return MG_OK;
 }
 
-// rho and kappa moved to lambda + dl from the eigen-decomposition of the last
-// evaluation (first order in dl).
+// rho, kappa and the quasiparticle energies moved to lambda + dl from the
+// eigen-decomposition of the last evaluation (first order in dl).
 static int taylor_finish(mg_ctx* c, const double dl[2]) {
     Hfb& H = c->hfb;
     const int hmax = H.hmax;
@@ -513,6 +533,9 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
     MG_TRY(gemm_batched(c, H.d_taylor + 20, 4, hmax));
     k_taylor_update<<<g, kThreads, 0, c->stream>>>(H.tZ, H.tK, H.hsz, hmax, H.nmax, dl[0], dl[1],
                                                   H.rho, H.kappa);
+    MG_LAUNCHED(c);
+    k_taylor_energies<<<dim3(div_up(H.nmax, 128), 4), 128, 0, c->stream>>>(
+        H.eT.X, H.hsz, H.nmax, H.eT.wstride, dl[0], dl[1], H.eT.w);
     MG_LAUNCHED(c);
     return MG_OK;
 }

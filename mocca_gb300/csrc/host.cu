@@ -30,6 +30,7 @@ void free_all(mg_ctx* c) {
     F(c->tc_status);
     F(c->gs_Stc); F(c->gs_xd); F(c->gs_xe); F(c->can_xd); F(c->can_xe); F(c->gap_part); F(c->fields_df);
     F(c->field_y); F(c->field_xd); F(c->field_xe); F(c->field_ybase);
+    F(c->est); F(c->est_jobs); F(c->est_qn);
     for (int b = 0; b < 2; ++b) {
         Basis& B = c->bas[b];
         F(B.psi); F(B.der); F(B.lap); F(B.qn); F(B.occ); F(B.e); F(B.disp); F(B.jobs);
@@ -137,7 +138,8 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     const bool full = !p->pc && !p->sc && !p->tsc;
     if (!ev8 && !full) return MG_ERR_ARG;
     if (p->precision != MG_FP64 && p->precision != MG_MIXED) return MG_ERR_ARG;
-    if ((p->mixing_scheme != 0 && p->mixing_scheme != 2) || !(p->damping >= 0.0) ||
+    if ((p->parameter_estimation != 0 && p->parameter_estimation != 1) ||
+        (p->mixing_scheme != 0 && p->mixing_scheme != 2) || !(p->damping >= 0.0) ||
         p->damping > 1.0)
         return MG_ERR_ARG;
     if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
@@ -395,8 +397,22 @@ extern "C" int mg_hpsi(mg_ctx* c, int b, double* hpsi, double* e, double* disp) 
 
 extern "C" int mg_grad_desc(mg_ctx* c, double dt, double momentum) {
     if (!c) return MG_ERR_ARG;
-    MG_TRY(hpsi_basis(c, MG_HF_BASIS, nullptr, true, dt / c->f.hbar, momentum));
+    if (!c->step_set || c->p.parameter_estimation != 1) {
+        c->step_dt = dt;
+        c->step_mom = momentum;
+        c->step_set = true;
+    }
+    // ParameterEstimation = 1: IterativeEstimation first (src/ImaginaryTime.f90:465)
+    if (c->p.parameter_estimation == 1) MG_TRY(estimate_parameters(c));
+    MG_TRY(hpsi_basis(c, MG_HF_BASIS, nullptr, true, c->step_dt / c->f.hbar, c->step_mom));
     return gram_schmidt_impl(c, c->updates);
+}
+
+extern "C" int mg_get_step_parameters(mg_ctx* c, double* dt, double* momentum) {
+    if (!c || !dt || !momentum) return MG_ERR_ARG;
+    *dt = c->step_dt;
+    *momentum = c->step_mom;
+    return MG_OK;
 }
 
 extern "C" int mg_gram_schmidt(mg_ctx* c) {

@@ -352,4 +352,22 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     return MG_OK;
 }
 
+// h.psi of one spinor outside the bases (FP64 kernel, FP64 derivatives), for
+// IterativeEstimation: out = h psi, e_dev[0] = <psi|h psi> dv.
+int hpsi_single(mg_ctx* c, double* psi, const double* der, const double* lap, const int* qn_dev,
+                double* out, double* e_dev) {
+    const long V = c->V;
+    const int nchunk = div_up(V, kThreads);
+    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW};
+    const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
+    const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
+    k_hpsi<false><<<dim3(nchunk, 1), kThreads, 0, c->stream>>>(psi, der, lap, qn_dev, F, out,
+                                                               nullptr, c->red, V, kin0, kin1,
+                                                               0.0, 0.0);
+    MG_LAUNCHED(c);
+    k_finish_energies<<<1, 128, 0, c->stream>>>(c->red, nchunk, 1, c->dv, e_dev, e_dev + 1);
+    MG_LAUNCHED(c);
+    return MG_OK;
+}
+
 }  // namespace mg

@@ -249,6 +249,16 @@ struct mg_ctx {
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
 
+    // IterativeEstimation (est.cu): the probe spinor maxspwf with its
+    // derivatives and update, its derivative jobs and quantum numbers, and the
+    // dt / momentum in use
+    double* est = nullptr;              // psi 4V, der 12V, lap 4V, hpsi 4V, update 4V, (e, disp)
+    mg::GridJob* est_jobs = nullptr;
+    int* est_qn = nullptr;
+    int est_iter = 0;
+    bool step_set = false;
+    double step_dt = 0.0, step_mom = 0.0;
+
     mg::Hfb hfb;
 };
 
@@ -264,6 +274,9 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs);
 int tc_check(mg_ctx* c);
 
 int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom);
+int hpsi_single(mg_ctx* c, double* psi, const double* der, const double* lap, const int* qn_dev,
+                double* out, double* e_dev);
+int estimate_parameters(mg_ctx* c);
 int gram_schmidt(mg_ctx* c);
 int gram_schmidt_impl(mg_ctx* c, double* upd);
 bool gs_tc_prepare(mg_ctx* c);

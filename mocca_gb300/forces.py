@@ -81,6 +81,7 @@ class RunParams:
     mixing_scheme: int = 0      # MixingScheme: 0 linear density mixing, 2 preconditioned U
     damping: float = 0.75       # DampingParam
     precon_u: float = 1.0       # preconu
+    parameter_estimation: int = 0   # ParameterEstimation: 1 estimates dt, momentum every step
     extra: dict = field(default_factory=dict)
 
     @property

@@ -182,6 +182,13 @@ class MeshState:
     def GradDesc(self, dt: float, momentum: float = 0.0):
         self._call("mg_grad_desc", C.c_double(dt), C.c_double(momentum))
 
+    def StepParameters(self) -> tuple[float, float]:
+        """(dt, momentum) of the last GradDesc: IterativeEstimation's estimate
+        (src/ImaginaryTime.f90:28-211) when ParameterEstimation = 1."""
+        dt, mom = C.c_double(), C.c_double()
+        self._call("mg_get_step_parameters", C.byref(dt), C.byref(mom))
+        return dt.value, mom.value
+
     def GramSchmidt(self):
         self._call("mg_gram_schmidt")
 

@@ -75,6 +75,13 @@ struct orc_ctx {
     double pdisp[2] = {0.0, 0.0};
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     int last_evals = 0;
+
+    // IterativeEstimation (src/ImaginaryTime.f90:28-211): maxspwf and the step
+    // parameters in use
+    Basis est;
+    int est_iter = 0;
+    bool step_set = false;
+    double step_dt = 0.0, step_mom = 0.0;
 };
 
 // --------------------------------------------------------------------------
@@ -497,13 +504,129 @@ extern "C" int orc_gram_schmidt(orc_ctx* c) {
 }
 
 // --------------------------------------------------------------------------
-// GradDesc, src/ImaginaryTime.f90:439-500 (ParameterEstimation = 0, no
-// InverseKineticDamping)
+// IterativeEstimation, src/ImaginaryTime.f90:28-211.  The reference fills
+// the start with an unseeded random_number; this restatement (like the GPU
+// path) uses a fixed-seed splitmix64 stream so that runs repeat.
+// --------------------------------------------------------------------------
+static double est_start_value(unsigned long long k) {
+    unsigned long long z = 0x2545F4914F6CDD1Dull + (k + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static void est_derive(orc_ctx* c) {
+    Basis& E = c->est;
+    const long V = c->V;
+    const int P = E.qn[1], S = E.qn[2], TS = E.qn[3];
+    for (int l = 0; l < 4; ++l) {
+        for (int d = 0; d < 3; ++d)
+            derive_grid(c, &E.psi[l * V], d, P, S, TS, l + 1, &E.der[(d * 4 + l) * V]);
+        derive_grid(c, &E.psi[l * V], 3, P, S, TS, l + 1, &E.lap[l * V]);
+    }
+}
+
+static int iterative_estimation(orc_ctx* c) {
+    Basis& B = c->bas[MG_HF_BASIS];
+    Basis& E = c->est;
+    const long V = c->V, V4 = 4 * V;
+    const int nwt = c->p.nwt;
+    ++c->est_iter;
+    if (c->est_iter == 1) {
+        // maxspwf = HFBasis(nwt) (HFBasis(nwn) without protons), random start
+        int iw = nwt - 1;
+        if (c->p.protons < 1e-9)
+            for (int i = 0; i < nwt; ++i)
+                if (B.qn[4 * i] == -1) iw = i;
+        E.qn.assign(B.qn.begin() + 4 * iw, B.qn.begin() + 4 * iw + 4);
+        E.psi.assign(V4, 0.0);
+        E.der.assign(12 * V, 0.0);
+        E.lap.assign(V4, 0.0);
+        double norm = 0.0;
+        for (long k = 0; k < V4; ++k) {
+            E.psi[k] = est_start_value((unsigned long long)k);
+            norm += E.psi[k] * E.psi[k];
+        }
+        const double sc = 1.0 / std::sqrt(norm * c->dv);
+        for (long k = 0; k < V4; ++k) E.psi[k] *= sc;
+        est_derive(c);
+    }
+    std::vector<double> up(V4, 0.0), h(V4);
+    const double fac = c->step_dt / c->f.hbar, mom = c->step_mom;
+    double maxE = 0.0, prev = NAN, con = NAN;
+    for (int it = 0; it < 500; ++it) {
+        hpsi_one(c, E, 0, h.data());
+        maxE = inprod_real(c, E.psi.data(), h.data());
+        con = prev - maxE;
+        prev = maxE;
+        double norm = 0.0;
+        for (long k = 0; k < V4; ++k) {
+            up[k] = fac * (h[k] - maxE * E.psi[k]) + mom * up[k];
+            E.psi[k] = E.psi[k] + up[k];
+            norm += E.psi[k] * E.psi[k];
+        }
+        const double sc = 1.0 / std::sqrt(norm * c->dv);
+        for (long k = 0; k < V4; ++k) E.psi[k] *= sc;
+        est_derive(c);
+        if (std::fabs(con) < 1e-2) break;
+    }
+    if (std::isnan(maxE)) return MG_ERR_NAN;
+    double relE = 10000.0;
+    if (c->p.pairing == MG_PAIRING_HFB && c->hfb_ready) {
+        // the columns the HFB solution keeps (HFBcolumns) carry the upper
+        // half of each block's ascending spectrum
+        for (int b = 0; b < 4; ++b) {
+            const size_t N = c->qe[b].size() / 2;
+            for (size_t k = N / 2; k < N; ++k)
+                if (c->qe[b][k] > 0.0) relE = std::min(relE, std::fabs(c->qe[b][k]));
+        }
+    } else {
+        for (int i = 0; i < nwt; ++i) {
+            if (std::fabs(B.occ[i]) < 0.5) continue;
+            for (int k = 0; k < nwt; ++k) {
+                if (std::fabs(B.occ[k]) > 0.5 || B.qn[4 * k] != B.qn[4 * i]) continue;
+                const double d = B.e[k] - B.e[i];
+                if (d > 0.0) relE = std::min(relE, d);
+            }
+        }
+        if (relE < 0.1) relE = 0.1;
+    }
+    double minh = 10000.0;
+    for (int i = 0; i < nwt; ++i) minh = std::min(minh, B.e[i]);
+    maxE -= minh;
+    const double kappa = relE / maxE;
+    c->step_mom = std::pow((std::sqrt(kappa) - 1.0) / (std::sqrt(kappa) + 1.0), 2.0);
+    c->step_dt = 4.0 / (maxE + relE + 2.0 * std::sqrt(maxE * relE)) * c->f.hbar * 0.90;
+    return MG_OK;
+}
+
+extern "C" int orc_get_step_parameters(orc_ctx* c, double* dt, double* momentum) {
+    if (!c || !dt || !momentum) return MG_ERR_ARG;
+    *dt = c->step_dt;
+    *momentum = c->step_mom;
+    return MG_OK;
+}
+
+// --------------------------------------------------------------------------
+// GradDesc, src/ImaginaryTime.f90:439-500 (no InverseKineticDamping), with
+// IterativeEstimation first when ParameterEstimation = 1 (:465)
 // --------------------------------------------------------------------------
 extern "C" int orc_grad_desc(orc_ctx* c, double dt, double momentum) {
     if (!c) return MG_ERR_ARG;
     Basis& B = c->bas[MG_HF_BASIS];
     const long V4 = 4 * c->V;
+    if (!c->step_set || c->p.parameter_estimation != 1) {
+        c->step_dt = dt;
+        c->step_mom = momentum;
+        c->step_set = true;
+    }
+    if (c->p.parameter_estimation == 1) {
+        const int st = iterative_estimation(c);
+        if (st != MG_OK) return st;
+    }
+    dt = c->step_dt;
+    momentum = c->step_mom;
     const double fac = dt / c->f.hbar;
     std::vector<double> h(V4);
     for (int i = 0; i < c->p.nwt; ++i) {
@@ -1721,7 +1844,8 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
     const bool hfb = c->p.pairing == MG_PAIRING_HFB;
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
-        orc_grad_desc(c, dt, momentum);
+        st = orc_grad_desc(c, dt, momentum);
+        if (st != MG_OK) return st;
         if (hfb) {
             const int sp = orc_solve_pairing(c, nullptr);
             if (sp < 0) return sp;

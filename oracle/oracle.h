@@ -52,6 +52,7 @@ int orc_derive_basis(orc_ctx* c, int basis);
 int orc_derive_all(orc_ctx* c);
 int orc_hpsi(orc_ctx* c, int basis, double* hpsi, double* e, double* disp);
 int orc_grad_desc(orc_ctx* c, double dt, double momentum);
+int orc_get_step_parameters(orc_ctx* c, double* dt, double* momentum);
 int orc_gram_schmidt(orc_ctx* c);
 int orc_hf_fill(orc_ctx* c);
 int orc_update_densities(orc_ctx* c);

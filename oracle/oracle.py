@@ -41,6 +41,7 @@ _SIG = {
     "orc_derive_all": ([_P], C.c_int),
     "orc_hpsi": ([_P, C.c_int, _D, _D, _D], C.c_int),
     "orc_grad_desc": ([_P, C.c_double, C.c_double], C.c_int),
+    "orc_get_step_parameters": ([_P, _D, _D], C.c_int),
     "orc_gram_schmidt": ([_P], C.c_int),
     "orc_hf_fill": ([_P], C.c_int),
     "orc_update_densities": ([_P], C.c_int),
@@ -221,6 +222,13 @@ class OracleState:
 
     def GradDesc(self, dt, momentum=0.0):
         self._call("orc_grad_desc", C.c_double(dt), C.c_double(momentum))
+
+    def StepParameters(self):
+        """(dt, momentum) of the last GradDesc: IterativeEstimation's when
+        ParameterEstimation = 1."""
+        dt, mom = C.c_double(), C.c_double()
+        self._call("orc_get_step_parameters", C.byref(dt), C.byref(mom))
+        return dt.value, mom.value
 
     def GramSchmidt(self):
         self._call("orc_gram_schmidt")

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from mocca_gb300 import SLY4, _abi
+from mocca_gb300 import SLY4, RunParams, _abi
 
 ROOT = Path(__file__).resolve().parents[1]
 
@@ -56,6 +56,11 @@ def test_invalid_arguments_are_rejected(built):
     assert lib.mg_lagrange_matrices(2, -1.0, 1, d.ctypes.data_as(_abi._D),
                                     d.ctypes.data_as(_abi._D)) == _abi.MG_ERR_ARG
     assert lib.mg_destroy(None) == _abi.MG_ERR_ARG
+    # ParameterEstimation takes 0 or 1; the check comes before any CUDA call
+    params = RunParams(nx=10, ny=10, nz=10, parameter_estimation=2).to_c()
+    ctx = C.c_void_p()
+    assert lib.mg_create(C.byref(params), SLY4.to_c(), None, C.byref(ctx)) == _abi.MG_ERR_ARG
+    assert not ctx.value
 
 
 def test_skyrme_coefficients_match_oracle(built):

@@ -178,3 +178,47 @@ def test_mix_densities_scheme0():
     mixed = o.get_densities()
     for k in mixed:
         np.testing.assert_allclose(mixed[k], 0.25 * new[k] + 0.75 * prev[k], rtol=0, atol=1e-14)
+
+
+def _hf_gap(occ, e, iso):
+    """relE of IterativeEstimation's HF branch (src/ImaginaryTime.f90:110-129)."""
+    rel_e = 10000.0
+    for i in range(len(e)):
+        if abs(occ[i]) < 0.5:
+            continue
+        for k in range(len(e)):
+            if abs(occ[k]) > 0.5 or iso[k] != iso[i]:
+                continue
+            if e[k] - e[i] > 0.0:
+                rel_e = min(rel_e, e[k] - e[i])
+    return max(rel_e, 0.1)
+
+
+def test_iterative_estimation_step_parameters():
+    """ParameterEstimation = 1 (src/ImaginaryTime.f90:28-211): the momentum
+    gives kappa = relE / (maxE - min e) back, and dt must then equal
+    0.9 * 4 hbar / (sqrt(maxE - min e) + sqrt(relE))^2 with relE the HF gap of
+    the energies the estimation saw; the largest eigenvalue of h on a 0.8 fm
+    mesh lies between 100 MeV and 5 GeV, and repeated runs agree bit for bit."""
+    p, psi, qn, en = _mg24()
+    p.parameter_estimation = 1
+    runs = []
+    for _ in range(2):
+        o = O.OracleState(p, SLY4)
+        o.set_spinors(psi, qn)
+        o.set_energies(en)
+        o.Start()
+        o.Evolve(1, 0.010, 0.3)
+        occ = o.get_occupations()
+        e, _ = o.get_energies()
+        o.GradDesc(0.010, 0.3)
+        runs.append(o.StepParameters())
+    assert runs[0] == runs[1]
+    dt, mom = runs[0]
+    assert 0.0 < mom < 1.0 and dt > 0.0
+    rel_e = _hf_gap(occ, e, qn[:, 0])
+    sk = (1.0 - math.sqrt(mom)) / (1.0 + math.sqrt(mom))
+    max_e = rel_e / sk ** 2
+    assert 100.0 < max_e + e.min() < 5000.0
+    want = 0.9 * 4.0 * SLY4.hbar / (math.sqrt(max_e) + math.sqrt(rel_e)) ** 2
+    assert dt == pytest.approx(want, rel=1e-12, abs=0)
