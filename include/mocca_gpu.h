@@ -287,9 +287,51 @@ int mg_get_hfb_block(mg_ctx* ctx, int b, double* rho, double* kappa, double* del
 /* Pairing field (real, imaginary) and DensityFactor, 2V each, may be NULL. */
 int mg_get_pairing_field(mg_ctx* ctx, double* re, double* im, double* dfac);
 
-/* Electric multipole moments of the densities needed by the Coulomb
- * boundary (Calculate_Multipole, src/Moments.f90:1907-2004). */
+/* Electric multipole moments of the densities (Calculate_Multipole,
+ * src/Moments.f90:1907-2004) for the Coulomb boundary.  With constraints
+ * this is CalculateAllMoments (src/Moments.f90:2250-2334): the density
+ * cutoff, the constrained moments' values and squares (the first call also
+ * sets each constraint's running target to the current value, :2277-2297)
+ * and the constraint field (CalcConstraintEnergy :2368-2486) that
+ * mg_construct_potentials adds to U (src/MeanFields.f90:403). */
 int mg_calculate_moments(mg_ctx* ctx);
+
+/* One constraint of &MomentConstraint (src/Moments.f90:3575-3790) of the
+ * kind the namelist defaults to: alternating-direction (ConstraintType = 2)
+ * on the neutron + proton value (Isoswitch = 1, Total = .false.) of Re Q_lm,
+ * with the density-dependent cutoff (CutoffType = 0, RutzCutOff
+ * :2703-2871, radd = 4 fm, acut = 0.4 fm) and Damping = 0.  EV8 meshes only
+ * (l and m even). */
+typedef struct mg_moment_constraint {
+    int    l, m;          /* the constrained moment Re Q_lm                      */
+    double constraint;    /* Constraint: target <Q_lm> (fm^l)                     */
+    double intensity;     /* Intensity; 0 = estimated on the first readjustment  */
+    int    iteration;     /* iteration: switched off once the Evolve iteration    */
+                          /* count exceeds it (<= 0: never), src/Moments.f90:3516 */
+} mg_moment_constraint;
+
+typedef struct mg_constraint_state {
+    double value[2];      /* Value: <Q_lm> of neutrons, protons                  */
+    double squared[2];    /* Squared: <Q_lm^2> (one-body part)                   */
+    double constraint;    /* Constraint(1): the readjusted target of the field   */
+    double intensity;     /* Intensity(1)                                        */
+    int    active;        /* ConstraintType /= 0 (not switched off yet)          */
+} mg_constraint_state;
+
+/* Adds a constraint (before the start, like the namelist read in
+ * CheckForRutzMoments); returns its index >= 0. */
+int mg_add_constraint(mg_ctx* ctx, const mg_moment_constraint* mc);
+int mg_get_constraint(mg_ctx* ctx, int k, mg_constraint_state* out);
+/* Cutoff(:,:,:,it) and ConstraintEnergy, 2V each, either may be NULL. */
+int mg_get_constraint_fields(mg_ctx* ctx, double* cutoff, double* field);
+/* AlternateStep (src/ImaginaryTime.f90:306-437, no cranking): the HF
+ * spinors take psi - multipole(it) psi, multipole(it) = sum over the
+ * alternating constraints of 0.5 (<Q> - target) / (<Q^2> + d0) Cutoff(it)
+ * Q_lm, then the energy-ordered Gram-Schmidt. */
+int mg_alternate_step(mg_ctx* ctx);
+/* ReadjustAllMoments (src/Moments.f90:2336-2366, alternating branch of
+ * Readjust :2994-3058) then TurnOffConstraints(iteration) (:3516-3550). */
+int mg_readjust_moments(mg_ctx* ctx, int iteration);
 
 /* Coulomb solve (src/Coulomb.f90:255-346): multipole boundary, CG, Slater
  * exchange.  iters may be NULL.  Returns MG_NOT_CONVERGED when the CG hits
@@ -309,7 +351,11 @@ int mg_set_potentials(mg_ctx* ctx, const double* u, const double* b,
 int mg_energy(mg_ctx* ctx, mg_energy_terms* out);
 
 /* n_iter passes of the Evolve loop body (src/Main.f90:255-328) with fixed
- * dt and momentum; out (may be NULL) receives the last iteration's energy. */
+ * dt and momentum; out (may be NULL) receives the last iteration's energy.
+ * With constraints each pass also takes the AlternateStep first (while an
+ * alternating constraint was active at the previous pass's check, :261-274)
+ * and readjusts the constraints after the moments (:298-304); the context
+ * numbers the passes from 1 across calls for TurnOffConstraints. */
 int mg_iterate(mg_ctx* ctx, int n_iter, double dt, double momentum,
                mg_energy_terms* out);
 

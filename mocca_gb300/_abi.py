@@ -131,6 +131,21 @@ class MgEnergyTerms(C.Structure):
         }
 
 
+class MgMomentConstraint(C.Structure):
+    _fields_ = [("l", C.c_int), ("m", C.c_int), ("constraint", C.c_double),
+                ("intensity", C.c_double), ("iteration", C.c_int)]
+
+
+class MgConstraintState(C.Structure):
+    _fields_ = [("value", C.c_double * 2), ("squared", C.c_double * 2),
+                ("constraint", C.c_double), ("intensity", C.c_double), ("active", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {"value": list(self.value), "squared": list(self.squared),
+                "constraint": self.constraint, "intensity": self.intensity,
+                "active": bool(self.active)}
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -163,6 +178,11 @@ SIGNATURES = {
     "mg_get_densities": [_P, _D, _D, _D, _D, _D],
     "mg_set_densities": [_P, _D, _D, _D, _D, _D],
     "mg_calculate_moments": [_P],
+    "mg_add_constraint": [_P, C.POINTER(MgMomentConstraint)],
+    "mg_get_constraint": [_P, C.c_int, C.POINTER(MgConstraintState)],
+    "mg_get_constraint_fields": [_P, _D, _D],
+    "mg_alternate_step": [_P],
+    "mg_readjust_moments": [_P, C.c_int],
     "mg_solve_coulomb": [_P, _I],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],

@@ -318,9 +318,11 @@ void axis_eigen(int n, std::vector<double>& C, std::vector<double>& mu) {
     for (int i = 0; i < n; ++i) mu[i] = A[(size_t)i * n + i];
 }
 
+}  // namespace
+
 // ---- host-side restatement of the spherical harmonics of the moments -----
 // legendre_pnm src/Mesh.f90:96-262; SphericalHarmonics src/Moments.f90:584-691
-void legendre(int n, int m, double x, double* cx) {
+static void legendre(int n, int m, double x, double* cx) {
     for (int i = 0; i < m; ++i) cx[i] = 0.0;
     cx[m] = 1.0;
     const double somx2 = std::sqrt(1.0 - x * x);
@@ -332,7 +334,7 @@ void legendre(int n, int m, double x, double* cx) {
         cx[i] = (double(2 * i - 1) * x * cx[i - 1] - double(i + m - 1) * cx[i - 2]) / double(i - m);
 }
 
-double ipow(double x, int n) {
+static double ipow(double x, int n) {
     double r = 1.0;
     for (int i = 0; i < n; ++i) r *= x;
     return r;
@@ -351,8 +353,6 @@ double rlylm(int l, int m, int im, double X, double Y, double Z) {
     const double phi = std::atan2(Y, X);
     return fac * leg[l] * (im ? std::sin(m * phi) : std::cos(m * phi));
 }
-
-}  // namespace
 
 // Moment table (IniMoments, src/Moments.f90:372-582; EV8 selection of
 // NewMoment_Electric), spherical harmonics on the stored and extended

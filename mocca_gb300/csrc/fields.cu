@@ -10,7 +10,8 @@
 // One thread per mesh point computes U, B and the nine W components of both
 // isospins; the derivatives go through the Lagrange job kernels.
 // Moments: Calculate_Multipole (src/Moments.f90:1907-1966) for the electric
-// moments the Coulomb boundary uses.
+// moments the Coulomb boundary uses; the constrained moments, the cutoff and
+// the constraint field (added to U here) come from constraints.cu.
 #include <cmath>
 
 #include "mg_internal.cuh"
@@ -37,7 +38,8 @@ __global__ void __launch_bounds__(kThreads)
 k_potentials(const double* __restrict__ rho, const double* __restrict__ tau,
              const double* __restrict__ nablaj, const double* __restrict__ derrho,
              const double* __restrict__ laprho, const double* __restrict__ coul,
-             const double* __restrict__ coulex, Coef B, long V, double* __restrict__ U,
+             const double* __restrict__ coulex, const double* __restrict__ cons, Coef B, long V,
+             double* __restrict__ U,
              double* __restrict__ Bp, double* __restrict__ W) {
     const long v = (long)blockIdx.x * kThreads + threadIdx.x;
     if (v >= V) return;
@@ -67,6 +69,10 @@ k_potentials(const double* __restrict__ rho, const double* __restrict__ tau,
     }
     u[1] = u[1] + coul[v];
     if (B.cexchange == 2) u[1] = u[1] + coulex[v];
+    if (cons) {   // U = U + ConstraintEnergy (src/MeanFields.f90:403)
+        u[0] = u[0] + cons[v];
+        u[1] = u[1] + cons[V + v];
+    }
     U[v] = u[0];
     U[V + v] = u[1];
     for (int it = 0; it < 2; ++it) {
@@ -175,8 +181,8 @@ int potentials(mg_ctx* c) {
     Coef k{c->B.B1, c->B.B2, c->B.B3, c->B.B4, c->B.B5, c->B.B6, c->B.B7a, c->B.B7b, c->B.B8a,
            c->B.B8b, c->B.byt3a, c->B.byt3b, c->B.B9, c->B.B9q, c->f.cexchange};
     k_potentials<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(
-        c->rho, c->tau, c->nablaj, c->derrho, c->laprho, c->coulomb, c->coulex, k, V, c->U, c->Bp,
-        c->W);
+        c->rho, c->tau, c->nablaj, c->derrho, c->laprho, c->coulomb, c->coulex,
+        c->cons.list.empty() ? nullptr : c->cons.field, k, V, c->U, c->Bp, c->W);
     MG_LAUNCHED(c);
     MG_TRY(run_jobs(c, c->field_jobs + 2, c->n_field_jobs - 2));
     k_sum3<<<div_up(6 * V, kThreads), kThreads, 0, c->stream>>>(c->divw_tmp, 6 * V, c->divW);
@@ -185,11 +191,12 @@ int potentials(mg_ctx* c) {
 }
 
 int moments(mg_ctx* c) {
-    if (c->n_moments == 0) return MG_OK;
-    k_moments<<<c->n_moments, kThreads, 0, c->stream>>>(c->sh_mesh, c->rho, c->V, c->dv,
-                                                        c->moment_values);
-    MG_LAUNCHED(c);
-    return MG_OK;
+    if (c->n_moments > 0) {
+        k_moments<<<c->n_moments, kThreads, 0, c->stream>>>(c->sh_mesh, c->rho, c->V, c->dv,
+                                                            c->moment_values);
+        MG_LAUNCHED(c);
+    }
+    return constraint_moments(c);   // constraints.cu (nothing without constraints)
 }
 
 }  // namespace mg

@@ -44,6 +44,7 @@ void free_all(mg_ctx* c) {
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast);
     F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
     hfb_free(c);
+    constraints_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -614,6 +615,10 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
     const bool hfb = c->p.pairing == MG_PAIRING_HFB;
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
+        ++c->iteration;
+        // AlternateStep while an alternating constraint was active at the
+        // last check (src/Main.f90:261-263)
+        if (c->cons.alternate_check) MG_TRY(alternate_step(c));
         MG_TRY(mg_grad_desc(c, dt, momentum));
         if (hfb) {
             // DeriveAll of the HF basis needs only the new HF spinors: it runs
@@ -634,6 +639,7 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
             MG_TRY(mg_hf_fill(c));
             MG_TRY(mg_derive_all(c));
         }
+        c->cons.alternate_check = any_alternating(c);   // src/Main.f90:274
         // canonical single-particle energies with the previous potentials
         // (src/Main.f90:282-289)
         if (hfb) MG_TRY(hpsi_basis(c, MG_CAN_BASIS, nullptr, false, 0.0, 0.0));
@@ -641,6 +647,7 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         MG_TRY(densities(c));
         MG_TRY(mix_densities(c));
         MG_TRY(moments(c));
+        readjust_moments(c, c->iteration);   // src/Main.f90:299-304
         st = mg_construct_potentials(c, nullptr);
         if (st < 0) return st;
         if (out) MG_TRY(energy(c, out));

@@ -151,6 +151,35 @@ struct Hfb {
     int nref = 2;             // FP64 refinement steps per eigen-decomposition
 };
 
+// One multipole constraint of the alternating kind (constraints.cu): the
+// fields of the reference's Moment type that it uses.
+struct MomentConstraint {
+    int l = 0, m = 0;
+    int type = 2;               // 2 alternating, 0 switched off
+    int iteration = -1;         // last Evolve iteration with the constraint (<= 0: all)
+    double constraint = 0.0;    // running target of the constraint field
+    double true_constraint = 0.0;
+    double intensity = 0.0;     // 0: estimated on the first readjustment
+    double value[2] = {0.0, 0.0}, squared[2] = {0.0, 0.0};
+    bool started = false;       // moments computed once (running target set)
+};
+
+constexpr int kMaxConstraints = 8;
+
+struct Constraints {
+    std::vector<MomentConstraint> list;
+    double* sh = nullptr;       // [kMaxConstraints][V] r^l Y_lm on the stored mesh
+    double* cut = nullptr;      // [2][V] density cutoff
+    double* field = nullptr;    // [2][V] constraint field added to U
+    double* surf = nullptr;     // [2][3][cap] surface points of the cutoff
+    long cap = 0;
+    double* stat = nullptr;     // [2][2]: threshold, dv * sum rho
+    int* count = nullptr;       // [2] surface points found
+    double* red = nullptr;      // [kMaxConstraints][4]: value[2], squared[2]
+    double* h_red = nullptr;    // pinned host copy of red
+    bool alternate_check = false;
+};
+
 }  // namespace mg
 
 struct mg_ctx {
@@ -260,6 +289,10 @@ struct mg_ctx {
     double step_dt = 0.0, step_mom = 0.0;
 
     mg::Hfb hfb;
+
+    // multipole constraints (constraints.cu) and the Evolve iteration count
+    mg::Constraints cons;
+    int iteration = 0;
 };
 
 namespace mg {
@@ -311,6 +344,13 @@ int mixing_setup(mg_ctx* c);
 int save_density_history(mg_ctx* c);
 int mix_densities(mg_ctx* c);
 int precondition_u(mg_ctx* c);
+double rlylm(int l, int m, int im, double X, double Y, double Z);
+int add_constraint(mg_ctx* c, const mg_moment_constraint* mc);
+int constraint_moments(mg_ctx* c);
+int alternate_step(mg_ctx* c);
+void readjust_moments(mg_ctx* c, int iteration);
+bool any_alternating(const mg_ctx* c);
+void constraints_free(mg_ctx* c);
 
 // Lagrange matrix slot selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8.
 __host__ __device__ inline int lag_slot(int dir, int P, int S, int TS, int comp) {

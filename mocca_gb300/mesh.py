@@ -204,6 +204,31 @@ class MeshState:
     def CalculateAllMoments(self):
         self._call("mg_calculate_moments")
 
+    def add_constraint(self, l: int, m: int, constraint: float, intensity: float = 0.0,
+                       iteration: int = -1) -> int:
+        """&MomentConstraint l, m, Constraint, Intensity, iteration (alternating kind)."""
+        mc = _abi.MgMomentConstraint(l, m, constraint, intensity, iteration)
+        k = self.lib.mg_add_constraint(self.h, C.byref(mc))
+        if k < 0:
+            raise _abi.MgError("mg_add_constraint", k)
+        return k
+
+    def get_constraint(self, k: int = 0) -> dict:
+        st = _abi.MgConstraintState()
+        self._call("mg_get_constraint", int(k), C.byref(st))
+        return st.as_dict()
+
+    def get_constraint_fields(self):
+        cut, fld = np.empty(2 * self.V), np.empty(2 * self.V)
+        self._call("mg_get_constraint_fields", _dptr(cut), _dptr(fld))
+        return cut, fld
+
+    def AlternateStep(self):
+        self._call("mg_alternate_step")
+
+    def ReadjustAllMoments(self, iteration: int):
+        self._call("mg_readjust_moments", int(iteration))
+
     def SolveCoulomb(self) -> int:
         it = C.c_int(0)
         self._call("mg_solve_coulomb", C.byref(it), allow_not_converged=True)

@@ -31,6 +31,20 @@ struct Moment {  // one electric multipole moment (src/Moments.f90:372-582)
     double value[2] = {0.0, 0.0};
 };
 
+// One constrained moment: the fields of type Moment that the alternating
+// (ConstraintType 2), isoscalar (Isoswitch 1), non-total constraint uses
+// (src/Moments.f90:146-200).
+struct Constraint {
+    int l, m, mom;              // mom: index in orc_ctx::moments
+    int type = 2;               // ConstraintType; TurnOffConstraints sets 0
+    int iteration = -1;         // last iteration with the constraint
+    double constraint = 0.0;    // Constraint(1): the readjusted target
+    double true_constraint = 0.0;
+    double intensity = 0.0;     // Intensity(1); 0 = estimate on first Readjust
+    double value[2] = {0.0, 0.0}, squared[2] = {0.0, 0.0};
+    bool started = false;       // first CalculateAllMoments seen (src/Moments.f90:2277)
+};
+
 }  // namespace
 
 struct orc_ctx {
@@ -82,6 +96,15 @@ struct orc_ctx {
     int est_iter = 0;
     bool step_set = false;
     double step_dt = 0.0, step_mom = 0.0;
+
+    // Multipole constraints (src/Moments.f90:146-200, :2250-2531, :2929-3058)
+    // with the Rutz cutoff (:2703-2871) and the alternate step
+    // (src/ImaginaryTime.f90:306-437); the Evolve iteration counter of
+    // TurnOffConstraints (src/Main.f90:256-304)
+    std::vector<Constraint> cons;
+    std::vector<double> cutoff, cons_energy;   // Cutoff(:,:,:,it), ConstraintEnergy
+    bool alternate_check = false;              // AlternateCheck, src/Main.f90:247, :274
+    int iteration = 0;
 };
 
 // --------------------------------------------------------------------------
@@ -840,16 +863,217 @@ static void init_moments(orc_ctx* c) {
             }
 }
 
+// --------------------------------------------------------------------------
+// Multipole constraints: alternating-direction kind (ConstraintType 2, the
+// &MomentConstraint default), Isoswitch 1, Total false, CutoffType 0,
+// Damping 0 (src/Moments.f90:258, :280).
+// --------------------------------------------------------------------------
+static const double kRadd = 4.0, kAcut = 0.4;  // src/Moments.f90:258
+// d0 = 0.1 is a default-kind (single precision) literal assigned to a
+// real(dp) variable (src/Moments.f90:258): its value is 0.1f widened.
+static const double kD0 = (double)0.1f;
+
+// RutzCutOff, src/Moments.f90:2703-2871: distance DeltaR from each mesh
+// point to the surface rho = max(rho)/10 (linear interpolation between
+// neighbours of the stored box, negative inside), then
+// Cutoff = 1 / (1 + exp((DeltaR - radd) / acut)).
+static void rutz_cutoff(orc_ctx* c) {
+    const long V = c->V;
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const double dx = c->dx;
+    c->cutoff.assign(2 * V, 0.0);
+    auto mesh = [&](int i) { return dx / 2.0 + dx * i; };   // src/Mesh.f90:50
+    for (int it = 0; it < 2; ++it) {
+        const double* r = &c->rho[it * V];
+        double s = 0.0;
+        for (long v = 0; v < V; ++v) s += r[v];
+        if (c->dv * s < 0.0000000001) continue;   // no particles: Cutoff = 0
+        double mx = r[0];
+        for (long v = 1; v < V; ++v) mx = std::max(mx, r[v]);
+        const double tr = mx / 10.0;
+        auto R = [&](int i, int j, int k) { return r[i + (long)nx * (j + (long)ny * k)]; };
+        std::vector<double> sx, sy, sz;
+        for (int k = 0; k < nz - 1; ++k)
+            for (int j = 0; j < ny - 1; ++j)
+                for (int i = 0; i < nx - 1; ++i) {
+                    const double X = mesh(i), Y = mesh(j), Z = mesh(k);
+                    const double r0 = R(i, j, k);
+                    const double rx = R(i + 1, j, k), ry = R(i, j + 1, k), rz = R(i, j, k + 1);
+                    if ((r0 >= tr && rx <= tr) || (r0 <= tr && rx >= tr)) {
+                        sx.push_back(X + dx * (tr - r0) / (rx - r0)); sy.push_back(Y); sz.push_back(Z);
+                    }
+                    if ((r0 >= tr && ry <= tr) || (r0 <= tr && ry >= tr)) {
+                        sx.push_back(X); sy.push_back(Y + dx * (tr - r0) / (ry - r0)); sz.push_back(Z);
+                    }
+                    if ((r0 >= tr && rz <= tr) || (r0 <= tr && rz >= tr)) {
+                        sx.push_back(X); sy.push_back(Y); sz.push_back(Z + dx * (tr - r0) / (rz - r0));
+                    }
+                }
+        const size_t T = sx.size();
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const double X = mesh(i), Y = mesh(j), Z = mesh(k);
+                    double d = 1.0e12;
+                    for (size_t l = 0; l < T; ++l) {
+                        const double a = X - sx[l], b = Y - sy[l], e = Z - sz[l];
+                        d = std::min(d, a * a + b * b + e * e);
+                    }
+                    const long v = i + (long)nx * (j + (long)ny * k);
+                    const double sig = r[v] > tr ? -1.0 : 1.0;
+                    const double delta = sig * std::sqrt(d);
+                    c->cutoff[it * V + v] = 1.0 / (1.0 + std::exp((delta - kRadd) / kAcut));
+                }
+    }
+}
+
+// CalcConstraintEnergy, src/Moments.f90:2368-2486 (alternating constraints,
+// Isoswitch 1, not Total; Damping 0 so the old field is dropped):
+// ConstraintEnergy(it) += 2 I (<Q> - C) Q_lm Cutoff(it).
+static void calc_constraint_energy(orc_ctx* c) {
+    const long V = c->V;
+    c->cons_energy.assign(2 * V, 0.0);
+    for (const Constraint& k : c->cons) {
+        if (k.type != 2) continue;
+        const double factor = 2.0 * k.intensity;
+        const double value = k.value[0] + k.value[1];
+        const double a = factor * (value - k.constraint);
+        const std::vector<double>& sh = c->moments[k.mom].sh;
+        for (int it = 0; it < 2; ++it)
+            for (long v = 0; v < V; ++v)
+                c->cons_energy[it * V + v] += a * sh[v] * c->cutoff[it * V + v];
+    }
+}
+
+// Readjust (alternating branch), src/Moments.f90:2994-3058, over the
+// constrained moments as ReadjustAllMoments :2336-2366; then
+// TurnOffConstraints :3516-3550.
+static void readjust_moments(orc_ctx* c, int iteration) {
+    for (Constraint& k : c->cons) {
+        if (k.type != 2) continue;
+        if (k.intensity == 0.0) {
+            k.intensity = 2.0 / (k.squared[0] + k.squared[1]);
+            if (c->step_mom != 0.0) k.intensity = 0.5 * k.intensity;
+        }
+        k.constraint = k.constraint - ((k.value[0] + k.value[1]) - k.true_constraint);
+    }
+    for (Constraint& k : c->cons)
+        if (k.type != 0 && k.iteration > 0 && iteration > k.iteration) k.type = 0;
+}
+
+static bool any_alternating(const orc_ctx* c) {   // CheckForAlternateConstraints
+    for (const Constraint& k : c->cons)
+        if (k.type == 2) return true;
+    return false;
+}
+
+// CalculateAllMoments, src/Moments.f90:2250-2334 (electric moments): the
+// cutoff, every moment's value (Calculate_Multipole :1907-1966) and, for the
+// constrained ones, the squares; the first call sets each constraint's
+// running target to the current value (:2277-2297); then the constraint
+// field.
 extern "C" int orc_calculate_moments(orc_ctx* c) {
     if (!c) return MG_ERR_ARG;
     if (c->moments.empty()) init_moments(c);
+    if (!c->cons.empty()) rutz_cutoff(c);
     for (Moment& mo : c->moments)
         for (int it = 0; it < 2; ++it) {
             double s = 0.0;
             for (long v = 0; v < c->V; ++v) s += mo.sh[v] * c->rho[it * c->V + v];
             mo.value[it] = s * c->dv;
         }
+    if (c->cons.empty()) return MG_OK;
+    for (Constraint& k : c->cons) {
+        const std::vector<double>& sh = c->moments[k.mom].sh;
+        for (int it = 0; it < 2; ++it) {
+            double s = 0.0;
+            for (long v = 0; v < c->V; ++v) s += sh[v] * sh[v] * c->rho[it * c->V + v];
+            k.value[it] = c->moments[k.mom].value[it];
+            k.squared[it] = s * c->dv;
+        }
+        if (!k.started && k.type != 0) k.constraint = k.value[0] + k.value[1];
+        k.started = true;
+    }
+    calc_constraint_energy(c);
     return MG_OK;
+}
+
+extern "C" int orc_add_constraint(orc_ctx* c, const mg_moment_constraint* mc) {
+    if (!c || !mc || !c->folded || mc->l < 1) return MG_ERR_ARG;
+    if (c->moments.empty()) init_moments(c);
+    int mom = -1;
+    for (size_t q = 0; q < c->moments.size(); ++q)
+        if (c->moments[q].l == mc->l && c->moments[q].m == mc->m && c->moments[q].im == 0)
+            mom = (int)q;
+    if (mom < 0) return MG_ERR_ARG;
+    Constraint k;
+    k.l = mc->l; k.m = mc->m; k.mom = mom;
+    k.iteration = mc->iteration;
+    k.constraint = k.true_constraint = mc->constraint;   // src/Moments.f90:3719-3726
+    k.intensity = mc->intensity;
+    c->cons.push_back(k);
+    c->alternate_check = true;
+    if (c->cutoff.empty()) c->cutoff.assign(2 * c->V, 0.0);
+    if (c->cons_energy.empty()) c->cons_energy.assign(2 * c->V, 0.0);
+    return (int)c->cons.size() - 1;
+}
+
+extern "C" int orc_get_constraint(orc_ctx* c, int q, mg_constraint_state* out) {
+    if (!c || !out || q < 0 || q >= (int)c->cons.size()) return MG_ERR_ARG;
+    const Constraint& k = c->cons[q];
+    for (int it = 0; it < 2; ++it) { out->value[it] = k.value[it]; out->squared[it] = k.squared[it]; }
+    out->constraint = k.constraint;
+    out->intensity = k.intensity;
+    out->active = k.type != 0;
+    return MG_OK;
+}
+
+extern "C" int orc_get_constraint_fields(orc_ctx* c, double* cutoff, double* field) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    for (long v = 0; v < 2 * V; ++v) {
+        if (cutoff) cutoff[v] = c->cutoff.empty() ? 0.0 : c->cutoff[v];
+        if (field) field[v] = c->cons_energy.empty() ? 0.0 : c->cons_energy[v];
+    }
+    return MG_OK;
+}
+
+extern "C" int orc_readjust_moments(orc_ctx* c, int iteration) {
+    if (!c) return MG_ERR_ARG;
+    readjust_moments(c, iteration);
+    return MG_OK;
+}
+
+// AlternateStep, src/ImaginaryTime.f90:306-437 (no cranking):
+// psi <- psi - multipole(it) psi with
+// multipole(it) = sum 0.5 (<Q> - Q_target) / (<Q^2> + d0) Cutoff(it) Q_lm
+// over the alternating constraints, then GramSchmidt.
+extern "C" int orc_alternate_step(orc_ctx* c) {
+    if (!c) return MG_ERR_ARG;
+    const long V = c->V;
+    if (!c->cons.empty()) rutz_cutoff(c);
+    std::vector<double> mp(2 * V, 0.0);
+    bool any = false;
+    for (const Constraint& k : c->cons) {
+        if (k.type != 2) continue;
+        any = true;
+        const double o2 = k.squared[0] + k.squared[1];
+        const double value = k.value[0] + k.value[1];
+        const double f = 0.5 * (value - k.true_constraint) / (o2 + kD0);
+        const std::vector<double>& sh = c->moments[k.mom].sh;
+        for (int it = 0; it < 2; ++it)
+            for (long v = 0; v < V; ++v) mp[it * V + v] += f * c->cutoff[it * V + v] * sh[v];
+    }
+    if (any) {
+        Basis& B = c->bas[MG_HF_BASIS];
+        for (int i = 0; i < c->p.nwt; ++i) {
+            const int it = (B.qn[4 * i] + 3) / 2 - 1;
+            double* p = &B.psi[(long)i * 4 * V];
+            for (int l = 0; l < 4; ++l)
+                for (long v = 0; v < V; ++v) p[l * V + v] = p[l * V + v] - mp[it * V + v] * p[l * V + v];
+        }
+    }
+    return orc_gram_schmidt(c);
 }
 
 extern "C" int orc_get_moments(orc_ctx* c, double* values, int* lm, int max_count) {
@@ -1029,6 +1253,11 @@ static void calc_potentials(orc_ctx* c) {
         }
         u[1] = u[1] + c->coulomb[v];
         if (c->f.cexchange == 2) u[1] = u[1] + c->coulex[v];
+        // U = U + ConstraintEnergy (src/MeanFields.f90:403)
+        if (!c->cons_energy.empty()) {
+            u[0] = u[0] + c->cons_energy[v];
+            u[1] = u[1] + c->cons_energy[V + v];
+        }
         c->U[v] = u[0];
         c->U[V + v] = u[1];
     }
@@ -1844,6 +2073,8 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
     const bool hfb = c->p.pairing == MG_PAIRING_HFB;
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
+        ++c->iteration;
+        if (c->alternate_check) orc_alternate_step(c);   // src/Main.f90:261-263
         st = orc_grad_desc(c, dt, momentum);
         if (st != MG_OK) return st;
         if (hfb) {
@@ -1852,12 +2083,14 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
         } else {
             orc_hf_fill(c);
         }
+        c->alternate_check = any_alternating(c);           // src/Main.f90:274
         orc_derive_all(c);
         if (hfb) orc_hpsi(c, MG_CAN_BASIS, nullptr, c->bas[MG_CAN_BASIS].e.data(),
                           c->bas[MG_CAN_BASIS].disp.data());
         orc_update_densities(c);
         orc_mix_densities(c);
         orc_calculate_moments(c);
+        readjust_moments(c, c->iteration);                  // src/Main.f90:299-304
         st = orc_construct_potentials(c, nullptr);
         if (st < 0) return st;
         if (out) orc_energy(c, out);

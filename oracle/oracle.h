@@ -64,6 +64,12 @@ int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
                       const double* laprho);
 int orc_calculate_moments(orc_ctx* c);
 int orc_get_moments(orc_ctx* c, double* values, int* lm, int max_count);
+/* multipole constraints (alternating kind), as mg_add_constraint & co. */
+int orc_add_constraint(orc_ctx* c, const mg_moment_constraint* mc);
+int orc_get_constraint(orc_ctx* c, int k, mg_constraint_state* out);
+int orc_get_constraint_fields(orc_ctx* c, double* cutoff, double* field);
+int orc_alternate_step(orc_ctx* c);
+int orc_readjust_moments(orc_ctx* c, int iteration);
 int orc_solve_coulomb(orc_ctx* c, int* iters);
 int orc_construct_potentials(orc_ctx* c, int* iters);
 int orc_get_potentials(orc_ctx* c, double* u, double* b, double* nablab,

@@ -50,6 +50,11 @@ _SIG = {
     "orc_set_densities": ([_P, _D, _D, _D, _D, _D], C.c_int),
     "orc_calculate_moments": ([_P], C.c_int),
     "orc_get_moments": ([_P, _D, _I, C.c_int], C.c_int),
+    "orc_add_constraint": ([_P, C.POINTER(_abi.MgMomentConstraint)], C.c_int),
+    "orc_get_constraint": ([_P, C.c_int, C.POINTER(_abi.MgConstraintState)], C.c_int),
+    "orc_get_constraint_fields": ([_P, _D, _D], C.c_int),
+    "orc_alternate_step": ([_P], C.c_int),
+    "orc_readjust_moments": ([_P, C.c_int], C.c_int),
     "orc_solve_coulomb": ([_P, _I], C.c_int),
     "orc_construct_potentials": ([_P, _I], C.c_int),
     "orc_get_potentials": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
@@ -244,6 +249,29 @@ class OracleState:
 
     def CalculateAllMoments(self):
         self._call("orc_calculate_moments")
+
+    def add_constraint(self, l, m, constraint, intensity=0.0, iteration=-1):
+        mc = _abi.MgMomentConstraint(l, m, constraint, intensity, iteration)
+        k = self.lib.orc_add_constraint(self.h, C.byref(mc))
+        if k < 0:
+            raise _abi.MgError("orc_add_constraint", k)
+        return k
+
+    def get_constraint(self, k=0):
+        st = _abi.MgConstraintState()
+        self._call("orc_get_constraint", int(k), C.byref(st))
+        return st.as_dict()
+
+    def get_constraint_fields(self):
+        cut, fld = np.empty(2 * self.V), np.empty(2 * self.V)
+        self._call("orc_get_constraint_fields", _d(cut), _d(fld))
+        return cut, fld
+
+    def AlternateStep(self):
+        self._call("orc_alternate_step")
+
+    def ReadjustAllMoments(self, iteration):
+        self._call("orc_readjust_moments", int(iteration))
 
     def SolveCoulomb(self):
         it = C.c_int(0)

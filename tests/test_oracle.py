@@ -222,3 +222,76 @@ def test_iterative_estimation_step_parameters():
     assert 100.0 < max_e + e.min() < 5000.0
     want = 0.9 * 4.0 * SLY4.hbar / (math.sqrt(max_e) + math.sqrt(rel_e)) ** 2
     assert dt == pytest.approx(want, rel=1e-12, abs=0)
+
+
+def _rutz_numpy(rho, n, dx, dv):
+    """RutzCutOff (src/Moments.f90:2703-2871) restated with numpy on an
+    n^3 EV8 stored mesh: the oracle's loop form must agree with it."""
+    x = dx / 2 + dx * np.arange(n)
+    out = np.zeros_like(rho)
+    for it in range(2):
+        r = rho[it].reshape(n, n, n)            # [k][j][i], x fastest
+        if dv * r.sum() < 1e-10:
+            continue
+        tr = r.max() / 10.0
+        a = r[:-1, :-1, :-1]
+        Z, Y, X = np.meshgrid(x[:-1], x[:-1], x[:-1], indexing="ij")
+        pts = []
+        for b, axis in ((r[:-1, :-1, 1:], 0), (r[:-1, 1:, :-1], 1), (r[1:, :-1, :-1], 2)):
+            m = ((a >= tr) & (b <= tr)) | ((a <= tr) & (b >= tr))
+            p = [X[m], Y[m], Z[m]]
+            p[axis] = p[axis] + dx * (tr - a[m]) / (b[m] - a[m])
+            pts.append(np.stack(p, axis=1))
+        s = np.concatenate(pts)
+        Zg, Yg, Xg = np.meshgrid(x, x, x, indexing="ij")
+        g = np.stack([Xg.ravel(), Yg.ravel(), Zg.ravel()], axis=1)
+        d = ((g[:, None, 0] - s[None, :, 0]) ** 2 + (g[:, None, 1] - s[None, :, 1]) ** 2
+             + (g[:, None, 2] - s[None, :, 2]) ** 2).min(axis=1)
+        sig = np.where(r.ravel() > tr, -1.0, 1.0)
+        out[it] = 1.0 / (1.0 + np.exp((sig * np.sqrt(d) - 4.0) / 0.4))
+    return out
+
+
+def _constrained_start(iteration=10, target=50.0, n=10):
+    p = RunParams(nx=n, ny=n, nz=n, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.set_pairing()
+    k = o.add_constraint(2, 0, target, 0.0, iteration)
+    o.Start()
+    return p, o, k
+
+
+def test_rutz_cutoff_matches_numpy_restatement():
+    p, o, _ = _constrained_start()
+    rho = o.get_densities()["rho"].reshape(2, -1)
+    cut, field = o.get_constraint_fields()
+    ref = _rutz_numpy(rho, p.nx, p.dx, 8 * p.dx ** 3)
+    assert np.abs(cut.reshape(2, -1) - ref).max() < 1e-13
+    assert 0.0 <= cut.min() and cut.max() <= 1.0 and cut.max() > 0.99
+    # the intensity is estimated on the first readjustment: no field at the start
+    assert np.abs(field).max() == 0.0
+
+
+def test_q20_constraint_moves_the_moment_then_switches_off():
+    """A Q20 constraint (alternating kind) for 4 iterations: the
+    alternate steps and the constraint field push <Q20> from ~0 towards
+    the target; afterwards the constraint is inactive and its field zero."""
+    p, o, k = _constrained_start(iteration=4)
+    q0 = sum(o.get_constraint(k)["value"])
+    assert abs(q0) < 0.1
+    o.Evolve(1, 0.010, 0.3)
+    st = o.get_constraint(k)
+    # Readjust: Intensity = 2 / sum(Squared), halved under momentum
+    assert st["intensity"] == pytest.approx(0.5 * 2.0 / sum(st["squared"]), rel=1e-12)
+    o.Evolve(3, 0.010, 0.3)
+    st = o.get_constraint(k)
+    assert st["active"] and sum(st["value"]) > 20.0
+    assert np.abs(o.get_constraint_fields()[1]).max() > 0.0
+    o.Evolve(2, 0.010, 0.3)     # iteration 5 switches it off, 6 has no field
+    st = o.get_constraint(k)
+    assert not st["active"]
+    assert np.abs(o.get_constraint_fields()[1]).max() == 0.0
