@@ -30,6 +30,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -427,6 +428,7 @@ def run_ours(args, rank, world, local_rank):
         accuracy = accuracy_check(args.accuracy_iters, seed)
     micro = microbench_c2(torch, stream) if rank == 0 and args.micro else None
     poisson = poisson_64c(torch, stream) if rank == 0 and args.micro else None
+    batched = batched_64_uneven(torch) if rank == 0 and args.batch else None
 
     if rank != 0:
         return None
@@ -476,6 +478,71 @@ def run_ours(args, rank, world, local_rank):
         res["microbench_32c_200"] = micro
     if poisson:
         res["poisson_64c"] = poisson
+    if batched:
+        res["batched_64_uneven"] = batched
+    return res
+
+
+def batched_64_uneven(torch, rounds=20, seq_rounds=5):
+    """64 independent Q20-constrained HFB instances of uneven size (mixed
+    precision), run concurrently through mg_batch_* after the schedule
+    autotuner, then driven one after another (one worker) for comparison.
+    A round is one Evolve pass of every instance; the rate is instance
+    iterations per second (host clock around each batch call, which returns
+    when every instance's work is complete)."""
+    from mocca_gb300 import SLY4, synthetic
+    from mocca_gb300.mesh import Batch, MeshState
+    inst = synthetic.uneven_instances(64, seed=7)
+    states = []
+    t_setup = time.perf_counter()
+    for d in inst:
+        p = d["params"]
+        psi, qn, en = synthetic.ho_basis(p, d["n_neutron"], seed=d["seed"])
+        g = MeshState(p, SLY4)
+        g.set_spinors(psi, qn)
+        g.set_energies(en)
+        g.set_pairing()
+        g.add_constraint(2, 0, d["q20"])
+        g.Start()
+        states.append(g)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+    b = Batch(states)
+    t_tune = time.perf_counter()
+    workers = b.tune(1, DT, MOMENTUM)
+    t_tune = time.perf_counter() - t_tune
+    b.Evolve(2, DT, MOMENTUM)
+    t0 = time.perf_counter()
+    out = b.Evolve(rounds, DT, MOMENTUM)
+    t_batch = time.perf_counter() - t0
+    b.set_workers(1)
+    t0 = time.perf_counter()
+    b.Evolve(seq_rounds, DT, MOMENTUM)
+    t_seq = time.perf_counter() - t0
+    q20 = [sum(s.get_constraint(0)["value"]) for s in states]
+    rate = 64 * rounds / t_batch
+    rate_seq = 64 * seq_rounds / t_seq
+    res = {
+        "workload": "64 HFB instances, seed 7: beta2 ~ U[-0.3, 0.5] (Q20 constraint, alternating "
+                    "kind, always on), N, Z even in [8, 40], n^3 EV8 stored meshes n in [12, 28] "
+                    "(box holds the nucleus), nwt = round(1.4 A) in [20, 200]; SLy4, HFB "
+                    "G=1250 alpha=1, mixed precision, dt=0.010, momentum 0.3",
+        "meshes": sorted(d["params"].nx for d in inst),
+        "nwt_total": int(sum(d["params"].nwt for d in inst)),
+        "workers_tuned": workers,
+        "value": rate, "unit": "instance-iter/s",
+        "ms_per_round": t_batch / rounds * 1e3,
+        "sequential": {"value": rate_seq, "unit": "instance-iter/s",
+                       "ms_per_round": t_seq / seq_rounds * 1e3},
+        "speedup_vs_sequential": rate / rate_seq,
+        "rounds_timed": rounds, "setup_s": t_setup, "tune_s": t_tune,
+        "energies_finite": bool(all(math.isfinite(o["total"]) for o in out)),
+        "q20_rel_dev_max": float(max(abs(q - d["q20"]) / max(1.0, abs(d["q20"]))
+                                     for q, d in zip(q20, inst))),
+    }
+    b.close()
+    for s in states:
+        s.close()
     return res
 
 
@@ -534,6 +601,8 @@ def main():
     ap.add_argument("--breakdown", action="store_true")
     ap.add_argument("--no-micro", dest="micro", action="store_false",
                     help="skip the 32^3 mesh-kernel and 64^3 Poisson lines")
+    ap.add_argument("--no-batch", dest="batch", action="store_false",
+                    help="skip the 64-instance batched line")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run one iteration of --precision between profiler start/stop "
                          "(for ncu --profile-from-start off) and exit")

@@ -359,6 +359,40 @@ int mg_energy(mg_ctx* ctx, mg_energy_terms* out);
 int mg_iterate(mg_ctx* ctx, int n_iter, double dt, double momentum,
                mg_energy_terms* out);
 
+/* ---- batches of independent instances ------------------------------------- */
+
+/* A batch of independent HFB instances (uneven meshes, spwf counts,
+ * particle numbers, constraints) run concurrently: the reference runs one
+ * nucleus per process (src/Main.f90), so this has no single reference
+ * counterpart; each instance follows Evolve exactly as mg_iterate does.
+ * The contexts come from mg_create (each on its own stream: pass NULL) and
+ * stay owned by the caller, who prepares them (spinors, pairing,
+ * constraints, start) before batching.  Host worker threads drive the
+ * instances, each instance on its own streams, so the latency-bound steps of
+ * one overlap with the mesh kernels of others.  Until the batch is tuned
+ * the workers are min(n, host threads), instances assigned longest first by
+ * nwt * V. */
+typedef struct mg_batch mg_batch;
+int mg_batch_create(int n, mg_ctx* const* ctxs, mg_batch** out);
+int mg_batch_destroy(mg_batch* b);
+/* Schedule autotuner: `probe` passes of each instance alone give its pass
+ * time; then `probe` rounds for each candidate worker count (powers of two
+ * up to min(n, 4 x host threads), and n) with a longest-first assignment of
+ * those times; the fastest is kept (workers_out, may be NULL).  The tuning
+ * passes are ordinary Evolve passes: they advance every instance by
+ * probe * (1 + candidates) iterations.  dt, momentum: n values. */
+int mg_batch_tune(mg_batch* b, int probe, const double* dt, const double* momentum,
+                  int* workers_out);
+/* Fixes the worker count (longest-first assignment); returns it. */
+int mg_batch_set_workers(mg_batch* b, int workers);
+/* n_iter Evolve passes of every instance (mg_iterate with dt[i],
+ * momentum[i]); out (n entries, may be NULL) receives each instance's last
+ * energy.  Returns when all instances' work is complete: the first negative
+ * status of any instance, else MG_NOT_CONVERGED if any Coulomb solve hit its
+ * cap, else MG_OK. */
+int mg_batch_iterate(mg_batch* b, int n_iter, const double* dt, const double* momentum,
+                     mg_energy_terms* out);
+
 /* Number of kernels this context has launched so far (instrumentation; the
  * reference's only counterpart is the CoulombTime accumulator,
  * src/Coulomb.f90:288, :333-334). */

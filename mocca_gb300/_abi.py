@@ -190,6 +190,11 @@ SIGNATURES = {
     "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
     "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "mg_batch_create": [C.c_int, _PP, C.POINTER(_P)],
+    "mg_batch_destroy": [_P],
+    "mg_batch_tune": [_P, C.c_int, _D, _D, _I],
+    "mg_batch_set_workers": [_P, C.c_int],
+    "mg_batch_iterate": [_P, C.c_int, _D, _D, C.POINTER(MgEnergyTerms)],
     "mg_eigh_batched": [C.c_int, _I, C.c_int, _D, _D, _D],
     "mg_eigh_batched_noalloc": [C.c_int, _I, C.c_int, _P, _P, _P, _P],
     "mg_set_pairing": [_P, C.POINTER(MgPairingParams)],

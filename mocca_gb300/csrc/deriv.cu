@@ -16,8 +16,10 @@
 // Matrices are stored transposed, MT[q*n + i], so the threads of a warp
 // (consecutive output points i) read consecutive shared-memory words.
 #include <algorithm>
+#include <mutex>
 
 #include "df.cuh"
+
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -420,18 +422,19 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     // z planes per k_deriv_xy block: one when few grids (densities, fields)
     // would leave most SMs idle
     const int ppb = njobs < 64 ? 1 : 4;
-    static bool attr_done = false;
-    if (!attr_done) {
-        MG_CUDA(cudaFuncSetAttribute(k_deriv_xy, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
-        MG_CUDA(cudaFuncSetAttribute(k_deriv_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
-        MG_CUDA(cudaFuncSetAttribute(k_deriv_xy_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
-        MG_CUDA(cudaFuncSetAttribute(k_deriv_z_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
-        attr_done = true;
-    }
+    // once per process (contexts of a batch call this from several threads)
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        const void* fns[4] = {(const void*)k_deriv_xy, (const void*)k_deriv_z,
+                              (const void*)k_deriv_xy_df, (const void*)k_deriv_z_df};
+        for (const void* f : fns) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            if (e != cudaSuccess && attr_err == cudaSuccess) attr_err = e;
+        }
+    });
+    MG_CUDA(attr_err);
     if (c->cur_precision == MG_MIXED) {
         // out_df: the outputs stay double-float ({hi, lo} float pairs)
         MatPtrs32 mp = mat_ptrs32(c);

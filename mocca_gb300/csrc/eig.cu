@@ -369,7 +369,8 @@ k_oa_apply(const double* __restrict__ S, double* __restrict__ G, long stride, in
 __global__ void __launch_bounds__(kJThreads)
 k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* __restrict__ nsz,
                   const double* __restrict__ anorm, double* __restrict__ Q,
-                  double* __restrict__ w, long wstride, int* __restrict__ pfail) {
+                  double* __restrict__ w, long wstride, int* __restrict__ pfail,
+                  int max_sweeps) {
     extern __shared__ double smd[];
     __shared__ double red[32];
     __shared__ double cs[2][64];
@@ -398,7 +399,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     const int lane = tid & 127, kg = tid >> 7;
     const int half = n / 2;
     int sweep = 0;
-    for (; sweep < 12; ++sweep) {
+    for (; sweep < max_sweeps; ++sweep) {
         // a pair rotates when its coupling is above the FP64 noise of X^T A X
         // (~ sqrt(n) eps |A|): rotating noise would only churn, at FP64 cost.
         // Only the rounds holding such a pair at the start of the sweep run
@@ -475,7 +476,7 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
             __syncthreads();
         }
     }
-    if (tid == 0 && pfail) pfail[b] = sweep == 12 ? 1 : 0;
+    if (tid == 0 && pfail) pfail[b] = sweep == max_sweeps ? 1 : 0;
     for (int i = tid; i < n0; i += kJThreads) w[b * wstride + i] = a[i * l2 + i];
 }
 
@@ -627,7 +628,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
         MG_LAUNCHED(c);
         k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(
-            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail);
+            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail, 12);
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
         MG_LAUNCHED(c);
@@ -646,6 +647,37 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
     }
+    return MG_OK;
+}
+
+// The whole batch by cyclic FP64 Jacobi on A itself (the polish kernel
+// started from the identity, up to 40 sweeps), eigenvalues ascending: the
+// fallback when a refined decomposition is found wanting.  Slow (every
+// rotation in FP64) but it converges for any symmetric matrix.
+int eig_jacobi_fp64(mg_ctx* c, EigBatch& E) {
+    const int np = E.nmax + (E.nmax & 1);
+    const size_t psm = (size_t)np * (np + 1) * sizeof(double);
+    if (psm > 200 * 1024) return MG_ERR_ARG;
+    if (!E.attr_done) {
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+        E.attr_done = true;
+    }
+    k_frob<<<E.nb, 1024, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
+    MG_LAUNCHED(c);
+    k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm,
+                                                           E.X, E.w, E.wstride, E.pfail, 40);
+    MG_LAUNCHED(c);
+    k_sort_cols<<<dim3(div_up(E.nmax, kSortRows), E.nb), 128, 0, c->stream>>>(
+        E.X, E.X2, E.w, E.part, E.stride, E.ld, E.wstride, E.nsz);
+    MG_LAUNCHED(c);
+    MG_CUDA(cudaMemcpyAsync(E.w, E.part, (size_t)E.nb * E.wstride * sizeof(double),
+                            cudaMemcpyDeviceToDevice, c->stream));
+    MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
+                            cudaMemcpyDeviceToDevice, c->stream));
+    E.have_vectors = true;
     return MG_OK;
 }
 

@@ -45,6 +45,15 @@ constexpr double kRefineTol = 1e-8;
 // expansion instead of an evaluation (the second-order remainder in N is
 // below 1e-13 for the curvatures seen, far inside FermiPrec = 1e-12).
 constexpr double kTaylorStep = 2e-7;
+// ... and only while the step is small against the quasiparticle gap around
+// zero energy (2 min E): the expansion coefficients go as 1 / (E_m - E_n), so
+// the neglected second order is ~(dl / gap)^2.  A level at the Fermi energy
+// with vanishing pairing (unbound neutrons, say) closes the gap and takes
+// every step back to a full evaluation.
+constexpr double kTaylorGap = 1e-6;
+// Fermi-energy step (MeV) above which an evaluation re-seeds its
+// eigen-decomposition instead of refining the previous vectors.
+constexpr double kFarStep = 0.5;
 
 __device__ double cta_sum(double x, double* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -144,7 +153,7 @@ k_dn_dlambda(const double* __restrict__ X, const double* __restrict__ E,
 // angle seen by the last refinement step into out[8 + b].
 __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ hsz, int nmax,
                         const double* __restrict__ dpart, const double* __restrict__ emax,
-                        double* __restrict__ out) {
+                        const double* __restrict__ w, long wstride, double* __restrict__ out) {
     __shared__ double red[32];
     const int b = blockIdx.x;
     const int h = hsz[b], N = 2 * h;
@@ -165,6 +174,9 @@ __global__ void k_trace(const double* __restrict__ rho, const int* __restrict__ 
         out[b] = s;
         out[4 + b] = ds;
         out[8 + b] = em;
+        // quasiparticle gap around zero energy: the spectrum of a block is
+        // +-E pairs in ascending order, so it is w[h] - w[h-1] = 2 min E
+        out[12 + b] = h > 0 ? w[(long)b * wstride + h] - w[(long)b * wstride + h - 1] : 1e300;
     }
 }
 
@@ -260,9 +272,10 @@ k_occupations(const double* __restrict__ X, const double* __restrict__ w,
         const double x = X[(long)b * hmax * hmax + (long)r * hmax + C];
         cantr[(long)b * hmax * hmax + t] = fabs(x) < 1e-11 ? 0.0 : x;
     }
-    double part = 0.0;
+    double part = 0.0, omax = 0.0;
     for (int C = threadIdx.x; C < h; C += kThreads) {
         double o = w[(long)b * hmax + C];
+        omax = fmax(omax, o);
         if (o > 1.0 + 1e-5) atomicExch(flags + 3, 1);
         if (o < -0.1) o += 2.0;
         if (o < 0.0) o = 0.0;
@@ -272,7 +285,16 @@ k_occupations(const double* __restrict__ X, const double* __restrict__ w,
         part += o * (2.0 - o);
     }
     const double s = cta_sum(part, red);
-    if (threadIdx.x == 0) scal[4 + b] = s;
+    for (int o = 16; o > 0; o >>= 1) omax = fmax(omax, __shfl_xor_sync(0xffffffffu, omax, o));
+    __syncthreads();
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = omax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int k = 0; k < kThreads / 32; ++k) m = fmax(m, red[k]);
+        scal[4 + b] = s;
+        scal[8 + b] = m;   // largest canonical occupation v^2 of the block
+    }
 }
 
 // rho/kappa mixing with the previous iteration's matrices (HFBMix) and the
@@ -342,7 +364,7 @@ int hfb_prepare(mg_ctx* c) {
               A(&H.dfac, 2 * V) && A(&H.pcut, nwt) && A(&H.ktil, 4L * hmax * hmax) &&
               A(&H.fpart, 8 * V) && A(&H.fre, 2 * V) && A(&H.fim, 2 * V) &&
               A(&H.gpart, 4L * H.gchunk * hmax * hmax) && A(&H.cantr, 4L * hmax * hmax) &&
-              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.trace_d, 12) && A(&H.dpart, 4L * hmax) && A(&H.scal_d, 16) &&
+              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.trace_d, 16) && A(&H.dpart, 4L * hmax) && A(&H.scal_d, 16) &&
               cudaMalloc(&H.members, 4 * hmax * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.hsz, 4 * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.nsz_T, 4 * sizeof(int)) == cudaSuccess &&
@@ -453,7 +475,8 @@ static int eval_launches(mg_ctx* c, int seed) {
     MG_LAUNCHED(c);
     k_dn_dlambda<<<dim3(H.hmax, 4), 128, 0, c->stream>>>(H.eT.X, H.eT.w, H.hsz, H.nmax, H.dpart);
     MG_LAUNCHED(c);
-    k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.dpart, H.eT.emax, H.trace_d);
+    k_trace<<<4, 128, 0, c->stream>>>(H.rho, H.hsz, H.nmax, H.dpart, H.eT.emax, H.eT.w,
+                                      H.eT.wstride, H.trace_d);
     MG_LAUNCHED(c);
     return MG_OK;
 }
@@ -492,18 +515,20 @@ static int eval_run(mg_ctx* c, int seed) {
     return MG_OK;
 }
 
+// seed < 0: the Jacobi warm seed for a first evaluation (or a far jump of
+// lambda), refinement of the previous vectors otherwise.
 static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_out,
-                        bool first) {
+                        bool first, int seed = -1) {
     Hfb& H = c->hfb;
     double* hp = H.h_pinned;
     hp[24] = lam[0];
     hp[25] = lam[1];
     MG_CUDA(cudaMemcpyAsync(H.fermi_d, hp + 24, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    int seed = !H.eT.have_vectors ? kSeedCold : first ? kSeedJacobiWarm : kSeedRefine;
+    if (seed < 0) seed = !H.eT.have_vectors ? kSeedCold : first ? kSeedJacobiWarm : kSeedRefine;
     for (int attempt = 0; attempt < 2; ++attempt) {
         MG_TRY(eval_run(c, seed));
         H.eT.have_vectors = true;
-        MG_CUDA(cudaMemcpyAsync(hp, H.trace_d, 12 * sizeof(double), cudaMemcpyDeviceToHost,
+        MG_CUDA(cudaMemcpyAsync(hp, H.trace_d, 16 * sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
         const double em = std::max(std::max(hp[8], hp[9]), std::max(hp[10], hp[11]));
@@ -515,6 +540,8 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     N_out[1] = hp[2] + hp[3] - c->p.protons;
     dN_out[0] = hp[4] + hp[5];
     dN_out[1] = hp[6] + hp[7];
+    H.qp_gap[0] = std::min(hp[12], hp[13]);
+    H.qp_gap[1] = std::min(hp[14], hp[15]);
     if (std::isnan(N_out[0]) || std::isnan(N_out[1])) return MG_ERR_NAN;
     return MG_OK;
 }
@@ -607,7 +634,8 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         bool taylor = true;
         first_order = false;
         for (int it = 0; it < 2; ++it)
-            taylor = taylor && (conv[it] || (newton[it] && std::fabs(dl[it]) <= kTaylorStep));
+            taylor = taylor && (conv[it] || (newton[it] && std::fabs(dl[it]) <= kTaylorStep &&
+                                             std::fabs(dl[it]) <= kTaylorGap * H.qp_gap[it]));
         if (taylor) {
             MG_TRY(taylor_finish(c, dl));
             ++H.taylor_steps;
@@ -619,7 +647,10 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
             }
             break;
         }
-        MG_TRY(hfb_evaluate(c, lam, f, fp, false));
+        // a far move of lambda (a search that has not settled) starts from
+        // the Jacobi warm seed: refinement alone is for nearby vectors
+        const bool far = std::fabs(dl[0]) > kFarStep || std::fabs(dl[1]) > kFarStep;
+        MG_TRY(hfb_evaluate(c, lam, f, fp, far));
         ++evals;
         for (int it = 0; it < 2; ++it) {
             if (conv[it]) continue;
@@ -640,7 +671,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     H.fermi_hist[6] = std::fabs(f[0]) > 0.9 || std::fabs(f[1]) > 0.9;
     bool lost = true;
     for (int i = 0; i < 7; ++i) lost = lost && H.fermi_hist[i];
-    const double tr0 = f[0] + c->p.neutrons, tr1 = f[1] + c->p.protons;
+    double tr0 = f[0] + c->p.neutrons, tr1 = f[1] + c->p.protons;
 
     // ---- canonical basis, occupations, mixing, pairing energy ------------------
     double* hp = H.h_pinned;
@@ -656,6 +687,32 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax, H.cantr,
                                                  c->bas[MG_CAN_BASIS].occ, H.scal_d, c->flags);
     MG_LAUNCHED(c);
+    int oflag = 0;
+    MG_CUDA(cudaMemcpyAsync(&oflag, c->flags + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    if (oflag) {
+        // An occupation above one: a decomposition that lost orthonormality
+        // (the refinement can, on spectra clustered at 0 and 1).  Redo the
+        // evaluation at the final lambda from scratch and the canonical basis
+        // by plain FP64 Jacobi before reporting the state as the reference
+        // does.
+        double f2[2], fp2[2];
+        MG_TRY(hfb_evaluate(c, lam, f2, fp2, true, kSeedCold));
+        ++evals;
+        tr0 = f2[0] + c->p.neutrons;
+        tr1 = f2[1] + c->p.protons;
+        first_order = false;
+        MG_CUDA(cudaMemsetAsync(c->flags + 3, 0, sizeof(int), c->stream));
+        k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
+            H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
+        MG_LAUNCHED(c);
+        MG_TRY(eig_jacobi_fp64(c, H.eR));
+        k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax,
+                                                     H.cantr, c->bas[MG_CAN_BASIS].occ, H.scal_d,
+                                                     c->flags);
+        MG_LAUNCHED(c);
+        ++H.reseeds;
+    }
     MG_TRY(canonical_transform(c));
     k_hfb_mix<<<4, kThreads, 0, c->stream>>>(H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.hsz,
                                            H.nmax, H.pp.mix, H.oldrho_zero ? 0 : 1, 1, H.scal_d);
@@ -685,8 +742,20 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         info->dispersion[1] = H.disp[1];
         info->first_order = first_order ? 1 : 0;
     }
-    if (hflags[3]) return MG_ERR_STATE;  // occupation above one (src/HFB.f90:3392-3395)
-    if (lost) return MG_ERR_STATE;       // particle number lost 7 times (src/HFB.f90:2154-2158)
+    if (hflags[3]) {   // src/HFB.f90:3392-3395
+        double om[4];
+        MG_CUDA(cudaMemcpyAsync(om, H.scal_d + 8, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+        fprintf(stderr, "mocca_gpu: some occupations are bigger than one in the canonical basis "
+                "(largest v^2 per block: %.9f %.9f %.9f %.9f)\n", om[0], om[1], om[2], om[3]);
+        return MG_ERR_STATE;
+    }
+    if (lost) {        // src/HFB.f90:2154-2158
+        fprintf(stderr, "mocca_gpu: particle number lost in 7 consecutive Fermi searches "
+                "(last deviations %.3e %.3e)\n", f[0], f[1]);
+        return MG_ERR_STATE;
+    }
     return (conv[0] && conv[1]) ? MG_OK : MG_NOT_CONVERGED;
 }
 

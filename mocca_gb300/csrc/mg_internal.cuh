@@ -128,7 +128,8 @@ struct Hfb {
     double* trace_d = nullptr;                 // traces, dN/dlambda, refinement size
     double* dpart = nullptr;                   // 4*hmax dN/dlambda row sums
     double* scal_d = nullptr;                  // [energy(2), disp(2)]
-    double* h_pinned = nullptr;                // 8 pinned doubles
+    double* h_pinned = nullptr;                // 32 pinned doubles
+    double qp_gap[2] = {0.0, 0.0};             // per isospin: smallest 2 min E of its blocks
     double fermi[2] = {-10.0, -10.0};
     double fermi_prev[2] = {-10.0, -10.0};     // Fermi energies of the solve before
     int n_solved = 0;                          // consecutive converged solves
@@ -335,6 +336,7 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
 enum EigSeed { kSeedCold = 0, kSeedJacobiWarm = 1, kSeedRefine = 2 };
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish);
 int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim);
+int eig_jacobi_fp64(mg_ctx* c, EigBatch& E);
 void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);

@@ -16,6 +16,9 @@ every one of them runs on the GPU through the C ABI:
     CompEnergy         src/Energy.f90:62-179
     Evolve             src/Main.f90:255-328            (n passes of the loop body)
 
+`Batch` runs many independent instances (one MeshState each) concurrently
+through mg_batch_*.
+
 A non-zero status raises `MgError` (the reference stops through stp()).
 Arrays follow the reference's memory order: a spinor batch is
 [nwt, 4, nz, ny, nx] float64, fields are [it, ..., nz, ny, nx].
@@ -291,3 +294,58 @@ class MeshState:
         if hfb:
             self.hPsi(_abi.MG_CAN_BASIS, want_spinors=False)
         return it
+
+
+class Batch:
+    """Independent instances run concurrently (mg_batch_*): each MeshState
+    keeps its own mesh, spwf count, particle numbers and constraints; host
+    worker threads drive them, each on its own streams.  The states stay
+    owned by the caller and must be prepared (spinors, pairing, constraints,
+    Start) before they are batched."""
+
+    def __init__(self, states: list[MeshState]):
+        self.lib = _abi.load()
+        self.states = list(states)
+        arr = (C.c_void_p * len(self.states))(*[s.h.value for s in self.states])
+        h = C.c_void_p()
+        _abi.check("mg_batch_create", self.lib.mg_batch_create(len(self.states), arr, C.byref(h)))
+        self.h = h
+
+    def _vec(self, x) -> np.ndarray:
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64),
+                                                 (len(self.states),)))
+        return a
+
+    def tune(self, probe: int, dt, momentum) -> int:
+        """Schedule autotuner (mg_batch_tune); its passes advance every
+        instance.  Returns the chosen worker count."""
+        d, m = self._vec(dt), self._vec(momentum)
+        w = C.c_int(0)
+        _abi.check("mg_batch_tune", self.lib.mg_batch_tune(self.h, int(probe), _dptr(d), _dptr(m),
+                                                            C.byref(w)))
+        return w.value
+
+    def set_workers(self, workers: int) -> int:
+        w = self.lib.mg_batch_set_workers(self.h, int(workers))
+        if w < 0:
+            raise _abi.MgError("mg_batch_set_workers", w)
+        return w
+
+    def Evolve(self, n_iter: int, dt, momentum) -> list[dict]:
+        d, m = self._vec(dt), self._vec(momentum)
+        out = (_abi.MgEnergyTerms * len(self.states))()
+        _abi.check("mg_batch_iterate", self.lib.mg_batch_iterate(self.h, int(n_iter), _dptr(d),
+                                                                  _dptr(m), out),
+                   allow_not_converged=True)
+        return [e.as_dict() for e in out]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -9,6 +9,9 @@ for them:
   (src/InOut.f90:1418-1473), placed in the spinor component whose mirror
   parities match the orbital (the sign rules of
   src/Derivatives.f90:348-439), plus a seeded uniform perturbation.
+* `uneven_instances` -- the batched workload: quadrupole-constrained HFB
+  runs with random deformation targets, particle numbers, meshes and spwf
+  counts.
 * `gaussian_hermite_spinors` / `woods_saxon_fields` -- the mesh microbench
   (32^3 full box, 200 spinors): Gaussian envelopes of random width and
   centre times random Hermite polynomials, and Woods-Saxon U, B, W fields.
@@ -139,3 +142,40 @@ def woods_saxon_fields(p: RunParams, R: float = 3.5, a: float = 0.65, u0: float 
             W[:, n, m] = acc
     divW = np.zeros((2, 3, V))
     return U, B, nablaB, W, divW
+
+
+def beta2_to_q20(beta2: float, A: float) -> float:
+    """<Q20> (fm^2) of a deformation beta2, inverting CalcBeta
+    (src/Moments.f90:3472-3494): beta = 4 pi Q / (3 A R^2), R = 1.2 A^(1/3)."""
+    R = 1.2 * A ** (1.0 / 3.0)
+    return beta2 * 3.0 * A * R * R / (4.0 * math.pi)
+
+
+def uneven_instances(count: int = 64, seed: int = 7, n_range=(12, 28), dx: float = 0.8,
+                     precision: int = 1, pairing: int = 2):
+    """Seeded independent constrained-HFB instances of uneven size.
+
+    Per instance: beta2 ~ U[-0.3, 0.5]; N, Z even in [8, 40]; stored mesh n
+    uniform in [n_min(A), 28] with n_min(A) = max(12, ceil((1.2 A^(1/3) + 6) /
+    dx)) so the box holds the nucleus; nwt = round(1.4 (N + Z)) clipped to
+    [20, 200] and made even, split between neutrons and protons in
+    proportion to N and Z.  Returns a list of dicts with the RunParams, the
+    neutron spwf count, the Q20 target and the start seed.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        beta2 = float(rng.uniform(-0.3, 0.5))
+        N = int(rng.integers(4, 21)) * 2
+        Z = int(rng.integers(4, 21)) * 2
+        A = N + Z
+        n_min = max(n_range[0], math.ceil((1.2 * A ** (1.0 / 3.0) + 6.0) / dx))
+        n = int(rng.integers(min(n_min, n_range[1]), n_range[1] + 1))
+        nwt = int(min(200, max(20, round(1.4 * A))))
+        nwt += nwt % 2
+        n_neutron = max(N // 2 + 2, min(nwt - Z // 2 - 2, round(nwt * N / A)))
+        p = RunParams(nx=n, ny=n, nz=n, dx=dx, nwt=nwt, neutrons=float(N), protons=float(Z),
+                      precision=precision, pairing=pairing)
+        out.append({"params": p, "n_neutron": int(n_neutron), "beta2": beta2,
+                    "q20": beta2_to_q20(beta2, A), "seed": seed * 1000 + i})
+    return out

@@ -44,3 +44,4 @@ def test_max_over_ranks_single_process():
     sys.path.insert(0, str(ROOT))
     import bench
     assert bench.max_over_ranks(3.5, device="cpu") == 3.5
+
