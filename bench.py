@@ -10,6 +10,7 @@ DeriveAll, densities, moments, potentials with the Coulomb CG, energy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision mixed|fp64] [--accuracy-iters A] [--breakdown] [--no-micro]
+                  [--no-batch]
 
 One JSON line on rank 0.  `value` is the headline form (mixed precision by
 default): K steps with every input resident in HBM (CUDA events on the
@@ -22,8 +23,10 @@ the spinors plus the energy read back every step.  The working set
 (spinors, derivatives, updates: ~0.7 GB) is larger than the 129 MB L2, so
 no flush is needed between steps.  Multi-GPU runs are independent replicas
 (weak scaling).  `microbench_32c_200` times DeriveAll and h.psi of 200
-spinors on the 32^3 symmetry-free box in both precisions, and `poisson_64c`
-one Coulomb solve on a 64^3 mesh.
+spinors on the 32^3 symmetry-free box in both precisions, `poisson_64c`
+one Coulomb solve on a 64^3 mesh, and `batched_64_uneven` 64 independent
+Q20-constrained HFB instances of uneven size run concurrently through the
+batch API (after its schedule autotuner) and one after another.
 """
 from __future__ import annotations
 
