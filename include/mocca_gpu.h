@@ -160,7 +160,7 @@ int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* out);
 int mg_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2);
 
 /* Batched symmetric eigensolver used by the HFB step (replaces diagoncr8,
- * src/HFB.f90:5880-6087): nb matrices of sizes n[b] <= 128, row-major with
+ * src/HFB.f90:5880-6087): nb <= 64 matrices of sizes n[b] <= ld <= 160, row-major with
  * leading dimension ld and stride ld*ld in a (host arrays); w receives the
  * eigenvalues ascending (stride ld), z the eigenvectors (column k <-> w[k]).
  * Runs on the current CUDA device; FP64-accurate (FP32 Jacobi seed, FP64

@@ -36,6 +36,13 @@ constexpr int kTile = 16;
 // rounds (128 lanes for the columns / rows x 8 groups of rotation pairs)
 constexpr int kJThreads = 1024;
 constexpr int kJGroups = kJThreads / 128;
+// largest matrix whose FP32 Jacobi keeps its warm-start scratch in shared
+// memory (3 planes of n x (n+1) floats)
+constexpr int kJSmemMax = 128;
+// dynamic shared memory the Jacobi kernels opt in to: their largest need,
+// two float planes (FP32 seed) or one double plane (FP64 polish) of
+// kEigMax x (kEigMax + 1) -- 206 KB, which leaves room for their static arrays
+constexpr int kSmemOptIn = kEigMax * (kEigMax + 1) * 8;
 
 __device__ float cta_sumf(float x, float* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -76,16 +83,18 @@ __device__ __forceinline__ int rr_round(int p, int q, int n) {
 
 // One matrix per CTA.  A: FP64 n x n (lda) input; Xw: optional FP64 warm
 // start (n x n, ldx); X: FP64 output vectors (n x n, ldx, column k <-> w[k]);
-// w: eigenvalues ascending.  n <= 128.
+// w: eigenvalues ascending.  n <= kEigMax.  Above kJSmemMax the warm start's
+// product A V goes through X (FP64) instead of a third shared-memory plane;
+// Xw may alias X, whose contents are in v by then.
 __global__ void __launch_bounds__(kJThreads)
 k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __restrict__ nsz,
-           const double* __restrict__ Xw, double* __restrict__ X, long xstride, int ldx,
+           const double* Xw, double* X, long xstride, int ldx,
            double* __restrict__ w, long wstride, int max_sweeps, int* __restrict__ flag) {
     extern __shared__ float smf[];
     __shared__ float red[32];
-    __shared__ float cs[2][64];
-    __shared__ int pq[2][64];
-    __shared__ int perm[128];
+    __shared__ float cs[2][kEigMax / 2];
+    __shared__ int pq[2][kEigMax / 2];
+    __shared__ int perm[kEigMax];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
     if (n0 == 0) return;
@@ -93,7 +102,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     const int ld = n + 1;
     float* a = smf;             // n x ld
     float* v = a + n * ld;      // n x ld
-    float* t = v + n * ld;      // n x ld scratch
+    float* t = n <= kJSmemMax ? v + n * ld : nullptr;   // n x ld scratch
     const double* Ab = A + b * astride;
     const int tid = threadIdx.x;
     for (int q = tid; q < n * n; q += kJThreads) {
@@ -104,7 +113,7 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         v[i * ld + j] = vv;
     }
     __syncthreads();
-    if (Xw) {
+    if (Xw && t) {
         // a <- V^T A V
         for (int q = tid; q < n * n; q += kJThreads) {
             const int i = q / n, j = q % n;
@@ -120,6 +129,26 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
             a[i * ld + j] = s;
         }
         __syncthreads();
+    } else if (Xw) {
+        // the same through X: the padding row and column of A V and of
+        // V^T A V are zero (A's padding is zero, V's is the identity)
+        double* tg = X + b * xstride;
+        for (int q = tid; q < n0 * n0; q += kJThreads) {
+            const int i = q / n0, j = q % n0;
+            float s = 0.0f;
+            for (int k = 0; k < n0; ++k) s = fmaf(a[i * ld + k], v[k * ld + j], s);
+            tg[(long)i * ldx + j] = (double)s;
+        }
+        __syncthreads();
+        for (int q = tid; q < n0 * n0; q += kJThreads) {
+            const int i = q / n0, j = q % n0;
+            float s = 0.0f;
+            for (int k = 0; k < n0; ++k) s = fmaf(v[k * ld + i], (float)tg[(long)k * ldx + j], s);
+            a[i * ld + j] = s;
+        }
+        __syncthreads();
+    }
+    if (Xw) {
         // symmetrise
         for (int q = tid; q < n * n; q += kJThreads) {
             const int i = q / n, j = q % n;
@@ -131,20 +160,21 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         }
         __syncthreads();
     }
-    // thread (lane, kg): column / row `lane`, every kJGroups-th rotation pair from kg
+    // thread (lane, kg): columns / rows lane, lane + 128, ..., every
+    // kJGroups-th rotation pair from kg
     const int lane = tid & 127, kg = tid >> 7;
     const int half = n / 2;
     float part = 0.0f;
-    if (lane < n)
-        for (int i = kg; i < n; i += kJGroups) part += a[i * ld + lane] * a[i * ld + lane];
+    for (int col = lane; col < n; col += 128)
+        for (int i = kg; i < n; i += kJGroups) part += a[i * ld + col] * a[i * ld + col];
     const float norm2 = cta_sumf(part, red);
     const float tol2 = 1e-11f * norm2;  // off-diagonal <= 3e-6 |A|: an FP32-level seed
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         part = 0.0f;
-        if (lane < n)
+        for (int col = lane; col < n; col += 128)
             for (int i = kg; i < n; i += kJGroups)
-                if (i != lane) part += a[i * ld + lane] * a[i * ld + lane];
+                if (i != col) part += a[i * ld + col] * a[i * ld + col];
         const float off = cta_sumf(part, red);
         if (off <= tol2) break;
         for (int r = 0; r < n - 1; ++r) {
@@ -164,25 +194,25 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
                 pq[1][tid] = q;
             }
             __syncthreads();
-            if (lane < n)
+            for (int col = lane; col < n; col += 128)
                 for (int k = kg; k < half; k += kJGroups) {
                     const int p = pq[0][k], q = pq[1][k];
                     const float c = cs[0][k], s = cs[1][k];
-                    const float ap = a[p * ld + lane], aq = a[q * ld + lane];
-                    a[p * ld + lane] = c * ap - s * aq;
-                    a[q * ld + lane] = s * ap + c * aq;
+                    const float ap = a[p * ld + col], aq = a[q * ld + col];
+                    a[p * ld + col] = c * ap - s * aq;
+                    a[q * ld + col] = s * ap + c * aq;
                 }
             __syncthreads();
-            if (lane < n)
+            for (int row = lane; row < n; row += 128)
                 for (int k = kg; k < half; k += kJGroups) {
                     const int p = pq[0][k], q = pq[1][k];
                     const float c = cs[0][k], s = cs[1][k];
-                    const float ap = a[lane * ld + p], aq = a[lane * ld + q];
-                    a[lane * ld + p] = c * ap - s * aq;
-                    a[lane * ld + q] = s * ap + c * aq;
-                    const float vp = v[lane * ld + p], vq = v[lane * ld + q];
-                    v[lane * ld + p] = c * vp - s * vq;
-                    v[lane * ld + q] = s * vp + c * vq;
+                    const float ap = a[row * ld + p], aq = a[row * ld + q];
+                    a[row * ld + p] = c * ap - s * aq;
+                    a[row * ld + q] = s * ap + c * aq;
+                    const float vp = v[row * ld + p], vq = v[row * ld + q];
+                    v[row * ld + p] = c * vp - s * vq;
+                    v[row * ld + q] = s * vp + c * vq;
                 }
             __syncthreads();
         }
@@ -203,9 +233,9 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         if (rank < n0) perm[rank] = i;
     }
     __syncthreads();
-    if (lane < n0)
+    for (int col = lane; col < n0; col += 128)
         for (int i = kg; i < n0; i += kJGroups)
-            X[b * xstride + (long)i * ldx + lane] = (double)v[i * ld + perm[lane]];
+            X[b * xstride + (long)i * ldx + col] = (double)v[i * ld + perm[col]];
     for (int k = tid; k < n0; k += kJThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
 }
 
@@ -231,14 +261,14 @@ __device__ __forceinline__ bool skip_step(const SkipCtl& k, int b) {
     return true;
 }
 
-// Batched FP64 GEMM, C = alpha op(A) op(B) + beta C, m,n,k <= 128, row-major.
+// Batched FP64 GEMM, C = alpha op(A) op(B) + beta C, k <= kEigMax, row-major.
 // With g.sym (C symmetric, and C itself when beta != 0) only the upper
 // triangle is computed and written to both halves, which also makes C
 // exactly symmetric.
 __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict__ descs,
                                                      SkipCtl sk) {
-    __shared__ double sA[kTile][129];
-    __shared__ double sB[129][kTile + 1];
+    __shared__ double sA[kTile][kEigMax + 1];
+    __shared__ double sB[kEigMax + 1][kTile + 1];
     const GemmDesc g = descs[blockIdx.y];
     if (skip_step(sk, g.mat)) return;
     const int tiles_n = (g.n + kTile - 1) / kTile;
@@ -373,10 +403,10 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
                   int max_sweeps) {
     extern __shared__ double smd[];
     __shared__ double red[32];
-    __shared__ double cs[2][64];
-    __shared__ int act[64];
-    __shared__ int pqi[2][64];
-    __shared__ unsigned rmask[4];
+    __shared__ double cs[2][kEigMax / 2];
+    __shared__ int act[kEigMax / 2];
+    __shared__ int pqi[2][kEigMax / 2];
+    __shared__ unsigned rmask[(kEigMax + 31) / 32];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
     if (n0 == 0) return;
@@ -406,13 +436,13 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
         // (after a refinement these are the few near-degenerate clusters); a
         // pair that a rotation lifts above the threshold waits for the next
         // sweep.
-        if (tid < 4) rmask[tid] = 0u;
+        if (tid < (kEigMax + 31) / 32) rmask[tid] = 0u;
         __syncthreads();
         int any = 0;
-        if (lane < n)
-            for (int i = kg; i < lane; i += kJGroups)
-                if (fabs(a[i * l2 + lane]) > thr) {
-                    const int r = rr_round(i, lane, n);
+        for (int col = lane; col < n; col += 128)
+            for (int i = kg; i < col; i += kJGroups)
+                if (fabs(a[i * l2 + col]) > thr) {
+                    const int r = rr_round(i, col, n);
                     atomicOr(&rmask[r >> 5], 1u << (r & 31));
                     any = 1;
                 }
@@ -449,28 +479,28 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
             }
             // rounds without a pair above the threshold rotate nothing
             if (!__syncthreads_or(on)) continue;
-            if (lane < n)
+            for (int col = lane; col < n; col += 128)
                 for (int k = kg; k < half; k += kJGroups) {
                     if (!act[k]) continue;
                     const int p = pqi[0][k], qq = pqi[1][k];
                     const double c = cs[0][k], s = cs[1][k];
-                    const double ap = a[p * l2 + lane], aq = a[qq * l2 + lane];
-                    a[p * l2 + lane] = c * ap - s * aq;
-                    a[qq * l2 + lane] = s * ap + c * aq;
+                    const double ap = a[p * l2 + col], aq = a[qq * l2 + col];
+                    a[p * l2 + col] = c * ap - s * aq;
+                    a[qq * l2 + col] = s * ap + c * aq;
                 }
             __syncthreads();
-            if (lane < n)
+            for (int row = lane; row < n; row += 128)
                 for (int k = kg; k < half; k += kJGroups) {
                     if (!act[k]) continue;
                     const int p = pqi[0][k], qq = pqi[1][k];
                     const double c = cs[0][k], s = cs[1][k];
-                    const double ap = a[lane * l2 + p], aq = a[lane * l2 + qq];
-                    a[lane * l2 + p] = c * ap - s * aq;
-                    a[lane * l2 + qq] = s * ap + c * aq;
-                    if (lane < n0 && p < n0 && qq < n0) {
-                        const double vp = Qa(lane, p), vq = Qa(lane, qq);
-                        Qa(lane, p) = c * vp - s * vq;
-                        Qa(lane, qq) = s * vp + c * vq;
+                    const double ap = a[row * l2 + p], aq = a[row * l2 + qq];
+                    a[row * l2 + p] = c * ap - s * aq;
+                    a[row * l2 + qq] = s * ap + c * aq;
+                    if (row < n0 && p < n0 && qq < n0) {
+                        const double vp = Qa(row, p), vq = Qa(row, qq);
+                        Qa(row, p) = c * vp - s * vq;
+                        Qa(row, qq) = s * vp + c * vq;
                     }
                 }
             __syncthreads();
@@ -512,9 +542,9 @@ __global__ void __launch_bounds__(128)
 k_sort_cols(const double* __restrict__ X, double* __restrict__ X2, const double* __restrict__ w,
             double* __restrict__ w2, long stride, int ld, long wstride,
             const int* __restrict__ nsz) {
-    __shared__ unsigned long long key[128];
-    __shared__ double sw[128];
-    __shared__ int rank[128];
+    __shared__ unsigned long long key[kEigMax];
+    __shared__ double sw[kEigMax];
+    __shared__ int rank[kEigMax];
     const int b = blockIdx.y, n = nsz[b];
     const int r0 = blockIdx.x * kSortRows;
     if (r0 >= n) return;
@@ -557,7 +587,7 @@ __global__ void k_frob(const double* __restrict__ A, long stride, int ld, const 
 
 size_t jacobi_smem(int n) {
     const int np = n + (n & 1);
-    return (size_t)3 * np * (np + 1) * sizeof(float);
+    return (size_t)(np <= kJSmemMax ? 3 : 2) * np * (np + 1) * sizeof(float);
 }
 
 // Eigen-decomposition of a batch (nb <= 8) of symmetric matrices of sizes
@@ -567,9 +597,9 @@ size_t jacobi_smem(int n) {
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     if (!E.attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         E.attr_done = true;
     }
     if (seed != kSeedRefine) {
@@ -621,7 +651,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     if (polish) {
         const int np = E.nmax + (E.nmax & 1);
         const size_t psm = (size_t)np * (np + 1) * sizeof(double);
-        if (psm > 200 * 1024) return MG_ERR_ARG;
+        if (psm > (size_t)kSmemOptIn) return MG_ERR_ARG;
         // Rayleigh-Ritz matrix and the FP64 Jacobi polish
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax, none);
         MG_LAUNCHED(c);
@@ -657,12 +687,12 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
 int eig_jacobi_fp64(mg_ctx* c, EigBatch& E) {
     const int np = E.nmax + (E.nmax & 1);
     const size_t psm = (size_t)np * (np + 1) * sizeof(double);
-    if (psm > 200 * 1024) return MG_ERR_ARG;
+    if (psm > (size_t)kSmemOptIn) return MG_ERR_ARG;
     if (!E.attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         E.attr_done = true;
     }
     k_frob<<<E.nb, 1024, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
@@ -744,7 +774,7 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
 extern "C" int mg_eigh_batched(int nb, const int* n, int ld, const double* a, double* w,
                                double* z) {
     using namespace mg;
-    if (nb <= 0 || nb > 64 || !n || !a || !w || !z || ld <= 0 || ld > 128) return MG_ERR_ARG;
+    if (nb <= 0 || nb > 64 || !n || !a || !w || !z || ld <= 0 || ld > kEigMax) return MG_ERR_ARG;
     for (int b = 0; b < nb; ++b)
         if (n[b] < 0 || n[b] > ld) return MG_ERR_ARG;
     mg_ctx tmp;  // a throw-away context carrying only the stream, flags and counters
@@ -851,9 +881,9 @@ int noalloc_setup(int dev, unsigned char** base) {
         void* p = nullptr;
         MG_CUDA(cudaGetSymbolAddress(&p, g_eig_scratch));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     kSmemOptIn));
         cudaFuncAttributes fa;
         MG_CUDA(cudaFuncGetAttributes(&fa, k_gemm64));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_rows));

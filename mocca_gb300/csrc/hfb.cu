@@ -127,7 +127,7 @@ __global__ void k_rho_kappa(const double* __restrict__ X, const int* __restrict_
 __global__ void __launch_bounds__(128)
 k_dn_dlambda(const double* __restrict__ X, const double* __restrict__ E,
              const int* __restrict__ hsz, int nmax, double* __restrict__ dpart) {
-    __shared__ double xm[64];
+    __shared__ double xm[kEigMax / 2];
     __shared__ double red[32];
     const int b = blockIdx.y, h = hsz[b], N = 2 * h;
     const int mm = blockIdx.x;
@@ -341,7 +341,7 @@ int hfb_prepare(mg_ctx* c) {
         H.parity_h[b] = (b % 2) ? 1 : -1;
         hmax = std::max(hmax, H.hsz_h[b]);
     }
-    if (2 * hmax > 128) return MG_ERR_ARG;  // block matrices of the batched eigensolver
+    if (2 * hmax > kEigMax) return MG_ERR_ARG;  // block matrices of the batched eigensolver
     H.hmax = hmax;
     H.nmax = 2 * hmax;
     H.members_h.assign(4 * hmax, 0);

@@ -36,6 +36,7 @@ namespace mg {
 
 constexpr int kMaxN = 64;       // largest supported stored line length
 constexpr int kNumMoments = 64; // capacity of the multipole table
+constexpr int kEigMax = 160;    // largest matrix of the batched eigensolver (HFB block N = 2h)
 
 // One derivative job: a real grid and where its derivatives go.  slot[d] is
 // the Lagrange matrix slot (0 odd, 1 even) along axis d; a NULL output is

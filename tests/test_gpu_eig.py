@@ -74,3 +74,27 @@ def test_hfb_shaped(built):
         mats.append(np.block([[np.diag(e), d], [d.T, -np.diag(e)]]))
     for m, (w, z) in zip(mats, _run(mats)):
         _check(m, w, z)
+
+
+def test_large_blocks(built):
+    """Matrices above 128 (up to the solver's 160): the HFB blocks of a
+    300-spwf run (h up to 80), random, HFB-shaped and clustered, odd sizes
+    included."""
+    rng = np.random.default_rng(4)
+    mats = []
+    for n in (129, 151, 160):
+        x = rng.normal(size=(n, n))
+        mats.append(x + x.T)
+    for h in (75, 80):
+        e = np.sort(rng.uniform(-30, 30, size=h))
+        d = rng.normal(scale=1.5, size=(h, h))
+        d = 0.5 * (d + d.T)
+        mats.append(np.block([[np.diag(e), d], [d.T, -np.diag(e)]]))
+    base = np.repeat(np.linspace(0.0, 1.0, 40), 4)
+    mats.append(_sym(rng, 160, base + 1e-9 * rng.uniform(-1, 1, size=160)))
+    # a density-matrix-like spectrum: occupations clustered at 1 and 0
+    occ = np.concatenate([1.0 - 1e-9 * rng.uniform(0, 1, 60), 1e-9 * rng.uniform(0, 1, 90),
+                          rng.uniform(0, 1, 10)])
+    mats.append(_sym(rng, 160, occ))
+    for m, (w, z) in zip(mats, _run(mats)):
+        _check(m, w, z)
