@@ -10,7 +10,7 @@ DeriveAll, densities, moments, potentials with the Coulomb CG, energy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision mixed|fp64] [--accuracy-iters A] [--breakdown] [--no-micro]
-                  [--no-batch]
+                  [--no-batch] [--no-large]
 
 One JSON line on rank 0.  `value` is the headline form (mixed precision by
 default): K steps with every input resident in HBM (CUDA events on the
@@ -26,12 +26,15 @@ no flush is needed between steps.  Multi-GPU runs are independent replicas
 spinors on the 32^3 symmetry-free box in both precisions, `poisson_64c`
 one Coulomb solve on a 64^3 mesh, and `batched_64_uneven` 64 independent
 Q20-constrained HFB instances of uneven size run concurrently through the
-batch API (after its schedule autotuner) and one after another.
+batch API (after its schedule autotuner) and one after another, and
+`large_36c_300` 200 iterations of N=50, Z=40 on a 36^3 mesh with nwt=300,
+mixed (last 20 in FP64) against FP64.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes as C
+import dataclasses
 import json
 import math
 import os
@@ -432,6 +435,7 @@ def run_ours(args, rank, world, local_rank):
     micro = microbench_c2(torch, stream) if rank == 0 and args.micro else None
     poisson = poisson_64c(torch, stream) if rank == 0 and args.micro else None
     batched = batched_64_uneven(torch) if rank == 0 and args.batch else None
+    large = large_36c_300(torch) if rank == 0 and args.large else None
 
     if rank != 0:
         return None
@@ -483,6 +487,8 @@ def run_ours(args, rank, world, local_rank):
         res["poisson_64c"] = poisson
     if batched:
         res["batched_64_uneven"] = batched
+    if large:
+        res["large_36c_300"] = large
     return res
 
 
@@ -549,6 +555,48 @@ def batched_64_uneven(torch, rounds=20, seq_rounds=5):
     return res
 
 
+def large_36c_300(torch, iters=200, polish=POLISH):
+    """N=50, Z=40 on a 36^3 EV8 stored mesh with nwt=300 (150 n + 150 p),
+    HFB, from the seeded HO start: `iters` iterations of the mixed form
+    (the last `polish` in FP64) and `iters` of the FP64 path, each timed
+    whole with CUDA events; |dE_total| between them."""
+    from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, _abi, synthetic
+    from mocca_gb300.mesh import MeshState
+    p = RunParams(nx=36, ny=36, nz=36, dx=0.8, nwt=300, neutrons=50.0, protons=40.0,
+                  pairing=_abi.MG_PAIRING_HFB)
+    psi, qn, en = synthetic.ho_basis(p, 150, seed=1234)
+    stream = torch.cuda.Stream()
+    out = {"workload": "N=50, Z=40, 36^3 EV8 stored mesh, dx=0.8, nwt=300 (150 n + 150 p), "
+                       "SLy4, HFB G=1250 alpha=1, HO start (seed 1234), dt=0.010, momentum 0.3",
+           "iterations": iters, "fp64_polish": polish}
+    for name, prec in (("mixed", MG_MIXED), ("fp64", MG_FP64)):
+        with torch.cuda.stream(stream):
+            g = MeshState(dataclasses.replace(p, precision=prec), SLY4,
+                          stream=stream.cuda_stream)
+        g.set_spinors(psi, qn)
+        g.set_energies(en)
+        g.set_pairing()
+        g.Start()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        if prec == MG_MIXED:
+            g.Evolve(iters - polish, DT, MOMENTUM)
+            g.set_precision(MG_FP64)
+            e = g.Evolve(polish, DT, MOMENTUM)
+        else:
+            e = g.Evolve(iters, DT, MOMENTUM)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        out[name] = {"value": iters / t, "unit": "iter/s", "ms_per_iter": t / iters * 1e3,
+                     "E_total": e["total"]}
+        g.close()
+    out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["dE_total_MeV"] = out["mixed"]["E_total"] - out["fp64"]["E_total"]
+    return out
+
+
 def stage_breakdown(g, torch, stream):
     out = {}
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
@@ -606,6 +654,8 @@ def main():
                     help="skip the 32^3 mesh-kernel and 64^3 Poisson lines")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the 64-instance batched line")
+    ap.add_argument("--no-large", dest="large", action="store_false",
+                    help="skip the 36^3, nwt=300 line")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run one iteration of --precision between profiler start/stop "
                          "(for ncu --profile-from-start off) and exit")
