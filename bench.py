@@ -622,14 +622,45 @@ def stage_breakdown(g, torch, stream):
     return out
 
 
-def profile_iteration(precision, prepare):
-    """The state after `prepare` iterations (plus 3 warm-up steps), then one
-    HFB iteration between cudaProfilerStart and cudaProfilerStop, for
-    `ncu --profile-from-start off` (launch lists and kernel captures)."""
+def _profile_state(workload, precision, stream):
+    """A prepared context for --profile-iteration: the headline workload, the
+    36^3 nwt=300 one, or the 10^3 Mg24-type HFB start with a Q20 constraint
+    (50 fm^2, on for the first 10 iterations) and ParameterEstimation = 1."""
+    from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, _abi, synthetic
+    from mocca_gb300.mesh import MeshState
+    prec = MG_MIXED if precision == "mixed" else MG_FP64
+    if workload == "headline":
+        _, g = _make(precision, 1234, stream=stream.cuda_stream)
+        return g, PREPARE
+    if workload == "large":
+        p = RunParams(nx=36, ny=36, nz=36, dx=0.8, nwt=300, neutrons=50.0, protons=40.0,
+                      pairing=_abi.MG_PAIRING_HFB, precision=prec)
+        psi, qn, en = synthetic.ho_basis(p, 150, seed=1234)
+        prepare = 5
+    else:
+        p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12.0, protons=12.0,
+                      pairing=_abi.MG_PAIRING_HFB, precision=prec, parameter_estimation=1)
+        psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+        prepare = 2
+    g = MeshState(p, SLY4, stream=stream.cuda_stream)
+    g.set_spinors(psi, qn)
+    g.set_energies(en)
+    g.set_pairing()
+    if workload == "c1q20":
+        g.add_constraint(2, 0, 50.0, 0.0, 10)
+    g.Start()
+    return g, prepare
+
+
+def profile_iteration(precision, workload="headline"):
+    """The state after the workload's preparation iterations (plus 3 warm-up
+    steps), then one HFB iteration between cudaProfilerStart and
+    cudaProfilerStop, for `ncu --profile-from-start off` (launch lists and
+    kernel captures)."""
     import torch
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
-        _, g = _make(precision, 1234, stream=stream.cuda_stream)
+        g, prepare = _profile_state(workload, precision, stream)
     if prepare > 0:
         g.Evolve(prepare, DT, MOMENTUM)
     g.Evolve(3, DT, MOMENTUM)
@@ -656,6 +687,10 @@ def main():
                     help="skip the 64-instance batched line")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 36^3, nwt=300 line")
+    ap.add_argument("--profile-workload", default="headline",
+                    choices=["headline", "large", "c1q20"],
+                    help="state that --profile-iteration prepares: the headline 24^3 "
+                         "workload, the 36^3 nwt=300 one, or the 10^3 Q20-constrained start")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run one iteration of --precision between profiler start/stop "
                          "(for ncu --profile-from-start off) and exit")
@@ -663,7 +698,7 @@ def main():
     if args.profile_iteration:
         import __graft_entry__
         __graft_entry__.build()
-        profile_iteration(args.precision, PREPARE)
+        profile_iteration(args.precision, args.profile_workload)
         print("profiled one iteration")
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
