@@ -130,6 +130,10 @@ typedef struct mg_pairing_params {
     int    max_iter;      /* HFBIter, 50                                    */
     int    guess_kappa;   /* GuessKappa                                     */
     double fermi_start[2];/* initial Fermi energies (module default -10)    */
+    int    fermi_solver;  /* 0: Newton with the analytic dN/dlambda (this    */
+                          /* library's default); 1: the reference's damped   */
+                          /* Broyden search (HFBFindFermiEnergyBroyden,      */
+                          /* src/HFB.f90:1849-2161), iterate for iterate     */
 } mg_pairing_params;
 
 /* Per-call diagnostics of the HFB pairing step. */

@@ -72,7 +72,7 @@ class MgPairingParams(C.Structure):
         ("strength", C.c_double * 2), ("alpha", C.c_double * 2), ("rhosat", C.c_double),
         ("cut", C.c_double * 2), ("mu", C.c_double * 2), ("mix", C.c_double),
         ("fermi_prec", C.c_double), ("max_iter", C.c_int), ("guess_kappa", C.c_int),
-        ("fermi_start", C.c_double * 2),
+        ("fermi_start", C.c_double * 2), ("fermi_solver", C.c_int),
     ]
 
     @classmethod
@@ -89,6 +89,7 @@ class MgPairingParams(C.Structure):
         p.max_iter = 50
         p.guess_kappa = int(guess_kappa)
         p.fermi_start[0] = p.fermi_start[1] = -10.0
+        p.fermi_solver = 0
         return p
 
 

@@ -567,39 +567,30 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
     return MG_OK;
 }
 
-// SolvePairing for HFB (src/Pairing.f90:743-890, PairingIter 1).
-int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
+// ---- particle-number root finder: Newton with the analytic dN/dlambda,
+// safeguarded by the bracket the evaluations build (bisection when a step
+// leaves it, steps clamped to 5 MeV).  On return lam holds the Fermi
+// energies, f the particle-number deviations, conv which isospins met
+// FermiPrec; *first_order tells whether rho and kappa took the last step to
+// first order.
+static int fermi_newton(mg_ctx* c, double lam[2], double f[2], bool conv[2], int* evals_out,
+                        bool* first_order_out) {
     Hfb& H = c->hfb;
-    if (!H.ready) MG_TRY(hfb_prepare(c));
-    const long nm2 = 4L * H.nmax * H.nmax;
-    if (H.oldrho_zero) {
-        MG_CUDA(cudaMemcpyAsync(H.oldrho, H.rho, nm2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-        MG_CUDA(cudaMemcpyAsync(H.oldkappa, H.kappa, nm2 * sizeof(double), cudaMemcpyDeviceToDevice,
-                                c->stream));
-    }
-    H.pc.cut[0] = H.pp.cut[0];
-    H.pc.cut[1] = H.pp.cut[1];
-    H.pc.mu[0] = H.pp.mu[0];
-    H.pc.mu[1] = H.pp.mu[1];
-    MG_CUDA(cudaMemcpyAsync(H.fermi_d, H.fermi, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    MG_CUDA(cudaMemsetAsync(c->flags, 0, 16 * sizeof(int), c->stream));
-    MG_TRY(pairing_mesh(c));
-
-    // ---- particle-number root finder: Newton with the analytic dN/dlambda,
-    // safeguarded by the bracket the evaluations build (bisection when a step
-    // leaves it, steps clamped to 5 MeV) ----------------------------------------
     const double prec = H.pp.fermi_prec;
     int evals = 0;
     // start from the last Fermi energies, linearly extrapolated along the
     // iterations once two converged ones exist (the root is the same; the
     // first evaluation only lands closer to it)
-    double lam[2] = {H.fermi[0], H.fermi[1]}, f[2], fp[2];
+    lam[0] = H.fermi[0];
+    lam[1] = H.fermi[1];
+    double fp[2];
     for (int it = 0; it < 2; ++it)
         if (H.n_solved >= 2 && std::fabs(H.fermi[it] - H.fermi_prev[it]) < 0.5)
             lam[it] = 2.0 * H.fermi[it] - H.fermi_prev[it];
     MG_TRY(hfb_evaluate(c, lam, f, fp, true));
     ++evals;
-    bool conv[2] = {std::fabs(f[0]) < prec, std::fabs(f[1]) < prec};
+    conv[0] = std::fabs(f[0]) < prec;
+    conv[1] = std::fabs(f[1]) < prec;
     double lo[2] = {0, 0}, hi[2] = {0, 0};
     bool has_lo[2] = {false, false}, has_hi[2] = {false, false};
     auto bracket = [&](int it) {
@@ -657,6 +648,94 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
             if (std::fabs(f[it]) < prec) { conv[it] = true; continue; }
             bracket(it);
         }
+    }
+    *evals_out = evals;
+    *first_order_out = first_order;
+    return MG_OK;
+}
+
+// ---- the reference's particle-number search (HFBFindFermiEnergyBroyden,
+// src/HFB.f90:1849-2161, FermiSolver 'BROYDEN'): a second evaluation 0.01 MeV
+// above the start gives the secant slope, then damped (x 0.5) quasi-Newton
+// steps with Broyden's update of the slope, up to HFBIter of them; the slope
+// is replaced by +-1/0.99 when |J| < 0.001.  The same particle-number
+// equation and tolerance as fermi_newton, every step a full evaluation; it
+// follows the reference's iterates, including where they stop short of the
+// tolerance.
+static int fermi_broyden(mg_ctx* c, double lam[2], double f[2], bool conv[2], int* evals_out) {
+    Hfb& H = c->hfb;
+    const double prec = H.pp.fermi_prec;
+    int evals = 0;
+    double fp[2], hist[2] = {H.fermi[0] + 0.01, H.fermi[1] + 0.01}, NX[2], J[2];
+    double upd[2] = {0.0, 0.0}, norm[2] = {1.0, 1.0};
+    lam[0] = H.fermi[0];
+    lam[1] = H.fermi[1];
+    MG_TRY(hfb_evaluate(c, lam, f, fp, true));
+    ++evals;
+    for (int it = 0; it < 2; ++it) conv[it] = std::fabs(f[it]) < prec;
+    MG_TRY(hfb_evaluate(c, hist, NX, fp, false));
+    ++evals;
+    for (int it = 0; it < 2; ++it) J[it] = (f[it] - NX[it]) / (lam[it] - hist[it]);
+    const double step = 0.5;
+    const int maxit = H.pp.max_iter > 0 ? H.pp.max_iter : 50;
+    for (int iter = 1; iter <= maxit; ++iter) {
+        double invJ[2];
+        for (int it = 0; it < 2; ++it)
+            invJ[it] = std::fabs(J[it]) < 0.001 ? (J[it] >= 0 ? 0.99 : -0.99) : 1.0 / J[it];
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            upd[it] = -invJ[it] * f[it];
+            norm[it] = upd[it] * upd[it];
+        }
+        for (int it = 0; it < 2; ++it) upd[it] = step * upd[it];
+        bool far = false;
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            hist[it] = lam[it];
+            lam[it] = lam[it] + upd[it];
+            far = far || std::fabs(upd[it]) > kFarStep;
+        }
+        MG_TRY(hfb_evaluate(c, lam, f, fp, far));
+        ++evals;
+        for (int it = 0; it < 2; ++it)
+            if (std::fabs(f[it]) < prec) conv[it] = true;
+        if (conv[0] && conv[1]) break;
+        if (iter > 1)
+            for (int it = 0; it < 2; ++it) {
+                if (conv[it]) continue;
+                J[it] = J[it] + f[it] * upd[it] / norm[it];
+            }
+    }
+    *evals_out = evals;
+    return MG_OK;
+}
+
+// SolvePairing for HFB (src/Pairing.f90:743-890, PairingIter 1).
+int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
+    Hfb& H = c->hfb;
+    if (!H.ready) MG_TRY(hfb_prepare(c));
+    const long nm2 = 4L * H.nmax * H.nmax;
+    if (H.oldrho_zero) {
+        MG_CUDA(cudaMemcpyAsync(H.oldrho, H.rho, nm2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        MG_CUDA(cudaMemcpyAsync(H.oldkappa, H.kappa, nm2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c->stream));
+    }
+    H.pc.cut[0] = H.pp.cut[0];
+    H.pc.cut[1] = H.pp.cut[1];
+    H.pc.mu[0] = H.pp.mu[0];
+    H.pc.mu[1] = H.pp.mu[1];
+    MG_CUDA(cudaMemcpyAsync(H.fermi_d, H.fermi, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    MG_CUDA(cudaMemsetAsync(c->flags, 0, 16 * sizeof(int), c->stream));
+    MG_TRY(pairing_mesh(c));
+
+    double lam[2], f[2];
+    bool conv[2];
+    int evals = 0;
+    bool first_order = false;
+    if (H.pp.fermi_solver == 1) {
+        MG_TRY(fermi_broyden(c, lam, f, conv, &evals));
+    } else {
+        MG_TRY(fermi_newton(c, lam, f, conv, &evals, &first_order));
     }
     if (conv[0] && conv[1]) {
         H.fermi_prev[0] = H.fermi[0];

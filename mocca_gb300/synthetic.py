@@ -9,6 +9,9 @@ for them:
   (src/InOut.f90:1418-1473), placed in the spinor component whose mirror
   parities match the orbital (the sign rules of
   src/Derivatives.f90:348-439), plus a seeded uniform perturbation.
+* `nilsson_basis` -- the reference's own from-scratch guess (INITWF with the
+  Nilsson-model routine of nil8), restated with numpy, plus a seeded uniform
+  perturbation.
 * `uneven_instances` -- the batched workload: quadrupole-constrained HFB
   runs with random deformation targets, particle numbers, meshes and spwf
   counts.
@@ -179,3 +182,199 @@ def uneven_instances(count: int = 64, seed: int = 7, n_range=(12, 28), dx: float
         out.append({"params": p, "n_neutron": int(n_neutron), "beta2": beta2,
                     "q20": beta2_to_q20(beta2, A), "seed": seed * 1000 + i})
     return out
+
+
+def _nilsson_shell_states(meven: int, modd: int):
+    """Cartesian HO states (nx, ny, nz) of the first `meven` even and `modd`
+    odd major shells in nil8's order (src/nil8.f90:162-268): per shell the
+    four sub-blocks (x, y parities) one after another; returns the states,
+    the shell start offsets and the sub-block sizes of each shell."""
+    states, starts, subs = [], [0], []
+    shells = [2 * (ni - 1) for ni in range(1, meven + 1)] + [2 * ni - 1 for ni in range(1, modd + 1)]
+    for n in shells:
+        ni = n // 2 + 1 if n % 2 == 0 else (n + 1) // 2
+        blocks = []
+        if n % 2 == 0:
+            blocks.append([(2 * (i - 1), 2 * (j - 1)) for i in range(1, ni + 1)
+                           for j in range(1, ni - i + 2)])
+            if ni > 1:
+                blocks.append([(2 * (i - 1) + 1, 2 * (j - 1) + 1) for i in range(1, ni)
+                               for j in range(1, ni - i + 1)])
+                blocks.append([(2 * (i - 1) + 1, 2 * (j - 1)) for i in range(1, ni)
+                               for j in range(1, ni - i + 1)])
+                blocks.append([(2 * (i - 1), 2 * (j - 1) + 1) for i in range(1, ni)
+                               for j in range(1, ni - i + 1)])
+            else:
+                blocks += [[], [], []]
+        else:
+            blocks.append([(2 * (i - 1), 2 * (j - 1)) for i in range(1, ni + 1)
+                           for j in range(1, ni - i + 2)])
+            blocks.append([(2 * i - 1, 2 * j - 1) for i in range(1, ni) for j in range(1, ni - i + 1)])
+            blocks.append([(2 * i - 1, 2 * (j - 1)) for i in range(1, ni + 1)
+                           for j in range(1, ni - i + 2)])
+            blocks.append([(2 * (i - 1), 2 * j - 1) for i in range(1, ni + 1)
+                           for j in range(1, ni - i + 2)])
+        subs.append([len(b) for b in blocks])
+        for b in blocks:
+            states += [(a, c, n - a - c) for (a, c) in b]
+        starts.append(len(states))
+    return states, starts, subs
+
+
+def _nilsson_block_matrix(states, x, y, ax, ay, az):
+    """Nilsson Hamiltonian of one major shell in units of hbar omega0, with
+    stretched l.s (strength kappa = x) and l^2 (x mu = x y) terms
+    (src/nil8.f90:383-433)."""
+    n = len(states)
+    h = np.zeros((n, n))
+    for i in range(n):
+        nx1, ny1, nz1 = states[i]
+        nb = nx1 + ny1 + nz1
+        x1 = 1 - 2 * ((nb - nz1) % 2)
+        x2 = 1 - 2 * (ny1 % 2)
+        for j in range(i, n):
+            nx2, ny2, nz2 = states[j]
+            if j == i:
+                v = (ax * (nx1 + 0.5) + ay * (ny1 + 0.5) + az * (nz1 + 0.5)
+                     - x * y * ((nb * (nb + 1)) / 2.0 - nx1 ** 2 - ny1 ** 2 - nz1 ** 2))
+            elif nx1 == nx2:
+                v = 0.0
+                an, am = float(ny2), float(ny1)
+                if ny2 == ny1 + 1: v = x * math.sqrt(an * nz1)
+                if ny2 == ny1 - 1: v = x * math.sqrt(am * nz2)
+                if ny2 == ny1 + 2: v = -x * y * math.sqrt(an * (ny2 - 1) * nz1 * (nz1 - 1))
+                if ny2 == ny1 - 2: v = -x * y * math.sqrt(am * (ny1 - 1) * nz2 * (nz2 - 1))
+            elif nz1 == nz2:
+                v = 0.0
+                am, an = float(nx1), float(nx2)
+                if nx2 == nx1 + 1: v = -x * x1 * math.sqrt(an * ny1)
+                if nx2 == nx1 - 1: v = -x * x1 * math.sqrt(am * ny2)
+                if nx2 == nx1 + 2: v = -x * y * math.sqrt(an * (nx2 - 1) * ny1 * (ny1 - 1))
+                if nx2 == nx1 - 2: v = -x * y * math.sqrt(am * (nx1 - 1) * ny2 * (ny2 - 1))
+            else:
+                v = 0.0
+                if ny1 == ny2:
+                    x3 = 1.0 - 2.0 * (nx1 % 2)
+                    x4 = 1.0 - 2.0 * (nx2 % 2)
+                    an, am = float(nx2), float(nx1)
+                    if nz2 == nz1 + 1: v = -x * x2 * x3 * math.sqrt(am * nz2)
+                    if nz2 == nz1 - 1: v = -x * x2 * x4 * math.sqrt(an * nz1)
+                    if nz2 == nz1 + 2: v = x * y * math.sqrt(nz2 * (nz2 - 1) * am * (nx1 - 1))
+                    if nz2 == nz1 - 2: v = x * y * math.sqrt(nz1 * (nz1 - 1) * an * (nx2 - 1))
+            h[i, j] = h[j, i] = v
+    return h
+
+
+def _nilsson_hermite(nfun: int, npts: int, xho: float, dx: float) -> np.ndarray:
+    """The 1-D oscillator functions of nil8 on the stored half line
+    (src/nil8.f90:283-339): x^k exp(-x^2/2) built by multiplication,
+    orthogonalised against the lower functions of the same parity and
+    normalised on the mirrored full line."""
+    he = np.zeros((nfun, npts))
+    xs = xho * (np.arange(1, npts + 1) - 0.5)
+    for j in range(1, nfun // 2 + 1):
+        a, b = 2 * j - 2, 2 * j - 1
+        if j == 1:
+            he[0] = np.exp(-xs * xs / 2.0)
+            he[1] = xs * he[0]
+        else:
+            x2 = xs * xs
+            he[a] = he[a - 2] * x2
+            he[b] = he[b - 2] * x2
+            for k in range(1, j):
+                c, d = 2 * k - 2, 2 * k - 1
+                s1 = float(np.sum(he[a] * he[c])) * dx * 2.0
+                s2 = float(np.sum(he[b] * he[d])) * dx * 2.0
+                he[a] = he[a] - s1 * he[c]
+                he[b] = he[b] - s2 * he[d]
+        he[a] *= math.sqrt(0.5 / (dx * float(np.sum(he[a] ** 2))))
+        he[b] *= math.sqrt(0.5 / (dx * float(np.sum(he[b] ** 2))))
+    return he
+
+
+def nilsson_basis(p: RunParams, n_neutron: int, seed: int = 1234, amplitude: float = 1e-3,
+                  meven: int = 6, modd: int = 5, ho=(0.2, 0.2, 0.2)):
+    """The reference's from-scratch guess for an EV8 run: INITWF
+    (src/InOut.f90:1418-1473) calling the Nilsson routine of nil8
+    (src/nil8.f90:16-546) with 6 even and 5 odd shells and m omega / hbar =
+    0.2 fm^-2 on every axis, then a seeded uniform perturbation of the given
+    absolute amplitude on every spinor value (each spwf renormalised).
+
+    Returns (psi[nwt,4,nz,ny,nx], qn[nwt,4], energies) like `ho_basis`:
+    neutrons first (n_neutron of them), positive parity first within each
+    isospin, signature and time simplex +1.  The block diagonalisation uses
+    numpy's symmetric eigensolver, so inside an exactly degenerate Nilsson
+    level the eigenvectors may differ from the reference's diagoncr8 by a
+    rotation (and any vector by its sign).
+    """
+    if not (p.pc and p.sc and p.tsc):
+        raise ValueError("nilsson_basis builds EV8 (all spatial symmetries conserved) states")
+    if max(p.nx, p.ny) > p.nz:
+        raise ValueError("nil8 needs nz >= nx, ny")
+    nwt = p.nwt
+    n_proton = nwt - n_neutron
+    hox, hoy, hoz = ho
+    # the reference passes floor(neutrons) as npp and floor(protons) as npn
+    npp, npn = math.floor(p.neutrons), math.floor(p.protons)
+    xk = (0.08, 0.08, 0.0637, 0.0637)
+    xmu = (0.0, 0.0, 0.42, 0.60)
+    hbm = 6.58218 ** 2 / 1.044673
+    xis = (npn - npp) / (npn + npp)
+    cf = (1.0 + 0.14 * xis, 0.986 - 0.14 * xis)
+    states, starts, subs = _nilsson_shell_states(meven, modd)
+    nvec = len(states)
+    nmax = max(meven, modd)
+    rng = np.random.default_rng(seed)
+    psi = np.zeros((nwt, 4, p.nz, p.ny, p.nx))
+    qn = np.zeros((nwt, 4), dtype=np.int32)
+    en = np.zeros(nwt)
+    w = 0
+    for it, (iso, nw) in enumerate(((-1, n_neutron), (1, n_proton))):
+        nn = max(p.nx, p.ny, p.nz)
+        he = [_nilsson_hermite(2 * nmax, nn, math.sqrt(h) * p.dx * math.sqrt(cf[it]), p.dx)
+              for h in (hox, hoy, hoz)]
+        ho0 = (hox * hoy * hoz) ** (1.0 / 3.0)
+        ax, ay, az = hox / ho0, hoy / ho0, hoz / ho0
+        ho0 = ho0 * hbm * cf[it]
+        npart = npn if it == 0 else npp
+        x, y = (xk[it], xmu[it]) if npart <= 50 else (xk[it + 2], xmu[it + 2])
+        e = np.zeros(nvec)
+        vecs = []
+        for b in range(len(starts) - 1):
+            h = _nilsson_block_matrix(states[starts[b]:starts[b + 1]], x, y, ax, ay, az)
+            d, s = np.linalg.eigh(h)
+            vecs.append(s)
+            e[starts[b]:starts[b + 1]] = d * ho0 - 50.0
+        # exchange sort of nil8 (src/nil8.f90:437-449): ties keep its order
+        nor = list(range(nvec))
+        ev = e.copy()
+        for i in range(nvec - 1):
+            for j in range(i + 1, nvec):
+                if ev[j] < ev[i]:
+                    ev[i], ev[j] = ev[j], ev[i]
+                    nor[i], nor[j] = nor[j], nor[i]
+        npa = [1 - 2 * (sum(states[nor[i]]) % 2) for i in range(nvec)]
+        order = [i for i in range(nw) if npa[i] != -1] + [i for i in range(nw) if npa[i] != 1]
+        for i in order:
+            j = nor[i]
+            b = next(k for k in range(len(starts) - 1) if j < starts[k + 1])
+            s = vecs[b][:, j - starts[b]]
+            g = np.zeros((4, p.nz, p.ny, p.nx))
+            off = 0
+            for k in range(4):
+                flip = 3 if k in (0, 2) else 0
+                for q in range(off, off + subs[b][k]):
+                    a1, a2, a3 = states[starts[b] + q]
+                    xph = s[q]
+                    if (a2 + 1) % 4 == flip:
+                        xph = -xph
+                    g[k] += xph * (he[2][a3, :p.nz][:, None, None] * he[1][a2, :p.ny][None, :, None]
+                                   * he[0][a1, :p.nx][None, None, :])
+                off += subs[b][k]
+            g += amplitude * rng.uniform(-1.0, 1.0, size=g.shape)
+            g /= math.sqrt(float(np.sum(g ** 2)) * p.dv)
+            psi[w] = g
+            qn[w] = (iso, npa[i], 1, 1)
+            en[w] = ev[i]
+            w += 1
+    return psi, qn, en

@@ -38,7 +38,49 @@ def mg24_hf():
     }
 
 
+C1_CHECKPOINTS = (1, 10, 11, 20, 50, 100)
+
+
+def c1_state():
+    """The Mg24 run of the reference README (the CPU-runnable configuration):
+    10^3 stored EV8 mesh, dx=0.8, nwt=40 (20 n + 20 p) from the Nilsson
+    guess plus a seeded uniform perturbation of 1e-3, SLy4, HFB (G=1250,
+    alpha=1, GuessKappa), MixingScheme 2, ParameterEstimation 1, a Q20
+    constraint of 50 fm^2 for the first 10 iterations."""
+    from mocca_gb300 import _abi
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB, mixing_scheme=2, parameter_estimation=1)
+    psi, qn, en = synthetic.nilsson_basis(p, 20, seed=1234)
+    return p, psi, qn, en
+
+
+def mg24_c1():
+    p, psi, qn, en = c1_state()
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.set_pairing()
+    o.add_constraint(2, 0, 50.0, 0.0, 10)
+    o.Start()
+    rows = []
+    for k in range(1, C1_CHECKPOINTS[-1] + 1):
+        e = o.Evolve(1, 0.010, 0.3)
+        if k in C1_CHECKPOINTS:
+            dt, mom = o.StepParameters()
+            rows.append({"iteration": k, "E_total": e["total"], "pairing": e["pairing"],
+                         "q20": sum(o.get_constraint(0)["value"]), "dt": dt, "momentum": mom})
+    return {
+        "config": "Mg24 README run: N=Z=12, EV8+TRC, 10^3 stored mesh, dx=0.8, nwt=40, SLy4, "
+                  "HFB G=1250 alpha=1 GuessKappa, Nilsson start (6 even + 5 odd shells, "
+                  "m omega/hbar=0.2) + uniform perturbation 1e-3 seed 1234, MixingScheme 2, "
+                  "ParameterEstimation 1 (dt 0.010, momentum 0.3 seed the estimation), "
+                  "Q20 constraint 50 fm^2 for 10 iterations, 100 iterations",
+        "checkpoints": rows,
+    }
+
+
 if __name__ == "__main__":
-    out = Path(__file__).resolve().parent / "mg24_hf.json"
-    out.write_text(json.dumps(mg24_hf(), indent=1))
-    print(out)
+    here = Path(__file__).resolve().parent
+    (here / "mg24_hf.json").write_text(json.dumps(mg24_hf(), indent=1))
+    (here / "mg24_c1.json").write_text(json.dumps(mg24_c1(), indent=1))
+    print(here)

@@ -295,3 +295,45 @@ def test_q20_constraint_moves_the_moment_then_switches_off():
     st = o.get_constraint(k)
     assert not st["active"]
     assert np.abs(o.get_constraint_fields()[1]).max() == 0.0
+
+
+def test_nilsson_start():
+    """The restated Nilsson guess (nil8 via INITWF): orthonormal inside every
+    (isospin, parity) block, proton levels those of the neutrons scaled by
+    the proton oscillator factor, positive parity first within each isospin,
+    the s1/2 level at 1.5 hbar omega above the -50 MeV shift."""
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12)
+    psi, qn, en = synthetic.nilsson_basis(p, 20, amplitude=0.0)
+    S = np.einsum("iczyx,jczyx->ij", psi, psi) * p.dv
+    same = (qn[:, 0][:, None] == qn[:, 0][None, :]) & (qn[:, 1][:, None] == qn[:, 1][None, :])
+    assert np.abs((S - np.eye(40)) * same).max() < 1e-13
+    # N = Z: the proton oscillator is scaled by ca = 0.986 (src/nil8.f90:124, :271-274)
+    assert np.allclose(en[20:] + 50.0, 0.986 * (en[:20] + 50.0), atol=1e-12)
+    for iso in (-1, 1):
+        par = qn[qn[:, 0] == iso, 1]
+        assert np.all(np.diff(par) <= 0) and par[0] == 1
+    # the lowest level is the s1/2 state, 1.5 hbar omega above -50 MeV minus
+    # the l^2 shift (none for kappa mu = 0 below 50 particles)
+    hw = 0.2 * 6.58218 ** 2 / 1.044673
+    assert en[0] == pytest.approx(-50.0 + 1.5 * hw, abs=1e-9)
+    # the perturbed start keeps the same shapes and quantum numbers
+    psi2, qn2, en2 = synthetic.nilsson_basis(p, 20, seed=1234)
+    assert np.array_equal(qn2, qn) and np.array_equal(en2, en)
+    assert 0 < np.abs(psi2 - psi).max() < 2e-2
+
+
+def test_golden_c1_fixture():
+    """The README Mg24 run (Nilsson start, HFB, MixingScheme 2,
+    ParameterEstimation 1, Q20 constraint for 10 iterations, 100 iterations)
+    in the oracle reproduces the committed checkpoints (make_golden.py; the
+    Nilsson start is rebuilt here with the same numpy)."""
+    import sys
+    sys.path.insert(0, str(GOLDEN))
+    import make_golden
+    g = json.loads((GOLDEN / "mg24_c1.json").read_text())
+    d = make_golden.mg24_c1()
+    for a, b in zip(d["checkpoints"], g["checkpoints"]):
+        assert a["iteration"] == b["iteration"]
+        assert a["E_total"] == pytest.approx(b["E_total"], abs=1e-9), a["iteration"]
+        assert a["q20"] == pytest.approx(b["q20"], abs=1e-9)
+        assert a["dt"] == pytest.approx(b["dt"], rel=1e-12)
