@@ -391,11 +391,17 @@ int mg_batch_tune(mg_batch* b, int probe, const double* dt, const double* moment
 int mg_batch_set_workers(mg_batch* b, int workers);
 /* n_iter Evolve passes of every instance (mg_iterate with dt[i],
  * momentum[i]); out (n entries, may be NULL) receives each instance's last
- * energy.  Returns when all instances' work is complete: the first negative
- * status of any instance, else MG_NOT_CONVERGED if any Coulomb solve hit its
- * cap, else MG_OK. */
+ * energy.  An instance whose pass fails is marked failed and skipped from
+ * then on (the reference would stop that nucleus's run); the others carry
+ * on.  Returns when all instances' work is complete: a negative status if
+ * any instance failed in this call, else MG_NOT_CONVERGED if any Coulomb
+ * solve hit its cap, else MG_OK.  mg_batch_tune treats failures the same
+ * way. */
 int mg_batch_iterate(mg_batch* b, int n_iter, const double* dt, const double* momentum,
                      mg_energy_terms* out);
+/* Per-instance status after the last call (n ints): MG_OK, MG_NOT_CONVERGED,
+ * or the negative status with which the instance failed. */
+int mg_batch_status(mg_batch* b, int* status);
 
 /* Number of kernels this context has launched so far (instrumentation; the
  * reference's only counterpart is the CoulombTime accumulator,

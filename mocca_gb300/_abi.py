@@ -195,6 +195,7 @@ SIGNATURES = {
     "mg_batch_destroy": [_P],
     "mg_batch_tune": [_P, C.c_int, _D, _D, _I],
     "mg_batch_set_workers": [_P, C.c_int],
+    "mg_batch_status": [_P, _I],
     "mg_batch_iterate": [_P, C.c_int, _D, _D, C.POINTER(MgEnergyTerms)],
     "mg_eigh_batched": [C.c_int, _I, C.c_int, _D, _D, _D],
     "mg_eigh_batched_noalloc": [C.c_int, _I, C.c_int, _P, _P, _P, _P],

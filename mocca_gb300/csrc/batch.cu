@@ -24,6 +24,7 @@ struct mg_batch {
     std::vector<mg_ctx*> ctx;
     std::vector<double> cost;                // seconds per Evolve pass (measured, or a model)
     std::vector<std::vector<int>> lists;     // per worker: instance indices
+    std::vector<int> status;                 // per instance: last status (< 0: failed, skipped)
     int device = 0;
     int workers = 1;
 };
@@ -57,19 +58,28 @@ void assign(mg_batch* b, int workers) {
 int run(mg_batch* b, int n_iter, const double* dt, const double* mom, mg_energy_terms* out) {
     const int W = (int)b->lists.size();
     std::vector<int> status(W, MG_OK);
+    // An instance whose pass fails (negative status) is marked failed and
+    // skipped from then on; the others carry on.  A worker reports the first
+    // failure it saw, else the largest positive status.
     auto work = [&](int w) {
         if (cudaSetDevice(b->device) != cudaSuccess) { status[w] = MG_ERR_CUDA; return; }
         int st = MG_OK;
-        for (int k = 0; k < n_iter && st >= 0; ++k)
+        for (int k = 0; k < n_iter; ++k)
             for (int i : b->lists[w]) {
+                if (b->status[i] < 0) continue;
                 const int s = mg_iterate(b->ctx[i], 1, dt[i], mom[i], out ? &out[i] : nullptr);
-                if (s < 0) { st = s; break; }
-                st = std::max(st, s);
+                b->status[i] = s;
+                if (s < 0) { if (st >= 0) st = s; continue; }
+                if (st >= 0) st = std::max(st, s);
             }
         // every instance's work is complete when the call returns
         for (int i : b->lists[w]) {
+            if (b->status[i] < 0) continue;
             const int s = mg_synchronize(b->ctx[i]);
-            if (s < 0 && st >= 0) st = s;
+            if (s < 0) {
+                b->status[i] = s;
+                if (st >= 0) st = s;
+            }
         }
         status[w] = st;
     };
@@ -102,6 +112,7 @@ extern "C" int mg_batch_create(int n, mg_ctx* const* ctxs, mg_batch** out) {
     // cost model until measured: mesh work ~ nwt V per basis
     for (mg_ctx* c : b->ctx)
         b->cost.push_back((double)c->p.nwt * (double)c->V * (c->p.pairing == MG_PAIRING_HFB ? 2 : 1));
+    b->status.assign(n, MG_OK);
     if (cudaGetDevice(&b->device) != cudaSuccess) { delete b; return MG_ERR_CUDA; }
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
     assign(b, std::min(n, hw));
@@ -111,6 +122,12 @@ extern "C" int mg_batch_create(int n, mg_ctx* const* ctxs, mg_batch** out) {
 
 extern "C" int mg_batch_destroy(mg_batch* b) {
     delete b;
+    return MG_OK;
+}
+
+extern "C" int mg_batch_status(mg_batch* b, int* status) {
+    if (!b || !status) return MG_ERR_ARG;
+    for (size_t i = 0; i < b->status.size(); ++i) status[i] = b->status[i];
     return MG_OK;
 }
 
@@ -132,13 +149,18 @@ extern "C" int mg_batch_tune(mg_batch* b, int probe, const double* dt, const dou
     const int n = (int)b->ctx.size();
     // 1. each instance alone: its iteration time (this also makes every
     //    allocation an instance does lazily on its first passes)
+    int first_err = MG_OK;
     for (int i = 0; i < n; ++i) {
         double best = 1e30;
-        for (int k = 0; k < probe; ++k) {
-            MG_TRY(mg_synchronize(b->ctx[i]));
+        for (int k = 0; k < probe && b->status[i] >= 0; ++k) {
             const double t0 = now_s();
-            MG_TRY(mg_iterate(b->ctx[i], 1, dt[i], momentum[i], nullptr));
-            MG_TRY(mg_synchronize(b->ctx[i]));
+            int s = mg_iterate(b->ctx[i], 1, dt[i], momentum[i], nullptr);
+            if (s >= 0) {
+                const int s2 = mg_synchronize(b->ctx[i]);
+                if (s2 < 0) s = s2;
+            }
+            b->status[i] = s;
+            if (s < 0 && first_err == MG_OK) first_err = s;
             best = std::min(best, now_s() - t0);
         }
         b->cost[i] = best;
@@ -153,11 +175,12 @@ extern "C" int mg_batch_tune(mg_batch* b, int probe, const double* dt, const dou
     for (int w : cand) {
         assign(b, w);
         const double t0 = now_s();
-        MG_TRY(run(b, probe, dt, momentum, nullptr));
+        const int s = run(b, probe, dt, momentum, nullptr);
+        if (s < 0 && first_err == MG_OK) first_err = s;
         const double t = now_s() - t0;
         if (t < best_t) { best_t = t; best_w = b->workers; }
     }
     assign(b, best_w);
     if (workers_out) *workers_out = best_w;
-    return MG_OK;
+    return first_err;
 }

@@ -331,13 +331,22 @@ class Batch:
             raise _abi.MgError("mg_batch_set_workers", w)
         return w
 
-    def Evolve(self, n_iter: int, dt, momentum) -> list[dict]:
+    def Evolve(self, n_iter: int, dt, momentum, allow_failures: bool = False) -> list[dict]:
+        """n_iter passes of every instance; a failed instance is skipped from
+        then on (see status()); with allow_failures the call returns instead
+        of raising when one fails."""
         d, m = self._vec(dt), self._vec(momentum)
         out = (_abi.MgEnergyTerms * len(self.states))()
-        _abi.check("mg_batch_iterate", self.lib.mg_batch_iterate(self.h, int(n_iter), _dptr(d),
-                                                                  _dptr(m), out),
-                   allow_not_converged=True)
+        st = self.lib.mg_batch_iterate(self.h, int(n_iter), _dptr(d), _dptr(m), out)
+        if st < 0 and not allow_failures:
+            raise _abi.MgError("mg_batch_iterate", st)
         return [e.as_dict() for e in out]
+
+    def status(self) -> list[int]:
+        """Per-instance status after the last call (negative: failed, skipped)."""
+        st = np.zeros(len(self.states), dtype=np.int32)
+        _abi.check("mg_batch_status", self.lib.mg_batch_status(self.h, st.ctypes.data_as(_abi._I)))
+        return st.tolist()
 
     def close(self):
         if getattr(self, "h", None):

@@ -62,3 +62,30 @@ def test_batch_tune_and_continue(built):
     b.close()
     for s in states:
         s.close()
+
+
+def test_batch_failed_instance_is_skipped(built):
+    """An instance that fails (here: no spinors were ever uploaded, which the
+    library reports as MG_ERR_STATE before any device work) is marked failed
+    and skipped; the other instances of the batch carry on unchanged."""
+    inst = _instances(3, seed=13)
+    alone = []
+    for d in (inst[0], inst[2]):
+        g = _state(d)
+        alone.append(g.Evolve(2, 0.010, 0.3)["total"])
+        g.close()
+    states = [_state(inst[0]), MeshState(inst[1]["params"], SLY4), _state(inst[2])]
+    b = Batch(states)
+    b.set_workers(2)
+    out = b.Evolve(2, 0.010, 0.3, allow_failures=True)
+    st = b.status()
+    assert st[1] == _abi.MG_ERR_STATE and st[0] >= 0 and st[2] >= 0
+    for e_b, e_a in zip((out[0]["total"], out[2]["total"]), alone):
+        assert abs(e_b - e_a) <= 1e-10 * max(1.0, abs(e_a)), (e_b, e_a)
+    # later calls skip it and report the healthy instances' status
+    out = b.Evolve(1, 0.010, 0.3)
+    assert np.isfinite(out[0]["total"]) and np.isfinite(out[2]["total"])
+    assert b.status()[1] == _abi.MG_ERR_STATE
+    b.close()
+    for s in states:
+        s.close()
