@@ -416,12 +416,49 @@ int build_basis_jobs(mg_ctx* c, int b) {
     return MG_OK;
 }
 
+// Tile autotuner of the x/y kernels: z planes per block trade the per-block
+// staging of the axis matrices against parallelism, and the best count
+// depends on the mesh and on how many grids a call derives.  On the first
+// call of each (form, grid-count class) every candidate (1, 2, 4, 8 planes,
+// at most nz) runs twice on the real jobs, timed with events on the
+// context's stream, and the fastest is kept.  The x/y kernel writes the
+// same values whatever the count (every line is computed the same way), so
+// the repeated runs leave the outputs as one run does; the z kernel, which
+// adds to the Laplacian, runs once afterwards.
+template <class Launch>
+static int tuned_planes(mg_ctx* c, int& slot, Launch launch_xy) {
+    if (slot > 0) return MG_OK;
+    const int cand[4] = {1, 2, 4, 8};
+    cudaEvent_t ev[2];
+    MG_CUDA(cudaEventCreate(&ev[0]));
+    MG_CUDA(cudaEventCreate(&ev[1]));
+    float best = 1e30f;
+    int best_p = 1;
+    int st = MG_OK;
+    for (int p : cand) {
+        if (p > c->nz && p > 1) break;
+        if ((st = launch_xy(p)) != MG_OK) break;            // warm-up
+        if (cudaEventRecord(ev[0], c->stream) != cudaSuccess) { st = MG_ERR_CUDA; break; }
+        for (int r = 0; r < 2 && st == MG_OK; ++r) st = launch_xy(p);
+        if (st != MG_OK) break;
+        float ms = 0.0f;
+        if (cudaEventRecord(ev[1], c->stream) != cudaSuccess ||
+            cudaEventSynchronize(ev[1]) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess) { st = MG_ERR_CUDA; break; }
+        if (ms < best) { best = ms; best_p = p; }
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (st == MG_OK) slot = best_p;
+    return st;
+}
+
 int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     if (njobs <= 0) return MG_OK;
     const int nx = c->nx, ny = c->ny, nz = c->nz;
-    // z planes per k_deriv_xy block: one when few grids (densities, fields)
-    // would leave most SMs idle
-    const int ppb = njobs < 64 ? 1 : 4;
+    // z planes per k_deriv_xy block, tuned per (form, grid-count class):
+    // few grids (densities, fields) and whole bases
+    int& ppb = c->deriv_planes[c->cur_precision == MG_MIXED ? 1 : 0][njobs < 64 ? 0 : 1];
     // once per process (contexts of a batch call this from several threads)
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
@@ -444,9 +481,14 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
         const size_t sm_z = (size_t)(4 * nz * mp.ld4[2] + 2 * nz * kColTile) * sizeof(float);
         const int txy = std::min(256, div_up((long)nx * ny4, 32) * 32);
         const int tz = std::min(512, kColTile * nz4);
-        k_deriv_xy_df<<<dim3(njobs, div_up(nz, ppb)), txy, sm_xy, c->stream>>>(jobs, mp, nx, ny,
-                                                                             nz, ppb, out_df);
-        MG_LAUNCHED(c);
+        auto xy = [&](int p) {
+            k_deriv_xy_df<<<dim3(njobs, div_up(nz, p)), txy, sm_xy, c->stream>>>(jobs, mp, nx, ny,
+                                                                               nz, p, out_df);
+            MG_LAUNCHED(c);
+            return MG_OK;
+        };
+        if (ppb == 0) MG_TRY(tuned_planes(c, ppb, xy));
+        MG_TRY(xy(ppb));
         k_deriv_z_df<<<dim3(njobs, div_up((long)nx * ny, kColTile)), tz, sm_z, c->stream>>>(
             jobs, mp, nx, ny, nz, out_df ? 1 : 0);
         MG_LAUNCHED(c);
@@ -456,9 +498,14 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     MatPtrs mp = mat_ptrs(c);
     size_t sm_xy = (size_t)(2 * nx * nx + 2 * ny * ny + nx * ny) * sizeof(double);
     size_t sm_z = (size_t)(2 * nz * nz + nz * kColTile) * sizeof(double);
-    dim3 gxy(njobs, div_up(nz, ppb));
-    k_deriv_xy<<<gxy, kThreads, sm_xy, c->stream>>>(jobs, mp, nx, ny, nz, ppb);
-    MG_LAUNCHED(c);
+    auto xy = [&](int p) {
+        k_deriv_xy<<<dim3(njobs, div_up(nz, p)), kThreads, sm_xy, c->stream>>>(jobs, mp, nx, ny,
+                                                                              nz, p);
+        MG_LAUNCHED(c);
+        return MG_OK;
+    };
+    if (ppb == 0) MG_TRY(tuned_planes(c, ppb, xy));
+    MG_TRY(xy(ppb));
     dim3 gz(njobs, div_up((long)nx * ny, kColTile));
     k_deriv_z<<<gz, kThreads, sm_z, c->stream>>>(jobs, mp, nx, ny, nz);
     MG_LAUNCHED(c);

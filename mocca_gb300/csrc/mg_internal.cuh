@@ -214,6 +214,10 @@ struct mg_ctx {
     int tc_N[3] = {0, 0, 0};
     bool tc_ok = false;           // every line length <= 32
 
+    // z planes per block of the Lagrange x/y kernels, [0 FP64, 1 double-float]
+    // x [0 few grids, 1 whole bases]; 0 until deriv.cu's autotuner picks one
+    int deriv_planes[2][2] = {{0, 0}, {0, 0}};
+
     mg::Basis bas[2];
     double* updates = nullptr;   // nwt*4V heavy-ball history
     double* hbuf = nullptr;      // nwt*4V h.psi scratch
