@@ -403,6 +403,34 @@ int mg_batch_iterate(mg_batch* b, int n_iter, const double* dt, const double* mo
  * or the negative status with which the instance failed. */
 int mg_batch_status(mg_batch* b, int* status);
 
+/* Convergence thresholds of ConvergenceCheck (src/Main.f90:358-397), the
+ * &GenInfo values: EnergyPrec (default 0.01E-08, a single-precision
+ * literal), MomentPrec and PairingPrec (1e-4). */
+typedef struct mg_convergence {
+    double energy_prec;   /* relative change of E_total against each of the last 7 */
+    double moment_prec;   /* constrained moments against their running targets     */
+    double pairing_prec;  /* Fermi energies (HFB)                                   */
+} mg_convergence;
+
+/* ConvergenceCheck (src/Main.f90:358-397): ConverMultipoleAll
+ * (src/Moments.f90:2628-2701, constrained moments, value and the 7 previous
+ * ones against the running target), ConverEnergy (src/Energy.f90:1458-1481,
+ * E_total against the 7 previous CompEnergy results; mg_energy and every
+ * mg_iterate pass that computes the energy shift that history) and
+ * ConverFermi (src/Pairing.f90:1048-1070).  ConverFermi compares the Fermi
+ * energies with a history that the reference never writes (zeros), so an
+ * HFB run only passes when both |Fermi| <= PairingPrec: in practice HFB runs
+ * go to MaxIter, as in the reference.  prec may be NULL (defaults).  A total
+ * energy >= 0 returns MG_ERR_STATE (the reference stops: 'Positive total
+ * energy!'). */
+int mg_convergence_check(mg_ctx* ctx, const mg_convergence* prec, int* converged);
+/* The Evolve loop (src/Main.f90:255-328): up to max_iter passes of
+ * mg_iterate, each followed by mg_convergence_check, leaving the loop when
+ * it passes.  iterations (may be NULL): passes run; converged (may be NULL);
+ * out (may be NULL): the last energy. */
+int mg_evolve(mg_ctx* ctx, int max_iter, double dt, double momentum, const mg_convergence* prec,
+              int* iterations, int* converged, mg_energy_terms* out);
+
 /* Number of kernels this context has launched so far (instrumentation; the
  * reference's only counterpart is the CoulombTime accumulator,
  * src/Coulomb.f90:288, :333-334). */

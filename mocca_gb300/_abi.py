@@ -147,6 +147,11 @@ class MgConstraintState(C.Structure):
                 "active": bool(self.active)}
 
 
+class MgConvergence(C.Structure):
+    _fields_ = [("energy_prec", C.c_double), ("moment_prec", C.c_double),
+                ("pairing_prec", C.c_double)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -191,6 +196,9 @@ SIGNATURES = {
     "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
     "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "mg_convergence_check": [_P, C.POINTER(MgConvergence), _I],
+    "mg_evolve": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgConvergence), _I, _I,
+                  C.POINTER(MgEnergyTerms)],
     "mg_batch_create": [C.c_int, _PP, C.POINTER(_P)],
     "mg_batch_destroy": [_P],
     "mg_batch_tune": [_P, C.c_int, _D, _D, _I],

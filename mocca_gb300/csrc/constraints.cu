@@ -296,6 +296,10 @@ int constraint_moments(mg_ctx* c) {
     ConsCoef cf{};
     for (int q = 0; q < nc; ++q) {
         MomentConstraint& k = K.list[q];
+        // OldValue shifts and takes the previous Value (SaveOld = 1,
+        // src/Moments.f90:1921-1931)
+        for (int i = 6; i > 0; --i) k.old_value[i] = k.old_value[i - 1];
+        k.old_value[0] = k.value[0] + k.value[1];
         for (int it = 0; it < 2; ++it) {
             k.value[it] = K.h_red[4 * q + it];
             k.squared[it] = K.h_red[4 * q + 2 + it];
@@ -354,6 +358,26 @@ int alternate_step(mg_ctx* c) {
         MG_LAUNCHED(c);
     }
     return gram_schmidt(c);
+}
+
+// ConverMultipoleAll (src/Moments.f90:2628-2701) over the constrained moments.
+bool moments_converged(const mg_ctx* c, double prec) {
+    for (const MomentConstraint& k : c->cons.list) {
+        if (k.type == 0) continue;
+        const double C = k.constraint;
+        double d[8];
+        const double v = k.value[0] + k.value[1];
+        if (k.true_constraint != 0.0) {
+            d[0] = std::fabs((C - v) / C);
+            for (int i = 1; i < 8; ++i) d[i] = std::fabs((C - k.old_value[i - 1]) / C);
+        } else {
+            d[0] = std::fabs(C - v);
+            for (int i = 1; i < 8; ++i) d[i] = std::fabs(C - k.old_value[i - 1]);
+        }
+        for (int i = 0; i < 8; ++i)
+            if (d[i] >= prec) return false;
+    }
+    return true;
 }
 
 void constraints_free(mg_ctx* c) {

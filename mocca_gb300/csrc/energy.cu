@@ -211,6 +211,10 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     const double com = out->com[0][0] + out->com[1][0] + out->com[0][1] + out->com[1][1];
     out->total = sk + (out->kinetic[0] + out->kinetic[1]) + ec + com + ex +
                  (out->pairing[0] + out->pairing[1]);
+    // OldEnergy shifts and takes the previous TotalEnergy (src/Energy.f90:93-98)
+    for (int i = 6; i > 0; --i) c->old_energy[i] = c->old_energy[i - 1];
+    c->old_energy[0] = c->total_energy;
+    c->total_energy = out->total;
     double sp = 0.0;
     for (int i = 0; i < nwt; ++i) sp += occ[i] * e[i];
     sp = 0.5 * (sp + (out->kinetic[0] + out->kinetic[1])) -

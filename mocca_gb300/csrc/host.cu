@@ -655,3 +655,51 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
     MG_TRY(tc_check(c));
     return st;
 }
+
+// ---------------------------------------------------------------------------
+// ConvergenceCheck and the Evolve loop
+// ---------------------------------------------------------------------------
+static mg_convergence default_convergence() {
+    // &GenInfo defaults (src/GenInfo.f90:54-55); EnergyPrec = 0.01E-08 is a
+    // default-kind (single precision) literal
+    return mg_convergence{(double)0.01e-8f, 1e-4, 1e-4};
+}
+
+extern "C" int mg_convergence_check(mg_ctx* c, const mg_convergence* prec, int* converged) {
+    if (!c || !converged) return MG_ERR_ARG;
+    const mg_convergence P = prec ? *prec : default_convergence();
+    bool conv = moments_converged(c, P.moment_prec);
+    const double E = c->total_energy;
+    for (int i = 0; i < 7 && conv; ++i)   // ConverEnergy, src/Energy.f90:1458-1481
+        conv = conv && std::fabs((c->old_energy[i] - E) / E) <= P.energy_prec;
+    if (c->p.pairing == MG_PAIRING_HFB)   // ConverFermi: the history stays zero
+        for (int it = 0; it < 2; ++it)
+            if (std::fabs(c->hfb.fermi[it] - 0.0) > P.pairing_prec) conv = false;
+    *converged = conv ? 1 : 0;
+    if (E >= 0.0) {
+        fprintf(stderr, "mocca_gpu: positive total energy (%.6f MeV)\n", E);
+        return MG_ERR_STATE;
+    }
+    return MG_OK;
+}
+
+extern "C" int mg_evolve(mg_ctx* c, int max_iter, double dt, double momentum,
+                         const mg_convergence* prec, int* iterations, int* converged,
+                         mg_energy_terms* out) {
+    if (!c || max_iter < 0) return MG_ERR_ARG;
+    mg_energy_terms e{};
+    int st = MG_OK, conv = 0, k = 0;
+    while (k < max_iter) {
+        ++k;
+        const int s = mg_iterate(c, 1, dt, momentum, &e);
+        if (s < 0) { st = s; break; }
+        st = std::max(st, s);
+        const int sc = mg_convergence_check(c, prec, &conv);
+        if (sc < 0) { st = sc; break; }
+        if (conv) break;
+    }
+    if (iterations) *iterations = k;
+    if (converged) *converged = conv;
+    if (out) *out = e;
+    return st;
+}

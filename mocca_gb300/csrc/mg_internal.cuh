@@ -163,6 +163,7 @@ struct MomentConstraint {
     double true_constraint = 0.0;
     double intensity = 0.0;     // 0: estimated on the first readjustment
     double value[2] = {0.0, 0.0}, squared[2] = {0.0, 0.0};
+    double old_value[7] = {0, 0, 0, 0, 0, 0, 0};   // sums of OldValue(:, 1..7)
     bool started = false;       // moments computed once (running target set)
 };
 
@@ -299,6 +300,11 @@ struct mg_ctx {
     // multipole constraints (constraints.cu) and the Evolve iteration count
     mg::Constraints cons;
     int iteration = 0;
+
+    // ConvergenceCheck histories: OldEnergy(7) and the last TotalEnergy
+    // (src/Energy.f90:34, :93-98)
+    double old_energy[7] = {0, 0, 0, 0, 0, 0, 0};
+    double total_energy = 0.0;
 };
 
 namespace mg {
@@ -357,6 +363,7 @@ int constraint_moments(mg_ctx* c);
 int alternate_step(mg_ctx* c);
 void readjust_moments(mg_ctx* c, int iteration);
 bool any_alternating(const mg_ctx* c);
+bool moments_converged(const mg_ctx* c, double prec);
 void constraints_free(mg_ctx* c);
 
 // Lagrange matrix slot selection of Opt_LAG{X,Y,Z}_EV8 / Lapla_LAG_EV8.

@@ -253,6 +253,24 @@ class MeshState:
                    allow_not_converged=True)
         return e.as_dict()
 
+    def ConvergenceCheck(self, prec=None) -> bool:
+        """ConvergenceCheck (src/Main.f90:358-397); prec: MgConvergence or None."""
+        conv = C.c_int(0)
+        self._call("mg_convergence_check", C.byref(prec) if prec is not None else None,
+                   C.byref(conv))
+        return bool(conv.value)
+
+    def EvolveUntilConverged(self, max_iter: int, dt: float, momentum: float = 0.0,
+                             prec=None):
+        """The Evolve loop with its convergence exit (mg_evolve): returns
+        (energy terms, iterations run, converged)."""
+        e = _abi.MgEnergyTerms()
+        n, conv = C.c_int(0), C.c_int(0)
+        self._call("mg_evolve", int(max_iter), C.c_double(dt), C.c_double(momentum),
+                   C.byref(prec) if prec is not None else None, C.byref(n), C.byref(conv),
+                   C.byref(e), allow_not_converged=True)
+        return e.as_dict(), n.value, bool(conv.value)
+
     def set_pairing(self, pp=None):
         """&Pairing values of an HFB run (defaults: the README Mg24 input)."""
         pp = pp if pp is not None else _abi.MgPairingParams.defaults()
@@ -289,8 +307,12 @@ class MeshState:
             self.HFFill()
         self.DeriveAll()
         self.UpdateDensities()
-        self.CalculateAllMoments()
+        # three times, as the reference does (src/Main.f90:219-221): the
+        # moments' OldValue history then holds the start value thrice
+        for _ in range(3):
+            self.CalculateAllMoments()
         it = self.ConstructPotentials()
+        self.CompEnergy()   # src/Main.f90:223: the energy history starts here
         if hfb:
             self.hPsi(_abi.MG_CAN_BASIS, want_spinors=False)
         return it

@@ -42,6 +42,7 @@ struct Constraint {
     double true_constraint = 0.0;
     double intensity = 0.0;     // Intensity(1); 0 = estimate on first Readjust
     double value[2] = {0.0, 0.0}, squared[2] = {0.0, 0.0};
+    double old_value[7] = {0, 0, 0, 0, 0, 0, 0};   // sums of OldValue(:, 1..7)
     bool started = false;       // first CalculateAllMoments seen (src/Moments.f90:2277)
 };
 
@@ -105,6 +106,9 @@ struct orc_ctx {
     std::vector<double> cutoff, cons_energy;   // Cutoff(:,:,:,it), ConstraintEnergy
     bool alternate_check = false;              // AlternateCheck, src/Main.f90:247, :274
     int iteration = 0;
+    // OldEnergy(7) and TotalEnergy (src/Energy.f90:34), for ConvergenceCheck
+    double old_energy[7] = {0, 0, 0, 0, 0, 0, 0};
+    double total_energy = 0.0;
 };
 
 // --------------------------------------------------------------------------
@@ -985,6 +989,9 @@ extern "C" int orc_calculate_moments(orc_ctx* c) {
     if (c->cons.empty()) return MG_OK;
     for (Constraint& k : c->cons) {
         const std::vector<double>& sh = c->moments[k.mom].sh;
+        // SaveOld = 1: OldValue shifts and takes the previous Value (:1921-1931)
+        for (int i = 6; i > 0; --i) k.old_value[i] = k.old_value[i - 1];
+        k.old_value[0] = k.value[0] + k.value[1];
         for (int it = 0; it < 2; ++it) {
             double s = 0.0;
             for (long v = 0; v < c->V; ++v) s += sh[v] * sh[v] * c->rho[it * c->V + v];
@@ -1474,6 +1481,10 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
     double com = out->com[0][0] + out->com[1][0] + out->com[0][1] + out->com[1][1];
     out->total = sk + (out->kinetic[0] + out->kinetic[1]) + ec + com + ex +
                  (out->pairing[0] + out->pairing[1]);
+    // OldEnergy shifts and takes the previous TotalEnergy (src/Energy.f90:93-98)
+    for (int i = 6; i > 0; --i) c->old_energy[i] = c->old_energy[i - 1];
+    c->old_energy[0] = c->total_energy;
+    c->total_energy = out->total;
     // SpwfEnergy (TermByTerm)
     double sp = 0;
     for (int i = 0; i < c->p.nwt; ++i) sp += D.occ[i] * D.e[i];
@@ -2096,4 +2107,37 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
         if (out) orc_energy(c, out);
     }
     return st;
+}
+
+// ConvergenceCheck, src/Main.f90:358-397: ConverMultipoleAll
+// (src/Moments.f90:2628-2701), ConverEnergy (src/Energy.f90:1458-1481),
+// ConverFermi (src/Pairing.f90:1048-1070; its FermiHistory is never written,
+// so it stays zero), and the stop on a positive total energy.
+extern "C" int orc_convergence_check(orc_ctx* c, const mg_convergence* prec, int* converged) {
+    if (!c || !converged) return MG_ERR_ARG;
+    const mg_convergence P = prec ? *prec : mg_convergence{(double)0.01e-8f, 1e-4, 1e-4};
+    bool conv = true;
+    for (const Constraint& k : c->cons) {
+        if (k.type == 0) continue;
+        const double C = k.constraint;
+        const double v = k.value[0] + k.value[1];
+        double d[8];
+        if (k.true_constraint != 0.0) {
+            d[0] = std::fabs((C - v) / C);
+            for (int i = 1; i < 8; ++i) d[i] = std::fabs((C - k.old_value[i - 1]) / C);
+        } else {
+            d[0] = std::fabs(C - v);
+            for (int i = 1; i < 8; ++i) d[i] = std::fabs(C - k.old_value[i - 1]);
+        }
+        for (int i = 0; i < 8; ++i)
+            if (d[i] >= P.moment_prec) conv = false;
+    }
+    const double E = c->total_energy;
+    for (int i = 0; i < 7; ++i)
+        conv = conv && std::fabs((c->old_energy[i] - E) / E) <= P.energy_prec;
+    if (c->p.pairing == MG_PAIRING_HFB)
+        for (int it = 0; it < 2; ++it)
+            if (std::fabs(c->fermi[it] - 0.0) > P.pairing_prec) conv = false;
+    *converged = conv ? 1 : 0;
+    return E >= 0.0 ? MG_ERR_STATE : MG_OK;
 }

@@ -70,6 +70,8 @@ int orc_get_constraint(orc_ctx* c, int k, mg_constraint_state* out);
 int orc_get_constraint_fields(orc_ctx* c, double* cutoff, double* field);
 int orc_alternate_step(orc_ctx* c);
 int orc_readjust_moments(orc_ctx* c, int iteration);
+/* ConvergenceCheck, as mg_convergence_check */
+int orc_convergence_check(orc_ctx* c, const mg_convergence* prec, int* converged);
 int orc_solve_coulomb(orc_ctx* c, int* iters);
 int orc_construct_potentials(orc_ctx* c, int* iters);
 int orc_get_potentials(orc_ctx* c, double* u, double* b, double* nablab,

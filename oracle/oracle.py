@@ -55,6 +55,7 @@ _SIG = {
     "orc_get_constraint_fields": ([_P, _D, _D], C.c_int),
     "orc_alternate_step": ([_P], C.c_int),
     "orc_readjust_moments": ([_P, C.c_int], C.c_int),
+    "orc_convergence_check": ([_P, C.POINTER(_abi.MgConvergence), C.POINTER(C.c_int)], C.c_int),
     "orc_solve_coulomb": ([_P, _I], C.c_int),
     "orc_construct_potentials": ([_P, _I], C.c_int),
     "orc_get_potentials": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
@@ -270,6 +271,12 @@ class OracleState:
     def AlternateStep(self):
         self._call("orc_alternate_step")
 
+    def ConvergenceCheck(self, prec=None) -> bool:
+        conv = C.c_int(0)
+        self._call("orc_convergence_check", C.byref(prec) if prec is not None else None,
+                   C.byref(conv))
+        return bool(conv.value)
+
     def ReadjustAllMoments(self, iteration):
         self._call("orc_readjust_moments", int(iteration))
 
@@ -326,8 +333,12 @@ class OracleState:
             self.HFFill()
         self.DeriveAll()
         self.UpdateDensities()
-        self.CalculateAllMoments()
+        # three times, as the reference does (src/Main.f90:219-221): the
+        # moments' OldValue history then holds the start value thrice
+        for _ in range(3):
+            self.CalculateAllMoments()
         it = self.ConstructPotentials()
+        self.CompEnergy()   # src/Main.f90:223: the energy history starts here
         if hfb:
             _, e, d = self.hPsi(_abi.MG_CAN_BASIS, want_spinors=False)
             self.set_energies(e, _abi.MG_CAN_BASIS)

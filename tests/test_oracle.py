@@ -337,3 +337,44 @@ def test_golden_c1_fixture():
         assert a["E_total"] == pytest.approx(b["E_total"], abs=1e-9), a["iteration"]
         assert a["q20"] == pytest.approx(b["q20"], abs=1e-9)
         assert a["dt"] == pytest.approx(b["dt"], rel=1e-12)
+
+
+def _hf_pe_run():
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  parameter_estimation=1)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.Start()
+    return o
+
+
+def test_convergence_check():
+    """ConvergenceCheck in the oracle: an HF run (ParameterEstimation 1)
+    stops once E_total changed by at most EnergyPrec (relative) against each
+    of the last 7 iterations; an HFB run never passes, because ConverFermi
+    compares the Fermi energies with a history the reference never fills."""
+    P = _abi.MgConvergence(1e-7, 1e-4, 1e-4)
+    o = _hf_pe_run()
+    k = 0
+    while k < 400:
+        k += 1
+        e = o.Evolve(1, 0.010, 0.3)
+        if o.ConvergenceCheck(P):
+            break
+    assert k == 261, k
+    assert e["total"] == pytest.approx(-195.69968851824, abs=1e-8)
+    # HFB: not even a loose energy bar passes
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
+    h = O.OracleState(p, SLY4)
+    h.set_spinors(psi, qn)
+    h.set_energies(en)
+    h.set_pairing()
+    h.Start()
+    loose = _abi.MgConvergence(1.0, 1.0, 1e-4)
+    for _ in range(9):
+        h.Evolve(1, 0.010, 0.3)
+        assert not h.ConvergenceCheck(loose)
