@@ -28,7 +28,8 @@ one Coulomb solve on a 64^3 mesh, and `batched_64_uneven` 64 independent
 Q20-constrained HFB instances of uneven size run concurrently through the
 batch API (after its schedule autotuner) and one after another, and
 `large_36c_300` 200 iterations of N=50, Z=40 on a 36^3 mesh with nwt=300,
-mixed (last 20 in FP64) against FP64.
+mixed (last 20 in FP64) against FP64, and `c1_mg24_readme` the README Mg24
+run (100 iterations, FP64) on the GPU beside the oracle.
 """
 from __future__ import annotations
 
@@ -436,6 +437,7 @@ def run_ours(args, rank, world, local_rank):
     poisson = poisson_64c(torch, stream) if rank == 0 and args.micro else None
     batched = batched_64_uneven(torch) if rank == 0 and args.batch else None
     large = large_36c_300(torch) if rank == 0 and args.large else None
+    c1 = c1_mg24_readme(torch) if rank == 0 and args.micro else None
 
     if rank != 0:
         return None
@@ -489,6 +491,8 @@ def run_ours(args, rank, world, local_rank):
         res["batched_64_uneven"] = batched
     if large:
         res["large_36c_300"] = large
+    if c1:
+        res["c1_mg24_readme"] = c1
     return res
 
 
@@ -594,6 +598,56 @@ def large_36c_300(torch, iters=200, polish=POLISH):
         g.close()
     out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["dE_total_MeV"] = out["mixed"]["E_total"] - out["fp64"]["E_total"]
+    return out
+
+
+def c1_mg24_readme(torch):
+    """The reference README's Mg24 run (the CPU-runnable configuration):
+    10^3 stored EV8 mesh, nwt=40, N=Z=12, SLy4, HFB (GuessKappa), Nilsson
+    start + seeded 1e-3 perturbation, MixingScheme 2, ParameterEstimation 1,
+    a Q20 constraint of 50 fm^2 for 10 iterations, 100 iterations, FP64.
+    The GPU runs it with the reference's Fermi search (fermi_solver = 1) and
+    with the library's Newton search; the oracle (1 thread) runs it beside;
+    |dE_total| of the first against the oracle after the 100 iterations."""
+    sys.path[:0] = [str(ROOT / "tests" / "golden"), str(ROOT / "oracle")]
+    import make_golden
+    import oracle as O
+    from mocca_gb300 import SLY4, _abi
+    from mocca_gb300.mesh import MeshState
+    p, psi, qn, en = make_golden.c1_state()
+    n = 100
+    out = {"workload": "README Mg24 run: N=Z=12, 10^3 EV8 stored mesh, dx=0.8, nwt=40, SLy4, "
+                       "HFB G=1250 alpha=1 GuessKappa, Nilsson start + 1e-3 perturbation (seed "
+                       "1234), MixingScheme 2, ParameterEstimation 1, Q20 constraint 50 fm^2 "
+                       "for 10 iterations, FP64", "iterations": n}
+    for name, solver in (("gpu_reference_search", 1), ("gpu_newton_search", 0)):
+        g = MeshState(p, SLY4)
+        pp = _abi.MgPairingParams.defaults()
+        pp.fermi_solver = solver
+        g.set_spinors(psi, qn)
+        g.set_energies(en)
+        g.set_pairing(pp)
+        g.add_constraint(2, 0, 50.0, 0.0, 10)
+        g.Start()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e = g.Evolve(n, DT, MOMENTUM)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t
+        out[name] = {"value": n / t, "unit": "iter/s", "E_total": e["total"]}
+        g.close()
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.set_pairing()
+    o.add_constraint(2, 0, 50.0, 0.0, 10)
+    o.Start()
+    t = time.perf_counter()
+    e = o.Evolve(n, DT, MOMENTUM)
+    t = time.perf_counter() - t
+    out["cpu_oracle"] = {"value": n / t, "unit": "iter/s", "E_total": e["total"], "cores": 1,
+                         "kind": "port"}
+    out["dE_total_MeV"] = out["gpu_reference_search"]["E_total"] - e["total"]
     return out
 
 
