@@ -342,6 +342,11 @@ int mg_readjust_moments(mg_ctx* ctx, int iteration);
  * CoulombMax (the reference prints and continues; so does this library). */
 int mg_solve_coulomb(mg_ctx* ctx, int* iters);
 
+/* Relative residual |b - L phi| / |b| of the last Coulomb solve on the stored
+ * box, with the solver's Laplacian and boundary (a diagnostic; the
+ * reference's CG stops on sum(Residual**2), src/Coulomb.f90:883-889). */
+int mg_coulomb_residual(mg_ctx* ctx, double* rel);
+
 /* ConstructPotentials (src/PotentialMixing.f90:17-201, MixingScheme 0):
  * Coulomb, U, W (+div W), B (+grad B).  iters may be NULL. */
 int mg_construct_potentials(mg_ctx* ctx, int* coulomb_iters);

@@ -190,6 +190,7 @@ SIGNATURES = {
     "mg_alternate_step": [_P],
     "mg_readjust_moments": [_P, C.c_int],
     "mg_solve_coulomb": [_P, _I],
+    "mg_coulomb_residual": [_P, _D],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_set_potentials": [_P, _D, _D, _D, _D, _D],

@@ -454,6 +454,30 @@ int coulomb_setup(mg_ctx* c) {
     return MG_OK;
 }
 
+// Sums of r^2 and of the source's square over the stored box (a diagnostic:
+// atomics, so the last bits vary between runs).
+__global__ void k_residual_norms(const double* __restrict__ r, const double* __restrict__ src,
+                                 int nx, int ny, int nz, int mx, int my,
+                                 double* __restrict__ out) {
+    const long V = (long)nx * ny * nz;
+    double a = 0.0, b = 0.0;
+    for (long v = (long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long)nx * ny));
+        const double s = src[i + mx * (j + (long)my * k)];
+        a = fma(r[v], r[v], a);
+        b = fma(s, s, b);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (threadIdx.x % 32 == 0) {
+        atomicAdd(out, a);
+        atomicAdd(out + 1, b);
+    }
+}
+
 // Mixed form: two rounds of (FP64 residual, direct separable correction).
 static int coulomb_direct(mg_ctx* c) {
     const int nx = c->nx, ny = c->ny, nz = c->nz;
@@ -486,6 +510,26 @@ static int coulomb_direct(mg_ctx* c) {
         k_cfast_update<<<g, kThreads, 0, c->stream>>>(c->cpot, t2, nx, ny, nz, c->mx, c->my);
         MG_LAUNCHED(c);
     }
+    return MG_OK;
+}
+
+// |b - L phi| / |b| of the current Coulomb potential on the stored box, with
+// the solver's own Laplacian (CoulombLaplacian with the boundary planes).
+int coulomb_residual(mg_ctx* c, double* rel) {
+    if (!c->coulomb_init) return MG_ERR_STATE;
+    const long V = c->V;
+    const double dx2 = c->p.dx * c->p.dx;
+    k_cfast_residual<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(
+        c->cpot, c->csource, c->cres, c->nx, c->ny, c->nz, c->mx, c->my, 1.0 / dx2);
+    MG_LAUNCHED(c);
+    MG_CUDA(cudaMemsetAsync(c->red, 0, 2 * sizeof(double), c->stream));
+    k_residual_norms<<<std::min(div_up(V, kThreads), 4 * c->num_sms), kThreads, 0, c->stream>>>(
+        c->cres, c->csource, c->nx, c->ny, c->nz, c->mx, c->my, c->red);
+    MG_LAUNCHED(c);
+    double h[2];
+    MG_CUDA(cudaMemcpyAsync(h, c->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    *rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
     return MG_OK;
 }
 

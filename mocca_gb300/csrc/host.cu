@@ -506,6 +506,11 @@ extern "C" int mg_solve_coulomb(mg_ctx* c, int* iters) {
     return st;
 }
 
+extern "C" int mg_coulomb_residual(mg_ctx* c, double* rel) {
+    if (!c || !rel || !c->folded) return MG_ERR_ARG;
+    return coulomb_residual(c, rel);
+}
+
 extern "C" int mg_construct_potentials(mg_ctx* c, int* iters) {
     if (!c) return MG_ERR_ARG;
     int st = MG_OK;

@@ -334,6 +334,7 @@ int densities(mg_ctx* c);
 int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);
 int coulomb_solve(mg_ctx* c, int* iters);
+int coulomb_residual(mg_ctx* c, double* rel);
 int potentials(mg_ctx* c);
 int energy(mg_ctx* c, mg_energy_terms* out);
 int basis_dots(mg_ctx* c, const double* a, const double* b, double* out, bool b_df = false);

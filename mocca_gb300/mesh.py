@@ -237,6 +237,12 @@ class MeshState:
         self._call("mg_solve_coulomb", C.byref(it), allow_not_converged=True)
         return it.value
 
+    def CoulombResidual(self) -> float:
+        """|b - L phi| / |b| of the last Coulomb solve (mg_coulomb_residual)."""
+        r = C.c_double(0.0)
+        self._call("mg_coulomb_residual", C.byref(r))
+        return r.value
+
     def ConstructPotentials(self) -> int:
         it = C.c_int(0)
         self._call("mg_construct_potentials", C.byref(it), allow_not_converged=True)
