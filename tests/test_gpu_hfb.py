@@ -107,3 +107,16 @@ def test_hfb_iterations_first_order_finish(built):
     assert abs(eg["total"] - eo["total"]) < 1e-8, (eg["total"], eo["total"])
     assert abs(sum(eg["pairing"]) - sum(eo["pairing"])) < 1e-8
     g.close()
+
+
+def test_unknown_fermi_solver_is_rejected(built):
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB)
+    g = MeshState(p, SLY4)
+    pp = _abi.MgPairingParams.defaults()
+    pp.fermi_solver = 2
+    with pytest.raises(_abi.MgError):
+        g.set_pairing(pp)
+    pp.fermi_solver = 1
+    g.set_pairing(pp)
+    g.close()
