@@ -1,6 +1,6 @@
 """GPU parity of the FP64 path against the CPU oracle, through the C ABI.
 
-Tolerances (the benchmark spec plain form): h.psi and densities within 1e-12
+Tolerances of the plain FP64 form: h.psi and densities within 1e-12
 relative (norm-wise), total energy within 1e-8 MeV after a fixed number of
 iterations.  Derivatives, potentials and Gram-Schmidt use the same 1e-12
 norm-wise bar; single-particle energies 1e-9 MeV.
