@@ -77,7 +77,7 @@ class MgPairingParams(C.Structure):
 
     @classmethod
     def defaults(cls, strength=1250.0, alpha=1.0, guess_kappa=True):
-        """The README Mg24 &Pairing values with the reference's defaults."""
+        """The &Pairing values of the Mg24 example input in the reference's README.md, with the reference's defaults."""
         p = cls()
         p.strength[0] = p.strength[1] = strength
         p.alpha[0] = p.alpha[1] = alpha

@@ -278,7 +278,7 @@ class MeshState:
         return e.as_dict(), n.value, bool(conv.value)
 
     def set_pairing(self, pp=None):
-        """&Pairing values of an HFB run (defaults: the README Mg24 input)."""
+        """&Pairing values of an HFB run (defaults: the Mg24 example input of the reference's README.md)."""
         pp = pp if pp is not None else _abi.MgPairingParams.defaults()
         self._call("mg_set_pairing", C.byref(pp))
 
