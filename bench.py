@@ -414,6 +414,17 @@ def run_ours(args, rank, world, local_rank):
     flops = 48.0 * p.nx * p.V * p.nwt     # 4 comps x 6 line contractions x 2 n flops per point
     bytes_ = 160.0 * p.V * p.nwt          # FP64 psi in, 3 first derivatives + Laplacian out
 
+    # ---- h.psi of the canonical basis (energies only): psi, 3 derivatives and the
+    # Laplacian in (5 x 4V values of 8 bytes per spwf), the isospins' 17 fields once
+    torch.cuda.synchronize()
+    k0.record(stream)
+    for _ in range(reps):
+        _abi.check("mg_hpsi", g.lib.mg_hpsi(g.h, 1, None, None, None))
+    k1.record(stream)
+    torch.cuda.synchronize()
+    t_hpsi = k0.elapsed_time(k1) / 1e3 / reps
+    bytes_hpsi = 160.0 * p.V * p.nwt + 2 * 17 * 8.0 * p.V
+
     breakdown = stage_breakdown(g, torch, stream) if args.breakdown else None
     g.close()
 
@@ -472,6 +483,13 @@ def run_ours(args, rank, world, local_rank):
                                          "dgemm_tflops_measured": fp64_peak,
                                          "frac_of_dgemm": flops / t_der / 1e12 / fp64_peak},
                      "ms_per_derive": t_der * 1e3},
+        "roofline_hpsi": {"kernel": ("k_hpsi_df" if mixed else "k_hpsi") + " (h.psi of the "
+                                     "canonical basis, energies only, with its field staging "
+                                     "and energy reduction; each call ends with a host "
+                                     "synchronisation, so this is a lower bound)",
+                          "bound": "hbm", "achieved": bytes_hpsi / t_hpsi / 1e9, "peak": hbm,
+                          "unit": "GB/s", "frac": bytes_hpsi / t_hpsi / 1e9 / hbm,
+                          "ms_per_call": t_hpsi * 1e3},
         "cpu_baseline": cpu_baseline(1),
         "clocks": clocks,
         "gpu_launches": int(launches),
