@@ -75,3 +75,17 @@ def test_product_does_not_use_the_oracle():
     for p in list((ROOT / "mocca_gb300").rglob("*.py")) + list((ROOT / "mocca_gb300").rglob("*.cu")):
         txt = p.read_text()
         assert "import oracle" not in txt and "liboracle" not in txt and "orc_" not in txt, p
+
+
+def test_fortran_module_matches_header():
+    """include/mocca_gpu.f90 (the reference-side binding) declares exactly the
+    header's entry points and one bind(C) type per header struct."""
+    f90 = (ROOT / "include" / "mocca_gpu.f90").read_text()
+    fns = set(re.findall(r"function\s+(mg_\w+)\s*\(", f90))
+    assert fns == set(header_functions())
+    hdr = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "mocca_gpu.h").read_text(), flags=re.S)
+    structs = set(re.findall(r"typedef struct (\w+) \{", hdr))
+    types = set(re.findall(r"type, bind\(C\) :: (\w+)", f90))
+    assert types == structs
+    for name in fns:
+        assert f'bind(C, name="{name}")' in f90, name
