@@ -5,7 +5,7 @@
 ! array of c_ptr for the lists of grids (one c_loc(HFBasis(i)%Value%Grid)
 ! per spwf).  Every function returns the status of the C header (0 ok,
 ! > 0 not converged, < 0 error); gpu_check turns an error into the
-! reference's stp().
+! reference's stp().  Written by include/make_fortran_module.py.
 module mocca_gpu
   use iso_c_binding
   use GenInfo, only : stp

@@ -89,3 +89,9 @@ def test_fortran_module_matches_header():
     assert types == structs
     for name in fns:
         assert f'bind(C, name="{name}")' in f90, name
+    # and it is what include/make_fortran_module.py writes from the header
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mfm", ROOT / "include" / "make_fortran_module.py")
+    mfm = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mfm)
+    assert mfm.module_text((ROOT / "include" / "mocca_gpu.h").read_text()) == f90
