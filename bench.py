@@ -261,19 +261,44 @@ def _timed_steps(g, torch, stream, steps, barrier, clk_index=None):
     return ev0.elapsed_time(ev1) / 1e3, last, g.launch_count() - l0, clocks
 
 
+def state_errors(gm, gf):
+    """Mixed-against-FP64 differences of the final states: the single-particle
+    energies <psi|h|psi> of the HF basis (GradDesc's, energy-ordered), max
+    |de| in MeV (compared as sorted lists per isospin), and the density L2
+    norm, |rho_m - rho_f| / |rho_f|.  The canonical basis is not used for the
+    energies: inside a cluster of equal occupations its states may rotate
+    freely, which moves their individual energies but not the density."""
+    import numpy as np
+    from mocca_gb300 import _abi
+    out = {}
+    em, ef = gm.get_energies(_abi.MG_HF_BASIS)[0], gf.get_energies(_abi.MG_HF_BASIS)[0]
+    half = len(em) // 2   # both starts: the first half neutrons, the second protons
+    de = max(np.abs(np.sort(em[:half]) - np.sort(ef[:half])).max(),
+             np.abs(np.sort(em[half:]) - np.sort(ef[half:])).max())
+    rm, rf = gm.get_densities()["rho"], gf.get_densities()["rho"]
+    out["d_sp_energy_max_MeV"] = float(de)
+    out["density_l2_rel"] = float(np.linalg.norm(rm - rf) / np.linalg.norm(rf))
+    return out
+
+
 def accuracy_check(iters, seed):
-    """|dE_total| after `iters` iterations: mixed form (last POLISH in FP64) vs the FP64 path."""
+    """After `iters` iterations, the mixed form (last POLISH in FP64) against
+    the FP64 path: |dE_total|, the single-particle energies and the density
+    L2 difference.  The FP64 GPU path stands for the FP64 oracle here (its
+    parity tests hold it to the oracle at 1e-8 MeV); a 300-iteration oracle
+    run of this workload would take ~9 minutes of CPU."""
     from mocca_gb300 import MG_FP64
     _, gm = _make("mixed", seed)
     em = gm.Evolve(iters - POLISH, DT, MOMENTUM)["total"]
     gm.set_precision(MG_FP64)
     e_mix = gm.Evolve(POLISH, DT, MOMENTUM)["total"]
-    gm.close()
     _, gf = _make("fp64", seed)
     e_f64 = gf.Evolve(iters, DT, MOMENTUM)["total"]
+    errs = state_errors(gm, gf)
+    gm.close()
     gf.close()
     return {"iterations": iters, "fp64_polish": POLISH, "E_fp64": e_f64, "E_mixed": e_mix,
-            "E_mixed_before_polish": em, "dE_total_MeV": e_mix - e_f64,
+            "E_mixed_before_polish": em, "dE_total_MeV": e_mix - e_f64, **errs,
             "pass": abs(e_mix - e_f64) <= 1e-5}
 
 
@@ -601,6 +626,7 @@ def large_36c_300(torch, iters=200, polish=POLISH):
     out = {"workload": "N=50, Z=40, 36^3 EV8 stored mesh, dx=0.8, nwt=300 (150 n + 150 p), "
                        "SLy4, HFB G=1250 alpha=1, HO start (seed 1234), dt=0.010, momentum 0.3",
            "iterations": iters, "fp64_polish": polish}
+    states = {}
     for name, prec in (("mixed", MG_MIXED), ("fp64", MG_FP64)):
         with torch.cuda.stream(stream):
             g = MeshState(dataclasses.replace(p, precision=prec), SLY4,
@@ -623,9 +649,12 @@ def large_36c_300(torch, iters=200, polish=POLISH):
         t = a.elapsed_time(b) / 1e3
         out[name] = {"value": iters / t, "unit": "iter/s", "ms_per_iter": t / iters * 1e3,
                      "E_total": e["total"]}
-        g.close()
+        states[name] = g
     out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["dE_total_MeV"] = out["mixed"]["E_total"] - out["fp64"]["E_total"]
+    out.update(state_errors(states["mixed"], states["fp64"]))
+    for g in states.values():
+        g.close()
     return out
 
 
