@@ -360,7 +360,8 @@ int mg_set_potentials(mg_ctx* ctx, const double* u, const double* b,
 int mg_energy(mg_ctx* ctx, mg_energy_terms* out);
 
 /* n_iter passes of the Evolve loop body (src/Main.f90:255-328) with fixed
- * dt and momentum; out (may be NULL) receives the last iteration's energy.
+ * dt and momentum, each ending with CompEnergy as the reference's does; out
+ * (may be NULL) receives the last iteration's energy.
  * With constraints each pass also takes the AlternateStep first (while an
  * alternating constraint was active at the previous pass's check, :261-274)
  * and readjusts the constraints after the moments (:298-304); the context

@@ -656,7 +656,10 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         readjust_moments(c, c->iteration);   // src/Main.f90:299-304
         st = mg_construct_potentials(c, nullptr);
         if (st < 0) return st;
-        if (out) MG_TRY(energy(c, out));
+        // CompEnergy every pass (src/Main.f90:309): it also keeps the energy
+        // history of the convergence check
+        mg_energy_terms e{};
+        MG_TRY(energy(c, out ? out : &e));
     }
     MG_TRY(tc_check(c));
     return st;

@@ -2104,7 +2104,10 @@ extern "C" int orc_iterate(orc_ctx* c, int n_iter, double dt, double momentum,
         readjust_moments(c, c->iteration);                  // src/Main.f90:299-304
         st = orc_construct_potentials(c, nullptr);
         if (st < 0) return st;
-        if (out) orc_energy(c, out);
+        // CompEnergy every pass (src/Main.f90:309), which also keeps the
+        // energy history of ConvergenceCheck
+        mg_energy_terms e{};
+        orc_energy(c, out ? out : &e);
     }
     return st;
 }
