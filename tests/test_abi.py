@@ -95,3 +95,5 @@ def test_fortran_module_matches_header():
     mfm = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mfm)
     assert mfm.module_text((ROOT / "include" / "mocca_gpu.h").read_text()) == f90
+    # free-form Fortran: at most 132 characters per line
+    assert max(len(line) for line in f90.splitlines()) <= 132
