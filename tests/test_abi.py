@@ -97,3 +97,26 @@ def test_fortran_module_matches_header():
     assert mfm.module_text((ROOT / "include" / "mocca_gpu.h").read_text()) == f90
     # free-form Fortran: at most 132 characters per line
     assert max(len(line) for line in f90.splitlines()) <= 132
+
+
+def test_new_entry_points_reject_bad_arguments(built):
+    """Argument checks that return before any device work: NULL contexts and
+    outputs, eigensolver sizes beyond its 160 limit, empty batches."""
+    lib = _abi.load()
+    one = np.zeros(1)
+    d = one.ctypes.data_as(_abi._D)
+    n = np.array([161], dtype=np.int32)
+    big = np.zeros(1)
+    assert lib.mg_eigh_batched(1, n.ctypes.data_as(_abi._I), 161, big.ctypes.data_as(_abi._D),
+                               d, d) == _abi.MG_ERR_ARG
+    assert lib.mg_eigh_batched(65, n.ctypes.data_as(_abi._I), 8, d, d, d) == _abi.MG_ERR_ARG
+    conv = C.c_int(0)
+    assert lib.mg_convergence_check(None, None, C.byref(conv)) == _abi.MG_ERR_ARG
+    assert lib.mg_evolve(None, 1, 0.01, 0.3, None, None, None, None) == _abi.MG_ERR_ARG
+    assert lib.mg_coulomb_residual(None, d) == _abi.MG_ERR_ARG
+    assert lib.mg_add_constraint(None, None) == _abi.MG_ERR_ARG
+    assert lib.mg_alternate_step(None) == _abi.MG_ERR_ARG
+    assert lib.mg_readjust_moments(None, 1) == _abi.MG_ERR_ARG
+    assert lib.mg_batch_iterate(None, 1, d, d, None) == _abi.MG_ERR_ARG
+    assert lib.mg_batch_status(None, None) == _abi.MG_ERR_ARG
+    assert lib.mg_batch_set_workers(None, 2) == _abi.MG_ERR_ARG
