@@ -160,7 +160,7 @@ module mocca_gpu
       type(c_ptr), value :: w
       type(c_ptr), value :: z
     end function
-    integer(c_int) function mg_eigh_batched_noalloc(nb, n, ld, a, w, z, stream) bind(C, name="mg_eigh_batched_noalloc")
+    integer(c_int) function mg_eigh_batched_noalloc(nb, n, ld, a, w, z, info, stream) bind(C, name="mg_eigh_batched_noalloc")
       import
       integer(c_int), value :: nb
       type(c_ptr), value :: n
@@ -168,6 +168,7 @@ module mocca_gpu
       type(c_ptr), value :: a
       type(c_ptr), value :: w
       type(c_ptr), value :: z
+      type(c_ptr), value :: info
       type(c_ptr), value :: stream
     end function
     integer(c_int) function mg_create(p, f, stream, out) bind(C, name="mg_create")

@@ -168,24 +168,30 @@ int mg_lagrange_matrices(int n, double dx, int folded, double* d1, double* d2);
  * leading dimension ld and stride ld*ld in a (host arrays); w receives the
  * eigenvalues ascending (stride ld), z the eigenvectors (column k <-> w[k]).
  * Runs on the current CUDA device; FP64-accurate (FP32 Jacobi seed, FP64
- * refinement, FP64 Jacobi polish inside clusters). */
+ * refinement, FP64 Jacobi polish inside clusters).  Returns MG_NOT_CONVERGED
+ * (results written) when the polish of some matrix reached its sweep cap. */
 int mg_eigh_batched(int nb, const int* n, int ld, const double* a, double* w, double* z);
 
-/* mg_eigh_batched for callers that must not allocate device memory (hosts
- * that own every byte through their own pool, code running while a stream is
- * captured).  No reference counterpart: the Fortran code has no device.
+/* mg_eigh_batched for callers that must not allocate device memory: a host
+ * that owns every byte of the device through its own pool allocator (a
+ * solver framework, an embedding application with a fixed budget) cannot
+ * let a library call cudaMalloc behind its back.  No reference counterpart:
+ * the Fortran code has no device.
  * n: host array; a, w, z: DEVICE buffers laid out as for mg_eigh_batched;
- * stream: a cudaStream_t (NULL: the legacy default stream).  Work is only
- * enqueued on `stream`; the caller synchronises before reading w and z.
- * The workspace is one static device array of ~2.2 MiB per device, so the
- * limits are nb <= 64, ld <= 128 and nb*ld*ld <= 65536 (MG_ERR_ARG with a
- * message on stderr beyond that).  z outside each leading n x n block is set
- * to zero, w beyond n[b] is not written.  The first call on a device (that
- * device current) looks up the workspace and loads the kernels; make it
- * before any stream capture.  Calls share the workspace: two calls that can
- * overlap on one device (different streams, host threads) race. */
+ * info: DEVICE array of nb ints or NULL, receiving 1 for a matrix whose FP64
+ * Jacobi polish reached its sweep cap (results still written) and 0
+ * otherwise; stream: a cudaStream_t (NULL: the legacy default stream).  Work
+ * is only enqueued on `stream`; the caller synchronises before reading w, z
+ * and info.  The workspace is one static device array of ~2.2 MiB per
+ * device, so the limits are nb <= 64, ld <= 128 and nb*ld*ld <= 65536
+ * (MG_ERR_ARG with a message on stderr beyond that).  z outside each leading
+ * n x n block is set to zero, w beyond n[b] is not written.  The first call
+ * on a device (that device current) looks up the workspace address and loads
+ * the kernels; make it before any stream capture.  Calls share the
+ * workspace: two calls that can overlap on one device (different streams,
+ * host threads) race. */
 int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const double* a, double* w,
-                            double* z, void* stream);
+                            double* z, int* info, void* stream);
 
 /* ---- context --------------------------------------------------------------- */
 
@@ -381,7 +387,8 @@ int mg_iterate(mg_ctx* ctx, int n_iter, double dt, double momentum,
  * instances, each instance on its own streams, so the latency-bound steps of
  * one overlap with the mesh kernels of others.  Until the batch is tuned
  * the workers are min(n, host threads), instances assigned longest first by
- * nwt * V. */
+ * nwt * V.  MG_ERR_ARG when a context appears twice or was created on
+ * another device than the current one. */
 typedef struct mg_batch mg_batch;
 int mg_batch_create(int n, mg_ctx* const* ctxs, mg_batch** out);
 int mg_batch_destroy(mg_batch* b);

@@ -207,7 +207,7 @@ SIGNATURES = {
     "mg_batch_status": [_P, _I],
     "mg_batch_iterate": [_P, C.c_int, _D, _D, C.POINTER(MgEnergyTerms)],
     "mg_eigh_batched": [C.c_int, _I, C.c_int, _D, _D, _D],
-    "mg_eigh_batched_noalloc": [C.c_int, _I, C.c_int, _P, _P, _P, _P],
+    "mg_eigh_batched_noalloc": [C.c_int, _I, C.c_int, _P, _P, _P, _P, _P],
     "mg_set_pairing": [_P, C.POINTER(MgPairingParams)],
     "mg_solve_pairing": [_P, C.POINTER(MgPairingInfo)],
     "mg_get_hfb_block": [_P, C.c_int, _D, _D, _D],

@@ -107,13 +107,21 @@ extern "C" int mg_batch_create(int n, mg_ctx* const* ctxs, mg_batch** out) {
     if (n <= 0 || !ctxs) return MG_ERR_ARG;
     for (int i = 0; i < n; ++i)
         if (!ctxs[i]) return MG_ERR_ARG;
+    // one entry per context: two workers must never run the same context
+    std::vector<mg_ctx*> sorted(ctxs, ctxs + n);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return MG_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MG_ERR_CUDA;
+    for (int i = 0; i < n; ++i)
+        if (ctxs[i]->device != dev) return MG_ERR_ARG;   // all on the current device
     mg_batch* b = new mg_batch();
     b->ctx.assign(ctxs, ctxs + n);
     // cost model until measured: mesh work ~ nwt V per basis
     for (mg_ctx* c : b->ctx)
         b->cost.push_back((double)c->p.nwt * (double)c->V * (c->p.pairing == MG_PAIRING_HFB ? 2 : 1));
     b->status.assign(n, MG_OK);
-    if (cudaGetDevice(&b->device) != cudaSuccess) { delete b; return MG_ERR_CUDA; }
+    b->device = dev;
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
     assign(b, std::min(n, hw));
     *out = b;

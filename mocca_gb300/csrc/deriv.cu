@@ -459,19 +459,24 @@ int run_jobs(mg_ctx* c, const GridJob* jobs, int njobs, bool out_df) {
     // z planes per k_deriv_xy block, tuned per (form, grid-count class):
     // few grids (densities, fields) and whole bases
     int& ppb = c->deriv_planes[c->cur_precision == MG_MIXED ? 1 : 0][njobs < 64 ? 0 : 1];
-    // once per process (contexts of a batch call this from several threads)
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [] {
-        const void* fns[4] = {(const void*)k_deriv_xy, (const void*)k_deriv_z,
-                              (const void*)k_deriv_xy_df, (const void*)k_deriv_z_df};
-        for (const void* f : fns) {
-            const cudaError_t e =
-                cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            if (e != cudaSuccess && attr_err == cudaSuccess) attr_err = e;
+    // the shared-memory opt-in is a per-device attribute: set it once per
+    // device (contexts of a batch call this from several host threads)
+    {
+        static std::mutex attr_mu;
+        static bool attr_done[64] = {};
+        int dev = 0;
+        MG_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64) return MG_ERR_ARG;
+        std::lock_guard<std::mutex> lock(attr_mu);
+        if (!attr_done[dev]) {
+            const void* fns[4] = {(const void*)k_deriv_xy, (const void*)k_deriv_z,
+                                  (const void*)k_deriv_xy_df, (const void*)k_deriv_z_df};
+            for (const void* f : fns)
+                MG_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024));
+            attr_done[dev] = true;
         }
-    });
-    MG_CUDA(attr_err);
+    }
     if (c->cur_precision == MG_MIXED) {
         // out_df: the outputs stay double-float ({hi, lo} float pairs)
         MatPtrs32 mp = mat_ptrs32(c);

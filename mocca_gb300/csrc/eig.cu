@@ -409,7 +409,10 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     __shared__ unsigned rmask[(kEigMax + 31) / 32];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
-    if (n0 == 0) return;
+    if (n0 == 0) {
+        if (threadIdx.x == 0 && pfail) pfail[b] = 0;
+        return;
+    }
     const int n = n0 + (n0 & 1);
     const int l2 = n + 1;
     double* a = smd;
@@ -590,10 +593,12 @@ size_t jacobi_smem(int n) {
     return (size_t)(np <= kJSmemMax ? 3 : 2) * np * (np + 1) * sizeof(float);
 }
 
-// Eigen-decomposition of a batch (nb <= 8) of symmetric matrices of sizes
-// nsz (device) <= nmax, stored with leading dimension ld and stride `stride`.
-// X (in/out: warm start when warm != 0), w: eigenvalues, ws: workspace of
-// 4 * nb * stride doubles; descs: GemmDesc workspace (3 * nb entries).
+// Eigen-decomposition of a batch (nb <= 64: the GEMM grids hold 2 nb
+// matrices in y) of symmetric matrices of sizes nsz (device) <= nmax, stored
+// with leading dimension ld and stride `stride`.  E.X: in/out (the warm start
+// of kSeedJacobiWarm / kSeedRefine), E.w: eigenvalues; the work matrices,
+// norms and GEMM tables are E's (eig_setup).  E.pfail[b] is set to 1 when the
+// FP64 Jacobi polish of matrix b reached its sweep cap.
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     if (!E.attr_done) {
         MG_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -795,6 +800,11 @@ extern "C" int mg_eigh_batched(int nb, const int* n, int ld, const double* a, do
         MG_CUDA(cudaStreamSynchronize(tmp.stream));
         MG_CUDA(cudaMemcpy(w, E.w, nb * (size_t)ld * sizeof(double), cudaMemcpyDeviceToHost));
         MG_CUDA(cudaMemcpy(z, E.X, nb * stride * sizeof(double), cudaMemcpyDeviceToHost));
+        // the polish of a matrix that ran out of sweeps: results written, status > 0
+        std::vector<int> pf(nb, 0);
+        MG_CUDA(cudaMemcpy(pf.data(), E.pfail, nb * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int b = 0; b < nb; ++b)
+            if (pf[b]) st = MG_NOT_CONVERGED;
     }
     eig_free(E);
     cudaFree(dA);
@@ -885,6 +895,9 @@ int noalloc_setup(int dev, unsigned char** base) {
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kSmemOptIn));
         cudaFuncAttributes fa;
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_jacobi32));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_jacobi64_polish));
+        MG_CUDA(cudaFuncGetAttributes(&fa, k_sort_cols));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_gemm64));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_rows));
         MG_CUDA(cudaFuncGetAttributes(&fa, k_oa_apply));
@@ -902,7 +915,7 @@ int noalloc_setup(int dev, unsigned char** base) {
 }  // namespace mg
 
 extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const double* a, double* w,
-                                       double* z, void* stream) {
+                                       double* z, int* info, void* stream) {
     using namespace mg;
     if (nb <= 0 || !n || !a || !w || !z || ld <= 0) return MG_ERR_ARG;
     if (nb > kNoAllocNb || ld > kNoAllocLd || (long)nb * ld * ld > kNoAllocElems) {
@@ -966,7 +979,17 @@ extern "C" int mg_eigh_batched_noalloc(int nb, const int* n, int ld, const doubl
     k_eig_noalloc_tables<<<1, kNoAllocNb, 0, tmp.stream>>>(args, const_cast<int*>(E.nsz), E.d_ax,
                                                           E.d_sg, E.d_xf, E.d_rr);
     MG_CUDA(cudaGetLastError());
-    const int st = eig_batched(&tmp, E, kSeedCold, 3, true);
+    int st = eig_batched(&tmp, E, kSeedCold, 3, true);
+    // per-matrix polish status for the caller (read after its synchronisation)
+    if (st == MG_OK && info) {
+        const cudaError_t ce = cudaMemcpyAsync(info, E.pfail, (size_t)nb * sizeof(int),
+                                               cudaMemcpyDeviceToDevice, tmp.stream);
+        if (ce != cudaSuccess) {
+            fprintf(stderr, "mocca_gpu: mg_eigh_batched_noalloc: info copy failed: %s\n",
+                    cudaGetErrorString(ce));
+            st = MG_ERR_CUDA;
+        }
+    }
     tmp.flags = nullptr;
     tmp.stream = nullptr;
     return st;

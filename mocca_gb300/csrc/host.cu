@@ -147,6 +147,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     mg_ctx* c = new mg_ctx();
+    c->device = dev;
     c->p = *p;
     c->f = *f;
     mg_skyrme_coefficients(f, p->trc, &c->B);

@@ -193,6 +193,7 @@ struct mg_ctx {
     long V;
     double dv;
     bool folded;
+    int device = 0;                     // CUDA device current at mg_create
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaStream_t side = nullptr;        // low-priority stream for overlapped work

@@ -89,3 +89,14 @@ def test_batch_failed_instance_is_skipped(built):
     b.close()
     for s in states:
         s.close()
+
+
+def test_batch_rejects_a_context_listed_twice(built):
+    import ctypes as C
+    g = _state(_instances(1, seed=13)[0])
+    lib = _abi.load()
+    arr = (C.c_void_p * 2)(g.h.value, g.h.value)
+    h = C.c_void_p()
+    assert lib.mg_batch_create(2, arr, C.byref(h)) == _abi.MG_ERR_ARG
+    assert not h.value
+    g.close()

@@ -98,3 +98,16 @@ def test_large_blocks(built):
     mats.append(_sym(rng, 160, occ))
     for m, (w, z) in zip(mats, _run(mats)):
         _check(m, w, z)
+
+
+def test_batch_of_64(built):
+    """The largest batch both entry points accept (nb = 64) at a small
+    leading dimension: every matrix of the batch is solved to the same bars."""
+    rng = np.random.default_rng(5)
+    mats = []
+    for b in range(64):
+        n = 4 + (b % 13)
+        x = rng.normal(size=(n, n))
+        mats.append(x + x.T)
+    for m, (w, z) in zip(mats, _run(mats)):
+        _check(m, w, z)
