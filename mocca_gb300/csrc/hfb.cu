@@ -567,6 +567,24 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
     return MG_OK;
 }
 
+// Start of a Fermi search: the last Fermi energies, extrapolated along the
+// iterations by the polynomial through the last converged ones (up to cubic:
+// in the converging phase the cubic predictor lands within the first-order
+// finish's step, so one evaluation completes the search), as long as the
+// sequence moves by less than kFarStep per iteration.
+static void start_guess(const Hfb& H, double lam[2]) {
+    for (int it = 0; it < 2; ++it) {
+        const double l[4] = {H.fermi[it], H.fermi_prev[it], H.fermi_old[0][it], H.fermi_old[1][it]};
+        int k = std::min(H.n_solved, 4);
+        for (int j = 1; j < k; ++j)
+            if (std::fabs(l[j - 1] - l[j]) >= kFarStep) k = j;
+        if (k >= 4) lam[it] = 4.0 * l[0] - 6.0 * l[1] + 4.0 * l[2] - l[3];
+        else if (k == 3) lam[it] = 3.0 * l[0] - 3.0 * l[1] + l[2];
+        else if (k == 2) lam[it] = 2.0 * l[0] - l[1];
+        else lam[it] = l[0];
+    }
+}
+
 // ---- particle-number root finder: Newton with the analytic dN/dlambda,
 // safeguarded by the bracket the evaluations build (bisection when a step
 // leaves it, steps clamped to 5 MeV).  On return lam holds the Fermi
@@ -578,15 +596,10 @@ static int fermi_newton(mg_ctx* c, double lam[2], double f[2], bool conv[2], int
     Hfb& H = c->hfb;
     const double prec = H.pp.fermi_prec;
     int evals = 0;
-    // start from the last Fermi energies, linearly extrapolated along the
-    // iterations once two converged ones exist (the root is the same; the
-    // first evaluation only lands closer to it)
-    lam[0] = H.fermi[0];
-    lam[1] = H.fermi[1];
+    // start from the last Fermi energies extrapolated along the iterations
+    // (the root is the same; the first evaluation only lands closer to it)
     double fp[2];
-    for (int it = 0; it < 2; ++it)
-        if (H.n_solved >= 2 && std::fabs(H.fermi[it] - H.fermi_prev[it]) < 0.5)
-            lam[it] = 2.0 * H.fermi[it] - H.fermi_prev[it];
+    start_guess(H, lam);
     MG_TRY(hfb_evaluate(c, lam, f, fp, true));
     ++evals;
     conv[0] = std::fabs(f[0]) < prec;
@@ -738,8 +751,11 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         MG_TRY(fermi_newton(c, lam, f, conv, &evals, &first_order));
     }
     if (conv[0] && conv[1]) {
-        H.fermi_prev[0] = H.fermi[0];
-        H.fermi_prev[1] = H.fermi[1];
+        for (int it = 0; it < 2; ++it) {
+            H.fermi_old[1][it] = H.fermi_old[0][it];
+            H.fermi_old[0][it] = H.fermi_prev[it];
+            H.fermi_prev[it] = H.fermi[it];
+        }
         ++H.n_solved;
     } else {
         H.n_solved = 0;

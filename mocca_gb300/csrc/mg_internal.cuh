@@ -133,6 +133,7 @@ struct Hfb {
     double qp_gap[2] = {0.0, 0.0};             // per isospin: smallest 2 min E of its blocks
     double fermi[2] = {-10.0, -10.0};
     double fermi_prev[2] = {-10.0, -10.0};     // Fermi energies of the solve before
+    double fermi_old[2][2] = {{0, 0}, {0, 0}}; // the two before that ([0] newer)
     int n_solved = 0;                          // consecutive converged solves
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
