@@ -382,7 +382,8 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs) {
         P.ny = c->ny;
         P.status = c->tc_status;
         P.lap_stage = tc_smem_bytes(P.n, P.N, true) <= kSmemCap ? 1 : 0;
-        const int grid = std::min(c->num_sms, P.ntiles);
+        const int sms = c->tc_grid_cap > 0 ? std::min(c->tc_grid_cap, c->num_sms) : c->num_sms;
+        const int grid = std::min(sms, P.ntiles);
         k_deriv_tc<<<grid, kThreads, tc_smem_bytes(P.n, P.N, P.lap_stage != 0), c->stream>>>(P);
         MG_LAUNCHED(c);
     }

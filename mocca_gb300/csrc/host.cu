@@ -630,12 +630,17 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         if (hfb) {
             // DeriveAll of the HF basis needs only the new HF spinors: it runs
             // on the side stream while the pairing step (which reads the same
-            // spinors) runs on the main stream; the canonical basis follows
+            // spinors) runs on the main stream; the canonical basis follows.
+            // The persistent tensor-core kernel takes a whole SM per CTA, so
+            // on the side stream it keeps to half of the SMs: the pairing
+            // step's kernels find the other half free.
             MG_CUDA(cudaEventRecord(c->ev_fork, c->stream));
             MG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
             cudaStream_t main = c->stream;
             c->stream = c->side;
+            c->tc_grid_cap = c->num_sms / 2;
             const int sd = derive_basis(c, MG_HF_BASIS);
+            c->tc_grid_cap = 0;
             c->stream = main;
             MG_TRY(sd);
             MG_CUDA(cudaEventRecord(c->ev_join, c->side));

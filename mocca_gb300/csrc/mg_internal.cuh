@@ -216,6 +216,9 @@ struct mg_ctx {
     long tc_off[3][2];
     int tc_N[3] = {0, 0, 0};
     bool tc_ok = false;           // every line length <= 32
+    // largest grid of the persistent tensor-core derivative kernel (0: one CTA
+    // per SM); set while it runs beside other work on the side stream
+    int tc_grid_cap = 0;
 
     // z planes per block of the Lagrange x/y kernels, [0 FP64, 1 double-float]
     // x [0 few grids, 1 whole bases]; 0 until deriv.cu's autotuner picks one
