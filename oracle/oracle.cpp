@@ -14,6 +14,9 @@
 #include <cstring>
 #include <numeric>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -384,6 +387,7 @@ extern "C" int orc_derive_basis(orc_ctx* c, int b) {
     if (!c || b < 0 || b > 1) return MG_ERR_ARG;
     Basis& B = c->bas[b];
     const long V = c->V;
+#pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < c->p.nwt; ++i) {
         int P = B.qn[4 * i + 1], S = B.qn[4 * i + 2], TS = B.qn[4 * i + 3];
         const double* psi = &B.psi[(long)i * 4 * V];
@@ -480,8 +484,9 @@ extern "C" int orc_hpsi(orc_ctx* c, int b, double* hpsi, double* e, double* disp
     if (!c || b < 0 || b > 1) return MG_ERR_ARG;
     const Basis& B = c->bas[b];
     const long V4 = 4 * c->V;
-    std::vector<double> h(V4);
+#pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < c->p.nwt; ++i) {
+        std::vector<double> h(V4);
         hpsi_one(c, B, i, h.data());
         double en = inprod_real(c, &B.psi[i * V4], h.data());
         double hh = inprod_real(c, h.data(), h.data());
@@ -516,6 +521,7 @@ extern "C" int orc_gram_schmidt(orc_ctx* c) {
             double norm = inprod_real(c, pn, pn);
             double sc = 1.0 / std::sqrt(norm);
             for (long v = 0; v < V4; ++v) pn[v] = sc * pn[v];
+#pragma omp parallel for schedule(dynamic, 1)
             for (size_t l = k + 1; l < idx.size(); ++l) {
                 int mw = idx[l];
                 if (B.qn[4 * mw] != B.qn[4 * nw] || B.qn[4 * mw + 1] != B.qn[4 * nw + 1] ||
@@ -655,8 +661,9 @@ extern "C" int orc_grad_desc(orc_ctx* c, double dt, double momentum) {
     dt = c->step_dt;
     momentum = c->step_mom;
     const double fac = dt / c->f.hbar;
-    std::vector<double> h(V4);
+#pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < c->p.nwt; ++i) {
+        std::vector<double> h(V4);
         double* cur = &B.psi[i * V4];
         hpsi_one(c, B, i, h.data());
         double en = inprod_real(c, cur, h.data());
@@ -1505,6 +1512,18 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
 // implements), eigenvalues sorted ascending with their vectors.
 // a: n*n row-major symmetric input; w: eigenvalues; z: n*n, column k = vector k.
 // --------------------------------------------------------------------------
+// Host threads of the OpenMP build (the timing build of the CPU baseline);
+// returns the count in use, 1 in the parity build (compiled without OpenMP).
+extern "C" int orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
 extern "C" int orc_eigh(int n, const double* a_in, double* w, double* z) {
     if (n <= 0) return MG_ERR_ARG;
     std::vector<double> A(a_in, a_in + (size_t)n * n), d(n), e(n);
@@ -1724,6 +1743,7 @@ static void pairing_field(orc_ctx* c) {
                 const double factor = c1 * c2 * kij;
                 const double* pl = &B.psi[(long)jjj * 4 * V];
                 const double* pr = &B.psi[(long)iii * 4 * V];
+#pragma omp parallel for schedule(static)
                 for (long v = 0; v < V; ++v) {
                     const double l[4] = {pl[v], pl[V + v], pl[2 * V + v], pl[3 * V + v]};
                     const double r[4] = {pr[v], pr[V + v], pr[2 * V + v], pr[3 * V + v]};
@@ -1752,6 +1772,7 @@ static void pairing_gaps(orc_ctx* c) {
         const auto& idx = c->bidx[b];
         const int N = (int)idx.size();
         std::fill(c->delta[b].begin(), c->delta[b].end(), 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
         for (int i = 0; i < N; ++i) {
             const int ii = idx[i], iii = ii % nwt;
             const int sig1 = hfb_sig(c, ii);

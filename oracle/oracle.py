@@ -18,6 +18,8 @@ from mocca_gb300.forces import Force, RunParams
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
+# -O3 OpenMP build of the same sources: timing of the CPU baseline only
+LIB_OMP = HERE / "_build" / "liboracle_omp.so"
 
 _D = _abi._D
 _I = _abi._I
@@ -67,9 +69,10 @@ _SIG = {
     "orc_get_hfb_block": ([_P, C.c_int, _D, _D, _D], C.c_int),
     "orc_get_pairing_field": ([_P, _D, _D, _D], C.c_int),
     "orc_eigh": ([C.c_int, _D, _D, _D], C.c_int),
+    "orc_set_threads": ([C.c_int], C.c_int),
 }
 
-_lib = None
+_libs = {}
 
 
 def build_oracle() -> Path:
@@ -77,18 +80,19 @@ def build_oracle() -> Path:
     return LIB
 
 
-def load():
-    global _lib
-    if _lib is None:
-        if not LIB.exists():
+def load(timing: bool = False):
+    """The parity build, or with timing=True the -O3 OpenMP build."""
+    path = LIB_OMP if timing else LIB
+    if path not in _libs:
+        if not path.exists():
             build_oracle()
-        lib = C.CDLL(str(LIB))
+        lib = C.CDLL(str(path))
         for name, (args, res) in _SIG.items():
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = res
-        _lib = lib
-    return _lib
+        _libs[path] = lib
+    return _libs[path]
 
 
 def _d(a):
@@ -107,8 +111,8 @@ def lagrange_matrices(n: int, dx: float, folded: bool):
 
 
 class OracleState:
-    def __init__(self, params: RunParams, force: Force):
-        self.lib = load()
+    def __init__(self, params: RunParams, force: Force, timing: bool = False):
+        self.lib = load(timing)
         self.p = params
         self._cp = params.to_c()
         self._cf = force.to_c()
