@@ -397,18 +397,22 @@ def microbench_c2(torch, stream, reps=5):
 
 def poisson_64c(torch, stream):
     """Coulomb problem on the 64^3 stored EV8 mesh (128^3 full box), dx=0.8: a
-    deformed Gaussian proton density (Z=40, axes 1:1:1.3, width 3 fm), multipole
-    boundary values; one cold solve from the uniform-sphere guess.  FP64: the
-    reference's CG to its tolerance.  Mixed: the direct separable solve with
-    two FP64 refinement rounds."""
+    deformed Gaussian proton density (Z=40, axes 1:1:1.3, width 3 fm),
+    multipole boundary values; one cold solve from the uniform-sphere guess,
+    each solver to a relative residual of 1e-10: the FP64 CG (the
+    reference's algorithm), the FP32 multigrid V-cycles inside the FP64
+    conjugate-gradient iteration (CoulombSolver = 2), and the direct
+    separable solve with two FP64 refinement rounds (the mixed form's
+    default).  Best of two timed solves after one that sets the solver up."""
     import numpy as np
     from mocca_gb300 import MG_FP64, MG_MIXED, SLY4, RunParams, synthetic
     from mocca_gb300.mesh import MeshState
     out = {"workload": "64^3 EV8 stored (128^3 box), dx=0.8, Gaussian rho_p Z=40, "
-                       "axes 1:1:1.3, width 3 fm"}
-    for name, prec in (("fp64", MG_FP64), ("mixed", MG_MIXED)):
+                       "axes 1:1:1.3, width 3 fm; every solver to |b - L phi| <= 1e-10 |b|"}
+    for name, prec, solver in (("fp64_cg", MG_FP64, 1), ("fp32_multigrid_fp64_pcg", MG_FP64, 2),
+                               ("direct_fp64_refinement", MG_MIXED, 1)):
         p = RunParams(nx=64, ny=64, nz=64, dx=0.8, nwt=2, neutrons=40, protons=40,
-                      precision=prec)
+                      precision=prec, coulomb_solver=solver, coulomb_prec=1e-10)
         x, y, z = synthetic.mesh_axes(p)
         X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
         rp = np.exp(-(X ** 2 + Y ** 2) / 9.0 - Z ** 2 / (9.0 * 1.69)).transpose(2, 1, 0)
@@ -418,15 +422,23 @@ def poisson_64c(torch, stream):
             g = MeshState(p, SLY4, stream=stream.cuda_stream)
         g.set_densities(rho=rho)
         g.CalculateAllMoments()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        it = g.SolveCoulomb()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        out[name] = {"ms": e0.elapsed_time(e1), "iterations": it,
-                     "residual_rel": g.CoulombResidual()}
+        g.SolveCoulomb()   # first call: setup (hierarchy, eigenvectors, graph)
+        best = None
+        for rep in range(2):
+            g.set_densities(rho=rho)
+            g.CalculateAllMoments()
+            g.reset_coulomb_guess()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            it = g.SolveCoulomb()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best is None or ms < best["ms"]:
+                best = {"ms": ms, "iterations": it, "residual_rel": g.CoulombResidual()}
         g.close()
+        out[name] = best
     return out
 
 

@@ -32,6 +32,7 @@ module mocca_gpu
     real(c_double) :: damping
     real(c_double) :: precon_u
     integer(c_int) :: parameter_estimation
+    real(c_double) :: coulomb_prec
   end type mg_params
   type, bind(C) :: mg_force
     real(c_double) :: t0
@@ -369,6 +370,10 @@ module mocca_gpu
       import
       type(c_ptr), value :: ctx
       type(c_ptr), value :: rel
+    end function
+    integer(c_int) function mg_coulomb_reset(ctx) bind(C, name="mg_coulomb_reset")
+      import
+      type(c_ptr), value :: ctx
     end function
     integer(c_int) function mg_construct_potentials(ctx, coulomb_iters) bind(C, name="mg_construct_potentials")
       import

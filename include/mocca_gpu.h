@@ -72,7 +72,10 @@ typedef struct mg_params {
     int    pairing;            /* MG_PAIRING_HF or MG_PAIRING_HFB */
     int    coulomb_max;        /* CoulombMax, default 500 (src/Coulomb.f90:24) */
     int    max_l_coul;         /* MaxLCoul, default MaxMoment = 10 */
-    int    coulomb_solver;     /* 0 none, 1 CG (reference default) */
+    int    coulomb_solver;     /* CoulombSolver: 0 none, 1 CG (reference default; the mixed
+                                  form solves directly instead), 2 multigrid: FP32 V-cycles
+                                  preconditioning an FP64 conjugate-gradient iteration
+                                  (src/MultiGrid.f90:14-348) */
     int    mixing_scheme;      /* MixingScheme (src/DensityMixing.f90:22-86): 0 linear
                                   density mixing (reference default), 2 preconditioned
                                   U update (src/PotentialMixing.f90:143-154) */
@@ -81,6 +84,10 @@ typedef struct mg_params {
     int    parameter_estimation; /* ParameterEstimation (src/GenInfo.f90:72): 1 re-estimates
                                     dt and the momentum at every GradDesc
                                     (IterativeEstimation, src/ImaginaryTime.f90:28-211) */
+    double coulomb_prec;       /* > 0: the CG and multigrid solves stop at |b - L phi| <=
+                                  coulomb_prec |b| on the stored box; 0: the reference's CG
+                                  test |r|^2 <= 1e-9 / (dx^3 V) (src/Coulomb.f90:755-900), and
+                                  1e-10 relative for the multigrid */
 } mg_params;
 
 /*
@@ -352,6 +359,9 @@ int mg_solve_coulomb(mg_ctx* ctx, int* iters);
  * box, with the solver's Laplacian and boundary (a diagnostic; the
  * reference's CG stops on sum(Residual**2), src/Coulomb.f90:883-889). */
 int mg_coulomb_residual(mg_ctx* ctx, double* rel);
+/* Sets the Coulomb potential back to InitialGuess (the uniform-sphere
+ * potential, src/Coulomb.f90:542-581), the start of a cold solve. */
+int mg_coulomb_reset(mg_ctx* ctx);
 
 /* ConstructPotentials (src/PotentialMixing.f90:17-201, MixingScheme 0):
  * Coulomb, U, W (+div W), B (+grad B).  iters may be NULL. */

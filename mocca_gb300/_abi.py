@@ -48,6 +48,7 @@ class MgParams(C.Structure):
         ("damping", C.c_double),
         ("precon_u", C.c_double),
         ("parameter_estimation", C.c_int),
+        ("coulomb_prec", C.c_double),
     ]
 
 
@@ -191,6 +192,7 @@ SIGNATURES = {
     "mg_readjust_moments": [_P, C.c_int],
     "mg_solve_coulomb": [_P, _I],
     "mg_coulomb_residual": [_P, _D],
+    "mg_coulomb_reset": [_P],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_set_potentials": [_P, _D, _D, _D, _D, _D],

@@ -36,6 +36,7 @@ struct CgArgs {
     int nx, ny, nz, mx, my, mz;
     double inv_dx2;
     double prec;
+    double rel;           // > 0: stop at |r| <= rel |src| instead of |r|^2 <= prec
     int maxit;
 };
 
@@ -127,8 +128,25 @@ __global__ void __launch_bounds__(kThreads) k_cg(CgArgs a) {
     }
     double s = block_sum(loc, sh);
     if (threadIdx.x == 0) red2[blockIdx.x] = s;
+    double prec = a.prec;
+    if (a.rel > 0.0) {
+        // |src|^2 over the stored box for the relative test
+        loc = 0.0;
+        for (long o = t0; o < M; o += stride) {
+            const int i = (int)(o % a.mx), j = (int)((o / a.mx) % a.my);
+            const int k = (int)(o / ((long)a.mx * a.my));
+            if (i < a.nx && j < a.ny && k < a.nz) loc = fma(a.src[o], a.src[o], loc);
+        }
+        s = block_sum(loc, sh);
+        if (threadIdx.x == 0) red1[blockIdx.x] = s;
+    }
     if (!grid_barrier(a.bar, a.status)) return;
     double pnorm = grid_total(red2, &bcast);
+    if (a.rel > 0.0) {
+        prec = a.rel * a.rel * grid_total(red1, &bcast);
+        // every block has read red1 before the first iteration rewrites it
+        if (!grid_barrier(a.bar, a.status)) return;
+    }
     int it;
     for (it = 1; it <= a.maxit; ++it) {
         // t = Lap(p), integral = r.t
@@ -156,7 +174,7 @@ __global__ void __launch_bounds__(kThreads) k_cg(CgArgs a) {
         if (threadIdx.x == 0) red2[blockIdx.x] = s;
         if (!grid_barrier(a.bar, a.status)) return;
         const double nn = grid_total(red2, &bcast);
-        if (nn <= a.prec) break;
+        if (nn <= prec) break;
         const double ck = nn / pnorm;
         pnorm = nn;
         for (long o = t0; o < M; o += stride) a.p[o] = fma(ck, a.p[o], a.res[o]);
@@ -424,6 +442,8 @@ int coulomb_setup(mg_ctx* c) {
     for (double** b : {&c->cpot, &c->csource, &c->cres, &c->cp, &c->ct})
         MG_CUDA(cudaMalloc(b, M * sizeof(double)));
     MG_CUDA(cudaMemcpy(c->cpot, guess.data(), M * sizeof(double), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMalloc(&c->cguess, M * sizeof(double)));
+    MG_CUDA(cudaMemcpy(c->cguess, guess.data(), M * sizeof(double), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&c->cg_bar, 4 * sizeof(unsigned)));
     MG_CUDA(cudaMalloc(&c->cg_status, 4 * sizeof(int)));
     int per_sm = 0;
@@ -533,6 +553,14 @@ int coulomb_residual(mg_ctx* c, double* rel) {
     return MG_OK;
 }
 
+// The potential back to InitialGuess (the start of a cold solve).
+int coulomb_reset(mg_ctx* c) {
+    if (!c->coulomb_init) MG_TRY(coulomb_setup(c));
+    MG_CUDA(cudaMemcpyAsync(c->cpot, c->cguess, c->M * sizeof(double), cudaMemcpyDeviceToDevice,
+                            c->stream));
+    return MG_OK;
+}
+
 int coulomb_solve(mg_ctx* c, int* iters) {
     if (!c->coulomb_init) MG_TRY(coulomb_setup(c));
     const long M = c->M;
@@ -540,6 +568,18 @@ int coulomb_solve(mg_ctx* c, int* iters) {
         c->rho + c->V, c->sh_ext, c->rpow_ext, c->moment_values, c->mfac, c->n_bc_moments, c->nx,
         c->ny, c->nz, c->mx, c->my, c->mz, c->f.e2, c->csource, c->cpot);
     MG_LAUNCHED(c);
+    if (c->p.coulomb_solver == 2) {
+        const double pi_ = 4.0 * std::atan2(1.0, 1.0);
+        const int maxit = c->p.coulomb_max > 0 ? c->p.coulomb_max : 500;
+        const int st = coulomb_multigrid(c, c->p.coulomb_prec > 0 ? c->p.coulomb_prec : 1e-10,
+                                         maxit, iters);
+        if (st < 0) return st;
+        k_coulomb_out<<<div_up(c->V, kThreads), kThreads, 0, c->stream>>>(
+            c->cpot, c->rho + c->V, c->nx, c->ny, c->nz, c->mx, c->my,
+            -std::pow(3 / pi_, 1 / 3.0) * c->f.e2, c->coulomb, c->coulex);
+        MG_LAUNCHED(c);
+        return st;
+    }
     if (c->cur_precision == MG_MIXED) {
         MG_TRY(coulomb_direct(c));
         const double pi = 4.0 * std::atan2(1.0, 1.0);
@@ -559,6 +599,7 @@ int coulomb_solve(mg_ctx* c, int* iters) {
     a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.mx = c->mx; a.my = c->my; a.mz = c->mz;
     a.inv_dx2 = 1.0 / (c->p.dx * c->p.dx);
     a.prec = 1.0e-9 / (c->p.dx * c->p.dx * c->p.dx * c->nx * c->ny * c->nz);
+    a.rel = c->p.coulomb_prec > 0 ? c->p.coulomb_prec : 0.0;
     a.maxit = c->p.coulomb_max > 0 ? c->p.coulomb_max : 500;
     void* args[] = {&a};
     MG_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg, dim3(c->cg_blocks), dim3(kThreads), args,

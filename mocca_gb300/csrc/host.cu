@@ -41,8 +41,10 @@ void free_all(mg_ctx* c) {
     F(c->gs_S); F(c->gs_R); F(c->gs_index);
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
-    F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast);
+    F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast); F(c->cguess);
     F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
+    multigrid_free(c->mgrid);
+    c->mgrid = nullptr;
     hfb_free(c);
     constraints_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
@@ -144,6 +146,8 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
         p->damping > 1.0)
         return MG_ERR_ARG;
     if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
+    if (p->coulomb_solver < 0 || p->coulomb_solver > 2 || !(p->coulomb_prec >= 0.0))
+        return MG_ERR_ARG;
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     mg_ctx* c = new mg_ctx();
@@ -505,6 +509,11 @@ extern "C" int mg_solve_coulomb(mg_ctx* c, int* iters) {
     const int st = coulomb_solve(c, &it);
     if (iters) *iters = it;
     return st;
+}
+
+extern "C" int mg_coulomb_reset(mg_ctx* c) {
+    if (!c || !c->folded) return MG_ERR_ARG;
+    return coulomb_reset(c);
 }
 
 extern "C" int mg_coulomb_residual(mg_ctx* c, double* rel) {

@@ -100,6 +100,8 @@ struct EigBatch {
     bool have_vectors = false;
 };
 
+struct Multigrid;   // multigrid.cu: levels and work vectors of the Coulomb multigrid
+
 struct PairCoef {
     double cut[2];
     double mu[2];
@@ -276,6 +278,8 @@ struct mg_ctx {
     size_t red_len = 0;
     int* flags = nullptr;              // device status flags
     bool coulomb_init = false;
+    mg::Multigrid* mgrid = nullptr;    // CoulombSolver = 2 (multigrid.cu)
+    double* cguess = nullptr;          // InitialGuess on the extended box (M)
     double* cfast = nullptr;           // 1-D eigenvectors and eigenvalues of the direct solve
     long cfast_off[3][2];              // [axis][0: C (n x n), 1: mu (n)]
 
@@ -340,6 +344,10 @@ int moments(mg_ctx* c);
 int coulomb_setup(mg_ctx* c);
 int coulomb_solve(mg_ctx* c, int* iters);
 int coulomb_residual(mg_ctx* c, double* rel);
+int coulomb_reset(mg_ctx* c);
+int coulomb_multigrid(mg_ctx* c, double tol, int maxit, int* iters);
+void multigrid_free(Multigrid* M);
+int multigrid_levels(const mg_ctx* c);
 int potentials(mg_ctx* c);
 int energy(mg_ctx* c, mg_energy_terms* out);
 int basis_dots(mg_ctx* c, const double* a, const double* b, double* out, bool b_df = false);

@@ -82,6 +82,7 @@ class RunParams:
     damping: float = 0.75       # DampingParam
     precon_u: float = 1.0       # preconu
     parameter_estimation: int = 0   # ParameterEstimation: 1 estimates dt, momentum every step
+    coulomb_prec: float = 0.0   # > 0: relative residual of the CG / multigrid Coulomb solves
     extra: dict = field(default_factory=dict)
 
     @property

@@ -237,6 +237,10 @@ class MeshState:
         self._call("mg_solve_coulomb", C.byref(it), allow_not_converged=True)
         return it.value
 
+    def reset_coulomb_guess(self):
+        """The Coulomb potential back to InitialGuess (mg_coulomb_reset)."""
+        self._call("mg_coulomb_reset")
+
     def CoulombResidual(self) -> float:
         """|b - L phi| / |b| of the last Coulomb solve (mg_coulomb_residual)."""
         r = C.c_double(0.0)
