@@ -140,7 +140,12 @@ typedef struct mg_pairing_params {
     int    fermi_solver;  /* 0: Newton with the analytic dN/dlambda (this    */
                           /* library's default); 1: the reference's damped   */
                           /* Broyden search (HFBFindFermiEnergyBroyden,      */
-                          /* src/HFB.f90:1849-2161), iterate for iterate     */
+                          /* src/HFB.f90:1849-2161), iterate for iterate;    */
+                          /* 2: the gradient solver (FermiSolver 'GRADIENT', */
+                          /* HFBFermiGradient src/GradientHFB.f90:473-733),  */
+                          /* max_iter gradient steps at most (the reference  */
+                          /* defaults HFBIter to 500 for it); its first U, V */
+                          /* come from one diagonalisation at fermi_start    */
 } mg_pairing_params;
 
 /* Per-call diagnostics of the HFB pairing step. */

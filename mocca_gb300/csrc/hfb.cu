@@ -449,6 +449,8 @@ void hfb_free(mg_ctx* c) {
         if (g) cudaGraphExecDestroy(g);
     eig_free(H.eT);
     eig_free(H.eR);
+    gradient_hfb_free(H.grad);
+    H.grad = nullptr;
 }
 
 // One particle-number evaluation at lambda (both isospins): T(lambda),
@@ -544,6 +546,12 @@ static int hfb_evaluate(mg_ctx* c, const double* lam, double* N_out, double* dN_
     H.qp_gap[1] = std::min(hp[14], hp[15]);
     if (std::isnan(N_out[0]) || std::isnan(N_out[1])) return MG_ERR_NAN;
     return MG_OK;
+}
+
+// One evaluation at lambda from the Jacobi seed (the gradient solver's first
+// U and V).
+int hfb_evaluate_at(mg_ctx* c, const double* lam, double* N_out, double* dN_out) {
+    return hfb_evaluate(c, lam, N_out, dN_out, true);
 }
 
 // rho, kappa and the quasiparticle energies moved to lambda + dl from the
@@ -745,7 +753,9 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     bool conv[2];
     int evals = 0;
     bool first_order = false;
-    if (H.pp.fermi_solver == 1) {
+    if (H.pp.fermi_solver == 2) {
+        MG_TRY(fermi_gradient(c, lam, f, conv, &evals));
+    } else if (H.pp.fermi_solver == 1) {
         MG_TRY(fermi_broyden(c, lam, f, conv, &evals));
     } else {
         MG_TRY(fermi_newton(c, lam, f, conv, &evals, &first_order));

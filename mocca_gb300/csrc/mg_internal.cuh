@@ -101,6 +101,7 @@ struct EigBatch {
 };
 
 struct Multigrid;   // multigrid.cu: levels and work vectors of the Coulomb multigrid
+struct GradHfb;     // gradient_hfb.cu: U, V and work matrices of the gradient solver
 
 struct PairCoef {
     double cut[2];
@@ -154,6 +155,7 @@ struct Hfb {
     GemmDesc* d_taylor = nullptr;    // 4 + 8 + 8 + 4 descriptors
     long long taylor_steps = 0;      // pairing steps finished by the expansion
     int nref = 2;             // FP64 refinement steps per eigen-decomposition
+    GradHfb* grad = nullptr;  // fermi_solver 2 (gradient_hfb.cu)
 };
 
 // One multipole constraint of the alternating kind (constraints.cu): the
@@ -361,6 +363,10 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
 enum EigSeed { kSeedCold = 0, kSeedJacobiWarm = 1, kSeedRefine = 2 };
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish);
 int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim);
+int gemm_batched_skip(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim, int* done);
+int hfb_evaluate_at(mg_ctx* c, const double* lam, double* N_out, double* dN_out);
+int fermi_gradient(mg_ctx* c, double lam[2], double f[2], bool conv[2], int* iters);
+void gradient_hfb_free(GradHfb* g);
 int eig_jacobi_fp64(mg_ctx* c, EigBatch& E);
 void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);

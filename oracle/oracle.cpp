@@ -88,6 +88,12 @@ struct orc_ctx {
     std::vector<double> rho_h[4], kappa_h[4], oldrho[4], oldkappa[4], delta[4];
     std::vector<double> Um[4], Vm[4], qe[4], cantr[4], occs[4];
     double fermi[2] = {-10.0, -10.0};
+    // HFBFermiGradient (src/GradientHFB.f90): GradU, GradV of every block
+    // (N x N, the N columns the CR8 choice keeps) and the positive-signature
+    // column count SigBlocks
+    bool ghfb_ready = false;
+    std::vector<double> GU[4], GV[4];
+    int gsig[4] = {0, 0, 0, 0};
     std::vector<double> pcut, dfac, pf_re, pf_im;
     double epair[2] = {0.0, 0.0};
     double pdisp[2] = {0.0, 0.0};
@@ -2030,6 +2036,248 @@ static void hfb_energy(orc_ctx* c) {
 }
 
 // SolvePairing, src/Pairing.f90:743-890
+// --------------------------------------------------------------------------
+// HFBFermiGradient, src/GradientHFB.f90:473-733 (FermiSolver 'GRADIENT',
+// signature conserved: H20_sig :1014-1068, N20 :1070-1108, GradUpdate_sig
+// :884-920, ortho_sig :1148-1222; HFBReduce off, no blocking, no
+// Lipkin-Nogami, FermiMomentum off so step = 0.020 and mu = 0).  The U and V
+// it starts from are GetUandV's (:108-186): the module's U and V, which the
+// reference has from an earlier diagonalisation or a restart file; here the
+// first call takes them from one diagonalisation at the Fermi energies the
+// step starts from (hfb_number).  Later calls continue from the solver's own
+// GradU, GradV.  Matrices are N x N row-major, 0-based.
+// --------------------------------------------------------------------------
+static void ghfb_matmul(const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                        int m, int n, int k, bool ta) {
+    // C(m x n) = op(A) B with op(A) = A or A^T, sums in index order
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < n; ++j) {
+            double x = 0.0;
+            for (int q = 0; q < k; ++q)
+                x += (ta ? A[(size_t)q * lda + i] : A[(size_t)i * lda + q]) * B[(size_t)q * ldb + j];
+            C[(size_t)i * ldc + j] = x;
+        }
+}
+
+static int fermi_gradient(orc_ctx* c, int* iters_out) {
+    const Basis& B = c->bas[MG_HF_BASIS];
+    const int nwt = c->p.nwt;
+    if (!c->ghfb_ready) {
+        double Nt[2];
+        const int st = hfb_number(c, c->fermi, Nt);
+        if (st != MG_OK) return st;
+        for (int b = 0; b < 4; ++b) {
+            const int N = (int)c->bidx[b].size(), h = N / 2, N2 = 2 * N;
+            c->GU[b].assign((size_t)N * N, 0.0);
+            c->GV[b].assign((size_t)N * N, 0.0);
+            // the CR8 columns h..N-1 and 2N-h..2N-1, in increasing order
+            int ind = 0;
+            for (int j = 0; j < N2; ++j) {
+                const bool in = (j >= h && j < N) || j >= N2 - h;
+                if (!in) continue;
+                for (int i = 0; i < N; ++i) {
+                    c->GU[b][(size_t)i * N + ind] = c->Um[b][(size_t)i * N2 + j];
+                    c->GV[b][(size_t)i * N + ind] = c->Vm[b][(size_t)i * N2 + j];
+                }
+                bool sig = false;
+                for (int i = 0; i < h; ++i) sig = sig || std::fabs(c->GU[b][(size_t)i * N + ind]) > 1e-10;
+                for (int i = h; i < N; ++i) sig = sig || std::fabs(c->GV[b][(size_t)i * N + ind]) > 1e-10;
+                if (sig) ++c->gsig[b];
+                ++ind;
+            }
+        }
+        c->ghfb_ready = true;
+    }
+    const double prec = c->pp.fermi_prec;
+    const int maxit = c->pp.max_iter > 0 ? c->pp.max_iter : 500;
+    const double particles[2] = {c->p.neutrons, c->p.protons};
+    const double step = 0.020;
+    bool conv[2] = {false, false};
+    double n20norm[2] = {0.0, 0.0}, par[2] = {0.0, 0.0};
+    std::vector<double> grad[4], an20[4];
+    double gnorm[4] = {0.0, 0.0, 0.0, 0.0};
+    int iter = 0;
+    for (iter = 1; iter <= maxit; ++iter) {
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            n20norm[it] = 0.0;
+            for (int b = 2 * it; b < 2 * it + 2; ++b) {
+                const int N = (int)c->bidx[b].size(), h = N / 2, S = c->gsig[b];
+                const std::vector<double>& U = c->GU[b];
+                const std::vector<double>& V = c->GV[b];
+                const std::vector<double>& D = c->delta[b];
+                std::vector<double> e(N);
+                for (int i = 0; i < N; ++i) e[i] = B.e[c->bidx[b][i] % nwt];
+                // H20_sig: hU, hV, DsV, DsU (only the halves the formula reads)
+                std::vector<double> hU((size_t)N * N, 0.0), hV((size_t)N * N, 0.0),
+                    DsV((size_t)N * N, 0.0), DsU((size_t)N * N, 0.0);
+                for (int i = 0; i < h; ++i)
+                    for (int j = 0; j < S; ++j) hU[(size_t)i * N + j] = e[i] * U[(size_t)i * N + j];
+                for (int i = h; i < N; ++i)
+                    for (int j = 0; j < S; ++j) hV[(size_t)i * N + j] = e[i] * V[(size_t)i * N + j];
+                ghfb_matmul(&D[h], N, &V[(size_t)h * N], N, DsV.data(), N, h, S, N - h, false);
+                ghfb_matmul(&D[(size_t)h * N], N, U.data(), N, &DsU[(size_t)h * N], N, N - h, S, h,
+                            false);
+                std::vector<double>& G = grad[b];
+                G.assign((size_t)N * N, 0.0);
+                const int m = N - S;
+                std::vector<double> t1((size_t)m * S), t2((size_t)m * S), t3((size_t)m * S),
+                    t4((size_t)m * S);
+                ghfb_matmul(&U[(size_t)h * N + S], N, &hV[(size_t)h * N], N, t1.data(), S, m, S,
+                            N - h, true);
+                ghfb_matmul(&V[S], N, DsV.data(), N, t2.data(), S, m, S, h, true);
+                ghfb_matmul(&U[(size_t)h * N + S], N, &DsU[(size_t)h * N], N, t3.data(), S, m, S,
+                            N - h, true);
+                ghfb_matmul(&V[S], N, hU.data(), N, t4.data(), S, m, S, h, true);
+                for (int i = 0; i < m; ++i)
+                    for (int j = 0; j < S; ++j) {
+                        double x = t1[(size_t)i * S + j];
+                        x = x - t2[(size_t)i * S + j];
+                        x = x + t3[(size_t)i * S + j];
+                        x = x - t4[(size_t)i * S + j];
+                        G[(size_t)(S + i) * N + j] = x;
+                        G[(size_t)j * N + S + i] = -x;
+                    }
+                // N20 with signature: N20(0:S, S:N) = U(0:h,0:S)^T V(0:h,S:N)
+                //                                   - V(h:N,0:S)^T U(h:N,S:N)
+                std::vector<double>& A = an20[b];
+                A.assign((size_t)N * N, 0.0);
+                std::vector<double> u1((size_t)S * m), u2((size_t)S * m);
+                ghfb_matmul(U.data(), N, &V[S], N, u1.data(), m, S, m, h, true);
+                ghfb_matmul(&V[(size_t)h * N], N, &U[(size_t)h * N + S], N, u2.data(), m, S, m,
+                            N - h, true);
+                for (int i = 0; i < S; ++i)
+                    for (int j = 0; j < m; ++j) {
+                        const double x = u1[(size_t)i * m + j] - u2[(size_t)i * m + j];
+                        A[(size_t)i * N + S + j] = x;
+                        A[(size_t)(S + j) * N + i] = -x;
+                    }
+                for (int j = 0; j < N; ++j)
+                    for (int i = 0; i < N; ++i) n20norm[it] += A[(size_t)i * N + j] * A[(size_t)i * N + j];
+            }
+        }
+        // Fermi energies from the particle numbers of the current V
+        for (int it = 0; it < 2; ++it) {
+            par[it] = 0.0;
+            for (int b = 2 * it; b < 2 * it + 2; ++b) {
+                const int N = (int)c->bidx[b].size();
+                for (int i = 0; i < N; ++i)
+                    for (int j = 0; j < N; ++j) par[it] += c->GV[b][(size_t)i * N + j] * c->GV[b][(size_t)i * N + j];
+            }
+            if (std::fabs(n20norm[it]) > 1e-10)
+                c->fermi[it] = c->fermi[it] + (particles[it] - par[it]) / n20norm[it];
+            else
+                c->fermi[it] = c->fermi[it] + 0.1 * (particles[it] - par[it]);
+        }
+        // total gradient and convergence
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            bool ok = std::fabs(par[it] - particles[it]) < prec;
+            for (int b = 2 * it; b < 2 * it + 2; ++b) {
+                const int N = (int)c->bidx[b].size();
+                for (size_t q = 0; q < (size_t)N * N; ++q) grad[b][q] = grad[b][q] - c->fermi[it] * an20[b][q];
+                gnorm[b] = 0.0;
+                for (int i = 0; i < N; ++i)
+                    for (int j = 0; j < N; ++j) gnorm[b] += grad[b][(size_t)i * N + j] * grad[b][(size_t)j * N + i];
+                ok = ok && std::sqrt(std::fabs(gnorm[b])) < prec;
+            }
+            conv[it] = ok;
+        }
+        // gradient step and orthonormalisation
+        for (int it = 0; it < 2; ++it) {
+            if (conv[it]) continue;
+            for (int b = 2 * it; b < 2 * it + 2; ++b) {
+                const int N = (int)c->bidx[b].size(), h = N / 2, S = c->gsig[b], m = N - S;
+                std::vector<double>& U = c->GU[b];
+                std::vector<double>& V = c->GV[b];
+                const std::vector<double> tU = U, tV = V;
+                const std::vector<double>& G = grad[b];
+                std::vector<double> w;
+                // U(0:h,0:S) -= step tV(0:h,S:N) G(S:N,0:S)
+                w.assign((size_t)h * S, 0.0);
+                ghfb_matmul(&tV[S], N, &G[(size_t)S * N], N, w.data(), S, h, S, m, false);
+                for (int i = 0; i < h; ++i)
+                    for (int j = 0; j < S; ++j) U[(size_t)i * N + j] = U[(size_t)i * N + j] - step * w[(size_t)i * S + j];
+                // U(h:N,S:N) -= step tV(h:N,0:S) G(0:S,S:N)
+                w.assign((size_t)(N - h) * m, 0.0);
+                ghfb_matmul(&tV[(size_t)h * N], N, &G[S], N, w.data(), m, N - h, m, S, false);
+                for (int i = 0; i < N - h; ++i)
+                    for (int j = 0; j < m; ++j)
+                        U[(size_t)(h + i) * N + S + j] = U[(size_t)(h + i) * N + S + j] - step * w[(size_t)i * m + j];
+                // V(0:h,S:N) -= step tU(0:h,0:S) G(0:S,S:N)
+                w.assign((size_t)h * m, 0.0);
+                ghfb_matmul(tU.data(), N, &G[S], N, w.data(), m, h, m, S, false);
+                for (int i = 0; i < h; ++i)
+                    for (int j = 0; j < m; ++j) V[(size_t)i * N + S + j] = V[(size_t)i * N + S + j] - step * w[(size_t)i * m + j];
+                // V(h:N,0:S) -= step tU(h:N,S:N) G(S:N,0:S)
+                w.assign((size_t)(N - h) * S, 0.0);
+                ghfb_matmul(&tU[(size_t)h * N + S], N, &G[(size_t)S * N], N, w.data(), S, N - h, S, m,
+                            false);
+                for (int i = 0; i < N - h; ++i)
+                    for (int j = 0; j < S; ++j)
+                        V[(size_t)(h + i) * N + j] = V[(size_t)(h + i) * N + j] - step * w[(size_t)i * S + j];
+                // ortho_sig
+                for (int j = 0; j < S; ++j) {
+                    double ov = 0.0;
+                    for (int i = 0; i < h; ++i) ov = ov + U[(size_t)i * N + j] * U[(size_t)i * N + j];
+                    for (int i = h; i < N; ++i) ov = ov + V[(size_t)i * N + j] * V[(size_t)i * N + j];
+                    ov = 1.0 / std::sqrt(ov);
+                    for (int i = 0; i < h; ++i) U[(size_t)i * N + j] = U[(size_t)i * N + j] * ov;
+                    for (int i = h; i < N; ++i) V[(size_t)i * N + j] = V[(size_t)i * N + j] * ov;
+                    for (int i = j + 1; i < h; ++i) {
+                        double o = 0.0;
+                        for (int k = 0; k < h; ++k) o = o + U[(size_t)k * N + j] * U[(size_t)k * N + i];
+                        for (int k = h; k < N; ++k) o = o + V[(size_t)k * N + j] * V[(size_t)k * N + i];
+                        for (int k = 0; k < h; ++k) U[(size_t)k * N + i] = U[(size_t)k * N + i] - o * U[(size_t)k * N + j];
+                        for (int k = h; k < N; ++k) V[(size_t)k * N + i] = V[(size_t)k * N + i] - o * V[(size_t)k * N + j];
+                    }
+                }
+                for (int j = S; j < N; ++j) {
+                    double ov = 0.0;
+                    for (int i = 0; i < h; ++i) ov = ov + V[(size_t)i * N + j] * V[(size_t)i * N + j];
+                    for (int i = h; i < N; ++i) ov = ov + U[(size_t)i * N + j] * U[(size_t)i * N + j];
+                    ov = 1.0 / std::sqrt(ov);
+                    for (int i = h; i < N; ++i) U[(size_t)i * N + j] = U[(size_t)i * N + j] * ov;
+                    for (int i = 0; i < h; ++i) V[(size_t)i * N + j] = V[(size_t)i * N + j] * ov;
+                    for (int i = j + 1; i < N; ++i) {
+                        double o = 0.0;
+                        for (int k = 0; k < h; ++k) o = o + V[(size_t)k * N + j] * V[(size_t)k * N + i];
+                        for (int k = h; k < N; ++k) o = o + U[(size_t)k * N + j] * U[(size_t)k * N + i];
+                        for (int k = h; k < N; ++k) U[(size_t)k * N + i] = U[(size_t)k * N + i] - o * U[(size_t)k * N + j];
+                        for (int k = 0; k < h; ++k) V[(size_t)k * N + i] = V[(size_t)k * N + i] - o * V[(size_t)k * N + j];
+                    }
+                }
+            }
+        }
+        if (conv[0] && conv[1]) break;
+    }
+    *iters_out = std::min(iter, maxit);
+    // OutHFBModule: rho = V V^T, kappa(i > j) = sum_k V(i,k) U(j,k) over the
+    // kept columns (constructRhoHFB / ConstructKappaHFB, src/HFB.f90:3128-3154,
+    // :3335-3359)
+    for (int b = 0; b < 4; ++b) {
+        const int N = (int)c->bidx[b].size();
+        const std::vector<double>& U = c->GU[b];
+        const std::vector<double>& V = c->GV[b];
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                double x = 0.0;
+                for (int k = 0; k < N; ++k) x += V[(size_t)i * N + k] * V[(size_t)j * N + k];
+                c->rho_h[b][(size_t)i * N + j] = x;
+            }
+        for (int j = 0; j < N; ++j) {
+            c->kappa_h[b][(size_t)j * N + j] = 0.0;
+            for (int i = j + 1; i < N; ++i) {
+                double x = 0.0;
+                for (int k = 0; k < N; ++k) x += V[(size_t)i * N + k] * U[(size_t)j * N + k];
+                c->kappa_h[b][(size_t)i * N + j] = x;
+                c->kappa_h[b][(size_t)j * N + i] = -x;
+            }
+        }
+    }
+    return (conv[0] && conv[1]) ? MG_OK : MG_NOT_CONVERGED;
+}
+
 extern "C" int orc_solve_pairing(orc_ctx* c, mg_pairing_info* info) {
     if (!c || c->p.pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
     if (!c->hfb_ready) {
@@ -2051,7 +2299,7 @@ extern "C" int orc_solve_pairing(orc_ctx* c, mg_pairing_info* info) {
     pairing_field(c);
     pairing_gaps(c);
     int evals = 0;
-    const int st = fermi_broyden(c, &evals);
+    const int st = c->pp.fermi_solver == 2 ? fermi_gradient(c, &evals) : fermi_broyden(c, &evals);
     if (st < 0 && st != MG_ERR_STATE) return st;
     double tr[2] = {0.0, 0.0};
     for (int b = 0; b < 4; ++b) {

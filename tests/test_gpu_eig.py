@@ -111,3 +111,43 @@ def test_batch_of_64(built):
         mats.append(x + x.T)
     for m, (w, z) in zip(mats, _run(mats)):
         _check(m, w, z)
+
+
+def test_density_matrix_with_near_one_cluster(built):
+    """A density-matrix block of an HFB start whose occupations near one lie
+    within 3e-8 of each other (0.999999935, 0.999999964 twice) and near zero
+    within 3e-12: the refinement leaves that cluster unrotated, and the
+    polish must start from vectors orthonormal to FP64 rounding, or its
+    eigenvalues miss by the non-orthogonality (1.4e-7 was seen, above one)."""
+    rng = np.random.default_rng(8)
+    occ = np.array([2.13e-12, 2.41e-12, 2.55e-12, 2.93e-12, 3.04e-12, 3.56e-12, 3.56e-12,
+                    3.96e-12, 4.60e-12, 4.94e-12, 0.999999935, 0.999999964, 0.999999964])
+    mats = [_sym(rng, 13, occ) for _ in range(3)]
+    for m, (w, z) in zip(mats, _run(mats)):
+        _check(m, w, z)
+        assert w.max() <= 1.0
+
+
+def test_density_matrix_of_an_hfb_start(built):
+    """The rho_++ blocks of the first pairing step of the perturbed-HO 10^3
+    start (oracle), one of which has that near-one cluster: eigenvalues to
+    the usual bars, none above one."""
+    import oracle as O
+    from mocca_gb300 import SLY4
+    from test_gpu_gradient_hfb import _start
+    p, psi, qn, en, pp = _start()
+    pp.fermi_solver = 1
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    o.set_energies(en)
+    o.set_pairing(pp)
+    o.SolvePairing()
+    mats = []
+    for b in range(4):
+        r = o.get_hfb_block(b)[0]
+        h = r.shape[0] // 2
+        mats.append(np.ascontiguousarray(r[:h, :h]))
+    o.close()
+    for m, (w, z) in zip(mats, _run(mats)):
+        _check(m, w, z)
+        assert w.max() <= 1.0 + 1e-13

@@ -114,7 +114,7 @@ def test_unknown_fermi_solver_is_rejected(built):
                   pairing=_abi.MG_PAIRING_HFB)
     g = MeshState(p, SLY4)
     pp = _abi.MgPairingParams.defaults()
-    pp.fermi_solver = 2
+    pp.fermi_solver = 3
     with pytest.raises(_abi.MgError):
         g.set_pairing(pp)
     pp.fermi_solver = 1
