@@ -33,6 +33,7 @@ module mocca_gpu
     real(c_double) :: precon_u
     integer(c_int) :: parameter_estimation
     real(c_double) :: coulomb_prec
+    real(c_double) :: omega(3)
   end type mg_params
   type, bind(C) :: mg_force
     real(c_double) :: t0
@@ -390,6 +391,17 @@ module mocca_gpu
       type(c_ptr), value :: divw
       type(c_ptr), value :: coul
       type(c_ptr), value :: coulex
+    end function
+    integer(c_int) function mg_get_time_odd(ctx, vecj, vecs, rotj, rots, a, s, diva) bind(C, name="mg_get_time_odd")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: vecj
+      type(c_ptr), value :: vecs
+      type(c_ptr), value :: rotj
+      type(c_ptr), value :: rots
+      type(c_ptr), value :: a
+      type(c_ptr), value :: s
+      type(c_ptr), value :: diva
     end function
     integer(c_int) function mg_set_potentials(ctx, u, b, nablab, w, divw) bind(C, name="mg_set_potentials")
       import

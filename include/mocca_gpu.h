@@ -88,6 +88,10 @@ typedef struct mg_params {
                                   coulomb_prec |b| on the stored box; 0: the reference's CG
                                   test |r|^2 <= 1e-9 / (dx^3 V) (src/Coulomb.f90:755-900), and
                                   1e-10 relative for the multigrid */
+    double omega[3];           /* cranking frequencies OmegaX, OmegaY, OmegaZ (CrankType 0,
+                                  fixed; src/Cranking.f90:24-60); nonzero only with trc = 0,
+                                  and with EV8 symmetry only OmegaZ (the reference stops on
+                                  OmegaX with signature and OmegaY with time simplex) */
 } mg_params;
 
 /*
@@ -374,6 +378,15 @@ int mg_construct_potentials(mg_ctx* ctx, int* coulomb_iters);
 /* U,B,coul,coulex: 2V/2V/V/V; nablab,divw: 6V; w: 18V; any may be NULL. */
 int mg_get_potentials(mg_ctx* ctx, double* u, double* b, double* nablab,
                       double* w, double* divw, double* coul, double* coulex);
+
+/* Time-odd densities and fields of a run without time reversal (trc = 0):
+ * vecj, vecs and their curls (ComputeDensity's time-odd part,
+ * src/Densities.f90:1004-1106), A and S with the cranking fields (CalcAPot,
+ * CalcSPot, src/MeanFields.f90:411-492, :618-712; CrankAPot, CrankSPot,
+ * src/Cranking.f90:234-324) as [it][m][V] (6V each), div A as [it][V] (2V);
+ * any may be NULL.  MG_ERR_ARG with time reversal. */
+int mg_get_time_odd(mg_ctx* ctx, double* vecj, double* vecs, double* rotj, double* rots,
+                    double* a, double* s, double* diva);
 int mg_set_potentials(mg_ctx* ctx, const double* u, const double* b,
                       const double* nablab, const double* w, const double* divw);
 

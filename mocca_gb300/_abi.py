@@ -49,6 +49,7 @@ class MgParams(C.Structure):
         ("precon_u", C.c_double),
         ("parameter_estimation", C.c_int),
         ("coulomb_prec", C.c_double),
+        ("omega", C.c_double * 3),
     ]
 
 
@@ -193,6 +194,7 @@ SIGNATURES = {
     "mg_solve_coulomb": [_P, _I],
     "mg_coulomb_residual": [_P, _D],
     "mg_coulomb_reset": [_P],
+    "mg_get_time_odd": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_set_potentials": [_P, _D, _D, _D, _D, _D],

@@ -229,14 +229,9 @@ int rutz_cutoff(mg_ctx* c) {
 
 }  // namespace
 
-int add_constraint(mg_ctx* c, const mg_moment_constraint* mc) {
+// The cutoff's buffers (first constraint, or the cranking fields).
+static int cutoff_alloc(mg_ctx* c) {
     Constraints& K = c->cons;
-    if (!c->folded || mc->l < 1 || mc->l > 10 || mc->m < 0 || mc->m > mc->l ||
-        (int)K.list.size() >= kMaxConstraints)
-        return MG_ERR_ARG;
-    // moments kept by the conserved symmetries (NewMoment_Electric,
-    // src/Moments.f90:787-884, quantisation axis z): EV8 keeps even l, even m
-    if ((c->p.pc && mc->l % 2) || (c->p.sc && mc->m % 2)) return MG_ERR_ARG;
     const long V = c->V;
     if (!K.cut) {
         K.cap = 3L * std::max(1, c->nx - 1) * std::max(1, c->ny - 1) * std::max(1, c->nz - 1);
@@ -252,6 +247,25 @@ int add_constraint(mg_ctx* c, const mg_moment_constraint* mc) {
             return MG_ERR_CUDA;
         }
     }
+    return MG_OK;
+}
+
+int cranking_cutoff(mg_ctx* c) {
+    if (!c->folded) return MG_ERR_ARG;
+    MG_TRY(cutoff_alloc(c));
+    return rutz_cutoff(c);
+}
+
+int add_constraint(mg_ctx* c, const mg_moment_constraint* mc) {
+    Constraints& K = c->cons;
+    if (!c->folded || mc->l < 1 || mc->l > 10 || mc->m < 0 || mc->m > mc->l ||
+        (int)K.list.size() >= kMaxConstraints)
+        return MG_ERR_ARG;
+    // moments kept by the conserved symmetries (NewMoment_Electric,
+    // src/Moments.f90:787-884, quantisation axis z): EV8 keeps even l, even m
+    if ((c->p.pc && mc->l % 2) || (c->p.sc && mc->m % 2)) return MG_ERR_ARG;
+    const long V = c->V;
+    MG_TRY(cutoff_alloc(c));
     const int q = (int)K.list.size();
     std::vector<double> sh(V);
     for (int k = 0; k < c->nz; ++k)

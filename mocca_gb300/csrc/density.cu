@@ -191,7 +191,9 @@ int densities(mg_ctx* c) {
                                                                    c->nablaj);
     MG_LAUNCHED(c);
     // grad rho, lap rho: the first two field jobs
-    return run_jobs(c, c->field_jobs, 2);
+    MG_TRY(run_jobs(c, c->field_jobs, 2));
+    if (!c->p.trc) MG_TRY(time_odd_densities(c, B));
+    return MG_OK;
 }
 
 }  // namespace mg

@@ -191,6 +191,7 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     t[11] = B.B9q * S[14] + B.B9q * S[15];
     t[32] = B.B7b * S[5];
     t[33] = B.B8b * S[16] + B.B8b * S[17];
+    if (!c->p.trc) MG_TRY(time_odd_energy(c, t));
     for (int q = 0; q < 36; ++q) t[q] *= c->dv;
     double sk = 0.0;
     for (int q = 0; q < 36; ++q) sk += t[q];

@@ -187,6 +187,7 @@ int potentials(mg_ctx* c) {
     MG_TRY(run_jobs(c, c->field_jobs + 2, c->n_field_jobs - 2));
     k_sum3<<<div_up(6 * V, kThreads), kThreads, 0, c->stream>>>(c->divw_tmp, 6 * V, c->divW);
     MG_LAUNCHED(c);
+    if (!c->p.trc) MG_TRY(time_odd_potentials(c));
     return MG_OK;
 }
 
@@ -196,7 +197,11 @@ int moments(mg_ctx* c) {
                                                             c->moment_values);
         MG_LAUNCHED(c);
     }
-    return constraint_moments(c);   // constraints.cu (nothing without constraints)
+    MG_TRY(constraint_moments(c));   // constraints.cu (nothing without constraints)
+    // the cranking fields need the cutoff too (CompCutoff runs in every
+    // CalculateAllMoments, src/Moments.f90:2267)
+    if (cranking(c) && c->cons.list.empty()) MG_TRY(cranking_cutoff(c));
+    return MG_OK;
 }
 
 }  // namespace mg

@@ -43,6 +43,8 @@ void free_all(mg_ctx* c) {
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast); F(c->cguess);
     F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
+    F(c->odd); F(c->odd_hist); F(c->Apot); F(c->Spot); F(c->divA); F(c->odd_der); F(c->odd_tmp);
+    F(c->odd_jobs);
     multigrid_free(c->mgrid);
     c->mgrid = nullptr;
     hfb_free(c);
@@ -148,6 +150,14 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
     if (p->coulomb_solver < 0 || p->coulomb_solver > 2 || !(p->coulomb_prec >= 0.0))
         return MG_ERR_ARG;
+    // time reversal broken: the time-odd fields (timeodd.cu) on the EV8 box,
+    // HF filling, FP64; cranking only then, and with EV8 only about z (the
+    // reference stops on OmegaX with signature, OmegaY with time simplex)
+    const bool crank = p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0;
+    if (crank && p->trc) return MG_ERR_ARG;
+    if ((p->sc && p->omega[0] != 0.0) || (p->tsc && p->omega[1] != 0.0)) return MG_ERR_ARG;
+    if (!p->trc && (!ev8 || p->precision != MG_FP64 || p->pairing != MG_PAIRING_HF))
+        return MG_ERR_ARG;
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     mg_ctx* c = new mg_ctx();
@@ -219,6 +229,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     if ((st = upload_matrices(c)) != MG_OK) return fail(st);
     if ((st = build_field_jobs(c)) != MG_OK) return fail(st);
     if ((st = mixing_setup(c)) != MG_OK) return fail(st);
+    if (!p->trc && (st = time_odd_setup(c)) != MG_OK) return fail(st);
     if (ev8 && p->coulomb_solver != 0) {
         if ((st = coulomb_setup(c)) != MG_OK) return fail(st);
     }
@@ -228,6 +239,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
 
 extern "C" int mg_set_precision(mg_ctx* c, int precision) {
     if (!c || (precision != MG_FP64 && precision != MG_MIXED)) return MG_ERR_ARG;
+    if (!c->p.trc && precision != MG_FP64) return MG_ERR_ARG;   // time-odd path: FP64
     c->cur_precision = precision;
     return MG_OK;
 }

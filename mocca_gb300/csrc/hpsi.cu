@@ -29,6 +29,11 @@ struct Fields {
     const double* nablaB;
     const double* W;
     const double* divW;
+    // time-odd fields without time reversal ([it][m][V], div A [it][V]);
+    // nullptr with time reversal
+    const double* A = nullptr;
+    const double* S = nullptr;
+    const double* divA = nullptr;
 };
 
 __device__ __forceinline__ void pauli(const double* p, int dir, double* o) {
@@ -95,6 +100,31 @@ k_hpsi(double* __restrict__ psi, const double* __restrict__ der,
             const double b = t - sd;
             const double u = Uq * p[l];
             h[l] = (b + u) + wf[l];
+        }
+        if (F.A) {
+            // ActionOfS: sum_m S_m sigma_m psi; ActionOfA: -i (sum_m A_m d_m psi
+            // + 1/2 div A psi) (src/MeanFields.f90:1107-1147)
+            double sa[4] = {0.0, 0.0, 0.0, 0.0}, aa[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                double sg[4];
+                pauli(p, m + 1, sg);
+                const double sm = F.S[(it * 3 + m) * V + v], am = F.A[(it * 3 + m) * V + v];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    sa[l] = fma(sm, sg[l], sa[l]);
+                    aa[l] = fma(am, d[m][l], aa[l]);
+                }
+            }
+            const double hd = 0.5 * F.divA[it * V + v];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) aa[l] = fma(hd, p[l], aa[l]);
+            const double af[4] = {aa[1], -aa[0], aa[3], -aa[2]};
+#pragma unroll
+            for (int l = 0; l < 4; ++l) h[l] = (h[l] + sa[l]) + af[l];
+        }
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
             s_eh = fma(p[l], h[l], s_eh);
             s_hh = fma(h[l], h[l], s_hh);
         }
@@ -316,7 +346,7 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     if (!B.have_qn) return MG_ERR_STATE;
     const long V = c->V;
     const int nchunk = div_up(V, kThreads);
-    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW};
+    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW, c->Apot, c->Spot, c->divA};
     const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
     const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
     dim3 grid(nchunk, c->p.nwt);
@@ -358,7 +388,7 @@ int hpsi_single(mg_ctx* c, double* psi, const double* der, const double* lap, co
                 double* out, double* e_dev) {
     const long V = c->V;
     const int nchunk = div_up(V, kThreads);
-    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW};
+    Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW, c->Apot, c->Spot, c->divA};
     const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
     const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
     k_hpsi<false><<<dim3(nchunk, 1), kThreads, 0, c->stream>>>(psi, der, lap, qn_dev, F, out,

@@ -289,6 +289,13 @@ struct mg_ctx {
     double* dhist = nullptr;           // previous densities: rho, tau, nablaj, derrho, laprho (14V)
     bool have_dhist = false;
     double* Uold = nullptr;            // UpotOld (2V)
+    // time-odd densities and fields without time reversal (timeodd.cu):
+    // odd = [vecj 6V, vecs 6V, rot j 6V, rot s 6V] ([it][m][V] each), its
+    // history for the mixing, A and S ([it][m][V]), div A ([it][V]), the
+    // derivative scratch of the curls (36V) and of div A (6V), 18 jobs
+    double *odd = nullptr, *odd_hist = nullptr, *Apot = nullptr, *Spot = nullptr,
+           *divA = nullptr, *odd_der = nullptr, *odd_tmp = nullptr;
+    mg::GridJob* odd_jobs = nullptr;
     bool have_uold = false;            // UpotOld not all zero
     double* pc_buf = nullptr;          // preconditioner CG: res, dir, upd, lap, inv (10V)
     mg::GridJob* pc_jobs = nullptr;    // Laplacians of the two directions
@@ -373,6 +380,14 @@ int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
 void hfb_free(mg_ctx* c);
 int density_groups(const mg_ctx* c);
+int time_odd_setup(mg_ctx* c);
+int time_odd_densities(mg_ctx* c, const Basis& D);
+int time_odd_potentials(mg_ctx* c);
+int time_odd_energy(mg_ctx* c, double* t);
+int cranking_cutoff(mg_ctx* c);
+inline bool cranking(const mg_ctx* c) {
+    return c->p.omega[0] != 0.0 || c->p.omega[1] != 0.0 || c->p.omega[2] != 0.0;
+}
 int mixing_setup(mg_ctx* c);
 int save_density_history(mg_ctx* c);
 int mix_densities(mg_ctx* c);

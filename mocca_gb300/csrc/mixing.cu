@@ -152,6 +152,9 @@ int save_density_history(mg_ctx* c) {
                                 cudaMemcpyDeviceToDevice, c->stream));
         off += len[q];
     }
+    if (c->odd)
+        MG_CUDA(cudaMemcpyAsync(c->odd_hist, c->odd, 24 * V * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
     c->have_dhist = true;
     return MG_OK;
 }
@@ -167,6 +170,11 @@ int mix_densities(mg_ctx* c) {
                                                                     c->p.damping);
         MG_LAUNCHED(c);
         off += len[q];
+    }
+    if (c->odd) {   // the time-odd densities mix with the rest
+        k_mix<<<div_up(24 * V, kThreads), kThreads, 0, c->stream>>>(c->odd, c->odd_hist, 24 * V,
+                                                                    c->p.damping);
+        MG_LAUNCHED(c);
     }
     return MG_OK;
 }

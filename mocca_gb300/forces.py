@@ -83,6 +83,7 @@ class RunParams:
     precon_u: float = 1.0       # preconu
     parameter_estimation: int = 0   # ParameterEstimation: 1 estimates dt, momentum every step
     coulomb_prec: float = 0.0   # > 0: relative residual of the CG / multigrid Coulomb solves
+    omega: tuple = (0.0, 0.0, 0.0)  # cranking OmegaX, OmegaY, OmegaZ (needs trc = 0)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -96,5 +97,9 @@ class RunParams:
     def to_c(self) -> _abi.MgParams:
         p = _abi.MgParams()
         for name, _ in _abi.MgParams._fields_:
-            setattr(p, name, getattr(self, name))
+            if name == "omega":
+                for k in range(3):
+                    p.omega[k] = float(self.omega[k])
+            else:
+                setattr(p, name, getattr(self, name))
         return p

@@ -161,6 +161,16 @@ class MeshState:
                                           ("U", "B", "nablaB", "W", "divW", "coulomb", "coulex")))
         return out
 
+    def get_time_odd(self) -> dict:
+        """Time-odd densities and fields without time reversal (mg_get_time_odd):
+        vecj, vecs, rotj, rots, A, S as [it][m][V], divA as [it][V]."""
+        V = self.V
+        out = {k: np.empty(6 * V) for k in ("vecj", "vecs", "rotj", "rots", "A", "S")}
+        out["divA"] = np.empty(2 * V)
+        self._call("mg_get_time_odd", *(_dptr(out[k]) for k in
+                                         ("vecj", "vecs", "rotj", "rots", "A", "S", "divA")))
+        return out
+
     def set_potentials(self, U=None, B=None, nablaB=None, W=None, divW=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
                 for a in (U, B, nablaB, W, divW)]

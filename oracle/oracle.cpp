@@ -68,6 +68,11 @@ struct orc_ctx {
     std::vector<double> rho, tau, nablaj, derrho, laprho;
     std::vector<double> hrho, htau, hnablaj, hderrho, hlaprho;
     std::vector<double> Uold;   // UpotOld (src/PotentialMixing.f90:115)
+    // time-odd densities without time reversal (src/Densities.f90:39-94):
+    // vecj, vecs, their curls [it][m][V], and their history for the mixing
+    std::vector<double> vecj, vecs, rotj, rots, hvecj, hvecs, hrotj, hrots;
+    // time-odd fields (src/MeanFields.f90:79-85): A, S [it][m][V], div A [it][V]
+    std::vector<double> Apot, Spot, divA;
     // potentials (src/MeanFields.f90:79-85)
     std::vector<double> U, Bp, nablaB, W, divW;
     // Coulomb (src/Coulomb.f90:20-105)
@@ -335,7 +340,15 @@ extern "C" orc_ctx* orc_create(const mg_params* p, const mg_force* f) {
     c->U.assign(2 * V, 0); c->Bp.assign(2 * V, 0); c->nablaB.assign(6 * V, 0);
     c->W.assign(18 * V, 0); c->divW.assign(6 * V, 0);
     c->coulomb.assign(V, 0); c->coulex.assign(V, 0);
+    if (!p->trc)
+        for (auto* x : {&c->vecj, &c->vecs, &c->rotj, &c->rots, &c->Apot, &c->Spot})
+            x->assign(6 * V, 0.0);
+    if (!p->trc) c->divA.assign(2 * V, 0.0);
     return c;
+}
+
+static bool cranking(const orc_ctx* c) {
+    return c->p.omega[0] != 0.0 || c->p.omega[1] != 0.0 || c->p.omega[2] != 0.0;
 }
 
 extern "C" void orc_destroy(orc_ctx* c) { delete c; }
@@ -482,7 +495,27 @@ static void hpsi_one(const orc_ctx* c, const Basis& B, int i, double* out) {
         }
         // (-1) * MultiplyI(w): (w1,w2,w3,w4) -> (w2,-w1,w4,-w3)
         double wf[4] = {w[1], -w[0], w[3], -w[2]};
-        for (int l = 0; l < 4; ++l) out[l * V + v] = (b[l] + u[l]) + wf[l];
+        double h[4];
+        for (int l = 0; l < 4; ++l) h[l] = (b[l] + u[l]) + wf[l];
+        if (!c->p.trc) {
+            // ActionOfS: sum_m S_m sigma_m psi; ActionOfA: -i (sum_m A_m d_m psi
+            // + 1/2 div A psi) (src/MeanFields.f90:1107-1147)
+            double sa[4] = {0, 0, 0, 0}, aa[4] = {0, 0, 0, 0};
+            for (int m = 0; m < 3; ++m) {
+                double sg[4];
+                pauli(p, m + 1, sg);
+                const double sm = c->Spot[(it * 3 + m) * V + v], am = c->Apot[(it * 3 + m) * V + v];
+                for (int l = 0; l < 4; ++l) {
+                    sa[l] = sa[l] + sm * sg[l];
+                    aa[l] = aa[l] + am * d[m][l];
+                }
+            }
+            const double hd = 0.5 * c->divA[it * V + v];
+            for (int l = 0; l < 4; ++l) aa[l] = aa[l] + hd * p[l];
+            const double af[4] = {aa[1], -aa[0], aa[3], -aa[2]};
+            for (int l = 0; l < 4; ++l) h[l] = (h[l] + sa[l]) + af[l];
+        }
+        for (int l = 0; l < 4; ++l) out[l * V + v] = h[l];
     }
 }
 
@@ -726,12 +759,56 @@ static inline double imag_mult(const double* a, const double* b) {
     return a[0] * b[1] - a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
 }
 
+// Curls of vecj and vecs with the symmetry arguments of Table V of
+// Hellemans et al. (src/Densities.f90:1004-1106): d_y j_x, d_z j_x with
+// (-P, -S, TS, 2); d_x j_y, d_z j_y with (-P, -S, TS, 1); d_x j_z, d_y j_z
+// with (-P, S, TS, 2); d s_x with (P, -S, TS, 1), d s_y with (P, -S, TS, 2),
+// d s_z with (P, S, TS, 1).
+static void time_odd_curls(orc_ctx* c) {
+    const long V = c->V;
+    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+    std::vector<double> d[3][3];   // d[axis][component]
+    for (int it = 0; it < 2; ++it) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const std::vector<double>& f = pass == 0 ? c->vecj : c->vecs;
+            std::vector<double>& rot = pass == 0 ? c->rotj : c->rots;
+            for (int m = 0; m < 3; ++m)
+                for (int a = 0; a < 3; ++a) {
+                    d[a][m].assign(V, 0.0);
+                    if (a == m) continue;
+                    int pp, ss, comp;
+                    if (pass == 0) {
+                        pp = -P;
+                        ss = m == 2 ? S : -S;
+                        comp = m == 1 ? 1 : 2;
+                    } else {
+                        pp = P;
+                        ss = m == 2 ? S : -S;
+                        comp = m == 1 ? 2 : 1;
+                    }
+                    derive_grid(c, &f[(it * 3 + m) * V], a, pp, ss, TS, comp, d[a][m].data());
+                }
+            for (long v = 0; v < V; ++v) {
+                rot[(it * 3 + 0) * V + v] = d[1][2][v] - d[2][1][v];
+                rot[(it * 3 + 1) * V + v] = d[2][0][v] - d[0][2][v];
+                rot[(it * 3 + 2) * V + v] = d[0][1][v] - d[1][0][v];
+            }
+        }
+    }
+}
+
 extern "C" int orc_update_densities(orc_ctx* c) {
     if (!c) return MG_ERR_ARG;
     const long V = c->V;
     // UpdateDensities(0): DensityHistory(1) = Density before recomputing
     c->hrho = c->rho; c->htau = c->tau; c->hnablaj = c->nablaj;
     c->hderrho = c->derrho; c->hlaprho = c->laprho;
+    c->hvecj = c->vecj; c->hvecs = c->vecs; c->hrotj = c->rotj; c->hrots = c->rots;
+    const bool odd = !c->p.trc;
+    if (odd) {
+        std::fill(c->vecj.begin(), c->vecj.end(), 0.0);
+        std::fill(c->vecs.begin(), c->vecs.end(), 0.0);
+    }
     const Basis& B = c->bas[c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS];
     std::fill(c->rho.begin(), c->rho.end(), 0.0);
     std::fill(c->tau.begin(), c->tau.end(), 0.0);
@@ -764,6 +841,17 @@ extern "C" int orc_update_densities(orc_ctx* c) {
                 nj = nj + double(trip[q][3]) * imag_mult(d[trip[q][0] - 1], s);
             }
             c->nablaj[it * V + v] = c->nablaj[it * V + v] + occ * nj;
+            if (odd) {
+                // GetVecj: Im(psi^+ d_m psi); GetVecs: Re(psi^+ sigma_m psi)
+                // (src/Spwf.f90:2034-2085)
+                for (int m = 0; m < 3; ++m) {
+                    double s[4];
+                    pauli(p, m + 1, s);
+                    const double sm = p[0] * s[0] + p[1] * s[1] + p[2] * s[2] + p[3] * s[3];
+                    c->vecj[(it * 3 + m) * V + v] = c->vecj[(it * 3 + m) * V + v] + occ * imag_mult(p, d[m]);
+                    c->vecs[(it * 3 + m) * V + v] = c->vecs[(it * 3 + m) * V + v] + occ * sm;
+                }
+            }
         }
     }
     const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
@@ -772,10 +860,12 @@ extern "C" int orc_update_densities(orc_ctx* c) {
             derive_grid(c, &c->rho[it * V], d, P, S, TS, 1, &c->derrho[(it * 3 + d) * V]);
         derive_grid(c, &c->rho[it * V], 3, P, S, TS, 1, &c->laprho[it * V]);
     }
+    if (odd) time_odd_curls(c);
     return MG_OK;
 }
 
-// MixDensities, src/DensityMixing.f90:22-86: scheme 0 mixes every density,
+// MixDensities, src/DensityMixing.f90:22-86: scheme 0 mixes every density
+// (the time-odd ones too: the DensityVector operators combine all fields),
 // Density = (1 - DampingParam) Density + DampingParam DensityHistory(1);
 // scheme 2 leaves the densities (the U update is preconditioned instead).
 extern "C" int orc_mix_densities(orc_ctx* c) {
@@ -789,6 +879,19 @@ extern "C" int orc_mix_densities(orc_ctx* c) {
     };
     mix(c->rho, c->hrho); mix(c->tau, c->htau); mix(c->nablaj, c->hnablaj);
     mix(c->derrho, c->hderrho); mix(c->laprho, c->hlaprho);
+    mix(c->vecj, c->hvecj); mix(c->vecs, c->hvecs); mix(c->rotj, c->hrotj); mix(c->rots, c->hrots);
+    return MG_OK;
+}
+
+// Time-odd densities and fields ([it][m][V] vectors, div A [it][V]); any may be NULL.
+extern "C" int orc_get_time_odd(orc_ctx* c, double* vecj, double* vecs, double* rotj,
+                                double* rots, double* apot, double* spot, double* diva) {
+    if (!c || c->p.trc) return MG_ERR_ARG;
+    auto cp = [](double* dst, const std::vector<double>& s) {
+        if (dst) std::memcpy(dst, s.data(), s.size() * sizeof(double));
+    };
+    cp(vecj, c->vecj); cp(vecs, c->vecs); cp(rotj, c->rotj); cp(rots, c->rots);
+    cp(apot, c->Apot); cp(spot, c->Spot); cp(diva, c->divA);
     return MG_OK;
 }
 
@@ -992,7 +1095,9 @@ static bool any_alternating(const orc_ctx* c) {   // CheckForAlternateConstraint
 extern "C" int orc_calculate_moments(orc_ctx* c) {
     if (!c) return MG_ERR_ARG;
     if (c->moments.empty()) init_moments(c);
-    if (!c->cons.empty()) rutz_cutoff(c);
+    // CompCutoff runs in every CalculateAllMoments (src/Moments.f90:2267);
+    // the constraints and the cranking fields use it
+    if (!c->cons.empty() || cranking(c)) rutz_cutoff(c);
     for (Moment& mo : c->moments)
         for (int it = 0; it < 2; ++it) {
             double s = 0.0;
@@ -1244,6 +1349,74 @@ extern "C" int orc_solve_coulomb(orc_ctx* c, int* iters) {
 // Potentials: CalcUPot src/MeanFields.f90:269-409, CalcWPot :494-597,
 // CalcBPot :115-150; ConstructPotentials src/PotentialMixing.f90:17-201.
 // --------------------------------------------------------------------------
+// CalcAPot (src/MeanFields.f90:411-492) and CalcSPot (:618-712) for the
+// functional without tensor, N2LO and J2 terms, with the cranking fields
+// CrankAPot = -f_cut omega x r and CrankSPot = -f_cut omega / 2
+// (src/Cranking.f90:234-334); div A with the symmetry arguments of :476-481.
+static void time_odd_potentials(orc_ctx* c) {
+    const long V = c->V;
+    const mg_skyrme_b& B = c->B;
+    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+    const double* om = c->p.omega;
+    const bool crank = cranking(c);
+    auto lc = [](int i, int j, int k) {
+        if (i == j || j == k || k == i) return 0;
+        if ((i == 0 && j == 1 && k == 2) || (i == 2 && j == 0 && k == 1) || (i == 1 && j == 2 && k == 0))
+            return 1;
+        return -1;
+    };
+    for (int it = 0; it < 2; ++it) {
+        const int at = 1 - it;
+        for (int m = 0; m < 3; ++m)
+            for (long v = 0; v < V; ++v) {
+                const long q = (it * 3 + m) * V + v, qa = (at * 3 + m) * V + v;
+                double a = -2.0 * ((B.B3 + B.B4) * c->vecj[q] + B.B3 * c->vecj[qa]);
+                a = a + ((B.B9 + B.B9q) * c->rots[q] + B.B9 * c->rots[qa]);
+                c->Apot[q] = a;
+                const double rt = c->rho[v] + c->rho[V + v];
+                const double ra = std::pow(rt, B.byt3a);
+                double sv = (B.B9 + B.B9q) * c->rotj[q] + B.B9 * c->rotj[qa] +
+                            2.0 * ((B.B10 + B.B11) * c->vecs[q] + B.B10 * c->vecs[qa]) +
+                            2.0 * ((B.B12a + B.B13a) * (ra * c->vecs[q]) + B.B12a * (ra * c->vecs[qa]));
+                if (B.B12b != 0.0 || B.B13b != 0.0) {
+                    const double rb = std::pow(rt, B.byt3b);
+                    sv = sv + 2.0 * ((B.B12b + B.B13b) * (rb * c->vecs[q]) + B.B12b * (rb * c->vecs[qa]));
+                }
+                c->Spot[q] = sv;
+            }
+    }
+    if (crank) {
+        for (int it = 0; it < 2; ++it)
+            for (int k = 0; k < 3; ++k)
+                for (int j = 0; j < 3; ++j)
+                    for (int i = 0; i < 3; ++i) {
+                        const int e = lc(i, j, k);
+                        for (int z = 0; z < c->nz; ++z)
+                            for (int y = 0; y < c->ny; ++y)
+                                for (int x = 0; x < c->nx; ++x) {
+                                    const long v = x + (long)c->nx * (y + (long)c->ny * z);
+                                    const double r[3] = {c->dx / 2.0 + c->dx * x, c->dx / 2.0 + c->dx * y,
+                                                         c->dx / 2.0 + c->dx * z};
+                                    double& a = c->Apot[(it * 3 + i) * V + v];
+                                    a = a - e * om[j] * r[k] * c->cutoff[it * V + v];
+                                }
+                    }
+        for (int it = 0; it < 2; ++it)
+            for (int i = 0; i < 3; ++i)
+                for (long v = 0; v < V; ++v) {
+                    double& sv = c->Spot[(it * 3 + i) * V + v];
+                    sv = sv - 1 / 2.0 * om[i] * c->cutoff[it * V + v];
+                }
+    }
+    std::vector<double> t1(V), t2(V), t3(V);
+    for (int it = 0; it < 2; ++it) {
+        derive_grid(c, &c->Apot[(it * 3 + 0) * V], 0, -P, -S, TS, 2, t1.data());
+        derive_grid(c, &c->Apot[(it * 3 + 1) * V], 1, -P, -S, TS, 1, t2.data());
+        derive_grid(c, &c->Apot[(it * 3 + 2) * V], 2, -P, S, TS, 2, t3.data());
+        for (long v = 0; v < V; ++v) c->divA[it * V + v] = t1[v] + t2[v] + t3[v];
+    }
+}
+
 static void calc_potentials(orc_ctx* c) {
     const long V = c->V;
     const mg_skyrme_b& B = c->B;
@@ -1325,6 +1498,7 @@ static void calc_potentials(orc_ctx* c) {
         for (int d = 0; d < 3; ++d)
             derive_grid(c, &c->Bp[it * V], d, P, S, TS, 1, &c->nablaB[(it * 3 + d) * V]);
     }
+    if (!c->p.trc) time_odd_potentials(c);
 }
 
 // PreconditionPotential + preconoperator, src/Damping.f90:158-228: per
@@ -1463,6 +1637,44 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
         s10 += B.B8a * a10;
         s12 += B.B9q * a12;
         s34 += B.B8b * a34;
+    }
+    if (!c->p.trc) {
+        // time-odd terms 5, 6, 13-18, 35, 36 of compSkyrme (src/Energy.f90:623-860)
+        double j2 = 0, jrs = 0, s2t = 0, s2a = 0, s2b = 0;
+        double q6 = 0, q14 = 0, q16 = 0, q18 = 0, q36 = 0;
+        for (int m = 0; m < 3; ++m)
+            for (long v = 0; v < V; ++v) {
+                const double jt = c->vecj[m * V + v] + c->vecj[(3 + m) * V + v];
+                const double st = c->vecs[m * V + v] + c->vecs[(3 + m) * V + v];
+                const double rs = c->rots[m * V + v] + c->rots[(3 + m) * V + v];
+                const double rt = c->rho[v] + c->rho[V + v];
+                j2 += jt * jt;
+                jrs += jt * rs;
+                s2t += st * st;
+                s2a += std::pow(rt, B.byt3a) * (st * st);
+                if (B.B12b != 0.0) s2b += std::pow(rt, B.byt3b) * (st * st);
+            }
+        for (int it = 0; it < 2; ++it) {
+            double a6 = 0, a14 = 0, a16 = 0, a18 = 0, a36 = 0;
+            for (int m = 0; m < 3; ++m)
+                for (long v = 0; v < V; ++v) {
+                    const long q = (it * 3 + m) * V + v;
+                    const double rt = c->rho[v] + c->rho[V + v];
+                    a6 += c->vecj[q] * c->vecj[q];
+                    a14 += c->vecj[q] * c->rots[q];
+                    a16 += c->vecs[q] * c->vecs[q];
+                    a18 += std::pow(rt, B.byt3a) * (c->vecs[q] * c->vecs[q]);
+                    if (B.B13b != 0.0) a36 += std::pow(rt, B.byt3b) * (c->vecs[q] * c->vecs[q]);
+                }
+            q6 = q6 - B.B4 * a6;
+            q14 = q14 + B.B9q * a14;
+            q16 = q16 + B.B11 * a16;
+            q18 = q18 + B.B13a * a18;
+            q36 = q36 + B.B13b * a36;
+        }
+        t[4] = -B.B3 * j2; t[5] = q6; t[12] = B.B9 * jrs; t[13] = q14;
+        t[14] = B.B10 * s2t; t[15] = q16; t[16] = B.B12a * s2a; t[17] = q18;
+        t[34] = B.B12b * s2b; t[35] = q36;
     }
     t[0] = B.B1 * s1; t[1] = B.B2 * s2; t[2] = B.B3 * s3; t[3] = s4;
     t[6] = B.B5 * s7; t[7] = s8; t[8] = B.B7a * s9; t[9] = s10;

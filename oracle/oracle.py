@@ -70,6 +70,7 @@ _SIG = {
     "orc_get_pairing_field": ([_P, _D, _D, _D], C.c_int),
     "orc_eigh": ([C.c_int, _D, _D, _D], C.c_int),
     "orc_set_threads": ([C.c_int], C.c_int),
+    "orc_get_time_odd": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
 }
 
 _libs = {}
@@ -202,6 +203,14 @@ class OracleState:
                 ("coulex", 1))}
         self._call("orc_get_potentials", *(_d(out[k]) for k in
                                            ("U", "B", "nablaB", "W", "divW", "coulomb", "coulex")))
+        return out
+
+    def get_time_odd(self):
+        V = self.V
+        out = {k: np.empty(6 * V) for k in ("vecj", "vecs", "rotj", "rots", "A", "S")}
+        out["divA"] = np.empty(2 * V)
+        self._call("orc_get_time_odd", *(_d(out[k]) for k in
+                                          ("vecj", "vecs", "rotj", "rots", "A", "S", "divA")))
         return out
 
     def set_potentials(self, U=None, B=None, nablaB=None, W=None, divW=None):

@@ -120,3 +120,21 @@ def test_new_entry_points_reject_bad_arguments(built):
     assert lib.mg_batch_iterate(None, 1, d, d, None) == _abi.MG_ERR_ARG
     assert lib.mg_batch_status(None, None) == _abi.MG_ERR_ARG
     assert lib.mg_batch_set_workers(None, 2) == _abi.MG_ERR_ARG
+
+
+def test_time_odd_and_solver_parameters_are_checked(built):
+    """mg_create refuses, before any device work: cranking with time
+    reversal, OmegaX with signature or OmegaY with time simplex, the
+    time-odd path off the EV8 box, in mixed precision or with HFB, an
+    unknown Coulomb solver or a negative Coulomb tolerance."""
+    lib = _abi.load()
+    ctx = C.c_void_p()
+    bad = [dict(trc=1, omega=(0.0, 0.0, 0.5)), dict(trc=0, omega=(0.5, 0.0, 0.0)),
+           dict(trc=0, omega=(0.0, 0.5, 0.0)), dict(trc=0, precision=_abi.MG_MIXED),
+           dict(trc=0, pairing=_abi.MG_PAIRING_HFB), dict(trc=0, pc=0, sc=0, tsc=0),
+           dict(coulomb_solver=3), dict(coulomb_prec=-1.0)]
+    for kw in bad:
+        p = RunParams(nx=10, ny=10, nz=10, nwt=8, **kw).to_c()
+        assert lib.mg_create(C.byref(p), SLY4.to_c(), None, C.byref(ctx)) == _abi.MG_ERR_ARG, kw
+    assert lib.mg_get_time_odd(None, None, None, None, None, None, None, None) == _abi.MG_ERR_ARG
+    assert lib.mg_coulomb_reset(None) == _abi.MG_ERR_ARG
