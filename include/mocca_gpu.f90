@@ -403,6 +403,12 @@ module mocca_gpu
       type(c_ptr), value :: s
       type(c_ptr), value :: diva
     end function
+    integer(c_int) function mg_symmetry_operators(ctx, basis, out) bind(C, name="mg_symmetry_operators")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: basis
+      type(c_ptr), value :: out
+    end function
     integer(c_int) function mg_set_potentials(ctx, u, b, nablab, w, divw) bind(C, name="mg_set_potentials")
       import
       type(c_ptr), value :: ctx

@@ -387,6 +387,13 @@ int mg_get_potentials(mg_ctx* ctx, double* u, double* b, double* nablab,
  * any may be NULL.  MG_ERR_ARG with time reversal. */
 int mg_get_time_odd(mg_ctx* ctx, double* vecj, double* vecs, double* rotj, double* rots,
                     double* a, double* s, double* diva);
+
+/* SymmetryOperators + CalcRMSRadius (src/Spwf.f90:2289-2347) for every spwf
+ * of a basis: out[6*i + 0..5] = isospin, signature, parity, time simplex,
+ * x-simplex expectation values and the RMS radius sqrt(<r^2>).  A conserved
+ * symmetry gives the spwf's quantum number; on the symmetry-free box the
+ * expectation values of the mirror actions (src/Spinor.f90:391-490). */
+int mg_symmetry_operators(mg_ctx* ctx, int basis, double* out);
 int mg_set_potentials(mg_ctx* ctx, const double* u, const double* b,
                       const double* nablab, const double* w, const double* divw);
 

@@ -195,6 +195,7 @@ SIGNATURES = {
     "mg_coulomb_residual": [_P, _D],
     "mg_coulomb_reset": [_P],
     "mg_get_time_odd": [_P, _D, _D, _D, _D, _D, _D, _D],
+    "mg_symmetry_operators": [_P, C.c_int, _D],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_set_potentials": [_P, _D, _D, _D, _D, _D],

@@ -161,6 +161,13 @@ class MeshState:
                                           ("U", "B", "nablaB", "W", "divW", "coulomb", "coulex")))
         return out
 
+    def SymmetryOperators(self, basis: int = _abi.MG_HF_BASIS) -> np.ndarray:
+        """Per spwf: isospin, signature, parity, time simplex, x-simplex
+        expectation values and the RMS radius (mg_symmetry_operators)."""
+        out = np.empty((self.p.nwt, 6))
+        self._call("mg_symmetry_operators", int(basis), _dptr(out))
+        return out
+
     def get_time_odd(self) -> dict:
         """Time-odd densities and fields without time reversal (mg_get_time_odd):
         vecj, vecs, rotj, rots, A, S as [it][m][V], divA as [it][V]."""

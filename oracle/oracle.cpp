@@ -883,6 +883,65 @@ extern "C" int orc_mix_densities(orc_ctx* c) {
     return MG_OK;
 }
 
+// SymmetryOperators + CalcRMSRadius, src/Spwf.f90:2289-2347, with the
+// mirror actions of src/Spinor.f90:391-490 on the symmetry-free box and the
+// mesh of IniMesh (src/Mesh.f90:40-85).  out[6 i ..]: isospin, signature,
+// parity, time simplex, x-simplex, RMS radius.
+extern "C" int orc_symmetry_operators(orc_ctx* c, int b, double* out) {
+    if (!c || !out || b < 0 || b > 1) return MG_ERR_ARG;
+    const Basis& B = c->bas[b];
+    const long V = c->V;
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const double dx = c->dx;
+    const double ox = c->p.sc ? 0.0 : nx / 2.0 * dx, oy = c->p.tsc ? 0.0 : ny / 2.0 * dx,
+                 oz = c->p.pc ? 0.0 : nz / 2.0 * dx;
+    auto at = [&](const double* p, int l, int x, int y, int z) {
+        return p[l * V + x + (long)nx * (y + (long)ny * z)];
+    };
+    for (int i = 0; i < c->p.nwt; ++i) {
+        const double* p = &B.psi[(long)i * 4 * V];
+        const int* qn = &B.qn[4 * i];
+        double r2 = 0, par = 0, sig = 0, ts = 0, xs = 0;
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; ++x) {
+                    double a[4];
+                    for (int l = 0; l < 4; ++l) a[l] = at(p, l, x, y, z);
+                    const double X = dx / 2.0 + dx * x - ox, Y = dx / 2.0 + dx * y - oy,
+                                 Z = dx / 2.0 + dx * z - oz;
+                    r2 += (X * X + Y * Y + Z * Z) * (a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
+                    if (c->folded) continue;
+                    const int mx = nx - 1 - x, my = ny - 1 - y, mz = nz - 1 - z;
+                    for (int l = 0; l < 4; ++l) par += a[l] * at(p, l, mx, my, mz);
+                    {   // ActionOfSignature: MultiplyI(Pauli_z(psi(-x,-y,z)))
+                        const double c1 = at(p, 0, mx, my, z), c2 = at(p, 1, mx, my, z),
+                                     c3 = at(p, 2, mx, my, z), c4 = at(p, 3, mx, my, z);
+                        const double t[4] = {-c2, c1, c4, -c3};
+                        sig += t[1] * a[0] - t[0] * a[1] + t[3] * a[2] - t[2] * a[3];
+                    }
+                    {   // ActionOfTimeSimplex: Conj(psi(x,-y,z))
+                        const double t[4] = {at(p, 0, x, my, z), -at(p, 1, x, my, z),
+                                             at(p, 2, x, my, z), -at(p, 3, x, my, z)};
+                        for (int l = 0; l < 4; ++l) ts += a[l] * t[l];
+                    }
+                    {   // ActionOfXSimplex: -MultiplyI(spin-swapped psi(-x,y,z))
+                        const double c1 = at(p, 0, mx, y, z), c2 = at(p, 1, mx, y, z),
+                                     c3 = at(p, 2, mx, y, z), c4 = at(p, 3, mx, y, z);
+                        const double t[4] = {c4, -c3, c2, -c1};
+                        xs += t[1] * a[0] - t[0] * a[1] + t[3] * a[2] - t[2] * a[3];
+                    }
+                }
+        double* o = out + 6 * i;
+        o[0] = qn[0];
+        o[1] = qn[2] != 0 ? qn[2] : sig * c->dv;
+        o[2] = qn[1] != 0 ? qn[1] : par * c->dv;
+        o[3] = qn[3] != 0 ? qn[3] : ts * c->dv;
+        o[4] = qn[2] != 0 ? 0.0 : xs * c->dv;
+        o[5] = std::sqrt(r2 * c->dv);
+    }
+    return MG_OK;
+}
+
 // Time-odd densities and fields ([it][m][V] vectors, div A [it][V]); any may be NULL.
 extern "C" int orc_get_time_odd(orc_ctx* c, double* vecj, double* vecs, double* rotj,
                                 double* rots, double* apot, double* spot, double* diva) {

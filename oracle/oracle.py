@@ -71,6 +71,7 @@ _SIG = {
     "orc_eigh": ([C.c_int, _D, _D, _D], C.c_int),
     "orc_set_threads": ([C.c_int], C.c_int),
     "orc_get_time_odd": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
+    "orc_symmetry_operators": ([_P, C.c_int, _D], C.c_int),
 }
 
 _libs = {}
@@ -203,6 +204,11 @@ class OracleState:
                 ("coulex", 1))}
         self._call("orc_get_potentials", *(_d(out[k]) for k in
                                            ("U", "B", "nablaB", "W", "divW", "coulomb", "coulex")))
+        return out
+
+    def SymmetryOperators(self, basis=_abi.MG_HF_BASIS):
+        out = np.empty((self.p.nwt, 6))
+        self._call("orc_symmetry_operators", basis, _d(out))
         return out
 
     def get_time_odd(self):

@@ -59,3 +59,39 @@ def test_cranking_makes_time_odd_fields(built_oracle):
     for k in ("vecj", "vecs", "rotj", "rots", "A", "S", "divA"):
         assert np.abs(odd[k]).max() > 1e-5, k
     assert abs(e1[-1] - e0[-1]) > 1e-3
+
+
+def _full_box_state(builders):
+    """Normalised spinors on a 12^3 symmetry-free box from (component,
+    function of x, y, z) pairs."""
+    p = RunParams(nx=12, ny=12, nz=12, dx=0.8, pc=0, sc=0, tsc=0, nwt=len(builders),
+                  neutrons=2, protons=0)
+    c = (np.arange(12) + 0.5) * 0.8 - 12 / 2 * 0.8
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    psi = np.zeros((p.nwt, 4, 12, 12, 12))
+    for i, (comp, f) in enumerate(builders):
+        psi[i, comp] = f(X, Y, Z)
+    psi /= np.sqrt((psi ** 2).sum(axis=(1, 2, 3, 4)) * p.dv)[:, None, None, None, None]
+    qn = np.tile(np.array([-1, 0, 0, 0], dtype=np.int32), (p.nwt, 1))
+    return p, psi.reshape(p.nwt, -1), qn
+
+
+def test_symmetry_operators_known_answers(built_oracle):
+    """SymmetryOperators on the symmetry-free box for states of known
+    symmetry: a spin-up s wave (parity, signature and time simplex +1,
+    x-simplex 0), a spin-up p_x wave (parity -1, signature -1, time simplex
+    +1), a spin-up p_y wave (time simplex -1), and the RMS radius of a
+    Gaussian, sqrt(3/2) times its width parameter."""
+    g = lambda X, Y, Z: np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 4.0)  # noqa: E731
+    p, psi, qn = _full_box_state([(0, g), (0, lambda X, Y, Z: X * g(X, Y, Z)),
+                                  (0, lambda X, Y, Z: Y * g(X, Y, Z))])
+    o = O.OracleState(p, SLY4)
+    o.set_spinors(psi, qn)
+    s = o.SymmetryOperators()
+    o.close()
+    assert np.allclose(s[0, 1:5], [1.0, 1.0, 1.0, 0.0], atol=1e-12), s[0]
+    assert np.allclose(s[1, 1:4], [-1.0, -1.0, 1.0], atol=1e-12), s[1]
+    assert abs(s[2, 3] + 1.0) <= 1e-12, s[2]
+    # <r^2> of exp(-r^2/4)^2 = exp(-r^2/2): 3 (variance 1); the mesh sum is
+    # the exact integral to ~1e-6 at dx = 0.8 for this width
+    assert abs(s[0, 5] - np.sqrt(3.0)) <= 1e-4, s[0, 5]
