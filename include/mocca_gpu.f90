@@ -489,6 +489,18 @@ module mocca_gpu
       type(c_ptr), value :: ctx
       type(c_ptr), value :: count
     end function
+    integer(c_int) function mg_set_phase_timing(ctx, on) bind(C, name="mg_set_phase_timing")
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function mg_get_phase_times(ctx, ms, n, passes) bind(C, name="mg_get_phase_times")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: ms
+      integer(c_int), value :: n
+      type(c_ptr), value :: passes
+    end function
   end interface
 contains
   subroutine gpu_check(st, where)

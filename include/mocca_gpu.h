@@ -484,6 +484,33 @@ int mg_evolve(mg_ctx* ctx, int max_iter, double dt, double momentum, const mg_co
  * src/Coulomb.f90:288, :333-334). */
 int mg_launch_count(mg_ctx* ctx, long long* count);
 
+/* Phases of one mg_iterate pass, for the timer below (the reference's
+ * counterpart is its per-routine timing printout, e.g. CoulombTime,
+ * src/Coulomb.f90:288, :333-334).  Each phase is timed on the context's
+ * stream from the end of the phase before it; MG_PH_SIDE_DERIVE is the
+ * HF-basis DeriveAll on the side stream, overlapping the pairing phases. */
+#define MG_PH_GRAD_DESC     0   /* AlternateStep, GradDesc with Gram-Schmidt    */
+#define MG_PH_PAIRING_MESH  1   /* pairing field, gaps, cutoffs                 */
+#define MG_PH_FERMI         2   /* Fermi search (HFB evaluations)               */
+#define MG_PH_CANONICAL     3   /* canonical basis, occupations, HFB mixing     */
+#define MG_PH_DERIVE        4   /* DeriveAll (canonical basis after the join)   */
+#define MG_PH_HPSI_CAN      5   /* canonical single-particle energies           */
+#define MG_PH_DENSITIES     6   /* densities and MixDensities                   */
+#define MG_PH_MOMENTS       7   /* moments, readjustment                        */
+#define MG_PH_POTENTIALS    8   /* ConstructPotentials with the Coulomb solve   */
+#define MG_PH_ENERGY        9   /* CompEnergy                                   */
+#define MG_PH_SIDE_DERIVE  10   /* HF-basis DeriveAll on the side stream        */
+#define MG_PH_COUNT        11
+/* Switch the phase timer on (on != 0; clears the totals) or off.  While on,
+ * every mg_iterate pass records CUDA events between its phases and waits
+ * for the pass's last event to read them: a diagnostic mode, not for timed
+ * production runs. */
+int mg_set_phase_timing(mg_ctx* ctx, int on);
+/* Totals since the timer was switched on: ms[k] (n >= MG_PH_COUNT doubles)
+ * is the device time of phase k summed over the timed passes, whose count
+ * goes to *passes (may be NULL). */
+int mg_get_phase_times(mg_ctx* ctx, double* ms, int n, long long* passes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -202,6 +202,8 @@ SIGNATURES = {
     "mg_energy": [_P, C.POINTER(MgEnergyTerms)],
     "mg_iterate": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgEnergyTerms)],
     "mg_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "mg_set_phase_timing": [_P, C.c_int],
+    "mg_get_phase_times": [_P, _D, C.c_int, C.POINTER(C.c_longlong)],
     "mg_convergence_check": [_P, C.POINTER(MgConvergence), _I],
     "mg_evolve": [_P, C.c_int, C.c_double, C.c_double, C.POINTER(MgConvergence), _I, _I,
                   C.POINTER(MgEnergyTerms)],

@@ -43,6 +43,10 @@ constexpr int kJSmemMax = 128;
 // two float planes (FP32 seed) or one double plane (FP64 polish) of
 // kEigMax x (kEigMax + 1) -- 206 KB, which leaves room for their static arrays
 constexpr int kSmemOptIn = kEigMax * (kEigMax + 1) * 8;
+// FP32 Jacobi seed: couplings at or below kJacobiSkip |A|_F do not rotate
+// (at 1e-8, a cold seed of clusters split by 1e-10 left the FP64 polish
+// churning past its sweep cap; 1e-9 keeps most of the skipped rounds)
+constexpr float kJacobiSkip = 1e-9f;
 
 __device__ float cta_sumf(float x, float* red) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -81,19 +85,68 @@ __device__ __forceinline__ int rr_round(int p, int q, int n) {
 
 }  // namespace
 
+// C = op(A) B for n x n FP32 matrices in shared memory (leading dimension
+// ld), op(A) = A or A^T.  Each thread holds a 4 x 4 register tile: rows
+// 4 it .. 4 it + 3 and columns jt + m nq (m = 0..3), so that a warp's loads
+// of B's row k are consecutive words and its loads of A are broadcasts.  The
+// sums run over k in order with fused multiply-adds.
+__device__ void smem_mm32(const float* A, const float* B, float* C, int n, int ld, bool transA) {
+    const int nq = (n + 3) / 4;
+    for (int t = threadIdx.x; t < nq * nq; t += blockDim.x) {
+        const int it = t / nq, jt = t % nq;
+        float acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) acc[r][m] = 0.0f;
+        for (int k = 0; k < n; ++k) {
+            float x[4], y[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int i = 4 * it + r;
+                x[r] = i < n ? (transA ? A[k * ld + i] : A[i * ld + k]) : 0.0f;
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int j = jt + m * nq;
+                y[m] = j < n ? B[k * ld + j] : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int m = 0; m < 4; ++m) acc[r][m] = fmaf(x[r], y[m], acc[r][m]);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int i = 4 * it + r, j = jt + m * nq;
+                if (i < n && j < n) C[i * ld + j] = acc[r][m];
+            }
+    }
+}
+
 // One matrix per CTA.  A: FP64 n x n (lda) input; Xw: optional FP64 warm
 // start (n x n, ldx); X: FP64 output vectors (n x n, ldx, column k <-> w[k]);
 // w: eigenvalues ascending.  n <= kEigMax.  Above kJSmemMax the warm start's
 // product A V goes through X (FP64) instead of a third shared-memory plane;
 // Xw may alias X, whose contents are in v by then.
+//
+// A round-robin round's n/2 rotations J act on disjoint index pairs, so
+// A <- J^T A J splits into (n/2)^2 independent 2 x 2 blocks (rows of pair i,
+// columns of pair j): each thread rotates its blocks' rows, then their
+// columns, in registers, one pass over the matrix per round; V <- V J is the
+// same pass over V's rows.  A pair rotates when its coupling is above
+// kJacobiSkip |A| (FP32 rounding of the matrix entries is ~6e-8 |A|); a
+// round without such a pair is skipped, which makes the later sweeps of a
+// warm start cheap.
 __global__ void __launch_bounds__(kJThreads)
 k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __restrict__ nsz,
            const double* Xw, double* X, long xstride, int ldx,
            double* __restrict__ w, long wstride, int max_sweeps, int* __restrict__ flag) {
     extern __shared__ float smf[];
     __shared__ float red[32];
-    __shared__ float cs[2][kEigMax / 2];
-    __shared__ int pq[2][kEigMax / 2];
+    __shared__ float4 prm[kEigMax / 2];   // c, s, p, q (index bits) of the round's pairs
     __shared__ int perm[kEigMax];
     const int b = blockIdx.x;
     const int n0 = nsz[b];
@@ -115,19 +168,9 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
     __syncthreads();
     if (Xw && t) {
         // a <- V^T A V
-        for (int q = tid; q < n * n; q += kJThreads) {
-            const int i = q / n, j = q % n;
-            float s = 0.0f;
-            for (int k = 0; k < n; ++k) s = fmaf(a[i * ld + k], v[k * ld + j], s);
-            t[i * ld + j] = s;
-        }
+        smem_mm32(a, v, t, n, ld, false);
         __syncthreads();
-        for (int q = tid; q < n * n; q += kJThreads) {
-            const int i = q / n, j = q % n;
-            float s = 0.0f;
-            for (int k = 0; k < n; ++k) s = fmaf(v[k * ld + i], t[k * ld + j], s);
-            a[i * ld + j] = s;
-        }
+        smem_mm32(v, t, a, n, ld, true);
         __syncthreads();
     } else if (Xw) {
         // the same through X: the padding row and column of A V and of
@@ -160,60 +203,62 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         }
         __syncthreads();
     }
-    // thread (lane, kg): columns / rows lane, lane + 128, ..., every
-    // kJGroups-th rotation pair from kg
-    const int lane = tid & 127, kg = tid >> 7;
     const int half = n / 2;
     float part = 0.0f;
-    for (int col = lane; col < n; col += 128)
-        for (int i = kg; i < n; i += kJGroups) part += a[i * ld + col] * a[i * ld + col];
+    for (int q = tid; q < n * n; q += kJThreads) {
+        const float x = a[(q / n) * ld + q % n];
+        part += x * x;
+    }
     const float norm2 = cta_sumf(part, red);
     const float tol2 = 1e-11f * norm2;  // off-diagonal <= 3e-6 |A|: an FP32-level seed
+    const float thr = kJacobiSkip * sqrtf(norm2);
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         part = 0.0f;
-        for (int col = lane; col < n; col += 128)
-            for (int i = kg; i < n; i += kJGroups)
-                if (i != col) part += a[i * ld + col] * a[i * ld + col];
+        for (int q = tid; q < n * n; q += kJThreads) {
+            const int i = q / n, j = q % n;
+            if (i != j) part += a[i * ld + j] * a[i * ld + j];
+        }
         const float off = cta_sumf(part, red);
         if (off <= tol2) break;
         for (int r = 0; r < n - 1; ++r) {
+            int on = 0;
             if (tid < half) {
                 const int p = rr_player(tid, r, n), q = rr_player(n - 1 - tid, r, n);
                 const float apq = a[p * ld + q];
                 float c = 1.0f, s = 0.0f;
-                if (fabsf(apq) > 1e-30f) {
+                if (fabsf(apq) > thr) {
                     const float th = (a[q * ld + q] - a[p * ld + p]) / (2.0f * apq);
                     const float tt = (th >= 0.0f ? 1.0f : -1.0f) / (fabsf(th) + sqrtf(th * th + 1.0f));
                     c = rsqrtf(tt * tt + 1.0f);
                     s = tt * c;
+                    on = 1;
                 }
-                cs[0][tid] = c;
-                cs[1][tid] = s;
-                pq[0][tid] = p;
-                pq[1][tid] = q;
+                prm[tid] = make_float4(c, s, __int_as_float(p), __int_as_float(q));
             }
-            __syncthreads();
-            for (int col = lane; col < n; col += 128)
-                for (int k = kg; k < half; k += kJGroups) {
-                    const int p = pq[0][k], q = pq[1][k];
-                    const float c = cs[0][k], s = cs[1][k];
-                    const float ap = a[p * ld + col], aq = a[q * ld + col];
-                    a[p * ld + col] = c * ap - s * aq;
-                    a[q * ld + col] = s * ap + c * aq;
-                }
-            __syncthreads();
-            for (int row = lane; row < n; row += 128)
-                for (int k = kg; k < half; k += kJGroups) {
-                    const int p = pq[0][k], q = pq[1][k];
-                    const float c = cs[0][k], s = cs[1][k];
-                    const float ap = a[row * ld + p], aq = a[row * ld + q];
-                    a[row * ld + p] = c * ap - s * aq;
-                    a[row * ld + q] = s * ap + c * aq;
-                    const float vp = v[row * ld + p], vq = v[row * ld + q];
-                    v[row * ld + p] = c * vp - s * vq;
-                    v[row * ld + q] = s * vp + c * vq;
-                }
+            if (!__syncthreads_or(on)) continue;
+            for (int u = tid; u < half * half; u += kJThreads) {
+                const float4 R = prm[u / half], Cc = prm[u % half];
+                float* ap = a + __float_as_int(R.z) * ld;
+                float* aq = a + __float_as_int(R.w) * ld;
+                const int jp = __float_as_int(Cc.z), jq = __float_as_int(Cc.w);
+                const float x00 = ap[jp], x01 = ap[jq], x10 = aq[jp], x11 = aq[jq];
+                // rows of pair i, then columns of pair j
+                const float r00 = R.x * x00 - R.y * x10, r10 = R.y * x00 + R.x * x10;
+                const float r01 = R.x * x01 - R.y * x11, r11 = R.y * x01 + R.x * x11;
+                ap[jp] = Cc.x * r00 - Cc.y * r01;
+                ap[jq] = Cc.y * r00 + Cc.x * r01;
+                aq[jp] = Cc.x * r10 - Cc.y * r11;
+                aq[jq] = Cc.y * r10 + Cc.x * r11;
+            }
+            for (int u = tid; u < n * half; u += kJThreads) {
+                const float4 Cc = prm[u / n];
+                float* vr = v + (u % n) * ld;
+                const int jp = __float_as_int(Cc.z), jq = __float_as_int(Cc.w);
+                const float vp = vr[jp], vq = vr[jq];
+                vr[jp] = Cc.x * vp - Cc.y * vq;
+                vr[jq] = Cc.y * vp + Cc.x * vq;
+            }
             __syncthreads();
         }
     }
@@ -233,9 +278,10 @@ k_jacobi32(const double* __restrict__ A, long astride, int lda, const int* __res
         if (rank < n0) perm[rank] = i;
     }
     __syncthreads();
-    for (int col = lane; col < n0; col += 128)
-        for (int i = kg; i < n0; i += kJGroups)
-            X[b * xstride + (long)i * ldx + col] = (double)v[i * ld + perm[col]];
+    for (int q = tid; q < n0 * n0; q += kJThreads) {
+        const int i = q / n0, col = q % n0;
+        X[b * xstride + (long)i * ldx + col] = (double)v[i * ld + perm[col]];
+    }
     for (int k = tid; k < n0; k += kJThreads) w[b * wstride + k] = (double)a[perm[k] * ld + perm[k]];
 }
 

@@ -748,6 +748,10 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     MG_CUDA(cudaMemcpyAsync(H.fermi_d, H.fermi, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     MG_CUDA(cudaMemsetAsync(c->flags, 0, 16 * sizeof(int), c->stream));
     MG_TRY(pairing_mesh(c));
+    phase_mark(c, MG_PH_PAIRING_MESH);
+    // the HF-basis DeriveAll of the iteration (mg_iterate) overlaps the
+    // latency-bound rest of the step
+    if (c->side_derive_pending) MG_TRY(side_derive_hf(c));
 
     double lam[2], f[2];
     bool conv[2];
@@ -760,6 +764,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     } else {
         MG_TRY(fermi_newton(c, lam, f, conv, &evals, &first_order));
     }
+    phase_mark(c, MG_PH_FERMI);
     if (conv[0] && conv[1]) {
         for (int it = 0; it < 2; ++it) {
             H.fermi_old[1][it] = H.fermi_old[0][it];
@@ -833,6 +838,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     H.disp[1] = hp[22] + hp[23];
     c->pairing_energy[0] = H.epair[0];
     c->pairing_energy[1] = H.epair[1];
+    phase_mark(c, MG_PH_CANONICAL);
     if (info) {
         std::memset(info, 0, sizeof(*info));
         info->fermi[0] = H.fermi[0];

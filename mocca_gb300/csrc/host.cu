@@ -52,6 +52,10 @@ void free_all(mg_ctx* c) {
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    for (cudaEvent_t e : c->ph.ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ph.side)
+        if (e) cudaEventDestroy(e);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
@@ -636,6 +640,94 @@ extern "C" int mg_launch_count(mg_ctx* c, long long* count) {
     return MG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Phase timer
+// ---------------------------------------------------------------------------
+namespace mg {
+
+// The HF-basis DeriveAll on the side stream, after the work queued so far on
+// the main stream.  The persistent tensor-core kernel takes a whole SM per
+// CTA, so on the side stream it keeps to half of the SMs: the pairing step's
+// kernels find the other half free.  The caller joins on ev_join.
+int side_derive_hf(mg_ctx* c) {
+    c->side_derive_pending = false;
+    MG_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+    MG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    if (c->ph.on && c->ph.n > 0) {
+        MG_CUDA(cudaEventRecord(c->ph.side[0], c->side));
+        c->ph.side_used = true;
+    }
+    cudaStream_t main = c->stream;
+    c->stream = c->side;
+    c->tc_grid_cap = c->num_sms / 2;
+    const int sd = derive_basis(c, MG_HF_BASIS);
+    c->tc_grid_cap = 0;
+    c->stream = main;
+    MG_TRY(sd);
+    if (c->ph.side_used) MG_CUDA(cudaEventRecord(c->ph.side[1], c->side));
+    MG_CUDA(cudaEventRecord(c->ev_join, c->side));
+    return MG_OK;
+}
+
+int phase_begin(mg_ctx* c) {
+    if (!c->ph.on) return MG_OK;
+    c->ph.n = 0;
+    c->ph.side_used = false;
+    MG_CUDA(cudaEventRecord(c->ph.ev[0], c->stream));
+    c->ph.id[0] = -1;
+    c->ph.n = 1;
+    return MG_OK;
+}
+
+void phase_mark(mg_ctx* c, int id) {
+    if (!c->ph.on || c->ph.n == 0 || c->ph.n >= mg_ctx::PhaseTimer::kMarks) return;
+    if (cudaEventRecord(c->ph.ev[c->ph.n], c->stream) != cudaSuccess) return;
+    c->ph.id[c->ph.n++] = id;
+}
+
+int phase_end(mg_ctx* c) {
+    if (!c->ph.on || c->ph.n == 0) return MG_OK;
+    auto& P = c->ph;
+    MG_CUDA(cudaEventSynchronize(P.ev[P.n - 1]));
+    for (int i = 1; i < P.n; ++i) {
+        float ms = 0.0f;
+        MG_CUDA(cudaEventElapsedTime(&ms, P.ev[i - 1], P.ev[i]));
+        P.ms[P.id[i]] += ms;
+    }
+    if (P.side_used) {
+        float ms = 0.0f;
+        MG_CUDA(cudaEventSynchronize(P.side[1]));
+        MG_CUDA(cudaEventElapsedTime(&ms, P.side[0], P.side[1]));
+        P.ms[MG_PH_SIDE_DERIVE] += ms;
+    }
+    ++P.passes;
+    P.n = 0;
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" int mg_set_phase_timing(mg_ctx* c, int on) {
+    if (!c) return MG_ERR_ARG;
+    auto& P = c->ph;
+    if (on && !P.ev[0]) {
+        for (cudaEvent_t& e : P.ev) MG_CUDA(cudaEventCreate(&e));
+        for (cudaEvent_t& e : P.side) MG_CUDA(cudaEventCreate(&e));
+    }
+    P.on = on != 0;
+    P.n = 0;
+    P.passes = 0;
+    for (double& m : P.ms) m = 0.0;
+    return MG_OK;
+}
+
+extern "C" int mg_get_phase_times(mg_ctx* c, double* ms, int n, long long* passes) {
+    if (!c || !ms || n < MG_PH_COUNT) return MG_ERR_ARG;
+    for (int k = 0; k < MG_PH_COUNT; ++k) ms[k] = c->ph.ms[k];
+    if (passes) *passes = c->ph.passes;
+    return MG_OK;
+}
+
 extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
                           mg_energy_terms* out) {
     // Evolve loop body, src/Main.f90:255-328 (HF: SolvePairing = NaiveFill)
@@ -644,49 +736,50 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
     int st = MG_OK;
     for (int k = 0; k < n_iter; ++k) {
         ++c->iteration;
+        MG_TRY(phase_begin(c));
         // AlternateStep while an alternating constraint was active at the
         // last check (src/Main.f90:261-263)
         if (c->cons.alternate_check) MG_TRY(alternate_step(c));
         MG_TRY(mg_grad_desc(c, dt, momentum));
+        phase_mark(c, MG_PH_GRAD_DESC);
         if (hfb) {
             // DeriveAll of the HF basis needs only the new HF spinors: it runs
-            // on the side stream while the pairing step (which reads the same
-            // spinors) runs on the main stream; the canonical basis follows.
-            // The persistent tensor-core kernel takes a whole SM per CTA, so
-            // on the side stream it keeps to half of the SMs: the pairing
-            // step's kernels find the other half free.
-            MG_CUDA(cudaEventRecord(c->ev_fork, c->stream));
-            MG_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-            cudaStream_t main = c->stream;
-            c->stream = c->side;
-            c->tc_grid_cap = c->num_sms / 2;
-            const int sd = derive_basis(c, MG_HF_BASIS);
-            c->tc_grid_cap = 0;
-            c->stream = main;
-            MG_TRY(sd);
-            MG_CUDA(cudaEventRecord(c->ev_join, c->side));
-            MG_TRY(mg_solve_pairing(c, nullptr));
+            // on the side stream, forked by the pairing step once its mesh
+            // contractions are done (side_derive_hf), beside the Fermi search
+            // and the canonical basis; the canonical basis follows.
+            c->side_derive_pending = true;
+            const int sp = mg_solve_pairing(c, nullptr);
+            if (c->side_derive_pending) MG_TRY(side_derive_hf(c));   // not forked
+            MG_TRY(sp);
             MG_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
             MG_TRY(derive_basis(c, MG_CAN_BASIS));
         } else {
             MG_TRY(mg_hf_fill(c));
+            phase_mark(c, MG_PH_CANONICAL);
             MG_TRY(mg_derive_all(c));
         }
+        phase_mark(c, MG_PH_DERIVE);
         c->cons.alternate_check = any_alternating(c);   // src/Main.f90:274
         // canonical single-particle energies with the previous potentials
         // (src/Main.f90:282-289)
         if (hfb) MG_TRY(hpsi_basis(c, MG_CAN_BASIS, nullptr, false, 0.0, 0.0));
+        phase_mark(c, MG_PH_HPSI_CAN);
         MG_TRY(save_density_history(c));
         MG_TRY(densities(c));
         MG_TRY(mix_densities(c));
+        phase_mark(c, MG_PH_DENSITIES);
         MG_TRY(moments(c));
         readjust_moments(c, c->iteration);   // src/Main.f90:299-304
+        phase_mark(c, MG_PH_MOMENTS);
         st = mg_construct_potentials(c, nullptr);
         if (st < 0) return st;
+        phase_mark(c, MG_PH_POTENTIALS);
         // CompEnergy every pass (src/Main.f90:309): it also keeps the energy
         // history of the convergence check
         mg_energy_terms e{};
         MG_TRY(energy(c, out ? out : &e));
+        phase_mark(c, MG_PH_ENERGY);
+        MG_TRY(phase_end(c));
     }
     MG_TRY(tc_check(c));
     return st;

@@ -302,6 +302,21 @@ struct mg_ctx {
 
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
+    bool side_derive_pending = false;  // mg_iterate: the pairing step forks the HF DeriveAll
+
+    // phase timer (mg_set_phase_timing): events between the phases of the
+    // pass in progress, their phase ids, and the totals
+    struct PhaseTimer {
+        static constexpr int kMarks = 24;
+        bool on = false;
+        int n = 0;                          // marks of the pass in progress, 0: none
+        cudaEvent_t ev[kMarks] = {};
+        int id[kMarks] = {};
+        cudaEvent_t side[2] = {};           // side-stream DeriveAll start, end
+        bool side_used = false;
+        double ms[MG_PH_COUNT] = {};
+        long long passes = 0;
+    } ph;
 
     // IterativeEstimation (est.cu): the probe spinor maxspwf with its
     // derivatives and update, its derivative jobs and quantum numbers, and the
@@ -378,6 +393,12 @@ int eig_jacobi_fp64(mg_ctx* c, EigBatch& E);
 void eig_free(EigBatch& E);
 int hfb_prepare(mg_ctx* c);
 int hfb_solve(mg_ctx* c, mg_pairing_info* info);
+// phase timer: open a pass, mark the end of phase id on the stream, close
+// the pass (waits for its last event and adds up the intervals)
+int phase_begin(mg_ctx* c);
+int side_derive_hf(mg_ctx* c);
+void phase_mark(mg_ctx* c, int id);
+int phase_end(mg_ctx* c);
 void hfb_free(mg_ctx* c);
 int density_groups(const mg_ctx* c);
 int time_odd_setup(mg_ctx* c);

@@ -71,6 +71,24 @@ class MeshState:
         self._call("mg_launch_count", C.byref(n))
         return n.value
 
+    PHASES = ("grad_desc", "pairing_mesh", "fermi", "canonical", "derive", "hpsi_can",
+              "densities", "moments", "potentials", "energy", "side_derive")
+
+    def set_phase_timing(self, on: bool = True):
+        """Per-phase CUDA-event timing of the following Evolve passes
+        (mg_set_phase_timing; clears the totals)."""
+        self._call("mg_set_phase_timing", 1 if on else 0)
+
+    def phase_times(self) -> dict:
+        """Average device ms per timed pass of each phase (mg_get_phase_times);
+        side_derive overlaps the pairing phases on the side stream."""
+        ms = np.zeros(len(self.PHASES))
+        n = C.c_longlong(0)
+        self._call("mg_get_phase_times", _dptr(ms), len(ms), C.byref(n))
+        out = {k: float(v) / max(1, n.value) for k, v in zip(self.PHASES, ms)}
+        out["passes"] = n.value
+        return out
+
     def set_precision(self, precision: int):
         """MG_FP64 or MG_MIXED for the following calls (mixed iterations, FP64 polish)."""
         self._call("mg_set_precision", precision)

@@ -120,3 +120,39 @@ def test_unknown_fermi_solver_is_rejected(built):
     pp.fermi_solver = 1
     g.set_pairing(pp)
     g.close()
+
+
+def test_phase_timer_and_side_derive(built):
+    """mg_set_phase_timing / mg_get_phase_times over HFB passes: every phase
+    of the pass is timed, the side-stream HF DeriveAll too, and the timed
+    passes land on the same energies as untimed ones (the timer only records
+    events); the HF-basis derivatives forked inside the pairing step equal
+    a DeriveAll of the same spinors afterwards."""
+    p, g, o = _hfb_pair()
+    o.close()
+    g.Start()
+    ref = MeshState(p, SLY4)
+    psi, qn, en = synthetic.ho_basis(p, p.nwt // 2, seed=1234)
+    ref.set_spinors(psi, qn)
+    ref.set_energies(en)
+    ref.set_pairing()
+    ref.Start()
+    g.set_phase_timing(True)
+    e1 = g.Evolve(3, 0.01, 0.3)["total"]
+    t = g.phase_times()
+    e0 = ref.Evolve(3, 0.01, 0.3)["total"]
+    assert e1 == e0
+    assert t["passes"] == 3
+    for k in g.PHASES:
+        if k != "moments":
+            assert t[k] > 0.0, (k, t)
+    d_side = g.get_derivatives(_abi.MG_HF_BASIS)
+    g.DeriveAll()
+    d_again = g.get_derivatives(_abi.MG_HF_BASIS)
+    for a, b in zip(d_side, d_again):
+        assert np.array_equal(a, b)
+    g.set_phase_timing(False)
+    g.Evolve(1, 0.01, 0.3)
+    assert g.phase_times()["passes"] == 0
+    g.close()
+    ref.close()
