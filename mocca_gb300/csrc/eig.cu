@@ -24,6 +24,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "df.cuh"
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -559,6 +560,182 @@ k_jacobi64_polish(const double* __restrict__ S, long stride, int ld, const int* 
     for (int i = tid; i < n0; i += kJThreads) w[b * wstride + i] = a[i * l2 + i];
 }
 
+// The polish of the mixed form: k_jacobi64_polish in double-float
+// arithmetic (df.cuh) on the FP32 pipes, which GB300 issues at ~60x its FP64
+// rate.  S and the rotations Q are held in shared memory as {hi, lo} pairs
+// (48 significant bits; S split from FP64 with integer instructions), so
+// the threshold is 4e-14 |A| against the FP64 polish's 1e-14.  tan(theta)
+// is taken in FP32 -- an inexact angle only leaves a smaller coupling for
+// the next sweep -- and c = (1 + t^2)^(-1/2), s = t c are completed to
+// double-float precision by one Newton step on the FP32 reciprocal square
+// root, so that every rotation stays orthogonal to ~1e-14.  A round rotates
+// the 2 x 2 blocks (rows of pair i, columns of pair j) whose row or column
+// pair is active, and the columns of Q of its active pairs.  Q is written
+// back in FP64.  n <= kDfPolishMax.
+constexpr int kDfPolishMax = 112;
+
+size_t df_polish_smem(int n) {
+    const int np = n + (n & 1);
+    return (size_t)2 * np * (np + 1) * sizeof(float2);
+}
+
+__device__ __forceinline__ dfl df_rot_a(dfl c, dfl s, dfl x, dfl y) {   // c x - s y
+    return df_fma(c, x, df_neg(df_mul(s, y)));
+}
+
+__device__ __forceinline__ dfl df_rot_b(dfl c, dfl s, dfl x, dfl y) {   // s x + c y
+    return df_fma(s, x, df_mul(c, y));
+}
+
+__global__ void __launch_bounds__(kJThreads)
+k_jacobi_df_polish(const double* __restrict__ S, long stride, int ld, const int* __restrict__ nsz,
+                   const double* __restrict__ anorm, double* __restrict__ Q,
+                   double* __restrict__ w, long wstride, int* __restrict__ pfail,
+                   int max_sweeps) {
+    extern __shared__ float2 smq[];
+    __shared__ float4 cs[kDfPolishMax / 2];   // c.h, c.l, s.h, s.l
+    __shared__ int act[kDfPolishMax / 2];
+    __shared__ int pqi[2][kDfPolishMax / 2];
+    __shared__ unsigned rmask[(kDfPolishMax + 31) / 32];
+    const int b = blockIdx.x;
+    const int n0 = nsz[b];
+    if (n0 == 0) {
+        if (threadIdx.x == 0 && pfail) pfail[b] = 0;
+        return;
+    }
+    const int n = n0 + (n0 & 1);
+    const int l2 = n + 1;
+    float2* a = smq;            // n x l2
+    float2* qs = a + n * l2;    // n x l2 (rows and columns < n0 used)
+    const int tid = threadIdx.x;
+    for (int t = tid; t < n * n; t += kJThreads) {
+        const int i = t / n, j = t % n;
+        dfl x{0.0f, 0.0f};
+        if (i < n0 && j < n0) {
+            x = df_split(S[b * stride + (long)i * ld + j]);
+            if (i != j) {
+                // symmetrise: (x + y) / 2 (the halving is exact)
+                const dfl y = df_split(S[b * stride + (long)j * ld + i]);
+                x = df_add(x, y);
+                x.h *= 0.5f;
+                x.l *= 0.5f;
+            }
+        }
+        a[i * l2 + j] = make_float2(x.h, x.l);
+        qs[i * l2 + j] = make_float2(i == j ? 1.0f : 0.0f, 0.0f);
+    }
+    __syncthreads();
+    const float thr = (float)(4e-14 * anorm[b]);
+    const int half = n / 2;
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        // as in k_jacobi64_polish: only the rounds that hold a coupling above
+        // the threshold at the start of the sweep run
+        if (tid < (kDfPolishMax + 31) / 32) rmask[tid] = 0u;
+        __syncthreads();
+        int any = 0;
+        for (int t = tid; t < n * n; t += kJThreads) {
+            const int i = t / n, col = t % n;
+            if (i < col && fabsf(a[i * l2 + col].x) > thr) {
+                const int r = rr_round(i, col, n);
+                atomicOr(&rmask[r >> 5], 1u << (r & 31));
+                any = 1;
+            }
+        }
+        if (!__syncthreads_or(any)) break;
+        for (int r = 0; r < n - 1; ++r) {
+            if (!((rmask[r >> 5] >> (r & 31)) & 1u)) continue;
+            int on = 0;
+            if (tid < half) {
+                const int p = rr_player(tid, r, n), q = rr_player(n - 1 - tid, r, n);
+                const dfl apq = df_ld(a + p * l2 + q);
+                dfl c{1.0f, 0.0f}, sn{0.0f, 0.0f};
+                if (fabsf(apq.h) > thr) {
+                    const dfl d = df_sub(df_ld(a + q * l2 + q), df_ld(a + p * l2 + p));
+                    float tt;
+                    if (fabsf(d.h) > 1e6f * fabsf(apq.h)) {
+                        tt = apq.h / d.h;   // small angle: tan = a_pq / d to ~1e-12
+                    } else {
+                        const float th = d.h / (2.0f * apq.h);
+                        tt = (th >= 0.0f ? 1.0f : -1.0f) / (fabsf(th) + sqrtf(th * th + 1.0f));
+                    }
+                    // c = (1 + t^2)^(-1/2): FP32 estimate r, then r (3 - x r^2) / 2
+                    const dfl x = df_add(dfl{1.0f, 0.0f}, df_mul(dfl{tt, 0.0f}, dfl{tt, 0.0f}));
+                    const float r0 = rsqrtf(x.h);
+                    const dfl xr2 = df_mul(x, df_mul(dfl{r0, 0.0f}, dfl{r0, 0.0f}));
+                    dfl corr = df_sub(dfl{3.0f, 0.0f}, xr2);
+                    corr.h *= 0.5f;
+                    corr.l *= 0.5f;
+                    c = df_mul(dfl{r0, 0.0f}, corr);
+                    sn = df_mul(dfl{tt, 0.0f}, c);
+                    on = 1;
+                }
+                cs[tid] = make_float4(c.h, c.l, sn.h, sn.l);
+                act[tid] = on;
+                pqi[0][tid] = p;
+                pqi[1][tid] = q;
+            }
+            if (!__syncthreads_or(on)) continue;
+            for (int u = tid; u < half * half; u += kJThreads) {
+                const int i = u / half, j = u % half;
+                const int ai = act[i], aj = act[j];
+                if (!ai && !aj) continue;
+                float2* ap = a + pqi[0][i] * l2;
+                float2* aq = a + pqi[1][i] * l2;
+                const int jp = pqi[0][j], jq = pqi[1][j];
+                dfl x00 = df_ld(ap + jp), x01 = df_ld(ap + jq), x10 = df_ld(aq + jp),
+                    x11 = df_ld(aq + jq);
+                if (ai) {   // rows of pair i
+                    const float4 C = cs[i];
+                    const dfl c{C.x, C.y}, sn{C.z, C.w};
+                    const dfl r00 = df_rot_a(c, sn, x00, x10), r10 = df_rot_b(c, sn, x00, x10);
+                    const dfl r01 = df_rot_a(c, sn, x01, x11), r11 = df_rot_b(c, sn, x01, x11);
+                    x00 = r00;
+                    x10 = r10;
+                    x01 = r01;
+                    x11 = r11;
+                }
+                if (aj) {   // columns of pair j
+                    const float4 C = cs[j];
+                    const dfl c{C.x, C.y}, sn{C.z, C.w};
+                    const dfl r00 = df_rot_a(c, sn, x00, x01), r01 = df_rot_b(c, sn, x00, x01);
+                    const dfl r10 = df_rot_a(c, sn, x10, x11), r11 = df_rot_b(c, sn, x10, x11);
+                    x00 = r00;
+                    x01 = r01;
+                    x10 = r10;
+                    x11 = r11;
+                }
+                df_st(ap + jp, x00);
+                df_st(ap + jq, x01);
+                df_st(aq + jp, x10);
+                df_st(aq + jq, x11);
+            }
+            for (int u = tid; u < n0 * half; u += kJThreads) {
+                const int k = u / n0, row = u % n0;
+                if (!act[k]) continue;
+                const float4 C = cs[k];
+                const dfl c{C.x, C.y}, sn{C.z, C.w};
+                float2* qr = qs + row * l2;
+                const int p = pqi[0][k], q = pqi[1][k];
+                const dfl vp = df_ld(qr + p), vq = df_ld(qr + q);
+                df_st(qr + p, df_rot_a(c, sn, vp, vq));
+                df_st(qr + q, df_rot_b(c, sn, vp, vq));
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0 && pfail) pfail[b] = sweep == max_sweeps ? 1 : 0;
+    for (int t = tid; t < n0 * n0; t += kJThreads) {
+        const int r = t / n0, c = t % n0;
+        const float2 v = qs[r * l2 + c];
+        Q[b * stride + (long)r * ld + c] = df_to_fast(dfl{v.x, v.y});
+    }
+    for (int i = tid; i < n0; i += kJThreads) {
+        const float2 v = a[i * l2 + i];
+        w[b * wstride + i] = df_to_fast(dfl{v.x, v.y});
+    }
+}
+
 // Re-orthonormalisation X <- X (I + R/2 + 3/8 R^2), R = I - X^T X (third-order
 // accurate): from G = X^T X write R into Rm and I + R/2 into F.
 __global__ void k_orth_prep(const double* __restrict__ G, double* __restrict__ Rm,
@@ -651,6 +828,9 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
                                      kSmemOptIn));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kSmemOptIn));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi_df_polish,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)df_polish_smem(kDfPolishMax)));
         E.attr_done = true;
     }
     if (seed != kSeedRefine) {
@@ -715,8 +895,12 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
         MG_LAUNCHED(c);
-        k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(
-            E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail, 12);
+        if (c->cur_precision == MG_MIXED && E.nmax <= kDfPolishMax)
+            k_jacobi_df_polish<<<E.nb, kJThreads, df_polish_smem(E.nmax), c->stream>>>(
+                E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail, 12);
+        else
+            k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(
+                E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail, 12);
         MG_LAUNCHED(c);
         k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
         MG_LAUNCHED(c);
@@ -751,6 +935,9 @@ int eig_jacobi_fp64(mg_ctx* c, EigBatch& E) {
                                      kSmemOptIn));
         MG_CUDA(cudaFuncSetAttribute(k_jacobi64_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kSmemOptIn));
+        MG_CUDA(cudaFuncSetAttribute(k_jacobi_df_polish,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)df_polish_smem(kDfPolishMax)));
         E.attr_done = true;
     }
     k_frob<<<E.nb, 1024, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
