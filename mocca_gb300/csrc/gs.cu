@@ -115,66 +115,60 @@ __global__ void k_gs_sum(double* __restrict__ part, int nbmax, int nchunk) {
     if (lane == 0) pb[t] = s;
 }
 
-// Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].  The elimination
-// keeps the rows unscaled (one barrier per column): after step j row j holds
-// U[j][l] = R[j][j] R[j][l].  Then R = U / sqrt(diag) and each thread finds one
-// column of X by back substitution.
+// Cholesky S = R^T R (R upper), X = R^{-1}; X to xout[b].
 __global__ void __launch_bounds__(kThreads)
 k_gs_factor(const double* __restrict__ part, const int* __restrict__ starts, int nbmax,
             int nchunk, double dv, double* __restrict__ xout, int* __restrict__ flag) {
+    // S = L D L^T by symmetric elimination (L unit lower, D the pivots), so
+    // that R = D^(1/2) L^T; the same row operations applied to the identity
+    // leave W = L^(-1), and X = R^(-1) = W^T D^(-1/2) needs no back
+    // substitution.  GB300 issues a warp's FP64 instruction over ~16 clocks
+    // and a divide or square root is a sequence of them, so each pivot's
+    // reciprocal and reciprocal square root are taken once, by one thread.
     extern __shared__ double sm[];
     const int b = blockIdx.x;
     const int nb = starts[b + 1] - starts[b];
     if (nb == 0) return;
-    double* S = sm;              // nb x nb (upper used), becomes R
-    double* X = sm + nb * nb;    // nb x nb
-    __shared__ double rinv[256];
+    double* S = sm;              // nb x nb (upper used)
+    double* W = sm + nb * nb;    // nb x nb (lower used), L^(-1)
+    __shared__ double rsq[256];  // D^(-1/2)
     __shared__ double u[256];
+    __shared__ double inv_d;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     constexpr int kWarps = kThreads / 32;
     for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
         const int k = t / nb, l = t % nb;
         S[t] = k <= l ? part[(long)b * nchunk * nbmax * nbmax + k * nbmax + l] * dv : 0.0;
-        X[t] = 0.0;
+        W[t] = k == l ? 1.0 : 0.0;
     }
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
-        // pivot row scaled once (u_k = S_jk / S_jj), then one FMA per entry of
-        // the trailing upper triangle, a warp per row
-        const double d = S[j * nb + j];
-        if (threadIdx.x == 0 && !(d > 0.0)) atomicExch(flag, 1);
-        const double inv_d = 1.0 / fmax(d, 1e-300);
-        for (int k = j + 1 + threadIdx.x; k < nb; k += kThreads) u[k] = S[j * nb + k] * inv_d;
+        if (threadIdx.x == 0) {
+            const double d = S[j * nb + j];
+            if (!(d > 0.0)) atomicExch(flag, 1);
+            const double dd = fmax(d, 1e-300);
+            inv_d = 1.0 / dd;
+            rsq[j] = 1.0 / sqrt(dd);
+        }
+        __syncthreads();
+        // pivot row scaled once (u_k = S_jk / S_jj), then one FMA per entry
+        // of the trailing upper triangle and of W's rows below j, a warp per row
+        const double id = inv_d;
+        for (int k = j + 1 + threadIdx.x; k < nb; k += kThreads) u[k] = S[j * nb + k] * id;
         __syncthreads();
         for (int k = j + 1 + warp; k < nb; k += kWarps) {
             const double uk = u[k];
             for (int l = k + lane; l < nb; l += 32) S[k * nb + l] = fma(-uk, S[j * nb + l], S[k * nb + l]);
+            for (int l = lane; l <= j; l += 32) W[k * nb + l] = fma(-uk, W[j * nb + l], W[k * nb + l]);
         }
         __syncthreads();
     }
-    for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
-        const int j = t / nb, l = t % nb;
-        if (l > j) S[t] = S[t] / sqrt(fmax(S[j * nb + j], 1e-300));
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nb; j += kThreads) {
-        const double r = sqrt(fmax(S[j * nb + j], 1e-300));
-        S[j * nb + j] = r;
-        if (j < 256) rinv[j] = 1.0 / r;
-    }
-    __syncthreads();
-    // X[i][j] = -(sum_{i<k<=j} R[i][k] X[k][j]) / R[i][i], X[j][j] = 1 / R[j][j]
-    for (int j = threadIdx.x; j < nb; j += kThreads) {
-        X[j * nb + j] = rinv[j];
-        for (int i = j - 1; i >= 0; --i) {
-            double s = 0.0;
-            for (int k = i + 1; k <= j; ++k) s = fma(S[i * nb + k], X[k * nb + j], s);
-            X[i * nb + j] = -s * rinv[i];
-        }
-    }
-    __syncthreads();
+    // X[i][j] = W[j][i] d_j^(-1/2) (i <= j), zero below the diagonal
     double* xo = xout + (long)b * nbmax * nbmax;
-    for (int t = threadIdx.x; t < nb * nb; t += kThreads) xo[(t / nb) * nbmax + t % nb] = X[t];
+    for (int t = threadIdx.x; t < nb * nb; t += kThreads) {
+        const int i = t / nb, j = t % nb;
+        xo[i * nbmax + j] = i <= j ? W[j * nb + i] * rsq[j] : 0.0;
+    }
 }
 
 // psi'_l = sum_{k<=l} X[k][l] psi_k over a chunk of points, in place; when
