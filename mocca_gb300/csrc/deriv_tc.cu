@@ -18,12 +18,15 @@
 //              turns the current one into digit planes (two plane buffers);
 //   warp 4     MMA issue (one thread): 21 digit pairs x 2 K steps into one of
 //              two TMEM accumulator sets (4 accumulators of N columns each);
-//   warps 5-12 epilogue: two warps per TMEM lane quarter (column halves),
-//              combine the accumulators to double-float, scale, store; the
-//              Laplacian values they add to are loaded before the MMA wait.
+//   warps 5-20 epilogue: four warps per TMEM lane quarter (a 4-column
+//              quarter of every 16 columns), combine the accumulators to
+//              double-float, scale, store; the Laplacian values they add to
+//              are loaded before the MMA wait.
 // Hand-offs are mbarriers: fullA (128 slicer arrivals), emptyA and fullT
 // (tcgen05.commit), emptyT (256 epilogue arrivals); every wait is bounded
-// and a timeout sets the context's status word.
+// and a timeout sets the context's status word.  The slicers wait only for
+// the MMAs to release their plane buffer; the line exponents the epilogue
+// reads sit in a four-tile ring.
 // Three launches, one per axis: x writes d/dx and Lxx, y writes d/dy and
 // adds Lyy, z writes d/dz and adds Lzz, so the Laplacian is summed
 // (X + Y) + Z as in Lapla_LAG_EV8.
@@ -47,8 +50,8 @@ constexpr int kKp = 32;                         // padded K
 constexpr int kPlane = kTile * kKp * 2;         // bytes of one digit plane of a tile
 constexpr int kSlicers = 128;                   // warps 0-3
 constexpr int kMmaWarp = 4;
-constexpr int kEpi = 256;                       // warps 5-12
-constexpr int kThreads = kSlicers + 32 + kEpi;  // 416
+constexpr int kEpi = 512;                       // warps 5-20
+constexpr int kThreads = kSlicers + 32 + kEpi;  // 672
 constexpr uint32_t kTmemCols = 512;             // 2 sets x 4 accumulators x N (N <= 64)
 constexpr long long kWaitCycles = 4000000000LL; // ~2 s at the top SM clock
 
@@ -63,8 +66,12 @@ struct TcPass {
 
 struct TcShared {
     uint64_t fullA[2], emptyA[2], fullT[2], emptyT[2];
+    uint64_t emaxReady[4];   // tile k's line exponents written (128 slicer arrivals)
     uint32_t tmem;
-    int emax[2][kTile];
+    // line exponents of the last four tiles: the slicers write tile k's while
+    // the epilogue may still read tile k-2's (slicer k waits for MMA k-2,
+    // which waited for epilogue k-4)
+    int emax[4][kTile];
     float srow[2][64];
 };
 
@@ -113,6 +120,7 @@ k_deriv_tc(TcPass P) {
             tc::mbar_init(&S.fullT[b], 1);
             tc::mbar_init(&S.emptyT[b], kEpi);
         }
+        for (int b = 0; b < 4; ++b) tc::mbar_init(&S.emaxReady[b], kSlicers);
     }
     for (int s = 0; s < 2; ++s) {
         const uint4* src = reinterpret_cast<const uint4*>(P.bmat[s]);
@@ -155,12 +163,11 @@ k_deriv_tc(TcPass P) {
             if (Tn < P.ntiles) prefetch(Tn, buf ^ 1);
             tc::cp_async_commit();
             if (k >= 2) {
-                const uint32_t ph = ((k - 2) >> 1) & 1;
-                ok &= tc::mbar_wait(&S.emptyA[buf], ph, kWaitCycles);
-                ok &= tc::mbar_wait(&S.emptyT[buf], ph, kWaitCycles);
+                ok &= tc::mbar_wait(&S.emptyA[buf], ((k - 2) >> 1) & 1, kWaitCycles);
                 if (!ok) break;
             }
-            S.emax[buf][r] = emax;
+            S.emax[k & 3][r] = emax;
+            tc::mbar_arrive(&S.emaxReady[k & 3]);
             uint8_t* planes = sA + buf * kDigits * kPlane;
 #pragma unroll 1
             for (int g = 0; g < kKp / 8; ++g) {
@@ -210,7 +217,7 @@ k_deriv_tc(TcPass P) {
     } else {
         // ---------------- epilogue ----------------
         const int e = tid - (kSlicers + 32);
-        const int quarter = warp & 3, colh = e >> 7;
+        const int quarter = warp & 3, colg = e >> 7;
         const int erow = quarter * 32 + lane;   // TMEM lane = tile row
         const uint32_t tq = (uint32_t)(quarter * 32) << 16;
         const int nq = N / 16;
@@ -228,45 +235,46 @@ k_deriv_tc(TcPass P) {
             const bool stage = P.axis != 0 && gL != nullptr && live && P.lap_stage;
             if (stage) {
                 for (int q = 0; q < nq; ++q)
-                    for (int u = 0; u < 8; ++u) {
-                        const int j = 16 * q + 8 * colh + u;
+                    for (int u = 0; u < 4; ++u) {
+                        const int j = 16 * q + 4 * colg + u;
                         if (j >= n && j < 2 * n)
                             tc::cp_async8(sLap + erow * (n + 1) + (j - n),
                                           gL + off + (long)(j - n) * stride);
                     }
             }
             tc::cp_async_commit();
-            ok &= tc::mbar_wait(&S.fullA[buf], (k >> 1) & 1, kWaitCycles);
+            // ring of four: slicer k + 4 cannot arrive before this epilogue is done
+            ok &= tc::mbar_wait(&S.emaxReady[k & 3], (k >> 2) & 1, kWaitCycles);
             ok &= tc::mbar_wait(&S.fullT[buf], (k >> 1) & 1, kWaitCycles);
             if (!ok) break;
             tc::fence_after();
-            const int emax = S.emax[buf][erow];
+            const int emax = S.emax[k & 3][erow];
             const float sline = emax == 0 ? 0.0f : oz::pow2f(emax - 1023 - 12);
             const float* srow = S.srow[slot_of(J, P.axis)];
             const uint32_t tb = tmem + tq + (uint32_t)(buf * 4 * N);
             bool landed = !stage;
 #pragma unroll 1
             for (int q = 0; q < nq; ++q) {
-                const int c0 = 16 * q + 8 * colh;
+                const int c0 = 16 * q + 4 * colg;
                 // the staged Laplacian values are needed from the first
                 // chunk that holds second-derivative columns
-                if (!landed && c0 + 8 > n) {
+                if (!landed && c0 + 4 > n) {
                     tc::cp_async_wait_all();
                     landed = true;
                 }
-                uint32_t r0[8], r1[8], r2[8], r3[8];
+                uint32_t r0[4], r1[4], r2[4], r3[4];
                 __syncwarp();
-                tc::ld8(tb + (uint32_t)(0 * N + c0), r0);
-                tc::ld8(tb + (uint32_t)(1 * N + c0), r1);
-                tc::ld8(tb + (uint32_t)(2 * N + c0), r2);
-                tc::ld8(tb + (uint32_t)(3 * N + c0), r3);
+                tc::ld4(tb + (uint32_t)(0 * N + c0), r0);
+                tc::ld4(tb + (uint32_t)(1 * N + c0), r1);
+                tc::ld4(tb + (uint32_t)(2 * N + c0), r2);
+                tc::ld4(tb + (uint32_t)(3 * N + c0), r3);
                 tc::wait_ld(r0);
                 tc::wait_ld(r1);
                 tc::wait_ld(r2);
                 tc::wait_ld(r3);
                 if (!live) continue;
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
+                for (int u = 0; u < 4; ++u) {
                     const int j = c0 + u;
                     if (j >= 2 * n) break;
                     dfl o = oz::combine4(__uint_as_float(r0[u]), __uint_as_float(r1[u]),
@@ -300,7 +308,7 @@ k_deriv_tc(TcPass P) {
 
 }  // namespace
 
-constexpr size_t kSmemCap = 225 * 1024;
+constexpr size_t kSmemCap = 224 * 1024;   // plus ~2.7 KB of static TcShared
 
 size_t tc_smem_bytes(int n, int N, bool lap_stage) {
     size_t b = 128 + 2 * (size_t)kDigits * kPlane + 2 * (size_t)kDigits * N * tc::kRowBytes +

@@ -489,6 +489,12 @@ static int eval_launches(mg_ctx* c, int seed) {
 static int eval_run(mg_ctx* c, int seed) {
     Hfb& H = c->hfb;
     if (seed == kSeedCold || H.no_graph) return eval_launches(c, seed);
+    // the mixed and FP64 forms launch different polish kernels: recapture on
+    // a switch of form
+    if (H.eval_graph[seed] && H.eval_graph_prec[seed] != c->cur_precision) {
+        cudaGraphExecDestroy(H.eval_graph[seed]);
+        H.eval_graph[seed] = nullptr;
+    }
     if (!H.eval_graph[seed]) {
         if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();    // e.g. the legacy default stream: launch directly
@@ -510,6 +516,7 @@ static int eval_run(mg_ctx* c, int seed) {
             return MG_ERR_CUDA;
         }
         H.eval_graph_launches[seed] = c->launches - l0;
+        H.eval_graph_prec[seed] = c->cur_precision;
         c->launches = l0;
     }
     MG_CUDA(cudaGraphLaunch(H.eval_graph[seed], c->stream));

@@ -141,6 +141,7 @@ struct Hfb {
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
     long long eval_graph_launches[3] = {0, 0, 0};
+    int eval_graph_prec[3] = {-1, -1, -1};   // precision form the graph was captured in
     bool no_graph = false;
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};

@@ -148,6 +148,19 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 // 32 TMEM lanes x 8 consecutive 32-bit columns.
+__device__ __forceinline__ void ld4(uint32_t taddr, uint32_t (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void wait_ld(uint32_t (&r)[4]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3])
+                 :
+                 : "memory");
+}
+
 __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
