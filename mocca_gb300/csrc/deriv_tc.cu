@@ -322,6 +322,13 @@ size_t tc_smem_bytes(int n, int N, bool lap_stage) {
 int tc_setup(mg_ctx* c) {
     const int ns[3] = {c->nx, c->ny, c->nz};
     c->tc_ok = false;
+    // the mesh-sized GEMMs of meshgemm_tc.cu need no Lagrange planes: they
+    // run on any mesh
+    if (!c->tc_status) {
+        MG_CUDA(cudaMalloc(&c->tc_status, sizeof(int)));
+        MG_CUDA(cudaMemset(c->tc_status, 0, sizeof(int)));
+    }
+    c->tc_mesh_ok = true;
     for (int a = 0; a < 3; ++a)
         if (ns[a] > kKp) return MG_OK;
     long total = 0;
@@ -361,8 +368,6 @@ int tc_setup(mg_ctx* c) {
     MG_CUDA(cudaMemcpy(c->tcmats, h.data(), total * sizeof(uint16_t), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&c->tc_erow, he.size() * sizeof(int)));
     MG_CUDA(cudaMemcpy(c->tc_erow, he.data(), he.size() * sizeof(int), cudaMemcpyHostToDevice));
-    MG_CUDA(cudaMalloc(&c->tc_status, sizeof(int)));
-    MG_CUDA(cudaMemset(c->tc_status, 0, sizeof(int)));
     MG_CUDA(cudaFuncSetAttribute(k_deriv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kSmemCap));
     c->tc_ok = true;
@@ -399,9 +404,10 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs) {
 }
 
 // Status of the tensor-core waits since the last call (MG_ERR_TIMEOUT when an
-// MMA completion wait ran out of its cap); synchronises the stream.
+// MMA completion wait ran out of its cap, in the derivatives or the mesh
+// GEMMs); synchronises the stream.
 int tc_check(mg_ctx* c) {
-    if (!c->tc_ok) return MG_OK;
+    if (!c->tc_ok && !c->tc_mesh_ok) return MG_OK;
     int h = 0;
     MG_CUDA(cudaMemcpyAsync(&h, c->tc_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaStreamSynchronize(c->stream));

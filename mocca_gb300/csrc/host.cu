@@ -647,8 +647,10 @@ namespace mg {
 
 // The HF-basis DeriveAll on the side stream, after the work queued so far on
 // the main stream.  The persistent tensor-core kernel takes a whole SM per
-// CTA, so on the side stream it keeps to half of the SMs: the pairing step's
-// kernels find the other half free.  The caller joins on ev_join.
+// CTA, so on the side stream it keeps to two thirds of the SMs: the Fermi
+// search's kernels find the rest free (measured at 24^3, nwt=160: caps of
+// 1/4, 1/3, 1/2 and 2/3 of the SMs gave 3.376, 3.358, 3.353 and 3.325 ms per
+// mixed iteration).  The caller joins on ev_join.
 int side_derive_hf(mg_ctx* c) {
     c->side_derive_pending = false;
     MG_CUDA(cudaEventRecord(c->ev_fork, c->stream));
@@ -659,7 +661,7 @@ int side_derive_hf(mg_ctx* c) {
     }
     cudaStream_t main = c->stream;
     c->stream = c->side;
-    c->tc_grid_cap = c->num_sms / 2;
+    c->tc_grid_cap = c->num_sms * 2 / 3;
     const int sd = derive_basis(c, MG_HF_BASIS);
     c->tc_grid_cap = 0;
     c->stream = main;

@@ -2,6 +2,9 @@
 // tcgen05 tensor cores (exact BF16 digit products, ozaki.cuh): the
 // Gram-Schmidt overlap and apply, and the canonical-basis transform.
 //
+// Blocks of up to kMeshTcMax (80) spinors; above 64, four accumulators take
+// 512 TMEM columns and the kernels run one CTA per SM.
+//
 // Gram-Schmidt (gs.cu; GramSchmidt, src/SpwfStorage.f90:372-480, as
 // Q = Psi R^{-1} with S = R^T R per (isospin, parity, signature) block in
 // energy order):
@@ -38,7 +41,12 @@ constexpr int kRows = 128;            // MMA M
 constexpr int kChunk = 256;           // overlap points per CTA
 constexpr int kStage = 32;            // overlap points per MMA stage (K)
 constexpr int kStagePlane = kRows * kStage * 2;   // bytes of one digit plane of a stage
-constexpr uint32_t kTmemCols = 256;
+// TMEM columns for four accumulators of N columns: 256 up to N = 64, 512 above
+// (one CTA per SM then; the launches keep the shared memory above half of the
+// SM's so that a second CTA never waits in tcgen05.alloc)
+__host__ __device__ constexpr uint32_t tmem_cols(int N) { return 4 * N <= 256 ? 256u : 512u; }
+constexpr long kXdStride = (long)kMeshTcMax * kMeshTcMax;   // per block in the coefficient planes
+constexpr size_t kOneCtaSmem = 116 * 1024;
 constexpr long long kWaitCycles = 4000000000LL;
 
 // Block sizes and list offsets: Gram-Schmidt blocks come from a start table,
@@ -62,21 +70,23 @@ k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
-    __shared__ int sE[64];
+    __shared__ int sE[kRows];
     const int b = blockIdx.y, chunk = blockIdx.x;
     const int s0 = starts[b], nb = starts[b + 1] - s0;
     if (nb == 0) return;
     const int N = max(16, (nb + 15) / 16 * 16);
+    const uint32_t tcols = tmem_cols(N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int row = tid >> 2, g = tid & 3;   // a row's 4 K groups sit on 4 neighbouring lanes
-    const bool live = row < nb;
+    // rows row0 and row0 + 64 (blocks above 64 spinors); a row's 4 K groups
+    // sit on 4 neighbouring lanes
+    const int row0 = tid >> 2, g = tid & 3;
 
     const uint32_t s0a = tc::smem_u32(smraw);
     uint8_t* base = smraw + ((128u - (s0a & 127u)) & 127u);
     // two stage buffers of kDigits planes; rows >= nb stay zero
     for (int t = tid; t < 2 * kDigits * kStagePlane / 16; t += 256)
         reinterpret_cast<uint4*>(base)[t] = make_uint4(0u, 0u, 0u, 0u);
-    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (warp == 0) tc::alloc(&tmem_slot, tcols);
     if (tid == 0) {
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
@@ -84,22 +94,28 @@ k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
     const long p0 = (long)chunk * kChunk;
     const int npts = (int)min((long)kChunk, V4 - p0);
     const int nst = (npts + kStage - 1) / kStage;
-    const double* src = live ? psi + (long)ordered[s0 + row] * V4 + p0 : psi;
-
-    // largest exponent of the row over the chunk
-    int emax = 0;
-    if (live) {
-        for (int s = 0; s < nst; ++s) {
+    bool live[2];
+    const double* src[2];
+    int emax[2] = {0, 0};
 #pragma unroll
-            for (int h = 0; h < 8; ++h) {
-                const int q = s * kStage + 8 * g + h;
-                if (q < npts) emax = max(emax, oz::bexp(src[q]));
+    for (int r = 0; r < 2; ++r) {
+        const int row = row0 + 64 * r;
+        live[r] = row < nb;
+        src[r] = live[r] ? psi + (long)ordered[s0 + row] * V4 + p0 : psi;
+        // largest exponent of the row over the chunk
+        if (live[r]) {
+            for (int s = 0; s < nst; ++s) {
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int q = s * kStage + 8 * g + h;
+                    if (q < npts) emax[r] = max(emax[r], oz::bexp(src[r][q]));
+                }
             }
         }
+        emax[r] = max(emax[r], __shfl_xor_sync(0xffffffffu, emax[r], 1));
+        emax[r] = max(emax[r], __shfl_xor_sync(0xffffffffu, emax[r], 2));
+        if (live[r] && g == 0) sE[row] = emax[r];
     }
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-    if (live && g == 0) sE[row] = emax;
 
     tc::fence_before();
     __syncthreads();
@@ -111,19 +127,21 @@ k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
         const int buf = s & 1;
         uint8_t* planes = base + buf * kDigits * kStagePlane;
         if (s >= 2) ok &= tc::mbar_wait(&mbar[buf], ((s - 2) >> 1) & 1, kWaitCycles);
-        if (live) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!live[r]) continue;
             double v[8];
 #pragma unroll
             for (int h = 0; h < 8; ++h) {
                 const int q = s * kStage + 8 * g + h;
-                v[h] = q < npts ? src[q] : 0.0;
+                v[h] = q < npts ? src[r][q] : 0.0;
             }
             uint4 w[kDigits];
-            oz::digits8(v, emax, w);
+            oz::digits8(v, emax[r], w);
 #pragma unroll
             for (int a = 0; a < kDigits; ++a)
-                *reinterpret_cast<uint4*>(planes + a * kStagePlane + tc::kmajor_off(row, 8 * g)) =
-                    w[a];
+                *reinterpret_cast<uint4*>(planes + a * kStagePlane +
+                                          tc::kmajor_off(row0 + 64 * r, 8 * g)) = w[a];
         }
         tc::fence_proxy_async();
         tc::fence_before();
@@ -179,7 +197,7 @@ k_gs_overlap_tc(const double* __restrict__ psi, const int* __restrict__ starts,
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::dealloc(tmem, tcols);
 }
 
 // Digit planes of C (per block: kDigits planes of Np rows x Np, row l = output
@@ -194,11 +212,11 @@ __global__ void k_coef_digits(const double* __restrict__ coef, long bstride, int
     if (nb == 0 || l >= Np) return;
     const int ldc = ld > 0 ? ld : nb;
     const double* X = coef + (long)b * bstride;
-    uint16_t* out = xd + (long)b * kDigits * 64 * 64;
+    uint16_t* out = xd + (long)b * kDigits * kXdStride;
     int emax = 0;
     if (l < nb)
         for (int k = 0; k < nb; ++k) emax = max(emax, oz::bexp(X[k * ldc + l]));
-    xe[b * 64 + l] = emax;
+    xe[b * kMeshTcMax + l] = emax;
     for (int k = 0; k < Np; ++k) {
         const double v = (l < nb && k < nb) ? X[k * ldc + l] : 0.0;
         uint32_t d[kDigits];
@@ -212,7 +230,9 @@ __global__ void k_coef_digits(const double* __restrict__ coef, long bstride, int
 // out_l = sum_k C[k][l] in_k over 128 points (in_k = in[in_list[off + k]],
 // out_l = out[out_list[off + l]] or out[out_base[b] + l]); when upd is given,
 // upd_l = out_l - upd_l.  in and out may be the same array (in place).
-// Thread t: point row = t % 128, K groups {h, h + 2, h + 4} (h = t / 128).
+// Thread t: point row = t % 128, K groups h, h + 2, h + 4, ... (h = t / 128);
+// up to 48 spinors the point's values stay in registers between the
+// exponent and the digits, above they are read twice.
 __global__ void __launch_bounds__(256, 2)
 k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
            const int* __restrict__ in_list, const int* __restrict__ out_list,
@@ -222,14 +242,15 @@ k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int sEmax[256];
-    __shared__ int sXe[64];
-    __shared__ int sIdx[64];
-    __shared__ int sOut[64];
+    __shared__ int sXe[kMeshTcMax];
+    __shared__ int sIdx[kMeshTcMax];
+    __shared__ int sOut[kMeshTcMax];
     const int b = blockIdx.y;
     const int s0 = bi.off(b), nb = bi.nb(b);
     if (nb == 0) return;
     const int Np = max(16, (nb + 15) / 16 * 16);
     const int kg = Np / 8;
+    const uint32_t tcols = tmem_cols(Np);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int row = tid & (kRows - 1), half = tid >> 7;
     const long p = (long)blockIdx.x * kRows + row;
@@ -240,49 +261,82 @@ k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
     const int aPlane = kRows * Np * 2, bPlane = Np * Np * 2;
     uint8_t* sA = base;
     uint8_t* sB = sA + kDigits * aPlane;
-    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (warp == 0) tc::alloc(&tmem_slot, tcols);
     if (tid == 0) tc::mbar_init(&mbar, 1);
     {
-        const uint4* src = reinterpret_cast<const uint4*>(xd + (long)b * kDigits * 64 * 64);
+        const uint4* src = reinterpret_cast<const uint4*>(xd + (long)b * kDigits * kXdStride);
         uint4* dst = reinterpret_cast<uint4*>(sB);
         for (int t = tid; t < kDigits * bPlane / 16; t += 256) dst[t] = src[t];
-        if (tid < 64) {
-            sXe[tid] = tid < Np ? xe[b * 64 + tid] : 0;
+        if (tid < kMeshTcMax) {
+            sXe[tid] = tid < Np ? xe[b * kMeshTcMax + tid] : 0;
             sIdx[tid] = tid < nb ? in_list[s0 + tid] : 0;
             sOut[tid] = tid < nb ? (out_list ? out_list[s0 + tid] : out_base[b] + tid) : 0;
         }
     }
     __syncthreads();
-    // the point's values psi_k(p) for this thread's K groups
-    double v[24];
+    if (kg <= 6) {
+        // the point's values psi_k(p) for this thread's K groups
+        double v[24];
 #pragma unroll
-    for (int u = 0; u < 24; ++u) {
-        const int k = 8 * (half + 2 * (u >> 3)) + (u & 7);
-        v[u] = (live && k < nb) ? in[(long)sIdx[k] * V4 + p] : 0.0;
-    }
-    int emax = 0;
-#pragma unroll
-    for (int u = 0; u < 24; ++u) emax = max(emax, oz::bexp(v[u]));
-    sEmax[tid] = emax;
-    __syncthreads();
-    emax = max(sEmax[row], sEmax[row + kRows]);
-#pragma unroll
-    for (int gg = 0; gg < 3; ++gg) {
-        const int g = half + 2 * gg;
-        if (g >= kg) continue;
-        uint4 w[kDigits];
-        if (8 * g < nb) {
-            double v8[8];
-#pragma unroll
-            for (int h = 0; h < 8; ++h) v8[h] = v[8 * gg + h];
-            oz::digits8(v8, emax, w);
-        } else {
-#pragma unroll
-            for (int a = 0; a < kDigits; ++a) w[a] = make_uint4(0u, 0u, 0u, 0u);
+        for (int u = 0; u < 24; ++u) {
+            const int k = 8 * (half + 2 * (u >> 3)) + (u & 7);
+            v[u] = (live && k < nb) ? in[(long)sIdx[k] * V4 + p] : 0.0;
         }
+        int emax = 0;
 #pragma unroll
-        for (int a = 0; a < kDigits; ++a)
-            *reinterpret_cast<uint4*>(sA + a * aPlane + tc::kmajor_off_g(row, 8 * g, kg)) = w[a];
+        for (int u = 0; u < 24; ++u) emax = max(emax, oz::bexp(v[u]));
+        sEmax[tid] = emax;
+        __syncthreads();
+        emax = max(sEmax[row], sEmax[row + kRows]);
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg) {
+            const int g = half + 2 * gg;
+            if (g >= kg) continue;
+            uint4 w[kDigits];
+            if (8 * g < nb) {
+                double v8[8];
+#pragma unroll
+                for (int h = 0; h < 8; ++h) v8[h] = v[8 * gg + h];
+                oz::digits8(v8, emax, w);
+            } else {
+#pragma unroll
+                for (int a = 0; a < kDigits; ++a) w[a] = make_uint4(0u, 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (int a = 0; a < kDigits; ++a)
+                *reinterpret_cast<uint4*>(sA + a * aPlane + tc::kmajor_off_g(row, 8 * g, kg)) = w[a];
+        }
+    } else {
+        // blocks of 49 to kMeshTcMax spinors: the exponent pass, then the
+        // digits pass over the same values
+        int emax = 0;
+        for (int g = half; g < kg; g += 2)
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                const int k = 8 * g + h;
+                if (live && k < nb) emax = max(emax, oz::bexp(in[(long)sIdx[k] * V4 + p]));
+            }
+        sEmax[tid] = emax;
+        __syncthreads();
+        emax = max(sEmax[row], sEmax[row + kRows]);
+        for (int g = half; g < kg; g += 2) {
+            uint4 w[kDigits];
+            if (8 * g < nb) {
+                double v8[8];
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int k = 8 * g + h;
+                    v8[h] = (live && k < nb) ? in[(long)sIdx[k] * V4 + p] : 0.0;
+                }
+                oz::digits8(v8, emax, w);
+            } else {
+#pragma unroll
+                for (int a = 0; a < kDigits; ++a) w[a] = make_uint4(0u, 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (int a = 0; a < kDigits; ++a)
+                *reinterpret_cast<uint4*>(sA + a * aPlane + tc::kmajor_off_g(row, 8 * g, kg)) = w[a];
+        }
     }
     tc::fence_proxy_async();
     tc::fence_before();
@@ -299,8 +353,10 @@ k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
             oz::issue_pairs<2>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
         else if (kg == 6)
             oz::issue_pairs<3>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
-        else
+        else if (kg == 8)
             oz::issue_pairs<4>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
+        else
+            oz::issue_pairs<5>(tmem, Np, idesc, aB, aPlane, sbo, bB, bPlane, sbo, false);
         tc::commit(&mbar);
     }
     bool ok = tc::mbar_wait(&mbar, 0, kWaitCycles);
@@ -351,7 +407,7 @@ k_apply_tc(const double* in, double* out, double* __restrict__ upd, BlockIdx bi,
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::dealloc(tmem, tcols);
 }
 
 // Pairing gaps, HFBGaps (src/HFB.f90:520-632), per block b (isospin b / 2):
@@ -373,15 +429,16 @@ k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
-    __shared__ int sE[64], sEz[64], sFe[kGapPts];
+    __shared__ int sE[kRows], sEz[kRows], sFe[kGapPts];
     __shared__ float4 sF[kGapPts];   // (Fr hi, Fr lo, Fi hi, Fi lo)
     const int b = blockIdx.y, it = b >> 1, chunk = blockIdx.x;
     const int h = hsz[b];
     if (h == 0) return;
     const int N = max(16, (h + 15) / 16 * 16);
+    const uint32_t tcols = tmem_cols(N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int row = tid >> 2, c = tid & 3;
-    const bool live = row < h;
+    // rows row0 and row0 + 64 (blocks above 64 spinors), component c
+    const int row0 = tid >> 2, c = tid & 3;
     const int bPlane = N * tc::kRowBytes;
 
     const uint32_t s0a = tc::smem_u32(smraw);
@@ -390,7 +447,7 @@ k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
     uint8_t* sB = sA + kDigits * kStagePlane;    // kDigits planes of N x 32
     for (int t = tid; t < (kDigits * kStagePlane + kDigits * bPlane) / 16; t += 256)
         reinterpret_cast<uint4*>(base)[t] = make_uint4(0u, 0u, 0u, 0u);
-    if (warp == 0) tc::alloc(&tmem_slot, kTmemCols);
+    if (warp == 0) tc::alloc(&tmem_slot, tcols);
     if (tid == 0) tc::mbar_init(&mbar, 1);
     const long p0 = (long)chunk * kGapPts;
     const int npts = (int)min((long)kGapPts, V - p0);
@@ -406,21 +463,31 @@ k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
         sFe[tid] = max(oz::bexp(fr), oz::bexp(fi));
     }
     const int pc = c ^ 1;   // the partner component of Z
-    const double* src = live ? psi + ((long)members[b * hmax + row] * 4 + c) * V + p0 : psi;
-    const double* srp = live ? psi + ((long)members[b * hmax + row] * 4 + pc) * V + p0 : psi;
-    int emax = 0;
-    if (live)
-        for (int q = 0; q < npts; ++q) emax = max(emax, oz::bexp(src[q]));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    bool live[2];
+    const double *src[2], *srp[2];
+    int emax[2] = {0, 0}, ez[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int row = row0 + 64 * r;
+        live[r] = row < h;
+        src[r] = live[r] ? psi + ((long)members[b * hmax + row] * 4 + c) * V + p0 : psi;
+        srp[r] = live[r] ? psi + ((long)members[b * hmax + row] * 4 + pc) * V + p0 : psi;
+        if (live[r])
+            for (int q = 0; q < npts; ++q) emax[r] = max(emax[r], oz::bexp(src[r][q]));
+        emax[r] = max(emax[r], __shfl_xor_sync(0xffffffffu, emax[r], 1));
+        emax[r] = max(emax[r], __shfl_xor_sync(0xffffffffu, emax[r], 2));
+    }
     __syncthreads();
     int efmax = 0;
     for (int q = 0; q < kGapPts; ++q) efmax = max(efmax, sFe[q]);
-    // |Z| <= |F| (|psi_c| + |psi_c'|) < 2^(E_F + E_psi + 3)
-    const int ez = (emax == 0 || efmax == 0) ? 0 : emax + efmax - 1023 + 2;
-    if (live && c == 0) {
-        sE[row] = emax;
-        sEz[row] = ez;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        // |Z| <= |F| (|psi_c| + |psi_c'|) < 2^(E_F + E_psi + 3)
+        ez[r] = (emax[r] == 0 || efmax == 0) ? 0 : emax[r] + efmax - 1023 + 2;
+        if (live[r] && c == 0) {
+            sE[row0 + 64 * r] = emax[r];
+            sEz[row0 + 64 * r] = ez[r];
+        }
     }
     tc::fence_before();
     __syncthreads();
@@ -431,25 +498,28 @@ k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
     const int nst = kGapPts / 8;
     for (int s = 0; s < nst; ++s) {
         if (s > 0) ok &= tc::mbar_wait(&mbar, (s - 1) & 1, kWaitCycles);
-        if (live) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!live[r]) continue;
+            const int row = row0 + 64 * r;
             double a[8];
             long long zx[8];
 #pragma unroll
             for (int hh = 0; hh < 8; ++hh) {
                 const int q = 8 * s + hh;
                 const bool in = q < npts;
-                a[hh] = in ? src[q] : 0.0;
-                const double ap = in ? srp[q] : 0.0;
+                a[hh] = in ? src[r][q] : 0.0;
+                const double ap = in ? srp[r][q] : 0.0;
                 const float4 f = sF[q];
                 const dfl fr = {f.x, f.y}, fi = {f.z, f.w};
                 const dfl ac = df_split(a[hh]), ao = df_split(ap);
                 // c even: Z = -Fr a_c + Fi a_c' ; c odd: Z = -Fi a_c' - Fr a_c
                 const dfl t1 = df_mul(fr, ac), t2 = df_mul(fi, ao);
                 const dfl z = (c & 1) ? df_neg(df_add(t1, t2)) : df_sub(t2, t1);
-                zx[hh] = ez ? oz::fixed_f(z.h, ez) + oz::fixed_f(z.l, ez) : 0ll;
+                zx[hh] = ez[r] ? oz::fixed_f(z.h, ez[r]) + oz::fixed_f(z.l, ez[r]) : 0ll;
             }
             uint4 w[kDigits];
-            oz::digits8(a, emax, w);
+            oz::digits8(a, emax[r], w);
 #pragma unroll
             for (int d = 0; d < kDigits; ++d)
                 *reinterpret_cast<uint4*>(sA + d * kStagePlane + tc::kmajor_off(row, 8 * c)) = w[d];
@@ -509,7 +579,7 @@ k_gaps_tc(const double* __restrict__ psi, const int* __restrict__ members,
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::dealloc(tmem, tcols);
 }
 
 // Chunk partials of the gaps summed per entry, one warp each (fixed order):
@@ -578,18 +648,18 @@ k_field_contract(const double* __restrict__ Y, const double* __restrict__ psi,
 }  // namespace
 
 // Buffers and attributes of the tensor-core Gram-Schmidt (blocks of at most
-// 64 spinors).  Returns false when the blocks are larger.
+// kMeshTcMax spinors).  Returns false when the blocks are larger.
 bool gs_tc_prepare(mg_ctx* c) {
-    if (!c->tc_ok || c->gs_nbmax > 64) return false;
+    if (!c->tc_mesh_ok || c->gs_nbmax > kMeshTcMax) return false;
     if (c->gs_xd == nullptr) {
         const int nblk = c->gs_nblk;
         c->gs_nchunk_tc = div_up(4 * c->V, kChunk);
         if (cudaMalloc(&c->gs_Stc, (size_t)nblk * c->gs_nchunk_tc * c->gs_nbmax * c->gs_nbmax *
                                        sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&c->gs_xd, (size_t)nblk * kDigits * 64 * 64 * sizeof(uint16_t)) !=
+            cudaMalloc(&c->gs_xd, (size_t)nblk * kDigits * kXdStride * sizeof(uint16_t)) !=
                 cudaSuccess ||
-            cudaMalloc(&c->gs_xe, (size_t)nblk * 64 * sizeof(int)) != cudaSuccess ||
-            cudaMemset(c->gs_xd, 0, (size_t)nblk * kDigits * 64 * 64 * sizeof(uint16_t)) !=
+            cudaMalloc(&c->gs_xe, (size_t)nblk * kMeshTcMax * sizeof(int)) != cudaSuccess ||
+            cudaMemset(c->gs_xd, 0, (size_t)nblk * kDigits * kXdStride * sizeof(uint16_t)) !=
                 cudaSuccess)
             return false;
         cudaFuncSetAttribute(k_gs_overlap_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -601,7 +671,9 @@ bool gs_tc_prepare(mg_ctx* c) {
 }
 
 int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d_ordered) {
-    const size_t sm = 128 + 2 * (size_t)kDigits * kStagePlane;
+    size_t sm = 128 + 2 * (size_t)kDigits * kStagePlane;
+    const int N = std::max(16, (c->gs_nbmax + 15) / 16 * 16);
+    if (tmem_cols(N) > 256) sm = std::max(sm, kOneCtaSmem);
     k_gs_overlap_tc<<<dim3(c->gs_nchunk_tc, c->gs_nblk), 256, sm, c->stream>>>(
         psi, d_lists, d_ordered, c->gs_nbmax, 4 * c->V, c->gs_nchunk_tc, c->gs_Stc,
         c->tc_status);
@@ -612,11 +684,12 @@ int gs_overlap_tc(mg_ctx* c, const double* psi, const int* d_lists, const int* d
 static int apply_tc(mg_ctx* c, int nblk, int nbmax, const double* coef, long bstride, int ld,
                     BlockIdx bi, const double* in, double* out, double* upd, const int* in_list,
                     const int* out_list, const int* out_base, uint16_t* xd, int* xe) {
-    k_coef_digits<<<nblk, 64, 0, c->stream>>>(coef, bstride, ld, bi, xd, xe);
+    k_coef_digits<<<nblk, 96, 0, c->stream>>>(coef, bstride, ld, bi, xd, xe);
     MG_LAUNCHED(c);
     const int Np = std::max(16, (nbmax + 15) / 16 * 16);
     size_t sm = 128 + (size_t)kDigits * (kRows * Np * 2 + Np * Np * 2);
-    sm = std::max(sm, (size_t)80 * 1024);   // two CTAs per SM: 2 x 256 TMEM columns
+    // at most two CTAs per SM (2 x 256 TMEM columns), one above N = 64
+    sm = std::max(sm, tmem_cols(Np) > 256 ? kOneCtaSmem : (size_t)80 * 1024);
     const long V4 = 4 * c->V;
     k_apply_tc<<<dim3(div_up(V4, kRows), nblk), 256, sm, c->stream>>>(
         in, out, upd, bi, in_list, out_list, out_base, xd, xe, V4, c->tc_status);
@@ -631,15 +704,15 @@ int gs_apply_tc(mg_ctx* c, double* psi, double* upd, const int* d_lists, const i
                     c->gs_xe);
 }
 
-// Canonical basis of the four pairing blocks (hsz[b] <= 64): CanTransfo is
-// stored densely per block (ld = h) at b * hmax^2.
+// Canonical basis of the four pairing blocks (hsz[b] <= kMeshTcMax):
+// CanTransfo is stored densely per block (ld = h) at b * hmax^2.
 int can_transform_tc(mg_ctx* c) {
     Hfb& H = c->hfb;
-    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    if (!c->tc_mesh_ok || H.hmax > kMeshTcMax) return MG_ERR_STATE;
     if (c->can_xd == nullptr) {
-        MG_CUDA(cudaMalloc(&c->can_xd, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
-        MG_CUDA(cudaMemset(c->can_xd, 0, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
-        MG_CUDA(cudaMalloc(&c->can_xe, (size_t)4 * 64 * sizeof(int)));
+        MG_CUDA(cudaMalloc(&c->can_xd, (size_t)4 * kDigits * kXdStride * sizeof(uint16_t)));
+        MG_CUDA(cudaMemset(c->can_xd, 0, (size_t)4 * kDigits * kXdStride * sizeof(uint16_t)));
+        MG_CUDA(cudaMalloc(&c->can_xe, (size_t)4 * kMeshTcMax * sizeof(int)));
         MG_CUDA(cudaFuncSetAttribute(k_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      200 * 1024));
     }
@@ -653,7 +726,7 @@ int can_transform_tc(mg_ctx* c) {
 // gsum[b][i * h + j] (to be finished by k_gaps_finish with one chunk).
 int gaps_tc(mg_ctx* c, double* gsum) {
     Hfb& H = c->hfb;
-    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    if (!c->tc_mesh_ok || H.hmax > kMeshTcMax) return MG_ERR_STATE;
     const long V = c->V;
     const int nchunk = div_up(V, kGapPts);
     if (c->gap_part == nullptr) {
@@ -663,7 +736,8 @@ int gaps_tc(mg_ctx* c, double* gsum) {
     }
     const int Np = std::max(16, (H.hmax + 15) / 16 * 16);
     size_t sm = 128 + (size_t)kDigits * kStagePlane + (size_t)kDigits * Np * tc::kRowBytes;
-    sm = std::max(sm, (size_t)80 * 1024);   // two CTAs per SM: 2 x 256 TMEM columns
+    // two CTAs per SM (2 x 256 TMEM columns), one above N = 64
+    sm = std::max(sm, tmem_cols(Np) > 256 ? kOneCtaSmem : (size_t)80 * 1024);
     k_gaps_tc<<<dim3(nchunk, 4), 256, sm, c->stream>>>(c->bas[MG_HF_BASIS].psi, H.members, H.hsz,
                                                       H.hmax, H.fre, H.fim, V, nchunk, c->gap_part,
                                                       c->tc_status);
@@ -678,13 +752,13 @@ int gaps_tc(mg_ctx* c, double* gsum) {
 // (tensor cores) into the scratch basis, then the pointwise contraction.
 int pair_field_tc(mg_ctx* c) {
     Hfb& H = c->hfb;
-    if (!c->tc_ok || H.hmax > 64) return MG_ERR_STATE;
+    if (!c->tc_mesh_ok || H.hmax > kMeshTcMax) return MG_ERR_STATE;
     const long V = c->V;
     if (c->field_y == nullptr) {
         MG_CUDA(cudaMalloc(&c->field_y, (size_t)4 * H.hmax * 4 * V * sizeof(double)));
-        MG_CUDA(cudaMalloc(&c->field_xd, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
-        MG_CUDA(cudaMemset(c->field_xd, 0, (size_t)4 * kDigits * 64 * 64 * sizeof(uint16_t)));
-        MG_CUDA(cudaMalloc(&c->field_xe, (size_t)4 * 64 * sizeof(int)));
+        MG_CUDA(cudaMalloc(&c->field_xd, (size_t)4 * kDigits * kXdStride * sizeof(uint16_t)));
+        MG_CUDA(cudaMemset(c->field_xd, 0, (size_t)4 * kDigits * kXdStride * sizeof(uint16_t)));
+        MG_CUDA(cudaMalloc(&c->field_xe, (size_t)4 * kMeshTcMax * sizeof(int)));
         MG_CUDA(cudaMalloc(&c->field_ybase, 4 * sizeof(int)));
         const int yb[4] = {0, H.hmax, 2 * H.hmax, 3 * H.hmax};
         MG_CUDA(cudaMemcpy(c->field_ybase, yb, sizeof(yb), cudaMemcpyHostToDevice));

@@ -36,6 +36,7 @@ namespace mg {
 
 constexpr int kMaxN = 64;       // largest supported stored line length
 constexpr int kNumMoments = 64; // capacity of the multipole table
+constexpr int kMeshTcMax = 80;  // largest spwf block of the tensor-core mesh GEMMs (meshgemm_tc.cu)
 constexpr int kEigMax = 160;    // largest matrix of the batched eigensolver (HFB block N = 2h)
 
 // One derivative job: a real grid and where its derivatives go.  slot[d] is
@@ -221,6 +222,7 @@ struct mg_ctx {
     long tc_off[3][2];
     int tc_N[3] = {0, 0, 0};
     bool tc_ok = false;           // every line length <= 32
+    bool tc_mesh_ok = false;      // mesh-sized GEMMs on the tensor cores (blocks <= kMeshTcMax)
     // largest grid of the persistent tensor-core derivative kernel (0: one CTA
     // per SM); set while it runs beside other work on the side stream
     int tc_grid_cap = 0;

@@ -415,7 +415,7 @@ int pairing_mesh(mg_ctx* c) {
     MG_LAUNCHED(c);
     const size_t sm_f = (size_t)(hmax * hmax + hmax * 4 * kPts + 2 * kThreads) * sizeof(double);
     const bool mixed = c->cur_precision == MG_MIXED;
-    if (mixed && c->tc_ok && hmax <= 64)
+    if (mixed && c->tc_mesh_ok && hmax <= kMeshTcMax)
         MG_TRY(pair_field_tc(c));   // tensor cores (meshgemm_tc.cu)
     else if (mixed)
         k_pair_field_df<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
@@ -423,12 +423,12 @@ int pairing_mesh(mg_ctx* c) {
     else
         k_pair_field<<<dim3(div_up(V, kPts), 4), kThreads, sm_f, c->stream>>>(
             B.psi, H.members, H.hsz, hmax, H.ktil, V, H.fpart);
-    if (!(mixed && c->tc_ok && hmax <= 64)) MG_LAUNCHED(c);
+    if (!(mixed && c->tc_mesh_ok && hmax <= kMeshTcMax)) MG_LAUNCHED(c);
     k_pair_field_finish<<<div_up(2 * V, kThreads), kThreads, 0, c->stream>>>(H.fpart, H.dfac, V,
                                                                            H.fre, H.fim);
     MG_LAUNCHED(c);
     const size_t sm_g = (size_t)(2 * hmax * (4 * kGPts + 1) + hmax * hmax) * sizeof(double);
-    if (mixed && c->tc_ok && hmax <= 64) {
+    if (mixed && c->tc_mesh_ok && hmax <= kMeshTcMax) {
         // tensor cores (meshgemm_tc.cu): the summed partials go to chunk slot 0
         MG_TRY(gaps_tc(c, H.gpart));
         k_gaps_finish<<<dim3(div_up(nmax * nmax, 128), 4), 128, 0, c->stream>>>(
@@ -453,7 +453,7 @@ int canonical_transform(mg_ctx* c) {
     Hfb& H = c->hfb;
     const long V4 = 4 * c->V;
     const size_t sm = (size_t)(H.hmax * H.hmax + H.hmax * kPts) * sizeof(double);
-    if (c->cur_precision == MG_MIXED && c->tc_ok && H.hmax <= 64)
+    if (c->cur_precision == MG_MIXED && c->tc_mesh_ok && H.hmax <= kMeshTcMax)
         return can_transform_tc(c);   // tensor cores (meshgemm_tc.cu)
     if (c->cur_precision == MG_MIXED)
         k_can_transform_df<<<dim3(div_up(V4, kPts), 4), kThreads, sm, c->stream>>>(

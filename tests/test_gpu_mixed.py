@@ -192,11 +192,13 @@ def test_mixed_iterations_with_fp64_polish(built):
     mix.close()
 
 
-@pytest.mark.parametrize("n,nwt", [(10, 40), (24, 160)])
+@pytest.mark.parametrize("n,nwt", [(10, 40), (24, 160), (10, 224), (10, 300)])
 def test_mixed_gram_schmidt(built, n, nwt):
     """Tensor-core Gram-Schmidt (overlap and apply as exact digit products)
     against the FP64 oracle: 1e-11 relative on the spinors, orthonormal to
-    5e-12 within each (isospin, parity) block.  The apply rounds each point's
+    5e-12 within each (isospin, parity) block.  Block sizes 34/46 (nwt=160),
+    62/50 (224: K groups 7 and 8 of the apply) and 70/80 (300: 512 TMEM
+    columns, one CTA per SM).  The apply rounds each point's
     spinor values to 47 bits of the point's largest one and this basis is far
     from orthonormal (2% noise), so R^-1 amplifies that rounding a little."""
     p = RunParams(nx=n, ny=n, nz=n, dx=0.8, nwt=nwt, neutrons=nwt // 4, protons=nwt // 4,
@@ -220,3 +222,43 @@ def test_mixed_gram_schmidt(built, n, nwt):
     same = (qn[:, None, 0] == qn[None, :, 0]) & (qn[:, None, 1] == qn[None, :, 1])
     assert np.abs(S[same] - np.eye(p.nwt)[same]).max() < 5e-12
     g.close()
+
+
+@pytest.mark.parametrize("nwt,nz", [(224, 60), (300, 66)])
+def test_mixed_hfb_large_blocks(built, nwt, nz):
+    """Pairing field, gaps and canonical-basis transform on the tensor cores
+    for HFB blocks of 50-62 (nwt=224) and 70-80 spinors (nwt=300), against the
+    FP64 GPU path from the same start (the FP64 path is held to the oracle by
+    the parity tests; both run the same Newton Fermi search): pairing field
+    within 1e-10 of its scale, rho and tau within 1e-10, div J within 5e-10,
+    pairing energies within 1e-8 MeV.  N = Z = nz keeps the pairing alive on this start (pairing energies of
+    -18 and -31 MeV; at N = Z = nwt / 4 it collapses and the field is zero)."""
+    out = {}
+    for prec in (MG_FP64, MG_MIXED):
+        p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=nwt, neutrons=nz, protons=nz,
+                      pairing=_abi.MG_PAIRING_HFB, precision=prec)
+        psi, qn, en = synthetic.ho_basis(p, nwt // 2, seed=1234)
+        g = MeshState(p, SLY4)
+        g.set_spinors(psi, qn)
+        g.set_energies(en)
+        g.set_pairing()
+        info = g.SolvePairing()
+        assert info["converged"]
+        field = g.get_pairing_field()
+        g.DeriveAll()
+        g.UpdateDensities()
+        out[prec] = (info, field, g.get_densities())
+        g.close()
+    (i64, f64, d64), (imx, fmx, dmx) = out[MG_FP64], out[MG_MIXED]
+    # real and imaginary parts against the field's scale (the imaginary part
+    # vanishes with time reversal up to rounding), the density factor relative
+    scale = np.abs(f64[0]).max()
+    for k in (0, 1):
+        assert np.abs(fmx[k] - f64[k]).max() < 1e-10 * scale, k
+    assert rel(fmx[2], f64[2]) < 1e-12
+    for it in range(2):
+        assert abs(imx["pairing_energy"][it] - i64["pairing_energy"][it]) < 1e-8
+    # rho and tau within 1e-10; div J, a difference of derivative products
+    # summed over the canonical states, measured 1.8e-10 at nwt=224
+    for k, bar in (("rho", 1e-10), ("tau", 1e-10), ("nablaj", 5e-10)):
+        assert rel(dmx[k], d64[k]) < bar, k
