@@ -137,7 +137,9 @@ struct Hfb {
     double qp_gap[2] = {0.0, 0.0};             // per isospin: smallest 2 min E of its blocks
     double fermi[2] = {-10.0, -10.0};
     double fermi_prev[2] = {-10.0, -10.0};     // Fermi energies of the solve before
-    double fermi_old[2][2] = {{0, 0}, {0, 0}}; // the two before that ([0] newer)
+    double fermi_old[4][2] = {};               // the four before that ([0] newer)
+    double npp[2] = {0.0, 0.0};                // |d2N/dlambda2| from the last two-evaluation search
+    int npp_iter = -1000;                      // its iteration
     int n_solved = 0;                          // consecutive converged solves
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
