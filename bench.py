@@ -59,9 +59,10 @@ PREPARE = 100
 METRIC = "HFB iter/s at 24^3, nwt=160: mixed vs FP64 GPU at |dE|<=1e-5 MeV"
 # DRAM traffic of one mixed DeriveBasis (the three k_deriv_tc passes, nwt=160,
 # 24^3) from ncu dram__bytes_read.sum + dram__bytes_write.sum, and the tensor
-# pipe's active share over those launches (profiles/deriv_tc_24c_nwt160_full.md)
-DERIV_TC_TRAFFIC = 612.7e6
-DERIV_TC_TENSOR_ACTIVE = 0.069
+# pipe's active share over those launches, weighted by their durations
+# (profiles/deriv_tc_24c_nwt160_full.md)
+DERIV_TC_TRAFFIC = 610.3e6
+DERIV_TC_TENSOR_ACTIVE = 0.103
 
 
 def _params(precision):
