@@ -67,6 +67,7 @@ struct TcPass {
 struct TcShared {
     uint64_t fullA[2], emptyA[2], fullT[2], emptyT[2];
     uint64_t emaxReady[4];   // tile k's line exponents written (128 slicer arrivals)
+    uint64_t staged;         // x pass: every slicer's copies of the tile landed (128 arrivals)
     uint32_t tmem;
     // line exponents of the last four tiles: the slicers write tile k's while
     // the epilogue may still read tile k-2's (slicer k waits for MMA k-2,
@@ -121,6 +122,7 @@ k_deriv_tc(TcPass P) {
             tc::mbar_init(&S.emptyT[b], kEpi);
         }
         for (int b = 0; b < 4; ++b) tc::mbar_init(&S.emaxReady[b], kSlicers);
+        tc::mbar_init(&S.staged, kSlicers);
     }
     for (int s = 0; s < 2; ++s) {
         const uint4* src = reinterpret_cast<const uint4*>(P.bmat[s]);
@@ -138,10 +140,27 @@ k_deriv_tc(TcPass P) {
     if (warp < 4) {
         // ---------------- slicers ----------------
         const int r = tid;
+        // x pass: a tile's lines are one contiguous block, staged by all
+        // slicers with consecutive elements on consecutive lanes (element e
+        // is point e mod n of line e / n; (e * ceil(2^18 / n)) >> 18 = e / n
+        // exactly for n <= 32, e < 128 n); y and z passes: one line per
+        // thread, consecutive lines on consecutive lanes
+        const uint32_t magic = ((1u << 18) + (uint32_t)n - 1u) / (uint32_t)n;
         auto prefetch = [&](int T, int sbuf) {
-            const int job = T / P.tpj, l = (T % P.tpj) * kTile + r;
-            if (l >= P.nlines) return;
+            const int job = T / P.tpj, l0 = (T % P.tpj) * kTile;
             const double* in = P.jobs[job].in;
+            if (P.axis == 0) {
+                const int tot = min(kTile, P.nlines - l0) * n;
+                const double* blk = in + (long)l0 * n;
+                double* dst = sIn + (long)sbuf * kTile * (n + 1);
+                for (int e = r; e < tot; e += kSlicers) {
+                    const int line = (int)(((uint32_t)e * magic) >> 18);
+                    tc::cp_async8(dst + line * (n + 1) + (e - line * n), blk + e);
+                }
+                return;
+            }
+            const int l = l0 + r;
+            if (l >= P.nlines) return;
             long off, stride;
             line_geom(P, l, off, stride);
             double* dst = sIn + ((long)sbuf * kTile + r) * (n + 1);
@@ -153,6 +172,14 @@ k_deriv_tc(TcPass P) {
         for (int k = 0; T < P.ntiles; T += gridDim.x, ++k) {
             const int buf = k & 1;
             tc::cp_async_wait_all();
+            if (P.axis == 0) {
+                // the tile's lines come from every slicer's copies; passing this
+                // also means every slicer has finished the tile before, whose
+                // staging buffer the prefetch below reuses
+                tc::mbar_arrive(&S.staged);
+                ok &= tc::mbar_wait(&S.staged, k & 1, kWaitCycles);
+                if (!ok) break;
+            }
             const int Tn = T + gridDim.x;
             const bool live = (T % P.tpj) * kTile + r < P.nlines;
             const double* src = sIn + ((long)buf * kTile + r) * (n + 1);
