@@ -46,18 +46,26 @@ namespace {
 
 using oz::kDigits;
 constexpr int kTile = 128;                      // lines per tile (MMA M)
-constexpr int kKp = 32;                         // padded K
-constexpr int kPlane = kTile * kKp * 2;         // bytes of one digit plane of a tile
+// Two forms: KP = 32 (lines up to 32) with two plane buffers, two staging
+// buffers and two TMEM accumulator sets; KP = 48 (lines of 33 to kLongMax)
+// with one of each (N up to 80: four accumulators take 320 TMEM columns and
+// the planes of both parity slots ~92 KB of shared memory).  With one buffer
+// the slicers still work on tile k + 1 while the epilogue reads tile k; the
+// MMAs of tile k + 1 wait for that epilogue, and the next tile's lines are
+// fetched once the current ones are sliced.
+constexpr int kShortK = 32;
+constexpr int kLongK = 48;
+constexpr int kLongMax = 40;
 constexpr int kSlicers = 128;                   // warps 0-3
 constexpr int kMmaWarp = 4;
 constexpr int kEpi = 512;                       // warps 5-20
 constexpr int kThreads = kSlicers + 32 + kEpi;  // 672
-constexpr uint32_t kTmemCols = 512;             // 2 sets x 4 accumulators x N (N <= 64)
+constexpr uint32_t kTmemCols = 512;             // 2 sets x 4 x N (N <= 64) or 1 set x 4 x N (N <= 80)
 constexpr long long kWaitCycles = 4000000000LL; // ~2 s at the top SM clock
 
 struct TcPass {
     const GridJob* jobs;
-    const uint16_t* bmat[2];   // per slot: kDigits planes, N rows x 32, K-major core matrices
+    const uint16_t* bmat[2];   // per slot: kDigits planes, N rows x KP, K-major core matrices
     const int* erow[2];        // per slot: N row exponents
     int axis, n, N, nlines, tpj, ntiles, nx, ny;
     int lap_stage;             // y/z passes: Laplacian values staged in shared memory
@@ -73,7 +81,7 @@ struct TcShared {
     // the epilogue may still read tile k-2's (slicer k waits for MMA k-2,
     // which waited for epilogue k-4)
     int emax[4][kTile];
-    float srow[2][64];
+    float srow[2][96];
 };
 
 // global offset of element k of line l of a grid (axis order: x, y, z)
@@ -98,8 +106,12 @@ __device__ __forceinline__ double* out_of(const GridJob& J, int axis) {
     return axis == 0 ? J.dx : (axis == 1 ? J.dy : J.dz);
 }
 
+template <int KP, int NBUF>
 __global__ void __launch_bounds__(kThreads, 1)
 k_deriv_tc(TcPass P) {
+    constexpr int kPlane = kTile * KP * 2;     // bytes of one digit plane of a tile
+    constexpr int kKg = KP / 8;                // K groups of 8
+    constexpr uint32_t kSboK = 128u * kKg;     // stride byte offset of the planes
     extern __shared__ uint8_t smraw[];
     __shared__ TcShared S;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -107,11 +119,11 @@ k_deriv_tc(TcPass P) {
 
     const uint32_t s0 = tc::smem_u32(smraw);
     uint8_t* base = smraw + ((128u - (s0 & 127u)) & 127u);
-    uint8_t* sA = base;                                         // 2 x kDigits planes
-    uint8_t* sB = sA + 2 * kDigits * kPlane;                    // 2 slots x kDigits x N x 32
-    const int bBytes = kDigits * N * tc::kRowBytes;
-    double* sIn = reinterpret_cast<double*>(sB + 2 * bBytes);   // 2 x 128 x (n + 1)
-    float2* sLap = reinterpret_cast<float2*>(sIn + 2 * kTile * (n + 1));   // 128 x (n + 1)
+    uint8_t* sA = base;                                         // NBUF x kDigits planes
+    uint8_t* sB = sA + NBUF * kDigits * kPlane;                 // 2 slots x kDigits x N x KP
+    const int bBytes = kDigits * N * KP * 2;
+    double* sIn = reinterpret_cast<double*>(sB + 2 * bBytes);   // NBUF x 128 x (n + 1)
+    float2* sLap = reinterpret_cast<float2*>(sIn + NBUF * kTile * (n + 1));   // 128 x (n + 1)
 
     if (warp == 0) tc::alloc(&S.tmem, kTmemCols);
     if (tid == 0) {
@@ -149,7 +161,9 @@ k_deriv_tc(TcPass P) {
         auto prefetch = [&](int T, int sbuf) {
             const int job = T / P.tpj, l0 = (T % P.tpj) * kTile;
             const double* in = P.jobs[job].in;
-            if (P.axis == 0) {
+            // (with one staging buffer the next tile's lines are fetched while
+            // other slicers may still read the current ones: own line only)
+            if (NBUF == 2 && P.axis == 0) {
                 const int tot = min(kTile, P.nlines - l0) * n;
                 const double* blk = in + (long)l0 * n;
                 double* dst = sIn + (long)sbuf * kTile * (n + 1);
@@ -170,9 +184,9 @@ k_deriv_tc(TcPass P) {
         if (T < P.ntiles) prefetch(T, 0);
         tc::cp_async_commit();
         for (int k = 0; T < P.ntiles; T += gridDim.x, ++k) {
-            const int buf = k & 1;
+            const int buf = k % NBUF;
             tc::cp_async_wait_all();
-            if (P.axis == 0) {
+            if (NBUF == 2 && P.axis == 0) {
                 // the tile's lines come from every slicer's copies; passing this
                 // also means every slicer has finished the tile before, whose
                 // staging buffer the prefetch below reuses
@@ -187,17 +201,17 @@ k_deriv_tc(TcPass P) {
             if (live)
                 for (int q = 0; q < n; ++q) emax = max(emax, oz::bexp(src[q]));
             // the staging row of the other buffer was read in the iteration before
-            if (Tn < P.ntiles) prefetch(Tn, buf ^ 1);
+            if (NBUF == 2 && Tn < P.ntiles) prefetch(Tn, buf ^ 1);
             tc::cp_async_commit();
-            if (k >= 2) {
-                ok &= tc::mbar_wait(&S.emptyA[buf], ((k - 2) >> 1) & 1, kWaitCycles);
+            if (k >= NBUF) {
+                ok &= tc::mbar_wait(&S.emptyA[buf], ((k - NBUF) / NBUF) & 1, kWaitCycles);
                 if (!ok) break;
             }
             S.emax[k & 3][r] = emax;
             tc::mbar_arrive(&S.emaxReady[k & 3]);
             uint8_t* planes = sA + buf * kDigits * kPlane;
 #pragma unroll 1
-            for (int g = 0; g < kKp / 8; ++g) {
+            for (int g = 0; g < kKg; ++g) {
                 uint4 w[kDigits];
                 if (8 * g < n) {
                     double v8[8];
@@ -211,11 +225,17 @@ k_deriv_tc(TcPass P) {
                 }
 #pragma unroll
                 for (int a = 0; a < kDigits; ++a)
-                    *reinterpret_cast<uint4*>(planes + a * kPlane + tc::kmajor_off(r, 8 * g)) =
+                    *reinterpret_cast<uint4*>(planes + a * kPlane + tc::kmajor_off_g(r, 8 * g, kKg)) =
                         w[a];
             }
             tc::fence_proxy_async();
             tc::mbar_arrive(&S.fullA[buf]);
+            // one staging buffer: this thread's line of the next tile, once its
+            // line of this tile has been sliced
+            if (NBUF == 1 && Tn < P.ntiles) {
+                prefetch(Tn, 0);
+                tc::cp_async_commit();
+            }
         }
         tc::cp_async_wait_all();
     } else if (warp == kMmaWarp) {
@@ -224,21 +244,23 @@ k_deriv_tc(TcPass P) {
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16(kTile, N);
             for (; T < P.ntiles; T += gridDim.x, ++k) {
-                const int buf = k & 1;
+                const int buf = k % NBUF;
                 const int slot = slot_of(P.jobs[T / P.tpj], P.axis);
-                ok &= tc::mbar_wait(&S.fullA[buf], (k >> 1) & 1, kWaitCycles);
-                if (k >= 2) ok &= tc::mbar_wait(&S.emptyT[buf], ((k - 2) >> 1) & 1, kWaitCycles);
+                ok &= tc::mbar_wait(&S.fullA[buf], (k / NBUF) & 1, kWaitCycles);
+                if (k >= NBUF)
+                    ok &= tc::mbar_wait(&S.emptyT[buf], ((k - NBUF) / NBUF) & 1, kWaitCycles);
                 if (!ok) break;
                 tc::fence_after();
-                oz::issue_pairs<2>(tmem + (uint32_t)(buf * 4 * N), N, idesc,
-                                   tc::smem_u32(sA + buf * kDigits * kPlane), kPlane, tc::kSbo,
-                                   tc::smem_u32(sB + slot * bBytes), N * tc::kRowBytes,
-                                   tc::kSbo, false);
+                oz::issue_pairs<KP / 16>(tmem + (uint32_t)(buf * 4 * N), N, idesc,
+                                         tc::smem_u32(sA + buf * kDigits * kPlane), kPlane, kSboK,
+                                         tc::smem_u32(sB + slot * bBytes), N * KP * 2, kSboK,
+                                         false);
                 tc::commit(&S.emptyA[buf]);
                 tc::commit(&S.fullT[buf]);
             }
             // the last commit covers every MMA of this CTA
-            if (k > 0) ok &= tc::mbar_wait(&S.fullT[(k - 1) & 1], ((k - 1) >> 1) & 1, kWaitCycles);
+            if (k > 0)
+                ok &= tc::mbar_wait(&S.fullT[(k - 1) % NBUF], ((k - 1) / NBUF) & 1, kWaitCycles);
         }
         __syncwarp();
     } else {
@@ -249,7 +271,7 @@ k_deriv_tc(TcPass P) {
         const uint32_t tq = (uint32_t)(quarter * 32) << 16;
         const int nq = N / 16;
         for (int k = 0, T = blockIdx.x; T < P.ntiles; T += gridDim.x, ++k) {
-            const int buf = k & 1;
+            const int buf = k % NBUF;
             const GridJob& J = P.jobs[T / P.tpj];
             float2* gD = reinterpret_cast<float2*>(out_of(J, P.axis));
             float2* gL = reinterpret_cast<float2*>(J.lap);
@@ -270,9 +292,11 @@ k_deriv_tc(TcPass P) {
                     }
             }
             tc::cp_async_commit();
-            // ring of four: slicer k + 4 cannot arrive before this epilogue is done
+            // ring of four: slicer k + 4 waits for MMA k + 4 - NBUF, which waited
+            // for epilogue k + 4 - 2 NBUF >= k, so it cannot arrive before this
+            // epilogue is done
             ok &= tc::mbar_wait(&S.emaxReady[k & 3], (k >> 2) & 1, kWaitCycles);
-            ok &= tc::mbar_wait(&S.fullT[buf], (k >> 1) & 1, kWaitCycles);
+            ok &= tc::mbar_wait(&S.fullT[buf], (k / NBUF) & 1, kWaitCycles);
             if (!ok) break;
             tc::fence_after();
             const int emax = S.emax[k & 3][erow];
@@ -337,15 +361,17 @@ k_deriv_tc(TcPass P) {
 
 constexpr size_t kSmemCap = 224 * 1024;   // plus ~2.7 KB of static TcShared
 
-size_t tc_smem_bytes(int n, int N, bool lap_stage) {
-    size_t b = 128 + 2 * (size_t)kDigits * kPlane + 2 * (size_t)kDigits * N * tc::kRowBytes +
-               2 * (size_t)kTile * (n + 1) * sizeof(double);
+size_t tc_smem_bytes(int n, int N, bool lap_stage, int kp, int nbuf) {
+    size_t b = 128 + (size_t)nbuf * kDigits * kTile * kp * 2 + 2 * (size_t)kDigits * N * kp * 2 +
+               (size_t)nbuf * kTile * (n + 1) * sizeof(double);
     if (lap_stage) b += (size_t)kTile * (n + 1) * sizeof(float2);
     return b;
 }
 
 // Digit planes of the Lagrange blocks, built once per context.  The tensor
-// path serves line lengths up to 32 (K padded to 32, N = 2n rounded to 16).
+// path serves line lengths up to 32 (K padded to 32, two buffers) and up to
+// kLongMax (K padded to 48, one buffer); N = 2n rounded to 16.  Row exponents
+// sit at a stride of 96 per (axis, slot).
 int tc_setup(mg_ctx* c) {
     const int ns[3] = {c->nx, c->ny, c->nz};
     c->tc_ok = false;
@@ -356,18 +382,20 @@ int tc_setup(mg_ctx* c) {
         MG_CUDA(cudaMemset(c->tc_status, 0, sizeof(int)));
     }
     c->tc_mesh_ok = true;
-    for (int a = 0; a < 3; ++a)
-        if (ns[a] > kKp) return MG_OK;
+    const int nmax = std::max(ns[0], std::max(ns[1], ns[2]));
+    if (nmax > kLongMax) return MG_OK;
+    const int kp = nmax <= kShortK ? kShortK : kLongK;
+    c->tc_kp = kp;
     long total = 0;
     for (int a = 0; a < 3; ++a) {
         c->tc_N[a] = (2 * ns[a] + 15) / 16 * 16;
         for (int s = 0; s < 2; ++s) {
             c->tc_off[a][s] = total;
-            total += (long)kDigits * c->tc_N[a] * kKp;
+            total += (long)kDigits * c->tc_N[a] * kp;
         }
     }
     std::vector<uint16_t> h(total, 0);
-    std::vector<int> he(3 * 2 * 64, 0);
+    std::vector<int> he(3 * 2 * 96, 0);
     for (int a = 0; a < 3; ++a) {
         const int n = ns[a], N = c->tc_N[a];
         const long nn = (long)n * n;
@@ -380,13 +408,14 @@ int tc_setup(mg_ctx* c) {
                 double mx = 0.0;
                 for (int k = 0; k < n; ++k) mx = std::max(mx, std::fabs(row[k]));
                 const int E = oz::host_row_exponent(mx);
-                he[(a * 2 + s) * 64 + j] = E;
+                he[(a * 2 + s) * 96 + j] = E;
                 const int g = 8 * kDigits - 2 - E;
                 for (int k = 0; k < n; ++k) {
                     uint16_t dg[kDigits];
                     oz::host_digits(row[k], g, dg);
                     for (int b = 0; b < kDigits; ++b)
-                        h[c->tc_off[a][s] + (long)b * N * kKp + tc::kmajor_off(j, k) / 2] = dg[b];
+                        h[c->tc_off[a][s] + (long)b * N * kp + tc::kmajor_off_g(j, k, kp / 8) / 2] =
+                            dg[b];
                 }
             }
         }
@@ -395,8 +424,10 @@ int tc_setup(mg_ctx* c) {
     MG_CUDA(cudaMemcpy(c->tcmats, h.data(), total * sizeof(uint16_t), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&c->tc_erow, he.size() * sizeof(int)));
     MG_CUDA(cudaMemcpy(c->tc_erow, he.data(), he.size() * sizeof(int), cudaMemcpyHostToDevice));
-    MG_CUDA(cudaFuncSetAttribute(k_deriv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kSmemCap));
+    MG_CUDA(cudaFuncSetAttribute(k_deriv_tc<kShortK, 2>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap));
+    MG_CUDA(cudaFuncSetAttribute(k_deriv_tc<kLongK, 1>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap));
     c->tc_ok = true;
     return MG_OK;
 }
@@ -410,7 +441,7 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs) {
         P.jobs = jobs;
         for (int s = 0; s < 2; ++s) {
             P.bmat[s] = c->tcmats + c->tc_off[axis][s];
-            P.erow[s] = c->tc_erow + (axis * 2 + s) * 64;
+            P.erow[s] = c->tc_erow + (axis * 2 + s) * 96;
         }
         P.axis = axis;
         P.n = ns[axis];
@@ -421,10 +452,16 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs) {
         P.nx = c->nx;
         P.ny = c->ny;
         P.status = c->tc_status;
-        P.lap_stage = tc_smem_bytes(P.n, P.N, true) <= kSmemCap ? 1 : 0;
+        const int kp = c->tc_kp, nbuf = kp == kShortK ? 2 : 1;
+        P.lap_stage = tc_smem_bytes(P.n, P.N, true, kp, nbuf) <= kSmemCap ? 1 : 0;
+        const size_t sm = tc_smem_bytes(P.n, P.N, P.lap_stage != 0, kp, nbuf);
+        if (sm > kSmemCap) return MG_ERR_ARG;
         const int sms = c->tc_grid_cap > 0 ? std::min(c->tc_grid_cap, c->num_sms) : c->num_sms;
         const int grid = std::min(sms, P.ntiles);
-        k_deriv_tc<<<grid, kThreads, tc_smem_bytes(P.n, P.N, P.lap_stage != 0), c->stream>>>(P);
+        if (kp == kShortK)
+            k_deriv_tc<kShortK, 2><<<grid, kThreads, sm, c->stream>>>(P);
+        else
+            k_deriv_tc<kLongK, 1><<<grid, kThreads, sm, c->stream>>>(P);
         MG_LAUNCHED(c);
     }
     return MG_OK;

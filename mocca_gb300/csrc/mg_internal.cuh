@@ -225,6 +225,7 @@ struct mg_ctx {
     int tc_N[3] = {0, 0, 0};
     bool tc_ok = false;           // every line length <= 32
     bool tc_mesh_ok = false;      // mesh-sized GEMMs on the tensor cores (blocks <= kMeshTcMax)
+    int tc_kp = 32;               // padded K of the tensor-core derivative planes (32 or 48)
     // largest grid of the persistent tensor-core derivative kernel (0: one CTA
     // per SM); set while it runs beside other work on the side stream
     int tc_grid_cap = 0;
