@@ -499,7 +499,7 @@ __global__ void k_residual_norms(const double* __restrict__ r, const double* __r
 }
 
 // Mixed form: two rounds of (FP64 residual, direct separable correction).
-static int coulomb_direct(mg_ctx* c) {
+static int coulomb_direct_launches(mg_ctx* c) {
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     const long V = c->V;
     const int g = div_up(V, kThreads);
@@ -530,6 +530,39 @@ static int coulomb_direct(mg_ctx* c) {
         k_cfast_update<<<g, kThreads, 0, c->stream>>>(c->cpot, t2, nx, ny, nz, c->mx, c->my);
         MG_LAUNCHED(c);
     }
+    return MG_OK;
+}
+
+// The eighteen launches of the two rounds replay as one CUDA graph (fixed
+// buffers per context): a few microseconds each, they would otherwise run at
+// the host's enqueue rate.
+static int coulomb_direct(mg_ctx* c) {
+    if (c->cfast_no_graph) return coulomb_direct_launches(c);
+    if (!c->cfast_graph) {
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            c->cfast_no_graph = true;
+            return coulomb_direct_launches(c);
+        }
+        const long long l0 = c->launches;
+        const int st = coulomb_direct_launches(c);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (st != MG_OK || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return st != MG_OK ? st : MG_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&c->cfast_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            c->cfast_graph = nullptr;
+            return MG_ERR_CUDA;
+        }
+        c->cfast_graph_launches = c->launches - l0;
+        c->launches = l0;
+    }
+    MG_CUDA(cudaGraphLaunch(c->cfast_graph, c->stream));
+    c->launches += c->cfast_graph_launches;
     return MG_OK;
 }
 

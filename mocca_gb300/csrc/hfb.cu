@@ -210,11 +210,12 @@ __global__ void k_taylor_coef(const double* __restrict__ P, const double* __rest
 // rho += dl (Z + Z^T) in both diagonal blocks, kappa_-+ += dl K and
 // kappa_+- -= dl K^T, dl = the isospin's step (0: converged already)
 __global__ void k_taylor_update(const double* __restrict__ Z, const double* __restrict__ K,
-                                const int* __restrict__ hsz, int hmax, int nmax, double dl0,
-                                double dl1, double* __restrict__ rho, double* __restrict__ kappa) {
+                                const int* __restrict__ hsz, int hmax, int nmax,
+                                const double* __restrict__ dls, double* __restrict__ rho,
+                                double* __restrict__ kappa) {
     const int b = blockIdx.y, h = hsz[b], N = 2 * h;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const double dl = b / 2 == 0 ? dl0 : dl1;
+    const double dl = dls[b / 2];
     if (t >= h * h || dl == 0.0) return;
     const int r = t / h, s = t % h;
     const double* Zb = Z + (long)b * hmax * hmax;
@@ -233,11 +234,11 @@ __global__ void k_taylor_update(const double* __restrict__ Z, const double* __re
 // spectrum left behind belongs to the final lambda, as an evaluation there
 // would report it (to O(dl^2)).
 __global__ void k_taylor_energies(const double* __restrict__ X, const int* __restrict__ hsz,
-                                  int nmax, long wstride, double dl0, double dl1,
+                                  int nmax, long wstride, const double* __restrict__ dls,
                                   double* __restrict__ w) {
     const int b = blockIdx.y, h = hsz[b], N = 2 * h;
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const double dl = b / 2 == 0 ? dl0 : dl1;
+    const double dl = dls[b / 2];
     if (col >= N || dl == 0.0) return;
     const double* Xb = X + (long)b * nmax * nmax;
     double s = 0.0;
@@ -371,7 +372,7 @@ int hfb_prepare(mg_ctx* c) {
               A(&H.dfac, 2 * V) && A(&H.pcut, nwt) && A(&H.ktil, 4L * hmax * hmax) &&
               A(&H.fpart, 8 * V) && A(&H.fre, 2 * V) && A(&H.fim, 2 * V) &&
               A(&H.gpart, 4L * H.gchunk * hmax * hmax) && A(&H.cantr, 4L * hmax * hmax) &&
-              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.trace_d, 16) && A(&H.dpart, 4L * hmax) && A(&H.scal_d, 16) &&
+              A(&H.occ, 4L * hmax) && A(&H.fermi_d, 2) && A(&H.dl_d, 2) && A(&H.trace_d, 16) && A(&H.dpart, 4L * hmax) && A(&H.scal_d, 16) &&
               cudaMalloc(&H.members, 4 * hmax * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.hsz, 4 * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&H.nsz_T, 4 * sizeof(int)) == cudaSuccess &&
@@ -444,6 +445,7 @@ int hfb_prepare(mg_ctx* c) {
 
 void hfb_free(mg_ctx* c) {
     Hfb& H = c->hfb;
+    if (H.dl_d) cudaFree(H.dl_d);
     for (double* p : {H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.qe, H.dfac, H.pcut, H.ktil,
                       H.fpart, H.fre, H.fim, H.gpart, H.cantr, H.occ, H.fermi_d, H.trace_d, H.dpart,
                       H.scal_d, H.T, H.Rpp, H.tP, H.tC, H.tT1, H.tT2, H.tZ, H.tK})
@@ -454,6 +456,10 @@ void hfb_free(mg_ctx* c) {
     if (H.h_pinned) cudaFreeHost(H.h_pinned);
     for (cudaGraphExec_t& g : H.eval_graph)
         if (g) cudaGraphExecDestroy(g);
+    if (H.can_graph) cudaGraphExecDestroy(H.can_graph);
+    H.can_graph = nullptr;
+    if (H.taylor_graph) cudaGraphExecDestroy(H.taylor_graph);
+    H.taylor_graph = nullptr;
     eig_free(H.eT);
     eig_free(H.eR);
     gradient_hfb_free(H.grad);
@@ -570,7 +576,7 @@ int hfb_evaluate_at(mg_ctx* c, const double* lam, double* N_out, double* dN_out)
 
 // rho, kappa and the quasiparticle energies moved to lambda + dl from the
 // eigen-decomposition of the last evaluation (first order in dl).
-static int taylor_finish(mg_ctx* c, const double dl[2]) {
+static int taylor_launches(mg_ctx* c) {
     Hfb& H = c->hfb;
     const int hmax = H.hmax;
     const dim3 g(div_up(hmax * hmax, kThreads), 4);
@@ -580,12 +586,51 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
     MG_TRY(gemm_batched(c, H.d_taylor + 4, 8, hmax));
     MG_TRY(gemm_batched(c, H.d_taylor + 12, 8, hmax));
     MG_TRY(gemm_batched(c, H.d_taylor + 20, 4, hmax));
-    k_taylor_update<<<g, kThreads, 0, c->stream>>>(H.tZ, H.tK, H.hsz, hmax, H.nmax, dl[0], dl[1],
+    k_taylor_update<<<g, kThreads, 0, c->stream>>>(H.tZ, H.tK, H.hsz, hmax, H.nmax, H.dl_d,
                                                   H.rho, H.kappa);
     MG_LAUNCHED(c);
     k_taylor_energies<<<dim3(div_up(H.nmax, 128), 4), 128, 0, c->stream>>>(
-        H.eT.X, H.hsz, H.nmax, H.eT.wstride, dl[0], dl[1], H.eT.w);
+        H.eT.X, H.hsz, H.nmax, H.eT.wstride, H.dl_d, H.eT.w);
     MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+// The steps dl go to the device (from the pinned block; the host writes it
+// once per pairing step, several synchronisations before it is reused) and
+// the seven launches replay as one CUDA graph.
+static int taylor_finish(mg_ctx* c, const double dl[2]) {
+    Hfb& H = c->hfb;
+    double* hp = H.h_pinned;
+    hp[26] = dl[0];
+    hp[27] = dl[1];
+    MG_CUDA(cudaMemcpyAsync(H.dl_d, hp + 26, 2 * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    if (H.no_graph) return taylor_launches(c);
+    if (!H.taylor_graph) {
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            H.no_graph = true;
+            return taylor_launches(c);
+        }
+        const long long l0 = c->launches;
+        const int st = taylor_launches(c);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (st != MG_OK || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return st != MG_OK ? st : MG_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&H.taylor_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            H.taylor_graph = nullptr;
+            return MG_ERR_CUDA;
+        }
+        H.taylor_graph_launches = c->launches - l0;
+        c->launches = l0;
+    }
+    MG_CUDA(cudaGraphLaunch(H.taylor_graph, c->stream));
+    c->launches += H.taylor_graph_launches;
     return MG_OK;
 }
 
@@ -772,6 +817,49 @@ static int fermi_broyden(mg_ctx* c, double lam[2], double f[2], bool conv[2], in
 }
 
 // SolvePairing for HFB (src/Pairing.f90:743-890, PairingIter 1).
+// The canonical-basis decomposition of the four rho_++ blocks.  From the
+// second pairing step on it starts from last step's vectors (the Jacobi warm
+// seed) and replays as one CUDA graph, like the evaluations of the Fermi
+// search (recaptured when the precision form changes: the two forms launch
+// different polish kernels).
+static int canonical_eig(mg_ctx* c) {
+    Hfb& H = c->hfb;
+    if (!H.eR.have_vectors || H.no_graph) {
+        return eig_batched(c, H.eR, H.eR.have_vectors ? kSeedJacobiWarm : kSeedCold, H.nref, true);
+    }
+    if (H.can_graph && H.can_graph_prec != c->cur_precision) {
+        cudaGraphExecDestroy(H.can_graph);
+        H.can_graph = nullptr;
+    }
+    if (!H.can_graph) {
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            H.no_graph = true;
+            return eig_batched(c, H.eR, kSeedJacobiWarm, H.nref, true);
+        }
+        const long long l0 = c->launches;
+        const int st = eig_batched(c, H.eR, kSeedJacobiWarm, H.nref, true);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (st != MG_OK || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return st != MG_OK ? st : MG_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&H.can_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            H.can_graph = nullptr;
+            return MG_ERR_CUDA;
+        }
+        H.can_graph_launches = c->launches - l0;
+        H.can_graph_prec = c->cur_precision;
+        c->launches = l0;
+    }
+    MG_CUDA(cudaGraphLaunch(H.can_graph, c->stream));
+    c->launches += H.can_graph_launches;
+    return MG_OK;
+}
+
 int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     Hfb& H = c->hfb;
     if (!H.ready) MG_TRY(hfb_prepare(c));
@@ -832,7 +920,7 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
     // individual vectors matter, so the FP32 Jacobi seed (warm-started from
     // last iteration's vectors) resolves the clusters before the refinement
     // and the FP64 polish
-    MG_TRY(eig_batched(c, H.eR, H.eR.have_vectors ? kSeedJacobiWarm : kSeedCold, H.nref, true));
+    MG_TRY(canonical_eig(c));
     H.eR.have_vectors = true;
     k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax, H.cantr,
                                                  c->bas[MG_CAN_BASIS].occ, H.scal_d, c->flags);

@@ -50,6 +50,7 @@ void free_all(mg_ctx* c) {
     hfb_free(c);
     constraints_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
+    if (c->cfast_graph) cudaGraphExecDestroy(c->cfast_graph);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     for (cudaEvent_t e : c->ph.ev)

@@ -145,6 +145,12 @@ struct Hfb {
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
     long long eval_graph_launches[3] = {0, 0, 0};
     int eval_graph_prec[3] = {-1, -1, -1};   // precision form the graph was captured in
+    cudaGraphExec_t taylor_graph = nullptr;   // first-order finish of the Fermi search
+    long long taylor_graph_launches = 0;
+    double* dl_d = nullptr;                   // its steps per isospin
+    cudaGraphExec_t can_graph = nullptr;      // canonical-basis decomposition (warm seed)
+    long long can_graph_launches = 0;
+    int can_graph_prec = -1;
     bool no_graph = false;
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
@@ -309,6 +315,9 @@ struct mg_ctx {
     double pairing_energy[2] = {0.0, 0.0};
     long long launches = 0;
     bool side_derive_pending = false;  // mg_iterate: the pairing step forks the HF DeriveAll
+    cudaGraphExec_t cfast_graph = nullptr;   // the direct Coulomb solve's two rounds
+    long long cfast_graph_launches = 0;
+    bool cfast_no_graph = false;
 
     // phase timer (mg_set_phase_timing): events between the phases of the
     // pass in progress, their phase ids, and the totals
