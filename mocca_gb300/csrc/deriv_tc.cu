@@ -380,6 +380,8 @@ int tc_setup(mg_ctx* c) {
     if (!c->tc_status) {
         MG_CUDA(cudaMalloc(&c->tc_status, sizeof(int)));
         MG_CUDA(cudaMemset(c->tc_status, 0, sizeof(int)));
+        MG_CUDA(cudaMallocHost(&c->h_tc_status, sizeof(int)));
+        *c->h_tc_status = 0;
     }
     c->tc_mesh_ok = true;
     const int nmax = std::max(ns[0], std::max(ns[1], ns[2]));
@@ -470,6 +472,18 @@ int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs) {
 // Status of the tensor-core waits since the last call (MG_ERR_TIMEOUT when an
 // MMA completion wait ran out of its cap, in the derivatives or the mesh
 // GEMMs); synchronises the stream.
+int tc_status_async(mg_ctx* c) {
+    if (!c->tc_ok && !c->tc_mesh_ok) return MG_OK;
+    MG_CUDA(cudaMemcpyAsync(c->h_tc_status, c->tc_status, sizeof(int), cudaMemcpyDeviceToHost,
+                            c->stream));
+    return MG_OK;
+}
+
+int tc_status_result(mg_ctx* c) {
+    if (!c->tc_ok && !c->tc_mesh_ok) return MG_OK;
+    return *c->h_tc_status ? MG_ERR_TIMEOUT : MG_OK;
+}
+
 int tc_check(mg_ctx* c) {
     if (!c->tc_ok && !c->tc_mesh_ok) return MG_OK;
     int h = 0;

@@ -50,6 +50,7 @@ void free_all(mg_ctx* c) {
     hfb_free(c);
     constraints_free(c);
     if (c->h_cg_status) cudaFreeHost(c->h_cg_status);
+    if (c->h_tc_status) cudaFreeHost(c->h_tc_status);
     if (c->cfast_graph) cudaGraphExecDestroy(c->cfast_graph);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -780,11 +781,13 @@ extern "C" int mg_iterate(mg_ctx* c, int n_iter, double dt, double momentum,
         // CompEnergy every pass (src/Main.f90:309): it also keeps the energy
         // history of the convergence check
         mg_energy_terms e{};
+        // the tensor-core status word comes back with the energy's readback
+        if (k == n_iter - 1) MG_TRY(tc_status_async(c));
         MG_TRY(energy(c, out ? out : &e));
         phase_mark(c, MG_PH_ENERGY);
         MG_TRY(phase_end(c));
     }
-    MG_TRY(tc_check(c));
+    MG_TRY(n_iter > 0 ? tc_status_result(c) : tc_check(c));
     return st;
 }
 

@@ -232,6 +232,7 @@ struct mg_ctx {
     bool tc_ok = false;           // every line length <= 32
     bool tc_mesh_ok = false;      // mesh-sized GEMMs on the tensor cores (blocks <= kMeshTcMax)
     int tc_kp = 32;               // padded K of the tensor-core derivative planes (32 or 48)
+    int* h_tc_status = nullptr;   // pinned copy of tc_status, read with the energy's sync
     // largest grid of the persistent tensor-core derivative kernel (0: one CTA
     // per SM); set while it runs beside other work on the side stream
     int tc_grid_cap = 0;
@@ -365,6 +366,9 @@ int derive_basis(mg_ctx* c, int b);
 int tc_setup(mg_ctx* c);
 int run_jobs_tc(mg_ctx* c, const GridJob* jobs, int njobs);
 int tc_check(mg_ctx* c);
+// tc_check in two halves: enqueue the status copy, read it after a later sync
+int tc_status_async(mg_ctx* c);
+int tc_status_result(mg_ctx* c);
 
 int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double mom);
 int hpsi_single(mg_ctx* c, double* psi, const double* der, const double* lap, const int* qn_dev,
