@@ -309,7 +309,8 @@ k_occupations(const double* __restrict__ X, const double* __restrict__ w,
 // block pairing energy -sum Delta_ij kappa_ij (HFBEnergy) with mixed kappa.
 __global__ void __launch_bounds__(kThreads)
 k_hfb_mix(double* rho, double* kappa, double* oldrho, double* oldkappa, const double* delta,
-          const int* hsz, int nmax, double mix, int mix_rho, int mix_kappa, double* scal) {
+          const int* hsz, int nmax, double mix, int mix_rho, int mix_kappa, double* scal,
+          double* __restrict__ bak_rho, double* __restrict__ bak_kappa) {
     __shared__ double red[32];
     const int b = blockIdx.x;
     const int N = 2 * hsz[b];
@@ -318,8 +319,11 @@ k_hfb_mix(double* rho, double* kappa, double* oldrho, double* oldkappa, const do
     for (int t = threadIdx.x; t < N * N; t += kThreads) {
         const long o = o0 + t;
         double r = rho[o], k = kappa[o];
-        if (mix_rho) r = mix * r + (1.0 - mix) * oldrho[o];
-        if (mix_kappa) k = mix * k + (1.0 - mix) * oldkappa[o];
+        const double ro = oldrho[o], ko = oldkappa[o];
+        bak_rho[o] = ro;     // the history as it was, for a redo of the step
+        bak_kappa[o] = ko;
+        if (mix_rho) r = mix * r + (1.0 - mix) * ro;
+        if (mix_kappa) k = mix * k + (1.0 - mix) * ko;
         rho[o] = r;
         kappa[o] = k;
         oldrho[o] = r;
@@ -368,6 +372,7 @@ int hfb_prepare(mg_ctx* c) {
     };
     H.gchunk = std::max(1, (2 * c->num_sms) / 4);
     bool ok = A(&H.rho, nm2) && A(&H.kappa, nm2) && A(&H.oldrho, nm2) && A(&H.oldkappa, nm2) &&
+              A(&H.oldrho_bak, nm2) && A(&H.oldkappa_bak, nm2) &&
               A(&H.delta, nm2) && A(&H.T, nm2) && A(&H.Rpp, 4L * hmax * hmax) &&
               A(&H.dfac, 2 * V) && A(&H.pcut, nwt) && A(&H.ktil, 4L * hmax * hmax) &&
               A(&H.fpart, 8 * V) && A(&H.fre, 2 * V) && A(&H.fim, 2 * V) &&
@@ -446,6 +451,8 @@ int hfb_prepare(mg_ctx* c) {
 void hfb_free(mg_ctx* c) {
     Hfb& H = c->hfb;
     if (H.dl_d) cudaFree(H.dl_d);
+    if (H.oldrho_bak) cudaFree(H.oldrho_bak);
+    if (H.oldkappa_bak) cudaFree(H.oldkappa_bak);
     for (double* p : {H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.qe, H.dfac, H.pcut, H.ktil,
                       H.fpart, H.fre, H.fim, H.gpart, H.cantr, H.occ, H.fermi_d, H.trace_d, H.dpart,
                       H.scal_d, H.T, H.Rpp, H.tP, H.tC, H.tT1, H.tT2, H.tZ, H.tK})
@@ -913,27 +920,53 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
 
     // ---- canonical basis, occupations, mixing, pairing energy ------------------
     double* hp = H.h_pinned;
-    k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
-        H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
-    MG_LAUNCHED(c);
-    // canonical basis: the occupations cluster near 0 and 1 and the
-    // individual vectors matter, so the FP32 Jacobi seed (warm-started from
-    // last iteration's vectors) resolves the clusters before the refinement
-    // and the FP64 polish
-    MG_TRY(canonical_eig(c));
-    H.eR.have_vectors = true;
-    k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax, H.cantr,
-                                                 c->bas[MG_CAN_BASIS].occ, H.scal_d, c->flags);
-    MG_LAUNCHED(c);
-    int oflag = 0;
-    MG_CUDA(cudaMemcpyAsync(&oflag, c->flags + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    MG_CUDA(cudaStreamSynchronize(c->stream));
-    if (oflag) {
+    const bool was_zero = H.oldrho_zero;
+    int hflags[8];
+    // redo: the canonical basis by plain FP64 Jacobi instead of the warm-seeded
+    // decomposition.  One synchronisation at the end reads the pairing
+    // energies and the flags, the occupation check among them.
+    auto canonical_part = [&](bool redo) -> int {
+        k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
+            H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
+        MG_LAUNCHED(c);
+        if (redo) {
+            MG_TRY(eig_jacobi_fp64(c, H.eR));
+        } else {
+            // the occupations cluster near 0 and 1 and the individual vectors
+            // matter, so the FP32 Jacobi seed (warm-started from last
+            // iteration's vectors) resolves the clusters before the refinement
+            // and the polish
+            MG_TRY(canonical_eig(c));
+            H.eR.have_vectors = true;
+        }
+        k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax,
+                                                     H.cantr, c->bas[MG_CAN_BASIS].occ, H.scal_d,
+                                                     c->flags);
+        MG_LAUNCHED(c);
+        MG_TRY(canonical_transform(c));
+        k_hfb_mix<<<4, kThreads, 0, c->stream>>>(H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta,
+                                                 H.hsz, H.nmax, H.pp.mix, was_zero ? 0 : 1, 1,
+                                                 H.scal_d, H.oldrho_bak, H.oldkappa_bak);
+        MG_LAUNCHED(c);
+        MG_CUDA(cudaMemcpyAsync(hp + 16, H.scal_d, 8 * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        MG_CUDA(cudaMemcpyAsync(hflags, c->flags, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                                c->stream));
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+        return MG_OK;
+    };
+    MG_TRY(canonical_part(false));
+    if (hflags[3]) {
         // An occupation above one: a decomposition that lost orthonormality
-        // (the refinement can, on spectra clustered at 0 and 1).  Redo the
-        // evaluation at the final lambda from scratch and the canonical basis
-        // by plain FP64 Jacobi before reporting the state as the reference
-        // does.
+        // (the refinement can, on spectra clustered at 0 and 1).  Put the
+        // mixing history back, redo the evaluation at the final lambda from
+        // scratch and the canonical basis by plain FP64 Jacobi, then mix
+        // again, before reporting the state as the reference does.
+        const long nbytes = nm2 * (long)sizeof(double);
+        MG_CUDA(cudaMemcpyAsync(H.oldrho, H.oldrho_bak, nbytes, cudaMemcpyDeviceToDevice,
+                                c->stream));
+        MG_CUDA(cudaMemcpyAsync(H.oldkappa, H.oldkappa_bak, nbytes, cudaMemcpyDeviceToDevice,
+                                c->stream));
         double f2[2], fp2[2];
         MG_TRY(hfb_evaluate(c, lam, f2, fp2, true, kSeedCold));
         ++evals;
@@ -941,25 +974,10 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         tr1 = f2[1] + c->p.protons;
         first_order = false;
         MG_CUDA(cudaMemsetAsync(c->flags + 3, 0, sizeof(int), c->stream));
-        k_copy_rpp<<<dim3(div_up(H.hmax * H.hmax, kThreads), 4), kThreads, 0, c->stream>>>(
-            H.rho, H.hsz, H.members, H.hmax, H.nmax, H.Rpp, c->bas[MG_HF_BASIS].occ);
-        MG_LAUNCHED(c);
-        MG_TRY(eig_jacobi_fp64(c, H.eR));
-        k_occupations<<<4, kThreads, 0, c->stream>>>(H.eR.X, H.eR.w, H.hsz, H.cstart, H.hmax,
-                                                     H.cantr, c->bas[MG_CAN_BASIS].occ, H.scal_d,
-                                                     c->flags);
-        MG_LAUNCHED(c);
+        MG_TRY(canonical_part(true));
         ++H.reseeds;
     }
-    MG_TRY(canonical_transform(c));
-    k_hfb_mix<<<4, kThreads, 0, c->stream>>>(H.rho, H.kappa, H.oldrho, H.oldkappa, H.delta, H.hsz,
-                                           H.nmax, H.pp.mix, H.oldrho_zero ? 0 : 1, 1, H.scal_d);
-    MG_LAUNCHED(c);
     H.oldrho_zero = false;
-    MG_CUDA(cudaMemcpyAsync(hp + 16, H.scal_d, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    int hflags[8];
-    MG_CUDA(cudaMemcpyAsync(hflags, c->flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    MG_CUDA(cudaStreamSynchronize(c->stream));
     H.epair[0] = -0.5 * (hp[16] + hp[17]);
     H.epair[1] = -0.5 * (hp[18] + hp[19]);
     H.disp[0] = hp[20] + hp[21];

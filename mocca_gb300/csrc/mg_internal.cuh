@@ -148,6 +148,7 @@ struct Hfb {
     cudaGraphExec_t taylor_graph = nullptr;   // first-order finish of the Fermi search
     long long taylor_graph_launches = 0;
     double* dl_d = nullptr;                   // its steps per isospin
+    double *oldrho_bak = nullptr, *oldkappa_bak = nullptr;   // mixing history before the last mix
     cudaGraphExec_t can_graph = nullptr;      // canonical-basis decomposition (warm seed)
     long long can_graph_launches = 0;
     int can_graph_prec = -1;
