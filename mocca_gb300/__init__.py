@@ -2,8 +2,9 @@
 
 The compute lives in libmocca_gpu.so (C ABI: include/mocca_gpu.h); this
 package holds the ctypes binding (`_abi`), the reference-shaped host mirror
-(`mesh.MeshState`), Skyrme parameter sets (`forces`) and seeded synthetic
-inputs (`synthetic`).  There is no CPU fallback: without the library every
+(`mesh.MeshState`), the .wf wavefunction files (`wf.WavefunctionFile`, C
+ABI include/mocca_wf.h), Skyrme parameter sets (`forces`) and seeded
+synthetic inputs (`synthetic`).  There is no CPU fallback: without the library every
 entry point raises.
 """
 from ._abi import (MG_CAN_BASIS, MG_FP64, MG_HF_BASIS, MG_MIXED, MG_PAIRING_HF,  # noqa: F401

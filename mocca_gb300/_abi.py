@@ -1,4 +1,4 @@
-"""ctypes declarations of the C ABI in include/mocca_gpu.h.
+"""ctypes declarations of the C ABI in include/mocca_gpu.h and include/mocca_wf.h.
 
 The structures mirror the header field by field; `load()` opens the in-tree
 libmocca_gpu.so and declares every entry point's signature.  No compute
@@ -17,6 +17,7 @@ MG_ERR_CUDA = -2
 MG_ERR_STATE = -3
 MG_ERR_TIMEOUT = -4
 MG_ERR_NAN = -5
+MG_ERR_IO = -6
 
 MG_FP64 = 0
 MG_MIXED = 1
@@ -29,6 +30,7 @@ STATUS_NAMES = {
     MG_OK: "ok", MG_NOT_CONVERGED: "not converged", MG_ERR_ARG: "invalid argument",
     MG_ERR_CUDA: "CUDA error", MG_ERR_STATE: "call out of order",
     MG_ERR_TIMEOUT: "device wait timed out", MG_ERR_NAN: "NaN detected",
+    MG_ERR_IO: "wavefunction file missing, unreadable or not version 1",
 }
 
 
@@ -154,6 +156,39 @@ class MgConvergence(C.Structure):
                 ("pairing_prec", C.c_double)]
 
 
+class MgWfHeader(C.Structure):
+    _fields_ = [
+        ("version", C.c_int),
+        ("energy", C.c_double), ("denergy", C.c_double),
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("dx", C.c_double),
+        ("trc", C.c_int), ("pc", C.c_int), ("sc", C.c_int), ("tsc", C.c_int), ("ic", C.c_int),
+        ("nwt", C.c_int),
+        ("neutrons", C.c_double), ("protons", C.c_double),
+        ("fd_order", C.c_int), ("fd_lap_order", C.c_int), ("coulomb_lap_order", C.c_int),
+        ("force", C.c_char * 208),
+        ("skyrme", C.c_double * 14),
+        ("hbar", C.c_double), ("hbm", C.c_double * 2),
+        ("com1body", C.c_int), ("com2body", C.c_int),
+        ("coef", C.c_double * 28),
+        ("pairing_type", C.c_int),
+        ("pairing_strength", C.c_double * 2), ("pairing_alpha", C.c_double * 2),
+        ("pairing_cut", C.c_double * 2),
+        ("fermi", C.c_double * 2), ("ln_lambda", C.c_double * 2),
+        ("omega", C.c_double * 3), ("crank_values", C.c_double * 3),
+        ("hfb_size", C.c_int), ("pindex", C.c_int), ("iindex", C.c_int),
+        ("can_blocks", C.c_int), ("has_cutoffs", C.c_int), ("has_jmunu", C.c_int),
+        ("odd_records", C.c_int), ("n_moments", C.c_int),
+    ]
+
+
+# MG_WF_* field ids of include/mocca_wf.h, in order
+WF_FIELDS = ("grids", "spwf_real", "spwf_int", "rho", "derrho", "laprho", "tau", "nablaj",
+             "jmunu", "odd1", "odd2", "odd3", "odd4", "odd5", "cutoffs", "blocksizes", "U",
+             "V", "columns", "rhohfb", "kappahfb", "cantransfo", "moment_int", "moment_real")
+WF_INT_FIELDS = {"spwf_int", "blocksizes", "columns", "moment_int"}
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -219,6 +254,16 @@ SIGNATURES = {
     "mg_solve_pairing": [_P, C.POINTER(MgPairingInfo)],
     "mg_get_hfb_block": [_P, C.c_int, _D, _D, _D],
     "mg_get_pairing_field": [_P, _D, _D, _D],
+    "mg_wf_load": [C.c_char_p, C.POINTER(_P)],
+    "mg_wf_new": [C.POINTER(MgWfHeader), C.POINTER(_P)],
+    "mg_wf_save": [_P, C.c_char_p],
+    "mg_wf_free": [_P],
+    "mg_wf_get_header": [_P, C.POINTER(MgWfHeader)],
+    "mg_wf_set_scalars": [_P, C.POINTER(MgWfHeader)],
+    "mg_wf_field": [_P, C.c_int, C.POINTER(_P), C.POINTER(C.c_longlong)],
+    "mg_wf_from_context": [_P, C.c_char_p, C.POINTER(_P)],
+    "mg_wf_to_context": [_P, _P],
+    "mg_angular_momentum": [_P, C.c_int, _D],
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmocca_gpu.so"

@@ -1,7 +1,8 @@
 """Build libmocca_gpu.so in-tree for sm_103a (GB300).
 
 Each .cu file under csrc/ compiles to an object in parallel with one
--gencode (compute_103a -> sm_103a); the objects link into
+-gencode (compute_103a -> sm_103a), each .cpp file (host code) with nvcc's
+host compiler; the objects link into
 mocca_gb300/_lib/libmocca_gpu.so.  Rebuilds only when a source or header is
 newer than the library.
 """
@@ -34,14 +35,17 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    """Kernel sources (.cu) and host-only sources (.cpp, compiled by nvcc's
+    host compiler)."""
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+    deps = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")) + list(CSRC.glob("*.cuh"))
+            + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h")))
     return any(p.stat().st_mtime > t for p in deps)
 
 

@@ -312,8 +312,14 @@ int constraint_moments(mg_ctx* c) {
         MomentConstraint& k = K.list[q];
         // OldValue shifts and takes the previous Value (SaveOld = 1,
         // src/Moments.f90:1921-1931)
-        for (int i = 6; i > 0; --i) k.old_value[i] = k.old_value[i - 1];
+        for (int i = 6; i > 0; --i) {
+            k.old_value[i] = k.old_value[i - 1];
+            k.old_iso[i][0] = k.old_iso[i - 1][0];
+            k.old_iso[i][1] = k.old_iso[i - 1][1];
+        }
         k.old_value[0] = k.value[0] + k.value[1];
+        k.old_iso[0][0] = k.value[0];
+        k.old_iso[0][1] = k.value[1];
         for (int it = 0; it < 2; ++it) {
             k.value[it] = K.h_red[4 * q + it];
             k.squared[it] = K.h_red[4 * q + 2 + it];

@@ -430,6 +430,27 @@ int hfb_prepare(mg_ctx* c) {
             q[3] = 1;
         }
     MG_TRY(mg_upload_spinors(c, MG_CAN_BASIS, nullptr, cqn.data(), 0, nwt));
+    if (H.restart_pending) {
+        // RhoHFB / KappaHFB read from a wavefunction file (TransformHFBMatrices
+        // with matching symmetries copies them, src/Transform.f90:1056-1064);
+        // GuessKappa still overrides kappa afterwards, as the pairing
+        // initialisation guesses after the read (src/Pairing.f90:800-803)
+        for (int b = 0; b < 4; ++b)
+            if (H.restart_n[b] != 2 * H.hsz_h[b]) return MG_ERR_STATE;
+        std::vector<double> r(nm2, 0.0), k(nm2, 0.0);
+        for (int b = 0; b < 4; ++b) {
+            const size_t N2 = (size_t)H.restart_n[b] * H.restart_n[b];
+            std::copy(H.restart_rho[b].begin(), H.restart_rho[b].begin() + N2,
+                      r.begin() + (long)b * H.nmax * H.nmax);
+            std::copy(H.restart_kappa[b].begin(), H.restart_kappa[b].begin() + N2,
+                      k.begin() + (long)b * H.nmax * H.nmax);
+            H.restart_rho[b].clear();
+            H.restart_kappa[b].clear();
+        }
+        MG_CUDA(cudaMemcpy(H.rho, r.data(), nm2 * sizeof(double), cudaMemcpyHostToDevice));
+        MG_CUDA(cudaMemcpy(H.kappa, k.data(), nm2 * sizeof(double), cudaMemcpyHostToDevice));
+        H.restart_pending = false;
+    }
     // GuessHFBMatrices case(2) with time reversal: kappa(i, i+h) = -1/4,
     // kappa(i+h, i) = +1/4
     if (H.pp.guess_kappa) {

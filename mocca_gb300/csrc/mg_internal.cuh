@@ -167,6 +167,11 @@ struct Hfb {
     long long taylor_steps = 0;      // pairing steps finished by the expansion
     int nref = 2;             // FP64 refinement steps per eigen-decomposition
     GradHfb* grad = nullptr;  // fermi_solver 2 (gradient_hfb.cu)
+    // RhoHFB / KappaHFB of a wavefunction file (wf_ctx.cu), N x N per block,
+    // taken by hfb_prepare in place of the kappa guess
+    bool restart_pending = false;
+    int restart_n[4] = {0, 0, 0, 0};
+    std::vector<double> restart_rho[4], restart_kappa[4];
 };
 
 // One multipole constraint of the alternating kind (constraints.cu): the
@@ -180,6 +185,7 @@ struct MomentConstraint {
     double intensity = 0.0;     // 0: estimated on the first readjustment
     double value[2] = {0.0, 0.0}, squared[2] = {0.0, 0.0};
     double old_value[7] = {0, 0, 0, 0, 0, 0, 0};   // sums of OldValue(:, 1..7)
+    double old_iso[7][2] = {};  // OldValue(it, 1..7) per isospin (the wavefunction file's)
     bool started = false;       // moments computed once (running target set)
 };
 

@@ -86,6 +86,78 @@ k_symops(const double* __restrict__ psi, int nx, int ny, int nz, double dx, int 
     }
 }
 
+// DiagAng's <J> (src/Spwf.f90:976-1085): spin part sigma/2 plus the
+// orbital part -i r x nabla, real parts, per spwf.  der holds Der(1:3) as
+// [d][l][V] per spwf, FP64 or double-float {hi, lo} pairs.  jx / jy are
+// skipped where signature (and, for jy, time simplex) makes them zero.
+constexpr int kJ = 3;
+
+__device__ __forceinline__ double der_at(const double* p, long k, int df) {
+    if (!df) return p[k];
+    const float2 hl = reinterpret_cast<const float2*>(p)[k];
+    return (double)hl.x + (double)hl.y;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_angmom(const double* __restrict__ psi, const double* __restrict__ der, int df, int nx, int ny,
+         int nz, double dx, int full, int want_x, int want_y, long V, double* __restrict__ part) {
+    __shared__ double red[kThreads / 32][kJ];
+    const int i = blockIdx.y;
+    const double* p = psi + (long)i * 4 * V;
+    const double* d = der + (long)i * 12 * V;
+    double acc[kJ] = {0, 0, 0};
+    const double ox = full ? nx / 2.0 * dx : 0.0, oy = full ? ny / 2.0 * dx : 0.0,
+                 oz = full ? nz / 2.0 * dx : 0.0;
+    for (long v = (long)blockIdx.x * kThreads + threadIdx.x; v < V;
+         v += (long)gridDim.x * kThreads) {
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long)nx * ny));
+        const double X = dx / 2.0 + dx * x - ox, Y = dx / 2.0 + dx * y - oy,
+                     Z = dx / 2.0 + dx * z - oz;
+        double a[4], gx[4], gy[4], gz[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            a[l] = p[l * V + v];
+            gx[l] = der_at(d, (0 * 4 + l) * V + v, df);
+            gy[l] = der_at(d, (1 * 4 + l) * V + v, df);
+        }
+        // Jz: spin 1/2 (|1|^2 + |2|^2 - |3|^2 - |4|^2); orbital with the
+        // (re, im) pairs (1, 2) and (3, 4) of the two spin components
+        double jz = 0.5 * (a[0] * a[0] + a[1] * a[1] - a[2] * a[2] - a[3] * a[3]);
+        jz += a[1] * (Y * gx[0] - X * gy[0]) - a[0] * (Y * gx[1] - X * gy[1]) +
+              a[3] * (Y * gx[2] - X * gy[2]) - a[2] * (Y * gx[3] - X * gy[3]);
+        acc[2] += jz;
+        if (want_x | want_y) {
+#pragma unroll
+            for (int l = 0; l < 4; ++l) gz[l] = der_at(d, (2 * 4 + l) * V + v, df);
+            if (want_x) {
+                double jx = a[0] * a[2] + a[1] * a[3];
+                jx += a[1] * (Z * gy[0] - Y * gz[0]) - a[0] * (Z * gy[1] - Y * gz[1]) +
+                      a[3] * (Z * gy[2] - Y * gz[2]) - a[2] * (Z * gy[3] - Y * gz[3]);
+                acc[0] += jx;
+            }
+            if (want_y) {
+                double jy = a[0] * a[3] - a[1] * a[2];
+                jy += a[1] * (X * gz[0] - Z * gx[0]) - a[0] * (X * gz[1] - Z * gx[1]) +
+                      a[3] * (X * gz[2] - Z * gx[2]) - a[2] * (X * gz[3] - Z * gx[3]);
+                acc[1] += jy;
+            }
+        }
+    }
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+#pragma unroll
+    for (int q = 0; q < kJ; ++q) {
+        double s = acc[q];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[warp][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kJ) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += red[w][threadIdx.x];
+        part[((long)i * gridDim.x + blockIdx.x) * kJ + threadIdx.x] = s;
+    }
+}
+
 }  // namespace
 
 }  // namespace mg
@@ -122,6 +194,36 @@ extern "C" int mg_symmetry_operators(mg_ctx* c, int b, double* out) {
         o[3] = qn[3] != 0 ? qn[3] : s[3] * c->dv;
         o[4] = qn[2] != 0 ? 0.0 : s[4] * c->dv;
         o[5] = std::sqrt(s[0] * c->dv);
+    }
+    return MG_OK;
+}
+
+extern "C" int mg_angular_momentum(mg_ctx* c, int b, double* out) {
+    using namespace mg;
+    if (!c || !out || b < 0 || b > 1) return MG_ERR_ARG;
+    if (b == MG_CAN_BASIS && c->p.pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
+    Basis& B = c->bas[b];
+    if (!B.have_qn) return MG_ERR_STATE;
+    MG_TRY(derive_basis(c, b));
+    const long V = c->V;
+    const int nwt = c->p.nwt;
+    const int nch = std::max(1, std::min(16, div_up(V, kThreads * 4)));
+    if ((size_t)nwt * nch * kJ > c->red_len) return MG_ERR_STATE;
+    const int full = c->folded ? 0 : 1;
+    const int want_x = c->p.sc ? 0 : 1, want_y = (c->p.sc || c->p.tsc) ? 0 : 1;
+    k_angmom<<<dim3(nch, nwt), kThreads, 0, c->stream>>>(B.psi, B.der, B.der_df ? 1 : 0, c->nx,
+                                                         c->ny, c->nz, c->p.dx, full, want_x,
+                                                         want_y, V, c->red);
+    MG_LAUNCHED(c);
+    std::vector<double> h((size_t)nwt * nch * kJ);
+    MG_CUDA(cudaMemcpyAsync(h.data(), c->red, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nwt; ++i) {
+        double s[kJ] = {0, 0, 0};
+        for (int q = 0; q < nch; ++q)
+            for (int k = 0; k < kJ; ++k) s[k] += h[((size_t)i * nch + q) * kJ + k];
+        for (int k = 0; k < kJ; ++k) out[3 * i + k] = s[k] * c->dv;
     }
     return MG_OK;
 }

@@ -39,6 +39,7 @@ class Force:
     com1body: int = 0
     com2body: int = 0
     cexchange: int = 2
+    name: str = ""            # afor, the &skf group's name (written to .wf files)
 
     def to_c(self) -> _abi.MgForce:
         f = _abi.MgForce()
@@ -56,7 +57,7 @@ class Force:
 
 SLY4 = Force(t0=-2488.913, x0=0.834, t1=486.818, x1=-0.344, t2=-546.395, x2=-1.0,
              t3a=13777.0, x3a=1.354, yt3a=0.166666666666666666667, t3b=0.0, x3b=0.0,
-             yt3b=0.0, wso=123.0, wsoq=123.0, com1body=2)
+             yt3b=0.0, wso=123.0, wsoq=123.0, com1body=2, name="SLy4")
 
 
 @dataclass

@@ -15,6 +15,8 @@ every one of them runs on the GPU through the C ABI:
     ConstructPotentials src/PotentialMixing.f90:17-201
     CompEnergy         src/Energy.f90:62-179
     Evolve             src/Main.f90:255-328            (n passes of the loop body)
+    WriteMOCCa         src/InOut.f90:905-1046          (.wf version 1)
+    ReadMOCCa          src/InOut.f90:1050-1416         (restart from .wf)
 
 `Batch` runs many independent instances (one MeshState each) concurrently
 through mg_batch_*.
@@ -340,18 +342,44 @@ class MeshState:
         self._call("mg_get_pairing_field", _dptr(re), _dptr(im), _dptr(df))
         return re, im, df
 
-    def Start(self):
+    def AngularMomentum(self, basis: int = _abi.MG_HF_BASIS) -> np.ndarray:
+        """DiagAng's <J> (src/Spwf.f90:976-1085) per spwf, [nwt, 3]."""
+        out = np.empty(3 * self.p.nwt)
+        self._call("mg_angular_momentum", basis, _dptr(out))
+        return out.reshape(self.p.nwt, 3)
+
+    def WriteMOCCa(self, path, force_name: str | None = None):
+        """WriteMOCCa_v1 (src/InOut.f90:905-1046): this state as a version-1
+        .wf file."""
+        from .wf import WavefunctionFile
+        with WavefunctionFile.from_state(self, force_name) as w:
+            w.save(path)
+
+    def ReadMOCCa(self, path) -> dict:
+        """ReadMOCCa_v1 + Input (src/InOut.f90:1050-1416, :123-192): restart
+        from a .wf file with this state's mesh, symmetries and nwt (under HFB
+        after set_pairing, before the first pairing step); returns the file's
+        header.  Follow with Start()."""
+        from .wf import WavefunctionFile
+        with WavefunctionFile.load(path) as w:
+            w.to_state(self)
+            return w.header
+
+    def Start(self, recalc: bool = True):
         """Iteration-0 preparation of Evolve (src/Main.f90:177-231) for a run
         started from spinors with given energies: pairing step (HF filling or
         HFB), derivatives, densities, moments, potentials and, under HFB, the
-        canonical single-particle energies."""
+        canonical single-particle energies.  recalc=False keeps the densities
+        already set (a restart from a .wf file without Recalc,
+        src/Main.f90:213-215)."""
         hfb = self.p.pairing == _abi.MG_PAIRING_HFB
         if hfb:
             self.SolvePairing()
         else:
             self.HFFill()
         self.DeriveAll()
-        self.UpdateDensities()
+        if recalc:
+            self.UpdateDensities()
         # three times, as the reference does (src/Main.f90:219-221): the
         # moments' OldValue history then holds the start value thrice
         for _ in range(3):
