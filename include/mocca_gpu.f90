@@ -132,6 +132,14 @@ module mocca_gpu
     real(c_double) :: intensity
     integer(c_int) :: active
   end type mg_constraint_state
+  type, bind(C) :: mg_nilsson_params
+    integer(c_int) :: n_neutron
+    integer(c_int) :: meven
+    integer(c_int) :: modd
+    real(c_double) :: ho(3)
+    real(c_double) :: amplitude
+    integer(c_int) :: seed
+  end type mg_nilsson_params
   type, bind(C) :: mg_convergence
     real(c_double) :: energy_prec
     real(c_double) :: moment_prec
@@ -402,6 +410,16 @@ module mocca_gpu
       type(c_ptr), value :: a
       type(c_ptr), value :: s
       type(c_ptr), value :: diva
+    end function
+    integer(c_int) function mg_nilsson_start(ctx, np) bind(C, name="mg_nilsson_start")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: np
+    end function
+    integer(c_int) function mg_break_symmetries(ev8, full) bind(C, name="mg_break_symmetries")
+      import
+      type(c_ptr), value :: ev8
+      type(c_ptr), value :: full
     end function
     integer(c_int) function mg_symmetry_operators(ctx, basis, out) bind(C, name="mg_symmetry_operators")
       import

@@ -388,6 +388,31 @@ int mg_get_potentials(mg_ctx* ctx, double* u, double* b, double* nablab,
 int mg_get_time_odd(mg_ctx* ctx, double* vecj, double* vecs, double* rotj, double* rots,
                     double* a, double* s, double* diva);
 
+/* INITWF (src/InOut.f90:1418-1473) with nil8's Nilsson states
+ * (src/nil8.f90:16-546) for an EV8 context (nz >= nx, ny): the lowest
+ * n_neutron neutron and nwt - n_neutron proton levels of the deformed
+ * oscillator with l.s and l^2 terms in meven even and modd odd major shells
+ * (INITWF: 6 and 5, ho = 0.2 fm^-2 on every axis), positive parity first
+ * within each isospin, evaluated on the mesh on the device; then every
+ * grid value plus amplitude * u, u uniform in [-1, 1) from a generator
+ * keyed on (seed, spwf, component, point), and each spwf normalised.
+ * Sets the HF spinors, their quantum numbers and the Nilsson energies. */
+typedef struct mg_nilsson_params {
+    int    n_neutron;     /* stored neutron spwfs; the other nwt - n_neutron are protons */
+    int    meven, modd;   /* even / odd major shells of the basis                        */
+    double ho[3];         /* m omega / hbar per axis (fm^-2)                             */
+    double amplitude;     /* perturbation of every grid value (0: none)                  */
+    int    seed;
+} mg_nilsson_params;
+int mg_nilsson_start(mg_ctx* ctx, const mg_nilsson_params* np);
+
+/* BreakParity, BreakSignature, BreakTimeSimplex (src/Transform.f90:187-366),
+ * in TransformInput's order (:83-99), of every HF spwf of an EV8 context
+ * into a symmetry-free context (pc = sc = tsc = 0) with twice the points
+ * per axis, the same dx, nwt and time reversal: the full-box spinors, the
+ * isospins (the broken quantum numbers 0), occupations and energies. */
+int mg_break_symmetries(mg_ctx* ev8, mg_ctx* full);
+
 /* SymmetryOperators + CalcRMSRadius (src/Spwf.f90:2289-2347) for every spwf
  * of a basis: out[6*i + 0..5] = isospin, signature, parity, time simplex,
  * x-simplex expectation values and the RMS radius sqrt(<r^2>).  A conserved

@@ -156,6 +156,11 @@ class MgConvergence(C.Structure):
                 ("pairing_prec", C.c_double)]
 
 
+class MgNilssonParams(C.Structure):
+    _fields_ = [("n_neutron", C.c_int), ("meven", C.c_int), ("modd", C.c_int),
+                ("ho", C.c_double * 3), ("amplitude", C.c_double), ("seed", C.c_int)]
+
+
 class MgWfHeader(C.Structure):
     _fields_ = [
         ("version", C.c_int),
@@ -264,6 +269,8 @@ SIGNATURES = {
     "mg_wf_from_context": [_P, C.c_char_p, C.POINTER(_P)],
     "mg_wf_to_context": [_P, _P],
     "mg_angular_momentum": [_P, C.c_int, _D],
+    "mg_nilsson_start": [_P, C.POINTER(MgNilssonParams)],
+    "mg_break_symmetries": [_P, _P],
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmocca_gpu.so"

@@ -342,6 +342,24 @@ class MeshState:
         self._call("mg_get_pairing_field", _dptr(re), _dptr(im), _dptr(df))
         return re, im, df
 
+    def NilssonStart(self, n_neutron: int, meven: int = 6, modd: int = 5, ho=(0.2, 0.2, 0.2),
+                     amplitude: float = 0.0, seed: int = 1234):
+        """INITWF's Nilsson states (src/InOut.f90:1418-1473, src/nil8.f90:16-546)
+        built on the device, plus a seeded uniform perturbation of the given
+        amplitude and the normalisation of every spwf."""
+        npar = _abi.MgNilssonParams()
+        npar.n_neutron, npar.meven, npar.modd = n_neutron, meven, modd
+        for k in range(3):
+            npar.ho[k] = float(ho[k])
+        npar.amplitude, npar.seed = float(amplitude), int(seed)
+        self._call("mg_nilsson_start", C.byref(npar))
+
+    def BreakSymmetries(self, full: "MeshState"):
+        """BreakParity, BreakSignature, BreakTimeSimplex (src/Transform.f90:
+        187-366) of this EV8 state's HF spwfs into `full`, a symmetry-free
+        state with twice the points per axis."""
+        self._call("mg_break_symmetries", full.h)
+
     def AngularMomentum(self, basis: int = _abi.MG_HF_BASIS) -> np.ndarray:
         """DiagAng's <J> (src/Spwf.f90:976-1085) per spwf, [nwt, 3]."""
         out = np.empty(3 * self.p.nwt)
