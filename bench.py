@@ -659,6 +659,26 @@ def batched_64_uneven(torch, rounds=190, seq_rounds=5):
     q20 = [sum(s.get_constraint(0)["value"]) for s in states]
     rate = 64 * rounds / t_batch
     rate_seq = 64 * seq_rounds / t_seq
+    # INITWF's Nilsson start of the same 64 instances built on the device
+    # (mg_nilsson_start, into the finished states), against the numpy
+    # restatement with its upload for the first four (the batch itself
+    # starts from the HO states)
+    b.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d, s in zip(inst, states):
+        s.NilssonStart(d["n_neutron"], amplitude=1e-3, seed=d["seed"])
+    torch.cuda.synchronize()
+    t_nil_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for d, s in zip(inst[:4], states[:4]):
+        psi, qn, en = synthetic.nilsson_basis(d["params"], d["n_neutron"], seed=d["seed"])
+        s.set_spinors(psi, qn)
+        s.set_energies(en)
+    t_nil_host = (time.perf_counter() - t0) / 4
+    nilsson = {"device_ms_per_instance": t_nil_dev / 64 * 1e3,
+               "host_numpy_ms_per_instance": t_nil_host * 1e3,
+               "host_sample": "instances 0-3 (numpy restatement + upload)"}
     res = {
         "workload": "64 HFB instances, seed 7: beta2 ~ U[-0.3, 0.5] (Q20 constraint, alternating "
                     "kind, always on), N, Z even in [8, 40], n^3 EV8 stored meshes n in [12, 28] "
@@ -677,8 +697,8 @@ def batched_64_uneven(torch, rounds=190, seq_rounds=5):
         "energies_finite": bool(all(math.isfinite(o["total"]) for o in out)),
         "q20_rel_dev_max": float(max(abs(q - d["q20"]) / max(1.0, abs(d["q20"]))
                                      for q, d in zip(q20, inst))),
+        "nilsson_start": nilsson,
     }
-    b.close()
     for s in states:
         s.close()
     return res
