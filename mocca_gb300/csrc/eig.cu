@@ -355,6 +355,58 @@ __global__ void __launch_bounds__(kThreads) k_gemm64(const GemmDesc* __restrict_
     if (g.sym && gi < gj) g.C[(long)gj * g.ldc + gi] = v;
 }
 
+// The same GEMMs in double-float arithmetic for the mixed form: operands
+// split into FP32 pairs at the tile load (integer instructions, df_split),
+// products and sums with the exact FP32 error terms (df_acc, ~11 FP32
+// instructions per term), one FP64 add per output.  ~1e-14 relative like
+// the mixed form's Jacobi polish, at several times the rate of the FP64
+// pipe, which bounds k_gemm64 on GB300.
+__global__ void __launch_bounds__(kThreads) k_gemm_df(const GemmDesc* __restrict__ descs,
+                                                      SkipCtl sk) {
+    __shared__ float2 sA[kTile][kEigMax + 1];
+    __shared__ float2 sB[kEigMax + 1][kTile + 1];
+    const GemmDesc g = descs[blockIdx.y];
+    if (skip_step(sk, g.mat)) return;
+    const int tiles_n = (g.n + kTile - 1) / kTile;
+    const int ti = blockIdx.x / tiles_n, tj = blockIdx.x % tiles_n;
+    if (ti * kTile >= g.m || (g.sym && ti > tj)) return;
+    const int r = threadIdx.x / kTile, cidx = threadIdx.x % kTile;
+    for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
+        int i, kk;
+        if (g.ta) { i = q % kTile; kk = q / kTile; }
+        else { i = q / g.k; kk = q % g.k; }
+        const int gi = ti * kTile + i;
+        double x = 0.0;
+        if (gi < g.m) x = g.ta ? g.A[(long)kk * g.lda + gi] : g.A[(long)gi * g.lda + kk];
+        const dfl d = df_split(x);
+        sA[i][kk] = make_float2(d.h, d.l);
+    }
+    for (int q = threadIdx.x; q < kTile * g.k; q += kThreads) {
+        int kk, j;
+        if (g.tb) { kk = q % g.k; j = q / g.k; }
+        else { kk = q / kTile; j = q % kTile; }
+        const int gj = tj * kTile + j;
+        double x = 0.0;
+        if (gj < g.n) x = g.tb ? g.B[(long)gj * g.ldb + kk] : g.B[(long)kk * g.ldb + gj];
+        const dfl d = df_split(x);
+        sB[kk][j] = make_float2(d.h, d.l);
+    }
+    __syncthreads();
+    const int gi = ti * kTile + r, gj = tj * kTile + cidx;
+    if (gi >= g.m || gj >= g.n) return;
+    if (g.sym && gi > gj) return;
+    float sh = 0.0f, sl = 0.0f;
+    for (int kk = 0; kk < g.k; ++kk) {
+        const float2 a = sA[r][kk], b = sB[kk][cidx];
+        df_acc(sh, sl, dfl{a.x, a.y}, dfl{b.x, b.y});
+    }
+    const double s = df_to_fast(dfl{sh, sl});
+    double* c = g.C + (long)gi * g.ldc + gj;
+    const double v = g.beta == 0.0 ? g.alpha * s : fma(g.alpha, s, g.beta * *c);
+    *c = v;
+    if (g.sym && gi < gj) g.C[(long)gj * g.ldc + gi] = v;
+}
+
 // Ogita-Aishima correction, spread over one CTA per matrix row so that the
 // FP64 work (divisions included) runs on many SMs.  k_oa_rows: lambda_i =
 // s_ii / g_ii (into w) and the row sums of (S - diag lambda)^2 and
@@ -816,6 +868,14 @@ size_t jacobi_smem(int n) {
     return (size_t)(np <= kJSmemMax ? 3 : 2) * np * (np + 1) * sizeof(float);
 }
 
+// One launch of a GEMM table: double-float in the mixed form, FP64 otherwise.
+static void launch_gemm(mg_ctx* c, bool df, dim3 grid, const GemmDesc* descs, SkipCtl sk) {
+    if (df)
+        k_gemm_df<<<grid, kThreads, 0, c->stream>>>(descs, sk);
+    else
+        k_gemm64<<<grid, kThreads, 0, c->stream>>>(descs, sk);
+}
+
 // Eigen-decomposition of a batch (nb <= 64: the GEMM grids hold 2 nb
 // matrices in y) of symmetric matrices of sizes nsz (device) <= nmax, stored
 // with leading dimension ld and stride `stride`.  E.X: in/out (the warm start
@@ -844,16 +904,17 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     k_frob<<<E.nb, 1024, 0, c->stream>>>(E.A, E.stride, E.ld, E.nsz, E.anorm);
     MG_LAUNCHED(c);
     const int tiles = div_up(E.nmax, kTile) * div_up(E.nmax, kTile);
+    const bool dfg = c->cur_precision == MG_MIXED;
     const SkipCtl none{nullptr, nullptr, 0, 0, 0.0};
     if (E.skip_tol >= 0.0)
         MG_CUDA(cudaMemsetAsync(E.done, 0x7f, (size_t)E.nb * sizeof(int), c->stream));
     for (int s = 0; s < nref; ++s) {
         // AX = A X ; S = X^T AX ; G = X^T X ; F = I + E ; X2 = X F ; X <- X2
         SkipCtl sk{E.skip_tol >= 0.0 ? E.done : nullptr, E.offrel, s, 1, E.skip_tol};
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax, sk);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_ax, sk);
         MG_LAUNCHED(c);
         sk.decide = 0;
-        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, sk);
+        launch_gemm(c, dfg, dim3(tiles, 2 * E.nb), E.d_sg, sk);
         MG_LAUNCHED(c);
         k_oa_rows<<<dim3(E.nmax, E.nb), 128, 0, c->stream>>>(E.S, E.G, E.stride, E.ld, E.nsz,
                                                              E.w, E.wstride, E.part, sk);
@@ -862,7 +923,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
                                                               E.anorm, E.w, E.wstride, E.part,
                                                               E.emax, E.offrel, sk);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, sk);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_xf, sk);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
@@ -874,14 +935,14 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
     // of near-degenerate eigenvalues (density-matrix occupations ~1e-8 apart
     // near 0 or 1) can leave R ~ 1e-2, which one pass only brings to 1e-7.
     for (int pass = 0; pass < (polish ? 2 : 1); ++pass) {
-        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
+        launch_gemm(c, dfg, dim3(tiles, 2 * E.nb), E.d_sg, none);
         MG_LAUNCHED(c);
         k_orth_prep<<<dim3(div_up((long)E.nmax * E.nmax, kThreads), E.nb), kThreads, 0,
                       c->stream>>>(E.G, E.AX, E.G, E.stride, E.ld, E.nsz);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_rr, none);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_rr, none);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_xf, none);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
@@ -891,9 +952,9 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
         const size_t psm = (size_t)np * (np + 1) * sizeof(double);
         if (psm > (size_t)kSmemOptIn) return MG_ERR_ARG;
         // Rayleigh-Ritz matrix and the FP64 Jacobi polish
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_ax, none);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_ax, none);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, 2 * E.nb), kThreads, 0, c->stream>>>(E.d_sg, none);
+        launch_gemm(c, dfg, dim3(tiles, 2 * E.nb), E.d_sg, none);
         MG_LAUNCHED(c);
         if (c->cur_precision == MG_MIXED && E.nmax <= kDfPolishMax)
             k_jacobi_df_polish<<<E.nb, kJThreads, df_polish_smem(E.nmax), c->stream>>>(
@@ -902,7 +963,7 @@ int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish) {
             k_jacobi64_polish<<<E.nb, kJThreads, psm, c->stream>>>(
                 E.S, E.stride, E.ld, E.nsz, E.anorm, E.G, E.w, E.wstride, E.pfail, 12);
         MG_LAUNCHED(c);
-        k_gemm64<<<dim3(tiles, E.nb), kThreads, 0, c->stream>>>(E.d_xf, none);
+        launch_gemm(c, dfg, dim3(tiles, E.nb), E.d_xf, none);
         MG_LAUNCHED(c);
         MG_CUDA(cudaMemcpyAsync(E.X, E.X2, (size_t)E.nb * E.stride * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
@@ -965,11 +1026,12 @@ int gemm_batched_skip(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim, i
     return MG_OK;
 }
 
-// ndesc FP64 GEMMs of at most maxdim x maxdim from a device descriptor table.
-int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim) {
+// ndesc FP64 GEMMs of at most maxdim x maxdim from a device descriptor
+// table (double-float when df is set).
+int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim, bool df) {
     const SkipCtl none{nullptr, nullptr, 0, 0, 0.0};
     const int tiles = div_up(maxdim, kTile) * div_up(maxdim, kTile);
-    k_gemm64<<<dim3(tiles, ndesc), kThreads, 0, c->stream>>>(descs, none);
+    launch_gemm(c, df, dim3(tiles, ndesc), descs, none);
     MG_LAUNCHED(c);
     return MG_OK;
 }

@@ -608,12 +608,13 @@ static int taylor_launches(mg_ctx* c) {
     Hfb& H = c->hfb;
     const int hmax = H.hmax;
     const dim3 g(div_up(hmax * hmax, kThreads), 4);
-    MG_TRY(gemm_batched(c, H.d_taylor, 4, hmax));
+    const bool df = c->cur_precision == MG_MIXED;   // the mixed form's eigen GEMMs
+    MG_TRY(gemm_batched(c, H.d_taylor, 4, hmax, df));
     k_taylor_coef<<<g, kThreads, 0, c->stream>>>(H.tP, H.eT.w, H.eT.wstride, H.hsz, hmax, H.tC);
     MG_LAUNCHED(c);
-    MG_TRY(gemm_batched(c, H.d_taylor + 4, 8, hmax));
-    MG_TRY(gemm_batched(c, H.d_taylor + 12, 8, hmax));
-    MG_TRY(gemm_batched(c, H.d_taylor + 20, 4, hmax));
+    MG_TRY(gemm_batched(c, H.d_taylor + 4, 8, hmax, df));
+    MG_TRY(gemm_batched(c, H.d_taylor + 12, 8, hmax, df));
+    MG_TRY(gemm_batched(c, H.d_taylor + 20, 4, hmax, df));
     k_taylor_update<<<g, kThreads, 0, c->stream>>>(H.tZ, H.tK, H.hsz, hmax, H.nmax, H.dl_d,
                                                   H.rho, H.kappa);
     MG_LAUNCHED(c);
@@ -634,6 +635,10 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
     MG_CUDA(cudaMemcpyAsync(H.dl_d, hp + 26, 2 * sizeof(double), cudaMemcpyHostToDevice,
                             c->stream));
     if (H.no_graph) return taylor_launches(c);
+    if (H.taylor_graph && H.taylor_graph_prec != c->cur_precision) {
+        cudaGraphExecDestroy(H.taylor_graph);   // the two forms launch different GEMMs
+        H.taylor_graph = nullptr;
+    }
     if (!H.taylor_graph) {
         if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
@@ -655,6 +660,7 @@ static int taylor_finish(mg_ctx* c, const double dl[2]) {
             return MG_ERR_CUDA;
         }
         H.taylor_graph_launches = c->launches - l0;
+        H.taylor_graph_prec = c->cur_precision;
         c->launches = l0;
     }
     MG_CUDA(cudaGraphLaunch(H.taylor_graph, c->stream));

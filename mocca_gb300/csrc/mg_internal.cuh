@@ -147,6 +147,7 @@ struct Hfb {
     int eval_graph_prec[3] = {-1, -1, -1};   // precision form the graph was captured in
     cudaGraphExec_t taylor_graph = nullptr;   // first-order finish of the Fermi search
     long long taylor_graph_launches = 0;
+    int taylor_graph_prec = -1;
     double* dl_d = nullptr;                   // its steps per isospin
     double *oldrho_bak = nullptr, *oldkappa_bak = nullptr;   // mixing history before the last mix
     cudaGraphExec_t can_graph = nullptr;      // canonical-basis decomposition (warm seed)
@@ -410,7 +411,7 @@ int eig_setup(mg_ctx* c, EigBatch& E, int nb, int nmax, const int* nsz_dev, doub
 // the vectors in E.X, or refinement started directly from E.X.
 enum EigSeed { kSeedCold = 0, kSeedJacobiWarm = 1, kSeedRefine = 2 };
 int eig_batched(mg_ctx* c, EigBatch& E, int seed, int nref, bool polish);
-int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim);
+int gemm_batched(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim, bool df = false);
 int gemm_batched_skip(mg_ctx* c, const GemmDesc* descs, int ndesc, int maxdim, int* done);
 int hfb_evaluate_at(mg_ctx* c, const double* lam, double* N_out, double* dN_out);
 int fermi_gradient(mg_ctx* c, double lam[2], double f[2], bool conv[2], int* iters);
