@@ -224,8 +224,9 @@ int mg_synchronize(mg_ctx* ctx);
  * derivative contractions, the Gram-Schmidt overlap and apply, the pairing
  * gaps and the canonical-basis transform as exact BF16 digit products on the
  * tensor cores (47-bit operands), and h.psi, the densities and the pairing
- * field in double-float (FP32 pairs), with FP64 storage; the Cholesky
- * factor, energies, the HFB matrices and their diagonalisation stay FP64.
+ * field in double-float (FP32 pairs), with FP64 storage, and the small
+ * GEMMs and Jacobi polish of the HFB diagonalisation in double-float; the
+ * Cholesky factor, energies and the HFB matrices stay FP64.
  * No reference counterpart (the reference is FP64 throughout). */
 int mg_set_precision(mg_ctx* ctx, int precision);
 
