@@ -484,8 +484,10 @@ void hfb_free(mg_ctx* c) {
     if (H.h_pinned) cudaFreeHost(H.h_pinned);
     for (cudaGraphExec_t& g : H.eval_graph)
         if (g) cudaGraphExecDestroy(g);
-    if (H.can_graph) cudaGraphExecDestroy(H.can_graph);
-    H.can_graph = nullptr;
+    for (cudaGraphExec_t& g : H.can_graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
     if (H.taylor_graph) cudaGraphExecDestroy(H.taylor_graph);
     H.taylor_graph = nullptr;
     eig_free(H.eT);
@@ -711,7 +713,14 @@ static int fermi_newton(mg_ctx* c, double lam[2], double f[2], bool conv[2], int
     // (the root is the same; the first evaluation only lands closer to it)
     double fp[2];
     start_guess(H, lam);
-    MG_TRY(hfb_evaluate(c, lam, f, fp, true));
+    // The first evaluation starts from the FP32 Jacobi seed, except in the
+    // mixed form once the search has settled (the last step took one
+    // evaluation and the first-order finish): the previous vectors then
+    // refine in place in double-float, cheaper than the seed there (a
+    // refinement that falls short re-seeds itself).  In FP64 the refinement
+    // steps run on the slow FP64 pipe and the seed stays the cheaper start.
+    const bool refine = c->cur_precision == MG_MIXED && H.settled;
+    MG_TRY(hfb_evaluate(c, lam, f, fp, !refine));
     ++evals;
     conv[0] = std::fabs(f[0]) < prec;
     conv[1] = std::fabs(f[1]) < prec;
@@ -791,6 +800,7 @@ static int fermi_newton(mg_ctx* c, double lam[2], double f[2], bool conv[2], int
     }
     *evals_out = evals;
     *first_order_out = first_order;
+    H.settled = evals == 1 && first_order;
     return MG_OK;
 }
 
@@ -861,36 +871,41 @@ static int canonical_eig(mg_ctx* c) {
     if (!H.eR.have_vectors || H.no_graph) {
         return eig_batched(c, H.eR, H.eR.have_vectors ? kSeedJacobiWarm : kSeedCold, H.nref, true);
     }
-    if (H.can_graph && H.can_graph_prec != c->cur_precision) {
-        cudaGraphExecDestroy(H.can_graph);
-        H.can_graph = nullptr;
+    // as the Fermi search's first evaluation: the mixed form refines the
+    // last vectors in place once the search has settled
+    const int k = c->cur_precision == MG_MIXED && H.settled ? 1 : 0;
+    const int seed = k ? kSeedRefine : kSeedJacobiWarm;
+    cudaGraphExec_t& gr = H.can_graph[k];
+    if (gr && H.can_graph_prec[k] != c->cur_precision) {
+        cudaGraphExecDestroy(gr);
+        gr = nullptr;
     }
-    if (!H.can_graph) {
+    if (!gr) {
         if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
             H.no_graph = true;
-            return eig_batched(c, H.eR, kSeedJacobiWarm, H.nref, true);
+            return eig_batched(c, H.eR, seed, H.nref, true);
         }
         const long long l0 = c->launches;
-        const int st = eig_batched(c, H.eR, kSeedJacobiWarm, H.nref, true);
+        const int st = eig_batched(c, H.eR, seed, H.nref, true);
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
         if (st != MG_OK || ce != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
             return st != MG_OK ? st : MG_ERR_CUDA;
         }
-        const cudaError_t ie = cudaGraphInstantiate(&H.can_graph, graph, 0);
+        const cudaError_t ie = cudaGraphInstantiate(&gr, graph, 0);
         cudaGraphDestroy(graph);
         if (ie != cudaSuccess) {
-            H.can_graph = nullptr;
+            gr = nullptr;
             return MG_ERR_CUDA;
         }
-        H.can_graph_launches = c->launches - l0;
-        H.can_graph_prec = c->cur_precision;
+        H.can_graph_launches[k] = c->launches - l0;
+        H.can_graph_prec[k] = c->cur_precision;
         c->launches = l0;
     }
-    MG_CUDA(cudaGraphLaunch(H.can_graph, c->stream));
-    c->launches += H.can_graph_launches;
+    MG_CUDA(cudaGraphLaunch(gr, c->stream));
+    c->launches += H.can_graph_launches[k];
     return MG_OK;
 }
 

@@ -142,6 +142,7 @@ struct Hfb {
     int npp_iter = -1000;                      // its iteration
     int n_solved = 0;                          // consecutive converged solves
     long long reseeds = 0;                     // evaluations redone from a Jacobi seed
+    bool settled = false;                      // last search: one evaluation + first-order finish
     cudaGraphExec_t eval_graph[3] = {nullptr, nullptr, nullptr};  // per EigSeed
     long long eval_graph_launches[3] = {0, 0, 0};
     int eval_graph_prec[3] = {-1, -1, -1};   // precision form the graph was captured in
@@ -150,9 +151,9 @@ struct Hfb {
     int taylor_graph_prec = -1;
     double* dl_d = nullptr;                   // its steps per isospin
     double *oldrho_bak = nullptr, *oldkappa_bak = nullptr;   // mixing history before the last mix
-    cudaGraphExec_t can_graph = nullptr;      // canonical-basis decomposition (warm seed)
-    long long can_graph_launches = 0;
-    int can_graph_prec = -1;
+    cudaGraphExec_t can_graph[2] = {nullptr, nullptr};   // canonical-basis decomposition:
+    long long can_graph_launches[2] = {0, 0};            // [0] Jacobi warm seed,
+    int can_graph_prec[2] = {-1, -1};                    // [1] in-place refinement
     bool no_graph = false;
     bool fermi_hist[7] = {false, false, false, false, false, false, false};
     double epair[2] = {0.0, 0.0}, disp[2] = {0.0, 0.0};
