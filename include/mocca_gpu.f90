@@ -59,6 +59,7 @@ module mocca_gpu
     integer(c_int) :: com1body
     integer(c_int) :: com2body
     integer(c_int) :: cexchange
+    integer(c_int) :: j2terms
   end type mg_force
   type, bind(C) :: mg_skyrme_b
     real(c_double) :: B1
@@ -314,6 +315,16 @@ module mocca_gpu
       type(c_ptr), value :: nablaj
       type(c_ptr), value :: derrho
       type(c_ptr), value :: laprho
+    end function
+    integer(c_int) function mg_get_jmunu(ctx, jmunu) bind(C, name="mg_get_jmunu")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: jmunu
+    end function
+    integer(c_int) function mg_set_jmunu(ctx, jmunu) bind(C, name="mg_set_jmunu")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: jmunu
     end function
     integer(c_int) function mg_set_pairing(ctx, pp) bind(C, name="mg_set_pairing")
       import

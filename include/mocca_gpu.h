@@ -106,6 +106,8 @@ typedef struct mg_force {
     double hbm, e2, hbar;
     double nucleonmass[2];
     int    com1body, com2body, cexchange;
+    int    j2terms;      /* J2Terms: the central J^2 terms of t1, t2 and the tensor
+                            te, to in B14, B15 (B16, B17 follow te, to always) */
 } mg_force;
 
 /* The B-coefficients of the energy density (src/Force.f90:467-560). */
@@ -167,7 +169,8 @@ typedef struct mg_pairing_info {
 /* ---- host-side helpers (no device work) ---------------------------------- */
 
 /* B-coefficients from Skyrme parameters; replaces CalcEDFCoef
- * (src/Force.f90:467-560, TRC and J2Terms=.false. branch). */
+ * (src/Force.f90:467-560) up to B17 (the name-based overrides of SLy4T,
+ * SLy4Tmin and UNEDF2 aside). */
 int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* out);
 
 /* Lagrange derivative matrices for one axis; replaces IniLag + reduceLag
@@ -294,6 +297,11 @@ int mg_get_densities(mg_ctx* ctx, double* rho, double* tau, double* nablaj,
 int mg_set_densities(mg_ctx* ctx, const double* rho, const double* tau,
                      const double* nablaj, const double* derrho,
                      const double* laprho);
+/* The tensor density J_{mu nu} (src/Densities.f90:148, GetJMuNu
+ * src/Spwf.f90:2186-2204), 18V as [it][nu][mu][V]; only with J^2 terms
+ * (B14..B17 not all zero), MG_ERR_ARG otherwise. */
+int mg_get_jmunu(mg_ctx* ctx, double* jmunu);
+int mg_set_jmunu(mg_ctx* ctx, const double* jmunu);
 
 /* HFB pairing parameters (before the first mg_solve_pairing). */
 int mg_set_pairing(mg_ctx* ctx, const mg_pairing_params* pp);

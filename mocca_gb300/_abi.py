@@ -61,6 +61,7 @@ class MgForce(C.Structure):
         "te", "to", "wso", "wsoq", "hbm", "e2", "hbar")] + [
         ("nucleonmass", C.c_double * 2),
         ("com1body", C.c_int), ("com2body", C.c_int), ("cexchange", C.c_int),
+        ("j2terms", C.c_int),
     ]
 
 
@@ -225,6 +226,8 @@ SIGNATURES = {
     "mg_mix_densities": [_P],
     "mg_get_densities": [_P, _D, _D, _D, _D, _D],
     "mg_set_densities": [_P, _D, _D, _D, _D, _D],
+    "mg_get_jmunu": [_P, _D],
+    "mg_set_jmunu": [_P, _D],
     "mg_calculate_moments": [_P],
     "mg_add_constraint": [_P, C.POINTER(MgMomentConstraint)],
     "mg_get_constraint": [_P, C.c_int, C.POINTER(MgConstraintState)],

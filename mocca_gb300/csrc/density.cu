@@ -164,6 +164,66 @@ __global__ void k_dens_reduce(const double* __restrict__ part, int ngroups, long
     nablaj[v] = a[4]; nablaj[V + v] = a[5];
 }
 
+// The tensor density J_{mu nu}(it) = sum_i occ_i Im(psi_i^+ sigma_nu d_mu psi_i)
+// (GetJMuNu, src/Spwf.f90:2186-2204, summed as ComputeDensity does,
+// src/Densities.f90:486-490): one thread per mesh point, the spwfs in index
+// order, the derivatives FP64 or double-float; out [it][nu][mu][V].
+__device__ __forceinline__ double der_value(const double* p, long k, bool df) {
+    if (!df) return p[k];
+    const float2 hl = reinterpret_cast<const float2*>(p)[k];
+    return (double)hl.x + (double)hl.y;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_jmunu(const double* __restrict__ psi, const double* __restrict__ der, bool df,
+        const double* __restrict__ occ, const int* __restrict__ qn, int nwt, long V,
+        double* __restrict__ out) {
+    const long v = (long)blockIdx.x * kThreads + threadIdx.x;
+    if (v >= V) return;
+    double J[2][3][3];
+#pragma unroll
+    for (int it = 0; it < 2; ++it)
+#pragma unroll
+        for (int nu = 0; nu < 3; ++nu)
+#pragma unroll
+            for (int mu = 0; mu < 3; ++mu) J[it][nu][mu] = 0.0;
+    for (int i = 0; i < nwt; ++i) {
+        const double o = occ[i];
+        if (o == 0.0) continue;
+        const bool prot = qn[4 * i] > 0;
+        const double* p = psi + (long)i * 4 * V;
+        const double* d = der + (long)i * 12 * V;
+        const double a0 = p[v], a1 = p[V + v], a2 = p[2 * V + v], a3 = p[3 * V + v];
+#pragma unroll
+        for (int mu = 0; mu < 3; ++mu) {
+            const double g0 = der_value(d, (mu * 4 + 0) * V + v, df);
+            const double g1 = der_value(d, (mu * 4 + 1) * V + v, df);
+            const double g2 = der_value(d, (mu * 4 + 2) * V + v, df);
+            const double g3 = der_value(d, (mu * 4 + 3) * V + v, df);
+            // sigma_x g = (g2, g3, g0, g1); sigma_y g = (g3, -g2, -g1, g0);
+            // sigma_z g = (g0, g1, -g2, -g3); Im(a^+ b) = a0 b1 - a1 b0 + a2 b3 - a3 b2
+            const double jx = a0 * g3 - a1 * g2 + a2 * g1 - a3 * g0;
+            const double jy = a0 * -g2 - a1 * g3 + a2 * g0 - a3 * -g1;
+            const double jz = a0 * g1 - a1 * g0 + a2 * -g3 - a3 * -g2;
+            if (prot) {
+                J[1][0][mu] += o * jx;
+                J[1][1][mu] += o * jy;
+                J[1][2][mu] += o * jz;
+            } else {
+                J[0][0][mu] += o * jx;
+                J[0][1][mu] += o * jy;
+                J[0][2][mu] += o * jz;
+            }
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < 2; ++it)
+#pragma unroll
+        for (int nu = 0; nu < 3; ++nu)
+#pragma unroll
+            for (int mu = 0; mu < 3; ++mu) out[((it * 3 + nu) * 3 + mu) * V + v] = J[it][nu][mu];
+}
+
 }  // namespace
 
 int density_groups(const mg_ctx* c) {
@@ -192,6 +252,11 @@ int densities(mg_ctx* c) {
     MG_LAUNCHED(c);
     // grad rho, lap rho: the first two field jobs
     MG_TRY(run_jobs(c, c->field_jobs, 2));
+    if (c->tensor) {
+        k_jmunu<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(B.psi, B.der, B.der_df, B.occ,
+                                                                B.qn, c->p.nwt, V, c->jmunu);
+        MG_LAUNCHED(c);
+    }
     if (!c->p.trc) MG_TRY(time_odd_densities(c, B));
     return MG_OK;
 }

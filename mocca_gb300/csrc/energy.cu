@@ -2,9 +2,10 @@
 //
 // Device side: per-spwf <psi|lap psi> of the density basis (CompKinetic,
 // :1426-1456) and block partials of the mesh integrals of compSkyrme
-// (:623-860, time-even terms) and of the Coulomb direct / Slater exchange
-// energies (src/Coulomb.f90:215-253).  Host side: the block partials are
-// added in block order and combined exactly as CompEnergy / SpwfEnergy do.
+// (:623-860, time-even terms, the J^2 ones included) and of the Coulomb
+// direct / Slater exchange energies (src/Coulomb.f90:215-253).  Host side:
+// the block partials are added in block order and combined exactly as
+// CompEnergy / SpwfEnergy do.
 #include <cmath>
 #include <cstring>
 
@@ -16,7 +17,7 @@ namespace mg {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTerms = 20;
+constexpr int kTerms = 26;
 
 // per-spwf dot products over 4V, block partials (b as double-float pairs when
 // kBdf: the Laplacians of the mixed form)
@@ -57,7 +58,8 @@ struct ECoef {
 __global__ void __launch_bounds__(kThreads)
 k_energy_partial(const double* __restrict__ rho, const double* __restrict__ tau,
                  const double* __restrict__ laprho, const double* __restrict__ nablaj,
-                 const double* __restrict__ coul, ECoef k, long V, double* __restrict__ part) {
+                 const double* __restrict__ coul, const double* __restrict__ jm, ECoef k, long V,
+                 double* __restrict__ part) {
     double acc[kTerms];
 #pragma unroll
     for (int q = 0; q < kTerms; ++q) acc[q] = 0.0;
@@ -86,6 +88,26 @@ k_energy_partial(const double* __restrict__ rho, const double* __restrict__ tau,
         }
         acc[18] += rp * coul[v];                        // Coulomb direct
         acc[19] += rp * pow(rp, 1 / 3.0);               // Slater exchange
+        if (jm) {
+            // J^2 terms 19, 20, 23-26 (src/Energy.f90:763-810), J(m, n) of
+            // isospin q at jm[((q * 3 + n) * 3 + m) * V]
+            double tr[2] = {0.0, 0.0};
+            for (int m = 0; m < 3; ++m)
+                for (int n = 0; n < 3; ++n) {
+                    const double j0 = jm[((0 * 3 + n) * 3 + m) * V + v];
+                    const double j1 = jm[((1 * 3 + n) * 3 + m) * V + v];
+                    const double t0 = jm[((0 * 3 + m) * 3 + n) * V + v];   // J(n, m)
+                    const double t1 = jm[((1 * 3 + m) * 3 + n) * V + v];
+                    const double jt = j0 + j1;
+                    acc[20] += jt * jt;
+                    acc[24] += jt * (t0 + t1);
+                    acc[21] += j0 * j0 + j1 * j1;
+                    acc[25] += j0 * t0 + j1 * t1;
+                    if (m == n) { tr[0] += j0; tr[1] += j1; }
+                }
+            acc[22] += (tr[0] + tr[1]) * (tr[0] + tr[1]);
+            acc[23] += tr[0] * tr[0] + tr[1] * tr[1];
+        }
     }
     __shared__ double red[kThreads / 32];
     for (int q = 0; q < kTerms; ++q) {
@@ -155,7 +177,9 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     if (ndots + (size_t)nblk * kTerms > c->red_len) return MG_ERR_STATE;
     ECoef k{B.B4, B.B6, B.B8a, B.B8b, B.B9q, B.byt3a, B.byt3b, B.B7b};
     k_energy_partial<<<nblk, kThreads, 0, c->stream>>>(c->rho, c->tau, c->laprho, c->nablaj,
-                                                       c->coulomb, k, V, c->red + ndots);
+                                                       c->coulomb,
+                                                       c->tensor ? c->jmunu : nullptr, k, V,
+                                                       c->red + ndots);
     MG_LAUNCHED(c);
     std::vector<double> all(ndots + (size_t)nblk * kTerms);
     MG_CUDA(cudaMemcpyAsync(all.data(), c->red, all.size() * sizeof(double),
@@ -191,6 +215,14 @@ int energy(mg_ctx* c, mg_energy_terms* out) {
     t[11] = B.B9q * S[14] + B.B9q * S[15];
     t[32] = B.B7b * S[5];
     t[33] = B.B8b * S[16] + B.B8b * S[17];
+    if (c->tensor) {
+        t[18] = B.B14 * S[20];
+        t[19] = B.B15 * S[21];
+        t[22] = B.B16 * S[22];
+        t[23] = B.B17 * S[23];
+        t[24] = B.B16 * S[24];
+        t[25] = B.B17 * S[25];
+    }
     if (!c->p.trc) MG_TRY(time_odd_energy(c, t));
     for (int q = 0; q < 36; ++q) t[q] *= c->dv;
     double sk = 0.0;

@@ -4,7 +4,8 @@
 // MixingScheme 0):
 //   U  CalcUPot  src/MeanFields.f90:269-409 (time-even Skyrme part, Coulomb
 //      direct + Slater exchange on protons)
-//   W  CalcWPot  src/MeanFields.f90:494-597 (B9 spin-orbit part) and div W
+//   W  CalcWPot  src/MeanFields.f90:494-597 (the B9 spin-orbit part and the
+//      J^2 parts of B14..B17) and div W
 //      with the symmetry arguments of :575-591
 //   B  CalcBPot  src/MeanFields.f90:115-150 and grad B
 // One thread per mesh point computes U, B and the nine W components of both
@@ -25,6 +26,7 @@ constexpr int kThreads = 256;
 struct Coef {
     double B1, B2, B3, B4, B5, B6, B7a, B7b, B8a, B8b, byt3a, byt3b, B9, B9q;
     int cexchange;
+    double B14, B15, B16, B17;   // the J^2 terms (with jmunu)
 };
 
 __device__ __forceinline__ int levi(int i, int j, int k) {
@@ -38,8 +40,8 @@ __global__ void __launch_bounds__(kThreads)
 k_potentials(const double* __restrict__ rho, const double* __restrict__ tau,
              const double* __restrict__ nablaj, const double* __restrict__ derrho,
              const double* __restrict__ laprho, const double* __restrict__ coul,
-             const double* __restrict__ coulex, const double* __restrict__ cons, Coef B, long V,
-             double* __restrict__ U,
+             const double* __restrict__ coulex, const double* __restrict__ cons,
+             const double* __restrict__ jm, Coef B, long V, double* __restrict__ U,
              double* __restrict__ Bp, double* __restrict__ W) {
     const long v = (long)blockIdx.x * kThreads + threadIdx.x;
     if (v >= V) return;
@@ -84,6 +86,23 @@ k_potentials(const double* __restrict__ rho, const double* __restrict__ tau,
                     const int e = levi(k, m, n);
                     w = w - e * ((B.B9 + B.B9q) * derrho[(it * 3 + k - 1) * V + v] +
                                  B.B9 * derrho[((1 - it) * 3 + k - 1) * V + v]);
+                }
+                if (jm) {
+                    // CalcWPot's J^2 parts (src/MeanFields.f90:531-556) in its
+                    // order: B14, B15 on J(m, n); B16, B17 on J(n, m), then
+                    // on the traces along the diagonal
+                    auto J = [&](int q, int a, int b) {   // J(a, b) of isospin q
+                        return jm[((q * 3 + b - 1) * 3 + a - 1) * V + v];
+                    };
+                    const int at = 1 - it;
+                    if (B.B14 != 0.0 || B.B15 != 0.0)
+                        w = w + 2.0 * (B.B14 + B.B15) * J(it, m, n) + 2.0 * B.B14 * J(at, m, n);
+                    if (B.B16 != 0.0 || B.B17 != 0.0) {
+                        w = w + 2.0 * (B.B16 + B.B17) * J(it, n, m) + 2.0 * B.B16 * J(at, n, m);
+                        if (m == n)
+                            for (int k = 1; k <= 3; ++k)
+                                w = w + 2 * (B.B16 + B.B17) * J(it, k, k) + 2 * B.B16 * J(at, k, k);
+                    }
                 }
                 W[((it * 3 + n - 1) * 3 + m - 1) * V + v] = w;
             }
@@ -179,10 +198,12 @@ int build_field_jobs(mg_ctx* c) {
 int potentials(mg_ctx* c) {
     const long V = c->V;
     Coef k{c->B.B1, c->B.B2, c->B.B3, c->B.B4, c->B.B5, c->B.B6, c->B.B7a, c->B.B7b, c->B.B8a,
-           c->B.B8b, c->B.byt3a, c->B.byt3b, c->B.B9, c->B.B9q, c->f.cexchange};
+           c->B.B8b, c->B.byt3a, c->B.byt3b, c->B.B9, c->B.B9q, c->f.cexchange,
+           c->B.B14, c->B.B15, c->B.B16, c->B.B17};
     k_potentials<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(
         c->rho, c->tau, c->nablaj, c->derrho, c->laprho, c->coulomb, c->coulex,
-        c->cons.list.empty() ? nullptr : c->cons.field, k, V, c->U, c->Bp, c->W);
+        c->cons.list.empty() ? nullptr : c->cons.field, c->tensor ? c->jmunu : nullptr, k, V,
+        c->U, c->Bp, c->W);
     MG_LAUNCHED(c);
     MG_TRY(run_jobs(c, c->field_jobs + 2, c->n_field_jobs - 2));
     k_sum3<<<div_up(6 * V, kThreads), kThreads, 0, c->stream>>>(c->divw_tmp, 6 * V, c->divW);

@@ -42,7 +42,7 @@ void free_all(mg_ctx* c) {
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast); F(c->cguess);
-    F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs);
+    F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
     F(c->odd); F(c->odd_hist); F(c->Apot); F(c->Spot); F(c->divA); F(c->odd_der); F(c->odd_tmp);
     F(c->odd_jobs);
     multigrid_free(c->mgrid);
@@ -68,7 +68,7 @@ void free_all(mg_ctx* c) {
 // Host helpers
 // ---------------------------------------------------------------------------
 extern "C" int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* B) {
-    // CalcEDFCoef, src/Force.f90:467-560 (J2Terms = .false.)
+    // CalcEDFCoef, src/Force.f90:467-560
     if (!f || !B) return MG_ERR_ARG;
     std::memset(B, 0, sizeof(*B));
     B->B1 = f->t0 * (1.0 + 0.5 * f->x0) / 2.0;
@@ -92,6 +92,15 @@ extern "C" int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* B
         B->B13a = -f->t3a / 24.0;
         B->B12b = f->t3b * f->x3b / 24.0;
         B->B13b = -f->t3b / 24.0;
+    }
+    if (f->j2terms) {
+        // central J^2 terms of t1, t2 plus the tensor part
+        const double C14 = -(1.0 / 8.0) * (f->t1 * f->x1 + f->t2 * f->x2);
+        const double C15 = (1.0 / 8.0) * (f->t1 - f->t2);
+        const double T14 = (1.0 / 4.0) * (f->te + f->to);
+        const double T15 = -(1.0 / 4.0) * (f->te - f->to);
+        B->B14 = C14 + T14;
+        B->B15 = C15 + T15;
     }
     B->B16 = -(3.0 / 8.0) * (f->te + f->to);
     B->B17 = (3.0 / 8.0) * (f->te - f->to);
@@ -164,6 +173,14 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     if ((p->sc && p->omega[0] != 0.0) || (p->tsc && p->omega[1] != 0.0)) return MG_ERR_ARG;
     if (!p->trc && (!ev8 || p->precision != MG_FP64 || p->pairing != MG_PAIRING_HF))
         return MG_ERR_ARG;
+    {
+        // the J^2 (tensor) terms: time-even only (their time-odd partners T,
+        // F and the C, D fields are not built)
+        mg_skyrme_b tb;
+        mg_skyrme_coefficients(f, p->trc, &tb);
+        if ((tb.B14 != 0.0 || tb.B15 != 0.0 || tb.B16 != 0.0 || tb.B17 != 0.0) && !p->trc)
+            return MG_ERR_ARG;
+    }
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     mg_ctx* c = new mg_ctx();
@@ -171,6 +188,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     c->p = *p;
     c->f = *f;
     mg_skyrme_coefficients(f, p->trc, &c->B);
+    c->tensor = c->B.B14 != 0.0 || c->B.B15 != 0.0 || c->B.B16 != 0.0 || c->B.B17 != 0.0;
     c->nx = p->nx; c->ny = p->ny; c->nz = p->nz;
     c->V = (long)p->nx * p->ny * p->nz;
     const int nsym = (p->pc ? 1 : 0) + (p->sc ? 1 : 0) + (p->tsc ? 1 : 0);
@@ -219,12 +237,13 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
          A(&c->nablaj, 2 * V) && A(&c->derrho, 6 * V) && A(&c->laprho, 2 * V) &&
          A(&c->U, 2 * V) && A(&c->Bp, 2 * V) && A(&c->nablaB, 6 * V) && A(&c->W, 18 * V) &&
          A(&c->divW, 6 * V) && A(&c->divw_tmp, 18 * V) && A(&c->coulomb, V) && A(&c->coulex, V);
+    if (ok && c->tensor) ok = A(&c->jmunu, 18 * V) && A(&c->jmunu_hist, 18 * V);
     if (!ok) return fail(MG_ERR_CUDA);
     // reduction scratch: the largest of the per-kernel partial tables
     const long hp = nwt * div_up(V, 256) * 2;
     const long dens = (long)density_groups(c) * 6 * V;
     const long dots = 64 * nwt;
-    const long en = 2L * c->num_sms * 20 + 4L * c->num_sms;
+    const long en = 2L * c->num_sms * 26 + 4L * c->num_sms;
     c->red_len = (size_t)std::max(std::max(hp, dens), dots + en);   // energy uses both
     if (!A(&c->red, (long)c->red_len)) return fail(MG_ERR_CUDA);
     if (cudaMalloc(&c->flags, 16 * sizeof(int)) != cudaSuccess ||
@@ -499,6 +518,20 @@ extern "C" int mg_get_densities(mg_ctx* c, double* rho, double* tau, double* nab
     MG_TRY(copy_out(c, nablaj, c->nablaj, 2 * V));
     MG_TRY(copy_out(c, derrho, c->derrho, 6 * V));
     MG_TRY(copy_out(c, laprho, c->laprho, 2 * V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_get_jmunu(mg_ctx* c, double* jmunu) {
+    if (!c || !jmunu || !c->tensor) return MG_ERR_ARG;
+    MG_TRY(copy_out(c, jmunu, c->jmunu, 18 * c->V));
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return MG_OK;
+}
+
+extern "C" int mg_set_jmunu(mg_ctx* c, const double* jmunu) {
+    if (!c || !jmunu || !c->tensor) return MG_ERR_ARG;
+    MG_TRY(copy_in(c, c->jmunu, jmunu, 18 * c->V));
     MG_CUDA(cudaStreamSynchronize(c->stream));
     return MG_OK;
 }

@@ -309,6 +309,10 @@ struct mg_ctx {
 
     // mixing between iterations (mixing.cu)
     double* dhist = nullptr;           // previous densities: rho, tau, nablaj, derrho, laprho (14V)
+    // the tensor density J_{mu nu} [it][nu][mu][V] and its history, when any
+    // of B14..B17 is not zero (time reversal conserved)
+    bool tensor = false;
+    double *jmunu = nullptr, *jmunu_hist = nullptr;
     bool have_dhist = false;
     double* Uold = nullptr;            // UpotOld (2V)
     // time-odd densities and fields without time reversal (timeodd.cu):

@@ -155,6 +155,9 @@ int save_density_history(mg_ctx* c) {
     if (c->odd)
         MG_CUDA(cudaMemcpyAsync(c->odd_hist, c->odd, 24 * V * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
+    if (c->tensor)
+        MG_CUDA(cudaMemcpyAsync(c->jmunu_hist, c->jmunu, 18 * V * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
     c->have_dhist = true;
     return MG_OK;
 }
@@ -174,6 +177,11 @@ int mix_densities(mg_ctx* c) {
     if (c->odd) {   // the time-odd densities mix with the rest
         k_mix<<<div_up(24 * V, kThreads), kThreads, 0, c->stream>>>(c->odd, c->odd_hist, 24 * V,
                                                                     c->p.damping);
+        MG_LAUNCHED(c);
+    }
+    if (c->tensor) {   // and J_{mu nu}
+        k_mix<<<div_up(18 * V, kThreads), kThreads, 0, c->stream>>>(c->jmunu, c->jmunu_hist,
+                                                                    18 * V, c->p.damping);
         MG_LAUNCHED(c);
     }
     return MG_OK;

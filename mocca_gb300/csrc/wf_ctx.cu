@@ -184,6 +184,7 @@ int from_context(mg_ctx* c, const char* force_name, mg_wf& w) {
     h.fermi[1] = c->hfb.fermi[1];
     for (int k = 0; k < 3; ++k) h.omega[k] = c->p.omega[k];
     h.odd_records = (!c->p.trc && c->odd) ? 1 : 0;   // vecj, rotvecj
+    h.has_jmunu = c->tensor ? 1 : 0;
     h.n_moments = 0;
     for (const MomentConstraint& k : c->cons.list) h.n_moments += k.type != 0;
     // an HF context writes GuessHFBMatrices(0)'s CanTransfo(HFBSize,HFBSize,2,2)
@@ -224,6 +225,7 @@ int from_context(mg_ctx* c, const char* force_name, mg_wf& w) {
     MG_TRY(mg_get_densities(c, w.d[MG_WF_RHO].data(), w.d[MG_WF_TAU].data(),
                             w.d[MG_WF_NABLAJ].data(), w.d[MG_WF_DERRHO].data(),
                             w.d[MG_WF_LAPRHO].data()));
+    if (h.has_jmunu) MG_TRY(mg_get_jmunu(c, w.d[MG_WF_JMUNU].data()));
     if (h.odd_records & 1) {
         double* o = w.d[MG_WF_ODD1].data();
         MG_TRY(mg_get_time_odd(c, o, nullptr, o + 6 * V, nullptr, nullptr, nullptr, nullptr));
@@ -306,6 +308,16 @@ int to_context(mg_ctx* c, const mg_wf& w) {
     MG_TRY(mg_set_densities(c, w.d[MG_WF_RHO].data(), w.d[MG_WF_TAU].data(),
                             w.d[MG_WF_NABLAJ].data(), w.d[MG_WF_DERRHO].data(),
                             w.d[MG_WF_LAPRHO].data()));
+    // JMuNu as ReadDensity takes it: from the file when there, else zero
+    if (c->tensor) {
+        std::vector<double> zero;
+        const double* j = w.d[MG_WF_JMUNU].data();
+        if (!h.has_jmunu) {
+            zero.assign((size_t)18 * V, 0.0);
+            j = zero.data();
+        }
+        MG_TRY(mg_set_jmunu(c, j));
+    }
     if (hfb) {
         Hfb& H = c->hfb;
         const int m = h.hfb_size;

@@ -39,6 +39,7 @@ class Force:
     com1body: int = 0
     com2body: int = 0
     cexchange: int = 2
+    j2terms: bool = False     # J2Terms: J^2 terms in B14, B15 (tensor te, to)
     name: str = ""            # afor, the &skf group's name (written to .wf files)
 
     def to_c(self) -> _abi.MgForce:
@@ -52,8 +53,15 @@ class Force:
             m = (avg, avg)
         f.nucleonmass[0], f.nucleonmass[1] = m
         f.com1body, f.com2body, f.cexchange = self.com1body, self.com2body, self.cexchange
+        f.j2terms = int(bool(self.j2terms))
         return f
 
+
+# &skf "SLy5colo" (forces.param:145-154): SLy5 with the tensor te = 296,
+# to = -136 MeV fm^5 and J2Terms = T.
+SLY5_TENSOR = Force(t0=-2484.880, x0=0.778, t1=483.130, x1=-0.328, t2=-549.400, x2=-1.0,
+                    t3a=13763.0, x3a=1.267, yt3a=0.1666666666666667, wso=126.0, wsoq=126.0,
+                    te=296.0, to=-136.0, j2terms=True, com1body=2, name="SLy5colo")
 
 SLY4 = Force(t0=-2488.913, x0=0.834, t1=486.818, x1=-0.344, t2=-546.395, x2=-1.0,
              t3a=13777.0, x3a=1.354, yt3a=0.166666666666666666667, t3b=0.0, x3b=0.0,

@@ -167,6 +167,12 @@ class MeshState:
                                          ("rho", "tau", "nablaj", "derrho", "laprho")))
         return out
 
+    def get_jmunu(self) -> np.ndarray:
+        """J_{mu nu} [it][nu][mu][V] (forces with J^2 terms only)."""
+        out = np.empty(18 * self.V)
+        self._call("mg_get_jmunu", _dptr(out))
+        return out
+
     def set_densities(self, rho=None, tau=None, nablaj=None, derrho=None, laprho=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
                 for a in (rho, tau, nablaj, derrho, laprho)]

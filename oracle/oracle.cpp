@@ -71,6 +71,10 @@ struct orc_ctx {
     // time-odd densities without time reversal (src/Densities.f90:39-94):
     // vecj, vecs, their curls [it][m][V], and their history for the mixing
     std::vector<double> vecj, vecs, rotj, rots, hvecj, hvecs, hrotj, hrots;
+    // the tensor density J_{mu nu} [it][nu][mu][V] (src/Densities.f90:148)
+    // when B14..B17 are not all zero, and its history
+    bool tensor = false;
+    std::vector<double> jmunu, hjmunu;
     // time-odd fields (src/MeanFields.f90:79-85): A, S [it][m][V], div A [it][V]
     std::vector<double> Apot, Spot, divA;
     // potentials (src/MeanFields.f90:79-85)
@@ -153,6 +157,15 @@ extern "C" int orc_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* 
         B->B13a = -f->t3a / 24.0;
         B->B12b = f->t3b * f->x3b / 24.0;
         B->B13b = -f->t3b / 24.0;
+    }
+    if (f->j2terms) {
+        // central J^2 terms of t1, t2 plus the tensor part
+        const double C14 = -(1.0 / 8.0) * (f->t1 * f->x1 + f->t2 * f->x2);
+        const double C15 = (1.0 / 8.0) * (f->t1 - f->t2);
+        const double T14 = (1.0 / 4.0) * (f->te + f->to);
+        const double T15 = -(1.0 / 4.0) * (f->te - f->to);
+        B->B14 = C14 + T14;
+        B->B15 = C15 + T15;
     }
     B->B16 = -(3.0 / 8.0) * (f->te + f->to);
     B->B17 = (3.0 / 8.0) * (f->te - f->to);
@@ -339,6 +352,8 @@ extern "C" orc_ctx* orc_create(const mg_params* p, const mg_force* f) {
     c->derrho.assign(6 * V, 0); c->laprho.assign(2 * V, 0);
     c->U.assign(2 * V, 0); c->Bp.assign(2 * V, 0); c->nablaB.assign(6 * V, 0);
     c->W.assign(18 * V, 0); c->divW.assign(6 * V, 0);
+    c->tensor = c->B.B14 != 0.0 || c->B.B15 != 0.0 || c->B.B16 != 0.0 || c->B.B17 != 0.0;
+    if (c->tensor) c->jmunu.assign(18 * V, 0.0);
     c->coulomb.assign(V, 0); c->coulex.assign(V, 0);
     if (!p->trc)
         for (auto* x : {&c->vecj, &c->vecs, &c->rotj, &c->rots, &c->Apot, &c->Spot})
@@ -804,6 +819,8 @@ extern "C" int orc_update_densities(orc_ctx* c) {
     c->hrho = c->rho; c->htau = c->tau; c->hnablaj = c->nablaj;
     c->hderrho = c->derrho; c->hlaprho = c->laprho;
     c->hvecj = c->vecj; c->hvecs = c->vecs; c->hrotj = c->rotj; c->hrots = c->rots;
+    c->hjmunu = c->jmunu;
+    if (c->tensor) std::fill(c->jmunu.begin(), c->jmunu.end(), 0.0);
     const bool odd = !c->p.trc;
     if (odd) {
         std::fill(c->vecj.begin(), c->vecj.end(), 0.0);
@@ -841,6 +858,16 @@ extern "C" int orc_update_densities(orc_ctx* c) {
                 nj = nj + double(trip[q][3]) * imag_mult(d[trip[q][0] - 1], s);
             }
             c->nablaj[it * V + v] = c->nablaj[it * V + v] + occ * nj;
+            if (c->tensor) {
+                // GetJMuNu (src/Spwf.f90:2186-2204): Im(psi^+ sigma_nu d_mu psi)
+                for (int nu = 0; nu < 3; ++nu)
+                    for (int mu = 0; mu < 3; ++mu) {
+                        double s[4];
+                        pauli(d[mu], nu + 1, s);
+                        double& J = c->jmunu[((it * 3 + nu) * 3 + mu) * V + v];
+                        J = J + occ * imag_mult(p, s);
+                    }
+            }
             if (odd) {
                 // GetVecj: Im(psi^+ d_m psi); GetVecs: Re(psi^+ sigma_m psi)
                 // (src/Spwf.f90:2034-2085)
@@ -880,6 +907,7 @@ extern "C" int orc_mix_densities(orc_ctx* c) {
     mix(c->rho, c->hrho); mix(c->tau, c->htau); mix(c->nablaj, c->hnablaj);
     mix(c->derrho, c->hderrho); mix(c->laprho, c->hlaprho);
     mix(c->vecj, c->hvecj); mix(c->vecs, c->hvecs); mix(c->rotj, c->hrotj); mix(c->rots, c->hrots);
+    mix(c->jmunu, c->hjmunu);
     return MG_OK;
 }
 
@@ -963,6 +991,12 @@ extern "C" int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* n
     cp(rho, c->rho); cp(tau, c->tau); cp(nablaj, c->nablaj); cp(derrho, c->derrho); cp(laprho, c->laprho);
     return MG_OK;
 }
+extern "C" int orc_get_jmunu(orc_ctx* c, double* jmunu) {
+    if (!c || !jmunu || !c->tensor) return MG_ERR_ARG;
+    std::copy(c->jmunu.begin(), c->jmunu.end(), jmunu);
+    return MG_OK;
+}
+
 extern "C" int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
                                  const double* nablaj, const double* derrho, const double* laprho) {
     if (!c) return MG_ERR_ARG;
@@ -1532,6 +1566,39 @@ static void calc_potentials(orc_ctx* c) {
                     for (long v = 0; v < V; ++v)
                         w[v] = w[v] - e * ((B.B9 + B.B9q) * dq[v] + B.B9 * dqa[v]);
                 }
+    if (c->tensor) {
+        // CalcWPot's J^2 parts (src/MeanFields.f90:531-556): B14, B15 on
+        // J_{mu nu}; B16, B17 on J_{nu mu} and on the trace times delta
+        const double* J = c->jmunu.data();
+        auto jm = [&](int it, int m, int n, long v) {   // J(m, n, it), 1-based m, n
+            return J[((it * 3 + (n - 1)) * 3 + (m - 1)) * V + v];
+        };
+        for (int it = 0; it < 2; ++it) {
+            const int at = 1 - it;
+            for (int m = 1; m <= 3; ++m)
+                for (int n = 1; n <= 3; ++n) {
+                    double* w = &c->W[((it * 3 + (n - 1)) * 3 + (m - 1)) * V];
+                    if (B.B14 != 0.0 || B.B15 != 0.0)
+                        for (long v = 0; v < V; ++v)
+                            w[v] = w[v] + 2.0 * (B.B14 + B.B15) * jm(it, m, n, v) +
+                                   2.0 * B.B14 * jm(at, m, n, v);
+                }
+            if (B.B16 != 0.0 || B.B17 != 0.0)
+                for (int m = 1; m <= 3; ++m) {
+                    for (int n = 1; n <= 3; ++n) {
+                        double* w = &c->W[((it * 3 + (n - 1)) * 3 + (m - 1)) * V];
+                        for (long v = 0; v < V; ++v)
+                            w[v] = w[v] + 2.0 * (B.B16 + B.B17) * jm(it, n, m, v) +
+                                   2.0 * B.B16 * jm(at, n, m, v);
+                    }
+                    double* w = &c->W[((it * 3 + (m - 1)) * 3 + (m - 1)) * V];
+                    for (int k = 1; k <= 3; ++k)
+                        for (long v = 0; v < V; ++v)
+                            w[v] = w[v] + 2 * (B.B16 + B.B17) * jm(it, k, k, v) +
+                                   2 * B.B16 * jm(at, k, k, v);
+                }
+        }
+    }
     // div W with the symmetry arguments of src/MeanFields.f90:575-591
     std::vector<double> t1(V), t2(V), t3(V);
     struct Term { int dir, m, n, P, S, TS, comp; };
@@ -1734,6 +1801,36 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
         t[4] = -B.B3 * j2; t[5] = q6; t[12] = B.B9 * jrs; t[13] = q14;
         t[14] = B.B10 * s2t; t[15] = q16; t[16] = B.B12a * s2a; t[17] = q18;
         t[34] = B.B12b * s2b; t[35] = q36;
+    }
+    if (c->tensor) {
+        // J^2 terms 19, 20, 23-26 of compSkyrme (src/Energy.f90:763-810)
+        const double* J = c->jmunu.data();
+        auto jm = [&](int it, int m, int n, long v) {
+            return J[((it * 3 + n) * 3 + m) * V + v];
+        };
+        double s19 = 0, s20 = 0, s23 = 0, s24 = 0, s25 = 0, s26 = 0;
+        for (long v = 0; v < V; ++v)
+            for (int m = 0; m < 3; ++m)
+                for (int n = 0; n < 3; ++n) {
+                    const double jt = jm(0, m, n, v) + jm(1, m, n, v);
+                    s19 += jt * jt;
+                    s25 += jt * (jm(0, n, m, v) + jm(1, n, m, v));
+                    for (int it = 0; it < 2; ++it) {
+                        s20 += jm(it, m, n, v) * jm(it, m, n, v);
+                        s26 += jm(it, m, n, v) * jm(it, n, m, v);
+                    }
+                }
+        for (long v = 0; v < V; ++v) {
+            double trt = 0.0;
+            for (int it = 0; it < 2; ++it) {
+                const double tr = jm(it, 0, 0, v) + jm(it, 1, 1, v) + jm(it, 2, 2, v);
+                s24 += tr * tr;
+                trt += tr;
+            }
+            s23 += trt * trt;
+        }
+        t[18] = B.B14 * s19; t[19] = B.B15 * s20; t[22] = B.B16 * s23;
+        t[23] = B.B17 * s24; t[24] = B.B16 * s25; t[25] = B.B17 * s26;
     }
     t[0] = B.B1 * s1; t[1] = B.B2 * s2; t[2] = B.B3 * s3; t[3] = s4;
     t[6] = B.B5 * s7; t[7] = s8; t[8] = B.B7a * s9; t[9] = s10;

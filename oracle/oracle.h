@@ -59,6 +59,7 @@ int orc_update_densities(orc_ctx* c);
 int orc_mix_densities(orc_ctx* c);
 int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* nablaj,
                       double* derrho, double* laprho);
+int orc_get_jmunu(orc_ctx* c, double* jmunu);   /* 18V: [it][nu][mu][V] */
 int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
                       const double* nablaj, const double* derrho,
                       const double* laprho);

@@ -50,6 +50,7 @@ _SIG = {
     "orc_mix_densities": ([_P], C.c_int),
     "orc_get_densities": ([_P, _D, _D, _D, _D, _D], C.c_int),
     "orc_set_densities": ([_P, _D, _D, _D, _D, _D], C.c_int),
+    "orc_get_jmunu": ([_P, _D], C.c_int),
     "orc_calculate_moments": ([_P], C.c_int),
     "orc_get_moments": ([_P, _D, _I, C.c_int], C.c_int),
     "orc_add_constraint": ([_P, C.POINTER(_abi.MgMomentConstraint)], C.c_int),
@@ -190,6 +191,11 @@ class OracleState:
                (("rho", 2), ("tau", 2), ("nablaj", 2), ("derrho", 6), ("laprho", 2))}
         self._call("orc_get_densities", *(_d(out[k]) for k in
                                           ("rho", "tau", "nablaj", "derrho", "laprho")))
+        return out
+
+    def get_jmunu(self) -> np.ndarray:
+        out = np.empty(18 * self.V)
+        self._call("orc_get_jmunu", _d(out))
         return out
 
     def set_densities(self, rho=None, tau=None, nablaj=None, derrho=None, laprho=None):

@@ -63,12 +63,47 @@ def test_invalid_arguments_are_rejected(built):
     assert not ctx.value
 
 
-def test_skyrme_coefficients_match_oracle(built):
+@pytest.mark.parametrize("force", ["SLY4", "SLY5_TENSOR"])
+@pytest.mark.parametrize("trc", [1, 0])
+def test_skyrme_coefficients_match_oracle(built, force, trc):
+    import mocca_gb300.forces as F
+    f = getattr(F, force).to_c()
     a, b = _abi.MgSkyrmeB(), _abi.MgSkyrmeB()
-    assert _abi.load().mg_skyrme_coefficients(SLY4.to_c(), 1, a) == 0
-    assert O.load().orc_skyrme_coefficients(SLY4.to_c(), 1, b) == 0
+    assert _abi.load().mg_skyrme_coefficients(f, trc, a) == 0
+    assert O.load().orc_skyrme_coefficients(f, trc, b) == 0
     for name, _ in _abi.MgSkyrmeB._fields_:
         assert getattr(a, name) == pytest.approx(getattr(b, name), rel=1e-15, abs=0), name
+
+
+def test_tensor_coefficients():
+    """CalcEDFCoef's J^2 coefficients (src/Force.f90:526-537) for SLy5colo
+    (t1, x1, t2, x2 and te = 296, to = -136 MeV fm^5 of forces.param):
+    B14 = -(t1 x1 + t2 x2)/8 + (te + to)/4, B15 = (t1 - t2)/8 - (te - to)/4,
+    B16 = -3 (te + to)/8, B17 = 3 (te - to)/8; without J2Terms only B16, B17."""
+    import dataclasses
+    from mocca_gb300.forces import SLY5_TENSOR as T
+    a = _abi.MgSkyrmeB()
+    assert _abi.load().mg_skyrme_coefficients(T.to_c(), 1, a) == 0
+    assert a.B14 == pytest.approx(-(T.t1 * T.x1 + T.t2 * T.x2) / 8 + (T.te + T.to) / 4, rel=1e-14)
+    assert a.B15 == pytest.approx((T.t1 - T.t2) / 8 - (T.te - T.to) / 4, rel=1e-14)
+    assert a.B16 == pytest.approx(-3 * (T.te + T.to) / 8, rel=1e-14)
+    assert a.B17 == pytest.approx(3 * (T.te - T.to) / 8, rel=1e-14)
+    b = _abi.MgSkyrmeB()
+    assert _abi.load().mg_skyrme_coefficients(dataclasses.replace(T, j2terms=False).to_c(), 1,
+                                              b) == 0
+    assert b.B14 == 0.0 and b.B15 == 0.0 and b.B16 == a.B16 and b.B17 == a.B17
+
+
+def test_tensor_terms_need_time_reversal(built):
+    """The J^2 terms are built time-even only: a force with them and broken
+    time reversal is refused before any CUDA call."""
+    from mocca_gb300.forces import SLY5_TENSOR
+    lib = _abi.load()
+    params = RunParams(nx=10, ny=10, nz=10, trc=0).to_c()
+    ctx = C.c_void_p()
+    assert lib.mg_create(C.byref(params), SLY5_TENSOR.to_c(), None,
+                         C.byref(ctx)) == _abi.MG_ERR_ARG
+    assert not ctx.value
 
 
 def test_product_does_not_use_the_oracle():
