@@ -86,6 +86,10 @@ module mocca_gpu
     real(c_double) :: B15
     real(c_double) :: B16
     real(c_double) :: B17
+    real(c_double) :: B18
+    real(c_double) :: B19
+    real(c_double) :: B20
+    real(c_double) :: B21
   end type mg_skyrme_b
   type, bind(C) :: mg_energy_terms
     real(c_double) :: total
@@ -421,6 +425,17 @@ module mocca_gpu
       type(c_ptr), value :: a
       type(c_ptr), value :: s
       type(c_ptr), value :: diva
+    end function
+    integer(c_int) function mg_get_time_odd_tensor(ctx, vt, vf, ls, gds, c, d, divd) bind(C, name="mg_get_time_odd_tensor")
+      import
+      type(c_ptr), value :: ctx
+      type(c_ptr), value :: vt
+      type(c_ptr), value :: vf
+      type(c_ptr), value :: ls
+      type(c_ptr), value :: gds
+      type(c_ptr), value :: c
+      type(c_ptr), value :: d
+      type(c_ptr), value :: divd
     end function
     integer(c_int) function mg_nilsson_start(ctx, np) bind(C, name="mg_nilsson_start")
       import

@@ -110,10 +110,13 @@ typedef struct mg_force {
                             te, to in B14, B15 (B16, B17 follow te, to always) */
 } mg_force;
 
-/* The B-coefficients of the energy density (src/Force.f90:467-560). */
+/* The B-coefficients of the energy density (src/Force.f90:467-560).
+ * B18, B19 (J2Terms) and B20, B21 (te, to) are time-odd: zero with time
+ * reversal. */
 typedef struct mg_skyrme_b {
     double B1, B2, B3, B4, B5, B6, B7a, B7b, B8a, B8b, byt3a, byt3b, B9, B9q;
     double B10, B11, B12a, B12b, B13a, B13b, B14, B15, B16, B17;
+    double B18, B19, B20, B21;
 } mg_skyrme_b;
 
 /* Energy decomposition of CompEnergy (src/Energy.f90:62-179). */
@@ -396,6 +399,16 @@ int mg_get_potentials(mg_ctx* ctx, double* u, double* b, double* nablab,
  * any may be NULL.  MG_ERR_ARG with time reversal. */
 int mg_get_time_odd(mg_ctx* ctx, double* vecj, double* vecs, double* rotj, double* rots,
                     double* a, double* s, double* diva);
+
+/* The time-odd tensor densities and fields without time reversal, when
+ * B14..B21 are not all zero: T (GetVecT, src/Spwf.f90:2087-2129), F
+ * (GetVecF :2162-2180), lap s and grad div s (src/Densities.f90:1055-1185),
+ * the C and D fields (CalcCPot, CalcDPot, src/MeanFields.f90:714-790), each
+ * [it][m][V] (6V), and div D [it][V] (2V); any may be NULL.  The densities
+ * a coefficient does not use stay zero, as the reference leaves them
+ * unallocated.  MG_ERR_ARG with time reversal or without these terms. */
+int mg_get_time_odd_tensor(mg_ctx* ctx, double* vt, double* vf, double* ls, double* gds,
+                           double* c, double* d, double* divd);
 
 /* INITWF (src/InOut.f90:1418-1473) with nil8's Nilsson states
  * (src/nil8.f90:16-546) for an EV8 context (nz >= nx, ny): the lowest

@@ -69,7 +69,7 @@ class MgSkyrmeB(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "B1", "B2", "B3", "B4", "B5", "B6", "B7a", "B7b", "B8a", "B8b", "byt3a", "byt3b",
         "B9", "B9q", "B10", "B11", "B12a", "B12b", "B13a", "B13b", "B14", "B15", "B16",
-        "B17")]
+        "B17", "B18", "B19", "B20", "B21")]
 
 
 class MgPairingParams(C.Structure):
@@ -238,6 +238,7 @@ SIGNATURES = {
     "mg_coulomb_residual": [_P, _D],
     "mg_coulomb_reset": [_P],
     "mg_get_time_odd": [_P, _D, _D, _D, _D, _D, _D, _D],
+    "mg_get_time_odd_tensor": [_P, _D, _D, _D, _D, _D, _D, _D],
     "mg_symmetry_operators": [_P, C.c_int, _D],
     "mg_construct_potentials": [_P, _I],
     "mg_get_potentials": [_P, _D, _D, _D, _D, _D, _D, _D],

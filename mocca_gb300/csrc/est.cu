@@ -106,6 +106,7 @@ int estimate_parameters(mg_ctx* c) {
                 if (B.h_qn[4 * i] == -1) iw = i;
         const int* q = &B.h_qn[4 * iw];
         MG_CUDA(cudaMemcpy(c->est_qn, q, 4 * sizeof(int), cudaMemcpyHostToDevice));
+        for (int k = 0; k < 4; ++k) c->est_h_qn[k] = q[k];
         std::vector<GridJob> jobs(4);
         for (int l = 0; l < 4; ++l) {
             GridJob J{};

@@ -45,6 +45,8 @@ void free_all(mg_ctx* c) {
     F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
     F(c->odd); F(c->odd_hist); F(c->Apot); F(c->Spot); F(c->divA); F(c->odd_der); F(c->odd_tmp);
     F(c->odd_jobs);
+    F(c->Cpot); F(c->Dpot); F(c->dDpot); F(c->divD); F(c->todd_tmp); F(c->todd_work);
+    F(c->todd_x); F(c->todd_jobs); F(c->todd_act_jobs);
     multigrid_free(c->mgrid);
     c->mgrid = nullptr;
     hfb_free(c);
@@ -104,6 +106,19 @@ extern "C" int mg_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* B
     }
     B->B16 = -(3.0 / 8.0) * (f->te + f->to);
     B->B17 = (3.0 / 8.0) * (f->te - f->to);
+    if (f->j2terms && !trc) {
+        // s . lap s terms: central part of t1, t2 plus the tensor part
+        const double C18 = -(1.0 / 32.0) * (3 * f->t1 * f->x1 - f->t2 * f->x2);
+        const double C19 = (1.0 / 32.0) * (3 * f->t1 + f->t2);
+        const double T18 = (1.0 / 16.0) * (3 * f->te - f->to);
+        const double T19 = -(1.0 / 16.0) * (3 * f->te + f->to);
+        B->B18 = C18 + T18;
+        B->B19 = C19 + T19;
+    }
+    if (!trc) {
+        B->B20 = (3.0 / 16.0) * (3 * f->te - f->to);
+        B->B21 = -(3.0 / 16.0) * (3 * f->te + f->to);
+    }
     return MG_OK;
 }
 
@@ -173,14 +188,6 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     if ((p->sc && p->omega[0] != 0.0) || (p->tsc && p->omega[1] != 0.0)) return MG_ERR_ARG;
     if (!p->trc && (!ev8 || p->precision != MG_FP64 || p->pairing != MG_PAIRING_HF))
         return MG_ERR_ARG;
-    {
-        // the J^2 (tensor) terms: time-even only (their time-odd partners T,
-        // F and the C, D fields are not built)
-        mg_skyrme_b tb;
-        mg_skyrme_coefficients(f, p->trc, &tb);
-        if ((tb.B14 != 0.0 || tb.B15 != 0.0 || tb.B16 != 0.0 || tb.B17 != 0.0) && !p->trc)
-            return MG_ERR_ARG;
-    }
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     mg_ctx* c = new mg_ctx();
@@ -189,6 +196,11 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     c->f = *f;
     mg_skyrme_coefficients(f, p->trc, &c->B);
     c->tensor = c->B.B14 != 0.0 || c->B.B15 != 0.0 || c->B.B16 != 0.0 || c->B.B17 != 0.0;
+    // without time reversal the tensor terms have time-odd partners
+    // (tensor_odd.cu): T, F, lap s and grad div s behind the time-odd densities
+    c->todd = !p->trc && (c->tensor || c->B.B18 != 0.0 || c->B.B19 != 0.0 ||
+                          c->B.B20 != 0.0 || c->B.B21 != 0.0);
+    c->odd_len = c->todd ? 48 : 24;
     c->nx = p->nx; c->ny = p->ny; c->nz = p->nz;
     c->V = (long)p->nx * p->ny * p->nz;
     const int nsym = (p->pc ? 1 : 0) + (p->sc ? 1 : 0) + (p->tsc ? 1 : 0);

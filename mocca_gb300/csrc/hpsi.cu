@@ -34,6 +34,9 @@ struct Fields {
     const double* A = nullptr;
     const double* S = nullptr;
     const double* divA = nullptr;
+    // the C and D actions of the time-odd tensor terms per spwf
+    // ([i][2][l][V], tensor_odd.cu), or nullptr
+    const double* X = nullptr;
 };
 
 __device__ __forceinline__ void pauli(const double* p, int dir, double* o) {
@@ -122,6 +125,12 @@ k_hpsi(double* __restrict__ psi, const double* __restrict__ der,
             const double af[4] = {aa[1], -aa[0], aa[3], -aa[2]};
 #pragma unroll
             for (int l = 0; l < 4; ++l) h[l] = (h[l] + sa[l]) + af[l];
+        }
+        if (F.X) {
+            // ActionOfC, then ActionOfD (src/ImaginaryTime.f90:270-284)
+            const double* x = F.X + (long)i * 8 * V;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) h[l] = (h[l] + x[l * V + v]) + x[(4 + l) * V + v];
         }
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
@@ -350,6 +359,13 @@ int hpsi_basis(mg_ctx* c, int b, double* out, bool grad_step, double fac, double
     const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
     const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
     dim3 grid(nchunk, c->p.nwt);
+    if (c->todd) {
+        // the time-odd tensor actions first (the time-odd path is FP64)
+        if (B.der_df) return MG_ERR_STATE;
+        if (!c->todd_x) MG_CUDA(cudaMalloc(&c->todd_x, 8 * (size_t)c->p.nwt * V * sizeof(double)));
+        MG_TRY(tensor_odd_action(c, B.der, B.h_qn.data(), B.qn, c->p.nwt, c->todd_x));
+        F.X = c->todd_x;
+    }
     // the derivative format decides: double-float derivatives come from the
     // mixed kernels
     const bool mixed = B.der_df;
@@ -391,6 +407,11 @@ int hpsi_single(mg_ctx* c, double* psi, const double* der, const double* lap, co
     Fields F{c->U, c->Bp, c->nablaB, c->W, c->divW, c->Apot, c->Spot, c->divA};
     const double kin0 = c->f.hbm / 2.0 * reduced_mass(c, 0);
     const double kin1 = c->f.hbm / 2.0 * reduced_mass(c, 1);
+    if (c->todd) {
+        if (!c->todd_x) MG_CUDA(cudaMalloc(&c->todd_x, 8 * (size_t)c->p.nwt * V * sizeof(double)));
+        MG_TRY(tensor_odd_action(c, der, c->est_h_qn, qn_dev, 1, c->todd_x));
+        F.X = c->todd_x;
+    }
     k_hpsi<false><<<dim3(nchunk, 1), kThreads, 0, c->stream>>>(psi, der, lap, qn_dev, F, out,
                                                                nullptr, c->red, V, kin0, kin1,
                                                                0.0, 0.0);

@@ -322,6 +322,20 @@ struct mg_ctx {
     double *odd = nullptr, *odd_hist = nullptr, *Apot = nullptr, *Spot = nullptr,
            *divA = nullptr, *odd_der = nullptr, *odd_tmp = nullptr;
     mg::GridJob* odd_jobs = nullptr;
+    // the time-odd tensor terms (tensor_odd.cu), when B14..B21 are not all
+    // zero: odd grows to 48V with [T, F, lap s, grad div s] behind the
+    // curls (odd_len = 48, else 24, in units of V); the C and D fields
+    // ([it][m][V]), d_n D_m ([it][m][n][V]), div D ([it][V]), the d_z s_z
+    // scratch (2V), 16 fixed jobs; the h.psi scratch (60V per spwf), its
+    // job table (device, and the last upload's bytes on the host) and the
+    // C and D actions of the basis ([i][2][l][V])
+    bool todd = false;
+    int odd_len = 24;
+    double *Cpot = nullptr, *Dpot = nullptr, *dDpot = nullptr, *divD = nullptr,
+           *todd_tmp = nullptr, *todd_work = nullptr, *todd_x = nullptr;
+    mg::GridJob* todd_jobs = nullptr;
+    mg::GridJob* todd_act_jobs = nullptr;
+    std::vector<unsigned char> todd_jobs_host;
     bool have_uold = false;            // UpotOld not all zero
     double* pc_buf = nullptr;          // preconditioner CG: res, dir, upd, lap, inv (10V)
     mg::GridJob* pc_jobs = nullptr;    // Laplacians of the two directions
@@ -353,6 +367,7 @@ struct mg_ctx {
     double* est = nullptr;              // psi 4V, der 12V, lap 4V, hpsi 4V, update 4V, (e, disp)
     mg::GridJob* est_jobs = nullptr;
     int* est_qn = nullptr;
+    int est_h_qn[4] = {0, 0, 0, 0};   // the probe's quantum numbers on the host
     int est_iter = 0;
     bool step_set = false;
     double step_dt = 0.0, step_mom = 0.0;
@@ -437,6 +452,12 @@ int time_odd_setup(mg_ctx* c);
 int time_odd_densities(mg_ctx* c, const Basis& D);
 int time_odd_potentials(mg_ctx* c);
 int time_odd_energy(mg_ctx* c, double* t);
+int tensor_odd_setup(mg_ctx* c);
+int tensor_odd_densities(mg_ctx* c, const Basis& D);
+int tensor_odd_fields(mg_ctx* c);
+int tensor_odd_action(mg_ctx* c, const double* der, const int* h_qn, const int* d_qn, int count,
+                      double* x);
+int tensor_odd_energy(mg_ctx* c, double* t);
 int cranking_cutoff(mg_ctx* c);
 inline bool cranking(const mg_ctx* c) {
     return c->p.omega[0] != 0.0 || c->p.omega[1] != 0.0 || c->p.omega[2] != 0.0;

@@ -153,7 +153,7 @@ int save_density_history(mg_ctx* c) {
         off += len[q];
     }
     if (c->odd)
-        MG_CUDA(cudaMemcpyAsync(c->odd_hist, c->odd, 24 * V * sizeof(double),
+        MG_CUDA(cudaMemcpyAsync(c->odd_hist, c->odd, c->odd_len * V * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
     if (c->tensor)
         MG_CUDA(cudaMemcpyAsync(c->jmunu_hist, c->jmunu, 18 * V * sizeof(double),
@@ -175,7 +175,7 @@ int mix_densities(mg_ctx* c) {
         off += len[q];
     }
     if (c->odd) {   // the time-odd densities mix with the rest
-        k_mix<<<div_up(24 * V, kThreads), kThreads, 0, c->stream>>>(c->odd, c->odd_hist, 24 * V,
+        k_mix<<<div_up(c->odd_len * V, kThreads), kThreads, 0, c->stream>>>(c->odd, c->odd_hist, c->odd_len * V,
                                                                     c->p.damping);
         MG_LAUNCHED(c);
     }

@@ -1,7 +1,8 @@
 // timeodd.cu -- time-odd densities and fields without time-reversal
 // invariance (cranked, signature and time simplex conserved), FP64.
 //
-// Replaces, for the functional without tensor, N2LO and J2 terms:
+// Replaces, for the functional without N2LO terms (the time-odd tensor
+// terms are in tensor_odd.cu):
 //   ComputeDensity's time-odd part (src/Densities.f90:431-550, :1004-1106):
 //     vecj_q += v^2 Im(psi^+ d_m psi)   GetVecj src/Spwf.f90:2034-2046
 //     vecs_q += v^2 Re(psi^+ sigma_m psi)  GetVecs :2066-2079
@@ -112,15 +113,18 @@ __global__ void k_odd_curls(const double* __restrict__ d, long V, double* __rest
 
 struct OddCoef {
     double B3, B4, B9, B9q, B10, B11, B12a, B13a, B12b, B13b, byt3a, byt3b;
+    double B14, B15, B16, B17, B18, B19, B20, B21;
     double om[3];
     double dx;
     int nx, ny, crank;
 };
 
+// tz: T, F, lap s, grad div s ([it][m][V] each, tensor_odd.cu), or NULL
 __global__ void k_odd_potentials(const double* __restrict__ rho, const double* __restrict__ vecj,
                                  const double* __restrict__ vecs, const double* __restrict__ rotj,
                                  const double* __restrict__ rots, const double* __restrict__ cut,
-                                 OddCoef k, long V, double* __restrict__ A, double* __restrict__ S) {
+                                 const double* __restrict__ tz, OddCoef k, long V,
+                                 double* __restrict__ A, double* __restrict__ S) {
     const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const double rt = rho[v] + rho[V + v];
@@ -138,6 +142,17 @@ __global__ void k_odd_potentials(const double* __restrict__ rho, const double* _
             double sv = (k.B9 + k.B9q) * rotj[q] + k.B9 * rotj[qa] +
                         2.0 * ((k.B10 + k.B11) * vecs[q] + k.B10 * vecs[qa]) +
                         2.0 * ((k.B12a + k.B13a) * (ra * vecs[q]) + k.B12a * (ra * vecs[qa]));
+            if (tz) {
+                // the time-odd tensor terms (src/MeanFields.f90:651-670)
+                const double *T = tz, *F = tz + 6 * V, *L = tz + 12 * V, *G = tz + 18 * V;
+                if (k.B14 != 0.0 || k.B15 != 0.0)
+                    sv = sv - (k.B14 + k.B15) * T[q] - k.B14 * T[qa];
+                if (k.B16 != 0.0 || k.B17 != 0.0)
+                    sv = sv - 2.0 * (k.B16 + k.B17) * F[q] - 2.0 * k.B16 * F[qa];
+                if (k.B18 != 0.0 || k.B19 != 0.0 || k.B20 != 0.0 || k.B21 != 0.0)
+                    sv = sv + 2.0 * ((k.B18 + k.B19) * L[q] + k.B18 * L[qa]) -
+                         2.0 * ((k.B20 + k.B21) * G[q] - k.B20 * G[qa]);
+            }
             if (k.B12b != 0.0 || k.B13b != 0.0)
                 sv = sv + 2.0 * ((k.B12b + k.B13b) * (rb * vecs[q]) + k.B12b * (rb * vecs[qa]));
             if (k.crank) {
@@ -219,7 +234,7 @@ int time_odd_setup(mg_ctx* c) {
         return cudaMalloc(p, n * sizeof(double)) == cudaSuccess &&
                cudaMemset(*p, 0, n * sizeof(double)) == cudaSuccess;
     };
-    if (!(A(&c->odd, 24 * V) && A(&c->odd_hist, 24 * V) && A(&c->Apot, 6 * V) &&
+    if (!(A(&c->odd, c->odd_len * V) && A(&c->odd_hist, c->odd_len * V) && A(&c->Apot, 6 * V) &&
           A(&c->Spot, 6 * V) && A(&c->divA, 2 * V) && A(&c->odd_der, 36 * V) &&
           A(&c->odd_tmp, 6 * V)))
         return MG_ERR_CUDA;
@@ -261,6 +276,7 @@ int time_odd_setup(mg_ctx* c) {
     MG_CUDA(cudaMalloc(&c->odd_jobs, jobs.size() * sizeof(GridJob)));
     MG_CUDA(cudaMemcpy(c->odd_jobs, jobs.data(), jobs.size() * sizeof(GridJob),
                        cudaMemcpyHostToDevice));
+    if (c->todd) MG_TRY(tensor_odd_setup(c));
     return MG_OK;
 }
 
@@ -274,6 +290,7 @@ int time_odd_densities(mg_ctx* c, const Basis& D) {
     k_odd_curls<<<dim3(div_up(V, kThreads), 4), kThreads, 0, c->stream>>>(
         c->odd_der, V, c->odd + 12 * V, c->odd + 18 * V);
     MG_LAUNCHED(c);
+    if (c->todd) MG_TRY(tensor_odd_densities(c, D));
     return MG_OK;
 }
 
@@ -282,16 +299,18 @@ int time_odd_potentials(mg_ctx* c) {
     const long V = c->V;
     const mg_skyrme_b& B = c->B;
     OddCoef k{B.B3, B.B4, B.B9, B.B9q, B.B10, B.B11, B.B12a, B.B13a, B.B12b, B.B13b, B.byt3a,
-              B.byt3b, {c->p.omega[0], c->p.omega[1], c->p.omega[2]}, c->p.dx, c->nx, c->ny,
+              B.byt3b, B.B14, B.B15, B.B16, B.B17, B.B18, B.B19, B.B20, B.B21,
+              {c->p.omega[0], c->p.omega[1], c->p.omega[2]}, c->p.dx, c->nx, c->ny,
               cranking(c) ? 1 : 0};
     if (k.crank && !c->cons.cut) return MG_ERR_STATE;   // the moments pass computes it
     k_odd_potentials<<<div_up(V, kThreads), kThreads, 0, c->stream>>>(
-        c->rho, c->odd, c->odd + 6 * V, c->odd + 12 * V, c->odd + 18 * V, c->cons.cut, k, V,
-        c->Apot, c->Spot);
+        c->rho, c->odd, c->odd + 6 * V, c->odd + 12 * V, c->odd + 18 * V, c->cons.cut,
+        c->todd ? c->odd + 24 * V : nullptr, k, V, c->Apot, c->Spot);
     MG_LAUNCHED(c);
     MG_TRY(run_jobs(c, c->odd_jobs + 12, 6));
     k_odd_sum3<<<dim3(div_up(V, kThreads), 2), kThreads, 0, c->stream>>>(c->odd_tmp, V, c->divA);
     MG_LAUNCHED(c);
+    if (c->todd) MG_TRY(tensor_odd_fields(c));
     return MG_OK;
 }
 
@@ -321,6 +340,7 @@ int time_odd_energy(mg_ctx* c, double* t) {
     t[17] = B.B13a * S[8];
     t[34] = B.B12b != 0.0 ? B.B12b * S[4] : 0.0;
     t[35] = B.B13b != 0.0 ? B.B13b * S[9] : 0.0;
+    if (c->todd) MG_TRY(tensor_odd_energy(c, t));
     return MG_OK;
 }
 

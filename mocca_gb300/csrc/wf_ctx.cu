@@ -161,9 +161,8 @@ int from_context(mg_ctx* c, const char* force_name, mg_wf& w) {
     h.hbm[0] = h.hbm[1] = f.hbm;
     h.com1body = f.com1body;
     h.com2body = f.com2body;
-    // B1 ... B17 in the record's order; B18 ... B21 (terms this library does
-    // not carry) are zero
-    static_assert(sizeof(mg_skyrme_b) == 24 * sizeof(double), "B1 ... B17");
+    // B1 ... B21 in the record's order
+    static_assert(sizeof(mg_skyrme_b) == 28 * sizeof(double), "B1 ... B21");
     std::memcpy(h.coef, &c->B, sizeof(mg_skyrme_b));
     if (hfb) {
         const mg_pairing_params& pp = c->hfb.pp;

@@ -204,6 +204,17 @@ class MeshState:
                                          ("vecj", "vecs", "rotj", "rots", "A", "S", "divA")))
         return out
 
+    TENSOR_ODD = ("T", "F", "lapS", "gradDivS", "C", "D", "divD")
+
+    def get_time_odd_tensor(self) -> dict:
+        """Time-odd tensor densities and fields without time reversal
+        (mg_get_time_odd_tensor): T, F, lap s, grad div s, C, D as [it][m][V],
+        div D as [it][V]."""
+        V = self.V
+        out = {k: np.empty((2 if k == "divD" else 6) * V) for k in self.TENSOR_ODD}
+        self._call("mg_get_time_odd_tensor", *(_dptr(out[k]) for k in self.TENSOR_ODD))
+        return out
+
     def set_potentials(self, U=None, B=None, nablaB=None, W=None, divW=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
                 for a in (U, B, nablaB, W, divW)]

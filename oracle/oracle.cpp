@@ -77,6 +77,15 @@ struct orc_ctx {
     std::vector<double> jmunu, hjmunu;
     // time-odd fields (src/MeanFields.f90:79-85): A, S [it][m][V], div A [it][V]
     std::vector<double> Apot, Spot, divA;
+    // time-odd tensor terms without time reversal (B14..B21 not all zero):
+    // the densities T, F, lap s, grad div s [it][m][V] (src/Densities.f90:
+    // 55-64; each stays zero when no coefficient uses it, as the reference
+    // leaves it unallocated) and their history; the fields C, D [it][m][V],
+    // the derivatives of D [it][m][n][V] (d_n D_m) and div D [it][V]
+    // (src/MeanFields.f90:84-87)
+    bool todd = false;
+    std::vector<double> vecT, vecF, lapS, gdivS, hvecT, hvecF, hlapS, hgdivS;
+    std::vector<double> Cpot, Dpot, dD, divD;
     // potentials (src/MeanFields.f90:79-85)
     std::vector<double> U, Bp, nablaB, W, divW;
     // Coulomb (src/Coulomb.f90:20-105)
@@ -169,6 +178,19 @@ extern "C" int orc_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* 
     }
     B->B16 = -(3.0 / 8.0) * (f->te + f->to);
     B->B17 = (3.0 / 8.0) * (f->te - f->to);
+    if (f->j2terms && !trc) {
+        // s . lap s terms: central part of t1, t2 plus the tensor part
+        const double C18 = -(1.0 / 32.0) * (3 * f->t1 * f->x1 - f->t2 * f->x2);
+        const double C19 = (1.0 / 32.0) * (3 * f->t1 + f->t2);
+        const double T18 = (1.0 / 16.0) * (3 * f->te - f->to);
+        const double T19 = -(1.0 / 16.0) * (3 * f->te + f->to);
+        B->B18 = C18 + T18;
+        B->B19 = C19 + T19;
+    }
+    if (!trc) {
+        B->B20 = (3.0 / 16.0) * (3 * f->te - f->to);
+        B->B21 = -(3.0 / 16.0) * (3 * f->te + f->to);
+    }
     return MG_OK;
 }
 
@@ -359,6 +381,15 @@ extern "C" orc_ctx* orc_create(const mg_params* p, const mg_force* f) {
         for (auto* x : {&c->vecj, &c->vecs, &c->rotj, &c->rots, &c->Apot, &c->Spot})
             x->assign(6 * V, 0.0);
     if (!p->trc) c->divA.assign(2 * V, 0.0);
+    const mg_skyrme_b& B = c->B;
+    c->todd = !p->trc && (c->tensor || B.B18 != 0.0 || B.B19 != 0.0 || B.B20 != 0.0 ||
+                          B.B21 != 0.0);
+    if (c->todd) {
+        for (auto* x : {&c->vecT, &c->vecF, &c->lapS, &c->gdivS, &c->Cpot, &c->Dpot})
+            x->assign(6 * V, 0.0);
+        c->dD.assign(18 * V, 0.0);
+        c->divD.assign(2 * V, 0.0);
+    }
     return c;
 }
 
@@ -466,10 +497,94 @@ static double reduced_mass(const orc_ctx* c, int it) {
     return 1.0;
 }
 
+// ActionOfC and ActionOfD (src/MeanFields.f90:1149-1255) of spwf i into xc,
+// xd (4V each):
+//   C psi = sum_n d_n [-sum_m C_m sigma_m d_n psi]
+//   D psi = -1/2 [div D sigma.grad psi + sum_mn d_n D_m sigma_n d_m psi
+//                 + 2 sum_mn D_m sigma_n d_m d_n psi]
+// The outer derivatives take the symmetries of d_n psi: (-P, -S, TS) for
+// x, (-P, -S, -TS) for y, (-P, S, TS) for z; d_m d_n psi is d_m of the
+// stored d_n psi.
+static void tensor_odd_action(const orc_ctx* c, const Basis& Bs, int i, double* xc,
+                              double* xd) {
+    const long V = c->V;
+    const mg_skyrme_b& B = c->B;
+    const int it = (Bs.qn[4 * i] + 3) / 2 - 1;
+    const int P = Bs.qn[4 * i + 1], S = Bs.qn[4 * i + 2], TS = Bs.qn[4 * i + 3];
+    const double* der = &Bs.der[(long)i * 12 * V];
+    const int sp[3][2] = {{-S, TS}, {-S, -TS}, {S, TS}};
+    std::fill(xc, xc + 4 * V, 0.0);
+    std::fill(xd, xd + 4 * V, 0.0);
+    if (B.B14 != 0.0 || B.B15 != 0.0) {
+        std::vector<double> tmp(4 * V), dt(V);
+        for (int n = 0; n < 3; ++n) {
+            for (long v = 0; v < V; ++v) {
+                double dn[4], t[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int l = 0; l < 4; ++l) dn[l] = der[(n * 4 + l) * V + v];
+                for (int m = 0; m < 3; ++m) {
+                    double sg[4];
+                    pauli(dn, m + 1, sg);
+                    const double cm = c->Cpot[(it * 3 + m) * V + v];
+                    for (int l = 0; l < 4; ++l) t[l] = t[l] - cm * sg[l];
+                }
+                for (int l = 0; l < 4; ++l) tmp[l * V + v] = t[l];
+            }
+            for (int l = 0; l < 4; ++l) {
+                derive_grid(c, &tmp[l * V], n, -P, sp[n][0], sp[n][1], l + 1, dt.data());
+                for (long v = 0; v < V; ++v) xc[l * V + v] = xc[l * V + v] + dt[v];
+            }
+        }
+    }
+    if (B.B16 != 0.0 || B.B17 != 0.0) {
+        std::vector<double> dd(36 * V);   // [a][n][l][V] = d_a (d_n psi)_l
+        for (int n = 0; n < 3; ++n)
+            for (int l = 0; l < 4; ++l)
+                for (int a = 0; a < 3; ++a)
+                    derive_grid(c, &der[(n * 4 + l) * V], a, -P, sp[n][0], sp[n][1], l + 1,
+                                &dd[((a * 3 + n) * 4 + l) * V]);
+        for (long v = 0; v < V; ++v) {
+            double d[3][4];
+            for (int m = 0; m < 3; ++m)
+                for (int l = 0; l < 4; ++l) d[m][l] = der[(m * 4 + l) * V + v];
+            double t1[4] = {0, 0, 0, 0}, t2[4] = {0, 0, 0, 0}, t3[4] = {0, 0, 0, 0};
+            for (int m = 0; m < 3; ++m) {
+                double sg[4];
+                pauli(d[m], m + 1, sg);
+                for (int l = 0; l < 4; ++l) t1[l] = t1[l] + sg[l];
+            }
+            const double dvD = c->divD[it * V + v];
+            for (int l = 0; l < 4; ++l) t1[l] = dvD * t1[l];
+            for (int m = 0; m < 3; ++m)
+                for (int n = 0; n < 3; ++n) {
+                    double sg[4];
+                    pauli(d[m], n + 1, sg);
+                    const double g = c->dD[((it * 3 + m) * 3 + n) * V + v];
+                    for (int l = 0; l < 4; ++l) t2[l] = t2[l] + g * sg[l];
+                }
+            for (int m = 0; m < 3; ++m)
+                for (int n = 0; n < 3; ++n) {
+                    double q[4], sg[4];
+                    for (int l = 0; l < 4; ++l) q[l] = dd[((m * 3 + n) * 4 + l) * V + v];
+                    pauli(q, n + 1, sg);
+                    const double Dm = c->Dpot[(it * 3 + m) * V + v];
+                    for (int l = 0; l < 4; ++l) t3[l] = t3[l] + Dm * sg[l];
+                }
+            for (int l = 0; l < 4; ++l) xd[l * V + v] = -0.5 * (t1[l] + t2[l] + 2.0 * t3[l]);
+        }
+    }
+}
+
 // hPsi for one spwf: B (ActionOfBNew) + U + W, src/ImaginaryTime.f90:213-304,
-// src/MeanFields.f90:792-851, :1029-1065.
+// src/MeanFields.f90:792-851, :1029-1065; without time reversal S and A, and
+// with the time-odd tensor terms C and D.
 static void hpsi_one(const orc_ctx* c, const Basis& B, int i, double* out) {
     const long V = c->V;
+    std::vector<double> xc, xd;
+    if (c->todd) {
+        xc.resize(4 * V);
+        xd.resize(4 * V);
+        tensor_odd_action(c, B, i, xc.data(), xd.data());
+    }
     const int it = (B.qn[4 * i] + 3) / 2 - 1;
     const double* psi = &B.psi[(long)i * 4 * V];
     const double* der = &B.der[(long)i * 12 * V];
@@ -530,6 +645,8 @@ static void hpsi_one(const orc_ctx* c, const Basis& B, int i, double* out) {
             const double af[4] = {aa[1], -aa[0], aa[3], -aa[2]};
             for (int l = 0; l < 4; ++l) h[l] = (h[l] + sa[l]) + af[l];
         }
+        if (c->todd)
+            for (int l = 0; l < 4; ++l) h[l] = (h[l] + xc[l * V + v]) + xd[l * V + v];
         for (int l = 0; l < 4; ++l) out[l * V + v] = h[l];
     }
 }
@@ -820,11 +937,20 @@ extern "C" int orc_update_densities(orc_ctx* c) {
     c->hderrho = c->derrho; c->hlaprho = c->laprho;
     c->hvecj = c->vecj; c->hvecs = c->vecs; c->hrotj = c->rotj; c->hrots = c->rots;
     c->hjmunu = c->jmunu;
+    c->hvecT = c->vecT; c->hvecF = c->vecF; c->hlapS = c->lapS; c->hgdivS = c->gdivS;
     if (c->tensor) std::fill(c->jmunu.begin(), c->jmunu.end(), 0.0);
     const bool odd = !c->p.trc;
     if (odd) {
         std::fill(c->vecj.begin(), c->vecj.end(), 0.0);
         std::fill(c->vecs.begin(), c->vecs.end(), 0.0);
+    }
+    // T with B14 or B15, F with B16 or B17 (src/Densities.f90:502-510)
+    const mg_skyrme_b& Bc = c->B;
+    const bool wantT = c->todd && (Bc.B14 != 0.0 || Bc.B15 != 0.0);
+    const bool wantF = c->todd && (Bc.B16 != 0.0 || Bc.B17 != 0.0);
+    if (c->todd) {
+        std::fill(c->vecT.begin(), c->vecT.end(), 0.0);
+        std::fill(c->vecF.begin(), c->vecF.end(), 0.0);
     }
     const Basis& B = c->bas[c->p.pairing == MG_PAIRING_HFB ? MG_CAN_BASIS : MG_HF_BASIS];
     std::fill(c->rho.begin(), c->rho.end(), 0.0);
@@ -878,6 +1004,34 @@ extern "C" int orc_update_densities(orc_ctx* c) {
                     c->vecj[(it * 3 + m) * V + v] = c->vecj[(it * 3 + m) * V + v] + occ * imag_mult(p, d[m]);
                     c->vecs[(it * 3 + m) * V + v] = c->vecs[(it * 3 + m) * V + v] + occ * sm;
                 }
+                // GetVecT: T_m = sum_l Re(d_l psi^+ sigma_m d_l psi); GetVecF:
+                // F_m = Re(d_m psi^+ sum_n sigma_n d_n psi) (src/Spwf.f90:2087-2180)
+                auto re_mult = [](const double* a, const double* b) {
+                    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+                };
+                if (wantT)
+                    for (int m = 0; m < 3; ++m) {
+                        double t = 0.0;
+                        for (int l = 0; l < 3; ++l) {
+                            double sg[4];
+                            pauli(d[l], m + 1, sg);
+                            t = t + re_mult(d[l], sg);
+                        }
+                        double& T = c->vecT[(it * 3 + m) * V + v];
+                        T = T + occ * t;
+                    }
+                if (wantF) {
+                    double sd[4] = {0.0, 0.0, 0.0, 0.0};
+                    for (int n = 0; n < 3; ++n) {
+                        double sg[4];
+                        pauli(d[n], n + 1, sg);
+                        for (int l = 0; l < 4; ++l) sd[l] = sd[l] + sg[l];
+                    }
+                    for (int m = 0; m < 3; ++m) {
+                        double& F = c->vecF[(it * 3 + m) * V + v];
+                        F = F + occ * re_mult(d[m], sd);
+                    }
+                }
             }
         }
     }
@@ -888,6 +1042,22 @@ extern "C" int orc_update_densities(orc_ctx* c) {
         derive_grid(c, &c->rho[it * V], 3, P, S, TS, 1, &c->laprho[it * V]);
     }
     if (odd) time_odd_curls(c);
+    if (c->todd && (Bc.B18 != 0.0 || Bc.B19 != 0.0 || Bc.B20 != 0.0 || Bc.B21 != 0.0)) {
+        // lap s with the symmetries of the s components (P, -S, TS, 1),
+        // (P, -S, TS, 2), (P, S, TS, 1); grad div s as the reference forms
+        // it (src/Densities.f90:1055-1185): its divergence accumulator adds
+        // each d_i s_i to the never-assigned DivS field, so only d_z s_z
+        // survives, and the gradient takes (-P, S, TS, 1)
+        std::vector<double> dz(V);
+        for (int it = 0; it < 2; ++it) {
+            for (int m = 0; m < 3; ++m)
+                derive_grid(c, &c->vecs[(it * 3 + m) * V], 3, P, m == 2 ? S : -S, TS,
+                            m == 1 ? 2 : 1, &c->lapS[(it * 3 + m) * V]);
+            derive_grid(c, &c->vecs[(it * 3 + 2) * V], 2, P, S, TS, 1, dz.data());
+            for (int a = 0; a < 3; ++a)
+                derive_grid(c, dz.data(), a, -P, S, TS, 1, &c->gdivS[(it * 3 + a) * V]);
+        }
+    }
     return MG_OK;
 }
 
@@ -908,6 +1078,8 @@ extern "C" int orc_mix_densities(orc_ctx* c) {
     mix(c->derrho, c->hderrho); mix(c->laprho, c->hlaprho);
     mix(c->vecj, c->hvecj); mix(c->vecs, c->hvecs); mix(c->rotj, c->hrotj); mix(c->rots, c->hrots);
     mix(c->jmunu, c->hjmunu);
+    mix(c->vecT, c->hvecT); mix(c->vecF, c->hvecF); mix(c->lapS, c->hlapS);
+    mix(c->gdivS, c->hgdivS);
     return MG_OK;
 }
 
@@ -979,6 +1151,27 @@ extern "C" int orc_get_time_odd(orc_ctx* c, double* vecj, double* vecs, double* 
     };
     cp(vecj, c->vecj); cp(vecs, c->vecs); cp(rotj, c->rotj); cp(rots, c->rots);
     cp(apot, c->Apot); cp(spot, c->Spot); cp(diva, c->divA);
+    return MG_OK;
+}
+
+// ActionOfC and ActionOfD of spwf i of basis b, each 4V (test access).
+extern "C" int orc_tensor_odd_action(orc_ctx* c, int b, int i, double* xc, double* xd) {
+    if (!c || !c->todd || b < 0 || b > 1 || i < 0 || i >= c->p.nwt || !xc || !xd)
+        return MG_ERR_ARG;
+    tensor_odd_action(c, c->bas[b], i, xc, xd);
+    return MG_OK;
+}
+
+// Time-odd tensor densities and fields ([it][m][V] vectors, div D [it][V]).
+extern "C" int orc_get_time_odd_tensor(orc_ctx* c, double* vect, double* vecf, double* laps,
+                                       double* graddivs, double* cpot, double* dpot,
+                                       double* divd) {
+    if (!c || !c->todd) return MG_ERR_ARG;
+    auto cp = [](double* dst, const std::vector<double>& s) {
+        if (dst) std::memcpy(dst, s.data(), s.size() * sizeof(double));
+    };
+    cp(vect, c->vecT); cp(vecf, c->vecF); cp(laps, c->lapS); cp(graddivs, c->gdivS);
+    cp(cpot, c->Cpot); cp(dpot, c->Dpot); cp(divd, c->divD);
     return MG_OK;
 }
 
@@ -1471,6 +1664,16 @@ static void time_odd_potentials(orc_ctx* c) {
                 double sv = (B.B9 + B.B9q) * c->rotj[q] + B.B9 * c->rotj[qa] +
                             2.0 * ((B.B10 + B.B11) * c->vecs[q] + B.B10 * c->vecs[qa]) +
                             2.0 * ((B.B12a + B.B13a) * (ra * c->vecs[q]) + B.B12a * (ra * c->vecs[qa]));
+                if (c->todd) {
+                    // the time-odd tensor terms of CalcSPot (src/MeanFields.f90:651-670)
+                    if (B.B14 != 0.0 || B.B15 != 0.0)
+                        sv = sv - (B.B14 + B.B15) * c->vecT[q] - B.B14 * c->vecT[qa];
+                    if (B.B16 != 0.0 || B.B17 != 0.0)
+                        sv = sv - 2.0 * (B.B16 + B.B17) * c->vecF[q] - 2.0 * B.B16 * c->vecF[qa];
+                    if (B.B18 != 0.0 || B.B19 != 0.0 || B.B20 != 0.0 || B.B21 != 0.0)
+                        sv = sv + 2.0 * ((B.B18 + B.B19) * c->lapS[q] + B.B18 * c->lapS[qa]) -
+                             2.0 * ((B.B20 + B.B21) * c->gdivS[q] - B.B20 * c->gdivS[qa]);
+                }
                 if (B.B12b != 0.0 || B.B13b != 0.0) {
                     const double rb = std::pow(rt, B.byt3b);
                     sv = sv + 2.0 * ((B.B12b + B.B13b) * (rb * c->vecs[q]) + B.B12b * (rb * c->vecs[qa]));
@@ -1507,6 +1710,27 @@ static void time_odd_potentials(orc_ctx* c) {
         derive_grid(c, &c->Apot[(it * 3 + 1) * V], 1, -P, -S, TS, 1, t2.data());
         derive_grid(c, &c->Apot[(it * 3 + 2) * V], 2, -P, S, TS, 2, t3.data());
         for (long v = 0; v < V; ++v) c->divA[it * V + v] = t1[v] + t2[v] + t3[v];
+    }
+    if (!c->todd) return;
+    // CalcCPot: C_q = -B14 s_t - B15 s_q; CalcDPot: D_q = -2 B16 s_t - 2 B17 s_q,
+    // d_n D_m with the s symmetries, div D (src/MeanFields.f90:714-790)
+    for (int it = 0; it < 2; ++it)
+        for (int m = 0; m < 3; ++m)
+            for (long v = 0; v < V; ++v) {
+                const double st = c->vecs[m * V + v] + c->vecs[(3 + m) * V + v];
+                const double sq = c->vecs[(it * 3 + m) * V + v];
+                c->Cpot[(it * 3 + m) * V + v] = -(B.B14 * st) - B.B15 * sq;
+                c->Dpot[(it * 3 + m) * V + v] = -(2 * B.B16 * st) - 2 * B.B17 * sq;
+            }
+    for (int it = 0; it < 2; ++it) {
+        for (int m = 0; m < 3; ++m)
+            for (int n = 0; n < 3; ++n)
+                derive_grid(c, &c->Dpot[(it * 3 + m) * V], n, P, m == 2 ? S : -S, TS,
+                            m == 1 ? 2 : 1, &c->dD[((it * 3 + m) * 3 + n) * V]);
+        for (long v = 0; v < V; ++v)
+            c->divD[it * V + v] = c->dD[((it * 3 + 0) * 3 + 0) * V + v] +
+                                  c->dD[((it * 3 + 1) * 3 + 1) * V + v] +
+                                  c->dD[((it * 3 + 2) * 3 + 2) * V + v];
     }
 }
 
@@ -1801,6 +2025,39 @@ extern "C" int orc_energy(orc_ctx* c, mg_energy_terms* out) {
         t[4] = -B.B3 * j2; t[5] = q6; t[12] = B.B9 * jrs; t[13] = q14;
         t[14] = B.B10 * s2t; t[15] = q16; t[16] = B.B12a * s2a; t[17] = q18;
         t[34] = B.B12b * s2b; t[35] = q36;
+    }
+    if (c->todd) {
+        // time-odd tensor terms 21, 22, 27-32 of compSkyrme (src/Energy.f90:
+        // 775-845); 31 and 32 square the divergence of s, which the
+        // reference's density code never assigns (zero)
+        double sT = 0, sF = 0, sL = 0, qT = 0, qF = 0, qL = 0;
+        for (int m = 0; m < 3; ++m)
+            for (long v = 0; v < V; ++v) {
+                const double st = c->vecs[m * V + v] + c->vecs[(3 + m) * V + v];
+                sT += st * (c->vecT[m * V + v] + c->vecT[(3 + m) * V + v]);
+                sF += st * (c->vecF[m * V + v] + c->vecF[(3 + m) * V + v]);
+                sL += st * (c->lapS[m * V + v] + c->lapS[(3 + m) * V + v]);
+            }
+        for (int it = 0; it < 2; ++it) {
+            double aF = 0, aL = 0;
+            for (int m = 0; m < 3; ++m)
+                for (long v = 0; v < V; ++v) {
+                    const long q = (it * 3 + m) * V + v;
+                    qT += c->vecs[q] * c->vecT[q];
+                    aF += c->vecs[q] * c->vecF[q];
+                    aL += c->vecs[q] * c->lapS[q];
+                }
+            qF = qF - 2.0 * B.B17 * aF;
+            qL = qL + B.B19 * aL;
+        }
+        t[20] = B.B14 != 0.0 ? -B.B14 * sT : 0.0;
+        t[21] = B.B15 != 0.0 ? -B.B15 * qT : 0.0;
+        t[26] = B.B16 != 0.0 ? -2.0 * B.B16 * sF : 0.0;
+        t[27] = B.B17 != 0.0 ? qF : 0.0;
+        t[28] = B.B18 != 0.0 ? B.B18 * sL : 0.0;
+        t[29] = B.B19 != 0.0 ? qL : 0.0;
+        t[30] = 0.0;
+        t[31] = 0.0;
     }
     if (c->tensor) {
         // J^2 terms 19, 20, 23-26 of compSkyrme (src/Energy.f90:763-810)

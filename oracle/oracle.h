@@ -60,6 +60,12 @@ int orc_mix_densities(orc_ctx* c);
 int orc_get_densities(orc_ctx* c, double* rho, double* tau, double* nablaj,
                       double* derrho, double* laprho);
 int orc_get_jmunu(orc_ctx* c, double* jmunu);   /* 18V: [it][nu][mu][V] */
+/* time-odd tensor densities and fields without time reversal: T, F, lap s,
+ * grad div s, C, D as [it][m][V], div D as [it][V] (any may be NULL) */
+int orc_get_time_odd_tensor(orc_ctx* c, double* vect, double* vecf, double* laps,
+                            double* graddivs, double* cpot, double* dpot, double* divd);
+/* ActionOfC and ActionOfD of spwf i of basis b (4V each) */
+int orc_tensor_odd_action(orc_ctx* c, int b, int i, double* xc, double* xd);
 int orc_set_densities(orc_ctx* c, const double* rho, const double* tau,
                       const double* nablaj, const double* derrho,
                       const double* laprho);

@@ -72,6 +72,8 @@ _SIG = {
     "orc_eigh": ([C.c_int, _D, _D, _D], C.c_int),
     "orc_set_threads": ([C.c_int], C.c_int),
     "orc_get_time_odd": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
+    "orc_get_time_odd_tensor": ([_P, _D, _D, _D, _D, _D, _D, _D], C.c_int),
+    "orc_tensor_odd_action": ([_P, C.c_int, C.c_int, _D, _D], C.c_int),
     "orc_symmetry_operators": ([_P, C.c_int, _D], C.c_int),
 }
 
@@ -224,6 +226,21 @@ class OracleState:
         self._call("orc_get_time_odd", *(_d(out[k]) for k in
                                           ("vecj", "vecs", "rotj", "rots", "A", "S", "divA")))
         return out
+
+    TENSOR_ODD = ("T", "F", "lapS", "gradDivS", "C", "D", "divD")
+
+    def get_time_odd_tensor(self):
+        """T, F, lap s, grad div s, C, D as [it][m][V] and div D as [it][V]."""
+        V = self.V
+        out = {k: np.empty((2 if k == "divD" else 6) * V) for k in self.TENSOR_ODD}
+        self._call("orc_get_time_odd_tensor", *(_d(out[k]) for k in self.TENSOR_ODD))
+        return out
+
+    def tensor_odd_action(self, i, basis=_abi.MG_HF_BASIS):
+        """ActionOfC and ActionOfD of spwf i (4V each)."""
+        xc, xd = np.empty(4 * self.V), np.empty(4 * self.V)
+        self._call("orc_tensor_odd_action", basis, i, _d(xc), _d(xd))
+        return xc, xd
 
     def set_potentials(self, U=None, B=None, nablaB=None, W=None, divW=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)

@@ -94,16 +94,26 @@ def test_tensor_coefficients():
     assert b.B14 == 0.0 and b.B15 == 0.0 and b.B16 == a.B16 and b.B17 == a.B17
 
 
-def test_tensor_terms_need_time_reversal(built):
-    """The J^2 terms are built time-even only: a force with them and broken
-    time reversal is refused before any CUDA call."""
-    from mocca_gb300.forces import SLY5_TENSOR
+def test_time_odd_tensor_coefficients():
+    """CalcEDFCoef's time-odd tensor coefficients (src/Force.f90:539-551):
+    with broken time reversal B18 = -(3 t1 x1 - t2 x2)/32 + (3 te - to)/16,
+    B19 = (3 t1 + t2)/32 - (3 te + to)/16 (J2Terms only), B20 = 3 (3 te -
+    to)/16, B21 = -3 (3 te + to)/16 (te, to alone); all four zero with time
+    reversal."""
+    import dataclasses
+    from mocca_gb300.forces import SLY5_TENSOR as T
     lib = _abi.load()
-    params = RunParams(nx=10, ny=10, nz=10, trc=0).to_c()
-    ctx = C.c_void_p()
-    assert lib.mg_create(C.byref(params), SLY5_TENSOR.to_c(), None,
-                         C.byref(ctx)) == _abi.MG_ERR_ARG
-    assert not ctx.value
+    a, b, c = _abi.MgSkyrmeB(), _abi.MgSkyrmeB(), _abi.MgSkyrmeB()
+    assert lib.mg_skyrme_coefficients(T.to_c(), 0, a) == 0
+    assert a.B18 == pytest.approx(-(3 * T.t1 * T.x1 - T.t2 * T.x2) / 32 + (3 * T.te - T.to) / 16,
+                                  rel=1e-14)
+    assert a.B19 == pytest.approx((3 * T.t1 + T.t2) / 32 - (3 * T.te + T.to) / 16, rel=1e-14)
+    assert a.B20 == pytest.approx(3 * (3 * T.te - T.to) / 16, rel=1e-14)
+    assert a.B21 == pytest.approx(-3 * (3 * T.te + T.to) / 16, rel=1e-14)
+    assert lib.mg_skyrme_coefficients(dataclasses.replace(T, j2terms=False).to_c(), 0, b) == 0
+    assert b.B18 == 0.0 and b.B19 == 0.0 and b.B20 == a.B20 and b.B21 == a.B21
+    assert lib.mg_skyrme_coefficients(T.to_c(), 1, c) == 0
+    assert c.B18 == c.B19 == c.B20 == c.B21 == 0.0
 
 
 def test_product_does_not_use_the_oracle():
