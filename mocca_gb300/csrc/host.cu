@@ -42,7 +42,7 @@ void free_all(mg_ctx* c) {
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast); F(c->cguess);
-    F(c->dhist); F(c->Uold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
+    F(c->dhist); F(c->Uold); F(c->Sold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
     F(c->odd); F(c->odd_hist); F(c->Apot); F(c->Spot); F(c->divA); F(c->odd_der); F(c->odd_tmp);
     F(c->odd_jobs);
     F(c->Cpot); F(c->Dpot); F(c->dDpot); F(c->divD); F(c->todd_tmp); F(c->todd_work);
@@ -600,6 +600,9 @@ extern "C" int mg_construct_potentials(mg_ctx* c, int* iters) {
     // preconditions the update once UpotOld is not all zero
     MG_CUDA(cudaMemcpyAsync(c->Uold, c->U, 2 * c->V * sizeof(double), cudaMemcpyDeviceToDevice,
                             c->stream));
+    if (c->Sold)   // SpotOld = Spot (src/PotentialMixing.f90:122)
+        MG_CUDA(cudaMemcpyAsync(c->Sold, c->Spot, 6 * c->V * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
     MG_TRY(potentials(c));
     if (c->p.mixing_scheme == 2 && c->have_uold) MG_TRY(precondition_u(c));
     c->have_uold = true;

@@ -7,7 +7,9 @@
 //     densities as that history.
 //   scheme 2: the U update is preconditioned instead,
 //     Upot = UpotOld + PreconditionPotential(Upot - UpotOld)
-//     (src/PotentialMixing.f90:143-154, src/Damping.f90:158-228): per isospin
+//     and, without time reversal, each component of the S update with the
+//     symmetries of s (src/PotentialMixing.f90:143-168,
+//     src/Damping.f90:158-228): per isospin
 //     a CG on (beta + alpha Lap) x = dU with alpha = -preconu, beta = 1 and
 //     the Lagrange Laplacian, at most 300 steps, stopping when
 //     sum(residual^2) dv < 1e-8.  Both isospins step together with their own
@@ -89,9 +91,10 @@ __global__ void k_pc_direction(double* __restrict__ dir, const double* __restric
     dir[it * V + v] = res[it * V + v] + b * dir[it * V + v];
 }
 
-// dir = res = dU, inv = 0, block partials of dU.dU
+// dir = res = dU, inv = 0, block partials of dU.dU (the potential's
+// isospins stride apart)
 __global__ void __launch_bounds__(kThreads)
-k_pc_start(const double* __restrict__ U, const double* __restrict__ Uold,
+k_pc_start(const double* __restrict__ U, const double* __restrict__ Uold, long stride,
            double* __restrict__ res, double* __restrict__ dir, double* __restrict__ inv, long V,
            double* __restrict__ part) {
     __shared__ double red[kThreads / 32];
@@ -100,7 +103,7 @@ k_pc_start(const double* __restrict__ U, const double* __restrict__ Uold,
     double s = 0.0;
     if (v < V) {
         const long o = it * V + v;
-        const double d = U[o] - Uold[o];
+        const double d = U[it * stride + v] - Uold[it * stride + v];
         res[o] = d;
         dir[o] = d;
         inv[o] = 0.0;
@@ -110,10 +113,11 @@ k_pc_start(const double* __restrict__ U, const double* __restrict__ Uold,
     if (threadIdx.x == 0) part[(long)it * gridDim.x + blockIdx.x] = t;
 }
 
-__global__ void k_pc_finish(double* __restrict__ U, const double* __restrict__ Uold,
-                            const double* __restrict__ inv, long n) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) U[t] = Uold[t] + inv[t];
+__global__ void k_pc_finish(double* __restrict__ U, const double* __restrict__ Uold, long stride,
+                            const double* __restrict__ inv, long V) {
+    const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int it = blockIdx.y;
+    if (v < V) U[it * stride + v] = Uold[it * stride + v] + inv[it * V + v];
 }
 
 }  // namespace
@@ -127,17 +131,24 @@ int mixing_setup(mg_ctx* c) {
     };
     if (!(A(&c->dhist, 14 * V) && A(&c->Uold, 2 * V) && A(&c->pc_buf, 10 * V)))
         return MG_ERR_CUDA;
-    std::vector<GridJob> jobs(2);
+    if (!c->p.trc && !A(&c->Sold, 6 * V)) return MG_ERR_CUDA;
+    // the Laplacian of the direction: U (P, S, TS, 1), then the S components
+    // (P, -S, TS, 1), (P, -S, TS, 2), (P, S, TS, 1)
+    std::vector<GridJob> jobs(8);
     const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
-    for (int it = 0; it < 2; ++it) {
-        GridJob J{};
-        J.in = c->pc_buf + (2 + it) * V;        // direction
-        J.lap = c->pc_buf + (6 + it) * V;       // Laplacian of the direction
-        for (int d = 0; d < 3; ++d) J.slot[d] = (int8_t)lag_slot(d, P, S, TS, 1);
-        jobs[it] = J;
-    }
-    MG_CUDA(cudaMalloc(&c->pc_jobs, 2 * sizeof(GridJob)));
-    MG_CUDA(cudaMemcpy(c->pc_jobs, jobs.data(), 2 * sizeof(GridJob), cudaMemcpyHostToDevice));
+    const int sym[4][2] = {{S, 1}, {-S, 1}, {-S, 2}, {S, 1}};
+    for (int k = 0; k < 4; ++k)
+        for (int it = 0; it < 2; ++it) {
+            GridJob J{};
+            J.in = c->pc_buf + (2 + it) * V;        // direction
+            J.lap = c->pc_buf + (6 + it) * V;       // Laplacian of the direction
+            for (int d = 0; d < 3; ++d)
+                J.slot[d] = (int8_t)lag_slot(d, P, sym[k][0], TS, sym[k][1]);
+            jobs[2 * k + it] = J;
+        }
+    MG_CUDA(cudaMalloc(&c->pc_jobs, jobs.size() * sizeof(GridJob)));
+    MG_CUDA(cudaMemcpy(c->pc_jobs, jobs.data(), jobs.size() * sizeof(GridJob),
+                       cudaMemcpyHostToDevice));
     return MG_OK;
 }
 
@@ -199,8 +210,10 @@ static int read_pair(mg_ctx* c, int nblk, std::vector<double>& h, double out[2])
     return MG_OK;
 }
 
-// Upot = UpotOld + PreconditionPotential(Upot - UpotOld)
-int precondition_u(mg_ctx* c) {
+// F = Fold + PreconditionPotential(F - Fold) for a potential whose two
+// isospins lie stride apart, with the Laplacian jobs of its symmetry
+static int precondition_pot(mg_ctx* c, double* F, const double* Fold, long stride,
+                            const GridJob* jobs) {
     const long V = c->V;
     const int nblk = div_up(V, kThreads);
     const dim3 g2(nblk, 2);
@@ -212,12 +225,12 @@ int precondition_u(mg_ctx* c) {
     const double alpha = -c->p.precon_u, beta = 1.0;
     std::vector<double> h((size_t)2 * nblk);
     double nn[2], dd[2], nn_new[2];
-    k_pc_start<<<g2, kThreads, 0, c->stream>>>(c->U, c->Uold, res, dir, inv, V, c->red);
+    k_pc_start<<<g2, kThreads, 0, c->stream>>>(F, Fold, stride, res, dir, inv, V, c->red);
     MG_LAUNCHED(c);
     MG_TRY(read_pair(c, nblk, h, nn));
     bool conv[2] = {false, false};
     for (int iter = 1; iter <= 300 && !(conv[0] && conv[1]); ++iter) {
-        MG_TRY(run_jobs(c, c->pc_jobs, 2));
+        MG_TRY(run_jobs(c, jobs, 2));
         k_pc_update<<<g2, kThreads, 0, c->stream>>>(dir, lap, upd, V, alpha, beta, c->red);
         MG_LAUNCHED(c);
         MG_TRY(read_pair(c, nblk, h, dd));
@@ -237,8 +250,20 @@ int precondition_u(mg_ctx* c) {
         for (int it = 0; it < 2; ++it)
             if (!conv[it] && nn[it] < 1e-8) conv[it] = true;
     }
-    k_pc_finish<<<div_up(2 * V, kThreads), kThreads, 0, c->stream>>>(c->U, c->Uold, inv, 2 * V);
+    k_pc_finish<<<g2, kThreads, 0, c->stream>>>(F, Fold, stride, inv, V);
     MG_LAUNCHED(c);
+    return MG_OK;
+}
+
+// Upot = UpotOld + PreconditionPotential(Upot - UpotOld); without time
+// reversal each S component the same way
+int precondition_u(mg_ctx* c) {
+    const long V = c->V;
+    MG_TRY(precondition_pot(c, c->U, c->Uold, V, c->pc_jobs));
+    if (!c->p.trc)
+        for (int m = 0; m < 3; ++m)
+            MG_TRY(precondition_pot(c, c->Spot + m * V, c->Sold + m * V, 3 * V,
+                                    c->pc_jobs + 2 * (m + 1)));
     return MG_OK;
 }
 

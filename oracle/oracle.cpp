@@ -1853,13 +1853,12 @@ static void calc_potentials(orc_ctx* c) {
 
 // PreconditionPotential + preconoperator, src/Damping.f90:158-228: per
 // isospin, CG on (beta + alpha Lap) x = pot with alpha = -preconu, beta = 1,
-// the Lagrange Laplacian of a (P, S, TS)-even scalar, at most 300 steps,
-// stop when sum(residual^2) dv < 1e-8.
+// the Lagrange Laplacian with the potential's symmetry arguments, at most
+// 300 steps, stop when sum(residual^2) dv < 1e-8.
 static void precondition_potential(orc_ctx* c, const std::vector<double>& pot,
-                                   std::vector<double>& inv) {
+                                   std::vector<double>& inv, int P, int S, int TS, int comp) {
     const long V = c->V;
     const double alpha = -c->p.precon_u, beta = 1.0;
-    const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
     inv.assign(2 * V, 0.0);
     std::vector<double> res(V), dir(V), upd(V), lap(V);
     for (int it = 0; it < 2; ++it) {
@@ -1869,7 +1868,7 @@ static void precondition_potential(orc_ctx* c, const std::vector<double>& pot,
         for (long v = 0; v < V; ++v) nn = nn + dir[v] * dir[v];
         nn = nn * c->dv;
         for (int iter = 1; iter <= 300; ++iter) {
-            derive_grid(c, dir.data(), 3, P, S, TS, 1, lap.data());
+            derive_grid(c, dir.data(), 3, P, S, TS, comp, lap.data());
             for (long v = 0; v < V; ++v) upd[v] = beta * dir[v] + alpha * lap[v];
             double dd = 0.0;
             for (long v = 0; v < V; ++v) dd = dd + dir[v] * upd[v];
@@ -1893,6 +1892,7 @@ extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
     if (!c) return MG_ERR_ARG;
     int st = MG_OK;
     c->Uold = c->U;   // UpotOld = Upot (src/PotentialMixing.f90:115)
+    const std::vector<double> Sold = c->Spot;   // SpotOld = Spot (:122)
     if (c->p.coulomb_solver != 0) {
         st = orc_solve_coulomb(c, iters);
         if (st < 0) return st;
@@ -1909,8 +1909,24 @@ extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
     if (c->p.mixing_scheme == 2 && have_old) {
         std::vector<double> du(c->U.size()), inv;
         for (size_t k = 0; k < du.size(); ++k) du[k] = c->U[k] - c->Uold[k];
-        precondition_potential(c, du, inv);
+        const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
+        precondition_potential(c, du, inv, P, S, TS, 1);
         for (size_t k = 0; k < du.size(); ++k) c->U[k] = c->Uold[k] + inv[k];
+        if (!c->p.trc) {
+            // each S component: (P, -S, TS, 1), (P, -S, TS, 2), (P, S, TS, 1)
+            // (src/PotentialMixing.f90:156-168)
+            const long V = c->V;
+            for (int m = 0; m < 3; ++m) {
+                std::vector<double> ds(2 * V);
+                for (int it = 0; it < 2; ++it)
+                    for (long v = 0; v < V; ++v)
+                        ds[it * V + v] = c->Spot[(it * 3 + m) * V + v] - Sold[(it * 3 + m) * V + v];
+                precondition_potential(c, ds, inv, P, m == 2 ? S : -S, TS, m == 1 ? 2 : 1);
+                for (int it = 0; it < 2; ++it)
+                    for (long v = 0; v < V; ++v)
+                        c->Spot[(it * 3 + m) * V + v] = Sold[(it * 3 + m) * V + v] + inv[it * V + v];
+            }
+        }
     }
     return st;
 }

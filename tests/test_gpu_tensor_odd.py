@@ -8,8 +8,9 @@ other time-odd densities and fields and h.psi within 1e-12 norm-wise and
 pointwise (max |a - b| / max |b|), T and F within 1e-12 of max tau (the size
 of their terms, which time-reversed partners cancel), both sides computing
 them from the same spinors; the total energy within 1e-8 MeV at the start and after each of 4
-iterations, with the fixed step and with ParameterEstimation = 1 (whose
-probe takes the C and D actions too).  With Omega = 0 the 80-spwf run
+iterations, with the fixed step, with ParameterEstimation = 1 (whose
+probe takes the C and D actions too) and with MixingScheme 2 (the S update
+preconditioned like U's).  With Omega = 0 the 80-spwf run
 reproduces the 40-spwf time-reversal-invariant one (1e-9 MeV)."""
 import dataclasses
 
@@ -84,10 +85,12 @@ def test_tensor_odd_fields_and_hpsi_against_oracle(built):
     o.close()
 
 
-@pytest.mark.parametrize("estimate", [0, 1])
-def test_tensor_odd_iterations_against_oracle(built, estimate):
+@pytest.mark.parametrize("estimate,mixing", [(0, 0), (1, 0), (0, 2)])
+def test_tensor_odd_iterations_against_oracle(built, estimate, mixing):
+    """mixing 2: MixingScheme 2 preconditions the U update and, without
+    time reversal, each component of the S update."""
     _, _, p, s80 = cranked_start(0.5)
-    p = dataclasses.replace(p, parameter_estimation=estimate)
+    p = dataclasses.replace(p, parameter_estimation=estimate, mixing_scheme=mixing)
     g, o = _pair(p, *s80)
     de = [abs(g.CompEnergy()["total"] - o.CompEnergy()["total"])]
     for _ in range(4):
