@@ -29,6 +29,70 @@ int block_of(const mg_wf_header& h, const int* qn) {
     return P + h.pindex * it;
 }
 
+// The time-odd density records WriteDensity writes without time reversal
+// (src/Densities.f90:1214-1238): 1 j and rot j, 2 s, rot s and DerS, then,
+// where the functional allocates them (src/Densities.f90:163-178), 4 lap s,
+// div s and grad div s, 8 T, 16 F.
+int odd_record_mask(const mg_ctx* c) {
+    if (c->p.trc || !c->odd) return 0;
+    int rec = 1 | 2;
+    if (c->todd) {
+        const mg_skyrme_b& B = c->B;
+        if (B.B18 != 0.0 || B.B19 != 0.0 || B.B20 != 0.0 || B.B21 != 0.0) rec |= 4;
+        if (B.B14 != 0.0 || B.B15 != 0.0) rec |= 8;
+        if (B.B16 != 0.0 || B.B17 != 0.0) rec |= 16;
+    }
+    return rec;
+}
+
+// DerS as the reference's Density holds it after the iteration: the mixing
+// operators carry DerS only beside lap s (src/Densities.f90:262-266,
+// :328-333), so MixDensities' scheme 0 leaves it zero unless lap s is
+// allocated; otherwise it is d_a s_m of the current s (the mixed
+// derivatives equal the derivatives of the mixed s by linearity), with
+// the arguments (P, -S, TS, 1), (P, -S, TS, 2), (P, S, TS, 1) of the
+// components.  out: [it][m][a][V].
+int wf_ders(mg_ctx* c, bool with_laps, double* out) {
+    const long V = c->V;
+    if (c->p.mixing_scheme == 0 && !with_laps) {
+        std::fill(out, out + 18 * V, 0.0);
+        return MG_OK;
+    }
+    double* d = nullptr;
+    GridJob* jd = nullptr;
+    std::vector<GridJob> jobs(6);
+    auto done = [&](int st) {
+        if (d) cudaFree(d);
+        if (jd) cudaFree(jd);
+        return st;
+    };
+    if (cudaMalloc(&d, 18 * V * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&jd, jobs.size() * sizeof(GridJob)) != cudaSuccess)
+        return done(MG_ERR_CUDA);
+    for (int it = 0; it < 2; ++it)
+        for (int m = 0; m < 3; ++m) {
+            GridJob& J = jobs[it * 3 + m];
+            J = GridJob{};
+            J.in = c->odd + (6 + it * 3 + m) * V;
+            double* o = d + (it * 3 + m) * 3 * V;
+            J.dx = o;
+            J.dy = o + V;
+            J.dz = o + 2 * V;
+            const int ss = m == 2 ? 1 : -1, comp = m == 1 ? 2 : 1;
+            for (int a = 0; a < 3; ++a) J.slot[a] = (int8_t)lag_slot(a, 1, ss, 1, comp);
+        }
+    if (cudaMemcpy(jd, jobs.data(), jobs.size() * sizeof(GridJob), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return done(MG_ERR_CUDA);
+    int st = run_jobs(c, jd, 6);
+    if (st == MG_OK &&
+        (cudaMemcpyAsync(out, d, 18 * V * sizeof(double), cudaMemcpyDeviceToHost, c->stream) !=
+             cudaSuccess ||
+         cudaStreamSynchronize(c->stream) != cudaSuccess))
+        st = MG_ERR_CUDA;
+    return done(st);
+}
+
 // GuessHFBMatrices(0) (src/HFB.f90:3686-3718): blocksizes of the HFB
 // indices (stored spwfs, then their time-reversed partners with
 // opposite signature) and kappa = +-0.1 between opposite signatures, in
@@ -182,7 +246,7 @@ int from_context(mg_ctx* c, const char* force_name, mg_wf& w) {
     h.fermi[0] = c->hfb.fermi[0];
     h.fermi[1] = c->hfb.fermi[1];
     for (int k = 0; k < 3; ++k) h.omega[k] = c->p.omega[k];
-    h.odd_records = (!c->p.trc && c->odd) ? 1 : 0;   // vecj, rotvecj
+    h.odd_records = odd_record_mask(c);
     h.has_jmunu = c->tensor ? 1 : 0;
     h.n_moments = 0;
     for (const MomentConstraint& k : c->cons.list) h.n_moments += k.type != 0;
@@ -226,8 +290,18 @@ int from_context(mg_ctx* c, const char* force_name, mg_wf& w) {
                             w.d[MG_WF_LAPRHO].data()));
     if (h.has_jmunu) MG_TRY(mg_get_jmunu(c, w.d[MG_WF_JMUNU].data()));
     if (h.odd_records & 1) {
-        double* o = w.d[MG_WF_ODD1].data();
-        MG_TRY(mg_get_time_odd(c, o, nullptr, o + 6 * V, nullptr, nullptr, nullptr, nullptr));
+        double* o1 = w.d[MG_WF_ODD1].data();
+        double* o2 = w.d[MG_WF_ODD2].data();
+        MG_TRY(mg_get_time_odd(c, o1, o2, o1 + 6 * V, o2 + 6 * V, nullptr, nullptr, nullptr));
+        MG_TRY(wf_ders(c, (h.odd_records & 4) != 0, o2 + 12 * V));
+    }
+    if (h.odd_records & (4 | 8 | 16)) {
+        // lap s, div s (never assigned by the reference: zero), grad div s; T; F
+        double* o3 = (h.odd_records & 4) ? w.d[MG_WF_ODD3].data() : nullptr;
+        if (o3) std::fill(o3 + 6 * V, o3 + 8 * V, 0.0);
+        MG_TRY(mg_get_time_odd_tensor(c, (h.odd_records & 8) ? w.d[MG_WF_ODD4].data() : nullptr,
+                                      (h.odd_records & 16) ? w.d[MG_WF_ODD5].data() : nullptr,
+                                      o3, o3 ? o3 + 8 * V : nullptr, nullptr, nullptr, nullptr));
     }
     // pairing and the HFB matrices
     if (hfb) {
@@ -307,6 +381,30 @@ int to_context(mg_ctx* c, const mg_wf& w) {
     MG_TRY(mg_set_densities(c, w.d[MG_WF_RHO].data(), w.d[MG_WF_TAU].data(),
                             w.d[MG_WF_NABLAJ].data(), w.d[MG_WF_DERRHO].data(),
                             w.d[MG_WF_LAPRHO].data()));
+    // the time-odd densities as ReadDensity takes them
+    // (src/Densities.f90:1280-1340): from the records that are there, else
+    // zero (DerS and div s are not kept: the next densities recompute them)
+    if (!p.trc && c->odd) {
+        std::vector<double> o((size_t)c->odd_len * V, 0.0);
+        auto put = [&](int field, long src_off, long dst_off, long n) {
+            if (w.d[field].size() >= (size_t)(src_off + n))
+                std::copy(w.d[field].begin() + src_off, w.d[field].begin() + src_off + n,
+                          o.begin() + dst_off);
+        };
+        put(MG_WF_ODD1, 0, 0, 6 * V);             // j
+        put(MG_WF_ODD1, 6 * V, 12 * V, 6 * V);    // rot j
+        put(MG_WF_ODD2, 0, 6 * V, 6 * V);         // s
+        put(MG_WF_ODD2, 6 * V, 18 * V, 6 * V);    // rot s
+        if (c->todd) {
+            put(MG_WF_ODD4, 0, 24 * V, 6 * V);        // T
+            put(MG_WF_ODD5, 0, 30 * V, 6 * V);        // F
+            put(MG_WF_ODD3, 0, 36 * V, 6 * V);        // lap s
+            put(MG_WF_ODD3, 8 * V, 42 * V, 6 * V);    // grad div s
+        }
+        MG_CUDA(cudaMemcpyAsync(c->odd, o.data(), o.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, c->stream));
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+    }
     // JMuNu as ReadDensity takes it: from the file when there, else zero
     if (c->tensor) {
         std::vector<double> zero;

@@ -15,7 +15,8 @@ the last evaluation); CanTransfo's columns the eigenvectors of the block
 rho in DiagonaliseRhoHFB's order (1e-10).  An HF restart from the file
 reproduces the writer's energy (1e-7 MeV) and then runs exactly as a
 context handed the same state through the other entry points; an HFB
-restart starts from the file's kappa and Fermi energies.
+restart starts from the file's kappa and Fermi energies.  Without time
+reversal the time-odd density records are written and read back.
 """
 import numpy as np
 import pytest
@@ -256,3 +257,65 @@ def test_angular_momentum_mixed_derivatives(built):
     assert np.abs(jm - jd).max() < 1e-9 * max(1.0, np.abs(jd).max())
     assert np.abs(jd[:, :2]).max() == 0.0      # signature conserved: Jx = Jy = 0
     g.close()
+
+
+@pytest.mark.parametrize("tensor", [False, True])
+def test_time_odd_records(built, tmp_path, tensor):
+    """Without time reversal (cranked about z) the file carries the time-odd
+    density records WriteDensity writes: j and rot j; s, rot s and DerS;
+    with SLy5colo's tensor terms also lap s, div s (zero: the reference
+    never assigns it) and grad div s, T and F; each bit-exact with the
+    context's read-outs.  DerS is zero after SLy4's linearly mixed
+    iteration (the mixing carries it only beside lap s) and d_a s_m of the
+    current s (1e-12 against the oracle's Lagrange derivative) with lap s.
+    A restart from the file takes every time-odd density back bit-exact."""
+    import oracle as O
+    from mocca_gb300.forces import SLY5_TENSOR
+    from test_oracle_time_odd import cranked_start
+    force = SLY5_TENSOR if tensor else SLY4
+    _, _, p, (psi, qn, en) = cranked_start(0.5)
+    a = MeshState(p, force)
+    a.set_spinors(psi, qn)
+    a.set_energies(en)
+    a.Start()
+    a.Evolve(3, 0.010, 0.3)
+    V = a.V
+    path = tmp_path / "odd.wf"
+    a.WriteMOCCa(path)
+    with WavefunctionFile.load(path) as w:
+        h, arr = w.header, w.arrays()
+    t = a.get_time_odd()
+    assert h["odd_records"] == (31 if tensor else 3)
+    assert np.array_equal(arr["odd1"], np.concatenate([t["vecj"], t["rotj"]]))
+    assert np.array_equal(arr["odd2"][:12 * V], np.concatenate([t["vecs"], t["rots"]]))
+    ders = arr["odd2"][12 * V:].reshape(2, 3, 3, V)
+    if tensor:
+        tt = a.get_time_odd_tensor()
+        assert np.array_equal(arr["odd3"], np.concatenate([tt["lapS"], np.zeros(2 * V),
+                                                           tt["gradDivS"]]))
+        assert np.array_equal(arr["odd4"], tt["T"])
+        assert np.array_equal(arr["odd5"], tt["F"])
+        o = O.OracleState(p, force)
+        s = t["vecs"].reshape(2, 3, V)
+        for it in range(2):
+            for m in range(3):
+                for d in range(3):
+                    r = o.derive_grid(s[it, m], d, 1, 1 if m == 2 else -1, 1,
+                                      2 if m == 1 else 1).reshape(-1)
+                    err = np.abs(ders[it, m, d] - r).max() / np.abs(r).max()
+                    assert err <= 1e-12, (it, m, d, err)
+        o.close()
+    else:
+        assert not ders.any() and arr["odd3"].size == arr["odd4"].size == arr["odd5"].size == 0
+    b = MeshState(p, force)
+    b.set_spinors(psi, qn)
+    b.ReadMOCCa(path)
+    tb = b.get_time_odd()
+    for k in ("vecj", "vecs", "rotj", "rots"):
+        assert np.array_equal(tb[k], t[k]), k
+    if tensor:
+        ttb = b.get_time_odd_tensor()
+        for k in ("T", "F", "lapS", "gradDivS"):
+            assert np.array_equal(ttb[k], tt[k]), k
+    a.close()
+    b.close()
