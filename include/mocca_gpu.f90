@@ -60,6 +60,7 @@ module mocca_gpu
     integer(c_int) :: com2body
     integer(c_int) :: cexchange
     integer(c_int) :: j2terms
+    integer(c_int) :: coupling
   end type mg_force
   type, bind(C) :: mg_skyrme_b
     real(c_double) :: B1

@@ -108,7 +108,13 @@ typedef struct mg_force {
     int    com1body, com2body, cexchange;
     int    j2terms;      /* J2Terms: the central J^2 terms of t1, t2 and the tensor
                             te, to in B14, B15 (B16, B17 follow te, to always) */
+    int    coupling;     /* CalcEDFCoef's overrides of B14..B17 by force name
+                            (src/Force.f90:552-597): 0 none, MG_COUPLING_* */
 } mg_force;
+
+#define MG_COUPLING_SLY4T    1   /* "SLy4T":    B14 = 15, B15 = -120, B16 = B17 = 0 */
+#define MG_COUPLING_SLY4TMIN 2   /* "SLy4Tmin": the same values                     */
+#define MG_COUPLING_UNEDF2   3   /* "UNEDF2":   B14 = -54.43... + 65.90..., B15 = -2 x 65.90... */
 
 /* The B-coefficients of the energy density (src/Force.f90:467-560).
  * B18, B19 (J2Terms) and B20, B21 (te, to) are time-odd: zero with time

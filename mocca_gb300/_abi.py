@@ -61,7 +61,7 @@ class MgForce(C.Structure):
         "te", "to", "wso", "wsoq", "hbm", "e2", "hbar")] + [
         ("nucleonmass", C.c_double * 2),
         ("com1body", C.c_int), ("com2body", C.c_int), ("cexchange", C.c_int),
-        ("j2terms", C.c_int),
+        ("j2terms", C.c_int), ("coupling", C.c_int),
     ]
 
 

@@ -54,7 +54,12 @@ class Force:
         f.nucleonmass[0], f.nucleonmass[1] = m
         f.com1body, f.com2body, f.cexchange = self.com1body, self.com2body, self.cexchange
         f.j2terms = int(bool(self.j2terms))
+        f.coupling = COUPLING_OVERRIDES.get(self.name.strip().upper(), 0)
         return f
+
+
+# CalcEDFCoef overrides B14..B17 for these names (src/Force.f90:552-597)
+COUPLING_OVERRIDES = {"SLY4T": 1, "SLY4TMIN": 2, "UNEDF2": 3}
 
 
 # &skf "SLy5colo" (forces.param:145-154): SLy5 with the tensor te = 296,

@@ -191,6 +191,19 @@ extern "C" int orc_skyrme_coefficients(const mg_force* f, int trc, mg_skyrme_b* 
         B->B20 = (3.0 / 16.0) * (3 * f->te - f->to);
         B->B21 = -(3.0 / 16.0) * (3 * f->te + f->to);
     }
+    // parameterizations whose tensor couplings the relations above cannot
+    // give, selected by the force's name
+    if (f->coupling == MG_COUPLING_SLY4T || f->coupling == MG_COUPLING_SLY4TMIN) {
+        B->B14 = 15.0;
+        B->B15 = -120.0;
+        B->B16 = 0.0;
+        B->B17 = 0.0;
+    } else if (f->coupling == MG_COUPLING_UNEDF2) {
+        B->B14 = -54.4333635973721002 + 65.9030310445938028;
+        B->B15 = -65.9030310445938028 * 2.0;
+        B->B16 = 0.0;
+        B->B17 = 0.0;
+    }
     return MG_OK;
 }
 

@@ -116,6 +116,38 @@ def test_time_odd_tensor_coefficients():
     assert c.B18 == c.B19 == c.B20 == c.B21 == 0.0
 
 
+@pytest.mark.parametrize("name,b14,b15", [
+    ("SLy4T", 15.0, -120.0), ("sly4tmin", 15.0, -120.0),
+    ("UNEDF2", -54.4333635973721002 + 65.9030310445938028, -65.9030310445938028 * 2.0)])
+def test_named_coupling_overrides(built, name, b14, b15):
+    """CalcEDFCoef overrides B14..B17 for the SLy4T, SLy4Tmin and UNEDF2
+    parameterizations, by name, case-insensitively (src/Force.f90:552-597);
+    the library and the oracle agree, other names keep the relations."""
+    import dataclasses
+    f = dataclasses.replace(SLY4, j2terms=True, name=name)
+    for trc in (1, 0):
+        a, b = _abi.MgSkyrmeB(), _abi.MgSkyrmeB()
+        assert _abi.load().mg_skyrme_coefficients(f.to_c(), trc, a) == 0
+        assert O.load().orc_skyrme_coefficients(f.to_c(), trc, b) == 0
+        assert (a.B14, a.B15, a.B16, a.B17) == (b14, b15, 0.0, 0.0)
+        for n, _ in _abi.MgSkyrmeB._fields_:
+            assert getattr(a, n) == getattr(b, n), n
+    c = _abi.MgSkyrmeB()
+    assert _abi.load().mg_skyrme_coefficients(dataclasses.replace(f, name="SLy4").to_c(), 1,
+                                              c) == 0
+    assert c.B14 == pytest.approx(-(SLY4.t1 * SLY4.x1 + SLY4.t2 * SLY4.x2) / 8, rel=1e-14)
+
+
+def test_coupling_selector_is_checked(built):
+    lib = _abi.load()
+    f = SLY4.to_c()
+    f.coupling = 4
+    params = RunParams(nx=10, ny=10, nz=10).to_c()
+    ctx = C.c_void_p()
+    assert lib.mg_create(C.byref(params), f, None, C.byref(ctx)) == _abi.MG_ERR_ARG
+    assert not ctx.value
+
+
 def test_product_does_not_use_the_oracle():
     for p in list((ROOT / "mocca_gb300").rglob("*.py")) + list((ROOT / "mocca_gb300").rglob("*.cu")):
         txt = p.read_text()
