@@ -203,7 +203,7 @@ __global__ void k_fields_df(Fields F, long V, double kin0, double kin1, float2* 
 }
 
 template <bool kGradStep>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 k_hpsi_df(double* __restrict__ psi, const float2* __restrict__ der,
           const float2* __restrict__ lap, const int* __restrict__ qn,
           const float2* __restrict__ Fd, double* __restrict__ hout, double* __restrict__ upd,
