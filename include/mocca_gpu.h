@@ -160,7 +160,11 @@ typedef struct mg_pairing_params {
                           /* HFBFermiGradient src/GradientHFB.f90:473-733),  */
                           /* max_iter gradient steps at most (the reference  */
                           /* defaults HFBIter to 500 for it); its first U, V */
-                          /* come from one diagonalisation at fermi_start    */
+                          /* come from one diagonalisation at fermi_start;   */
+                          /* 3: FermiSolver 'BISECTION' (bracketing and      */
+                          /* Brent's method, HFBFindFermiEnergyBisection and */
+                          /* FermiBrent, src/HFB.f90:1074-1342, 2273-2487),  */
+                          /* fermi_prec the tolerance on lambda              */
 } mg_pairing_params;
 
 /* Per-call diagnostics of the HFB pairing step. */

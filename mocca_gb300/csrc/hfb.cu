@@ -860,6 +860,133 @@ static int fermi_broyden(mg_ctx* c, double lam[2], double f[2], bool conv[2], in
     return MG_OK;
 }
 
+// FermiBrent (src/HFB.f90:2273-2487): Brent's root search on N(lambda) - N0
+// per isospin from the bracket [a, b] (a == b: nothing to search), both
+// isospins evaluated together at b; the tolerance is prec on lambda.
+static int fermi_brent(mg_ctx* c, double a[2], double b[2], double fa[2], double fb[2],
+                       double prec, bool found[2], int* evals) {
+    double cc[2], fc[2], d[2] = {0.0, 0.0}, e[2] = {0.0, 0.0}, dN[2];
+    for (int it = 0; it < 2; ++it) {
+        found[it] = a[it] == b[it];
+        if (!found[it] && fa[it] * fb[it] > 0.0) return MG_ERR_STATE;   // not bracketed
+        cc[it] = b[it];
+        fc[it] = fb[it];
+    }
+    // each step shrinks the bracket by prec at least; the cap only guards
+    // a non-finite bracket
+    for (int iter = 0; iter < 100000 && !(found[0] && found[1]); ++iter) {
+        for (int it = 0; it < 2; ++it) {
+            if (found[it]) continue;
+            if ((fb[it] > 0.0 && fc[it] > 0.0) || (fb[it] < 0.0 && fc[it] < 0.0)) {
+                cc[it] = a[it];
+                fc[it] = fa[it];
+                d[it] = b[it] - a[it];
+                e[it] = d[it];
+            }
+            if (std::fabs(fc[it]) < std::fabs(fb[it])) {
+                a[it] = b[it];
+                fa[it] = fb[it];
+                b[it] = cc[it];
+                fb[it] = fc[it];
+                cc[it] = a[it];
+                fc[it] = fa[it];
+            }
+            const double tol = prec, xm = 0.5 * (cc[it] - b[it]);
+            if (std::fabs(xm) <= tol) {
+                found[it] = true;
+                continue;
+            }
+            if (std::fabs(e[it]) >= tol && std::fabs(fa[it]) > std::fabs(fb[it])) {
+                const double sv = fb[it] / fa[it];
+                double p, q;
+                if (a[it] == cc[it]) {
+                    p = 2.0 * xm * sv;
+                    q = 1.0 - sv;
+                } else {
+                    const double qa = fa[it] / fc[it], r = fb[it] / fc[it];
+                    p = sv * (2.0 * xm * qa * (qa - r) - (b[it] - a[it]) * (r - 1.0));
+                    q = (qa - 1.0) * (r - 1.0) * (sv - 1.0);
+                }
+                if (p > 0.0) q = -q;
+                p = std::fabs(p);
+                if (2.0 * p < std::min(3.0 * xm * q - std::fabs(tol * q), std::fabs(e[it] * q))) {
+                    e[it] = d[it];
+                    d[it] = p / q;
+                } else {
+                    d[it] = xm;
+                    e[it] = d[it];
+                }
+            } else {
+                d[it] = xm;
+                e[it] = d[it];
+            }
+            a[it] = b[it];
+            fa[it] = fb[it];
+            b[it] = b[it] + (std::fabs(d[it]) > tol ? d[it] : std::copysign(tol, xm));
+        }
+        MG_TRY(hfb_evaluate(c, b, fb, dN, false));
+        ++*evals;
+    }
+    return MG_OK;
+}
+
+// HFBFindFermiEnergyBisection (src/HFB.f90:1074-1342, FermiSolver
+// 'BISECTION', without LN and the emergency handling the reference keeps
+// off): from the stored Fermi energies, step the boundary on the side of
+// the root out by 0.01 MeV times the attempt (0.01, 0.03, 0.06, ...) until
+// N - N0 changes sign, then Brent's method to prec on lambda.
+static int fermi_bisection(mg_ctx* c, double lam[2], double f[2], bool conv[2], int* evals_out) {
+    Hfb& H = c->hfb;
+    const double prec = H.pp.fermi_prec;
+    const double part[2] = {c->p.neutrons, c->p.protons};
+    int evals = 0;
+    double dN[2];
+    for (int it = 0; it < 2; ++it) lam[it] = part[it] < 0.1 ? -100.0 : H.fermi[it];
+    MG_TRY(hfb_evaluate(c, lam, f, dN, true));
+    ++evals;
+    conv[0] = conv[1] = false;
+    if (std::fabs(f[0]) < prec && std::fabs(f[1]) < prec) {
+        conv[0] = conv[1] = true;
+        *evals_out = evals;
+        return MG_OK;
+    }
+    double br[2][2], fa[2], fb[2];
+    int idir[2], sig[2];
+    bool notfound[2] = {true, true};
+    for (int it = 0; it < 2; ++it) {
+        br[0][it] = br[1][it] = lam[it];
+        idir[it] = f[it] < 0.0 ? 1 : 0;
+        sig[it] = f[it] < 0.0 ? 1 : -1;
+    }
+    for (int fail = 0;; ++fail) {
+        for (int it = 0; it < 2; ++it)
+            if (std::fabs(f[it]) < prec) notfound[it] = false;
+        for (int it = 0; it < 2; ++it)
+            if (notfound[it]) br[idir[it]][it] = br[idir[it]][it] + sig[it] * 0.01 * (fail + 1);
+        MG_TRY(hfb_evaluate(c, br[0], fa, dN, false));
+        MG_TRY(hfb_evaluate(c, br[1], fb, dN, false));
+        evals += 2;
+        for (int it = 0; it < 2; ++it)
+            if (notfound[it] && fa[it] * fb[it] <= 0.0) notfound[it] = false;
+        if (!notfound[0] && !notfound[1]) break;
+        if (fail + 1 > 130) {   // the reference stops: no bracket within ~85 MeV
+            *evals_out = evals;
+            return MG_ERR_STATE;
+        }
+        for (int it = 0; it < 2; ++it)
+            if (notfound[it]) br[1 - idir[it]][it] = br[idir[it]][it];
+    }
+    bool found[2];
+    MG_TRY(fermi_brent(c, br[0], br[1], fa, fb, prec, found, &evals));
+    for (int it = 0; it < 2; ++it) {
+        lam[it] = br[1][it];
+        f[it] = fb[it];
+        conv[it] = found[it];
+    }
+    *evals_out = evals;
+    return MG_OK;
+}
+
 // SolvePairing for HFB (src/Pairing.f90:743-890, PairingIter 1).
 // The canonical-basis decomposition of the four rho_++ blocks.  From the
 // second pairing step on it starts from last step's vectors (the Jacobi warm
@@ -938,6 +1065,8 @@ int hfb_solve(mg_ctx* c, mg_pairing_info* info) {
         MG_TRY(fermi_gradient(c, lam, f, conv, &evals));
     } else if (H.pp.fermi_solver == 1) {
         MG_TRY(fermi_broyden(c, lam, f, conv, &evals));
+    } else if (H.pp.fermi_solver == 3) {
+        MG_TRY(fermi_bisection(c, lam, f, conv, &evals));
     } else {
         MG_TRY(fermi_newton(c, lam, f, conv, &evals, &first_order));
     }

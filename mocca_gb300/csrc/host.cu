@@ -662,7 +662,7 @@ extern "C" int mg_set_pairing(mg_ctx* c, const mg_pairing_params* pp) {
     if (c->hfb.ready) return MG_ERR_STATE;
     if (!(pp->rhosat > 0) || pp->mu[0] <= 0 || pp->mu[1] <= 0 || pp->cut[0] <= 0 || pp->cut[1] <= 0)
         return MG_ERR_ARG;
-    if (pp->fermi_solver < 0 || pp->fermi_solver > 2) return MG_ERR_ARG;
+    if (pp->fermi_solver < 0 || pp->fermi_solver > 3) return MG_ERR_ARG;
     c->hfb.pp = *pp;
     c->hfb.fermi[0] = pp->fermi_start[0];
     c->hfb.fermi[1] = pp->fermi_start[1];

@@ -2587,6 +2587,131 @@ static int fermi_broyden(orc_ctx* c, int* evals) {
     return (conv[0] && conv[1]) ? MG_OK : MG_NOT_CONVERGED;
 }
 
+// FermiBrent, src/HFB.f90:2273-2487: Brent's method per isospin on
+// N(lambda) - N0 from the bracket [a, b] (a == b: nothing to search), both
+// isospins evaluated together at b, tolerance prec on lambda.
+static int fermi_brent(orc_ctx* c, double a[2], double b[2], double fa[2], double fb[2],
+                       double prec, bool found[2], int* ne) {
+    const double part[2] = {c->p.neutrons, c->p.protons};
+    double cc[2], fc[2], d[2] = {0, 0}, e[2] = {0, 0}, N[2];
+    for (int it = 0; it < 2; ++it) {
+        found[it] = a[it] == b[it];
+        if (!found[it] && fa[it] * fb[it] > 0.0) return MG_ERR_STATE;
+        cc[it] = b[it];
+        fc[it] = fb[it];
+    }
+    for (int iter = 0; iter < 100000 && !(found[0] && found[1]); ++iter) {
+        for (int it = 0; it < 2; ++it) {
+            if (found[it]) continue;
+            if ((fb[it] > 0.0 && fc[it] > 0.0) || (fb[it] < 0.0 && fc[it] < 0.0)) {
+                cc[it] = a[it];
+                fc[it] = fa[it];
+                d[it] = b[it] - a[it];
+                e[it] = d[it];
+            }
+            if (std::fabs(fc[it]) < std::fabs(fb[it])) {
+                a[it] = b[it]; fa[it] = fb[it];
+                b[it] = cc[it]; fb[it] = fc[it];
+                cc[it] = a[it]; fc[it] = fa[it];
+            }
+            const double tol = prec, xm = 0.5 * (cc[it] - b[it]);
+            if (std::fabs(xm) <= tol) {
+                found[it] = true;
+                continue;
+            }
+            if (std::fabs(e[it]) >= tol && std::fabs(fa[it]) > std::fabs(fb[it])) {
+                const double sv = fb[it] / fa[it];
+                double p, q;
+                if (a[it] == cc[it]) {
+                    p = 2.0 * xm * sv;
+                    q = 1.0 - sv;
+                } else {
+                    const double qa = fa[it] / fc[it], r = fb[it] / fc[it];
+                    p = sv * (2.0 * xm * qa * (qa - r) - (b[it] - a[it]) * (r - 1.0));
+                    q = (qa - 1.0) * (r - 1.0) * (sv - 1.0);
+                }
+                if (p > 0.0) q = -q;
+                p = std::fabs(p);
+                if (2.0 * p < std::min(3.0 * xm * q - std::fabs(tol * q), std::fabs(e[it] * q))) {
+                    e[it] = d[it];
+                    d[it] = p / q;
+                } else {
+                    d[it] = xm;
+                    e[it] = d[it];
+                }
+            } else {
+                d[it] = xm;
+                e[it] = d[it];
+            }
+            a[it] = b[it];
+            fa[it] = fb[it];
+            b[it] = b[it] + (std::fabs(d[it]) > tol ? d[it] : std::copysign(tol, xm));
+        }
+        int st;
+        if ((st = hfb_number(c, b, N)) != MG_OK) return st;
+        ++*ne;
+        for (int it = 0; it < 2; ++it) fb[it] = N[it] - part[it];
+    }
+    return MG_OK;
+}
+
+// HFBFindFermiEnergyBisection, src/HFB.f90:1074-1342 (no LN; the emergency
+// handling is off in the reference): bracket the root by stepping the
+// boundary on its side out by 0.01 MeV times the attempt, then FermiBrent.
+static int fermi_bisection(orc_ctx* c, int* evals) {
+    const double part[2] = {c->p.neutrons, c->p.protons};
+    const double prec = c->pp.fermi_prec;
+    int ne = 0, st;
+    double N[2];
+    for (int it = 0; it < 2; ++it)
+        if (part[it] < 0.1) c->fermi[it] = -100.0;
+    if ((st = hfb_number(c, c->fermi, N)) != MG_OK) return st;
+    ++ne;
+    for (int it = 0; it < 2; ++it) N[it] -= part[it];
+    bool conv[2] = {std::fabs(N[0]) < prec, std::fabs(N[1]) < prec};
+    if (!(conv[0] && conv[1])) {
+        double br[2][2], fa[2], fb[2], X[2];
+        int idir[2], sig[2];
+        bool notfound[2] = {true, true};
+        for (int it = 0; it < 2; ++it) {
+            br[0][it] = br[1][it] = c->fermi[it];
+            idir[it] = N[it] < 0.0 ? 1 : 0;
+            sig[it] = N[it] < 0.0 ? 1 : -1;
+        }
+        for (int fail = 0;; ++fail) {
+            for (int it = 0; it < 2; ++it)
+                if (std::fabs(N[it]) < prec) notfound[it] = false;
+            for (int it = 0; it < 2; ++it)
+                if (notfound[it]) br[idir[it]][it] = br[idir[it]][it] + sig[it] * 0.01 * (fail + 1);
+            if ((st = hfb_number(c, br[0], X)) != MG_OK) return st;
+            for (int it = 0; it < 2; ++it) fa[it] = X[it] - part[it];
+            if ((st = hfb_number(c, br[1], X)) != MG_OK) return st;
+            for (int it = 0; it < 2; ++it) fb[it] = X[it] - part[it];
+            ne += 2;
+            for (int it = 0; it < 2; ++it)
+                if (notfound[it] && fa[it] * fb[it] <= 0.0) notfound[it] = false;
+            if (!notfound[0] && !notfound[1]) break;
+            if (fail + 1 > 130) return MG_ERR_STATE;
+            for (int it = 0; it < 2; ++it)
+                if (notfound[it]) br[1 - idir[it]][it] = br[idir[it]][it];
+        }
+        bool found[2];
+        if ((st = fermi_brent(c, br[0], br[1], fa, fb, prec, found, &ne)) != MG_OK) return st;
+        for (int it = 0; it < 2; ++it) {
+            c->fermi[it] = br[1][it];
+            N[it] = fb[it];
+            conv[it] = found[it];
+        }
+    }
+    for (int i = 0; i < 6; ++i) c->fermi_hist[i] = c->fermi_hist[i + 1];
+    c->fermi_hist[6] = std::fabs(N[0]) > 0.9 || std::fabs(N[1]) > 0.9;
+    bool lost = true;
+    for (int i = 0; i < 7; ++i) lost = lost && c->fermi_hist[i];
+    if (evals) *evals = ne;
+    if (lost) return MG_ERR_STATE;
+    return (conv[0] && conv[1]) ? MG_OK : MG_NOT_CONVERGED;
+}
+
 // DiagonaliseRhoHFB + HFBOccupations, src/HFB.f90:3156-3284, :3361-3560:
 // canonical basis from the eigenvectors of rho, occupations, rho / kappa mixing.
 static int hfb_occupations(orc_ctx* c) {
@@ -2953,7 +3078,9 @@ extern "C" int orc_solve_pairing(orc_ctx* c, mg_pairing_info* info) {
     pairing_field(c);
     pairing_gaps(c);
     int evals = 0;
-    const int st = c->pp.fermi_solver == 2 ? fermi_gradient(c, &evals) : fermi_broyden(c, &evals);
+    const int st = c->pp.fermi_solver == 2   ? fermi_gradient(c, &evals)
+                   : c->pp.fermi_solver == 3 ? fermi_bisection(c, &evals)
+                                             : fermi_broyden(c, &evals);
     if (st < 0 && st != MG_ERR_STATE) return st;
     double tr[2] = {0.0, 0.0};
     for (int b = 0; b < 4; ++b) {

@@ -109,12 +109,44 @@ def test_hfb_iterations_first_order_finish(built):
     g.close()
 
 
+def test_bisection_fermi_solver(built):
+    """FermiSolver 'BISECTION' (fermi_solver = 3: bracketing by growing
+    steps from the stored Fermi energies, then Brent's method to fermi_prec
+    on lambda) against the oracle's restatement: Fermi energies within 1e-9
+    MeV at the first pairing step (from the module's -10 MeV start, tens of
+    bracketing evaluations) and the energies of 4 iterations within 1e-8
+    MeV; its root is the Newton search's within 1e-9 MeV."""
+    p, g, o = _hfb_pair(seed=5)
+    pp = _abi.MgPairingParams.defaults()
+    pp.fermi_solver = 3
+    g.set_pairing(pp)
+    o.set_pairing(pp)
+    ig, io = g.SolvePairing(), o.SolvePairing()
+    assert ig["converged"] and io["converged"]
+    assert ig["evaluations"] > 10
+    for it in range(2):
+        assert abs(ig["fermi"][it] - io["fermi"][it]) < 1e-9, (ig["fermi"], io["fermi"])
+        assert abs(ig["particles"][it] - (p.neutrons, p.protons)[it]) < 1e-9
+    _, n, _ = _hfb_pair(seed=5)
+    inew = n.SolvePairing()
+    for it in range(2):
+        assert abs(ig["fermi"][it] - inew["fermi"][it]) < 1e-9
+    n.close()
+    g.Start()
+    o.Start()
+    eg = g.Evolve(4, 0.010, 0.3)
+    eo = o.Evolve(4, 0.010, 0.3)
+    assert abs(eg["total"] - eo["total"]) < 1e-8, (eg["total"], eo["total"])
+    g.close()
+    o.close()
+
+
 def test_unknown_fermi_solver_is_rejected(built):
     p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
                   pairing=_abi.MG_PAIRING_HFB)
     g = MeshState(p, SLY4)
     pp = _abi.MgPairingParams.defaults()
-    pp.fermi_solver = 3
+    pp.fermi_solver = 4
     with pytest.raises(_abi.MgError):
         g.set_pairing(pp)
     pp.fermi_solver = 1
