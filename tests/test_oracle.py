@@ -378,3 +378,30 @@ def test_convergence_check():
     for _ in range(9):
         h.Evolve(1, 0.010, 0.3)
         assert not h.ConvergenceCheck(loose)
+
+
+def test_bisection_fermi_search_finds_the_broyden_root():
+    """The oracle's FermiSolver 'BISECTION' (bracketing by steps of 0.01 MeV
+    times the attempt, then Brent's method to fermi_prec on lambda) lands on
+    the root of its damped Broyden search (1e-10 MeV) with the particle
+    numbers within 1e-9, after more evaluations (the bracket from -10 MeV)."""
+    from mocca_gb300 import SLY4 as F
+    p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
+                  pairing=_abi.MG_PAIRING_HFB)
+    psi, qn, en = synthetic.ho_basis(p, 20, seed=5)
+    out = {}
+    for solver in (1, 3):
+        o = O.OracleState(p, F)
+        o.set_spinors(psi, qn)
+        o.set_energies(en)
+        pp = _abi.MgPairingParams.defaults()
+        pp.fermi_solver = solver
+        o.set_pairing(pp)
+        out[solver] = o.SolvePairing()
+        o.close()
+    a, b = out[1], out[3]
+    assert a["converged"] and b["converged"]
+    assert b["evaluations"] > 2 * a["evaluations"] > 0
+    for it in range(2):
+        assert abs(a["fermi"][it] - b["fermi"][it]) < 1e-10
+        assert abs(b["particles"][it] - 12.0) < 1e-9
