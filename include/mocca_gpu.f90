@@ -34,6 +34,7 @@ module mocca_gpu
     integer(c_int) :: parameter_estimation
     real(c_double) :: coulomb_prec
     real(c_double) :: omega(3)
+    real(c_double) :: precon_w
   end type mg_params
   type, bind(C) :: mg_force
     real(c_double) :: t0

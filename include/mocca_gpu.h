@@ -92,6 +92,10 @@ typedef struct mg_params {
                                   fixed; src/Cranking.f90:24-60); nonzero only with trc = 0,
                                   and with EV8 symmetry only OmegaZ (the reference stops on
                                   OmegaX with signature and OmegaY with time simplex) */
+    double precon_w;           /* PreConW, 0 (src/Densities.f90:37): > 0 also preconditions
+                                  the update of each W component under MixingScheme 2
+                                  (src/PotentialMixing.f90:169-210), with alpha = -preconu
+                                  like U (the reference's own PreConW alpha is commented out) */
 } mg_params;
 
 /*

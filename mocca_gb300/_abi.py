@@ -52,6 +52,7 @@ class MgParams(C.Structure):
         ("parameter_estimation", C.c_int),
         ("coulomb_prec", C.c_double),
         ("omega", C.c_double * 3),
+        ("precon_w", C.c_double),
     ]
 
 

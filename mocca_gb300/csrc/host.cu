@@ -42,7 +42,7 @@ void free_all(mg_ctx* c) {
     F(c->cpot); F(c->csource); F(c->cres); F(c->cp); F(c->ct); F(c->sh_ext); F(c->sh_mesh);
     F(c->coulomb); F(c->coulex); F(c->moment_values); F(c->rpow_ext); F(c->mfac);
     F(c->cg_bar); F(c->cg_status); F(c->red); F(c->flags); F(c->cfast); F(c->cguess);
-    F(c->dhist); F(c->Uold); F(c->Sold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
+    F(c->dhist); F(c->Uold); F(c->Sold); F(c->Wold); F(c->pc_buf); F(c->pc_jobs); F(c->jmunu); F(c->jmunu_hist);
     F(c->odd); F(c->odd_hist); F(c->Apot); F(c->Spot); F(c->divA); F(c->odd_der); F(c->odd_tmp);
     F(c->odd_jobs);
     F(c->Cpot); F(c->Dpot); F(c->dDpot); F(c->divD); F(c->todd_tmp); F(c->todd_work);
@@ -189,6 +189,7 @@ extern "C" int mg_create(const mg_params* p, const mg_force* f, void* stream, mg
     if (p->precision != MG_FP64 && p->precision != MG_MIXED) return MG_ERR_ARG;
     if ((p->parameter_estimation != 0 && p->parameter_estimation != 1) ||
         (p->mixing_scheme != 0 && p->mixing_scheme != 2) || !(p->damping >= 0.0) ||
+        !(p->precon_w >= 0.0) ||
         p->damping > 1.0)
         return MG_ERR_ARG;
     if (p->pairing != MG_PAIRING_HF && p->pairing != MG_PAIRING_HFB) return MG_ERR_ARG;
@@ -614,6 +615,9 @@ extern "C" int mg_construct_potentials(mg_ctx* c, int* iters) {
     // preconditions the update once UpotOld is not all zero
     MG_CUDA(cudaMemcpyAsync(c->Uold, c->U, 2 * c->V * sizeof(double), cudaMemcpyDeviceToDevice,
                             c->stream));
+    if (c->Wold)   // WpotOld = Wpot (src/PotentialMixing.f90:117)
+        MG_CUDA(cudaMemcpyAsync(c->Wold, c->W, 18 * c->V * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
     if (c->Sold)   // SpotOld = Spot (src/PotentialMixing.f90:122)
         MG_CUDA(cudaMemcpyAsync(c->Sold, c->Spot, 6 * c->V * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));

@@ -316,6 +316,7 @@ struct mg_ctx {
     bool have_dhist = false;
     double* Uold = nullptr;            // UpotOld (2V)
     double* Sold = nullptr;            // SpotOld without time reversal (6V)
+    double* Wold = nullptr;            // WpotOld with PreConW > 0 (18V)
     // time-odd densities and fields without time reversal (timeodd.cu):
     // odd = [vecj 6V, vecs 6V, rot j 6V, rot s 6V] ([it][m][V] each), its
     // history for the mixing, A and S ([it][m][V]), div A ([it][V]), the

@@ -8,7 +8,8 @@
 //   scheme 2: the U update is preconditioned instead,
 //     Upot = UpotOld + PreconditionPotential(Upot - UpotOld)
 //     and, without time reversal, each component of the S update with the
-//     symmetries of s (src/PotentialMixing.f90:143-168,
+//     symmetries of s, and with PreConW > 0 each W component's
+//     (src/PotentialMixing.f90:143-210,
 //     src/Damping.f90:158-228): per isospin
 //     a CG on (beta + alpha Lap) x = dU with alpha = -preconu, beta = 1 and
 //     the Lagrange Laplacian, at most 300 steps, stopping when
@@ -132,18 +133,22 @@ int mixing_setup(mg_ctx* c) {
     if (!(A(&c->dhist, 14 * V) && A(&c->Uold, 2 * V) && A(&c->pc_buf, 10 * V)))
         return MG_ERR_CUDA;
     if (!c->p.trc && !A(&c->Sold, 6 * V)) return MG_ERR_CUDA;
-    // the Laplacian of the direction: U (P, S, TS, 1), then the S components
-    // (P, -S, TS, 1), (P, -S, TS, 2), (P, S, TS, 1)
-    std::vector<GridJob> jobs(8);
+    if (c->p.precon_w > 0.0 && !A(&c->Wold, 18 * V)) return MG_ERR_CUDA;
+    // the Laplacian of the direction: U (P, S, TS, 1); the S components
+    // (P, -S, TS, 1), (P, -S, TS, 2), (P, S, TS, 1); the W classes
+    // (-P, S, TS, 2) of W_11, W_22, W_33, (-P, S, TS, 1) of W_12, W_21,
+    // (-P, -S, TS, 2) of W_13, W_31, (-P, -S, TS, 1) of W_23, W_32
+    std::vector<GridJob> jobs(16);
     const int P = c->p.pc, S = c->p.sc, TS = c->p.tsc;
-    const int sym[4][2] = {{S, 1}, {-S, 1}, {-S, 2}, {S, 1}};
-    for (int k = 0; k < 4; ++k)
+    const int sym[8][3] = {{P, S, 1},   {P, -S, 1},  {P, -S, 2},  {P, S, 1},
+                           {-P, S, 2},  {-P, S, 1},  {-P, -S, 2}, {-P, -S, 1}};
+    for (int k = 0; k < 8; ++k)
         for (int it = 0; it < 2; ++it) {
             GridJob J{};
             J.in = c->pc_buf + (2 + it) * V;        // direction
             J.lap = c->pc_buf + (6 + it) * V;       // Laplacian of the direction
             for (int d = 0; d < 3; ++d)
-                J.slot[d] = (int8_t)lag_slot(d, P, sym[k][0], TS, sym[k][1]);
+                J.slot[d] = (int8_t)lag_slot(d, sym[k][0], sym[k][1], TS, sym[k][2]);
             jobs[2 * k + it] = J;
         }
     MG_CUDA(cudaMalloc(&c->pc_jobs, jobs.size() * sizeof(GridJob)));
@@ -228,7 +233,9 @@ static int precondition_pot(mg_ctx* c, double* F, const double* Fold, long strid
     k_pc_start<<<g2, kThreads, 0, c->stream>>>(F, Fold, stride, res, dir, inv, V, c->red);
     MG_LAUNCHED(c);
     MG_TRY(read_pair(c, nblk, h, nn));
-    bool conv[2] = {false, false};
+    // an isospin whose update is identically zero keeps it (its first CG
+    // step would divide 0 by 0), e.g. W_11 of a functional without J^2 terms
+    bool conv[2] = {nn[0] == 0.0, nn[1] == 0.0};
     for (int iter = 1; iter <= 300 && !(conv[0] && conv[1]); ++iter) {
         MG_TRY(run_jobs(c, jobs, 2));
         k_pc_update<<<g2, kThreads, 0, c->stream>>>(dir, lap, upd, V, alpha, beta, c->red);
@@ -264,6 +271,16 @@ int precondition_u(mg_ctx* c) {
         for (int m = 0; m < 3; ++m)
             MG_TRY(precondition_pot(c, c->Spot + m * V, c->Sold + m * V, 3 * V,
                                     c->pc_jobs + 2 * (m + 1)));
+    if (c->Wold) {
+        // W (mu, nu) at [it][nu][mu]; its symmetry class by (mu, nu)
+        const int cls[3][3] = {{4, 5, 6}, {5, 4, 7}, {6, 7, 4}};
+        for (int mu = 0; mu < 3; ++mu)
+            for (int nu = 0; nu < 3; ++nu) {
+                const long off = (nu * 3 + mu) * V;
+                MG_TRY(precondition_pot(c, c->W + off, c->Wold + off, 9 * V,
+                                        c->pc_jobs + 2 * cls[mu][nu]));
+            }
+    }
     return MG_OK;
 }
 

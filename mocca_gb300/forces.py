@@ -95,6 +95,7 @@ class RunParams:
     mixing_scheme: int = 0      # MixingScheme: 0 linear density mixing, 2 preconditioned U
     damping: float = 0.75       # DampingParam
     precon_u: float = 1.0       # preconu
+    precon_w: float = 0.0       # PreConW: > 0 preconditions the W update too (MixingScheme 2)
     parameter_estimation: int = 0   # ParameterEstimation: 1 estimates dt, momentum every step
     coulomb_prec: float = 0.0   # > 0: relative residual of the CG / multigrid Coulomb solves
     omega: tuple = (0.0, 0.0, 0.0)  # cranking OmegaX, OmegaY, OmegaZ (needs trc = 0)

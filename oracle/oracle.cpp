@@ -1880,6 +1880,7 @@ static void precondition_potential(orc_ctx* c, const std::vector<double>& pot,
         double nn = 0.0;
         for (long v = 0; v < V; ++v) nn = nn + dir[v] * dir[v];
         nn = nn * c->dv;
+        if (nn == 0.0) continue;   // a zero update stays zero (0/0 otherwise)
         for (int iter = 1; iter <= 300; ++iter) {
             derive_grid(c, dir.data(), 3, P, S, TS, comp, lap.data());
             for (long v = 0; v < V; ++v) upd[v] = beta * dir[v] + alpha * lap[v];
@@ -1906,6 +1907,7 @@ extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
     int st = MG_OK;
     c->Uold = c->U;   // UpotOld = Upot (src/PotentialMixing.f90:115)
     const std::vector<double> Sold = c->Spot;   // SpotOld = Spot (:122)
+    const std::vector<double> Wold = c->W;      // WpotOld = Wpot (:117)
     if (c->p.coulomb_solver != 0) {
         st = orc_solve_coulomb(c, iters);
         if (st < 0) return st;
@@ -1939,6 +1941,31 @@ extern "C" int orc_construct_potentials(orc_ctx* c, int* iters) {
                     for (long v = 0; v < V; ++v)
                         c->Spot[(it * 3 + m) * V + v] = Sold[(it * 3 + m) * V + v] + inv[it * V + v];
             }
+        }
+        if (c->p.precon_w > 0.0) {
+            // each W (mu, nu) ([it][nu][mu]) with the symmetries of its class
+            // (src/PotentialMixing.f90:169-210)
+            const long V = c->V;
+            for (int mu = 0; mu < 3; ++mu)
+                for (int nu = 0; nu < 3; ++nu) {
+                    int ss = S, comp = 2;
+                    if (mu == nu) { ss = S; comp = 2; }
+                    else if ((mu == 0 && nu == 1) || (mu == 1 && nu == 0)) { ss = S; comp = 1; }
+                    else if ((mu == 0 && nu == 2) || (mu == 2 && nu == 0)) { ss = -S; comp = 2; }
+                    else { ss = -S; comp = 1; }
+                    std::vector<double> dw(2 * V);
+                    for (int it = 0; it < 2; ++it)
+                        for (long v = 0; v < V; ++v) {
+                            const long q = ((it * 3 + nu) * 3 + mu) * V + v;
+                            dw[it * V + v] = c->W[q] - Wold[q];
+                        }
+                    precondition_potential(c, dw, inv, -P, ss, TS, comp);
+                    for (int it = 0; it < 2; ++it)
+                        for (long v = 0; v < V; ++v) {
+                            const long q = ((it * 3 + nu) * 3 + mu) * V + v;
+                            c->W[q] = Wold[q] + inv[it * V + v];
+                        }
+                }
         }
     }
     return st;

@@ -155,11 +155,13 @@ def test_hf_iterations_match_oracle_24(built):
     g.close()
 
 
-def test_hf_iterations_precondition_scheme2(built):
-    """MixingScheme 2 (PreconditionPotential on the U update) on the GPU
-    against the oracle: 4 iterations, E_total within 1e-8 MeV."""
+@pytest.mark.parametrize("precon_w", [0.0, 1.0])
+def test_hf_iterations_precondition_scheme2(built, precon_w):
+    """MixingScheme 2 (PreconditionPotential on the U update; with PreConW >
+    0 on each W component's too) on the GPU against the oracle: 4
+    iterations, E_total within 1e-8 MeV, U and W within 1e-10."""
     p = RunParams(nx=10, ny=10, nz=10, dx=0.8, nwt=40, neutrons=12, protons=12,
-                  mixing_scheme=2)
+                  mixing_scheme=2, precon_w=precon_w)
     psi, qn, en = synthetic.ho_basis(p, 20, seed=1234)
     g, o = _pair(p, psi, qn, en)
     g.Start()
@@ -169,4 +171,5 @@ def test_hf_iterations_precondition_scheme2(built):
     assert abs(eg["total"] - eo["total"]) < 1e-8, (eg["total"], eo["total"])
     pg, po = g.get_potentials(), o.get_potentials()
     assert rel(pg["U"], po["U"]) < 1e-10
+    assert rel(pg["W"], po["W"]) < 1e-10
     g.close()
